@@ -1,0 +1,219 @@
+/*
+ * fest_gpu.h - C ABI of the GB300 (sm_103a) explicit residual-and-update path
+ * of the FEST-3D structured finite-volume solver.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns an int status (FEST_OK == 0).  Host arrays use exactly the
+ * Fortran column-major shapes of the reference, including lower bounds, so
+ * a Fortran caller passes c_loc() of its own arrays unchanged:
+ *
+ *   qp      (-2:imx+2,-2:jmx+2,-2:kmx+2,1:n_var)         double
+ *   Temp, mu, mu_t, sst_F1, dist  (-2:imx+2,-2:jmx+2,-2:kmx+2)
+ *   cells   (-2:imx+2,-2:jmx+2,-2:kmx+2) of {volume,cx,cy,cz}   (AoS, 32 B)
+ *   Ifaces  (-2:imx+3,-2:jmx+2,-2:kmx+2) of {A,nx,ny,nz}        (AoS, 32 B)
+ *   Jfaces  (-2:imx+2,-2:jmx+3,-2:kmx+2) of {A,nx,ny,nz}
+ *   Kfaces  (-2:imx+2,-2:jmx+2,-2:kmx+3) of {A,nx,ny,nz}
+ *   nodes   (-2:imx+3,-2:jmx+3,-2:kmx+3) of {x,y,z}
+ *   x_qp_left/right (0:imx+1,1:jmx-1,1:kmx-1,1:n_var), y_* and z_* alike
+ *   F (1:imx,1:jmx-1,1:kmx-1,n_var), G (1:imx-1,1:jmx,1:kmx-1,n_var),
+ *   H (1:imx-1,1:jmx-1,1:kmx,n_var), residue (1:imx-1,1:jmx-1,1:kmx-1,n_var)
+ *   gradqp_x/y/z (0:imx,0:jmx,0:kmx,1:n_grad)   n_grad = 4 laminar, 6 SST
+ *   delta_t (1:imx-1,1:jmx-1,1:kmx-1)
+ *
+ * imx, jmx, kmx are NODE counts (vartypes.f90:21-26): a block has
+ * (imx-1)(jmx-1)(kmx-1) interior cells and 3 ghost layers per side.
+ *
+ * Ownership: the caller owns host arrays; a handle owns device copies of
+ * the state, metrics and every module-level array of the reference
+ * (face states, gradients, viscosities, fluxes, residue, time step).
+ * No host pointer is retained past a call.  A handle is synchronous on its
+ * own CUDA stream and must not be used from two threads at once; distinct
+ * handles are independent.
+ *
+ * Module entry points take nullable host pointers: a non-NULL input is
+ * uploaded before the kernel runs, a non-NULL output is downloaded after
+ * it; NULL means "use / keep the device-resident copy in the handle".
+ */
+#ifndef FEST_GPU_H
+#define FEST_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference aborts through Fatal_error, error.h:1) */
+#define FEST_OK                  0
+#define FEST_ERR_ARG             1  /* bad argument / unsupported option       */
+#define FEST_ERR_CUDA            2  /* a CUDA runtime call failed              */
+#define FEST_ERR_NAN             3  /* NaN in a flux/gradient/state (ausm.f90:195) */
+#define FEST_ERR_NEGATIVE_STATE  4  /* rho<0 or p<0 after update (update.f90:448) */
+#define FEST_ERR_TIMEOUT         5  /* a bounded device wait gave up           */
+#define FEST_ERR_NOMEM           6  /* device allocation failed                */
+#define FEST_ERR_NO_DEVICE       7  /* no CUDA device visible                  */
+
+/* ---- scheme selectors (schemetype, vartypes.f90:197-232) ---------------- */
+enum { FEST_FLUX_AUSM = 0, FEST_FLUX_AUSMP = 1, FEST_FLUX_AUSMUP = 2,
+       FEST_FLUX_SLAU = 3, FEST_FLUX_LDFSS0 = 4, FEST_FLUX_VAN_LEER = 5 };
+enum { FEST_INTERP_NONE = 0, FEST_INTERP_MUSCL = 1, FEST_INTERP_PPM = 2,
+       FEST_INTERP_WENO = 3, FEST_INTERP_WENO_NM = 4 };
+enum { FEST_TIME_NONE = 0, FEST_TIME_RK2 = 1, FEST_TIME_RK4 = 2,
+       FEST_TIME_TVDRK2 = 3, FEST_TIME_TVDRK3 = 4 };
+enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2 };
+enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
+/* MUSCL limiter: the reference hard-codes Koren's alpha family
+ * (muscl.f90:258,283); van Albada (muscl.f90:285, commented out there) is an
+ * extension selectable here. */
+enum { FEST_LIMITER_KOREN = 0, FEST_LIMITER_VAN_ALBADA = 1 };
+/* arithmetic of the hot path */
+enum { FEST_FP64 = 0, FEST_MIXED = 1 };
+
+/* boundary condition ids (bc_primitive.f90:160-206, bc.f90:27-32) */
+enum { FEST_BC_SUPERSONIC_INLET = -1, FEST_BC_SUPERSONIC_OUTLET = -2,
+       FEST_BC_SUBSONIC_INLET = -3, FEST_BC_SUBSONIC_OUTLET = -4,
+       FEST_BC_WALL = -5, FEST_BC_SLIP_WALL = -6, FEST_BC_POLE = -7,
+       FEST_BC_FAR_FIELD = -8, FEST_BC_PERIODIC_SINGLE = -9,
+       FEST_BC_INTERFACE = -10, FEST_BC_TOTAL_PRESSURE = -11 };
+
+typedef struct {            /* extent, vartypes.f90:21-26 */
+  int imx, jmx, kmx, n_var;
+} fest_extent;
+
+typedef struct {            /* flowtype, vartypes.f90:235-286 */
+  double density_inf, x_speed_inf, y_speed_inf, z_speed_inf, pressure_inf;
+  double tk_inf, tw_inf;
+  double vel_mag, MInf;     /* derived by init_infinity_values, state.f90:87-88 */
+  double gm, R_gas, mu_ref, T_ref, Sutherland_temp, Pr, tPr;
+  int mu_variation;         /* FEST_MU_* */
+  int reserved;
+} fest_flow;
+
+typedef struct {            /* schemetype, vartypes.f90:197-232 */
+  int scheme_name;          /* FEST_FLUX_* */
+  int interpolant;          /* FEST_INTERP_* */
+  int time_stepping_method; /* 'l' (local) or 'g' (global) */
+  int time_step_accuracy;   /* FEST_TIME_* */
+  double global_time_step;  /* used by 'g' when > 0 (time.f90:275) */
+  int ilimiter_switch, jlimiter_switch, klimiter_switch;
+  int itlimiter_switch, jtlimiter_switch, ktlimiter_switch;
+  int iPB_switch, jPB_switch, kPB_switch;
+  int turbulence;           /* FEST_TURB_* */
+  int accur;                /* higher-order ghost switch (bc.f90:48-50) */
+  int limiter;              /* FEST_LIMITER_* */
+} fest_scheme;
+
+typedef struct {            /* boundarytype, vartypes.f90:289-367 */
+  int id[6];                /* imin,imax,jmin,jmax,kmin,kmax */
+  /* interface partner of a face whose id is -10 (or >= 0): the ghost layer
+   * l of this face receives interior layer l of face partner_face[f] of
+   * block partner_block[f] (interface1.f90:496-700).  For a single-block
+   * handle partner_block must be 0.  A face paired with itself reproduces
+   * what MPI_SENDRECV to the own rank does in the reference (a mirror). */
+  int partner_block[6];
+  int partner_face[6];
+  double fixed_density[6], fixed_pressure[6];
+  double fixed_x_speed[6], fixed_y_speed[6], fixed_z_speed[6];
+  double fixed_tk[6], fixed_tw[6];
+  double fixed_wall_temperature[6];
+  double fixed_Tpressure[6], fixed_Ttemperature[6];
+} fest_bc;
+
+typedef struct fest_handle fest_handle;
+
+/* ---- lifetime ---------------------------------------------------------- */
+/* setup_scheme/setup_bc/setup_gradients/setup_viscosity/setup_update of the
+ * reference (scheme.f90:29, bc.f90:18, gradients.f90:94, viscosity.f90:553,
+ * update.f90:92) in one call.  Allocates every device array of the block. */
+int fest_create(const fest_extent *dims, const fest_flow *flow,
+                const fest_scheme *scheme, const fest_bc *bc,
+                fest_handle **out);
+int fest_destroy(fest_handle *h);
+/* FEST_FP64 (default) or FEST_MIXED for fest_step */
+int fest_set_precision(fest_handle *h, int precision);
+/* last device-side error word (FEST_ERR_*), cleared by the call */
+int fest_last_device_error(fest_handle *h);
+/* number of kernels this handle has launched so far */
+long long fest_kernel_launches(const fest_handle *h);
+
+/* ---- geometry (grid.f90:137-236 ghost_grid, geometry.f90:548-580) ------ */
+/* nodes: interior nodes (1:imx,1:jmx,1:kmx) filled, ghosts extrapolated
+ * here.  Outputs (nullable) receive the metrics; they also stay on device. */
+int fest_setup_geometry(fest_handle *h, double *nodes, double *cells,
+                        double *Ifaces, double *Jfaces, double *Kfaces);
+/* upload metrics computed elsewhere (e.g. by the Fortran setup_geometry) */
+int fest_set_metrics(fest_handle *h, const double *cells, const double *Ifaces,
+                     const double *Jfaces, const double *Kfaces);
+/* wall distance (wall_dist.f90:84-131): min node distance to the given wall
+ * node list, averaged to cells.  dist (nullable) receives the result. */
+int fest_find_wall_dist(fest_handle *h, const double *wall_xyz, int n_wall,
+                        double *dist);
+int fest_set_wall_dist(fest_handle *h, const double *dist);
+
+/* ---- state ------------------------------------------------------------- */
+int fest_upload_state(fest_handle *h, const double *qp);
+int fest_download_state(fest_handle *h, double *qp);
+
+/* ---- module-level entry points (drop-ins for the Fortran procedures) --- */
+/* apply_interface (interface1.f90:96) + populate_ghost_primitive
+ * (bc_primitive.f90:55): ghost layers of qp for every face, then the 0.33
+ * corner averaging (bc_primitive.f90:209-224). */
+int fest_populate_ghost_primitive(fest_handle *h, double *qp, int current_iter);
+/* Temp = p/(R rho) over the padded block (update.f90:170) */
+int fest_compute_temperature(fest_handle *h, const double *qp, double *Temp);
+/* compute_face_interpolant (face_interpolant.f90:79) */
+int fest_compute_face_interpolant(fest_handle *h, const double *qp,
+                                  double *x_qp_left, double *x_qp_right,
+                                  double *y_qp_left, double *y_qp_right,
+                                  double *z_qp_left, double *z_qp_right);
+/* reconstruct_boundary_state (boundary_state_reconstruction.f90:28); the
+ * face-state arrays are in/out (nullable: device-resident ones) */
+int fest_reconstruct_boundary_state(fest_handle *h, const double *qp,
+                                    double *x_qp_left, double *x_qp_right,
+                                    double *y_qp_left, double *y_qp_right,
+                                    double *z_qp_left, double *z_qp_right);
+/* compute_fluxes (scheme.f90:68) from the face states held in the handle */
+int fest_compute_fluxes(fest_handle *h, double *F, double *G, double *H);
+/* evaluate_all_gradients (gradients.f90:276) incl. apply_gradient_bc */
+int fest_evaluate_all_gradients(fest_handle *h, const double *qp,
+                                const double *Temp, double *gradqp_x,
+                                double *gradqp_y, double *gradqp_z);
+/* calculate_viscosity (viscosity.f90:52): mu, mu_t and sst_F1 */
+int fest_calculate_viscosity(fest_handle *h, const double *qp, double *mu,
+                             double *mu_t, double *sst_F1);
+/* compute_viscous_fluxes (viscous.f90:55): adds into F, G, H (in/out) */
+int fest_compute_viscous_fluxes(fest_handle *h, const double *qp, double *F,
+                                double *G, double *H);
+/* compute_residue (scheme.f90:111) */
+int fest_compute_residue(fest_handle *h, const double *F, const double *G,
+                         const double *H, double *residue);
+/* add_source_term_residue (source.f90:94): residue in/out */
+int fest_add_source_term_residue(fest_handle *h, const double *qp,
+                                 double *residue);
+/* compute_time_step (time.f90:291), using the face states of the handle */
+int fest_compute_time_step(fest_handle *h, const double *qp, double CFL,
+                           double *delta_t);
+/* get_total_conservative_Residue (update.f90:495): all of the above in the
+ * reference's order on the resident state; outputs nullable */
+int fest_get_total_conservative_residue(fest_handle *h, double *qp,
+                                        int current_iter, double *residue);
+/* get_next_solution (update.f90:129): one iteration of the configured
+ * integrator on the resident state.  qp (nullable) is uploaded before and
+ * downloaded after; residue/delta_t (nullable) receive the last stage's. */
+int fest_get_next_solution(fest_handle *h, double *qp, int current_iter,
+                           double CFL, double *residue, double *delta_t);
+/* find_resnorm (resnorm.f90:62): res_abs[0..n_var] from the last residue
+ * and fluxes; res_abs[0] is |net mass flux| (resnorm.f90:190-198),
+ * res_abs[l] = sqrt(sum R_l^2) / scale_l (resnorm.f90:171-176, 221). */
+int fest_find_resnorm(fest_handle *h, double *res_abs);
+
+/* ---- fused fast path ----------------------------------------------------- */
+/* n_iters iterations starting at iteration number first_iter, state kept on
+ * device, in the precision chosen by fest_set_precision.  In FEST_MIXED the
+ * stencil arithmetic runs in FP32 and the primitive state, the metrics and
+ * the norm stay FP64.  res_abs (nullable) receives the last norm. */
+int fest_step(fest_handle *h, int n_iters, int first_iter, double CFL,
+              double *res_abs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEST_GPU_H */
