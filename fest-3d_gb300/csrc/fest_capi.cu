@@ -1,0 +1,660 @@
+// fest_capi.cu - the extern "C" boundary: handle lifetime, host<->device
+// movement of the reference's Fortran-layout arrays, and the module-level
+// and integrator entry points built from the module kernels.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "fest_fused.cuh"
+#include "fest_kernels.cuh"
+
+using namespace fest;
+
+struct fest_handle {
+  Params p;
+  fest_extent ext;
+  fest_flow flow;
+  fest_scheme sc;
+  fest_bc bc;
+  cudaStream_t s = nullptr;
+  DevBlock d{};
+  BlockRef* d_table = nullptr;
+  double* d_resnorm = nullptr;
+  double* d_nodedist = nullptr;
+  double* d_wall = nullptr;
+  int n_wall_cap = 0;
+  int precision = FEST_FP64;
+  long long launches = 0;
+  FusedState* fused = nullptr;
+  std::vector<void*> allocs;
+  Launcher L() { return Launcher{s, &launches}; }
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return FEST_OK;
+  if (e == cudaErrorMemoryAllocation) return FEST_ERR_NOMEM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return FEST_ERR_NO_DEVICE;
+  return FEST_ERR_CUDA;
+}
+
+#define CK(x)                                  \
+  do {                                         \
+    cudaError_t e_ = (x);                      \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+int dalloc(fest_handle* h, double** p, long long n) {
+  if (n <= 0) n = 1;
+  CK(cudaMalloc((void**)p, sizeof(double) * (size_t)n));
+  h->allocs.push_back(*p);
+  CK(cudaMemsetAsync(*p, 0, sizeof(double) * (size_t)n, h->s));
+  return FEST_OK;
+}
+
+struct Sizes {
+  long long qp, pad, cells, faces[3], nodes, fs[3], fl[3], res, grad, dt;
+};
+Sizes sizes_of(const Dims& d, int n_grad) {
+  Sizes z;
+  z.pad = d.P;
+  z.qp = d.P * d.nv;
+  z.cells = 4 * d.P;
+  for (int dir = 0; dir < 3; ++dir) {
+    z.faces[dir] = 4 * nfaces(d, dir);
+    z.fs[dir] = fsdim(d, dir).N * d.nv;
+    z.fl[dir] = fldim(d, dir).N * d.nv;
+  }
+  z.nodes = 3LL * (d.imx + 6) * (d.jmx + 6) * (d.kmx + 6);
+  z.res = ncells(d) * d.nv;
+  z.grad = ngrad(d) * n_grad;
+  z.dt = ncells(d);
+  return z;
+}
+
+int up(fest_handle* h, double* dst, const double* src, long long n) {
+  if (!src) return FEST_OK;
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, h->s));
+  return FEST_OK;
+}
+int down(fest_handle* h, double* dst, const double* src, long long n) {
+  if (!dst) return FEST_OK;
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->s));
+  return FEST_OK;
+}
+
+// wait for the stream; report CUDA errors, then the device error word
+int finish(fest_handle* h) {
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->s));
+  int err = 0;
+  CK(cudaMemcpy(&err, h->d.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    CK(cudaMemset(h->d.err, 0, sizeof(int)));
+    return err;
+  }
+  return FEST_OK;
+}
+
+#define RET(x)                \
+  do {                        \
+    int r_ = (x);             \
+    if (r_) return r_;        \
+  } while (0)
+
+bool valid_id(int id) { return id >= -11 && id <= -1 ? true : id >= 0; }
+
+void fill_params(fest_handle* h) {
+  Params& p = h->p;
+  memset(&p, 0, sizeof(p));
+  const fest_extent& e = h->ext;
+  p.d.imx = e.imx; p.d.jmx = e.jmx; p.d.kmx = e.kmx; p.d.nv = e.n_var;
+  p.d.ni = e.imx + 5; p.d.nj = e.jmx + 5; p.d.nk = e.kmx + 5;
+  p.d.P = (long long)p.d.ni * p.d.nj * p.d.nk;
+  const fest_flow& f = h->flow;
+  p.gm = f.gm; p.R = f.R_gas; p.mu_ref = f.mu_ref; p.T_ref = f.T_ref; p.S = f.Sutherland_temp;
+  p.Pr = f.Pr; p.tPr = f.tPr; p.MInf = f.MInf; p.p_inf = f.pressure_inf; p.rho_inf = f.density_inf;
+  p.u_inf = f.x_speed_inf; p.v_inf = f.y_speed_inf; p.w_inf = f.z_speed_inf;
+  p.mu_var = f.mu_variation;
+  const fest_scheme& s = h->sc;
+  p.flux = s.scheme_name; p.interp = s.interpolant; p.limiter = s.limiter; p.turb = s.turbulence;
+  p.tstep = s.time_stepping_method; p.gdt = s.global_time_step;
+  p.lam[0] = s.ilimiter_switch; p.lam[1] = s.jlimiter_switch; p.lam[2] = s.klimiter_switch;
+  p.tlim[0] = s.itlimiter_switch; p.tlim[1] = s.jtlimiter_switch; p.tlim[2] = s.ktlimiter_switch;
+  p.pb[0] = s.iPB_switch; p.pb[1] = s.jPB_switch; p.pb[2] = s.kPB_switch;
+  p.n_grad = s.turbulence == FEST_TURB_NONE ? 4 : 6;
+  // setup_bc (bc.f90:48-50)
+  p.c2 = 1 + s.accur; p.c3 = 0.5 * s.accur; p.c1 = p.c2 - p.c3;
+  const fest_bc& b = h->bc;
+  // ppm_flag (boundary_state_reconstruction.f90:45-47)
+  p.ppm_flag = (s.interpolant == FEST_INTERP_PPM || s.interpolant == FEST_INTERP_WENO ||
+                s.interpolant == FEST_INTERP_WENO_NM);
+  for (int i = 0; i < 6; ++i) {
+    p.id[i] = b.id[i];
+    if (b.id[i] == -7) p.ppm_flag = 1;
+    p.part_block[i] = b.partner_block[i];
+    p.part_face[i] = b.partner_face[i];
+    p.fix_rho[i] = b.fixed_density[i]; p.fix_p[i] = b.fixed_pressure[i];
+    p.fix_u[i] = b.fixed_x_speed[i]; p.fix_v[i] = b.fixed_y_speed[i]; p.fix_w[i] = b.fixed_z_speed[i];
+    p.fix_tk[i] = b.fixed_tk[i]; p.fix_tw[i] = b.fixed_tw[i];
+    p.Tw[i] = b.fixed_wall_temperature[i]; p.Tp[i] = b.fixed_Tpressure[i];
+  }
+}
+
+double* arr_ptr(fest_handle* h, int which) {
+  DevBlock& d = h->d;
+  switch (which) {
+    case FEST_ARR_QP: return d.qp;
+    case FEST_ARR_TEMP: return d.Temp;
+    case FEST_ARR_CELLS: return d.cells;
+    case FEST_ARR_IFACES: return d.faces[0];
+    case FEST_ARR_JFACES: return d.faces[1];
+    case FEST_ARR_KFACES: return d.faces[2];
+    case FEST_ARR_NODES: return d.nodes;
+    case FEST_ARR_X_QP_LEFT: return d.fsL[0];
+    case FEST_ARR_X_QP_RIGHT: return d.fsR[0];
+    case FEST_ARR_Y_QP_LEFT: return d.fsL[1];
+    case FEST_ARR_Y_QP_RIGHT: return d.fsR[1];
+    case FEST_ARR_Z_QP_LEFT: return d.fsL[2];
+    case FEST_ARR_Z_QP_RIGHT: return d.fsR[2];
+    case FEST_ARR_F: return d.flux[0];
+    case FEST_ARR_G: return d.flux[1];
+    case FEST_ARR_H: return d.flux[2];
+    case FEST_ARR_RESIDUE: return d.res;
+    case FEST_ARR_GRADQP_X: return d.grad[0];
+    case FEST_ARR_GRADQP_Y: return d.grad[1];
+    case FEST_ARR_GRADQP_Z: return d.grad[2];
+    case FEST_ARR_MU: return d.mu;
+    case FEST_ARR_MU_T: return d.mut;
+    case FEST_ARR_SST_F1: return d.F1;
+    case FEST_ARR_DIST: return d.dist;
+    case FEST_ARR_DELTA_T: return d.dt;
+    default: return nullptr;
+  }
+}
+
+long long arr_size(const fest_handle* h, int which) {
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  switch (which) {
+    case FEST_ARR_QP: return z.qp;
+    case FEST_ARR_TEMP: case FEST_ARR_MU: case FEST_ARR_MU_T: case FEST_ARR_SST_F1:
+    case FEST_ARR_DIST: return z.pad;
+    case FEST_ARR_CELLS: return z.cells;
+    case FEST_ARR_IFACES: return z.faces[0];
+    case FEST_ARR_JFACES: return z.faces[1];
+    case FEST_ARR_KFACES: return z.faces[2];
+    case FEST_ARR_NODES: return z.nodes;
+    case FEST_ARR_X_QP_LEFT: case FEST_ARR_X_QP_RIGHT: return z.fs[0];
+    case FEST_ARR_Y_QP_LEFT: case FEST_ARR_Y_QP_RIGHT: return z.fs[1];
+    case FEST_ARR_Z_QP_LEFT: case FEST_ARR_Z_QP_RIGHT: return z.fs[2];
+    case FEST_ARR_F: return z.fl[0];
+    case FEST_ARR_G: return z.fl[1];
+    case FEST_ARR_H: return z.fl[2];
+    case FEST_ARR_RESIDUE: return z.res;
+    case FEST_ARR_GRADQP_X: case FEST_ARR_GRADQP_Y: case FEST_ARR_GRADQP_Z: return z.grad;
+    case FEST_ARR_DELTA_T: return z.dt;
+    default: return 0;
+  }
+}
+
+__global__ void k_fill(double* x, long long n, double v) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) x[t] = v;
+}
+
+// get_total_conservative_Residue (update.f90:495-547) on the resident state
+int residual_fp64(fest_handle* h, int iter) {
+  const Params& p = h->p;
+  Launcher L = h->L();
+  launch_ghosts(p, h->d, h->d_table, iter, L);
+  launch_face_states(p, h->d, 1, L);
+  launch_fluxes(p, h->d, L);
+  if (p.mu_ref != 0.0) {
+    launch_gradients(p, h->d, L);
+    launch_viscosity(p, h->d, L);
+    launch_viscous_fluxes(p, h->d, L);
+  }
+  launch_residue(p, h->d, true, L);
+  return FEST_OK;
+}
+
+// get_next_solution (update.f90:129-226) on the resident state, FP64
+int next_solution_fp64(fest_handle* h, int it, double CFL) {
+  const Params& p = h->p;
+  Launcher L = h->L();
+  const Dims& d = p.d;
+  launch_temperature(p, h->d, L);
+  auto store = [&]() {
+    CK(cudaMemcpyAsync(h->d.Ustore, h->d.qp, sizeof(double) * d.P * d.nv, cudaMemcpyDeviceToDevice, h->s));
+    return FEST_OK;
+  };
+  auto zeroR = [&]() {
+    CK(cudaMemsetAsync(h->d.Rstore, 0, sizeof(double) * ncells(d) * d.nv, h->s));
+    return FEST_OK;
+  };
+  switch (h->sc.time_step_accuracy) {
+    case FEST_TIME_NONE:
+      residual_fp64(h, it);
+      launch_time_step(p, h->d, CFL, L);
+      launch_update(p, h->d, 1., 1., 0, 0, L);
+      break;
+    case FEST_TIME_RK4:
+      RET(zeroR()); RET(store());
+      residual_fp64(h, it);
+      launch_time_step(p, h->d, CFL, L);
+      launch_update(p, h->d, 0.5, 1., 0, 1, L);
+      residual_fp64(h, it); launch_update(p, h->d, 0.5, 2., 0, 1, L);
+      residual_fp64(h, it); launch_update(p, h->d, 1.0, 2., 0, 1, L);
+      residual_fp64(h, it); launch_update(p, h->d, 1. / 6., 1., 1, 1, L);
+      break;
+    case FEST_TIME_RK2:
+      RET(zeroR()); RET(store());
+      residual_fp64(h, it);
+      launch_time_step(p, h->d, CFL, L);
+      launch_update(p, h->d, 0.5, 1., 0, 1, L);
+      residual_fp64(h, it); launch_update(p, h->d, 0.5, 1., 1, 1, L);
+      break;
+    case FEST_TIME_TVDRK3:
+      RET(store());
+      residual_fp64(h, it);
+      launch_time_step(p, h->d, CFL, L);
+      launch_update(p, h->d, 1.0, 1., 0, 0, L);
+      residual_fp64(h, it); launch_update(p, h->d, 1.0, 1., 0, 0, L);
+      launch_blend(p, h->d, 0.75, 0.25, L);
+      residual_fp64(h, it); launch_update(p, h->d, 1.0, 1., 0, 0, L);
+      launch_blend(p, h->d, 1. / 3., 2. / 3., L);
+      break;
+    case FEST_TIME_TVDRK2:
+      RET(store());
+      residual_fp64(h, it);
+      launch_time_step(p, h->d, CFL, L);
+      launch_update(p, h->d, 1.0, 1., 0, 0, L);
+      residual_fp64(h, it); launch_update(p, h->d, 1.0, 1., 0, 0, L);
+      launch_blend(p, h->d, 0.5, 0.5, L);
+      break;
+    default:
+      return FEST_ERR_ARG;
+  }
+  return FEST_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_scheme* scheme,
+                const fest_bc* bc, fest_handle** out) {
+  if (!dims || !flow || !scheme || !bc || !out) return FEST_ERR_ARG;
+  *out = nullptr;
+  if (dims->imx < 2 || dims->jmx < 2 || dims->kmx < 2) return FEST_ERR_ARG;
+  int nv_need = scheme->turbulence == FEST_TURB_NONE ? 5 : 7;
+  if (dims->n_var != nv_need) return FEST_ERR_ARG;
+  if (scheme->scheme_name < 0 || scheme->scheme_name > 5) return FEST_ERR_ARG;
+  if (scheme->interpolant < 0 || scheme->interpolant > 4) return FEST_ERR_ARG;
+  if (scheme->turbulence < 0 || scheme->turbulence > 2) return FEST_ERR_ARG;
+  if (scheme->time_step_accuracy < 0 || scheme->time_step_accuracy > 4) return FEST_ERR_ARG;
+  if (scheme->time_stepping_method != 'l' && scheme->time_stepping_method != 'g') return FEST_ERR_ARG;
+  for (int f = 0; f < 6; ++f) {
+    if (!valid_id(bc->id[f])) return FEST_ERR_ARG;
+    if (bc->id[f] == -10 || bc->id[f] >= 0) {
+      if (bc->partner_block[f] != 0 || bc->partner_face[f] < 0 || bc->partner_face[f] > 5)
+        return FEST_ERR_ARG;
+      int pf = bc->partner_face[f];
+      int na = (f / 2 == 0 ? dims->jmx : dims->imx), nb = (f / 2 == 2 ? dims->jmx : dims->kmx);
+      int pa = (pf / 2 == 0 ? dims->jmx : dims->imx), pb = (pf / 2 == 2 ? dims->jmx : dims->kmx);
+      if (na != pa || nb != pb) return FEST_ERR_ARG;
+      // the exchange copies interior layers 1..3 of the partner face
+      int n = f / 2 == 0 ? dims->imx : f / 2 == 1 ? dims->jmx : dims->kmx;
+      int pn = pf / 2 == 0 ? dims->imx : pf / 2 == 1 ? dims->jmx : dims->kmx;
+      if (n - 1 < 3 || pn - 1 < 3) return FEST_ERR_ARG;
+    }
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return FEST_ERR_NO_DEVICE;
+  fest_handle* h = new fest_handle();
+  h->ext = *dims;
+  h->flow = *flow;
+  h->sc = *scheme;
+  h->bc = *bc;
+  fill_params(h);
+  int rc = FEST_OK;
+  if (cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return FEST_ERR_CUDA;
+  }
+  const Dims& d = h->p.d;
+  Sizes z = sizes_of(d, h->p.n_grad);
+  DevBlock& b = h->d;
+  auto A = [&](double** p, long long n) {
+    if (rc == FEST_OK) rc = dalloc(h, p, n);
+  };
+  A(&b.qp, z.qp); A(&b.Temp, z.pad); A(&b.cells, z.cells); A(&b.nodes, z.nodes);
+  for (int dir = 0; dir < 3; ++dir) {
+    A(&b.faces[dir], z.faces[dir]);
+    A(&b.fsL[dir], z.fs[dir]);
+    A(&b.fsR[dir], z.fs[dir]);
+    A(&b.flux[dir], z.fl[dir]);
+    A(&b.grad[dir], z.grad);
+  }
+  A(&b.res, z.res); A(&b.mu, z.pad); A(&b.mut, z.pad); A(&b.F1, z.pad); A(&b.dist, z.pad);
+  A(&b.dt, z.dt); A(&b.Ustore, z.qp); A(&b.Rstore, z.res); A(&b.red, kRedSlots);
+  A(&h->d_resnorm, 16);
+  if (rc == FEST_OK) {
+    if (cudaMalloc((void**)&b.err, sizeof(int)) != cudaSuccess) rc = FEST_ERR_NOMEM;
+    else {
+      h->allocs.push_back(b.err);
+      cudaMemsetAsync(b.err, 0, sizeof(int), h->s);
+    }
+  }
+  if (rc == FEST_OK) {
+    // setup_viscosity: mu = mu_ref everywhere (viscosity.f90:562-566)
+    k_fill<<<(unsigned)((z.pad + 255) / 256), 256, 0, h->s>>>(b.mu, z.pad, flow->mu_ref);
+    ++h->launches;
+    BlockRef self{b, d};
+    if (cudaMalloc((void**)&h->d_table, sizeof(BlockRef)) != cudaSuccess) rc = FEST_ERR_NOMEM;
+    else {
+      h->allocs.push_back(h->d_table);
+      cudaMemcpyAsync(h->d_table, &self, sizeof(BlockRef), cudaMemcpyHostToDevice, h->s);
+    }
+  }
+  if (rc == FEST_OK) rc = finish(h);
+  if (rc != FEST_OK) {
+    fest_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return FEST_OK;
+}
+
+int fest_destroy(fest_handle* h) {
+  if (!h) return FEST_OK;
+  if (h->s) cudaStreamSynchronize(h->s);
+  if (h->fused) fused_destroy(h->fused);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->s) cudaStreamDestroy(h->s);
+  delete h;
+  return FEST_OK;
+}
+
+int fest_set_precision(fest_handle* h, int precision) {
+  if (!h || (precision != FEST_FP64 && precision != FEST_MIXED)) return FEST_ERR_ARG;
+  h->precision = precision;
+  return FEST_OK;
+}
+
+int fest_last_device_error(fest_handle* h) {
+  if (!h) return FEST_ERR_ARG;
+  return finish(h);
+}
+
+long long fest_kernel_launches(const fest_handle* h) { return h ? h->launches : 0; }
+
+long long fest_array_size(const fest_handle* h, int which) { return h ? arr_size(h, which) : 0; }
+
+int fest_set_array(fest_handle* h, int which, const double* host) {
+  if (!h || !host) return FEST_ERR_ARG;
+  double* d = arr_ptr(h, which);
+  if (!d) return FEST_ERR_ARG;
+  RET(up(h, d, host, arr_size(h, which)));
+  return finish(h);
+}
+
+int fest_get_array(fest_handle* h, int which, double* host) {
+  if (!h || !host) return FEST_ERR_ARG;
+  double* d = arr_ptr(h, which);
+  if (!d) return FEST_ERR_ARG;
+  RET(down(h, host, d, arr_size(h, which)));
+  return finish(h);
+}
+
+int fest_setup_geometry(fest_handle* h, double* nodes, double* cells, double* Ifaces,
+                        double* Jfaces, double* Kfaces) {
+  if (!h || !nodes) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.nodes, nodes, z.nodes));
+  launch_geometry(h->p, h->d, h->L());
+  RET(down(h, nodes, h->d.nodes, z.nodes));
+  RET(down(h, cells, h->d.cells, z.cells));
+  RET(down(h, Ifaces, h->d.faces[0], z.faces[0]));
+  RET(down(h, Jfaces, h->d.faces[1], z.faces[1]));
+  RET(down(h, Kfaces, h->d.faces[2], z.faces[2]));
+  return finish(h);
+}
+
+int fest_set_metrics(fest_handle* h, const double* cells, const double* Ifaces,
+                     const double* Jfaces, const double* Kfaces) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.cells, cells, z.cells));
+  RET(up(h, h->d.faces[0], Ifaces, z.faces[0]));
+  RET(up(h, h->d.faces[1], Jfaces, z.faces[1]));
+  RET(up(h, h->d.faces[2], Kfaces, z.faces[2]));
+  return finish(h);
+}
+
+int fest_find_wall_dist(fest_handle* h, const double* wall_xyz, int n_wall, double* dist) {
+  if (!h || !wall_xyz || n_wall <= 0) return FEST_ERR_ARG;
+  const Dims& d = h->p.d;
+  if (n_wall > h->n_wall_cap) {
+    if (h->d_wall) cudaFree(h->d_wall);
+    CK(cudaMalloc((void**)&h->d_wall, sizeof(double) * 3 * (size_t)n_wall));
+    h->n_wall_cap = n_wall;
+  }
+  if (!h->d_nodedist) RET(dalloc(h, &h->d_nodedist, (long long)(d.imx + 6) * (d.jmx + 6) * (d.kmx + 6)));
+  RET(up(h, h->d_wall, wall_xyz, 3LL * n_wall));
+  launch_wall_dist(h->p, h->d, h->d_wall, n_wall, h->d_nodedist, h->L());
+  RET(down(h, dist, h->d.dist, d.P));
+  int rc = finish(h);
+  cudaFree(h->d_wall);
+  h->d_wall = nullptr;
+  h->n_wall_cap = 0;
+  return rc;
+}
+
+int fest_set_wall_dist(fest_handle* h, const double* dist) {
+  if (!h || !dist) return FEST_ERR_ARG;
+  RET(up(h, h->d.dist, dist, h->p.d.P));
+  return finish(h);
+}
+
+int fest_upload_state(fest_handle* h, const double* qp) {
+  if (!h || !qp) return FEST_ERR_ARG;
+  RET(up(h, h->d.qp, qp, h->p.d.P * h->p.d.nv));
+  if (h->fused) fused_invalidate(h->fused);
+  return finish(h);
+}
+
+int fest_download_state(fest_handle* h, double* qp) {
+  if (!h || !qp) return FEST_ERR_ARG;
+  if (h->fused && h->precision == FEST_MIXED) RET(fused_export_state(h->fused, h->d.qp, h->s));
+  RET(down(h, qp, h->d.qp, h->p.d.P * h->p.d.nv));
+  return finish(h);
+}
+
+int fest_populate_ghost_primitive(fest_handle* h, double* qp, int current_iter) {
+  if (!h) return FEST_ERR_ARG;
+  long long n = h->p.d.P * h->p.d.nv;
+  RET(up(h, h->d.qp, qp, n));
+  launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
+  RET(down(h, qp, h->d.qp, n));
+  return finish(h);
+}
+
+int fest_compute_temperature(fest_handle* h, const double* qp, double* Temp) {
+  if (!h) return FEST_ERR_ARG;
+  RET(up(h, h->d.qp, qp, h->p.d.P * h->p.d.nv));
+  launch_temperature(h->p, h->d, h->L());
+  RET(down(h, Temp, h->d.Temp, h->p.d.P));
+  return finish(h);
+}
+
+static int face_state_call(fest_handle* h, const double* qp, double* xl, double* xr, double* yl,
+                           double* yr, double* zl, double* zr, int mode) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.qp, qp, z.qp));
+  double* hs[6] = {xl, xr, yl, yr, zl, zr};
+  if (mode == 2)
+    for (int m = 0; m < 6; ++m) RET(up(h, m % 2 ? h->d.fsR[m / 2] : h->d.fsL[m / 2], hs[m], z.fs[m / 2]));
+  launch_face_states(h->p, h->d, mode, h->L());
+  for (int m = 0; m < 6; ++m) RET(down(h, hs[m], m % 2 ? h->d.fsR[m / 2] : h->d.fsL[m / 2], z.fs[m / 2]));
+  return finish(h);
+}
+
+int fest_compute_face_interpolant(fest_handle* h, const double* qp, double* xl, double* xr,
+                                  double* yl, double* yr, double* zl, double* zr) {
+  return face_state_call(h, qp, xl, xr, yl, yr, zl, zr, 0);
+}
+
+int fest_reconstruct_boundary_state(fest_handle* h, const double* qp, double* xl, double* xr,
+                                    double* yl, double* yr, double* zl, double* zr) {
+  return face_state_call(h, qp, xl, xr, yl, yr, zl, zr, 2);
+}
+
+int fest_compute_fluxes(fest_handle* h, double* F, double* G, double* H) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  launch_fluxes(h->p, h->d, h->L());
+  RET(down(h, F, h->d.flux[0], z.fl[0]));
+  RET(down(h, G, h->d.flux[1], z.fl[1]));
+  RET(down(h, H, h->d.flux[2], z.fl[2]));
+  return finish(h);
+}
+
+int fest_evaluate_all_gradients(fest_handle* h, const double* qp, const double* Temp,
+                                double* gx, double* gy, double* gz) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.qp, qp, z.qp));
+  RET(up(h, h->d.Temp, Temp, z.pad));
+  launch_gradients(h->p, h->d, h->L());
+  RET(down(h, gx, h->d.grad[0], z.grad));
+  RET(down(h, gy, h->d.grad[1], z.grad));
+  RET(down(h, gz, h->d.grad[2], z.grad));
+  return finish(h);
+}
+
+int fest_calculate_viscosity(fest_handle* h, const double* qp, double* mu, double* mu_t,
+                             double* sst_F1) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.qp, qp, z.qp));
+  launch_viscosity(h->p, h->d, h->L());
+  RET(down(h, mu, h->d.mu, z.pad));
+  RET(down(h, mu_t, h->d.mut, z.pad));
+  RET(down(h, sst_F1, h->d.F1, z.pad));
+  return finish(h);
+}
+
+int fest_compute_viscous_fluxes(fest_handle* h, const double* qp, double* F, double* G, double* H) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.qp, qp, z.qp));
+  RET(up(h, h->d.flux[0], F, z.fl[0]));
+  RET(up(h, h->d.flux[1], G, z.fl[1]));
+  RET(up(h, h->d.flux[2], H, z.fl[2]));
+  launch_viscous_fluxes(h->p, h->d, h->L());
+  RET(down(h, F, h->d.flux[0], z.fl[0]));
+  RET(down(h, G, h->d.flux[1], z.fl[1]));
+  RET(down(h, H, h->d.flux[2], z.fl[2]));
+  return finish(h);
+}
+
+int fest_compute_residue(fest_handle* h, const double* F, const double* G, const double* H,
+                         double* residue) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.flux[0], F, z.fl[0]));
+  RET(up(h, h->d.flux[1], G, z.fl[1]));
+  RET(up(h, h->d.flux[2], H, z.fl[2]));
+  launch_residue(h->p, h->d, false, h->L());
+  RET(down(h, residue, h->d.res, z.res));
+  return finish(h);
+}
+
+int fest_add_source_term_residue(fest_handle* h, const double* qp, double* residue) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.qp, qp, z.qp));
+  RET(up(h, h->d.res, residue, z.res));
+  launch_source(h->p, h->d, h->L());
+  RET(down(h, residue, h->d.res, z.res));
+  return finish(h);
+}
+
+int fest_compute_time_step(fest_handle* h, const double* qp, double CFL, double* delta_t) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.qp, qp, z.qp));
+  launch_time_step(h->p, h->d, CFL, h->L());
+  RET(down(h, delta_t, h->d.dt, z.dt));
+  return finish(h);
+}
+
+int fest_get_total_conservative_residue(fest_handle* h, double* qp, int current_iter,
+                                        double* residue) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.qp, qp, z.qp));
+  RET(residual_fp64(h, current_iter));
+  RET(down(h, qp, h->d.qp, z.qp));
+  RET(down(h, residue, h->d.res, z.res));
+  return finish(h);
+}
+
+int fest_get_next_solution(fest_handle* h, double* qp, int current_iter, double CFL,
+                           double* residue, double* delta_t) {
+  if (!h) return FEST_ERR_ARG;
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  RET(up(h, h->d.qp, qp, z.qp));
+  RET(next_solution_fp64(h, current_iter, CFL));
+  RET(down(h, qp, h->d.qp, z.qp));
+  RET(down(h, residue, h->d.res, z.res));
+  RET(down(h, delta_t, h->d.dt, z.dt));
+  return finish(h);
+}
+
+int fest_find_resnorm(fest_handle* h, double* res_abs) {
+  if (!h || !res_abs) return FEST_ERR_ARG;
+  launch_resnorm(h->p, h->d, h->d_resnorm, h->L());
+  double sums[NVMAX + 1];
+  RET(down(h, sums, h->d_resnorm, h->p.d.nv + 1));
+  RET(finish(h));
+  // setup_scale (resnorm.f90:128-169) and assemble (resnorm.f90:211-225)
+  const fest_flow& f = h->flow;
+  double sc[NVMAX + 1];
+  sc[0] = 1.;
+  sc[1] = f.density_inf * f.vel_mag;
+  sc[2] = sc[3] = sc[4] = f.density_inf * f.vel_mag * f.vel_mag;
+  sc[5] = (0.5 * f.density_inf * (f.vel_mag * f.vel_mag * f.vel_mag) +
+           ((f.gm / (f.gm - 1.)) * f.pressure_inf));
+  sc[6] = f.density_inf * f.vel_mag * f.tk_inf;
+  sc[7] = f.density_inf * f.vel_mag * f.tw_inf;
+  res_abs[0] = fabs(sums[0] / sc[0]);
+  for (int l = 1; l <= h->p.d.nv; ++l) res_abs[l] = sqrt(sums[l] / (sc[l] * sc[l]));
+  return FEST_OK;
+}
+
+int fest_step(fest_handle* h, int n_iters, int first_iter, double CFL, double* res_abs) {
+  if (!h || n_iters < 0) return FEST_ERR_ARG;
+  if (h->precision == FEST_MIXED || fused_supported(h->p, FEST_FP64)) {
+    if (!h->fused) {
+      int rc = fused_create(h->p, h->d, h->d_table, h->s, &h->fused);
+      if (rc) return rc;
+    }
+    int rc = fused_run(h->fused, h->p, h->d, h->precision, n_iters, first_iter, CFL, h->s, &h->launches);
+    if (rc) return rc;
+  } else {
+    for (int n = 0; n < n_iters; ++n) RET(next_solution_fp64(h, first_iter + n, CFL));
+  }
+  if (res_abs) {
+    if (h->fused && h->precision == FEST_MIXED) RET(fused_export_residual(h->fused, h->d, h->s));
+    return fest_find_resnorm(h, res_abs);
+  }
+  return finish(h);
+}
+
+}  // extern "C"

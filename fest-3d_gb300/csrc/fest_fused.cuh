@@ -1,0 +1,24 @@
+// fest_fused.cuh - the fused fast path: one sweep kernel per RK stage that
+// reconstructs, evaluates fluxes, sums the residual and updates the state,
+// in FP32 (FEST_MIXED) or FP64 arithmetic.
+#pragma once
+#include "fest_kernels.cuh"
+
+namespace fest {
+
+struct FusedState;
+// true when the fused sweep covers this scheme in this precision
+bool fused_supported(const Params& p, int precision);
+int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cudaStream_t s,
+                 FusedState** out);
+void fused_destroy(FusedState* f);
+// the FP64 state in the DevBlock changed: re-seed the fused buffers
+void fused_invalidate(FusedState* f);
+int fused_run(FusedState* f, const Params& p, const DevBlock& b, int precision, int n_iters,
+              int first_iter, double CFL, cudaStream_t s, long long* launches);
+// copy the fused path's FP64 state into qp (the reference layout)
+int fused_export_state(FusedState* f, double* qp, cudaStream_t s);
+// materialise the last stage's residual and boundary fluxes for find_resnorm
+int fused_export_residual(FusedState* f, const DevBlock& b, cudaStream_t s);
+
+}  // namespace fest

@@ -1,0 +1,56 @@
+// fest_kernels.cuh - host-side launchers of the module kernels (FP64, the
+// reference's structure: one kernel per Fortran procedure, module arrays
+// materialised in HBM).
+#pragma once
+#include "fest_common.cuh"
+
+namespace fest {
+
+// device arrays of one block, all in the reference's Fortran layouts
+struct DevBlock {
+  double *qp, *Temp, *cells, *faces[3], *nodes;
+  double *fsL[3], *fsR[3];  // x/y/z_qp_left/right
+  double *flux[3];          // F, G, H
+  double *res, *grad[3], *mu, *mut, *F1, *dist, *dt, *Ustore, *Rstore;
+  double *red;              // reduction scratch (kRedSlots doubles)
+  int *err;                 // device error word
+};
+constexpr int kRedSlots = 1 << 16;
+
+// a block as seen by the interface exchange of another block
+struct BlockRef {
+  DevBlock b;
+  Dims d;
+};
+
+struct Launcher {
+  cudaStream_t s;
+  long long* count;  // kernels launched through this launcher
+};
+
+// ghost cells: interface exchange + populate_ghost_primitive + corners
+// d_table: device array of every block a face of this block may pair with
+void launch_ghosts(const Params& p, const DevBlock& b, const BlockRef* d_table, int iter,
+                   const Launcher& L);
+bool ghosts_need_sequential(const Params& p);
+void launch_temperature(const Params& p, const DevBlock& b, const Launcher& L);
+// mode 0: compute_face_interpolant only; 1: + reconstruct_boundary_state;
+// 2: reconstruct_boundary_state alone on the held face states
+void launch_face_states(const Params& p, const DevBlock& b, int mode, const Launcher& L);
+void launch_fluxes(const Params& p, const DevBlock& b, const Launcher& L);
+void launch_gradients(const Params& p, const DevBlock& b, const Launcher& L);
+void launch_viscosity(const Params& p, const DevBlock& b, const Launcher& L);
+void launch_viscous_fluxes(const Params& p, const DevBlock& b, const Launcher& L);
+void launch_residue(const Params& p, const DevBlock& b, bool with_source, const Launcher& L);
+void launch_source(const Params& p, const DevBlock& b, const Launcher& L);
+void launch_time_step(const Params& p, const DevBlock& b, double CFL, const Launcher& L);
+void launch_update(const Params& p, const DevBlock& b, double TF, double SF, int TU, int use_store,
+                   const Launcher& L);
+void launch_blend(const Params& p, const DevBlock& b, double a, double c, const Launcher& L);
+// res_abs partials of this block: out[0] mass imbalance, out[l] sum R_l^2
+void launch_resnorm(const Params& p, const DevBlock& b, double* d_out, const Launcher& L);
+void launch_geometry(const Params& p, const DevBlock& b, const Launcher& L);
+void launch_wall_dist(const Params& p, const DevBlock& b, const double* d_wall, int n_wall,
+                      double* d_node_dist, const Launcher& L);
+
+}  // namespace fest

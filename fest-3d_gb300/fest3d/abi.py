@@ -198,7 +198,8 @@ _SIGS = {
     "fest_find_resnorm": [C.c_void_p, _DP],
     "fest_step": [C.c_void_p, C.c_int, C.c_int, C.c_double, _DP],
 }
-EXPORTED = tuple(_SIGS) + ("fest_kernel_launches",)
+EXPORTED = tuple(_SIGS) + ("fest_kernel_launches", "fest_array_size", "fest_set_array",
+                          "fest_get_array")
 
 
 def load(path=None):

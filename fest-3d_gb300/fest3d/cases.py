@@ -1,0 +1,218 @@
+"""Synthetic, seeded inputs in the reference's own layouts.
+
+No dataset is involved: every workload is analytic or drawn from a fixed
+seed.  Node arrays hold interior nodes (1:imx,1:jmx,1:kmx) as FEST-3D's grid
+reader fills them (grid.f90:110-127); ghost nodes are left to
+``setup_geometry``.  States fill the whole padded block, ghosts included, as
+init_state_with_infinity_values does (state.f90:195-278).
+"""
+import numpy as np
+
+from . import abi
+
+
+def empty_nodes(ext):
+    return np.zeros((3, ext.imx + 6, ext.jmx + 6, ext.kmx + 6), order="F")
+
+
+def set_interior_nodes(nodes, x, y, z):
+    """x,y,z of shape (imx,jmx,kmx) -> nodes(1:imx,1:jmx,1:kmx)."""
+    imx, jmx, kmx = x.shape
+    nodes[0, 3:3 + imx, 3:3 + jmx, 3:3 + kmx] = x
+    nodes[1, 3:3 + imx, 3:3 + jmx, 3:3 + kmx] = y
+    nodes[2, 3:3 + imx, 3:3 + jmx, 3:3 + kmx] = z
+    return nodes
+
+
+def box_nodes(ext, L=(1.0, 1.0, 1.0), perturb=0.0, seed=0, stretch_j=1.0):
+    """Cartesian box, optional wall-normal stretching in j and a smooth
+    sinusoidal node perturbation of amplitude perturb x local spacing."""
+    imx, jmx, kmx = ext.imx, ext.jmx, ext.kmx
+    s = np.linspace(0.0, 1.0, imx)
+    if stretch_j != 1.0:
+        r = stretch_j ** np.arange(jmx - 1)
+        t = np.concatenate([[0.0], np.cumsum(r)])
+        t = t / t[-1]
+    else:
+        t = np.linspace(0.0, 1.0, jmx)
+    u = np.linspace(0.0, 1.0, kmx)
+    X, Y, Z = np.meshgrid(s * L[0], t * L[1], u * L[2], indexing="ij")
+    if perturb:
+        rng = np.random.default_rng(seed)
+        dx, dy, dz = L[0] / (imx - 1), L[1] / (jmx - 1), L[2] / (kmx - 1)
+        ph = rng.uniform(0, 2 * np.pi, 6)
+        fx = np.sin(2 * np.pi * Y / L[1] + ph[0]) * np.sin(2 * np.pi * Z / L[2] + ph[1])
+        fy = np.sin(2 * np.pi * X / L[0] + ph[2]) * np.sin(2 * np.pi * Z / L[2] + ph[3])
+        fz = np.sin(2 * np.pi * X / L[0] + ph[4]) * np.sin(2 * np.pi * Y / L[1] + ph[5])
+        X = X + perturb * dx * fx
+        Y = Y + perturb * dy * fy
+        Z = Z + perturb * dz * fz
+    return set_interior_nodes(empty_nodes(ext), X, Y, Z)
+
+
+def bump_nodes(ext, x0=-1.5, x1=1.5, top=0.8, stretch=1.02, depth=0.1):
+    """Channel over y_b = 0.0625 exp(-25 x^2), geometric stretching in j."""
+    imx, jmx, kmx = ext.imx, ext.jmx, ext.kmx
+    x = np.linspace(x0, x1, imx)
+    yb = 0.0625 * np.exp(-25.0 * x * x)
+    r = stretch ** np.arange(jmx - 1)
+    t = np.concatenate([[0.0], np.cumsum(r)])
+    t = t / t[-1]
+    z = np.linspace(0.0, depth, kmx)
+    X = np.repeat(np.repeat(x[:, None, None], jmx, 1), kmx, 2)
+    Y = yb[:, None, None] + (top - yb)[:, None, None] * t[None, :, None]
+    Y = np.repeat(Y, kmx, 2)
+    Z = np.broadcast_to(z[None, None, :], (imx, jmx, kmx)).copy()
+    return set_interior_nodes(empty_nodes(ext), X, Y, Z)
+
+
+def plate_nodes(ext, length=2.0, dy1=1e-6, stretch=1.12, height=1.0, depth=0.01):
+    """Flat plate x in [0, length] clustered at the leading edge; wall-normal
+    first cell dy1 growing geometrically by stretch, capped at height."""
+    imx, jmx, kmx = ext.imx, ext.jmx, ext.kmx
+    x = length * np.linspace(0.0, 1.0, imx) ** 1.5
+    dy = dy1 * stretch ** np.arange(jmx - 1)
+    y = np.concatenate([[0.0], np.cumsum(dy)])
+    if y[-1] > height:
+        y = y * (height / y[-1])
+    z = np.linspace(0.0, depth, kmx)
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    return set_interior_nodes(empty_nodes(ext), X, Y, Z)
+
+
+def uniform_state(ext, flow, tk=0.0, tw=0.0):
+    qp = abi.farray(ext, "qp")
+    qp[..., 0] = flow.density_inf
+    qp[..., 1] = flow.x_speed_inf
+    qp[..., 2] = flow.y_speed_inf
+    qp[..., 3] = flow.z_speed_inf
+    qp[..., 4] = flow.pressure_inf
+    if ext.n_var > 5:
+        qp[..., 5] = tk
+        qp[..., 6] = tw
+    return qp
+
+
+def random_state(ext, seed=0, mach=0.3, amp=0.1, p0=101325.0, rho0=1.2, tk=1.0, tw=1000.0):
+    """Smooth 3-mode Fourier field over the padded block: rho in
+    rho0*(1 +- amp), |u| up to mach*c, p0*(1 +- amp), positive tk/tw."""
+    rng = np.random.default_rng(seed)
+    ni, nj, nk = ext.imx + 5, ext.jmx + 5, ext.kmx + 5
+    I, J, K = np.meshgrid(np.arange(ni) / ni, np.arange(nj) / nj, np.arange(nk) / nk, indexing="ij")
+
+    def field():
+        f = np.zeros_like(I)
+        for _ in range(3):
+            a = rng.uniform(-1, 1)
+            kx, ky, kz = rng.integers(1, 4, 3)
+            ph = rng.uniform(0, 2 * np.pi, 3)
+            f += a * np.sin(2 * np.pi * kx * I + ph[0]) * np.sin(2 * np.pi * ky * J + ph[1]) * \
+                np.cos(2 * np.pi * kz * K + ph[2])
+        return f / 3.0
+
+    c = np.sqrt(1.4 * p0 / rho0)
+    qp = abi.farray(ext, "qp")
+    qp[..., 0] = rho0 * (1 + amp * field())
+    for l in (1, 2, 3):
+        qp[..., l] = mach * c * field()
+    qp[..., 4] = p0 * (1 + amp * field())
+    if ext.n_var > 5:
+        qp[..., 5] = tk * (1 + 0.5 * field())
+        qp[..., 6] = tw * (1 + 0.5 * field())
+    return qp
+
+
+# ---------------------------------------------------------------------------
+# the benchmark configurations (one structured block each)
+def ldc_case(nc=(64, 64, 4)):
+    """Laminar lid-driven cavity: 64x64x4 cells over 1 x 1 x 0.0625 m,
+    gamma 1.4, R 287, rho 1.2, p 101325, lid at jmax moving +x at 34.7 m/s
+    (id -3, FIX_DENSITY/X_SPEED, COPY_PRESSURE), other x/y faces adiabatic
+    no-slip walls (-5), z faces periodic (-10, kmin<->kmax); constant mu for
+    Re=100 on the lid; MUSCL + AUSM, local time step, forward Euler, CFL 0.5."""
+    ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 5)
+    flow = abi.make_flow(density_inf=1.2, x_speed_inf=0.0, pressure_inf=101325.0,
+                         mu_ref=1.2 * 34.7 * 1.0 / 100.0, mu_variation="constant")
+    scheme = abi.make_scheme(scheme_name="ausm", interpolant="muscl", time_step_accuracy="none",
+                             time_stepping_method="l")
+    fixed = {k: [0.0] * 6 for k in ("fixed_density", "fixed_x_speed", "fixed_y_speed",
+                                    "fixed_z_speed", "fixed_wall_temperature")}
+    fixed["fixed_density"][3] = 1.2
+    fixed["fixed_x_speed"][3] = 34.7
+    bc = abi.make_bc([-5, -5, -5, -3, -10, -10], partners={4: (0, 5), 5: (0, 4)}, **fixed)
+    nodes = box_nodes(ext, L=(1.0, 1.0, 0.0625))
+    qp = uniform_state(ext, flow)
+    return dict(name="lid-driven cavity 64x64x4, MUSCL+AUSM, laminar, forward Euler",
+                ext=ext, flow=flow, scheme=scheme, bc=bc, nodes=nodes, qp=qp, CFL=0.5)
+
+
+def bump_case(nc=(256, 96, 4), mach=0.5):
+    """Inviscid channel over a smooth bump: 256x96x4 cells, subsonic total
+    pressure inlet (-11) for Mach 0.5, back-pressure outlet (-4), slip walls
+    (-6) top and bottom, periodic z (-10); WENO5 + SLAU, TVD-RK3, CFL 0.8."""
+    ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 5)
+    p0, rho0, gm = 101325.0, 1.2, 1.4
+    c = np.sqrt(gm * p0 / rho0)
+    flow = abi.make_flow(density_inf=rho0, x_speed_inf=mach * c, pressure_inf=p0, mu_ref=0.0)
+    scheme = abi.make_scheme(scheme_name="slau", interpolant="weno", time_step_accuracy="TVDRK3",
+                             time_stepping_method="l")
+    pt = p0 * (1 + 0.5 * (gm - 1) * mach * mach) ** (gm / (gm - 1))
+    fixed = {k: [0.0] * 6 for k in ("fixed_pressure", "fixed_Tpressure")}
+    fixed["fixed_pressure"][1] = p0
+    fixed["fixed_Tpressure"][0] = pt
+    bc = abi.make_bc([-11, -4, -6, -6, -10, -10], partners={4: (0, 5), 5: (0, 4)}, **fixed)
+    nodes = bump_nodes(ext)
+    qp = uniform_state(ext, flow)
+    return dict(name="smooth bump 256x96x4, WENO5+SLAU, inviscid, TVD-RK3", ext=ext, flow=flow,
+                scheme=scheme, bc=bc, nodes=nodes, qp=qp, CFL=0.8)
+
+
+def plate_case(nc=(192, 128, 1), mach=0.2, Re_per_m=5e6, Tu=0.1, mut_ratio=0.01):
+    """Turbulent flat plate with k-omega SST: 192x128x1 cells (kmx=2), one
+    block whose jmin face is the no-slip adiabatic plate (-5); subsonic inlet
+    (-3) with free-stream k/omega, outlets (-4) at imax and jmax, slip k
+    faces (-6); MUSCL + AUSM-UP, RK4, CFL 1.0."""
+    ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 7)
+    p0, T0, gm, R = 101325.0, 300.0, 1.4, 287.0
+    rho0 = p0 / (R * T0)
+    c = np.sqrt(gm * p0 / rho0)
+    U = mach * c
+    mu_ref = rho0 * U / Re_per_m
+    tk = 1.5 * (U * Tu / 100.0) ** 2
+    tw = rho0 * tk / (mu_ref * mut_ratio)
+    flow = abi.make_flow(density_inf=rho0, x_speed_inf=U, pressure_inf=p0, mu_ref=mu_ref,
+                         mu_variation="sutherland_law", T_ref=T0, tk_inf=tk, tw_inf=tw)
+    scheme = abi.make_scheme(scheme_name="ausmUP", interpolant="muscl", time_step_accuracy="RK4",
+                             time_stepping_method="l", turbulence="sst")
+    fixed = {k: [0.0] * 6 for k in ("fixed_density", "fixed_x_speed", "fixed_y_speed",
+                                    "fixed_z_speed", "fixed_pressure", "fixed_tk", "fixed_tw",
+                                    "fixed_wall_temperature")}
+    fixed["fixed_density"][0] = rho0
+    fixed["fixed_x_speed"][0] = U
+    fixed["fixed_tk"][0] = tk
+    fixed["fixed_tw"][0] = tw
+    fixed["fixed_pressure"][1] = p0
+    bc = abi.make_bc([-3, -4, -5, -4, -6, -6], **fixed)
+    nodes = plate_nodes(ext)
+    qp = uniform_state(ext, flow, tk=tk, tw=tw)
+    return dict(name="SST flat plate 192x128x1, MUSCL+AUSM-UP, RK4", ext=ext, flow=flow,
+                scheme=scheme, bc=bc, nodes=nodes, qp=qp, CFL=1.0)
+
+
+def wall_nodes_of(nodes, ext, bc):
+    """Wall node list (surface_points, wall.f90:200-286): every node of a
+    face with id -5, in the reference's face order."""
+    pts = []
+    imx, jmx, kmx = ext.imx, ext.jmx, ext.kmx
+    rng = {0: ((1, 1), (1, jmx), (1, kmx)), 1: ((imx, imx), (1, jmx), (1, kmx)),
+           2: ((1, imx), (1, 1), (1, kmx)), 3: ((1, imx), (jmx, jmx), (1, kmx)),
+           4: ((1, imx), (1, jmx), (1, 1)), 5: ((1, imx), (1, jmx), (kmx, kmx))}
+    for f in range(6):
+        if bc.id[f] != -5:
+            continue
+        (i0, i1), (j0, j1), (k0, k1) = rng[f]
+        for k in range(k0, k1 + 1):
+            for j in range(j0, j1 + 1):
+                for i in range(i0, i1 + 1):
+                    pts.append(nodes[:, i + 2, j + 2, k + 2])
+    return np.array(pts, dtype=np.float64)

@@ -1,0 +1,120 @@
+"""A Python object over one ``fest_handle`` of the C ABI.
+
+Every method is one C call (include/fest_gpu.h) with the reference's
+Fortran-shaped arrays; ``None`` passes NULL (keep the device-resident copy).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+ARR = {"qp": 0, "Temp": 1, "cells": 2, "Ifaces": 3, "Jfaces": 4, "Kfaces": 5, "nodes": 6,
+       "x_qp_left": 7, "x_qp_right": 8, "y_qp_left": 9, "y_qp_right": 10, "z_qp_left": 11,
+       "z_qp_right": 12, "F": 13, "G": 14, "H": 15, "residue": 16, "gradqp_x": 17,
+       "gradqp_y": 18, "gradqp_z": 19, "mu": 20, "mu_t": 21, "sst_F1": 22, "dist": 23,
+       "delta_t": 24}
+
+
+class Handle:
+    def __init__(self, ext, flow, scheme, bc, lib=None):
+        self.lib = lib or abi.load()
+        self.ext, self.flow, self.scheme, self.bc = ext, flow, scheme, bc
+        self.h = C.c_void_p()
+        abi.check(self.lib.fest_create(C.byref(ext), C.byref(flow), C.byref(scheme), C.byref(bc),
+                                       C.byref(self.h)), "fest_create")
+        ng = 6 if ext.n_var == 7 else 4
+        sh = abi.shapes(ext, ng)
+        self.shape = {"qp": sh["qp"], "Temp": sh["pad"], "cells": sh["cells"],
+                      "Ifaces": sh["Ifaces"], "Jfaces": sh["Jfaces"], "Kfaces": sh["Kfaces"],
+                      "nodes": sh["nodes"], "x_qp_left": sh["x_qp"], "x_qp_right": sh["x_qp"],
+                      "y_qp_left": sh["y_qp"], "y_qp_right": sh["y_qp"], "z_qp_left": sh["z_qp"],
+                      "z_qp_right": sh["z_qp"], "F": sh["F"], "G": sh["G"], "H": sh["H"],
+                      "residue": sh["residue"], "gradqp_x": sh["grad"], "gradqp_y": sh["grad"],
+                      "gradqp_z": sh["grad"], "mu": sh["pad"], "mu_t": sh["pad"],
+                      "sst_F1": sh["pad"], "dist": sh["pad"], "delta_t": sh["delta_t"]}
+
+    def close(self):
+        if self.h:
+            self.lib.fest_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name, *args):
+        return abi.check(getattr(self.lib, name)(self.h, *args), name)
+
+    def get(self, name):
+        a = np.empty(self.shape[name], order="F")
+        self._call("fest_get_array", ARR[name], abi.ptr(a))
+        return a
+
+    def set(self, name, a):
+        a = np.asfortranarray(a, dtype=np.float64)
+        self._call("fest_set_array", ARR[name], abi.ptr(a))
+
+    @property
+    def launches(self):
+        return self.lib.fest_kernel_launches(self.h)
+
+    def set_precision(self, p):
+        self._call("fest_set_precision", int(p))
+
+    def setup_geometry(self, nodes):
+        nodes = np.array(nodes, order="F", dtype=np.float64)
+        self._call("fest_setup_geometry", abi.ptr(nodes), None, None, None, None)
+        return nodes
+
+    def set_metrics(self, cells, If, Jf, Kf):
+        self._call("fest_set_metrics", abi.ptr(cells), abi.ptr(If), abi.ptr(Jf), abi.ptr(Kf))
+
+    def find_wall_dist(self, wall_xyz):
+        w = np.ascontiguousarray(wall_xyz, dtype=np.float64)
+        d = np.empty(self.shape["dist"], order="F")
+        self._call("fest_find_wall_dist", w.ctypes.data_as(C.POINTER(C.c_double)), len(w),
+                   abi.ptr(d))
+        return d
+
+    def upload_state(self, qp):
+        self._call("fest_upload_state", abi.ptr(np.asfortranarray(qp)))
+
+    def download_state(self):
+        q = np.empty(self.shape["qp"], order="F")
+        self._call("fest_download_state", abi.ptr(q))
+        return q
+
+    def populate_ghost_primitive(self, qp, it):
+        q = np.array(qp, order="F")
+        self._call("fest_populate_ghost_primitive", abi.ptr(q), int(it))
+        return q
+
+    def compute_temperature(self, qp=None):
+        T = np.empty(self.shape["Temp"], order="F")
+        self._call("fest_compute_temperature", abi.ptr(qp), abi.ptr(T))
+        return T
+
+    def get_next_solution(self, qp, it, CFL):
+        q = np.array(qp, order="F")
+        self._call("fest_get_next_solution", abi.ptr(q), int(it), float(CFL), None, None)
+        return q
+
+    def residual(self, qp, it):
+        q = np.array(qp, order="F")
+        r = np.empty(self.shape["residue"], order="F")
+        self._call("fest_get_total_conservative_residue", abi.ptr(q), int(it), abi.ptr(r))
+        return q, r
+
+    def step(self, n, first_iter, CFL, with_norm=True):
+        out = np.zeros(8) if with_norm else None
+        self._call("fest_step", int(n), int(first_iter), float(CFL),
+                   out.ctypes.data_as(C.POINTER(C.c_double)) if with_norm else None)
+        return out[:self.ext.n_var + 1] if with_norm else None
+
+    def resnorm(self):
+        out = np.zeros(8)
+        self._call("fest_find_resnorm", out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out[:self.ext.n_var + 1]

@@ -152,6 +152,23 @@ int fest_set_wall_dist(fest_handle *h, const double *dist);
 int fest_upload_state(fest_handle *h, const double *qp);
 int fest_download_state(fest_handle *h, double *qp);
 
+/* ---- module arrays held by the handle -----------------------------------
+ * The reference keeps these as module variables (face_interpolant.f90:17-22,
+ * gradients.f90:17-19, viscosity.f90:41-44, global_sst.f90:25,
+ * wall_dist.f90, time.f90, scheme.f90:29-63); a drop-in shim reads and writes
+ * them through these two calls.  Sizes are in doubles. */
+enum { FEST_ARR_QP = 0, FEST_ARR_TEMP, FEST_ARR_CELLS, FEST_ARR_IFACES,
+       FEST_ARR_JFACES, FEST_ARR_KFACES, FEST_ARR_NODES,
+       FEST_ARR_X_QP_LEFT, FEST_ARR_X_QP_RIGHT, FEST_ARR_Y_QP_LEFT,
+       FEST_ARR_Y_QP_RIGHT, FEST_ARR_Z_QP_LEFT, FEST_ARR_Z_QP_RIGHT,
+       FEST_ARR_F, FEST_ARR_G, FEST_ARR_H, FEST_ARR_RESIDUE,
+       FEST_ARR_GRADQP_X, FEST_ARR_GRADQP_Y, FEST_ARR_GRADQP_Z,
+       FEST_ARR_MU, FEST_ARR_MU_T, FEST_ARR_SST_F1, FEST_ARR_DIST,
+       FEST_ARR_DELTA_T, FEST_ARR_COUNT };
+long long fest_array_size(const fest_handle *h, int which);
+int fest_set_array(fest_handle *h, int which, const double *host);
+int fest_get_array(fest_handle *h, int which, double *host);
+
 /* ---- module-level entry points (drop-ins for the Fortran procedures) --- */
 /* apply_interface (interface1.f90:96) + populate_ghost_primitive
  * (bc_primitive.f90:55): ghost layers of qp for every face, then the 0.33
