@@ -17,7 +17,8 @@ struct fest_handle {
   fest_flow flow;
   fest_scheme sc;
   fest_bc bc;
-  cudaStream_t s = nullptr;
+  cudaStream_t s = nullptr;      // stream in use
+  cudaStream_t own = nullptr;    // the handle's own stream
   DevBlock d{};
   BlockRef* d_table = nullptr;
   double* d_resnorm = nullptr;
@@ -121,6 +122,7 @@ void fill_params(fest_handle* h) {
   const fest_scheme& s = h->sc;
   p.flux = s.scheme_name; p.interp = s.interpolant; p.limiter = s.limiter; p.turb = s.turbulence;
   p.tstep = s.time_stepping_method; p.gdt = s.global_time_step;
+  p.integ = s.time_step_accuracy;
   p.lam[0] = s.ilimiter_switch; p.lam[1] = s.jlimiter_switch; p.lam[2] = s.klimiter_switch;
   p.tlim[0] = s.itlimiter_switch; p.tlim[1] = s.jtlimiter_switch; p.tlim[2] = s.ktlimiter_switch;
   p.pb[0] = s.iPB_switch; p.pb[1] = s.jPB_switch; p.pb[2] = s.kPB_switch;
@@ -197,6 +199,13 @@ long long arr_size(const fest_handle* h, int which) {
     case FEST_ARR_DELTA_T: return z.dt;
     default: return 0;
   }
+}
+
+// the fused path may hold the current state in one of its own buffers:
+// bring it back to the handle's qp before a module entry point reads it
+int sync_fused(fest_handle* h) {
+  if (h->fused) RET(fused_export_state(h->fused, h->d.qp, h->s));
+  return FEST_OK;
 }
 
 __global__ void k_fill(double* x, long long n, double v) {
@@ -325,6 +334,7 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
     delete h;
     return FEST_ERR_CUDA;
   }
+  h->own = h->s;
   const Dims& d = h->p.d;
   Sizes z = sizes_of(d, h->p.n_grad);
   DevBlock& b = h->d;
@@ -374,7 +384,7 @@ int fest_destroy(fest_handle* h) {
   if (h->s) cudaStreamSynchronize(h->s);
   if (h->fused) fused_destroy(h->fused);
   for (void* p : h->allocs) cudaFree(p);
-  if (h->s) cudaStreamDestroy(h->s);
+  if (h->own) cudaStreamDestroy(h->own);
   delete h;
   return FEST_OK;
 }
@@ -396,6 +406,7 @@ long long fest_array_size(const fest_handle* h, int which) { return h ? arr_size
 
 int fest_set_array(fest_handle* h, int which, const double* host) {
   if (!h || !host) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   double* d = arr_ptr(h, which);
   if (!d) return FEST_ERR_ARG;
   RET(up(h, d, host, arr_size(h, which)));
@@ -404,6 +415,7 @@ int fest_set_array(fest_handle* h, int which, const double* host) {
 
 int fest_get_array(fest_handle* h, int which, double* host) {
   if (!h || !host) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   double* d = arr_ptr(h, which);
   if (!d) return FEST_ERR_ARG;
   RET(down(h, host, d, arr_size(h, which)));
@@ -469,13 +481,14 @@ int fest_upload_state(fest_handle* h, const double* qp) {
 
 int fest_download_state(fest_handle* h, double* qp) {
   if (!h || !qp) return FEST_ERR_ARG;
-  if (h->fused && h->precision == FEST_MIXED) RET(fused_export_state(h->fused, h->d.qp, h->s));
+  RET(sync_fused(h));
   RET(down(h, qp, h->d.qp, h->p.d.P * h->p.d.nv));
   return finish(h);
 }
 
 int fest_populate_ghost_primitive(fest_handle* h, double* qp, int current_iter) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   long long n = h->p.d.P * h->p.d.nv;
   RET(up(h, h->d.qp, qp, n));
   launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
@@ -485,6 +498,7 @@ int fest_populate_ghost_primitive(fest_handle* h, double* qp, int current_iter) 
 
 int fest_compute_temperature(fest_handle* h, const double* qp, double* Temp) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   RET(up(h, h->d.qp, qp, h->p.d.P * h->p.d.nv));
   launch_temperature(h->p, h->d, h->L());
   RET(down(h, Temp, h->d.Temp, h->p.d.P));
@@ -494,6 +508,7 @@ int fest_compute_temperature(fest_handle* h, const double* qp, double* Temp) {
 static int face_state_call(fest_handle* h, const double* qp, double* xl, double* xr, double* yl,
                            double* yr, double* zl, double* zr, int mode) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
   double* hs[6] = {xl, xr, yl, yr, zl, zr};
@@ -516,6 +531,7 @@ int fest_reconstruct_boundary_state(fest_handle* h, const double* qp, double* xl
 
 int fest_compute_fluxes(fest_handle* h, double* F, double* G, double* H) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   launch_fluxes(h->p, h->d, h->L());
   RET(down(h, F, h->d.flux[0], z.fl[0]));
@@ -527,6 +543,7 @@ int fest_compute_fluxes(fest_handle* h, double* F, double* G, double* H) {
 int fest_evaluate_all_gradients(fest_handle* h, const double* qp, const double* Temp,
                                 double* gx, double* gy, double* gz) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
   RET(up(h, h->d.Temp, Temp, z.pad));
@@ -540,6 +557,7 @@ int fest_evaluate_all_gradients(fest_handle* h, const double* qp, const double* 
 int fest_calculate_viscosity(fest_handle* h, const double* qp, double* mu, double* mu_t,
                              double* sst_F1) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
   launch_viscosity(h->p, h->d, h->L());
@@ -551,6 +569,7 @@ int fest_calculate_viscosity(fest_handle* h, const double* qp, double* mu, doubl
 
 int fest_compute_viscous_fluxes(fest_handle* h, const double* qp, double* F, double* G, double* H) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
   RET(up(h, h->d.flux[0], F, z.fl[0]));
@@ -566,6 +585,7 @@ int fest_compute_viscous_fluxes(fest_handle* h, const double* qp, double* F, dou
 int fest_compute_residue(fest_handle* h, const double* F, const double* G, const double* H,
                          double* residue) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.flux[0], F, z.fl[0]));
   RET(up(h, h->d.flux[1], G, z.fl[1]));
@@ -577,6 +597,7 @@ int fest_compute_residue(fest_handle* h, const double* F, const double* G, const
 
 int fest_add_source_term_residue(fest_handle* h, const double* qp, double* residue) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
   RET(up(h, h->d.res, residue, z.res));
@@ -587,6 +608,7 @@ int fest_add_source_term_residue(fest_handle* h, const double* qp, double* resid
 
 int fest_compute_time_step(fest_handle* h, const double* qp, double CFL, double* delta_t) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
   launch_time_step(h->p, h->d, CFL, h->L());
@@ -597,6 +619,7 @@ int fest_compute_time_step(fest_handle* h, const double* qp, double CFL, double*
 int fest_get_total_conservative_residue(fest_handle* h, double* qp, int current_iter,
                                         double* residue) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
   RET(residual_fp64(h, current_iter));
@@ -608,6 +631,7 @@ int fest_get_total_conservative_residue(fest_handle* h, double* qp, int current_
 int fest_get_next_solution(fest_handle* h, double* qp, int current_iter, double CFL,
                            double* residue, double* delta_t) {
   if (!h) return FEST_ERR_ARG;
+  RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
   RET(next_solution_fp64(h, current_iter, CFL));
@@ -638,23 +662,47 @@ int fest_find_resnorm(fest_handle* h, double* res_abs) {
   return FEST_OK;
 }
 
-int fest_step(fest_handle* h, int n_iters, int first_iter, double CFL, double* res_abs) {
+static int step_enqueue(fest_handle* h, int n_iters, int first_iter, double CFL) {
   if (!h || n_iters < 0) return FEST_ERR_ARG;
-  if (h->precision == FEST_MIXED || fused_supported(h->p, FEST_FP64)) {
-    if (!h->fused) {
-      int rc = fused_create(h->p, h->d, h->d_table, h->s, &h->fused);
-      if (rc) return rc;
-    }
-    int rc = fused_run(h->fused, h->p, h->d, h->precision, n_iters, first_iter, CFL, h->s, &h->launches);
-    if (rc) return rc;
-  } else {
-    for (int n = 0; n < n_iters; ++n) RET(next_solution_fp64(h, first_iter + n, CFL));
+  if (fused_supported(h->p, h->precision)) {
+    if (!h->fused) RET(fused_create(h->p, h->d, h->d_table, h->s, &h->fused));
+    return fused_run(h->fused, h->p, h->d, h->precision, n_iters, first_iter, CFL, h->s,
+                     &h->launches);
   }
-  if (res_abs) {
-    if (h->fused && h->precision == FEST_MIXED) RET(fused_export_residual(h->fused, h->d, h->s));
-    return fest_find_resnorm(h, res_abs);
-  }
+  if (h->precision == FEST_MIXED) return FEST_ERR_ARG;  // mixed needs the fused sweep
+  RET(sync_fused(h));
+  for (int n = 0; n < n_iters; ++n) RET(next_solution_fp64(h, first_iter + n, CFL));
+  return FEST_OK;
+}
+
+int fest_step(fest_handle* h, int n_iters, int first_iter, double CFL, double* res_abs) {
+  RET(step_enqueue(h, n_iters, first_iter, CFL));
+  if (res_abs) return fest_find_resnorm(h, res_abs);
   return finish(h);
+}
+
+int fest_step_async(fest_handle* h, int n_iters, int first_iter, double CFL) {
+  return step_enqueue(h, n_iters, first_iter, CFL);
+}
+
+int fest_set_stream(fest_handle* h, void* stream) {
+  if (!h) return FEST_ERR_ARG;
+  CK(cudaStreamSynchronize(h->s));
+  h->s = stream ? (cudaStream_t)stream : h->own;
+  return FEST_OK;
+}
+
+int fest_profile(fest_handle* h, int enable) {
+  if (!h) return FEST_ERR_ARG;
+  if (!h->fused && fused_supported(h->p, h->precision))
+    RET(fused_create(h->p, h->d, h->d_table, h->s, &h->fused));
+  fused_profile(h->fused, enable != 0);
+  return FEST_OK;
+}
+
+int fest_profile_read(fest_handle* h, long long* launches, double* total_ms) {
+  if (!h || !h->fused) return FEST_ERR_ARG;
+  return fused_profile_read(h->fused, launches, total_ms);
 }
 
 }  // extern "C"

@@ -24,6 +24,7 @@ struct Params {
   double gm, R, mu_ref, T_ref, S, Pr, tPr, MInf, p_inf, rho_inf, u_inf, v_inf, w_inf;
   int flux, interp, limiter, turb, mu_var, ppm_flag, n_grad, tstep;
   double gdt;  // schemetype%global_time_step
+  int integ;   // schemetype%time_step_accuracy (FEST_TIME_*)
   int lam[3], tlim[3], pb[3];
   int id[6];
   int part_block[6], part_face[6];

@@ -18,6 +18,9 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int precision, 
               int first_iter, double CFL, cudaStream_t s, long long* launches);
 // copy the fused path's FP64 state into qp (the reference layout)
 int fused_export_state(FusedState* f, double* qp, cudaStream_t s);
+// event timing of the stage-sweep launches
+void fused_profile(FusedState* f, bool enable);
+int fused_profile_read(FusedState* f, long long* launches, double* total_ms);
 // materialise the last stage's residual and boundary fluxes for find_resnorm
 int fused_export_residual(FusedState* f, const DevBlock& b, cudaStream_t s);
 

@@ -197,6 +197,10 @@ _SIGS = {
     "fest_get_next_solution": [C.c_void_p, _DP, C.c_int, C.c_double, _DP, _DP],
     "fest_find_resnorm": [C.c_void_p, _DP],
     "fest_step": [C.c_void_p, C.c_int, C.c_int, C.c_double, _DP],
+    "fest_step_async": [C.c_void_p, C.c_int, C.c_int, C.c_double],
+    "fest_set_stream": [C.c_void_p, C.c_void_p],
+    "fest_profile": [C.c_void_p, C.c_int],
+    "fest_profile_read": [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)],
 }
 EXPORTED = tuple(_SIGS) + ("fest_kernel_launches", "fest_array_size", "fest_set_array",
                           "fest_get_array")

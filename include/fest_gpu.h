@@ -230,6 +230,18 @@ int fest_find_resnorm(fest_handle *h, double *res_abs);
 int fest_step(fest_handle *h, int n_iters, int first_iter, double CFL,
               double *res_abs);
 
+/* enqueue fest_step's work on the handle's stream and return at once;
+ * errors surface at the next synchronous call (fest_last_device_error) */
+int fest_step_async(fest_handle *h, int n_iters, int first_iter, double CFL);
+/* run the handle's work on a caller-owned CUDA stream (cudaStream_t passed
+ * as void*); NULL restores the handle's own stream */
+int fest_set_stream(fest_handle *h, void *cuda_stream);
+/* time every fused stage-sweep launch with CUDA events on the handle's
+ * stream (enable != 0 starts and clears the record); read the launch count
+ * and their summed device time */
+int fest_profile(fest_handle *h, int enable);
+int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,114 @@
+"""The fused stage sweep (fest_step) against the oracle's get_next_solution.
+
+FP64: interior state after three iterations within 1e-11 of each variable's
+magnitude (ghost layers of the returned state are those of the last BC
+application, not the reference's blended copies; the next iteration's BCs
+rewrite them, so only interior cells are compared).
+FEST_MIXED: FP32 stencil arithmetic with FP64 accumulation; the interior
+state stays within 2e-5 of each variable's magnitude over three iterations."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from fest3d import abi
+from parity import make_pair, rel_err, small_case
+
+pytestmark = pytest.mark.gpu
+
+COMBOS = {
+    "weno-slau": dict(scheme_kw=dict(interpolant="weno", scheme_name="slau"),
+                      ids=(-11, -4, -6, -6, -10, -10)),
+    "muscl-ausm": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ausm"),
+                       ids=(-5, -4, -6, -3, -10, -10)),
+    "ppm-ausmP": dict(scheme_kw=dict(interpolant="ppm", scheme_name="ausmP", iPB_switch=1),
+                      ids=(-3, -4, -5, -6, -6, -6)),
+    "wenoNM-ausmUP": dict(scheme_kw=dict(interpolant="weno_NM", scheme_name="ausmUP"),
+                          ids=(-8, -2, -6, -6, -10, -10), flow_kw=dict(MInf=0.3)),
+    "none-vanleer": dict(scheme_kw=dict(interpolant="none", scheme_name="van_leer"),
+                         ids=(-1, -4, -6, -6, -10, -10)),
+    "muscl-ldfss-vanalbada": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ldfss0",
+                                                 limiter="van_albada"),
+                                  ids=(-3, -4, -6, -5, -10, -10)),
+}
+
+
+def interior(q, ext):
+    return q[3:ext.imx + 2, 3:ext.jmx + 2, 3:ext.kmx + 2, :]
+
+
+def run_pair(name, acc, precision, iters=3, nc=(37, 14, 5)):
+    kw = dict(COMBOS[name])
+    sk = dict(kw.pop("scheme_kw"))
+    sk["time_step_accuracy"] = acc
+    kw.setdefault("nc", nc)
+    ext, flow, scheme, bc, nodes, qp = small_case(scheme_kw=sk, **kw)
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
+    h.set_precision(precision)
+    norm = h.step(iters, 1, 0.5)
+    for it in range(1, iters + 1):
+        assert O.get_next_solution([blk], it, 0.5) == 0
+    return ext, blk, h, h.download_state(), norm
+
+
+@pytest.mark.parametrize("name", list(COMBOS))
+@pytest.mark.parametrize("acc", ["none", "RK2", "RK4", "TVDRK2", "TVDRK3"])
+def test_fused_fp64(gpu_lib, name, acc):
+    ext, blk, h, q, norm = run_pair(name, acc, abi.FEST_FP64)
+    e = rel_err(interior(q, ext), interior(blk["qp"], ext))
+    assert e <= 1e-11, f"fused FP64 interior state differs by {e:.3e}"
+    ref = O.find_resnorm([blk])
+    assert np.allclose(norm, ref, rtol=1e-9, atol=1e-300), (norm, ref)
+
+
+@pytest.mark.parametrize("name", list(COMBOS))
+@pytest.mark.parametrize("acc", ["none", "TVDRK3", "RK4"])
+def test_fused_mixed(gpu_lib, name, acc):
+    ext, blk, h, q, norm = run_pair(name, acc, abi.FEST_MIXED)
+    e = rel_err(interior(q, ext), interior(blk["qp"], ext))
+    assert e <= 2e-5, f"mixed interior state differs by {e:.3e}"
+    ref = O.find_resnorm([blk])
+    assert np.allclose(norm[1:], ref[1:], rtol=2e-2), (norm, ref)
+
+
+@pytest.mark.parametrize("nc,ids", [((40, 9, 1), (-3, -4, -6, -5, -6, -6)),
+                                    ((37, 14, 5), (-1, -4, -6, -6, -9, -9))])
+def test_in_place_cases_use_module_path(gpu_lib, nc, ids):
+    """thin blocks and -9 faces read other faces' ghosts: FP64 fest_step
+    runs the in-place module path (exact), FEST_MIXED refuses them."""
+    ext, flow, scheme, bc, nodes, qp = small_case(
+        nc=nc, ids=ids, scheme_kw=dict(interpolant="muscl", scheme_name="ausm",
+                                       time_step_accuracy="TVDRK3"))
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
+    h.step(3, 1, 0.5)
+    for it in (1, 2, 3):
+        assert O.get_next_solution([blk], it, 0.5) == 0
+    assert rel_err(h.download_state(), blk["qp"]) <= 1e-11
+    h.set_precision(abi.FEST_MIXED)
+    with pytest.raises(abi.FestError):
+        h.step(1, 4, 0.5)
+
+
+def test_fused_state_roundtrip_and_module_interplay(gpu_lib):
+    """after fused steps the module entry points see the fused state."""
+    ext, blk, h, q, norm = run_pair("weno-slau", "TVDRK3", abi.FEST_FP64, iters=2)
+    q2 = h.get_next_solution(q, 3, 0.5)  # module path continues from the fused state
+    assert O.get_next_solution([blk], 3, 0.5) == 0
+    assert rel_err(interior(q2, ext), interior(blk["qp"], ext)) <= 1e-11
+
+
+def test_profile_counts_stage_launches(gpu_lib):
+    ext, flow, scheme, bc, nodes, qp = small_case(
+        nc=(37, 14, 5), scheme_kw=dict(interpolant="weno", scheme_name="slau",
+                                       time_step_accuracy="TVDRK3"),
+        ids=(-11, -4, -6, -6, -10, -10))
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
+    h.set_precision(abi.FEST_MIXED)
+    L = h.lib
+    abi.check(L.fest_profile(h.h, 1), "profile")
+    h.step(4, 1, 0.5, with_norm=False)
+    n = C.c_longlong()
+    ms = C.c_double()
+    abi.check(L.fest_profile_read(h.h, C.byref(n), C.byref(ms)), "profile_read")
+    assert n.value == 12 and ms.value > 0
