@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 explicit residual-and-update path.
+
+Metric: Mcell-residuals/s (one cell-residual = one residual evaluation of one
+interior cell, its update included), FEST_MIXED (FP32 stencil arithmetic,
+FP64 state/metrics/norm) with the FP64 rate and the mixed-vs-FP64 wall-Cp
+difference reported beside it.
+
+Workload (default): the smooth-bump channel, 256x96x4 cells, WENO5 + SLAU,
+TVD-RK3 with local time steps, CFL 0.8; one step = one TVD-RK3 iteration
+(3 cell-residuals per cell).  Inputs are synthetic (analytic grid, uniform
+Mach 0.5 start).  L2 is flushed (256 MiB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's path (the
+reference itself is Fortran+MPI and cannot be built on these machines) on
+all host cores for a bounded number of the same steps.
+With N > 1 (torchrun), every rank advances its own replica of the block
+(replicas only: one block per GPU needs no exchange); value = all ranks'
+cell-residuals / max rank time.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fest-3d_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "Mcell-residuals/s (mixed precision; FP64 and mixed-vs-FP64 wall-Cp error reported)"
+# algorithmic bytes per cell-residual of the fused sweep (FP64 state in and
+# out, one I/J/K face record and the volume per cell): 184 B in stage 1, 224 B
+# in stages 2-3 (the blend also reads U_store)
+BYTES_STAGE = (184.0, 224.0, 224.0)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="bump", choices=["bump"])
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of the SM clock and throttle reasons."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.gpu)],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    p = os.path.join(ROOT, "profiles", "k_stage_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def wall_cp(q, ext, flow):
+    """Cp on the first cell row above the lower wall (j=1), all i, k=1."""
+    p = q[3:ext.imx + 2, 3, 3, 4]
+    qinf = 0.5 * flow.density_inf * flow.vel_mag ** 2
+    return (p - flow.pressure_inf) / qinf
+
+
+def cpu_rate(case, seconds=10.0, threads=None):
+    """The oracle (plain C, OpenMP over all host cores) on the same block;
+    returns (Mcell-residuals/s, iterations timed, threads)."""
+    import oracle as O
+    threads = threads or (os.cpu_count() or 1)
+    O.set_threads(threads)
+    ext = case["ext"]
+    blk = O.Block(ext, case["flow"], case["scheme"], case["bc"])
+    blk["nodes"] = case["nodes"]
+    blk.setup_geometry()
+    blk["qp"] = case["qp"]
+    O.get_next_solution([blk], 1, case["CFL"])  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        O.get_next_solution([blk], 2 + n, case["CFL"])
+        n += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
+    return N * 3 * n / dt / 1e6, n, threads
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from fest3d import cases
+    case = cases.bump_case()
+    import oracle as O
+    O.build()
+    ext = case["ext"]
+    N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    blk = O.Block(ext, case["flow"], case["scheme"], case["bc"])
+    blk["nodes"] = case["nodes"]
+    blk.setup_geometry()
+    blk["qp"] = case["qp"]
+    it = 1
+    for _ in range(min(args.warmup, 2)):
+        O.get_next_solution([blk], it, case["CFL"])
+        it += 1
+    t0 = time.perf_counter()
+    steps = 0
+    budget = 90.0
+    while steps < args.steps:
+        O.get_next_solution([blk], it, case["CFL"])
+        it += 1
+        steps += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    dt = time.perf_counter() - t0
+    v = N * 3 * steps / dt / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mcell-residuals/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": min(args.warmup, 2),
+            "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": case["name"], "cells": N, "cell_residuals_per_step": 3 * N,
+                       "parallelism": "cpu"},
+            "cpu_baseline": {"value": v, "unit": "Mcell-residuals/s", "cores": threads, "kind": "port",
+                             "sample": f"{steps} TVD-RK3 iterations of the full block (bounded to "
+                                       f"{budget:.0f} s), C restatement of the reference path, "
+                                       f"OpenMP {threads} threads"},
+            "e2e": {"value": v, "unit": "Mcell-residuals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl")
+    from fest3d import abi, build, cases
+    from fest3d.handle import Handle
+    if not os.path.exists(abi.LIB_PATH):
+        build.build()
+    lib = abi.load()
+    case = cases.bump_case()
+    ext, flow, CFL = case["ext"], case["flow"], case["CFL"]
+    N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
+    STAGES = 3
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def make(precision):
+        h = Handle(ext, flow, case["scheme"], case["bc"], lib=lib)
+        h.setup_geometry(case["nodes"])
+        h.upload_state(case["qp"])
+        h.set_precision(precision)
+        abi.check(lib.fest_set_stream(h.h, C.c_void_p(stream.cuda_stream)), "set_stream")
+        return h
+
+    def timed(h, steps, it0):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        it = it0
+        barrier()
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            abi.check(lib.fest_step_async(h.h, 1, it, CFL), "fest_step_async")
+            e1.record(stream)
+            it += 1
+        barrier()
+        abi.check(lib.fest_last_device_error(h.h), "device error")
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, it
+
+    results = {}
+    for prec in (abi.FEST_FP64, abi.FEST_MIXED):
+        h = make(prec)
+        it = 1
+        for _ in range(args.warmup):
+            abi.check(lib.fest_step_async(h.h, 1, it, CFL), "warmup")
+            it += 1
+        barrier()
+        abi.check(lib.fest_last_device_error(h.h), "warmup error")
+        steps = args.steps if prec == abi.FEST_MIXED else max(10, args.steps // 4)
+        n0 = h.launches
+        with Clocks(local) as ck:
+            ms, it = timed(h, steps, it)
+        launches = h.launches - n0
+        results[prec] = dict(h=h, ms=ms, steps=steps, it=it, launches=launches, clocks=ck.summary())
+    mixed, fp64 = results[abi.FEST_MIXED], results[abi.FEST_FP64]
+    rate = lambda r: ws * N * STAGES * r["steps"] / (r["ms"] / 1e3) / 1e6
+
+    # roofline of the dominant kernel: event-timed stage-sweep launches
+    h = mixed["h"]
+    abi.check(lib.fest_profile(h.h, 1), "profile")
+    prof_steps = min(200, args.steps)
+    it = mixed["it"]
+    for _ in range(prof_steps):
+        flush.zero_()
+        abi.check(lib.fest_step_async(h.h, 1, it, CFL), "profiled step")
+        it += 1
+    torch.cuda.synchronize()
+    nl, tot = C.c_longlong(), C.c_double()
+    abi.check(lib.fest_profile_read(h.h, C.byref(nl), C.byref(tot)), "profile_read")
+    abi.check(lib.fest_profile(h.h, 0), "profile off")
+    avg_s = tot.value / 1e3 / max(nl.value, 1)
+    bytes_launch = N * sum(BYTES_STAGE) / len(BYTES_STAGE)
+    achieved = bytes_launch / avg_s / 1e9
+    peak, peak_kind = measured_peak()
+    tr = committed_traffic()
+    traffic = tr.get("bytes_per_launch") if tr else None
+
+    # mixed vs FP64 wall Cp after the same number of iterations
+    qm = mixed["h"].download_state()
+    q64 = fp64["h"].download_state()
+    # bring both to the same iteration count
+    lag = (mixed["it"] + prof_steps) - fp64["it"]
+    if lag > 0:
+        fp64["h"].step(lag, fp64["it"], CFL, with_norm=False)
+        q64 = fp64["h"].download_state()
+    cp_err = float(np.abs(wall_cp(qm, ext, flow) - wall_cp(q64, ext, flow)).max())
+
+    # e2e through the host-buffer C ABI: upload, one iteration, download
+    he = make(abi.FEST_MIXED)
+    host = torch.empty(abi.shapes(ext)["qp"][::-1], dtype=torch.float64, pin_memory=True)
+    qhost = host.numpy().T  # Fortran-ordered view of pinned memory
+    qhost[...] = case["qp"]
+    ptr = abi.ptr(qhost)
+    e2e_steps = max(10, args.steps // 4)
+    it = 1
+    tot_e2e = 0.0
+    barrier()
+    for _ in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        abi.check(lib.fest_upload_state(he.h, ptr), "upload")
+        abi.check(lib.fest_step(he.h, 1, it, CFL, None), "fest_step")
+        abi.check(lib.fest_download_state(he.h, ptr), "download")
+        tot_e2e += time.perf_counter() - t0
+        it += 1
+    if dist:
+        t = torch.tensor([tot_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_e2e = float(t.item())
+    e2e_rate = ws * N * STAGES * e2e_steps / tot_e2e / 1e6
+    nbytes = int(qhost.nbytes)
+
+    cpu = None
+    if rank == 0 and ws == 1:
+        v, n_it, threads = cpu_rate(case, seconds=10.0)
+        cpu = {"value": v, "unit": "Mcell-residuals/s", "cores": threads, "kind": "port",
+               "sample": f"{n_it} TVD-RK3 iterations of the full 256x96x4 block (~10 s), "
+                         f"C restatement of the reference path, OpenMP {threads} threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": rate(mixed), "unit": "Mcell-residuals/s", "n_gpus": ws,
+            "steps": mixed["steps"], "warmup": args.warmup,
+            "ms_per_step": mixed["ms"] / mixed["steps"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 stencil / f64 state",
+            "data": "synthetic (analytic bump grid, uniform Mach 0.5 start)",
+            "config": {"workload": case["name"], "cells": N, "cell_residuals_per_step": STAGES * N,
+                       "l2": "flushed (256 MiB write) before every timed step",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "fp64": {"value": rate(fp64), "unit": "Mcell-residuals/s", "steps": fp64["steps"],
+                     "ms_per_step": fp64["ms"] / fp64["steps"]},
+            "mixed_over_fp64": rate(mixed) / rate(fp64),
+            "wall_cp_abs_err_mixed_vs_fp64": cp_err,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_stage<float> (fused WENO5+SLAU sweep + update)",
+                         "peak_source": peak_kind, "launches_timed": int(nl.value),
+                         "avg_launch_us": avg_s * 1e6, "bytes_per_launch": bytes_launch},
+            "clocks": mixed["clocks"],
+            "e2e": {"value": e2e_rate, "unit": "Mcell-residuals/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes,
+                    "path": "fest_upload_state + fest_step + fest_download_state, pinned host buffer"},
+            "gpu_launches": int(mixed["launches"]),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

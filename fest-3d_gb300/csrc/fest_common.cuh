@@ -100,6 +100,18 @@ template <typename T> __device__ __forceinline__ T subsonic(T m) {
   return v > T(0) ? v : T(0);
 }
 
+// ---- arithmetic policy ---------------------------------------------------------
+// FP64 keeps IEEE division and square root (the reference's arithmetic).
+// The FP32 path of FEST_MIXED uses the hardware approximations: a reciprocal
+// based divide (2 ulp), x*rsqrt(x) for the square root (negative -> NaN, as
+// IEEE), and a multiplication by the folded reciprocal for constant divisors.
+__device__ __forceinline__ double dv(double a, double b) { return a / b; }
+__device__ __forceinline__ float dv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double dvc(double a, double c) { return a / c; }
+__device__ __forceinline__ float dvc(float a, float c) { return a * (1.0f / c); }
+__device__ __forceinline__ double sq(double x) { return sqrt(x); }
+__device__ __forceinline__ float sq(float x) { return x == 0.0f ? 0.0f : x * rsqrtf(x); }
+
 // ---- per-cell reconstruction along a line -----------------------------------
 // A Line gives the cell values of one variable along direction dir through a
 // fixed (tangential) position: q(c) is the cell at normal coordinate c.
@@ -110,7 +122,7 @@ template <typename T, typename S> struct Line {
 };
 
 template <typename T> __device__ __forceinline__ T limiter_fn(T r, int lim) {
-  if (lim == FEST_LIMITER_VAN_ALBADA) return ((r * r) + r) / ((r * r) + T(1));
+  if (lim == FEST_LIMITER_VAN_ALBADA) return dv(((r * r) + r), ((r * r) + T(1)));
   const T alpha = T(2) / T(3);  // Koren alpha family, muscl.f90:258,283
   return fmax2(T(0), fmin2(fmin2(T(2) * r, alpha * (r - T(1)) + T(1)), T(2)));
 }
@@ -123,9 +135,9 @@ __device__ __forceinline__ void muscl_cell(const Lq& q, int c, T sw, int lim, T&
   T qc = q(c);
   T fd = q(c + 1) - qc;
   T bd = qc - q(c - 1);
-  T r = fd / (bd + copysign(eps, bd));
+  T r = dv(fd, bd + copysign(eps, bd));
   T psi1 = limiter_fn(r, lim);
-  r = bd / (fd + copysign(eps, fd));
+  r = dv(bd, fd + copysign(eps, fd));
   T psi2 = limiter_fn(r, lim);
   psi1 = (T(1) - (T(1) - psi1) * sw);
   psi2 = (T(1) - (T(1) - psi2) * sw);
@@ -141,11 +153,11 @@ __device__ __forceinline__ void muscl_noeps_cell(const Lq& q, int c, T sw, T& Rm
   T qc = q(c);
   T fd = q(c + 1) - qc;
   T bd = qc - q(c - 1);
-  T r = fd / bd;
-  T psi1 = fmax2(T(0), fmin2(fmin2(T(2) * r, (T(2) + r) / T(3)), T(2)));
+  T r = dv(fd, bd);
+  T psi1 = fmax2(T(0), fmin2(fmin2(T(2) * r, dvc((T(2) + r), T(3))), T(2)));
   psi1 = (T(1) - (T(1) - psi1) * sw);
-  r = bd / fd;
-  T psi2 = fmax2(T(0), fmin2(fmin2(T(2) * r, (T(2) + r) / T(3)), T(2)));
+  r = dv(bd, fd);
+  T psi2 = fmax2(T(0), fmin2(fmin2(T(2) * r, dvc((T(2) + r), T(3))), T(2)));
   psi2 = (T(1) - (T(1) - psi2) * sw);
   // 0/0 (flat data) leaves psi undefined in the reference; any finite psi
   // multiplies a zero difference there
@@ -169,16 +181,16 @@ __device__ __forceinline__ void weno_cell(const Lq& q, int c, T& Rm, T& Lp) {
   t1 = u0 - T(2) * up1 + up2; t2 = T(3) * u0 - T(4) * up1 + up2;
   B2 = (T(13) / T(12)) * (t1 * t1) + (T(1) / T(4)) * (t2 * t2);
   T e0 = eps + B0, e1 = eps + B1, e2 = eps + B2;
-  T w0 = g0 / (e0 * e0), w1 = g1 / (e1 * e1), w2 = g2 / (e2 * e2);
-  T P0 = (T(2) * um2 - T(7) * um1 + T(11) * u0) / T(6);
-  T P1 = (-T(1) * um1 + T(5) * u0 + T(2) * up1) / T(6);
-  T P2 = (T(2) * u0 + T(5) * up1 - T(1) * up2) / T(6);
-  Lp = (w0 * P0 + w1 * P1 + w2 * P2) / (w0 + w1 + w2);
-  P0 = (T(2) * up2 - T(7) * up1 + T(11) * u0) / T(6);
-  P1 = (-T(1) * up1 + T(5) * u0 + T(2) * um1) / T(6);
-  P2 = (T(2) * u0 + T(5) * um1 - T(1) * um2) / T(6);
-  w0 = g0 / (e2 * e2); w1 = g1 / (e1 * e1); w2 = g2 / (e0 * e0);
-  Rm = (w0 * P0 + w1 * P1 + w2 * P2) / (w0 + w1 + w2);
+  T w0 = dv(g0, (e0 * e0)), w1 = dv(g1, (e1 * e1)), w2 = dv(g2, (e2 * e2));
+  T P0 = dvc((T(2) * um2 - T(7) * um1 + T(11) * u0), T(6));
+  T P1 = dvc((-T(1) * um1 + T(5) * u0 + T(2) * up1), T(6));
+  T P2 = dvc((T(2) * u0 + T(5) * up1 - T(1) * up2), T(6));
+  Lp = dv((w0 * P0 + w1 * P1 + w2 * P2), (w0 + w1 + w2));
+  P0 = dvc((T(2) * up2 - T(7) * up1 + T(11) * u0), T(6));
+  P1 = dvc((-T(1) * up1 + T(5) * u0 + T(2) * um1), T(6));
+  P2 = dvc((T(2) * u0 + T(5) * um1 - T(1) * um2), T(6));
+  w0 = dv(g0, (e2 * e2)); w1 = dv(g1, (e1 * e1)); w2 = dv(g2, (e0 * e0));
+  Rm = dv((w0 * P0 + w1 * P1 + w2 * P2), (w0 + w1 + w2));
 }
 
 // WENO on non-uniform cells (weno_NM.f90:191-235); v(c) are cell volumes
@@ -188,7 +200,8 @@ __device__ __forceinline__ void weno_nm_cell(const Lq& q, const Lv& v, int c, T&
   const T g0 = T(1) / T(10), g1 = T(6) / T(10), g2 = T(3) / T(10);
   T um2 = q(c - 2), um1 = q(c - 1), u0 = q(c), up1 = q(c + 1), up2 = q(c + 2);
   T vm2 = v(c - 2), vm1 = v(c - 1), v0 = v(c), vp1 = v(c + 1), vp2 = v(c + 2);
-  T a12 = vp2 / (vp1 + vp2), a01 = vp1 / (v0 + vp1), a10 = v0 / (vm1 + v0), a21 = vm1 / (vm2 + vm1);
+  T a12 = dv(vp2, (vp1 + vp2)), a01 = dv(vp1, (v0 + vp1)), a10 = dv(v0, (vm1 + v0)),
+    a21 = dv(vm1, (vm2 + vm1));
   T U01 = (T(1) - a01) * u0 + a01 * up1;
   T U12 = (T(1) - a12) * up1 + a12 * up2;
   T U10 = (T(1) - a10) * um1 + a10 * u0;
@@ -196,9 +209,9 @@ __device__ __forceinline__ void weno_nm_cell(const Lq& q, const Lv& v, int c, T&
   T U00 = um1 + (T(1) - a21) * (um1 - um2);
   T U11 = up1 + a12 * (up1 - up2);
   T t1, t2, B0, B1, B2, P0, P1, P2, e;
-  P0 = (T(6) * u0 - T(1) * U10 - T(2) * U00) / T(3);
-  P1 = (-T(1) * U10 + T(2) * u0 + T(2) * U01) / T(3);
-  P2 = (T(2) * U01 + T(2) * up1 - T(1) * U12) / T(3);
+  P0 = dvc((T(6) * u0 - T(1) * U10 - T(2) * U00), T(3));
+  P1 = dvc((-T(1) * U10 + T(2) * u0 + T(2) * U01), T(3));
+  P2 = dvc((T(2) * U01 + T(2) * up1 - T(1) * U12), T(3));
   t1 = T(2) * U10 - T(2) * U00; t2 = T(4) * u0 - T(2) * U10 - T(2) * U00;
   B0 = (T(13) / T(12)) * (t1 * t1) + (T(1) / T(4)) * (t2 * t2);
   t1 = T(2) * U10 - T(4) * u0 + T(2) * U01; t2 = -T(2) * U10 + T(2) * U01;
@@ -206,28 +219,28 @@ __device__ __forceinline__ void weno_nm_cell(const Lq& q, const Lv& v, int c, T&
   t1 = T(2) * U01 - T(4) * up1 + T(2) * U12; t2 = -T(6) * U01 + T(8) * up1 - T(2) * U12;
   B2 = (T(13) / T(12)) * (t1 * t1) + (T(1) / T(4)) * (t2 * t2);
   T w0, w1, w2;
-  e = eps + B0; w0 = g0 / (e * e);
-  e = eps + B1; w1 = g1 / (e * e);
-  e = eps + B2; w2 = g2 / (e * e);
-  Lp = (w0 * P0 + w1 * P1 + w2 * P2) / (w0 + w1 + w2);
-  P0 = (T(6) * u0 - T(1) * U01 - T(2) * U11) / T(3);
-  P1 = (-T(1) * U01 + T(2) * u0 + T(2) * U10) / T(3);
-  P2 = (T(2) * U10 + T(2) * um1 - T(1) * U21) / T(3);
+  e = eps + B0; w0 = dv(g0, (e * e));
+  e = eps + B1; w1 = dv(g1, (e * e));
+  e = eps + B2; w2 = dv(g2, (e * e));
+  Lp = dv((w0 * P0 + w1 * P1 + w2 * P2), (w0 + w1 + w2));
+  P0 = dvc((T(6) * u0 - T(1) * U01 - T(2) * U11), T(3));
+  P1 = dvc((-T(1) * U01 + T(2) * u0 + T(2) * U10), T(3));
+  P2 = dvc((T(2) * U10 + T(2) * um1 - T(1) * U21), T(3));
   t1 = T(2) * U01 - T(2) * U11; t2 = T(4) * u0 - T(2) * U01 - T(2) * U11;
   B0 = (T(13) / T(12)) * (t1 * t1) + (T(1) / T(4)) * (t2 * t2);
   t1 = T(2) * U01 - T(4) * u0 + T(2) * U10; t2 = -T(2) * U01 + T(2) * U10;
   B1 = (T(13) / T(12)) * (t1 * t1) + (T(1) / T(4)) * (t2 * t2);
   t1 = T(2) * U10 - T(4) * um1 + T(2) * U21; t2 = -T(6) * U10 + T(8) * um1 - T(2) * U21;
   B2 = (T(13) / T(12)) * (t1 * t1) + (T(1) / T(4)) * (t2 * t2);
-  e = eps + B0; w0 = g0 / (e * e);
-  e = eps + B1; w1 = g1 / (e * e);
-  e = eps + B2; w2 = g2 / (e * e);
-  Rm = (w0 * P0 + w1 * P1 + w2 * P2) / (w0 + w1 + w2);
+  e = eps + B0; w0 = dv(g0, (e * e));
+  e = eps + B1; w1 = dv(g1, (e * e));
+  e = eps + B2; w2 = dv(g2, (e * e));
+  Rm = dv((w0 * P0 + w1 * P1 + w2 * P2), (w0 + w1 + w2));
 }
 
 // PPM face estimate (ppm.f90:317-319) and extremum removal (ppm.f90:356-371)
 template <typename T, class Lq> __device__ __forceinline__ T ppm_estimate(const Lq& q, int f) {
-  return (T(7) * (q(f) + q(f - 1)) - (q(f + 1) + q(f - 2))) / T(12);
+  return dvc((T(7) * (q(f) + q(f - 1)) - (q(f + 1) + q(f - 2))), T(12));
 }
 template <typename T, class Lq>
 __device__ __forceinline__ void ppm_cell(const Lq& q, int c, bool lim, T& Rm, T& Lp) {
@@ -252,25 +265,28 @@ template <typename T, class Lp_>
 __device__ __forceinline__ T pdif_cell(const Lp_& p, int c, int n, T p_inf) {
   int cc = c < 1 ? 1 : (c > n - 1 ? n - 1 : c);
   T pd2 = fabs(p(cc + 1) - p(cc - 1));
-  return T(1) - (pd2 / (pd2 + p_inf));
+  return T(1) - dv(pd2, (pd2 + p_inf));
 }
 
 // One cell's two face-side states for variable l along direction dir: the
 // interior reconstruction of compute_face_interpolant with the optional
 // pressure switch (face_interpolant.f90:79-105).
-template <typename T, class Lq, class Lpres, class Lvol>
+// INTERP >= 0 fixes the method at compile time (the fused sweeps); -1 reads
+// it from the parameter block (the module kernels).
+template <typename T, int INTERP = -1, class Lq, class Lpres, class Lvol>
 __device__ __forceinline__ void recon_interior(const Params& p, int dir, int c, int l, const Lq& q,
                                                const Lpres& pres, const Lvol& vol, T& Rm, T& Lp) {
   int n = extent_of(p.d, dir);
   T sw = T((l >= 6) ? p.tlim[dir] : p.lam[dir]);
-  switch (p.interp) {
+  const int interp = INTERP >= 0 ? INTERP : p.interp;
+  switch (interp) {
     case FEST_INTERP_NONE: Rm = q(c); Lp = q(c); break;
     case FEST_INTERP_MUSCL: muscl_cell<T>(q, c, sw, p.limiter, Rm, Lp); break;
     case FEST_INTERP_PPM: ppm_cell<T>(q, c, p.lam[dir] == 1, Rm, Lp); break;
     case FEST_INTERP_WENO: weno_cell<T>(q, c, Rm, Lp); break;
     default: weno_nm_cell<T>(q, vol, c, Rm, Lp); break;
   }
-  if ((p.interp == FEST_INTERP_MUSCL || p.interp == FEST_INTERP_PPM) && p.pb[dir] == 1) {
+  if ((interp == FEST_INTERP_MUSCL || interp == FEST_INTERP_PPM) && p.pb[dir] == 1) {
     T qc = q(c);
     T pd = pdif_cell<T>(pres, c, n, T(p.p_inf));
     if (c <= n - 1) Lp = qc + (pd * (Lp - qc));
@@ -281,10 +297,10 @@ __device__ __forceinline__ void recon_interior(const Params& p, int dir, int c, 
 // reconstruct_boundary_state (boundary_state_reconstruction.f90:28-412) for
 // cell c: overrides applied in the reference's order, imin-type writes
 // first and imax-type writes last, so thin blocks resolve the same way.
-template <typename T, class Lq>
+template <typename T, int INTERP = -1, class Lq>
 __device__ __forceinline__ void boundary_override(const Params& p, int dir, int c, int l,
                                                   const Lq& q, T& Rm, T& Lp) {
-  if (p.interp == FEST_INTERP_NONE) return;
+  if ((INTERP >= 0 ? INTERP : p.interp) == FEST_INTERP_NONE) return;
   int n = extent_of(p.d, dir);
   T sw = T((l >= 6) ? p.tlim[dir] : p.lam[dir]);
   int idmin = p.id[2 * dir], idmax = p.id[2 * dir + 1];
@@ -307,11 +323,11 @@ __device__ __forceinline__ bool near_boundary(const Params& p, int dir, int c) {
   return c <= 1 || c >= n - 1;
 }
 
-template <typename T, class Lq, class Lpres, class Lvol>
+template <typename T, int INTERP = -1, class Lq, class Lpres, class Lvol>
 __device__ __forceinline__ void recon_cell(const Params& p, int dir, int c, int l, const Lq& q,
                                            const Lpres& pres, const Lvol& vol, T& Rm, T& Lp) {
-  recon_interior<T>(p, dir, c, l, q, pres, vol, Rm, Lp);
-  if (near_boundary(p, dir, c)) boundary_override<T>(p, dir, c, l, q, Rm, Lp);
+  recon_interior<T, INTERP>(p, dir, c, l, q, pres, vol, Rm, Lp);
+  if (near_boundary(p, dir, c)) boundary_override<T, INTERP>(p, dir, c, l, q, Rm, Lp);
 }
 
 // ---- convective fluxes: one face, all variables -----------------------------
@@ -319,8 +335,9 @@ __device__ __forceinline__ void recon_cell(const Params& p, int dir, int c, int 
 template <typename T>
 __device__ __forceinline__ void flux_ausm_family(int kind, int nv, T gm, const T* qL, const T* qR,
                                                  T A, T nx, T ny, T nz, T mask, T* Fo) {
-  T c = T(0.5) * (sqrt(gm * qL[4] / qL[0]) + sqrt(gm * qR[4] / qR[0]));
-  T ML = (qL[1] * nx + qL[2] * ny + qL[3] * nz) / c;
+  T c = T(0.5) * (sq(dv(gm * qL[4], qL[0])) + sq(dv(gm * qR[4], qR[0])));
+  T ic = dv(T(1), c);
+  T ML = (qL[1] * nx + qL[2] * ny + qL[3] * nz) * ic;
   T ap = T(0.5) * (T(1) + fsign1(ML));
   T bL = -subsonic(ML);
   T t = T(1) + ML;
@@ -328,7 +345,7 @@ __device__ __forceinline__ void flux_ausm_family(int kind, int nv, T gm, const T
   T Dp = T(0.25) * (t * t) * (T(2) - ML);
   T cp = (ap * (T(1) + bL) * ML) - bL * Mp;
   T sDp = (ap * (T(1) + bL)) - (bL * Dp);
-  T MR = (qR[1] * nx + qR[2] * ny + qR[3] * nz) / c;
+  T MR = (qR[1] * nx + qR[2] * ny + qR[3] * nz) * ic;
   T am = T(0.5) * (T(1) - fsign1(MR));
   T bR = -subsonic(MR);
   t = T(1) - MR;
@@ -341,18 +358,18 @@ __device__ __forceinline__ void flux_ausm_family(int kind, int nv, T gm, const T
     cp = fmax2(T(0), tc);
     cm = fmin2(T(0), tc);
   } else if (kind == FEST_FLUX_LDFSS0) {
-    T s = sqrt((ML * ML + MR * MR) * T(0.5)) - T(1);
+    T s = sq((ML * ML + MR * MR) * T(0.5)) - T(1);
     T Ml = T(0.25) * bL * bR * (s * s);
-    T Mpl = Ml * (T(1) - (qL[4] - qR[4]) / (T(2) * qL[0] * (c * c)));
-    T Mml = Ml * (T(1) - (qL[4] - qR[4]) / (T(2) * qR[0] * (c * c)));
+    T Mpl = Ml * (T(1) - dv((qL[4] - qR[4]), (T(2) * qL[0] * (c * c))));
+    T Mml = Ml * (T(1) - dv((qL[4] - qR[4]), (T(2) * qR[0] * (c * c))));
     cp = cp - Mpl;
     cm = cm + Mml;
   }
-  T g1 = gm / (gm - T(1));
+  T g1 = dv(gm, (gm - T(1)));
   T Fp0 = qL[0] * c * cp * mask;
   T Fm0 = qR[0] * c * cm * mask;
-  T hL = (T(0.5) * (qL[1] * qL[1] + qL[2] * qL[2] + qL[3] * qL[3])) + (g1 * qL[4] / qL[0]);
-  T hR = (T(0.5) * (qR[1] * qR[1] + qR[2] * qR[2] + qR[3] * qR[3])) + (g1 * qR[4] / qR[0]);
+  T hL = (T(0.5) * (qL[1] * qL[1] + qL[2] * qL[2] + qL[3] * qL[3])) + dv(g1 * qL[4], qL[0]);
+  T hR = (T(0.5) * (qR[1] * qR[1] + qR[2] * qR[2] + qR[3] * qR[3])) + dv(g1 * qR[4], qR[0]);
   Fo[0] = Fp0 * A + Fm0 * A;
   Fo[1] = ((Fp0 * qL[1]) + (sDp * qL[4] * nx)) * A + ((Fm0 * qR[1]) + (sDm * qR[4] * nx)) * A;
   Fo[2] = ((Fp0 * qL[2]) + (sDp * qL[4] * ny)) * A + ((Fm0 * qR[2]) + (sDm * qR[4] * ny)) * A;
@@ -370,49 +387,51 @@ __device__ __forceinline__ void flux_mass_family(int kind, int nv, T gm, T MInf,
                                                  T* Fo) {
   T rL = qL[0], uL = qL[1], vL = qL[2], wL = qL[3], pL = qL[4];
   T rR = qR[0], uR = qR[1], vR = qR[2], wR = qR[3], pR = qR[4];
-  T g1 = gm / (gm - T(1));
-  T HL = (T(0.5) * (uL * uL + vL * vL + wL * wL)) + (g1 * pL / rL);
-  T HR = (T(0.5) * (uR * uR + vR * vR + wR * wR)) + (g1 * pR / rR);
+  T g1 = dv(gm, (gm - T(1)));
+  T HL = (T(0.5) * (uL * uL + vL * vL + wL * wL)) + dv(g1 * pL, rL);
+  T HR = (T(0.5) * (uR * uR + vR * vR + wR * wR)) + dv(g1 * pR, rR);
   T VnL = uL * nx + vL * ny + wL * nz;
   T VnR = uR * nx + vR * ny + wR * nz;
   T mass, pbar;
   if (kind == FEST_FLUX_SLAU) {
-    T C = T(0.5) * (sqrt(gm * pL / rL) + sqrt(gm * pR / rR));
-    T ML = VnL / C, MR = VnR / C;
+    T C = T(0.5) * (sq(dv(gm * pL, rL)) + sq(dv(gm * pR, rR)));
+    T iC = dv(T(1), C);
+    T ML = VnL * iC, MR = VnR * iC;
     T aL = fmax2(T(0), T(1) - floor(fabs(ML)));
     T aR = fmax2(T(0), T(1) - floor(fabs(MR)));
     T betaL = (T(1) - aL) * T(0.5) * (T(1) + fsign1(ML)) +
               (aL) * T(0.25) * (T(2) - ML) * ((ML + T(1)) * (ML + T(1)));
     T betaR = (T(1) - aR) * T(0.5) * (T(1) - fsign1(MR)) +
               (aR) * T(0.25) * (T(2) + MR) * ((MR - T(1)) * (MR - T(1)));
-    T vt = sqrt(T(0.5) * ((uL * uL) + (vL * vL) + (wL * wL) + (uR * uR) + (vR * vR) + (wR * wR)));
-    T Mcap = fmin2(T(1), vt / C);
+    T vt = sq(T(0.5) * ((uL * uL) + (vL * vL) + (wL * wL) + (uR * uR) + (vR * vR) + (wR * wR)));
+    T Mcap = fmin2(T(1), vt * iC);
     T Xi = (T(1) - Mcap) * (T(1) - Mcap);
-    T Vnabs = (rL * fabs(VnL) + rR * fabs(VnR)) / (rL + rR);
+    T Vnabs = dv((rL * fabs(VnL) + rR * fabs(VnR)), (rL + rR));
     T fnG = -fmax2(fmin2(ML, T(0)), T(-1)) * fmin2(fmax2(MR, T(0)), T(1));
     pbar = T(0.5) * ((pL + pR) + (betaL - betaR) * (pL - pR) +
                      (T(1) - Xi) * (betaL + betaR - T(1)) * (pL + pR));
     T VnabsL = (T(1) - fnG) * Vnabs + fnG * fabs(VnL);
     T VnabsR = (T(1) - fnG) * Vnabs + fnG * fabs(VnR);
-    mass = T(0.5) * ((rL * (VnL + VnabsL) + rR * (VnR - VnabsR)) - (Xi * (pR - pL) / C));
+    mass = T(0.5) * ((rL * (VnL + VnabsL) + rR * (VnR - VnabsR)) - (Xi * (pR - pL) * iC));
   } else {
-    T cs = sqrt(T(2) * (gm - T(1)) * (T(0.5) * (HL + HR)) / (gm + T(1)));
+    T cs = sq(dv(T(2) * (gm - T(1)) * (T(0.5) * (HL + HR)), (gm + T(1))));
     T cL, cR;
     if (kind == FEST_FLUX_AUSMP) {
-      cL = cs * cs / (fmax2(cs, fabs(VnL)));
-      cR = cs * cs / (fmax2(cs, fabs(VnR)));
+      cL = dv(cs * cs, (fmax2(cs, fabs(VnL))));
+      cR = dv(cs * cs, (fmax2(cs, fabs(VnR))));
     } else {
-      cL = cs * cs / (fmax2(cs, VnL));
-      cR = cs * cs / (fmax2(cs, -VnR));
+      cL = dv(cs * cs, (fmax2(cs, VnL)));
+      cR = dv(cs * cs, (fmax2(cs, -VnR)));
     }
     T C = fmin2(cL, cR);
-    T ML = VnL / C, MR = VnR / C;
+    T iC = dv(T(1), C);
+    T ML = VnL * iC, MR = VnR * iC;
     T Mb = T(0), fna = T(0), alfa = T(0.1875);
     if (kind == FEST_FLUX_AUSMUP) {
-      Mb = sqrt(T(0.5) * ((VnL * VnL) + (VnR * VnR)) / (C * C));
-      T Mo = sqrt(fmin2(T(1), fmax2(Mb * Mb, MInf * MInf)));
+      Mb = sq(dv(T(0.5) * ((VnL * VnL) + (VnR * VnR)), (C * C)));
+      T Mo = sq(fmin2(T(1), fmax2(Mb * Mb, MInf * MInf)));
       fna = Mo * (T(2) - Mo);
-      alfa = T(3) * (T(-4) + (T(5) * fna * fna)) / T(16);
+      alfa = dvc(T(3) * (T(-4) + (T(5) * fna * fna)), T(16));
     }
     T aL = subsonic(ML), aR = subsonic(MR);
     T t = T(1) + ML;
@@ -432,8 +451,8 @@ __device__ __forceinline__ void flux_mass_family(int kind, int nv, T gm, T MInf,
     if (kind == FEST_FLUX_AUSMUP) {
       const T Kp = T(0.25), Ku = T(0.75), sigma = T(1);
       T Pu = -Ku * betaL * betaR * (rL + rR) * fna * C * (VnR - VnL);
-      T Mp = -T(2) * Kp * fmax2(T(1) - (sigma * Mb * Mb), T(0)) * (pR - pL) /
-             (fna * (rL + rR) * C * C);
+      T Mp = dv(-T(2) * Kp * fmax2(T(1) - (sigma * Mb * Mb), T(0)) * (pR - pL),
+                (fna * (rL + rR) * C * C));
       Mface = FmL + FmR + Mp;
       pbar = betaL * pL + betaR * pR + Pu;
     }
@@ -452,13 +471,15 @@ __device__ __forceinline__ void flux_mass_family(int kind, int nv, T gm, T MInf,
     if (l < nv) Fo[l] = (Fp0 * qL[l] + Fm0 * qR[l]) * A;
 }
 
-template <typename T>
+// FLUX >= 0 fixes the scheme at compile time (the fused sweeps)
+template <typename T, int FLUX = -1>
 __device__ __forceinline__ void face_flux(const Params& p, const T* qL, const T* qR, T A, T nx,
                                           T ny, T nz, T mask, T* Fo) {
-  if (p.flux == FEST_FLUX_AUSM || p.flux == FEST_FLUX_VAN_LEER || p.flux == FEST_FLUX_LDFSS0)
-    flux_ausm_family<T>(p.flux, p.d.nv, T(p.gm), qL, qR, A, nx, ny, nz, mask, Fo);
+  const int kind = FLUX >= 0 ? FLUX : p.flux;
+  if (kind == FEST_FLUX_AUSM || kind == FEST_FLUX_VAN_LEER || kind == FEST_FLUX_LDFSS0)
+    flux_ausm_family<T>(kind, p.d.nv, T(p.gm), qL, qR, A, nx, ny, nz, mask, Fo);
   else
-    flux_mass_family<T>(p.flux, p.d.nv, T(p.gm), T(p.MInf), qL, qR, A, nx, ny, nz, mask, Fo);
+    flux_mass_family<T>(kind, p.d.nv, T(p.gm), T(p.MInf), qL, qR, A, nx, ny, nz, mask, Fo);
 }
 
 // wall mass-flux mask of a face (bc.f90:57-66): 0 at the first/last face of a

@@ -1,0 +1,447 @@
+// fest_stage.cuh - the fused RK-stage sweep kernel, templated on the
+// arithmetic type, the reconstruction and the flux scheme; instantiated per
+// reconstruction in fest_stage_<method>.cu.
+//
+// One kernel per RK stage does, for a tile of cells, what the reference
+// spreads over compute_face_interpolant, reconstruct_boundary_state,
+// compute_fluxes, compute_residue, compute_time_step (stage 1) and
+// update_with (update.f90:129-547): between the state read and the state
+// write nothing touches HBM except the metrics.
+//
+// Tile: a CTA of 32x8 threads covers 30 interior cells in i (lanes 1..30,
+// lanes 0/31 are the i-halo) by 6 in j (warps 1..6, warps 0/7 the j-halo)
+// and marches along k over a chunk of interior planes (several chunks per
+// column when the block is small, so every SM gets work).  A 5-plane ring
+// in shared memory holds the stencil (planes k-2..k+2, 36x12 cells each,
+// converted to the arithmetic type on load).  i-face fluxes travel by warp
+// shuffles, j-face fluxes through shared memory, k-face fluxes stay in
+// registers across the march.
+//
+// T = float  (FEST_MIXED): reconstruction, flux, residual and the update's
+//             increments in FP32; the state stays FP64 and is advanced by
+//             adding an FP64 increment (delta form); metrics are read FP64.
+// T = double (FEST_FP64): the reference's arithmetic, update_with verbatim.
+#pragma once
+#include "fest_common.cuh"
+
+namespace fest {
+
+struct StageArgs {
+  const double* qin;    // stencil state (padded, ghosts filled)
+  double* qout;         // output state (interior written)
+  const double* qbase;  // state the update starts from (qin, or U_store for RK2/4)
+  const double* qU;     // blend source (U_store) when bA != 0
+  double bA, bB;        // out = bA*U + bB*updated (TVD-RK blends)
+  double TF, SF;        // update_with time/store factors
+  int TU, use_rn;       // RK2/RK4 residual accumulation
+  double* Rn;           // accumulator (interior, nv)
+  double* dt;           // local time step (interior)
+  int compute_dt;
+  double CFL;
+  double* res_out;      // nullable: FP64 residual of this stage (interior)
+  double* mflux[3];     // nullable: boundary mass fluxes (F,G,H var 1)
+  const double* faces[3];
+  const double* cells;
+  int* err;
+  int k_chunk;          // interior k planes per CTA (gridDim.z chunks)
+};
+
+namespace stage {
+
+constexpr int TX = 32, TY = 8;        // threads per CTA
+constexpr int IX = TX - 2, IY = TY - 2;  // interior cells per CTA
+constexpr int SW = TX + 4, SH = TY + 4;  // stencil plane extents (halo 2)
+constexpr int NRING = 5;
+
+
+
+template <typename T> struct SmemLine {
+  const T* p;   // element of normal coordinate c0
+  int c0, stride;
+  __device__ __forceinline__ T operator()(int c) const { return p[(c - c0) * stride]; }
+};
+template <typename T> struct RingLine {
+  const T* ring;  // ring + var/row/col offset; plane c lives in slot (c+2)%5
+  int plane_stride;
+  __device__ __forceinline__ T operator()(int c) const { return ring[((c + 2) % NRING) * plane_stride]; }
+};
+struct VolLine {
+  const double* p;  // cells + 4*pidx(cell at normal coordinate 0)
+  long long stride;
+  int n;            // extent along the line: coordinates clamp to [-2, n+2]
+  __device__ __forceinline__ double operator()(int c) const {
+    c = c < -2 ? -2 : (c > n + 2 ? n + 2 : c);
+    return p[4 * c * stride];
+  }
+};
+template <typename T> struct VolLineT {
+  VolLine v;
+  __device__ __forceinline__ T operator()(int c) const { return (T)v(c); }
+};
+
+template <typename T>
+__device__ __forceinline__ void load_face(const double* faces, long long idx, T& A, T& nx, T& ny, T& nz) {
+  const double2* f2 = reinterpret_cast<const double2*>(faces + 4 * idx);
+  double2 a = __ldg(f2), b = __ldg(f2 + 1);
+  A = (T)a.x; nx = (T)a.y; ny = (T)b.x; nz = (T)b.y;
+}
+
+// sound-speed term of compute_local_time_step (time.f90:167-231) for a face
+template <typename T>
+__device__ __forceinline__ T lambda_face(T gm, const T* L, const T* R, T A, T nx, T ny, T nz, T u,
+                                         T v, T w) {
+  T c = T(0.5) * (sqrt(gm * L[4] / L[0]) + sqrt(gm * R[4] / R[0]));
+  return A * (fabs((u * nx) + (v * ny) + (w * nz)) + c);
+}
+
+// ---- the update of one cell -------------------------------------------------
+// FP64: update_with(...,'conservative',...) (update.f90:367-485) verbatim.
+__device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
+                                            long long ci, const double* R_in, double dtc,
+                                            double vol) {
+  const long long P = p.d.P, N = ncells(p.d);
+  const double gm = p.gm;
+  double R[5], u1[5], u2[5];
+#pragma unroll
+  for (int l = 0; l < 5; ++l) R[l] = R_in[l];
+  u1[0] = a.qbase[c0];
+#pragma unroll
+  for (int l = 1; l < 5; ++l) u1[l] = a.qbase[c0 + P * l] * u1[0];
+  double s1 = u1[1] * u1[1] + u1[2] * u1[2] + u1[3] * u1[3];
+  u1[4] = (u1[4] / (gm - 1.) + 0.5 * s1) / u1[0];
+  if (a.use_rn) {
+#pragma unroll
+    for (int l = 0; l < 5; ++l) {
+      double rn = a.Rn[ci + N * l] + a.SF * R[l];
+      a.Rn[ci + N * l] = rn;
+      if (a.TU) R[l] = rn;
+    }
+  }
+  const double fac = (a.TF * dtc / vol);
+#pragma unroll
+  for (int l = 0; l < 5; ++l) u2[l] = u1[l] - R[l] * fac;
+#pragma unroll
+  for (int l = 1; l < 5; ++l) u2[l] = u2[l] / u2[0];
+  double s2 = u2[1] * u2[1] + u2[2] * u2[2] + u2[3] * u2[3];
+  u2[4] = (gm - 1.) * u2[0] * (u2[4] - (0.5 * s2));
+  bool bad = (u2[0] < 0.) || (u2[4] < 0.);
+#pragma unroll
+  for (int l = 0; l < 5; ++l) bad |= (u2[l] != u2[l]);
+  if (bad) return false;
+#pragma unroll
+  for (int l = 0; l < 5; ++l) {
+    double v = u2[l];
+    if (a.bA != 0.0) v = a.bA * a.qU[c0 + P * l] + a.bB * v;
+    a.qout[c0 + P * l] = v;
+  }
+  return true;
+}
+
+// FP32 arithmetic, FP64 accumulation: the conservative increment
+// dU = R*TF*dt/V is turned into primitive increments exactly (no
+// linearisation) in FP32 and added to the FP64 state.
+__device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
+                                            long long ci, const float* R_in, float dtc, float vol) {
+  const long long P = p.d.P, N = ncells(p.d);
+  const float gm1 = (float)(p.gm - 1.0);
+  float R[5];
+#pragma unroll
+  for (int l = 0; l < 5; ++l) R[l] = R_in[l];
+  if (a.use_rn) {
+#pragma unroll
+    for (int l = 0; l < 5; ++l) {
+      double rn = a.Rn[ci + N * l] + a.SF * (double)R[l];
+      a.Rn[ci + N * l] = rn;
+      if (a.TU) R[l] = (float)rn;
+    }
+  }
+  double b64[5];
+#pragma unroll
+  for (int l = 0; l < 5; ++l) b64[l] = a.qbase[c0 + P * l];
+  const float rho = (float)b64[0], u = (float)b64[1], v = (float)b64[2], w = (float)b64[3];
+  const float fac = (float)a.TF * dtc / vol;
+  const float dr = R[0] * fac, dmx = R[1] * fac, dmy = R[2] * fac, dmz = R[3] * fac, dE = R[4] * fac;
+  const float r2 = rho - dr;
+  const float ir2 = 1.0f / r2;
+  const float du = (u * dr - dmx) * ir2, dv = (v * dr - dmy) * ir2, dw = (w * dr - dmz) * ir2;
+  const float u2 = u + du, v2 = v + dv, w2 = w + dw;
+  const float dp = gm1 * (-dE + 0.5f * dr * (u2 * u2 + v2 * v2 + w2 * w2) -
+                          0.5f * rho * (2.0f * (u * du + v * dv + w * dw) + du * du + dv * dv + dw * dw));
+  double out[5] = {b64[0] - (double)dr, b64[1] + (double)du, b64[2] + (double)dv, b64[3] + (double)dw,
+                   b64[4] + (double)dp};
+  bool bad = (out[0] < 0.) || (out[4] < 0.);
+#pragma unroll
+  for (int l = 0; l < 5; ++l) bad |= (out[l] != out[l]);
+  if (bad) return false;
+#pragma unroll
+  for (int l = 0; l < 5; ++l) {
+    double val = out[l];
+    if (a.bA != 0.0) val = a.bA * a.qU[c0 + P * l] + a.bB * val;
+    a.qout[c0 + P * l] = val;
+  }
+  return true;
+}
+
+template <typename T, int INTERP, int FLUX>
+__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params p, StageArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NV = 5;
+  T* ring = reinterpret_cast<T*>(smem_raw);               // [NRING][NV][SH][SW]
+  T* xch = ring + NRING * NV * SH * SW;                   // [NV][TY][TX] j-face left states
+  T* gfl = xch + NV * TY * TX;                            // [NV][TY][TX] j-face fluxes
+  T* lam = gfl + NV * TY * TX;                            // [TY][TX]    j-face dt terms
+  const Dims& d = p.d;
+  const int lane = threadIdx.x, w = threadIdx.y, tid = w * TX + lane;
+  const int ib = 1 + IX * blockIdx.x, jb = 1 + IY * blockIdx.y;
+  const int i = ib - 1 + lane, j = jb - 1 + w;
+  const int i0 = ib - 3, j0 = jb - 3;  // stencil plane origin (col 0, row 0)
+  const bool in_i = lane >= 1 && lane <= IX && i <= d.imx - 1;
+  const bool in_j = w >= 1 && w <= IY && j <= d.jmx - 1;
+  const int plane = NV * SH * SW;
+  const T gm = (T)p.gm;
+  const bool thin = d.kmx == 2;
+
+  // clamp to the padded block so halo lanes past the edge stay finite
+  auto clampi = [&](int x, int hi) { return x < -2 ? -2 : (x > hi + 2 ? hi + 2 : x); };
+
+  // per-thread load offsets of the stencil plane (plane k adds (k+2)*ni*nj)
+  constexpr int NLOAD = (NV * SH * SW + TX * TY - 1) / (TX * TY);
+  int off[NLOAD];
+#pragma unroll
+  for (int m = 0; m < NLOAD; ++m) {
+    int e = tid + m * TX * TY;
+    if (e >= NV * SH * SW) e = NV * SH * SW - 1;
+    int l = e / (SH * SW), rem = e - l * (SH * SW), r = rem / SW, c = rem - r * SW;
+    int gi = clampi(i0 + c, d.imx), gj = clampi(j0 + r, d.jmx);
+    off[m] = (int)(pidx(d, gi, gj, -2) + d.P * l);
+  }
+  const int plane_stride = d.ni * d.nj;
+  auto load_plane = [&](int k) {
+    T* dst = ring + ((k + 2) % NRING) * plane;
+    const double* src = a.qin + (long long)(k + 2) * plane_stride;
+#pragma unroll
+    for (int m = 0; m < NLOAD; ++m) {
+      int e = tid + m * TX * TY;
+      if (e < NV * SH * SW) dst[e] = (T)__ldg(src + off[m]);
+    }
+  };
+  const int k0 = 1 + a.k_chunk * blockIdx.z;
+  const int k1 = min(k0 + a.k_chunk - 1, d.kmx - 1);
+
+  // per-thread march state for cell (i, j, k-1)
+  T Lp_prev[NV], H_prev[NV], dF_prev[NV], dG_prev[NV];
+  T lamk_prev = 0, lami_lo_prev = 0, lami_hi_prev = 0, lamj_lo_prev = 0, lamj_hi_prev = 0;
+#pragma unroll
+  for (int l = 0; l < NV; ++l) { Lp_prev[l] = 0; H_prev[l] = 0; dF_prev[l] = 0; dG_prev[l] = 0; }
+
+  const long long sj = d.ni, sk = (long long)d.ni * d.nj;
+  for (int kl = k0 - 3; kl <= k1 + 3; ++kl) {
+    __syncthreads();
+    load_plane(kl);
+    __syncthreads();
+    const int k = kl - 2;  // plane processed now
+    if (k < k0 - 1) continue;
+    const bool kin = k >= k0 && k <= k1;
+    T dF[NV], dG[NV];
+#pragma unroll
+    for (int l = 0; l < NV; ++l) { dF[l] = T(0); dG[l] = T(0); }
+    T lami_lo = 0, lami_hi = 0, lamj_lo = 0, lamj_hi = 0;
+    const int r = w + 2;               // own row in the stencil plane
+    const int cc = lane + 2;           // own column
+    const T* own = ring + ((k + 2) % NRING) * plane + r * SW + cc;  // var 0 of own cell
+    T qc[NV];
+#pragma unroll
+    for (int l = 0; l < NV; ++l) qc[l] = own[l * SH * SW];
+    // ---------------- i-faces (warp shuffles) ----------------
+    if (kin && in_j) {  // warp-uniform
+      T Rm[NV], Lp[NV];
+      const T* rowp = ring + ((k + 2) % NRING) * plane + r * SW;
+      const long long cbase = pidx(d, 0, clampi(j, d.jmx), k);
+      VolLineT<T> vol{VolLine{a.cells + 4 * cbase, 1, d.imx}};
+      SmemLine<T> pres{rowp + 4 * SH * SW + cc, i, 1};
+#pragma unroll
+      for (int l = 0; l < NV; ++l) {
+        SmemLine<T> q{rowp + l * SH * SW + cc, i, 1};
+        recon_cell<T, INTERP>(p, 0, i, l + 1, q, pres, vol, Rm[l], Lp[l]);
+      }
+      T L[NV], F[NV];
+#pragma unroll
+      for (int l = 0; l < NV; ++l) L[l] = __shfl_up_sync(0xffffffffu, Lp[l], 1);
+      T A, nx, ny, nz;
+      load_face<T>(a.faces[0], fidx(d, 0, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
+      face_flux<T, FLUX>(p, L, Rm, A, nx, ny, nz, (T)wall_mask(p, 0, i), F);
+      if (a.compute_dt) lami_lo = lambda_face<T>(gm, L, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
+      lami_hi = __shfl_down_sync(0xffffffffu, lami_lo, 1);
+#pragma unroll
+      for (int l = 0; l < NV; ++l) {
+        T Fh = __shfl_down_sync(0xffffffffu, F[l], 1);
+        dF[l] = Fh - F[l];
+      }
+      if (a.mflux[0] && in_j && (i == 1 || i == d.imx) && lane >= 1)
+        a.mflux[0][flidx(fldim(d, 0), i, j, k)] = (double)F[0];
+    }
+    // ---------------- j-faces (shared memory) ----------------
+    if (kin) {
+      T Rm[NV], Lp[NV];
+      const T* colp = ring + ((k + 2) % NRING) * plane + cc;
+      const long long cbase = pidx(d, clampi(i, d.imx), 0, k);
+      VolLineT<T> vol{VolLine{a.cells + 4 * cbase, sj, d.jmx}};
+      SmemLine<T> pres{colp + 4 * SH * SW + r * SW, j, SW};
+#pragma unroll
+      for (int l = 0; l < NV; ++l) {
+        SmemLine<T> q{colp + l * SH * SW + r * SW, j, SW};
+        recon_cell<T, INTERP>(p, 1, j, l + 1, q, pres, vol, Rm[l], Lp[l]);
+      }
+#pragma unroll
+      for (int l = 0; l < NV; ++l) xch[(l * TY + w) * TX + lane] = Lp[l];
+      __syncthreads();
+      T F[NV];
+#pragma unroll
+      for (int l = 0; l < NV; ++l) F[l] = T(0);
+      if (w >= 1) {
+        T L[NV];
+#pragma unroll
+        for (int l = 0; l < NV; ++l) L[l] = xch[(l * TY + w - 1) * TX + lane];
+        T A, nx, ny, nz;
+        load_face<T>(a.faces[1], fidx(d, 1, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
+        face_flux<T, FLUX>(p, L, Rm, A, nx, ny, nz, (T)wall_mask(p, 1, j), F);
+#pragma unroll
+        for (int l = 0; l < NV; ++l) gfl[(l * TY + w) * TX + lane] = F[l];
+        if (a.compute_dt) {
+          lamj_lo = lambda_face<T>(gm, L, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
+          lam[w * TX + lane] = lamj_lo;
+        }
+        if (a.mflux[1] && in_i && (j == 1 || j == d.jmx))
+          a.mflux[1][flidx(fldim(d, 1), i, j, k)] = (double)F[0];
+      }
+      __syncthreads();
+      if (w <= TY - 2) {
+#pragma unroll
+        for (int l = 0; l < NV; ++l) dG[l] = gfl[(l * TY + w + 1) * TX + lane] - F[l];
+        if (a.compute_dt) lamj_hi = lam[(w + 1) * TX + lane];
+      }
+    } else {
+      __syncthreads();
+      __syncthreads();
+    }
+    // ---------------- k-faces (registers, marching) ----------------
+    if (in_i && in_j) {
+      T Rm[NV], Lp[NV];
+      const T* cp = ring + r * SW + cc;
+      const long long cbase = pidx(d, i, j, 0);
+      VolLineT<T> vol{VolLine{a.cells + 4 * cbase, sk, d.kmx}};
+      RingLine<T> pres{cp + 4 * SH * SW, plane};
+#pragma unroll
+      for (int l = 0; l < NV; ++l) {
+        RingLine<T> q{cp + l * SH * SW, plane};
+        recon_cell<T, INTERP>(p, 2, k, l + 1, q, pres, vol, Rm[l], Lp[l]);
+      }
+      T H[NV];
+      T lamk = 0;
+      if (k >= k0) {
+        T A, nx, ny, nz;
+        load_face<T>(a.faces[2], fidx(d, 2, i, j, k), A, nx, ny, nz);
+        if (thin) {
+#pragma unroll
+          for (int l = 0; l < NV; ++l) H[l] = T(0);
+        } else {
+          face_flux<T, FLUX>(p, Lp_prev, Rm, A, nx, ny, nz, (T)wall_mask(p, 2, k), H);
+        }
+        if (a.compute_dt) lamk = lambda_face<T>(gm, Lp_prev, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
+        if (a.mflux[2] && (k == 1 || k == d.kmx)) a.mflux[2][flidx(fldim(d, 2), i, j, k)] = (double)H[0];
+        if (k >= k0 + 1) {
+          // cell (i, j, k-1) is complete: residual (scheme.f90:133-135)
+          const int kc = k - 1;
+          const long long c0 = pidx(d, i, j, kc), ci = cidx(d, i, j, kc);
+          T R[NV];
+#pragma unroll
+          for (int l = 0; l < NV; ++l) R[l] = (dF_prev[l] + dG_prev[l]) + (H[l] - H_prev[l]);
+          const T vol_c = (T)a.cells[4 * c0];
+          T dtc;
+          if (a.compute_dt) {
+            T s = lami_lo_prev + lamj_lo_prev + lamk_prev + lami_hi_prev + lamj_hi_prev + lamk;
+            dtc = (T(1) / s) * vol_c * (T)a.CFL;
+            a.dt[ci] = (double)dtc;
+          } else {
+            dtc = (T)a.dt[ci];
+          }
+          if (a.res_out)
+#pragma unroll
+            for (int l = 0; l < NV; ++l) a.res_out[ci + ncells(d) * l] = (double)R[l];
+          if (!update_cell(p, a, c0, ci, R, dtc, vol_c)) raise_error(a.err, FEST_ERR_NEGATIVE_STATE);
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < NV; ++l) {
+        Lp_prev[l] = Lp[l];
+        if (k >= k0) H_prev[l] = H[l];
+        if (kin) { dF_prev[l] = dF[l]; dG_prev[l] = dG[l]; }
+      }
+      if (k >= k0) lamk_prev = lamk;
+      if (kin) {
+        lami_lo_prev = lami_lo; lami_hi_prev = lami_hi;
+        lamj_lo_prev = lamj_lo; lamj_hi_prev = lamj_hi;
+      }
+    }
+  }
+}
+
+template <typename T> inline size_t stage_smem() {
+  return sizeof(T) * ((size_t)NRING * 5 * SH * SW + 2 * 5 * TY * TX + TY * TX);
+}
+
+
+}  // namespace stage
+
+// one host launcher per reconstruction (fest_stage_<method>.cu)
+#define FEST_STAGE_LAUNCHER(name) \
+  int name(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a)
+FEST_STAGE_LAUNCHER(launch_stage_none);
+FEST_STAGE_LAUNCHER(launch_stage_muscl);
+FEST_STAGE_LAUNCHER(launch_stage_ppm);
+FEST_STAGE_LAUNCHER(launch_stage_weno);
+FEST_STAGE_LAUNCHER(launch_stage_weno_nm);
+
+template <int INTERP>
+int launch_stage_t(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a) {
+  using namespace stage;
+  const dim3 blk(TX, TY);
+  static bool attrs = false;
+#define FEST_SET(T, F)                                                                     \
+  cudaFuncSetAttribute(k_stage<T, INTERP, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)stage_smem<T>())
+  if (!attrs) {
+    FEST_SET(float, 0); FEST_SET(float, 1); FEST_SET(float, 2);
+    FEST_SET(float, 3); FEST_SET(float, 4); FEST_SET(float, 5);
+    FEST_SET(double, 0); FEST_SET(double, 1); FEST_SET(double, 2);
+    FEST_SET(double, 3); FEST_SET(double, 4); FEST_SET(double, 5);
+    attrs = true;
+  }
+#undef FEST_SET
+#define FEST_GO(T, F) k_stage<T, INTERP, F><<<grid, blk, stage_smem<T>(), s>>>(p, a)
+  if (prec == FEST_MIXED) {
+    switch (flux) {
+      case 0: FEST_GO(float, 0); break;
+      case 1: FEST_GO(float, 1); break;
+      case 2: FEST_GO(float, 2); break;
+      case 3: FEST_GO(float, 3); break;
+      case 4: FEST_GO(float, 4); break;
+      case 5: FEST_GO(float, 5); break;
+      default: return FEST_ERR_ARG;
+    }
+  } else {
+    switch (flux) {
+      case 0: FEST_GO(double, 0); break;
+      case 1: FEST_GO(double, 1); break;
+      case 2: FEST_GO(double, 2); break;
+      case 3: FEST_GO(double, 3); break;
+      case 4: FEST_GO(double, 4); break;
+      case 5: FEST_GO(double, 5); break;
+      default: return FEST_ERR_ARG;
+    }
+  }
+#undef FEST_GO
+  return FEST_OK;
+}
+
+}  // namespace fest

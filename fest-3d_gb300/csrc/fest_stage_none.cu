@@ -1,0 +1,7 @@
+// fest_stage_none.cu - fused stage sweeps with the none reconstruction
+// (all six flux schemes, FP32 and FP64); see fest_stage.cuh.
+#include "fest_stage.cuh"
+
+namespace fest {
+FEST_STAGE_LAUNCHER(launch_stage_none) { return launch_stage_t<FEST_INTERP_NONE>(prec, flux, grid, s, p, a); }
+}  // namespace fest

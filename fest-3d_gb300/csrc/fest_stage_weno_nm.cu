@@ -1,0 +1,7 @@
+// fest_stage_weno_nm.cu - fused stage sweeps with the weno_nm reconstruction
+// (all six flux schemes, FP32 and FP64); see fest_stage.cuh.
+#include "fest_stage.cuh"
+
+namespace fest {
+FEST_STAGE_LAUNCHER(launch_stage_weno_nm) { return launch_stage_t<FEST_INTERP_WENO_NM>(prec, flux, grid, s, p, a); }
+}  // namespace fest
