@@ -23,9 +23,10 @@ FEST_ERR_NEGATIVE_STATE = 4
 FEST_ERR_TIMEOUT = 5
 FEST_ERR_NOMEM = 6
 FEST_ERR_NO_DEVICE = 7
+FEST_ERR_SCRATCH = 8
 ERR_NAMES = {0: "FEST_OK", 1: "FEST_ERR_ARG", 2: "FEST_ERR_CUDA", 3: "FEST_ERR_NAN",
              4: "FEST_ERR_NEGATIVE_STATE", 5: "FEST_ERR_TIMEOUT", 6: "FEST_ERR_NOMEM",
-             7: "FEST_ERR_NO_DEVICE"}
+             7: "FEST_ERR_NO_DEVICE", 8: "FEST_ERR_SCRATCH"}
 
 FLUX = {"ausm": 0, "ausmP": 1, "ausmUP": 2, "slau": 3, "ldfss0": 4, "van_leer": 5}
 INTERP = {"none": 0, "muscl": 1, "ppm": 2, "weno": 3, "weno_NM": 4}
@@ -201,6 +202,8 @@ _SIGS = {
     "fest_set_stream": [C.c_void_p, C.c_void_p],
     "fest_profile": [C.c_void_p, C.c_int],
     "fest_profile_read": [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)],
+    "fest_find_resnorm_noalloc": [C.POINTER(Extent), C.POINTER(Flow), C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, _DP, C.c_void_p],
 }
 EXPORTED = tuple(_SIGS) + ("fest_kernel_launches", "fest_array_size", "fest_set_array",
                           "fest_get_array")

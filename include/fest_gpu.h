@@ -50,6 +50,7 @@ extern "C" {
 #define FEST_ERR_TIMEOUT         5  /* a bounded device wait gave up           */
 #define FEST_ERR_NOMEM           6  /* device allocation failed                */
 #define FEST_ERR_NO_DEVICE       7  /* no CUDA device visible                  */
+#define FEST_ERR_SCRATCH         8  /* request exceeds a fixed scratch area    */
 
 /* ---- scheme selectors (schemetype, vartypes.f90:197-232) ---------------- */
 enum { FEST_FLUX_AUSM = 0, FEST_FLUX_AUSMP = 1, FEST_FLUX_AUSMUP = 2,
@@ -241,6 +242,25 @@ int fest_set_stream(fest_handle *h, void *cuda_stream);
  * and their summed device time */
 int fest_profile(fest_handle *h, int enable);
 int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
+
+/* ---- allocation-free norm ------------------------------------------------ */
+/* No counterpart in the reference.  find_resnorm (resnorm.f90:62) without a
+ * handle, on caller-owned DEVICE arrays: residue in the FEST_ARR_RESIDUE
+ * layout, F/G/H in the FEST_ARR_F/G/H layouts (only variable 1, the mass
+ * flux, is read); res_abs (host, n_var+1) as fest_find_resnorm returns it.
+ * For callers that cannot allocate device memory where they need the norm
+ * (memory held by their own pool, or an asynchronous loop that a
+ * cudaMalloc/cudaFree pair would synchronise).  It allocates nothing: its
+ * scratch is a fixed 32 KiB area per device, so n_var may be at most 7
+ * (FEST_ERR_SCRATCH otherwise).  Calls that overlap in time on one device
+ * race on that area and must be serialised by the caller.  The first call
+ * on each device (with that device current) does the setup and should come
+ * before any stream capture.  Runs on cuda_stream (NULL: the legacy default
+ * stream) and returns after synchronising it. */
+int fest_find_resnorm_noalloc(const fest_extent *ext, const fest_flow *flow,
+                              const double *residue, const double *F,
+                              const double *G, const double *H,
+                              double *res_abs, void *cuda_stream);
 
 #ifdef __cplusplus
 }
