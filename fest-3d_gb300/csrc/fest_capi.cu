@@ -422,9 +422,21 @@ int fest_get_array(fest_handle* h, int which, double* host) {
   return finish(h);
 }
 
+// the fused path keeps FP32 copies of the metrics: new metrics retire it
+// (its state goes back to qp first; it is rebuilt at the next fest_step)
+static int drop_fused(fest_handle* h) {
+  if (!h->fused) return FEST_OK;
+  RET(sync_fused(h));
+  CK(cudaStreamSynchronize(h->s));
+  fused_destroy(h->fused);
+  h->fused = nullptr;
+  return FEST_OK;
+}
+
 int fest_setup_geometry(fest_handle* h, double* nodes, double* cells, double* Ifaces,
                         double* Jfaces, double* Kfaces) {
   if (!h || !nodes) return FEST_ERR_ARG;
+  RET(drop_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.nodes, nodes, z.nodes));
   launch_geometry(h->p, h->d, h->L());
@@ -439,6 +451,7 @@ int fest_setup_geometry(fest_handle* h, double* nodes, double* cells, double* If
 int fest_set_metrics(fest_handle* h, const double* cells, const double* Ifaces,
                      const double* Jfaces, const double* Kfaces) {
   if (!h) return FEST_ERR_ARG;
+  RET(drop_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.cells, cells, z.cells));
   RET(up(h, h->d.faces[0], Ifaces, z.faces[0]));

@@ -18,7 +18,8 @@ using namespace stage;
 // BCs stop rewriting them (fix() after iteration 2).  Non-interior cells:
 // q = a*Us + b*X with Us the state before the iteration's BCs and X the last
 // stage's input (its ghosts as that stage's BCs left them).
-__global__ void k_ghost_blend(Dims d, double* q, const double* Us, const double* X, double a, double b) {
+__global__ void k_ghost_blend(Dims d, double* q, float* q32, const double* Us, const double* X,
+                              double a, double b) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= d.P * d.nv) return;
   long long c = t % d.P;
@@ -26,8 +27,33 @@ __global__ void k_ghost_blend(Dims d, double* q, const double* Us, const double*
   long long r = c / d.ni;
   int j = (int)(r % d.nj) - 2, k = (int)(r / d.nj) - 2;
   bool interior = i >= 1 && i <= d.imx - 1 && j >= 1 && j <= d.jmx - 1 && k >= 1 && k <= d.kmx - 1;
-  if (!interior) q[t] = a * Us[t] + b * X[t];
+  if (interior) return;
+  const double v = a * Us[t] + b * X[t];
+  q[t] = v;
+  if (q32) q32[t] = (float)v;
 }
+
+// FP32 mirrors for the mixed sweep: state (whole padded array), face
+// records {A,nx,ny,nz} and cell volumes.  Rounding to nearest, as a
+// conversion on load would do.
+__global__ void k_to_f32(const double* src, float* dst, long long n) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    dst[t] = (float)src[t];
+}
+__global__ void k_faces_to_f32(const double* faces, float4* dst, long long n) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double* f = faces + 4 * t;
+    dst[t] = make_float4((float)f[0], (float)f[1], (float)f[2], (float)f[3]);
+  }
+}
+__global__ void k_vol_to_f32(const double* cells, float* dst, long long n) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    dst[t] = (float)cells[4 * t];
+}
+unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
 
@@ -38,6 +64,13 @@ struct FusedState {
   BlockRef* table[3] = {nullptr, nullptr, nullptr};
   int cur = 0;       // buffer holding the current state
   bool seeded = false;
+  // mixed sweep: FP32 mirrors of the three state buffers and of the metrics
+  float* Q32[3] = {nullptr, nullptr, nullptr};
+  float4* F32[3] = {nullptr, nullptr, nullptr};
+  float* V32 = nullptr;
+  bool mirror_valid = false;  // Q32 interiors match Q
+  int kc[2] = {0, 0};         // tuned k-chunk per precision (0: not tuned yet)
+  int* tune_err = nullptr;    // error word of the tuning launches
   std::vector<void*> allocs;
   bool profiling = false;
   std::vector<cudaEvent_t> ev;  // start/end pairs of profiled launches
@@ -72,6 +105,9 @@ int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cuda
     if (cudaMalloc((void**)&f->Us, bytes) != cudaSuccess) { fused_destroy(f); return FEST_ERR_NOMEM; }
     f->allocs.push_back(f->Us);
   }
+  if (cudaMalloc((void**)&f->tune_err, sizeof(int)) != cudaSuccess) { fused_destroy(f); return FEST_ERR_NOMEM; }
+  f->allocs.push_back(f->tune_err);
+  cudaMemsetAsync(f->tune_err, 0, sizeof(int), s);
   for (int n = 0; n < 3; ++n) {
     BlockRef ref{b, p.d};
     ref.b.qp = f->Q[n];
@@ -101,15 +137,105 @@ static void seed(FusedState* f, cudaStream_t s) {
   for (int n = 0; n < 3; ++n)
     if (n != f->cur) cudaMemcpyAsync(f->Q[n], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
   f->seeded = true;
+  f->mirror_valid = false;
+}
+
+// allocate and fill the FP32 mirrors the mixed sweep reads (once per
+// handle for the metrics; the state mirror whenever it went stale)
+static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long long* cnt) {
+  const Dims& d = f->d;
+  const long long n = d.P * d.nv;
+  if (!f->V32) {  // V32 is allocated last: a partial earlier attempt retries
+    for (int m = 0; m < 3; ++m) {
+      if (cudaMalloc((void**)&f->Q32[m], sizeof(float) * (size_t)n) != cudaSuccess) return FEST_ERR_NOMEM;
+      f->allocs.push_back(f->Q32[m]);
+      const long long nf = nfaces(d, m);
+      if (cudaMalloc((void**)&f->F32[m], sizeof(float4) * (size_t)nf) != cudaSuccess) return FEST_ERR_NOMEM;
+      f->allocs.push_back(f->F32[m]);
+      k_faces_to_f32<<<grid_for(nf), 256, 0, s>>>(b.faces[m], f->F32[m], nf);
+      ++*cnt;
+    }
+    if (cudaMalloc((void**)&f->V32, sizeof(float) * (size_t)d.P) != cudaSuccess) return FEST_ERR_NOMEM;
+    f->allocs.push_back(f->V32);
+    k_vol_to_f32<<<grid_for(d.P), 256, 0, s>>>(b.cells, f->V32, d.P);
+    ++*cnt;
+    f->mirror_valid = false;
+  }
+  if (!f->mirror_valid) {
+    // whole padded arrays, so that the edge and corner cells the halo lanes
+    // read (results discarded) hold finite values
+    for (int m = 0; m < 3; ++m) {
+      k_to_f32<<<grid_for(n), 256, 0, s>>>(f->Q[m], f->Q32[m], n);
+      ++*cnt;
+    }
+    f->mirror_valid = true;
+  }
+  return FEST_OK;
+}
+
+static void launch_sweep(const Params& p, int prec, dim3 grid, cudaStream_t s, const StageArgs& a) {
+  switch (p.interp) {
+    case FEST_INTERP_NONE: launch_stage_none(prec, p.flux, grid, s, p, a); break;
+    case FEST_INTERP_MUSCL: launch_stage_muscl(prec, p.flux, grid, s, p, a); break;
+    case FEST_INTERP_PPM: launch_stage_ppm(prec, p.flux, grid, s, p, a); break;
+    case FEST_INTERP_WENO: launch_stage_weno(prec, p.flux, grid, s, p, a); break;
+    default: launch_stage_weno_nm(prec, p.flux, grid, s, p, a); break;
+  }
+}
+
+// Pick the k-chunk (interior planes per CTA) by timing the sweep itself on
+// the current inputs: short chunks give more CTAs, long chunks re-read fewer
+// halo planes.  The trial launches write only the stage's output buffers
+// (rewritten by the real launch) and a private error word; the RK
+// accumulator is left alone.  Chunking does not change any result.
+static int tune_chunk(FusedState* f, const Params& p, int prec, StageArgs a, cudaStream_t s,
+                      long long* cnt) {
+  const int nk = p.d.kmx - 1;
+  const dim3 g0((p.d.imx - 1 + IX - 1) / IX, (p.d.jmx - 1 + IY - 1) / IY, 1);
+  a.use_rn = 0; a.TU = 0; a.res_out = nullptr;
+  for (int dir = 0; dir < 3; ++dir) a.mflux[dir] = nullptr;
+  a.err = f->tune_err;
+  const int cand[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = nk, last_chunks = -1;
+  float best_ms = 1e30f;
+  for (int kc : cand) {
+    if (kc > nk) kc = nk;
+    const int chunks = (nk + kc - 1) / kc;
+    if (chunks == last_chunks) continue;
+    last_chunks = chunks;
+    a.k_chunk = (nk + chunks - 1) / chunks;
+    dim3 g = g0;
+    g.z = chunks;
+    launch_sweep(p, prec, g, s, a);  // warm-up
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; ++r) launch_sweep(p, prec, g, s, a);
+    cudaEventRecord(e1, s);
+    *cnt += 4;
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess) break;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) { best_ms = ms; best = a.k_chunk; }
+    if (chunks == 1) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaMemsetAsync(f->tune_err, 0, sizeof(int), s);
+  return best;
 }
 
 static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int prec, int in, int out,
                   int base, double bA, double bB, double TF, double SF, int TU, int use_rn,
                   int compute_dt, double CFL, int iter, bool last, cudaStream_t s, long long* cnt) {
+  const bool mixed = prec == FEST_MIXED;
   DevBlock bb = b;
   bb.qp = f->Q[in];
+  bb.qp32 = mixed ? f->Q32[in] : nullptr;
   Launcher L{s, cnt};
-  launch_ghosts(p, bb, f->table[in], iter, L);
+  // edge/corner ghosts are never read by an interior update: no averaging
+  launch_ghosts(p, bb, f->table[in], iter, L, false);
   StageArgs a;
   a.qin = f->Q[in];
   a.qout = f->Q[out];
@@ -124,12 +250,15 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   }
   a.cells = b.cells;
   a.err = b.err;
-  // enough CTAs to give every SM two: split the k-march into chunks
-  const int tiles = ((p.d.imx - 1 + IX - 1) / IX) * ((p.d.jmx - 1 + IY - 1) / IY);
+  a.qin32 = mixed ? f->Q32[in] : nullptr;
+  a.qout32 = mixed ? f->Q32[out] : nullptr;
+  for (int dir = 0; dir < 3; ++dir) a.faces32[dir] = mixed ? f->F32[dir] : nullptr;
+  a.vol32 = mixed ? f->V32 : nullptr;
   const int nk = p.d.kmx - 1;
-  int chunks = std::max(1, std::min(nk, (4 * 152 + tiles - 1) / tiles));
-  a.k_chunk = (nk + chunks - 1) / chunks;
-  chunks = (nk + a.k_chunk - 1) / a.k_chunk;
+  int& kc = f->kc[mixed ? 1 : 0];
+  if (kc == 0) kc = tune_chunk(f, p, prec, a, s, cnt);
+  a.k_chunk = kc;
+  const int chunks = (nk + kc - 1) / kc;
   dim3 grid((p.d.imx - 1 + IX - 1) / IX, (p.d.jmx - 1 + IY - 1) / IY, chunks);
   if (f->profiling) {
     if (f->nev + 2 > f->ev.size())
@@ -140,13 +269,7 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
       }
     cudaEventRecord(f->ev[f->nev], s);
   }
-  switch (p.interp) {
-    case FEST_INTERP_NONE: launch_stage_none(prec, p.flux, grid, s, p, a); break;
-    case FEST_INTERP_MUSCL: launch_stage_muscl(prec, p.flux, grid, s, p, a); break;
-    case FEST_INTERP_PPM: launch_stage_ppm(prec, p.flux, grid, s, p, a); break;
-    case FEST_INTERP_WENO: launch_stage_weno(prec, p.flux, grid, s, p, a); break;
-    default: launch_stage_weno_nm(prec, p.flux, grid, s, p, a); break;
-  }
+  launch_sweep(p, prec, grid, s, a);
   if (f->profiling) {
     cudaEventRecord(f->ev[f->nev + 1], s);
     f->nev += 2;
@@ -158,6 +281,13 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
               int first_iter, double CFL, cudaStream_t s, long long* cnt) {
   if (!f) return FEST_ERR_ARG;
   if (!f->seeded) seed(f, s);
+  const bool mixed = prec == FEST_MIXED;
+  if (mixed) {
+    int rc = ensure_mirrors(f, b, s, cnt);
+    if (rc) return rc;
+  } else {
+    f->mirror_valid = false;  // FP64 stages do not maintain the mirror
+  }
   for (int n = 0; n < n_iters; ++n) {
     const int it = first_iter + n;
     const bool lastit = (n == n_iters - 1);
@@ -170,7 +300,8 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
         if (n == U) continue;
         DevBlock bb = b;
         bb.qp = f->Q[n];
-        launch_ghosts(p, bb, f->table[n], it, Launcher{s, cnt});
+        bb.qp32 = mixed ? f->Q32[n] : nullptr;
+        launch_ghosts(p, bb, f->table[n], it, Launcher{s, cnt}, false);
       }
     }
     const size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
@@ -186,7 +317,8 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
         run_stage(f, p, b, prec, A, U, A, 0.5, 0.5, 1., 1., 0, 0, 0, CFL, it, lastit, s, cnt);
         if (tvd_early) {
           long long n = p.d.P * p.d.nv;
-          k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], f->Us, f->Q[A], 0.5, 0.5);
+          k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
+                                                                   f->Us, f->Q[A], 0.5, 0.5);
           ++*cnt;
         }
         break;
@@ -196,7 +328,8 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
         run_stage(f, p, b, prec, B, U, B, 1. / 3., 2. / 3., 1., 1., 0, 0, 0, CFL, it, lastit, s, cnt);
         if (tvd_early) {
           long long n = p.d.P * p.d.nv;
-          k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], f->Us, f->Q[B], 1. / 3., 2. / 3.);
+          k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
+                                                                   f->Us, f->Q[B], 1. / 3., 2. / 3.);
           ++*cnt;
         }
         break;
@@ -218,19 +351,23 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
     // the blended ghosts must persist in every buffer once fix() stops
     if (tvd_early)
       for (int n = 0; n < 3; ++n)
-        if (n != f->cur) cudaMemcpyAsync(f->Q[n], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
+        if (n != f->cur) {
+          cudaMemcpyAsync(f->Q[n], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
+          if (mixed)
+            cudaMemcpyAsync(f->Q32[n], f->Q32[f->cur], bytes / 2, cudaMemcpyDeviceToDevice, s);
+        }
   }
   return FEST_OK;
 }
 
 int fused_export_state(FusedState* f, double* qp, cudaStream_t s) {
   if (!f) return FEST_ERR_ARG;
-  if (f->Q[f->cur] != qp) {
+  if (f->Q[f->cur] != qp)
     cudaMemcpyAsync(qp, f->Q[f->cur], sizeof(double) * (size_t)f->d.P * f->d.nv,
                     cudaMemcpyDeviceToDevice, s);
-    f->cur = 0;
-    f->seeded = false;
-  }
+  // the caller may now change qp: the next fused run starts from it again
+  f->cur = 0;
+  f->seeded = false;
   return FEST_OK;
 }
 

@@ -293,6 +293,15 @@ __global__ void k_ghosts(Params p, DevBlock b, const BlockRef* blocks, int iter,
       }
     }
   }
+  // the mixed fused path reads its stencil from an FP32 mirror: refresh the
+  // face ghosts of this column there (edges and corners are never read by
+  // an interior update)
+  if (b.qp32 && interior && id != -9)
+    for (int l = 0; l < d.nv; ++l)
+      for (int L = 1; L <= 3; ++L) {
+        const long long g = ghost_p(d, f, L, ta, tb) + d.P * l;
+        b.qp32[g] = (float)b.qp[g];
+      }
 }
 
 // bc_primitive.f90:209-224 corner/edge averaging, 16 ordered statements
@@ -1046,7 +1055,7 @@ bool ghosts_need_sequential(const Params& p) {
 }
 
 void launch_ghosts(const Params& p, const DevBlock& b, const BlockRef* tab, int iter,
-                   const Launcher& L) {
+                   const Launcher& L, bool corners) {
   const Dims& d = p.d;
   int wmax = 0;
   for (int f = 0; f < 6; ++f) {
@@ -1075,6 +1084,7 @@ void launch_ghosts(const Params& p, const DevBlock& b, const BlockRef* tab, int 
     k_ghosts<<<g, TPB, 0, L.s>>>(p, b, tab, iter, 63);
     ++*L.count;
   }
+  if (!corners) return;
   k_corners<<<1, 256, 0, L.s>>>(p, b.qp);
   ++*L.count;
 }

@@ -14,6 +14,7 @@ struct DevBlock {
   double *res, *grad[3], *mu, *mut, *F1, *dist, *dt, *Ustore, *Rstore;
   double *red;              // reduction scratch (kRedSlots doubles)
   int *err;                 // device error word
+  float *qp32;              // FP32 mirror of qp kept by the mixed fused path (else null)
 };
 constexpr int kRedSlots = 1 << 16;
 
@@ -31,7 +32,7 @@ struct Launcher {
 // ghost cells: interface exchange + populate_ghost_primitive + corners
 // d_table: device array of every block a face of this block may pair with
 void launch_ghosts(const Params& p, const DevBlock& b, const BlockRef* d_table, int iter,
-                   const Launcher& L);
+                   const Launcher& L, bool corners = true);
 bool ghosts_need_sequential(const Params& p);
 void launch_temperature(const Params& p, const DevBlock& b, const Launcher& L);
 // mode 0: compute_face_interpolant only; 1: + reconstruct_boundary_state;

@@ -44,6 +44,11 @@ struct StageArgs {
   const double* cells;
   int* err;
   int k_chunk;          // interior k planes per CTA (gridDim.z chunks)
+  // FP32 mirrors read by the mixed sweep (T = float); unused in FP64
+  const float* qin32;   // stencil state (interior from the previous stage, ghosts from the fill)
+  float* qout32;        // mirror of qout (interior written)
+  const float4* faces32[3];  // {A,nx,ny,nz} per face
+  const float* vol32;   // cell volumes (padded)
 };
 
 namespace stage {
@@ -79,12 +84,39 @@ template <typename T> struct VolLineT {
   __device__ __forceinline__ T operator()(int c) const { return (T)v(c); }
 };
 
-template <typename T>
-__device__ __forceinline__ void load_face(const double* faces, long long idx, T& A, T& nx, T& ny, T& nz) {
-  const double2* f2 = reinterpret_cast<const double2*>(faces + 4 * idx);
-  double2 a = __ldg(f2), b = __ldg(f2 + 1);
-  A = (T)a.x; nx = (T)a.y; ny = (T)b.x; nz = (T)b.y;
+__device__ __forceinline__ void load_face(const StageArgs& a, int dir, long long idx, double& A,
+                                          double& nx, double& ny, double& nz) {
+  const double2* f2 = reinterpret_cast<const double2*>(a.faces[dir] + 4 * idx);
+  double2 u = __ldg(f2), v = __ldg(f2 + 1);
+  A = u.x; nx = u.y; ny = v.x; nz = v.y;
 }
+__device__ __forceinline__ void load_face(const StageArgs& a, int dir, long long idx, float& A,
+                                          float& nx, float& ny, float& nz) {
+  const float4 u = __ldg(a.faces32[dir] + idx);
+  A = u.x; nx = u.y; ny = u.z; nz = u.w;
+}
+// cell volume along a line: AoS cells (FP64) or the FP32 mirror
+struct VolLine32 {
+  const float* p;  // vol32 + pidx(cell at normal coordinate 0)
+  long long stride;
+  int n;
+  __device__ __forceinline__ float operator()(int c) const {
+    c = c < -2 ? -2 : (c > n + 2 ? n + 2 : c);
+    return p[c * stride];
+  }
+};
+__device__ __forceinline__ VolLineT<double> vol_line(const StageArgs& a, double, long long base,
+                                                     long long stride, int n) {
+  return VolLineT<double>{VolLine{a.cells + 4 * base, stride, n}};
+}
+__device__ __forceinline__ VolLine32 vol_line(const StageArgs& a, float, long long base,
+                                              long long stride, int n) {
+  return VolLine32{a.vol32 + base, stride, n};
+}
+__device__ __forceinline__ double cell_vol(const StageArgs& a, double, long long c0) { return a.cells[4 * c0]; }
+__device__ __forceinline__ float cell_vol(const StageArgs& a, float, long long c0) { return a.vol32[c0]; }
+__device__ __forceinline__ const double* stencil_src(const StageArgs& a, double) { return a.qin; }
+__device__ __forceinline__ const float* stencil_src(const StageArgs& a, float) { return a.qin32; }
 
 // sound-speed term of compute_local_time_step (time.f90:167-231) for a face
 template <typename T>
@@ -98,7 +130,7 @@ __device__ __forceinline__ T lambda_face(T gm, const T* L, const T* R, T A, T nx
 // FP64: update_with(...,'conservative',...) (update.f90:367-485) verbatim.
 __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
                                             long long ci, const double* R_in, double dtc,
-                                            double vol) {
+                                            double vol, const double*) {
   const long long P = p.d.P, N = ncells(p.d);
   const double gm = p.gm;
   double R[5], u1[5], u2[5];
@@ -141,7 +173,8 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
 // dU = R*TF*dt/V is turned into primitive increments exactly (no
 // linearisation) in FP32 and added to the FP64 state.
 __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
-                                            long long ci, const float* R_in, float dtc, float vol) {
+                                            long long ci, const float* R_in, float dtc, float vol,
+                                            const float* qc) {
   const long long P = p.d.P, N = ncells(p.d);
   const float gm1 = (float)(p.gm - 1.0);
   float R[5];
@@ -158,7 +191,11 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
   double b64[5];
 #pragma unroll
   for (int l = 0; l < 5; ++l) b64[l] = a.qbase[c0 + P * l];
-  const float rho = (float)b64[0], u = (float)b64[1], v = (float)b64[2], w = (float)b64[3];
+  // FP32 copies of the base state: the stencil's own cell when the update
+  // starts from the stencil state (bit-identical to converting b64)
+  const bool own = a.qbase == a.qin;
+  const float rho = own ? qc[0] : (float)b64[0], u = own ? qc[1] : (float)b64[1],
+              v = own ? qc[2] : (float)b64[2], w = own ? qc[3] : (float)b64[3];
   const float fac = (float)a.TF * dtc / vol;
   const float dr = R[0] * fac, dmx = R[1] * fac, dmy = R[2] * fac, dmz = R[3] * fac, dE = R[4] * fac;
   const float r2 = rho - dr;
@@ -178,6 +215,7 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
     double val = out[l];
     if (a.bA != 0.0) val = a.bA * a.qU[c0 + P * l] + a.bB * val;
     a.qout[c0 + P * l] = val;
+    a.qout32[c0 + P * l] = (float)val;
   }
   return true;
 }
@@ -216,13 +254,14 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
     off[m] = (int)(pidx(d, gi, gj, -2) + d.P * l);
   }
   const int plane_stride = d.ni * d.nj;
+  const T* qsrc = stencil_src(a, T(0));
   auto load_plane = [&](int k) {
     T* dst = ring + ((k + 2) % NRING) * plane;
-    const double* src = a.qin + (long long)(k + 2) * plane_stride;
+    const T* src = qsrc + (long long)(k + 2) * plane_stride;
 #pragma unroll
     for (int m = 0; m < NLOAD; ++m) {
       int e = tid + m * TX * TY;
-      if (e < NV * SH * SW) dst[e] = (T)__ldg(src + off[m]);
+      if (e < NV * SH * SW) dst[e] = __ldg(src + off[m]);
     }
   };
   const int k0 = 1 + a.k_chunk * blockIdx.z;
@@ -256,8 +295,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
     if (kin && in_j) {  // warp-uniform
       T Rm[NV], Lp[NV];
       const T* rowp = ring + ((k + 2) % NRING) * plane + r * SW;
-      const long long cbase = pidx(d, 0, clampi(j, d.jmx), k);
-      VolLineT<T> vol{VolLine{a.cells + 4 * cbase, 1, d.imx}};
+      const auto vol = vol_line(a, T(0), pidx(d, 0, clampi(j, d.jmx), k), 1, d.imx);
       SmemLine<T> pres{rowp + 4 * SH * SW + cc, i, 1};
 #pragma unroll
       for (int l = 0; l < NV; ++l) {
@@ -268,7 +306,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
 #pragma unroll
       for (int l = 0; l < NV; ++l) L[l] = __shfl_up_sync(0xffffffffu, Lp[l], 1);
       T A, nx, ny, nz;
-      load_face<T>(a.faces[0], fidx(d, 0, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
+      load_face(a, 0, fidx(d, 0, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
       face_flux<T, FLUX>(p, L, Rm, A, nx, ny, nz, (T)wall_mask(p, 0, i), F);
       if (a.compute_dt) lami_lo = lambda_face<T>(gm, L, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
       lami_hi = __shfl_down_sync(0xffffffffu, lami_lo, 1);
@@ -284,8 +322,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
     if (kin) {
       T Rm[NV], Lp[NV];
       const T* colp = ring + ((k + 2) % NRING) * plane + cc;
-      const long long cbase = pidx(d, clampi(i, d.imx), 0, k);
-      VolLineT<T> vol{VolLine{a.cells + 4 * cbase, sj, d.jmx}};
+      const auto vol = vol_line(a, T(0), pidx(d, clampi(i, d.imx), 0, k), sj, d.jmx);
       SmemLine<T> pres{colp + 4 * SH * SW + r * SW, j, SW};
 #pragma unroll
       for (int l = 0; l < NV; ++l) {
@@ -303,7 +340,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
 #pragma unroll
         for (int l = 0; l < NV; ++l) L[l] = xch[(l * TY + w - 1) * TX + lane];
         T A, nx, ny, nz;
-        load_face<T>(a.faces[1], fidx(d, 1, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
+        load_face(a, 1, fidx(d, 1, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
         face_flux<T, FLUX>(p, L, Rm, A, nx, ny, nz, (T)wall_mask(p, 1, j), F);
 #pragma unroll
         for (int l = 0; l < NV; ++l) gfl[(l * TY + w) * TX + lane] = F[l];
@@ -328,8 +365,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
     if (in_i && in_j) {
       T Rm[NV], Lp[NV];
       const T* cp = ring + r * SW + cc;
-      const long long cbase = pidx(d, i, j, 0);
-      VolLineT<T> vol{VolLine{a.cells + 4 * cbase, sk, d.kmx}};
+      const auto vol = vol_line(a, T(0), pidx(d, i, j, 0), sk, d.kmx);
       RingLine<T> pres{cp + 4 * SH * SW, plane};
 #pragma unroll
       for (int l = 0; l < NV; ++l) {
@@ -340,7 +376,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
       T lamk = 0;
       if (k >= k0) {
         T A, nx, ny, nz;
-        load_face<T>(a.faces[2], fidx(d, 2, i, j, k), A, nx, ny, nz);
+        load_face(a, 2, fidx(d, 2, i, j, k), A, nx, ny, nz);
         if (thin) {
 #pragma unroll
           for (int l = 0; l < NV; ++l) H[l] = T(0);
@@ -356,7 +392,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
           T R[NV];
 #pragma unroll
           for (int l = 0; l < NV; ++l) R[l] = (dF_prev[l] + dG_prev[l]) + (H[l] - H_prev[l]);
-          const T vol_c = (T)a.cells[4 * c0];
+          const T vol_c = cell_vol(a, T(0), c0);
           T dtc;
           if (a.compute_dt) {
             T s = lami_lo_prev + lamj_lo_prev + lamk_prev + lami_hi_prev + lamj_hi_prev + lamk;
@@ -368,7 +404,12 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
           if (a.res_out)
 #pragma unroll
             for (int l = 0; l < NV; ++l) a.res_out[ci + ncells(d) * l] = (double)R[l];
-          if (!update_cell(p, a, c0, ci, R, dtc, vol_c)) raise_error(a.err, FEST_ERR_NEGATIVE_STATE);
+          // the finished cell's own stencil values (plane k-1 of the ring)
+          T qo[4];
+          const T* own1 = ring + ((kc + 2) % NRING) * plane + r * SW + cc;
+#pragma unroll
+          for (int l = 0; l < 4; ++l) qo[l] = own1[l * SH * SW];
+          if (!update_cell(p, a, c0, ci, R, dtc, vol_c, qo)) raise_error(a.err, FEST_ERR_NEGATIVE_STATE);
         }
       }
 #pragma unroll
