@@ -18,8 +18,8 @@ using namespace stage;
 // BCs stop rewriting them (fix() after iteration 2).  Non-interior cells:
 // q = a*Us + b*X with Us the state before the iteration's BCs and X the last
 // stage's input (its ghosts as that stage's BCs left them).
-__global__ void k_ghost_blend(Dims d, double* q, float* q32, const double* Us, const double* X,
-                              double a, double b) {
+__global__ void k_ghost_blend(Dims d, double* q, float* q32, int pitch, const double* Us,
+                              const double* X, double a, double b) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= d.P * d.nv) return;
   long long c = t % d.P;
@@ -30,16 +30,17 @@ __global__ void k_ghost_blend(Dims d, double* q, float* q32, const double* Us, c
   if (interior) return;
   const double v = a * Us[t] + b * X[t];
   q[t] = v;
-  if (q32) q32[t] = (float)v;
+  if (q32) q32[mirror_index(d, pitch, c, (int)(t / d.P))] = (float)v;
 }
 
 // FP32 mirrors for the mixed sweep: state (whole padded array), face
 // records {A,nx,ny,nz} and cell volumes.  Rounding to nearest, as a
 // conversion on load would do.
-__global__ void k_to_f32(const double* src, float* dst, long long n) {
+__global__ void k_to_mirror(Dims d, int pitch, const double* src, float* dst) {
+  const long long n = d.P * d.nv;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x)
-    dst[t] = (float)src[t];
+    dst[mirror_index(d, pitch, t % d.P, (int)(t / d.P))] = (float)src[t];
 }
 __global__ void k_faces_to_f32(const double* faces, float4* dst, long long n) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
@@ -70,6 +71,10 @@ struct FusedState {
   float* V32 = nullptr;
   bool mirror_valid = false;  // Q32 interiors match Q
   int kc[2] = {0, 0};         // tuned k-chunk per precision (0: not tuned yet)
+  int mpitch = 0;             // row pitch of Q32
+  long long m_elems = 0;      // floats per Q32 buffer
+  CUtensorMap tm[3];          // TMA descriptors of Q32[0..2]
+  CUtensorMap tm_none{};      // placeholder for FP64 launches
   int* tune_err = nullptr;    // error word of the tuning launches
   std::vector<void*> allocs;
   bool profiling = false;
@@ -142,13 +147,46 @@ static void seed(FusedState* f, cudaStream_t s) {
 
 // allocate and fill the FP32 mirrors the mixed sweep reads (once per
 // handle for the metrics; the state mirror whenever it went stale)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// 4-D view (i, j, k, variable) of one FP32 state mirror; box = one stencil
+// plane of a tile (40 x 12 x 1 x 5).  Out-of-range elements read as zero.
+static int encode_mirror_map(CUtensorMap* tm, float* base, const Dims& d, int pitch) {
+  static EncodeTiledFn encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return FEST_ERR_CUDA;
+    encode = (EncodeTiledFn)fn;
+  }
+  const cuuint64_t dims[4] = {(cuuint64_t)d.ni, (cuuint64_t)d.nj, (cuuint64_t)d.nk, (cuuint64_t)d.nv};
+  const cuuint64_t strides[3] = {(cuuint64_t)pitch * 4, (cuuint64_t)pitch * d.nj * 4,
+                                 (cuuint64_t)pitch * d.nj * d.nk * 4};
+  const cuuint32_t box[4] = {(cuuint32_t)RingGeom<float>::W, (cuuint32_t)SH, 1, 5};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? FEST_OK : FEST_ERR_CUDA;
+}
+
 static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long long* cnt) {
   const Dims& d = f->d;
-  const long long n = d.P * d.nv;
   if (!f->V32) {  // V32 is allocated last: a partial earlier attempt retries
+    f->mpitch = (d.ni + 3) & ~3;
+    f->m_elems = (long long)f->mpitch * d.nj * d.nk * d.nv;
     for (int m = 0; m < 3; ++m) {
-      if (cudaMalloc((void**)&f->Q32[m], sizeof(float) * (size_t)n) != cudaSuccess) return FEST_ERR_NOMEM;
+      if (cudaMalloc((void**)&f->Q32[m], sizeof(float) * (size_t)f->m_elems) != cudaSuccess)
+        return FEST_ERR_NOMEM;
       f->allocs.push_back(f->Q32[m]);
+      int rc = encode_mirror_map(&f->tm[m], f->Q32[m], d, f->mpitch);
+      if (rc) return rc;
       const long long nf = nfaces(d, m);
       if (cudaMalloc((void**)&f->F32[m], sizeof(float4) * (size_t)nf) != cudaSuccess) return FEST_ERR_NOMEM;
       f->allocs.push_back(f->F32[m]);
@@ -165,7 +203,8 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
     // whole padded arrays, so that the edge and corner cells the halo lanes
     // read (results discarded) hold finite values
     for (int m = 0; m < 3; ++m) {
-      k_to_f32<<<grid_for(n), 256, 0, s>>>(f->Q[m], f->Q32[m], n);
+      // pitch padding columns are outside the tensor map: never read
+      k_to_mirror<<<grid_for(d.P * d.nv), 256, 0, s>>>(d, f->mpitch, f->Q[m], f->Q32[m]);
       ++*cnt;
     }
     f->mirror_valid = true;
@@ -173,13 +212,14 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
   return FEST_OK;
 }
 
-static void launch_sweep(const Params& p, int prec, dim3 grid, cudaStream_t s, const StageArgs& a) {
+static void launch_sweep(const Params& p, int prec, dim3 grid, cudaStream_t s, const StageArgs& a,
+                         const CUtensorMap& tm) {
   switch (p.interp) {
-    case FEST_INTERP_NONE: launch_stage_none(prec, p.flux, grid, s, p, a); break;
-    case FEST_INTERP_MUSCL: launch_stage_muscl(prec, p.flux, grid, s, p, a); break;
-    case FEST_INTERP_PPM: launch_stage_ppm(prec, p.flux, grid, s, p, a); break;
-    case FEST_INTERP_WENO: launch_stage_weno(prec, p.flux, grid, s, p, a); break;
-    default: launch_stage_weno_nm(prec, p.flux, grid, s, p, a); break;
+    case FEST_INTERP_NONE: launch_stage_none(prec, p.flux, grid, s, p, a, tm); break;
+    case FEST_INTERP_MUSCL: launch_stage_muscl(prec, p.flux, grid, s, p, a, tm); break;
+    case FEST_INTERP_PPM: launch_stage_ppm(prec, p.flux, grid, s, p, a, tm); break;
+    case FEST_INTERP_WENO: launch_stage_weno(prec, p.flux, grid, s, p, a, tm); break;
+    default: launch_stage_weno_nm(prec, p.flux, grid, s, p, a, tm); break;
   }
 }
 
@@ -188,8 +228,8 @@ static void launch_sweep(const Params& p, int prec, dim3 grid, cudaStream_t s, c
 // halo planes.  The trial launches write only the stage's output buffers
 // (rewritten by the real launch) and a private error word; the RK
 // accumulator is left alone.  Chunking does not change any result.
-static int tune_chunk(FusedState* f, const Params& p, int prec, StageArgs a, cudaStream_t s,
-                      long long* cnt) {
+static int tune_chunk(FusedState* f, const Params& p, int prec, StageArgs a, const CUtensorMap& tm,
+                      cudaStream_t s, long long* cnt) {
   const int nk = p.d.kmx - 1;
   const dim3 g0((p.d.imx - 1 + IX - 1) / IX, (p.d.jmx - 1 + IY - 1) / IY, 1);
   a.use_rn = 0; a.TU = 0; a.res_out = nullptr;
@@ -209,9 +249,9 @@ static int tune_chunk(FusedState* f, const Params& p, int prec, StageArgs a, cud
     a.k_chunk = (nk + chunks - 1) / chunks;
     dim3 g = g0;
     g.z = chunks;
-    launch_sweep(p, prec, g, s, a);  // warm-up
+    launch_sweep(p, prec, g, s, a, tm);  // warm-up
     cudaEventRecord(e0, s);
-    for (int r = 0; r < 3; ++r) launch_sweep(p, prec, g, s, a);
+    for (int r = 0; r < 3; ++r) launch_sweep(p, prec, g, s, a, tm);
     cudaEventRecord(e1, s);
     *cnt += 4;
     float ms = 0.f;
@@ -233,6 +273,7 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   DevBlock bb = b;
   bb.qp = f->Q[in];
   bb.qp32 = mixed ? f->Q32[in] : nullptr;
+  bb.qp32_pitch = f->mpitch;
   Launcher L{s, cnt};
   // edge/corner ghosts are never read by an interior update: no averaging
   launch_ghosts(p, bb, f->table[in], iter, L, false);
@@ -254,9 +295,11 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   a.qout32 = mixed ? f->Q32[out] : nullptr;
   for (int dir = 0; dir < 3; ++dir) a.faces32[dir] = mixed ? f->F32[dir] : nullptr;
   a.vol32 = mixed ? f->V32 : nullptr;
+  a.mpitch = f->mpitch;
+  const CUtensorMap& tm = mixed ? f->tm[in] : f->tm_none;
   const int nk = p.d.kmx - 1;
   int& kc = f->kc[mixed ? 1 : 0];
-  if (kc == 0) kc = tune_chunk(f, p, prec, a, s, cnt);
+  if (kc == 0) kc = tune_chunk(f, p, prec, a, tm, s, cnt);
   a.k_chunk = kc;
   const int chunks = (nk + kc - 1) / kc;
   dim3 grid((p.d.imx - 1 + IX - 1) / IX, (p.d.jmx - 1 + IY - 1) / IY, chunks);
@@ -269,7 +312,7 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
       }
     cudaEventRecord(f->ev[f->nev], s);
   }
-  launch_sweep(p, prec, grid, s, a);
+  launch_sweep(p, prec, grid, s, a, tm);
   if (f->profiling) {
     cudaEventRecord(f->ev[f->nev + 1], s);
     f->nev += 2;
@@ -301,6 +344,7 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
         DevBlock bb = b;
         bb.qp = f->Q[n];
         bb.qp32 = mixed ? f->Q32[n] : nullptr;
+        bb.qp32_pitch = f->mpitch;
         launch_ghosts(p, bb, f->table[n], it, Launcher{s, cnt}, false);
       }
     }
@@ -318,7 +362,7 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
         if (tvd_early) {
           long long n = p.d.P * p.d.nv;
           k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
-                                                                   f->Us, f->Q[A], 0.5, 0.5);
+                                                                   f->mpitch, f->Us, f->Q[A], 0.5, 0.5);
           ++*cnt;
         }
         break;
@@ -329,7 +373,7 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
         if (tvd_early) {
           long long n = p.d.P * p.d.nv;
           k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
-                                                                   f->Us, f->Q[B], 1. / 3., 2. / 3.);
+                                                                   f->mpitch, f->Us, f->Q[B], 1. / 3., 2. / 3.);
           ++*cnt;
         }
         break;
@@ -354,7 +398,8 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
         if (n != f->cur) {
           cudaMemcpyAsync(f->Q[n], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
           if (mixed)
-            cudaMemcpyAsync(f->Q32[n], f->Q32[f->cur], bytes / 2, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(f->Q32[n], f->Q32[f->cur], sizeof(float) * (size_t)f->m_elems,
+                            cudaMemcpyDeviceToDevice, s);
         }
   }
   return FEST_OK;

@@ -299,8 +299,8 @@ __global__ void k_ghosts(Params p, DevBlock b, const BlockRef* blocks, int iter,
   if (b.qp32 && interior && id != -9)
     for (int l = 0; l < d.nv; ++l)
       for (int L = 1; L <= 3; ++L) {
-        const long long g = ghost_p(d, f, L, ta, tb) + d.P * l;
-        b.qp32[g] = (float)b.qp[g];
+        const long long g = ghost_p(d, f, L, ta, tb);
+        b.qp32[mirror_index(d, b.qp32_pitch, g, l)] = (float)b.qp[g + d.P * l];
       }
 }
 

@@ -15,7 +15,16 @@ struct DevBlock {
   double *red;              // reduction scratch (kRedSlots doubles)
   int *err;                 // device error word
   float *qp32;              // FP32 mirror of qp kept by the mixed fused path (else null)
+  int qp32_pitch;           // its row pitch (imx+5 rounded up to a multiple of 4)
 };
+
+// index in the FP32 state mirror of padded cell c (a pidx) of variable l:
+// the mirror has the padded layout of qp with rows padded to `pitch` so
+// that TMA tiles can address it (row strides a multiple of 16 bytes)
+__host__ __device__ __forceinline__ long long mirror_index(const Dims& d, int pitch, long long c, int l) {
+  const int ci = (int)c;  // P * n_var < 2^31 on the fused path
+  return (long long)(ci % d.ni) + (long long)pitch * (ci / d.ni + (long long)d.nj * d.nk * l);
+}
 constexpr int kRedSlots = 1 << 16;
 
 // a block as seen by the interface exchange of another block

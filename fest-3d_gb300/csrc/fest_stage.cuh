@@ -11,17 +11,22 @@
 // Tile: a CTA of 32x8 threads covers 30 interior cells in i (lanes 1..30,
 // lanes 0/31 are the i-halo) by 6 in j (warps 1..6, warps 0/7 the j-halo)
 // and marches along k over a chunk of interior planes (several chunks per
-// column when the block is small, so every SM gets work).  A 5-plane ring
-// in shared memory holds the stencil (planes k-2..k+2, 36x12 cells each,
-// converted to the arithmetic type on load).  i-face fluxes travel by warp
-// shuffles, j-face fluxes through shared memory, k-face fluxes stay in
-// registers across the march.
+// column when the block is small, so every SM gets work).  A ring of
+// stencil planes in shared memory holds planes k-2..k+2 (12 rows x 36
+// columns x 5 variables each).  In FP32 the planes arrive by TMA
+// (cp.async.bulk.tensor from the FP32 state mirror, one 4-D box per plane,
+// completion on an mbarrier per ring slot, one plane prefetched ahead of
+// the march); in FP64 the threads load and store them.  i-face fluxes travel
+// by warp shuffles, j-face fluxes through shared memory, k-face fluxes stay
+// in registers across the march.
 //
 // T = float  (FEST_MIXED): reconstruction, flux, residual and the update's
 //             increments in FP32; the state stays FP64 and is advanced by
 //             adding an FP64 increment (delta form); metrics are read FP64.
 // T = double (FEST_FP64): the reference's arithmetic, update_with verbatim.
 #pragma once
+#include <cuda.h>  // CUtensorMap
+
 #include "fest_common.cuh"
 
 namespace fest {
@@ -49,6 +54,7 @@ struct StageArgs {
   float* qout32;        // mirror of qout (interior written)
   const float4* faces32[3];  // {A,nx,ny,nz} per face
   const float* vol32;   // cell volumes (padded)
+  int mpitch;           // row pitch of the state mirror (imx+5 rounded up to 4)
 };
 
 namespace stage {
@@ -56,7 +62,13 @@ namespace stage {
 constexpr int TX = 32, TY = 8;        // threads per CTA
 constexpr int IX = TX - 2, IY = TY - 2;  // interior cells per CTA
 constexpr int SW = TX + 4, SH = TY + 4;  // stencil plane extents (halo 2)
-constexpr int NRING = 5;
+// ring geometry per arithmetic type: FP32 rows are 40 wide so that the TMA
+// box can start on a 16-byte boundary (the tile origin 30*bx is 2 mod 4 for
+// odd bx; the box starts 0 or 2 columns early), 6 slots for one plane of
+// prefetch; FP64 keeps 36-wide rows and 5 slots
+template <typename T> struct RingGeom;
+template <> struct RingGeom<float> { static constexpr int W = 40, N = 6; };
+template <> struct RingGeom<double> { static constexpr int W = 36, N = 5; };
 
 
 
@@ -66,10 +78,55 @@ template <typename T> struct SmemLine {
   __device__ __forceinline__ T operator()(int c) const { return p[(c - c0) * stride]; }
 };
 template <typename T> struct RingLine {
-  const T* ring;  // ring + var/row/col offset; plane c lives in slot (c+2)%5
-  int plane_stride;
-  __device__ __forceinline__ T operator()(int c) const { return ring[((c + 2) % NRING) * plane_stride]; }
+  const T* ring;  // ring + var/row/col offset; plane c lives in slot (c-base)%N
+  int plane_stride, base;
+  __device__ __forceinline__ T operator()(int c) const {
+    return ring[((c - base) % RingGeom<T>::N) * plane_stride];
+  }
 };
+
+// ---- TMA and mbarrier (PTX) -------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// one 4-D tile (x, y, z, w) of the tensor map into shared memory; the
+// mbarrier expects its bytes
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* tm, int x, int y, int z,
+                                            int w, uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+      : "memory");
+}
+// wait for phase `parity` of the barrier, giving up after ~2^31 cycles
+// (about a second): returns false then
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > (1ll << 31)) return false;
+  }
+}
 struct VolLine {
   const double* p;  // cells + 4*pidx(cell at normal coordinate 0)
   long long stride;
@@ -130,7 +187,7 @@ __device__ __forceinline__ T lambda_face(T gm, const T* L, const T* R, T A, T nx
 // FP64: update_with(...,'conservative',...) (update.f90:367-485) verbatim.
 __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
                                             long long ci, const double* R_in, double dtc,
-                                            double vol, const double*) {
+                                            double vol, const double*, long long) {
   const long long P = p.d.P, N = ncells(p.d);
   const double gm = p.gm;
   double R[5], u1[5], u2[5];
@@ -174,7 +231,7 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
 // linearisation) in FP32 and added to the FP64 state.
 __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
                                             long long ci, const float* R_in, float dtc, float vol,
-                                            const float* qc) {
+                                            const float* qc, long long m0) {
   const long long P = p.d.P, N = ncells(p.d);
   const float gm1 = (float)(p.gm - 1.0);
   float R[5];
@@ -191,6 +248,7 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
   double b64[5];
 #pragma unroll
   for (int l = 0; l < 5; ++l) b64[l] = a.qbase[c0 + P * l];
+  const long long mvar = (long long)a.mpitch * p.d.nj * p.d.nk;  // mirror variable stride
   // FP32 copies of the base state: the stencil's own cell when the update
   // starts from the stencil state (bit-identical to converting b64)
   const bool own = a.qbase == a.qin;
@@ -215,19 +273,24 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
     double val = out[l];
     if (a.bA != 0.0) val = a.bA * a.qU[c0 + P * l] + a.bB * val;
     a.qout[c0 + P * l] = val;
-    a.qout32[c0 + P * l] = (float)val;
+    a.qout32[m0 + mvar * l] = (float)val;
   }
   return true;
 }
 
 template <typename T, int INTERP, int FLUX>
-__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params p, StageArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
+    k_stage(Params p, StageArgs a, const __grid_constant__ CUtensorMap tm) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
   constexpr int NV = 5;
-  T* ring = reinterpret_cast<T*>(smem_raw);               // [NRING][NV][SH][SW]
-  T* xch = ring + NRING * NV * SH * SW;                   // [NV][TY][TX] j-face left states
+  constexpr int RW = RingGeom<T>::W, NR = RingGeom<T>::N;
+  constexpr bool kTma = sizeof(T) == 4;
+  T* ring = reinterpret_cast<T*>(smem_raw);               // [NR][NV][SH][RW]
+  T* xch = ring + NR * NV * SH * RW;                      // [NV][TY][TX] j-face left states
   T* gfl = xch + NV * TY * TX;                            // [NV][TY][TX] j-face fluxes
   T* lam = gfl + NV * TY * TX;                            // [TY][TX]    j-face dt terms
+  uint64_t* bars = reinterpret_cast<uint64_t*>(lam + TY * TX);  // [NR] ring-slot barriers
+  __shared__ int abort_flag;
   const Dims& d = p.d;
   const int lane = threadIdx.x, w = threadIdx.y, tid = w * TX + lane;
   const int ib = 1 + IX * blockIdx.x, jb = 1 + IY * blockIdx.y;
@@ -235,28 +298,38 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
   const int i0 = ib - 3, j0 = jb - 3;  // stencil plane origin (col 0, row 0)
   const bool in_i = lane >= 1 && lane <= IX && i <= d.imx - 1;
   const bool in_j = w >= 1 && w <= IY && j <= d.jmx - 1;
-  const int plane = NV * SH * SW;
+  const int plane = NV * SH * RW;
   const T gm = (T)p.gm;
+  // FP32: the TMA box starts ox columns left of the tile's stencil origin
+  const int ox = kTma ? ((IX * (int)blockIdx.x) & 3) : 0;
   const bool thin = d.kmx == 2;
 
   // clamp to the padded block so halo lanes past the edge stay finite
   auto clampi = [&](int x, int hi) { return x < -2 ? -2 : (x > hi + 2 ? hi + 2 : x); };
 
-  // per-thread load offsets of the stencil plane (plane k adds (k+2)*ni*nj)
-  constexpr int NLOAD = (NV * SH * SW + TX * TY - 1) / (TX * TY);
+  const int k0 = 1 + a.k_chunk * blockIdx.z;
+  const int k1 = min(k0 + a.k_chunk - 1, d.kmx - 1);
+  const int base = k0 - 3;                 // first plane of the chunk's march
+  const int nplanes = (k1 + 3) - base + 1;
+  auto slot = [&](int c) { return (c - base) % NR; };
+
+  // FP64: per-thread load offsets of the stencil plane (plane k adds (k+2)*ni*nj)
+  constexpr int NLOAD = kTma ? 1 : (NV * SH * SW + TX * TY - 1) / (TX * TY);
   int off[NLOAD];
+  if constexpr (!kTma) {
 #pragma unroll
-  for (int m = 0; m < NLOAD; ++m) {
-    int e = tid + m * TX * TY;
-    if (e >= NV * SH * SW) e = NV * SH * SW - 1;
-    int l = e / (SH * SW), rem = e - l * (SH * SW), r = rem / SW, c = rem - r * SW;
-    int gi = clampi(i0 + c, d.imx), gj = clampi(j0 + r, d.jmx);
-    off[m] = (int)(pidx(d, gi, gj, -2) + d.P * l);
+    for (int m = 0; m < NLOAD; ++m) {
+      int e = tid + m * TX * TY;
+      if (e >= NV * SH * SW) e = NV * SH * SW - 1;
+      int l = e / (SH * SW), rem = e - l * (SH * SW), r = rem / SW, c = rem - r * SW;
+      int gi = clampi(i0 + c, d.imx), gj = clampi(j0 + r, d.jmx);
+      off[m] = (int)(pidx(d, gi, gj, -2) + d.P * l);
+    }
   }
   const int plane_stride = d.ni * d.nj;
   const T* qsrc = stencil_src(a, T(0));
-  auto load_plane = [&](int k) {
-    T* dst = ring + ((k + 2) % NRING) * plane;
+  auto load_plane = [&](int k) {  // FP64 path
+    T* dst = ring + slot(k) * plane;
     const T* src = qsrc + (long long)(k + 2) * plane_stride;
 #pragma unroll
     for (int m = 0; m < NLOAD; ++m) {
@@ -264,8 +337,25 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
       if (e < NV * SH * SW) dst[e] = __ldg(src + off[m]);
     }
   };
-  const int k0 = 1 + a.k_chunk * blockIdx.z;
-  const int k1 = min(k0 + a.k_chunk - 1, d.kmx - 1);
+  // FP32 path: plane c of the mirror -> ring slot, box (40 x 12 x 1 x 5)
+  // at array coordinates (30*bx - ox, 6*by, c+2, 0); columns or rows past
+  // the array are zero-filled and feed only discarded halo lanes
+  constexpr uint32_t kPlaneBytes = (uint32_t)(NV * SH * RW * sizeof(T));
+  auto issue = [&](int c) {
+    fence_proxy_async();  // earlier generic reads of the slot come first
+    tma_load_4d(ring + slot(c) * plane, &tm, IX * (int)blockIdx.x - ox, IY * (int)blockIdx.y, c + 2, 0,
+                bars + slot(c), kPlaneBytes);
+  };
+  if constexpr (kTma) {
+    if (tid == 0) {
+      abort_flag = 0;
+      for (int n = 0; n < NR; ++n) mbar_init(bars + n, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (int n = 0; n < NR && n < nplanes; ++n) issue(base + n);
+  }
 
   // per-thread march state for cell (i, j, k-1)
   T Lp_prev[NV], H_prev[NV], dF_prev[NV], dG_prev[NV];
@@ -274,10 +364,21 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
   for (int l = 0; l < NV; ++l) { Lp_prev[l] = 0; H_prev[l] = 0; dF_prev[l] = 0; dG_prev[l] = 0; }
 
   const long long sj = d.ni, sk = (long long)d.ni * d.nj;
-  for (int kl = k0 - 3; kl <= k1 + 3; ++kl) {
+  for (int n = 0; n < nplanes; ++n) {
+    const int kl = base + n;  // plane arriving now
     __syncthreads();
-    load_plane(kl);
-    __syncthreads();
+    if constexpr (kTma) {
+      if (abort_flag) return;  // uniform: read after the barrier
+      // the slot of plane n+1 last held plane n+1-NR, read up to iteration n-1
+      if (tid == 0 && n + 1 >= NR && n + 1 < nplanes) issue(kl + 1);
+      if (!mbar_wait(bars + slot(kl), (uint32_t)((n / NR) & 1))) {
+        raise_error(a.err, FEST_ERR_TIMEOUT);
+        abort_flag = 1;
+      }
+    } else {
+      load_plane(kl);
+      __syncthreads();
+    }
     const int k = kl - 2;  // plane processed now
     if (k < k0 - 1) continue;
     const bool kin = k >= k0 && k <= k1;
@@ -286,20 +387,20 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
     for (int l = 0; l < NV; ++l) { dF[l] = T(0); dG[l] = T(0); }
     T lami_lo = 0, lami_hi = 0, lamj_lo = 0, lamj_hi = 0;
     const int r = w + 2;               // own row in the stencil plane
-    const int cc = lane + 2;           // own column
-    const T* own = ring + ((k + 2) % NRING) * plane + r * SW + cc;  // var 0 of own cell
+    const int cc = lane + 2 + ox;      // own column
+    const T* own = ring + slot(k) * plane + r * RW + cc;  // var 0 of own cell
     T qc[NV];
 #pragma unroll
-    for (int l = 0; l < NV; ++l) qc[l] = own[l * SH * SW];
+    for (int l = 0; l < NV; ++l) qc[l] = own[l * SH * RW];
     // ---------------- i-faces (warp shuffles) ----------------
     if (kin && in_j) {  // warp-uniform
       T Rm[NV], Lp[NV];
-      const T* rowp = ring + ((k + 2) % NRING) * plane + r * SW;
+      const T* rowp = ring + slot(k) * plane + r * RW;
       const auto vol = vol_line(a, T(0), pidx(d, 0, clampi(j, d.jmx), k), 1, d.imx);
-      SmemLine<T> pres{rowp + 4 * SH * SW + cc, i, 1};
+      SmemLine<T> pres{rowp + 4 * SH * RW + cc, i, 1};
 #pragma unroll
       for (int l = 0; l < NV; ++l) {
-        SmemLine<T> q{rowp + l * SH * SW + cc, i, 1};
+        SmemLine<T> q{rowp + l * SH * RW + cc, i, 1};
         recon_cell<T, INTERP>(p, 0, i, l + 1, q, pres, vol, Rm[l], Lp[l]);
       }
       T L[NV], F[NV];
@@ -321,12 +422,12 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
     // ---------------- j-faces (shared memory) ----------------
     if (kin) {
       T Rm[NV], Lp[NV];
-      const T* colp = ring + ((k + 2) % NRING) * plane + cc;
+      const T* colp = ring + slot(k) * plane + cc;
       const auto vol = vol_line(a, T(0), pidx(d, clampi(i, d.imx), 0, k), sj, d.jmx);
-      SmemLine<T> pres{colp + 4 * SH * SW + r * SW, j, SW};
+      SmemLine<T> pres{colp + 4 * SH * RW + r * RW, j, RW};
 #pragma unroll
       for (int l = 0; l < NV; ++l) {
-        SmemLine<T> q{colp + l * SH * SW + r * SW, j, SW};
+        SmemLine<T> q{colp + l * SH * RW + r * RW, j, RW};
         recon_cell<T, INTERP>(p, 1, j, l + 1, q, pres, vol, Rm[l], Lp[l]);
       }
 #pragma unroll
@@ -364,12 +465,12 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
     // ---------------- k-faces (registers, marching) ----------------
     if (in_i && in_j) {
       T Rm[NV], Lp[NV];
-      const T* cp = ring + r * SW + cc;
+      const T* cp = ring + r * RW + cc;
       const auto vol = vol_line(a, T(0), pidx(d, i, j, 0), sk, d.kmx);
-      RingLine<T> pres{cp + 4 * SH * SW, plane};
+      RingLine<T> pres{cp + 4 * SH * RW, plane, base};
 #pragma unroll
       for (int l = 0; l < NV; ++l) {
-        RingLine<T> q{cp + l * SH * SW, plane};
+        RingLine<T> q{cp + l * SH * RW, plane, base};
         recon_cell<T, INTERP>(p, 2, k, l + 1, q, pres, vol, Rm[l], Lp[l]);
       }
       T H[NV];
@@ -406,10 +507,12 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
             for (int l = 0; l < NV; ++l) a.res_out[ci + ncells(d) * l] = (double)R[l];
           // the finished cell's own stencil values (plane k-1 of the ring)
           T qo[4];
-          const T* own1 = ring + ((kc + 2) % NRING) * plane + r * SW + cc;
+          const T* own1 = ring + slot(kc) * plane + r * RW + cc;
 #pragma unroll
-          for (int l = 0; l < 4; ++l) qo[l] = own1[l * SH * SW];
-          if (!update_cell(p, a, c0, ci, R, dtc, vol_c, qo)) raise_error(a.err, FEST_ERR_NEGATIVE_STATE);
+          for (int l = 0; l < 4; ++l) qo[l] = own1[l * SH * RW];
+          const long long m0 = (long long)(i + 2) + (long long)a.mpitch * ((j + 2) + (long long)d.nj * (kc + 2));
+          if (!update_cell(p, a, c0, ci, R, dtc, vol_c, qo, m0))
+            raise_error(a.err, FEST_ERR_NEGATIVE_STATE);
         }
       }
 #pragma unroll
@@ -428,15 +531,17 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1) k_stage(Params
 }
 
 template <typename T> inline size_t stage_smem() {
-  return sizeof(T) * ((size_t)NRING * 5 * SH * SW + 2 * 5 * TY * TX + TY * TX);
+  return sizeof(T) * ((size_t)RingGeom<T>::N * 5 * SH * RingGeom<T>::W + 2 * 5 * TY * TX + TY * TX) +
+         sizeof(uint64_t) * RingGeom<T>::N + 16;
 }
 
 
 }  // namespace stage
 
 // one host launcher per reconstruction (fest_stage_<method>.cu)
-#define FEST_STAGE_LAUNCHER(name) \
-  int name(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a)
+#define FEST_STAGE_LAUNCHER(name)                                                         \
+  int name(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a, \
+           const CUtensorMap& tm)
 FEST_STAGE_LAUNCHER(launch_stage_none);
 FEST_STAGE_LAUNCHER(launch_stage_muscl);
 FEST_STAGE_LAUNCHER(launch_stage_ppm);
@@ -444,7 +549,8 @@ FEST_STAGE_LAUNCHER(launch_stage_weno);
 FEST_STAGE_LAUNCHER(launch_stage_weno_nm);
 
 template <int INTERP>
-int launch_stage_t(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a) {
+int launch_stage_t(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a,
+                   const CUtensorMap& tm) {
   using namespace stage;
   const dim3 blk(TX, TY);
   static bool attrs = false;
@@ -459,7 +565,7 @@ int launch_stage_t(int prec, int flux, dim3 grid, cudaStream_t s, const Params& 
     attrs = true;
   }
 #undef FEST_SET
-#define FEST_GO(T, F) k_stage<T, INTERP, F><<<grid, blk, stage_smem<T>(), s>>>(p, a)
+#define FEST_GO(T, F) k_stage<T, INTERP, F><<<grid, blk, stage_smem<T>(), s>>>(p, a, tm)
   if (prec == FEST_MIXED) {
     switch (flux) {
       case 0: FEST_GO(float, 0); break;

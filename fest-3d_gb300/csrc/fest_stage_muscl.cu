@@ -3,5 +3,5 @@
 #include "fest_stage.cuh"
 
 namespace fest {
-FEST_STAGE_LAUNCHER(launch_stage_muscl) { return launch_stage_t<FEST_INTERP_MUSCL>(prec, flux, grid, s, p, a); }
+FEST_STAGE_LAUNCHER(launch_stage_muscl) { return launch_stage_t<FEST_INTERP_MUSCL>(prec, flux, grid, s, p, a, tm); }
 }  // namespace fest
