@@ -249,6 +249,12 @@ def run_ours(args):
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
+    # a dedicated stream, current for everything below: the events, the L2
+    # flush and the library's work (fest_set_stream) share it.  (torch's
+    # default stream is handle 0, which fest_set_stream reads as "the
+    # handle's own stream".)
+    work_stream = torch.cuda.Stream()
+    torch.cuda.set_stream(work_stream)
     dist = None
     if ws > 1:
         import torch.distributed as dist
@@ -263,6 +269,7 @@ def run_ours(args):
     N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
     STAGES = 3
     stream = torch.cuda.current_stream()
+    assert stream.cuda_stream != 0
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def barrier():

@@ -54,6 +54,172 @@ __global__ void k_vol_to_f32(const double* cells, float* dst, long long n) {
        t += (long long)gridDim.x * blockDim.x)
     dst[t] = (float)cells[4 * t];
 }
+// ---- ghost cells on the FP32 mirror (mixed sweep, iterations > 2) ----------
+// The same face procedures as the FP64 ghost fill (bc_primitive.f90:160-206,
+// copy_bc.f90:129-202, FT_bc.f90:15-107, bc_primitive.f90:1237-1776,
+// interface1.f90:496-700), evaluated in FP32 on the mirror that the mixed
+// sweep reads.  After iteration 2 no fix() BC writes anything
+// (bc_primitive.f90:236,318,366), so only the copy, wall, tangency, Riemann
+// and interface procedures remain.  One thread per interior column of a
+// face; on the fused path every one of them reads interior cells only
+// (blocks have >= 4 interior cells per direction, no -9 faces) and writes
+// its own ghost cells, so the faces run concurrently.
+struct Mirror {
+  float* q;
+  int rp, nj, nk;
+  long long vs;
+  __device__ __forceinline__ float& at(int i, int j, int k, int l) const {
+    return q[(i + 2) + (long long)rp * ((j + 2) + (long long)nj * (k + 2)) + vs * l];
+  }
+};
+struct GhostPlan {
+  int nf;
+  int face[6];
+  int na[6];
+  long long start[7];
+};
+// ghost (layer L) and interior (layer m) cell of face f at (ta, tb)
+__device__ __forceinline__ void gcell(const Dims& d, int f, int L, int ta, int tb, int& i, int& j, int& k) {
+  switch (f) {
+    case 0: i = 1 - L; j = ta; k = tb; break;
+    case 1: i = d.imx + L - 1; j = ta; k = tb; break;
+    case 2: i = ta; j = 1 - L; k = tb; break;
+    case 3: i = ta; j = d.jmx + L - 1; k = tb; break;
+    case 4: i = ta; j = tb; k = 1 - L; break;
+    default: i = ta; j = tb; k = d.kmx + L - 1;
+  }
+}
+__device__ __forceinline__ void icell(const Dims& d, int f, int m, int ta, int tb, int& i, int& j, int& k) {
+  switch (f) {
+    case 0: i = m; j = ta; k = tb; break;
+    case 1: i = d.imx - m; j = ta; k = tb; break;
+    case 2: i = ta; j = m; k = tb; break;
+    case 3: i = ta; j = d.jmx - m; k = tb; break;
+    case 4: i = ta; j = tb; k = m; break;
+    default: i = ta; j = tb; k = d.kmx - m;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_ghosts_mirror(Params p, Mirror M, GhostPlan plan,
+                                                       const float4* F0, const float4* F1,
+                                                       const float4* F2) {
+  const Dims& d = p.d;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= plan.start[plan.nf]) return;
+  int n = 0;
+  while (t >= plan.start[n + 1]) ++n;
+  const int f = plan.face[n];
+  const long long u = t - plan.start[n];
+  const int ta = 1 + (int)(u % plan.na[n]), tb = 1 + (int)(u / plan.na[n]);
+  const int id = p.id[f];
+  auto G = [&](int L, int l) -> float& { int i, j, k; gcell(d, f, L, ta, tb, i, j, k); return M.at(i, j, k, l); };
+  auto I = [&](int m, int l) -> float { int i, j, k; icell(d, f, m, ta, tb, i, j, k); return M.at(i, j, k, l); };
+  const float c1 = (float)p.c1, c2 = (float)p.c2, c3 = (float)p.c3;
+  auto flat = [&](int l) { const float v = I(1, l); for (int L = 1; L <= 3; ++L) G(L, l) = v; };
+  auto symm = [&](int l) { for (int L = 1; L <= 3; ++L) G(L, l) = (c2 * I(L, l) - c3 * I(L + 1, l)) / c1; };
+  auto anti = [&](int l) { for (int L = 1; L <= 3; ++L) G(L, l) = -I(L, l); };
+  const float gm = (float)p.gm, R = (float)p.R;
+  // boundary face record of this column
+  int fi, fj, fk;
+  {
+    const int c = (f % 2 == 0) ? 1 : extent_of(d, f / 2);
+    if (f / 2 == 0) { fi = c; fj = ta; fk = tb; }
+    else if (f / 2 == 1) { fi = ta; fj = c; fk = tb; }
+    else { fi = ta; fj = tb; fk = c; }
+  }
+  const float4* Fd = f / 2 == 0 ? F0 : (f / 2 == 1 ? F1 : F2);
+  switch (id) {
+    case -1: break;  // supersonic inlet: fix() only
+    case -2:
+    case -7:
+      for (int l = 0; l < d.nv; ++l) flat(l);
+      break;
+    case -3: flat(4); break;      // subsonic inlet: pressure copied (fix() for the rest)
+    case -4:                      // subsonic outlet: rho,u,v,w copied (fix() for p)
+      for (int l = 0; l < 4; ++l) flat(l);
+      break;
+    case -5: {  // wall (bc_primitive.f90:392-402)
+      symm(4);
+      const float Tw = (float)p.Tw[f];
+      if (Tw < 0.f) {  // temp_based_density (bc_primitive.f90:1778-1945)
+        const float pp = I(1, 4), rho = I(1, 0);
+        const float stag = (pp / (R * rho)) * (1.f + (0.5f * (gm - 1.f) * gm * pp / rho));
+        for (int L = 1; L <= 3; ++L) G(L, 0) = G(L, 4) / (R * stag);
+      } else if (Tw > 1.f) {
+        for (int L = 1; L <= 3; ++L) {
+          const float Ti = I(L, 4) / (R * I(L, 0));
+          G(L, 0) = G(L, 4) / (R * (2.f * Tw - Ti));
+        }
+      } else {
+        symm(0);
+      }
+      anti(1); anti(2); anti(3);
+    } break;
+    case -6: {  // slip wall + flow tangency with I-face normals (FT_bc.f90:67-69)
+      symm(0); symm(4);
+      const float4 fn = __ldg(Fd + fidx(d, f / 2, fi, fj, fk));
+      const float4 fr = __ldg(F0 + fidx(d, 0, fi, fj, fk));
+      for (int L = 1; L <= 3; ++L) {
+        const float uu = I(L, 1), vv = I(L, 2), ww = I(L, 3);
+        const float dot = uu * fn.y + vv * fn.z + ww * fn.w;
+        G(L, 1) = uu - (2.f * dot * fr.y);
+        G(L, 2) = vv - (2.f * dot * fr.z);
+        G(L, 3) = ww - (2.f * dot * fr.w);
+      }
+    } break;
+    case -8:
+    case -11: {  // Riemann invariants on layer 1, copied to layers 2-3
+      const bool tp = id == -11;
+      const float4 fc = __ldg(Fd + fidx(d, f / 2, fi, fj, fk));
+      const float sg = (f % 2 == 0) ? -1.f : 1.f;
+      const float nx = sg * fc.y, ny = sg * fc.z, nz = sg * fc.w;
+      const float uu = I(1, 1), vv = I(1, 2), ww = I(1, 3), pI = I(1, 4), rI = I(1, 0);
+      const float uinf = (float)p.u_inf, vinf = (float)p.v_inf, winf = (float)p.w_inf;
+      const float pinf = (float)p.p_inf, rinf = (float)p.rho_inf;
+      const float cexp = sqrtf(gm * pI / rI), cinf = sqrtf(gm * pinf / rinf);
+      const float Unexp = uu * nx + vv * ny + ww * nz, Uninf = uinf * nx + vinf * ny + winf * nz;
+      const float Rinf = Uninf - 2.f * cinf / (gm - 1.f), Rexp = Unexp + 2.f * cexp / (gm - 1.f);
+      const float Unb = 0.5f * (Rexp + Rinf), Cb = 0.25f * (gm - 1.f) * (Rexp - Rinf);
+      float ug, vg, wg, rg = 0.f, pg = 0.f;
+      if (Unb > 0.f) {
+        const float vd = Unb - Unexp;
+        ug = uu + vd * nx; vg = vv + vd * ny; wg = ww + vd * nz;
+        if (!tp) {
+          const float sv = pI / powf(rI, gm);
+          rg = powf(Cb * Cb / (gm * sv), 1.f / (gm - 1.f));
+          pg = rg * Cb * Cb / gm;
+        }
+      } else {
+        const float vd = Unb - Uninf;
+        ug = uinf + vd * nx; vg = vinf + vd * ny; wg = winf + vd * nz;
+        if (!tp) {
+          const float sv = pinf / powf(rinf, gm);
+          rg = powf(Cb * Cb / (gm * sv), 1.f / (gm - 1.f));
+          pg = rg * Cb * Cb / gm;
+        }
+      }
+      if (tp) {
+        const float Mb = sqrtf(ug * ug + vg * vg + wg * wg) / Cb;
+        pg = (float)p.Tp[f] / powf((1.f + 0.5f * (gm - 1.f) * Mb * Mb), gm / (gm - 1.f));
+        rg = gm * pg / (Cb * Cb);
+      }
+      for (int L = 1; L <= 3; ++L) {
+        G(L, 0) = rg; G(L, 1) = ug; G(L, 2) = vg; G(L, 3) = wg; G(L, 4) = pg;
+      }
+    } break;
+    default:
+      if (id == -10 || id >= 0) {  // interface of a single block: ghost L <- partner layer L
+        const int pf = p.part_face[f];
+        for (int l = 0; l < d.nv; ++l)
+          for (int L = 1; L <= 3; ++L) {
+            int i, j, k;
+            icell(d, pf, L, ta, tb, i, j, k);
+            G(L, l) = M.at(i, j, k, l);
+          }
+      }
+  }
+}
+
 unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
@@ -275,8 +441,30 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   bb.qp32 = mixed ? f->Q32[in] : nullptr;
   bb.qp32_pitch = f->mpitch;
   Launcher L{s, cnt};
-  // edge/corner ghosts are never read by an interior update: no averaging
-  launch_ghosts(p, bb, f->table[in], iter, L, false);
+  if (mixed && iter > 2) {
+    // FP32 ghost fill of the stencil mirror (the FP64 ghosts of Q[in] are
+    // read by nothing on this path after iteration 2)
+    GhostPlan plan{};
+    for (int fc = 0; fc < 6; ++fc) {
+      if (p.id[fc] == -1) continue;  // fix() only
+      const int dir = fc / 2;
+      const int na = (dir == 0 ? p.d.jmx : p.d.imx) - 1, nb = (dir == 2 ? p.d.jmx : p.d.kmx) - 1;
+      plan.face[plan.nf] = fc;
+      plan.na[plan.nf] = na;
+      plan.start[plan.nf + 1] = plan.start[plan.nf] + (long long)na * nb;
+      ++plan.nf;
+    }
+    const long long work = plan.start[plan.nf];
+    if (work > 0) {
+      Mirror M{f->Q32[in], f->mpitch, p.d.nj, p.d.nk, (long long)f->mpitch * p.d.nj * p.d.nk};
+      k_ghosts_mirror<<<(unsigned)((work + 127) / 128), 128, 0, s>>>(p, M, plan, f->F32[0], f->F32[1],
+                                                                       f->F32[2]);
+      ++*cnt;
+    }
+  } else {
+    // edge/corner ghosts are never read by an interior update: no averaging
+    launch_ghosts(p, bb, f->table[in], iter, L, false);
+  }
   StageArgs a;
   a.qin = f->Q[in];
   a.qout = f->Q[out];
