@@ -241,6 +241,17 @@ struct FusedState {
   long long m_elems = 0;      // floats per Q32 buffer
   CUtensorMap tm[3];          // TMA descriptors of Q32[0..2]
   CUtensorMap tm_none{};      // placeholder for FP64 launches
+  // captured iterations (see graph_for)
+  struct Graph {
+    int prec;
+    double CFL;
+    bool last;
+    int cur;
+    cudaGraphExec_t exec;
+    int kernels;
+  };
+  std::vector<Graph> graphs;
+  bool use_graphs = true;
   int* tune_err = nullptr;    // error word of the tuning launches
   std::vector<void*> allocs;
   bool profiling = false;
@@ -293,6 +304,7 @@ int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cuda
 void fused_destroy(FusedState* f) {
   if (!f) return;
   for (cudaEvent_t e : f->ev) cudaEventDestroy(e);
+  for (auto& g : f->graphs) cudaGraphExecDestroy(g.exec);
   for (void* x : f->allocs) cudaFree(x);
   delete f;
 }
@@ -508,6 +520,122 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   ++*cnt;
 }
 
+// one iteration of the integrator (update.f90:129-226) on the stream
+static int enqueue_iteration(FusedState* f, const Params& p, const DevBlock& b, int prec, int it,
+                             bool lastit, double CFL, cudaStream_t s, long long* cnt) {
+  const bool mixed = prec == FEST_MIXED;
+  const int U = f->cur, A = (U + 1) % 3, B = (U + 2) % 3;
+  if (it <= 2) {
+    // fix() ghosts are written only while current_iter <= 2
+    // (bc_primitive.f90:236,318,366) and persist afterwards: every
+    // buffer that later serves as a stage input must receive them
+    for (int n = 0; n < 3; ++n) {
+      if (n == U) continue;
+      DevBlock bb = b;
+      bb.qp = f->Q[n];
+      bb.qp32 = mixed ? f->Q32[n] : nullptr;
+      bb.qp32_pitch = f->mpitch;
+      launch_ghosts(p, bb, f->table[n], it, Launcher{s, cnt}, false);
+    }
+  }
+  const size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
+  const bool tvd_early = it <= 2 && (p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3);
+  if (tvd_early) cudaMemcpyAsync(f->Us, f->Q[U], bytes, cudaMemcpyDeviceToDevice, s);
+  switch (p.integ) {
+    case FEST_TIME_NONE:
+      run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, lastit, s, cnt);
+      f->cur = A;
+      break;
+    case FEST_TIME_TVDRK2:
+      run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, false, s, cnt);
+      run_stage(f, p, b, prec, A, U, A, 0.5, 0.5, 1., 1., 0, 0, 0, CFL, it, lastit, s, cnt);
+      if (tvd_early) {
+        long long n = p.d.P * p.d.nv;
+        k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
+                                                                 f->mpitch, f->Us, f->Q[A], 0.5, 0.5);
+        ++*cnt;
+      }
+      break;
+    case FEST_TIME_TVDRK3:
+      run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, false, s, cnt);
+      run_stage(f, p, b, prec, A, B, A, 0.75, 0.25, 1., 1., 0, 0, 0, CFL, it, false, s, cnt);
+      run_stage(f, p, b, prec, B, U, B, 1. / 3., 2. / 3., 1., 1., 0, 0, 0, CFL, it, lastit, s, cnt);
+      if (tvd_early) {
+        long long n = p.d.P * p.d.nv;
+        k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
+                                                                 f->mpitch, f->Us, f->Q[B], 1. / 3., 2. / 3.);
+        ++*cnt;
+      }
+      break;
+    case FEST_TIME_RK2:
+      cudaMemsetAsync(b.Rstore, 0, sizeof(double) * ncells(p.d) * p.d.nv, s);
+      run_stage(f, p, b, prec, U, A, U, 0, 1, 0.5, 1., 0, 1, 1, CFL, it, false, s, cnt);
+      run_stage(f, p, b, prec, A, U, U, 0, 1, 0.5, 1., 1, 1, 0, CFL, it, lastit, s, cnt);
+      break;
+    case FEST_TIME_RK4:
+      cudaMemsetAsync(b.Rstore, 0, sizeof(double) * ncells(p.d) * p.d.nv, s);
+      run_stage(f, p, b, prec, U, A, U, 0, 1, 0.5, 1., 0, 1, 1, CFL, it, false, s, cnt);
+      run_stage(f, p, b, prec, A, B, U, 0, 1, 0.5, 2., 0, 1, 0, CFL, it, false, s, cnt);
+      run_stage(f, p, b, prec, B, A, U, 0, 1, 1.0, 2., 0, 1, 0, CFL, it, false, s, cnt);
+      run_stage(f, p, b, prec, A, U, U, 0, 1, 1. / 6., 1., 1, 1, 0, CFL, it, lastit, s, cnt);
+      break;
+    default:
+      return FEST_ERR_ARG;
+  }
+  // the blended ghosts must persist in every buffer once fix() stops
+  if (tvd_early)
+    for (int n = 0; n < 3; ++n)
+      if (n != f->cur) {
+        cudaMemcpyAsync(f->Q[n], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
+        if (mixed)
+          cudaMemcpyAsync(f->Q32[n], f->Q32[f->cur], sizeof(float) * (size_t)f->m_elems,
+                          cudaMemcpyDeviceToDevice, s);
+      }
+  return FEST_OK;
+}
+
+// Iterations after the second repeat the same launches with the same
+// arguments (fix() BCs and the TVD ghost blends stop), so each distinct
+// (precision, CFL, last-iteration flag, current buffer) is captured once as
+// a CUDA graph and replayed: one graph launch per iteration instead of one
+// launch per kernel.
+static int graph_for(FusedState* f, const Params& p, const DevBlock& b, int prec, int it, bool lastit,
+                     double CFL, cudaStream_t s, cudaGraphExec_t* out, int* kernels) {
+  for (const auto& g : f->graphs)
+    if (g.prec == prec && g.CFL == CFL && g.last == lastit && g.cur == f->cur) {
+      *out = g.exec;
+      *kernels = g.kernels;
+      return FEST_OK;
+    }
+  const int cur0 = f->cur;
+  long long n = 0;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return FEST_ERR_CUDA;
+  int rc = enqueue_iteration(f, p, b, prec, it, lastit, CFL, s, &n);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  f->cur = cur0;  // the capture only recorded the iteration
+  if (rc || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return rc ? rc : FEST_ERR_CUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return FEST_ERR_CUDA;
+  }
+  if (f->graphs.size() >= 16) {
+    cudaGraphExecDestroy(f->graphs.front().exec);
+    f->graphs.erase(f->graphs.begin());
+  }
+  f->graphs.push_back(FusedState::Graph{prec, CFL, lastit, cur0, exec, (int)n});
+  *out = exec;
+  *kernels = (int)n;
+  return FEST_OK;
+}
+
 int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n_iters,
               int first_iter, double CFL, cudaStream_t s, long long* cnt) {
   if (!f) return FEST_ERR_ARG;
@@ -519,76 +647,28 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
   } else {
     f->mirror_valid = false;  // FP64 stages do not maintain the mirror
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cap);
   for (int n = 0; n < n_iters; ++n) {
     const int it = first_iter + n;
     const bool lastit = (n == n_iters - 1);
-    const int U = f->cur, A = (U + 1) % 3, B = (U + 2) % 3;
-    if (it <= 2) {
-      // fix() ghosts are written only while current_iter <= 2
-      // (bc_primitive.f90:236,318,366) and persist afterwards: every
-      // buffer that later serves as a stage input must receive them
-      for (int n = 0; n < 3; ++n) {
-        if (n == U) continue;
-        DevBlock bb = b;
-        bb.qp = f->Q[n];
-        bb.qp32 = mixed ? f->Q32[n] : nullptr;
-        bb.qp32_pitch = f->mpitch;
-        launch_ghosts(p, bb, f->table[n], it, Launcher{s, cnt}, false);
+    // graphs once the k-chunk is tuned (tuning synchronises), never inside
+    // a caller's own capture, never while stage launches are being timed
+    const bool replay = f->use_graphs && it > 2 && f->kc[mixed ? 1 : 0] != 0 && !f->profiling &&
+                        cap == cudaStreamCaptureStatusNone;
+    if (replay) {
+      cudaGraphExec_t exec;
+      int kernels = 0;
+      if (graph_for(f, p, b, prec, it, lastit, CFL, s, &exec, &kernels) == FEST_OK) {
+        if (cudaGraphLaunch(exec, s) != cudaSuccess) return FEST_ERR_CUDA;
+        *cnt += kernels;
+        if (p.integ == FEST_TIME_NONE) f->cur = (f->cur + 1) % 3;
+        continue;
       }
+      f->use_graphs = false;  // capture refused: launch directly from now on
     }
-    const size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
-    const bool tvd_early = it <= 2 && (p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3);
-    if (tvd_early) cudaMemcpyAsync(f->Us, f->Q[U], bytes, cudaMemcpyDeviceToDevice, s);
-    switch (p.integ) {
-      case FEST_TIME_NONE:
-        run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, lastit, s, cnt);
-        f->cur = A;
-        break;
-      case FEST_TIME_TVDRK2:
-        run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, false, s, cnt);
-        run_stage(f, p, b, prec, A, U, A, 0.5, 0.5, 1., 1., 0, 0, 0, CFL, it, lastit, s, cnt);
-        if (tvd_early) {
-          long long n = p.d.P * p.d.nv;
-          k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
-                                                                   f->mpitch, f->Us, f->Q[A], 0.5, 0.5);
-          ++*cnt;
-        }
-        break;
-      case FEST_TIME_TVDRK3:
-        run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, false, s, cnt);
-        run_stage(f, p, b, prec, A, B, A, 0.75, 0.25, 1., 1., 0, 0, 0, CFL, it, false, s, cnt);
-        run_stage(f, p, b, prec, B, U, B, 1. / 3., 2. / 3., 1., 1., 0, 0, 0, CFL, it, lastit, s, cnt);
-        if (tvd_early) {
-          long long n = p.d.P * p.d.nv;
-          k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
-                                                                   f->mpitch, f->Us, f->Q[B], 1. / 3., 2. / 3.);
-          ++*cnt;
-        }
-        break;
-      case FEST_TIME_RK2:
-        cudaMemsetAsync(b.Rstore, 0, sizeof(double) * ncells(p.d) * p.d.nv, s);
-        run_stage(f, p, b, prec, U, A, U, 0, 1, 0.5, 1., 0, 1, 1, CFL, it, false, s, cnt);
-        run_stage(f, p, b, prec, A, U, U, 0, 1, 0.5, 1., 1, 1, 0, CFL, it, lastit, s, cnt);
-        break;
-      case FEST_TIME_RK4:
-        cudaMemsetAsync(b.Rstore, 0, sizeof(double) * ncells(p.d) * p.d.nv, s);
-        run_stage(f, p, b, prec, U, A, U, 0, 1, 0.5, 1., 0, 1, 1, CFL, it, false, s, cnt);
-        run_stage(f, p, b, prec, A, B, U, 0, 1, 0.5, 2., 0, 1, 0, CFL, it, false, s, cnt);
-        run_stage(f, p, b, prec, B, A, U, 0, 1, 1.0, 2., 0, 1, 0, CFL, it, false, s, cnt);
-        run_stage(f, p, b, prec, A, U, U, 0, 1, 1. / 6., 1., 1, 1, 0, CFL, it, lastit, s, cnt);
-        break;
-      default:
-        return FEST_ERR_ARG;
-    }
-    // the blended ghosts must persist in every buffer once fix() stops
-    if (tvd_early)
-      for (int n = 0; n < 3; ++n)
-        if (n != f->cur) {
-          cudaMemcpyAsync(f->Q[n], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
-          if (mixed)
-            cudaMemcpyAsync(f->Q32[n], f->Q32[f->cur], sizeof(float) * (size_t)f->m_elems,
-                            cudaMemcpyDeviceToDevice, s);
-        }
+    int rc = enqueue_iteration(f, p, b, prec, it, lastit, CFL, s, cnt);
+    if (rc) return rc;
   }
   return FEST_OK;
 }
