@@ -1,0 +1,293 @@
+// fest_adjoint.cu - reverse-mode product with the transposed Jacobian of the
+// inviscid residual: dq = (dR/dq)^T lambda, R as get_total_conservative_Residue
+// computes it (update.f90:495-547: ghost cells, face states, fluxes, residue)
+// and q the interior primitive state.  No counterpart in the reference.
+//
+// Reverse order of the primal:
+//   residue  R(c) = sum over the faces of c of +-F(face)   (scheme.f90:133-135)
+//     -> every face's flux receives mu = lambda(left cell) - lambda(right cell)
+//   flux     F = F(qL, qR) (one of the six schemes)
+//     -> qL, qR receive (dF/dqL)^T mu, (dF/dqR)^T mu
+//   face states qL = Lp(left cell), qR = Rm(right cell) (reconstruction with
+//   its boundary overrides)
+//     -> the up-to-5 cells of each stencil receive their share
+//   ghost cells (the BC of each face at this iteration)
+//     -> the interior cells they were computed from
+// The local Jacobians come from the primal's own templated device code run
+// on dual numbers (fest_dual.cuh).  Face contributions meet in cells by FP64
+// atomic adds.
+#include <algorithm>
+
+#include "fest_dual.cuh"
+#include "fest_kernels.cuh"
+
+namespace fest {
+
+namespace {
+
+constexpr int TPB_ADJ = 128;
+
+template <typename T, int N> struct DualLine {
+  const double* base;  // variable l, cell at normal coordinate 0
+  long long stride;
+  int center;  // seeds the cells center-2 .. center+2
+  __device__ __forceinline__ Dual<T, N> operator()(int c) const {
+    return Dual<T, N>::var((T)base[c * stride], c - center + 2);
+  }
+};
+template <typename T, int N> struct ConstLine {
+  const double* base;
+  long long stride;
+  __device__ __forceinline__ Dual<T, N> operator()(int c) const {
+    return Dual<T, N>::cst((T)base[c * stride]);
+  }
+};
+template <typename T, int N> struct VolConst {
+  const double* p;  // cells + 4*pidx(cell at normal coordinate 0)
+  long long stride;
+  int n;
+  __device__ __forceinline__ Dual<T, N> operator()(int c) const {
+    c = c < -2 ? -2 : (c > n + 2 ? n + 2 : c);
+    return Dual<T, N>::cst((T)p[4 * c * stride]);
+  }
+};
+
+__device__ __forceinline__ void cell_of(int dir, int c, int ta, int tb, int& i, int& j, int& k) {
+  if (dir == 0) { i = c; j = ta; k = tb; }
+  else if (dir == 1) { i = ta; j = c; k = tb; }
+  else { i = ta; j = tb; k = c; }
+}
+
+// one thread per face of direction dir (faces 1..n along dir, interior
+// tangential positions)
+template <typename T>
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, const double* lam,
+                                                       double* bar, int dir) {
+  using D5 = Dual<T, 5>;
+  using D10 = Dual<T, 10>;
+  const Dims& d = p.d;
+  const int n = extent_of(d, dir);
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * na * nb) return;
+  const int c = 1 + (int)(t % n);
+  const long long r = t / n;
+  const int ta = 1 + (int)(r % na), tb = 1 + (int)(r / na);
+  const long long P = d.P, N = ncells(d);
+  const long long st = pstride(d, dir);
+  // mu = lambda(left) - lambda(right); ghost cells carry no residual
+  T mu[5];
+  int i, j, k;
+#pragma unroll
+  for (int l = 0; l < 5; ++l) mu[l] = T(0);
+  if (c - 1 >= 1) {
+    cell_of(dir, c - 1, ta, tb, i, j, k);
+#pragma unroll
+    for (int l = 0; l < 5; ++l) mu[l] += (T)lam[cidx(d, i, j, k) + N * l];
+  }
+  if (c <= n - 1) {
+    cell_of(dir, c, ta, tb, i, j, k);
+#pragma unroll
+    for (int l = 0; l < 5; ++l) mu[l] -= (T)lam[cidx(d, i, j, k) + N * l];
+  }
+  // face states with their stencil derivatives
+  cell_of(dir, 0, ta, tb, i, j, k);
+  const long long c0 = pidx(d, i, j, k);
+  D5 qL[5], qR[5];
+  {
+    VolConst<T, 5> vol{b.cells + 4 * c0, st, n};
+    ConstLine<T, 5> pres{b.qp + c0 + P * 4, st};
+#pragma unroll
+    for (int l = 0; l < 5; ++l) {
+      D5 Rm, Lp;
+      DualLine<T, 5> qa{b.qp + c0 + P * l, st, c - 1};
+      recon_cell<D5>(p, dir, c - 1, l + 1, qa, pres, vol, Rm, Lp);
+      qL[l] = Lp;
+      DualLine<T, 5> qb{b.qp + c0 + P * l, st, c};
+      recon_cell<D5>(p, dir, c, l + 1, qb, pres, vol, Rm, Lp);
+      qR[l] = Rm;
+    }
+  }
+  // flux Jacobian, transposed onto mu
+  T bx[10];
+  {
+    D10 xl[5], xr[5], Fo[NVMAX];
+#pragma unroll
+    for (int l = 0; l < 5; ++l) {
+      xl[l] = D10::var(qL[l].v, l);
+      xr[l] = D10::var(qR[l].v, 5 + l);
+    }
+    const double* fc = b.faces[dir] + 4 * fidx(d, dir, i + (dir == 0 ? c : 0), j + (dir == 1 ? c : 0),
+                                               k + (dir == 2 ? c : 0));
+    const D10 A = D10::cst((T)fc[0]), nx = D10::cst((T)fc[1]), ny = D10::cst((T)fc[2]),
+              nz = D10::cst((T)fc[3]);
+    const D10 mask = D10::cst((T)wall_mask(p, dir, c));
+    face_flux<D10>(p, xl, xr, A, nx, ny, nz, mask, Fo);
+#pragma unroll
+    for (int m = 0; m < 10; ++m) {
+      T s = T(0);
+#pragma unroll
+      for (int l = 0; l < 5; ++l) s += mu[l] * Fo[l].d[m];
+      bx[m] = s;
+    }
+  }
+  // face states -> stencil cells
+#pragma unroll
+  for (int l = 0; l < 5; ++l)
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+      const T gL = bx[l] * qL[l].d[s], gR = bx[5 + l] * qR[l].d[s];
+      if (gL != T(0)) atomicAdd(bar + c0 + (c - 1 + s - 2) * st + P * l, (double)gL);
+      if (gR != T(0)) atomicAdd(bar + c0 + (c + s - 2) * st + P * l, (double)gR);
+    }
+}
+
+// ghost (layer L) / interior (layer m) cell of face f at (ta, tb)
+__device__ __forceinline__ long long gcell_p(const Dims& d, int f, int L, int ta, int tb) {
+  switch (f) {
+    case 0: return pidx(d, 1 - L, ta, tb);
+    case 1: return pidx(d, d.imx + L - 1, ta, tb);
+    case 2: return pidx(d, ta, 1 - L, tb);
+    case 3: return pidx(d, ta, d.jmx + L - 1, tb);
+    case 4: return pidx(d, ta, tb, 1 - L);
+    default: return pidx(d, ta, tb, d.kmx + L - 1);
+  }
+}
+__device__ __forceinline__ long long icell_p(const Dims& d, int f, int m, int ta, int tb) {
+  switch (f) {
+    case 0: return pidx(d, m, ta, tb);
+    case 1: return pidx(d, d.imx - m, ta, tb);
+    case 2: return pidx(d, ta, m, tb);
+    case 3: return pidx(d, ta, d.jmx - m, tb);
+    case 4: return pidx(d, ta, tb, m);
+    default: return pidx(d, ta, tb, d.kmx - m);
+  }
+}
+
+// the ghost cells' adjoints flow back into the interior cells the BC of
+// their face computed them from (bc_primitive.f90:160-206 and the
+// procedures it calls, at iteration iter); the ghost entries end at zero
+template <typename T>
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_ghosts(Params p, DevBlock b, double* bar, int iter) {
+  const Dims& d = p.d;
+  const int f = blockIdx.z, dir = f / 2;
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nb) return;
+  const int ta = 1 + (int)(t % na), tb = 1 + (int)(t / na);
+  const long long P = d.P;
+  const int id = p.id[f];
+  auto take = [&](int L, int l) -> double {  // read and clear a ghost adjoint
+    double* g = bar + gcell_p(d, f, L, ta, tb) + P * l;
+    const double v = *g;
+    *g = 0.0;
+    return v;
+  };
+  auto give = [&](int m, int l, double v) {
+    if (v != 0.0) atomicAdd(bar + icell_p(d, f, m, ta, tb) + P * l, v);
+  };
+  auto flat = [&](int l) { give(1, l, take(1, l) + take(2, l) + take(3, l)); };
+  auto symm = [&](int l) {
+    for (int L = 1; L <= 3; ++L) {
+      const double g = take(L, l);
+      give(L, l, p.c2 / p.c1 * g);
+      give(L + 1, l, -p.c3 / p.c1 * g);
+    }
+  };
+  auto anti = [&](int l) { for (int L = 1; L <= 3; ++L) give(L, l, -take(L, l)); };
+  auto none = [&](int l) { for (int L = 1; L <= 3; ++L) take(L, l); };  // constant ghosts
+  int fi, fj, fk;
+  {
+    const int c = (f % 2 == 0) ? 1 : extent_of(d, dir);
+    if (dir == 0) { fi = c; fj = ta; fk = tb; }
+    else if (dir == 1) { fi = ta; fj = c; fk = tb; }
+    else { fi = ta; fj = tb; fk = c; }
+  }
+  switch (id) {
+    case -1: for (int l = 0; l < 5; ++l) none(l); break;
+    case -2:
+    case -7: for (int l = 0; l < 5; ++l) flat(l); break;
+    case -3: for (int l = 0; l < 4; ++l) none(l); flat(4); break;
+    case -4: for (int l = 0; l < 4; ++l) flat(l); none(4); break;
+    case -5:  // adiabatic wall (the host admits Tw in [0,1] only)
+      symm(4); symm(0); anti(1); anti(2); anti(3);
+      break;
+    case -6: {  // slip wall: g = u - 2 (u.fn) fr  ->  bar_u += g_bar - 2 fn (fr.g_bar)
+      symm(0); symm(4);
+      const double* fn = b.faces[dir] + 4 * fidx(d, dir, fi, fj, fk);
+      const double* fr = b.faces[0] + 4 * fidx(d, 0, fi, fj, fk);
+      for (int L = 1; L <= 3; ++L) {
+        const double gu = take(L, 1), gv = take(L, 2), gw = take(L, 3);
+        const double s = fr[1] * gu + fr[2] * gv + fr[3] * gw;
+        give(L, 1, gu - 2.0 * fn[1] * s);
+        give(L, 2, gv - 2.0 * fn[2] * s);
+        give(L, 3, gw - 2.0 * fn[3] * s);
+      }
+    } break;
+    case -8:
+    case -11: {  // all three layers = riemann_ghost(interior layer 1)
+      using D5 = Dual<T, 5>;
+      double gs[5];
+      for (int l = 0; l < 5; ++l) gs[l] = take(1, l) + take(2, l) + take(3, l);
+      const double* fc = b.faces[dir] + 4 * fidx(d, dir, fi, fj, fk);
+      const double sg = (f % 2 == 0) ? -1.0 : 1.0;
+      const long long in1 = icell_p(d, f, 1, ta, tb);
+      D5 in[5], g[5];
+      for (int l = 0; l < 5; ++l) in[l] = D5::var((T)b.qp[in1 + P * l], l);
+      riemann_ghost<D5>(p, f, id == -11, D5::cst((T)(sg * fc[1])), D5::cst((T)(sg * fc[2])),
+                        D5::cst((T)(sg * fc[3])), in, g);
+      for (int m = 0; m < 5; ++m) {
+        double s = 0.0;
+        for (int l = 0; l < 5; ++l) s += gs[l] * (double)g[l].d[m];
+        give(1, m, s);
+      }
+    } break;
+    default:
+      if (id == -10 || id >= 0) {  // ghost L <- layer L of the partner face (same block)
+        const int pf = p.part_face[f];
+        for (int l = 0; l < 5; ++l)
+          for (int L = 1; L <= 3; ++L) {
+            const double g = take(L, l);
+            if (g != 0.0) atomicAdd(bar + icell_p(d, pf, L, ta, tb) + P * l, g);
+          }
+      } else {
+        for (int l = 0; l < 5; ++l) none(l);
+      }
+  }
+}
+
+unsigned nblocks(long long n) { return (unsigned)((n + TPB_ADJ - 1) / TPB_ADJ); }
+
+}  // namespace
+
+bool vjp_supported(const Params& p) {
+  if (p.mu_ref != 0.0 || p.turb != FEST_TURB_NONE || p.d.nv != 5) return false;
+  if (p.pb[0] || p.pb[1] || p.pb[2]) return false;  // pressure switch couples variables
+  if (ghosts_need_sequential(p) || p.d.kmx == 2) return false;
+  for (int f = 0; f < 6; ++f) {
+    const int id = p.id[f];
+    if (id == -9) return false;
+    if (id == -5 && (p.Tw[f] < 0.0 || p.Tw[f] > 1.0)) return false;
+  }
+  return true;
+}
+
+void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
+                         double* bar, const Launcher& L) {
+  const Dims& d = p.d;
+  cudaMemsetAsync(bar, 0, sizeof(double) * (size_t)d.P * d.nv, L.s);
+  for (int dir = 0; dir < 3; ++dir) {
+    const int n = extent_of(d, dir);
+    const long long nf = (long long)n * ((dir == 0 ? d.jmx : d.imx) - 1) * ((dir == 2 ? d.jmx : d.kmx) - 1);
+    k_vjp_faces<double><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, dir);
+    ++*L.count;
+  }
+  long long wmax = 0;
+  for (int dir = 0; dir < 3; ++dir)
+    wmax = std::max<long long>(wmax, (long long)((dir == 0 ? d.jmx : d.imx) - 1) *
+                                         ((dir == 2 ? d.jmx : d.kmx) - 1));
+  k_vjp_ghosts<double><<<dim3(nblocks(wmax), 1, 6), TPB_ADJ, 0, L.s>>>(p, b, bar, iter);
+  ++*L.count;
+}
+
+}  // namespace fest

@@ -28,6 +28,8 @@ struct fest_handle {
   int precision = FEST_FP64;
   long long launches = 0;
   FusedState* fused = nullptr;
+  double* d_vjp_bar = nullptr;  // adjoint work arrays, allocated on first use
+  double* d_vjp_lam = nullptr;
   std::vector<void*> allocs;
   Launcher L() { return Launcher{s, &launches}; }
 };
@@ -638,6 +640,22 @@ int fest_get_total_conservative_residue(fest_handle* h, double* qp, int current_
   RET(residual_fp64(h, current_iter));
   RET(down(h, qp, h->d.qp, z.qp));
   RET(down(h, residue, h->d.res, z.res));
+  return finish(h);
+}
+
+int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const double* lambda,
+                      double* dq) {
+  if (!h || !lambda || !dq) return FEST_ERR_ARG;
+  if (!vjp_supported(h->p)) return FEST_ERR_ARG;
+  RET(sync_fused(h));
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
+  if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
+  if (qp) RET(up(h, h->d.qp, qp, z.qp));
+  RET(up(h, h->d_vjp_lam, lambda, z.res));
+  launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
+  launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L());
+  RET(down(h, dq, h->d_vjp_bar, z.qp));
   return finish(h);
 }
 

@@ -62,5 +62,10 @@ void launch_resnorm(const Params& p, const DevBlock& b, double* d_out, const Lau
 void launch_geometry(const Params& p, const DevBlock& b, const Launcher& L);
 void launch_wall_dist(const Params& p, const DevBlock& b, const double* d_wall, int n_wall,
                       double* d_node_dist, const Launcher& L);
+// adjoint of the inviscid residual: bar (padded qp layout) = (dR/dq)^T lam
+// (residue layout), ghost cells filled for iteration iter beforehand
+bool vjp_supported(const Params& p);
+void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
+                         double* bar, const Launcher& L);
 
 }  // namespace fest

@@ -202,6 +202,7 @@ _SIGS = {
     "fest_set_stream": [C.c_void_p, C.c_void_p],
     "fest_profile": [C.c_void_p, C.c_int],
     "fest_profile_read": [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)],
+    "fest_residual_vjp": [C.c_void_p, _DP, C.c_int, _DP, _DP],
     "fest_find_resnorm_noalloc": [C.POINTER(Extent), C.POINTER(Flow), C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, _DP, C.c_void_p],
 }

@@ -114,6 +114,14 @@ class Handle:
                    out.ctypes.data_as(C.POINTER(C.c_double)) if with_norm else None)
         return out[:self.ext.n_var + 1] if with_norm else None
 
+    def residual_vjp(self, qp, it, lam):
+        """(dR/dq)^T lam for the residual of iteration it at state qp."""
+        q = None if qp is None else np.array(qp, order="F")
+        lam = np.asfortranarray(lam, dtype=np.float64)
+        dq = np.empty(self.shape["qp"], order="F")
+        self._call("fest_residual_vjp", abi.ptr(q), int(it), abi.ptr(lam), abi.ptr(dq))
+        return dq
+
     def resnorm(self):
         out = np.zeros(8)
         self._call("fest_find_resnorm", out.ctypes.data_as(C.POINTER(C.c_double)))

@@ -243,6 +243,19 @@ int fest_set_stream(fest_handle *h, void *cuda_stream);
 int fest_profile(fest_handle *h, int enable);
 int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
 
+/* ---- adjoint ------------------------------------------------------------- */
+/* No counterpart in the reference.  Reverse-mode product with the
+ * transposed Jacobian of the residual that fest_get_total_conservative_residue
+ * computes at this iteration: dq = (dR/dq)^T lambda, q the interior primitive
+ * state (ghost cells follow it through the BCs of the iteration), lambda in
+ * the residue layout, dq in the qp layout (ghost entries zero).  qp
+ * (nullable: the device state) is uploaded and its ghosts filled first.
+ * FP64.  Inviscid blocks of the fused-path kind (n_var 5, >= 4 interior
+ * cells per direction, no -9 face, no pressure switch, adiabatic -5 walls);
+ * FEST_ERR_ARG otherwise. */
+int fest_residual_vjp(fest_handle *h, const double *qp, int current_iter,
+                      const double *lambda, double *dq);
+
 /* ---- allocation-free norm ------------------------------------------------ */
 /* No counterpart in the reference.  find_resnorm (resnorm.f90:62) without a
  * handle, on caller-owned DEVICE arrays: residue in the FEST_ARR_RESIDUE
