@@ -258,6 +258,69 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_ghosts(Params p, DevBlock b, do
 
 unsigned nblocks(long long n) { return (unsigned)((n + TPB_ADJ - 1) / TPB_ADJ); }
 
+// mu = P^T phi with P = (dt/V) dq/dU, the local-time-step preconditioner of
+// the forward-Euler update (update.f90:431) mapping a conservative residual
+// to a primitive increment; dq/dU of q = (rho,u,v,w,p), U = (rho,rho u,
+// rho v, rho w, E)
+__global__ void k_adj_precond(Params p, DevBlock b, const double* phi, double* mu) {
+  const Dims& d = p.d;
+  const long long N = ncells(d);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= N) return;
+  const int i = 1 + (int)(t % (d.imx - 1));
+  const long long r = t / (d.imx - 1);
+  const int j = 1 + (int)(r % (d.jmx - 1)), k = 1 + (int)(r / (d.jmx - 1));
+  const long long c = pidx(d, i, j, k), ci = cidx(d, i, j, k), P = d.P;
+  const double rho = b.qp[c], u = b.qp[c + P], v = b.qp[c + 2 * P], w = b.qp[c + 3 * P];
+  const double g1 = p.gm - 1.0;
+  const double f0 = phi[c], fu = phi[c + P], fv = phi[c + 2 * P], fw = phi[c + 3 * P], fp = phi[c + 4 * P];
+  const double s = b.dt[ci] / b.cells[4 * c];
+  mu[ci] = s * (f0 - (u * fu + v * fv + w * fw) / rho + 0.5 * g1 * (u * u + v * v + w * w) * fp);
+  mu[ci + N] = s * (fu / rho - g1 * u * fp);
+  mu[ci + 2 * N] = s * (fv / rho - g1 * v * fp);
+  mu[ci + 3 * N] = s * (fw / rho - g1 * w * fp);
+  mu[ci + 4 * N] = s * (g1 * fp);
+}
+
+// out = c0 x0 + c1 x1 + c2 x2 + c3 x3 on interior cells (null x: term
+// absent); with sq, also sum |out - x0|^2
+__global__ void k_adj_combine(Dims d, double* out, double c0, const double* x0, double c1,
+                              const double* x1, double c2, const double* x2, double c3,
+                              const double* x3, double* sq) {
+  __shared__ double red[TPB_ADJ];
+  const long long N = ncells(d);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (t < N) {
+    const int i = 1 + (int)(t % (d.imx - 1));
+    const long long r = t / (d.imx - 1);
+    const int j = 1 + (int)(r % (d.jmx - 1)), k = 1 + (int)(r / (d.jmx - 1));
+    const long long c = pidx(d, i, j, k);
+    for (int l = 0; l < 5; ++l) {
+      const long long e = c + d.P * l;
+      double v = c0 * x0[e];
+      if (x1) v += c1 * x1[e];
+      if (x2) v += c2 * x2[e];
+      if (x3) v += c3 * x3[e];
+      if (sq) acc += (v - x0[e]) * (v - x0[e]);
+      out[e] = v;
+    }
+  }
+  if (!sq) return;
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && red[0] != 0.0) atomicAdd(sq, red[0]);
+}
+
+__global__ void k_adj_psi(Dims d, const double* mu, double* psi) {  // psi = -mu
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < ncells(d) * 5) psi[t] = -mu[t];
+}
+
 }  // namespace
 
 bool vjp_supported(const Params& p) {
@@ -270,6 +333,57 @@ bool vjp_supported(const Params& p) {
     if (id == -5 && (p.Tw[f] < 0.0 || p.Tw[f] > 1.0)) return false;
   }
   return true;
+}
+
+// S^T v = v - (dR/dq)^T (P^T v): the transpose of one forward-Euler stage
+// linearised at the fixed point
+static void apply_ST(const Params& p, const DevBlock& b, const double* v, double* out, AdjointWork& w,
+                     const Launcher& L) {
+  const long long N = ncells(p.d);
+  k_adj_precond<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p, b, v, w.mu);
+  launch_residual_vjp(p, b, 3, w.mu, w.bar, L);
+  k_adj_combine<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p.d, out, 1.0, v, -1.0, w.bar, 0.0, nullptr, 0.0,
+                                                 nullptr, nullptr);
+  *L.count += 2;
+}
+
+// One step phi <- G^T phi + dJ/dq of the transposed integrator map
+// linearised at the fixed point (S = I - P dR/dq):
+//   forward Euler  G = S
+//   TVD-RK3        G = I/3 + S/2 + S^3/6  (update.f90:196-206 blends)
+void launch_adjoint_iteration(const Params& p, const DevBlock& b, AdjointWork& w, const Launcher& L) {
+  const long long N = ncells(p.d);
+  if (p.integ == FEST_TIME_TVDRK3) {
+    apply_ST(p, b, w.phi, w.a, w, L);
+    apply_ST(p, b, w.a, w.b, w, L);
+    apply_ST(p, b, w.b, w.c, w, L);
+    k_adj_combine<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p.d, w.phi, 1.0 / 3.0, w.phi, 0.5, w.a, 1.0 / 6.0,
+                                                   w.c, 1.0, w.dJ, w.sq);
+  } else {
+    apply_ST(p, b, w.phi, w.a, w, L);
+    k_adj_combine<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p.d, w.phi, 0.0, w.phi, 1.0, w.a, 1.0, w.dJ, 0.0,
+                                                   nullptr, w.sq);
+  }
+  ++*L.count;
+}
+
+// psi = -P^T H phi with H = I (forward Euler) or 2/3 I + S^T/6 + (S^T)^2/6
+// (TVD-RK3), so that (dR/dq)^T psi = -dJ/dq at the fixed point of phi
+void launch_adjoint_psi(const Params& p, const DevBlock& b, AdjointWork& w, double* psi,
+                        const Launcher& L) {
+  const long long N = ncells(p.d);
+  const double* h = w.phi;
+  if (p.integ == FEST_TIME_TVDRK3) {
+    apply_ST(p, b, w.phi, w.a, w, L);
+    apply_ST(p, b, w.a, w.b, w, L);
+    k_adj_combine<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p.d, w.c, 2.0 / 3.0, w.phi, 1.0 / 6.0, w.a,
+                                                   1.0 / 6.0, w.b, 0.0, nullptr, nullptr);
+    ++*L.count;
+    h = w.c;
+  }
+  k_adj_precond<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p, b, h, w.mu);
+  k_adj_psi<<<nblocks(N * 5), TPB_ADJ, 0, L.s>>>(p.d, w.mu, psi);
+  *L.count += 2;
 }
 
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,

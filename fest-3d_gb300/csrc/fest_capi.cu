@@ -1,6 +1,8 @@
 // fest_capi.cu - the extern "C" boundary: handle lifetime, host<->device
 // movement of the reference's Fortran-layout arrays, and the module-level
 // and integrator entry points built from the module kernels.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -657,6 +659,62 @@ int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const 
   launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L());
   RET(down(h, dq, h->d_vjp_bar, z.qp));
   return finish(h);
+}
+
+int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_iters, double tol,
+                       double* psi, int* n_done, double* drop) {
+  if (!h || !dJdq || max_iters < 0) return FEST_ERR_ARG;
+  if (!vjp_supported(h->p) || h->p.tstep != 'l') return FEST_ERR_ARG;
+  if (h->p.integ != FEST_TIME_NONE && h->p.integ != FEST_TIME_TVDRK3) return FEST_ERR_ARG;
+  RET(sync_fused(h));
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
+  if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
+  AdjointWork w{};
+  w.bar = h->d_vjp_bar;
+  w.mu = h->d_vjp_lam;
+  const size_t n0 = h->allocs.size();
+  int rc = FEST_OK;
+  for (double** x : {&w.phi, &w.dJ, &w.a, &w.b, &w.c})
+    if (!rc) rc = dalloc(h, x, z.qp);
+  if (!rc) rc = dalloc(h, &w.sq, 1);
+  auto release = [&]() {  // the work arrays are the allocations made here
+    cudaStreamSynchronize(h->s);
+    while (h->allocs.size() > n0) {
+      cudaFree(h->allocs.back());
+      h->allocs.pop_back();
+    }
+  };
+  if (!rc) rc = up(h, w.dJ, dJdq, z.qp);
+  // the frozen primal: ghost cells, face states and the local time step
+  if (!rc) rc = residual_fp64(h, 3);
+  if (!rc) launch_time_step(h->p, h->d, CFL, h->L());
+  Launcher L = h->L();
+  double first = -1.0, last = 0.0;
+  int it = 0;
+  while (!rc && it < max_iters) {
+    const int chunk = std::min(20, max_iters - it);
+    cudaMemsetAsync(w.sq, 0, sizeof(double), h->s);
+    for (int n = 0; n < chunk; ++n) launch_adjoint_iteration(h->p, h->d, w, L);
+    it += chunk;
+    double s2 = 0.0;
+    rc = down(h, &s2, w.sq, 1);
+    if (!rc) rc = finish(h);
+    if (rc) break;
+    last = sqrt(s2 / chunk);
+    if (first < 0.0) first = last;
+    if (!(last == last)) { rc = FEST_ERR_NAN; break; }
+    if (first > 0.0 && last <= tol * first) break;
+  }
+  if (!rc && psi) {
+    launch_adjoint_psi(h->p, h->d, w, w.mu, L);
+    rc = down(h, psi, w.mu, z.res);
+    if (!rc) rc = finish(h);
+  }
+  if (n_done) *n_done = it;
+  if (drop) *drop = first > 0.0 ? last / first : 0.0;
+  release();
+  return rc;
 }
 
 int fest_get_next_solution(fest_handle* h, double* qp, int current_iter, double CFL,

@@ -67,5 +67,16 @@ void launch_wall_dist(const Params& p, const DevBlock& b, const double* d_wall, 
 bool vjp_supported(const Params& p);
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
                          double* bar, const Launcher& L);
+// work arrays of the fixed-point adjoint: phi, dJ, a, b, c, bar in the qp
+// layout, mu in the residue layout, sq one double
+struct AdjointWork {
+  double *phi, *dJ, *a, *b, *c, *bar, *mu, *sq;
+};
+// one step phi <- G^T phi + dJ/dq (G the integrator's map linearised at the
+// fixed point: forward Euler or TVD-RK3); sq += |change of phi|^2
+void launch_adjoint_iteration(const Params& p, const DevBlock& b, AdjointWork& w, const Launcher& L);
+// psi = -P^T H phi (residue layout), the adjoint of the residual
+void launch_adjoint_psi(const Params& p, const DevBlock& b, AdjointWork& w, double* psi,
+                        const Launcher& L);
 
 }  // namespace fest

@@ -122,6 +122,17 @@ class Handle:
         self._call("fest_residual_vjp", abi.ptr(q), int(it), abi.ptr(lam), abi.ptr(dq))
         return dq
 
+    def adjoint_solve(self, dJdq, CFL, max_iters, tol):
+        """psi with (dR/dq)^T psi = -dJ/dq at the device state; returns
+        (psi, iterations, drop)."""
+        dj = np.asfortranarray(dJdq, dtype=np.float64)
+        psi = np.empty(self.shape["residue"], order="F")
+        n = C.c_int()
+        drop = C.c_double()
+        self._call("fest_adjoint_solve", abi.ptr(dj), float(CFL), int(max_iters), float(tol),
+                   abi.ptr(psi), C.byref(n), C.byref(drop))
+        return psi, n.value, drop.value
+
     def resnorm(self):
         out = np.zeros(8)
         self._call("fest_find_resnorm", out.ctypes.data_as(C.POINTER(C.c_double)))

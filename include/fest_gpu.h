@@ -255,6 +255,19 @@ int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
  * FEST_ERR_ARG otherwise. */
 int fest_residual_vjp(fest_handle *h, const double *qp, int current_iter,
                       const double *lambda, double *dq);
+/* No counterpart in the reference.  Adjoint of the steady residual at the
+ * device state (a converged primal, local time steps at CFL): solves
+ * (dR/dq)^T psi = -dJ/dq for psi (residue layout) as the fixed point
+ * phi = G^T phi + dJ/dq, G the handle's integrator map (forward Euler or
+ * TVD-RK3) linearised at the primal fixed point, built from stages
+ * S = I - P dR/dq with P = (dt/V) dq/dU; it converges where that primal
+ * iteration does.  dJdq in the qp layout (interior entries used).
+ * Stops after max_iters or when the RMS update has dropped by tol;
+ * n_done, drop (nullable) report the iterations and that drop.  Then
+ * dJ/dalpha = dJ/dalpha|_q + psi . dR/dalpha for any parameter alpha. */
+int fest_adjoint_solve(fest_handle *h, const double *dJdq, double CFL,
+                       int max_iters, double tol, double *psi, int *n_done,
+                       double *drop);
 
 /* ---- allocation-free norm ------------------------------------------------ */
 /* No counterpart in the reference.  find_resnorm (resnorm.f90:62) without a

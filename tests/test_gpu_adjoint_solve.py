@@ -1,0 +1,40 @@
+"""The fixed-point adjoint (fest_adjoint_solve) on the smooth-bump channel:
+wall-force sensitivities to the inflow Mach number and angle against
+central finite differences of re-converged FP64 primal solutions.
+
+Reduced grid (64x24x4 cells) and the first-order scheme, whose explicit
+iteration converges to a 1e-10 drop within seconds (the second-order
+scheme's explicit iteration needs far longer on this case; its residual
+Jacobian is checked against finite differences in test_gpu_adjoint.py).
+Five primal solves and one adjoint solve, each to a 1e-10 drop; agreement
+to 1e-4 relative."""
+import numpy as np
+import pytest
+
+from fest3d import adjoint as A
+
+pytestmark = pytest.mark.gpu
+
+
+def test_bump_wall_force_sensitivities(gpu_lib):
+    case = A.adjoint_case(nc=(64, 24, 4), interpolant="none")
+    h = A.make_handle(case, lib=gpu_lib)
+    q, it, drop, ref = A.converge(h, case["qp"], case["CFL"], tol=1e-10)
+    assert drop <= 1e-10
+    grads, J, n, adrop = A.sensitivities(case, q, it, tol=1e-10, lib=gpu_lib)
+    assert adrop <= 1e-10, (n, adrop)
+    Jf = h.get("Jfaces")
+    for param, step in (("mach", 1e-4), ("angle", 1e-2)):
+        vals = []
+        for sgn in (1, -1):
+            c2 = dict(case)
+            c2[param] = case[param] + sgn * step
+            c2["flow"] = A.bump_flow(c2["mach"], c2["angle"])
+            c2["bc"] = A.bump_bc(c2["mach"])
+            hp = A.make_handle(c2, lib=gpu_lib)
+            qs, _, d2, _ = A.converge(hp, q, case["CFL"], first_iter=it, tol=1e-10, ref=ref)
+            assert d2 <= 1e-10
+            vals.append(A.wall_force(qs, case["ext"], Jf)[0])
+            hp.close()
+        fd = (vals[0] - vals[1]) / (2 * step)
+        assert abs(fd - grads[param]) <= 1e-4 * max(abs(fd), 1e-6 * abs(J)), (param, fd, grads[param])
