@@ -62,7 +62,7 @@ __device__ __forceinline__ void cell_of(int dir, int c, int ta, int tb, int& i, 
 // tangential positions)
 template <typename T>
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, const double* lam,
-                                                       double* bar, int dir) {
+                                                       double* bar, double* bar_face, int dir) {
   using D5 = Dual<T, 5>;
   using D10 = Dual<T, 10>;
   const Dims& d = p.d;
@@ -131,6 +131,28 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
       bx[m] = s;
     }
   }
+  // face metrics {A, nx, ny, nz} (the flux at fixed face states)
+  if (bar_face) {
+    using D4 = Dual<T, 4>;
+    D4 xl[5], xr[5], Fo[NVMAX];
+#pragma unroll
+    for (int l = 0; l < 5; ++l) {
+      xl[l] = D4::cst(qL[l].v);
+      xr[l] = D4::cst(qR[l].v);
+    }
+    const long long fi = fidx(d, dir, i + (dir == 0 ? c : 0), j + (dir == 1 ? c : 0), k + (dir == 2 ? c : 0));
+    const double* fc = b.faces[dir] + 4 * fi;
+    const D4 mask = D4::cst((T)wall_mask(p, dir, c));
+    face_flux<D4>(p, xl, xr, D4::var((T)fc[0], 0), D4::var((T)fc[1], 1), D4::var((T)fc[2], 2),
+                  D4::var((T)fc[3], 3), mask, Fo);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      T s = T(0);
+#pragma unroll
+      for (int l = 0; l < 5; ++l) s += mu[l] * Fo[l].d[m];
+      if (s != T(0)) atomicAdd(bar_face + 4 * fi + m, (double)s);
+    }
+  }
   // face states -> stencil cells
 #pragma unroll
   for (int l = 0; l < 5; ++l)
@@ -168,7 +190,9 @@ __device__ __forceinline__ long long icell_p(const Dims& d, int f, int m, int ta
 // their face computed them from (bc_primitive.f90:160-206 and the
 // procedures it calls, at iteration iter); the ghost entries end at zero
 template <typename T>
-__global__ void __launch_bounds__(TPB_ADJ) k_vjp_ghosts(Params p, DevBlock b, double* bar, int iter) {
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_ghosts(Params p, DevBlock b, double* bar, int iter,
+                                                        double* bf0, double* bf1, double* bf2) {
+  double* bfd[3] = {bf0, bf1, bf2};  // face-metric adjoints (null: not wanted)
   const Dims& d = p.d;
   const int f = blockIdx.z, dir = f / 2;
   const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
@@ -214,32 +238,50 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_ghosts(Params p, DevBlock b, do
       break;
     case -6: {  // slip wall: g = u - 2 (u.fn) fr  ->  bar_u += g_bar - 2 fn (fr.g_bar)
       symm(0); symm(4);
-      const double* fn = b.faces[dir] + 4 * fidx(d, dir, fi, fj, fk);
-      const double* fr = b.faces[0] + 4 * fidx(d, 0, fi, fj, fk);
+      const long long in_n = fidx(d, dir, fi, fj, fk), in_r = fidx(d, 0, fi, fj, fk);
+      const double* fn = b.faces[dir] + 4 * in_n;
+      const double* fr = b.faces[0] + 4 * in_r;
+      double bn[3] = {0, 0, 0}, br[3] = {0, 0, 0};
       for (int L = 1; L <= 3; ++L) {
         const double gu = take(L, 1), gv = take(L, 2), gw = take(L, 3);
         const double s = fr[1] * gu + fr[2] * gv + fr[3] * gw;
         give(L, 1, gu - 2.0 * fn[1] * s);
         give(L, 2, gv - 2.0 * fn[2] * s);
         give(L, 3, gw - 2.0 * fn[3] * s);
+        if (bf0) {  // g = u - 2 (u.fn) fr
+          const long long in = icell_p(d, f, L, ta, tb);
+          const double u[3] = {b.qp[in + P], b.qp[in + 2 * P], b.qp[in + 3 * P]};
+          const double un = u[0] * fn[1] + u[1] * fn[2] + u[2] * fn[3];
+          for (int m = 0; m < 3; ++m) {
+            bn[m] += -2.0 * u[m] * s;
+            br[m] += -2.0 * un * (m == 0 ? gu : m == 1 ? gv : gw);
+          }
+        }
       }
+      if (bf0)
+        for (int m = 0; m < 3; ++m) {
+          if (bn[m] != 0.0) atomicAdd(bfd[dir] + 4 * in_n + 1 + m, bn[m]);
+          if (br[m] != 0.0) atomicAdd(bf0 + 4 * in_r + 1 + m, br[m]);
+        }
     } break;
     case -8:
     case -11: {  // all three layers = riemann_ghost(interior layer 1)
-      using D5 = Dual<T, 5>;
+      using D8 = Dual<T, 8>;  // interior layer 1 (5) and the face normal (3)
       double gs[5];
       for (int l = 0; l < 5; ++l) gs[l] = take(1, l) + take(2, l) + take(3, l);
-      const double* fc = b.faces[dir] + 4 * fidx(d, dir, fi, fj, fk);
+      const long long fnx = fidx(d, dir, fi, fj, fk);
+      const double* fc = b.faces[dir] + 4 * fnx;
       const double sg = (f % 2 == 0) ? -1.0 : 1.0;
       const long long in1 = icell_p(d, f, 1, ta, tb);
-      D5 in[5], g[5];
-      for (int l = 0; l < 5; ++l) in[l] = D5::var((T)b.qp[in1 + P * l], l);
-      riemann_ghost<D5>(p, f, id == -11, D5::cst((T)(sg * fc[1])), D5::cst((T)(sg * fc[2])),
-                        D5::cst((T)(sg * fc[3])), in, g);
-      for (int m = 0; m < 5; ++m) {
+      D8 in[5], g[5];
+      for (int l = 0; l < 5; ++l) in[l] = D8::var((T)b.qp[in1 + P * l], l);
+      riemann_ghost<D8>(p, f, id == -11, D8::var((T)(sg * fc[1]), 5), D8::var((T)(sg * fc[2]), 6),
+                        D8::var((T)(sg * fc[3]), 7), in, g);
+      for (int m = 0; m < 8; ++m) {
         double s = 0.0;
         for (int l = 0; l < 5; ++l) s += gs[l] * (double)g[l].d[m];
-        give(1, m, s);
+        if (m < 5) give(1, m, s);
+        else if (bf0 && s != 0.0) atomicAdd(bfd[dir] + 4 * fnx + 1 + (m - 5), sg * s);
       }
     } break;
     default:
@@ -387,21 +429,115 @@ void launch_adjoint_psi(const Params& p, const DevBlock& b, AdjointWork& w, doub
 }
 
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
-                         double* bar, const Launcher& L) {
+                         double* bar, const Launcher& L, double* const* bar_faces) {
   const Dims& d = p.d;
   cudaMemsetAsync(bar, 0, sizeof(double) * (size_t)d.P * d.nv, L.s);
   for (int dir = 0; dir < 3; ++dir) {
     const int n = extent_of(d, dir);
     const long long nf = (long long)n * ((dir == 0 ? d.jmx : d.imx) - 1) * ((dir == 2 ? d.jmx : d.kmx) - 1);
-    k_vjp_faces<double><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, dir);
+    k_vjp_faces<double><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar,
+                                                          bar_faces ? bar_faces[dir] : nullptr, dir);
     ++*L.count;
   }
   long long wmax = 0;
   for (int dir = 0; dir < 3; ++dir)
     wmax = std::max<long long>(wmax, (long long)((dir == 0 ? d.jmx : d.imx) - 1) *
                                          ((dir == 2 ? d.jmx : d.kmx) - 1));
-  k_vjp_ghosts<double><<<dim3(nblocks(wmax), 1, 6), TPB_ADJ, 0, L.s>>>(p, b, bar, iter);
+  k_vjp_ghosts<double><<<dim3(nblocks(wmax), 1, 6), TPB_ADJ, 0, L.s>>>(
+      p, b, bar, iter, bar_faces ? bar_faces[0] : nullptr, bar_faces ? bar_faces[1] : nullptr,
+      bar_faces ? bar_faces[2] : nullptr);
   ++*L.count;
+}
+
+namespace {
+
+__device__ __forceinline__ long long node_i(const Dims& d, int i, int j, int k) {
+  return 3 * (((long long)(k + 2) * (d.jmx + 6) + (j + 2)) * (d.imx + 6) + (i + 2));
+}
+
+// transpose of the face records {A, n} = {|S|, S/|S|}, S = (d1 x d2)/2 with
+// the diagonals of the face (geometry.f90, as k_face_vectors)
+__global__ void k_vjp_face_vectors(Dims d, const double* nd, const double* faces, const double* bar_face,
+                                   double* bar_nodes, int dir) {
+  const int ni = d.imx + 5 + (dir == 0), nj = d.jmx + 5 + (dir == 1), nk = d.kmx + 5 + (dir == 2);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ni * nj * nk) return;
+  const int i = -2 + (int)(t % ni);
+  const long long r = t / ni;
+  const int j = -2 + (int)(r % nj), k = -2 + (int)(r / nj);
+  const long long fi = fidx(d, dir, i, j, k);
+  const double* g = bar_face + 4 * fi;
+  if (g[0] == 0.0 && g[1] == 0.0 && g[2] == 0.0 && g[3] == 0.0) return;
+  long long a1, a0, b1, b0;
+  if (dir == 0) { a1 = node_i(d, i, j + 1, k + 1); a0 = node_i(d, i, j, k); b1 = node_i(d, i, j, k + 1); b0 = node_i(d, i, j + 1, k); }
+  else if (dir == 1) { a1 = node_i(d, i + 1, j, k + 1); a0 = node_i(d, i, j, k); b1 = node_i(d, i + 1, j, k); b0 = node_i(d, i, j, k + 1); }
+  else { a1 = node_i(d, i + 1, j + 1, k); a0 = node_i(d, i, j, k); b1 = node_i(d, i, j + 1, k); b0 = node_i(d, i + 1, j, k); }
+  double d1[3], d2[3];
+  for (int c = 0; c < 3; ++c) { d1[c] = nd[a1 + c] - nd[a0 + c]; d2[c] = nd[b1 + c] - nd[b0 + c]; }
+  const double* f = faces + 4 * fi;
+  const double A = f[0], n[3] = {f[1], f[2], f[3]};
+  if (A == 0.0) return;
+  // S-bar = A-bar n + (n-bar - n (n . n-bar)) / A
+  const double ndot = n[0] * g[1] + n[1] * g[2] + n[2] * g[3];
+  double sb[3];
+  for (int c = 0; c < 3; ++c) sb[c] = g[0] * n[c] + (g[1 + c] - n[c] * ndot) / A;
+  // S = (d1 x d2)/2: d1-bar = (d2 x S-bar)/2, d2-bar = (S-bar x d1)/2
+  const double d1b[3] = {0.5 * (d2[1] * sb[2] - d2[2] * sb[1]), 0.5 * (d2[2] * sb[0] - d2[0] * sb[2]),
+                         0.5 * (d2[0] * sb[1] - d2[1] * sb[0])};
+  const double d2b[3] = {0.5 * (sb[1] * d1[2] - sb[2] * d1[1]), 0.5 * (sb[2] * d1[0] - sb[0] * d1[2]),
+                         0.5 * (sb[0] * d1[1] - sb[1] * d1[0])};
+  for (int c = 0; c < 3; ++c) {
+    atomicAdd(bar_nodes + a1 + c, d1b[c]);
+    atomicAdd(bar_nodes + a0 + c, -d1b[c]);
+    atomicAdd(bar_nodes + b1 + c, d2b[c]);
+    atomicAdd(bar_nodes + b0 + c, -d2b[c]);
+  }
+}
+
+// transpose of the ghost-node extrapolation of direction dir (grid.f90,
+// as k_ghost_nodes): its statements in reverse order
+__global__ void k_vjp_ghost_nodes(Dims d, double* bn, int dir) {
+  const int n0 = (dir == 0 ? d.jmx : d.imx) + 6, n1 = (dir == 2 ? d.jmx : d.kmx) + 6;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n0 * n1) return;
+  const int a = -2 + (int)(t % n0), b = -2 + (int)(t / n0);
+  const int n = extent_of(d, dir);
+  auto N = [&](int c) -> double* {
+    return bn + (dir == 0 ? node_i(d, c, a, b) : dir == 1 ? node_i(d, a, c, b) : node_i(d, a, b, c));
+  };
+  for (int c = 0; c < 3; ++c) {
+    // N(m) = 2 N(m-1) - N(m-2) etc., undone last statement first
+    auto back = [&](int dst, int s1, int s2) {  // N(dst) = 2 N(s1) - N(s2)
+      const double g = N(dst)[c];
+      N(dst)[c] = 0.0;
+      N(s1)[c] += 2.0 * g;
+      N(s2)[c] -= g;
+    };
+    back(n + 3, n + 2, n + 1);
+    back(n + 2, n + 1, n);
+    back(n + 1, n, n - 1);
+    back(-2, -1, 0);
+    back(-1, 0, 1);
+    back(0, 1, 2);
+  }
+}
+
+}  // namespace
+
+void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_faces, double* bar_nodes,
+                         const Launcher& L) {
+  const Dims& d = p.d;
+  cudaMemsetAsync(bar_nodes, 0, sizeof(double) * 3 * (size_t)(d.imx + 6) * (d.jmx + 6) * (d.kmx + 6), L.s);
+  for (int dir = 0; dir < 3; ++dir) {
+    const long long nf = (long long)(d.imx + 5 + (dir == 0)) * (d.jmx + 5 + (dir == 1)) * (d.kmx + 5 + (dir == 2));
+    k_vjp_face_vectors<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(d, b.nodes, b.faces[dir], bar_faces[dir], bar_nodes, dir);
+    ++*L.count;
+  }
+  for (int dir = 2; dir >= 0; --dir) {
+    const long long n = (long long)((dir == 0 ? d.jmx : d.imx) + 6) * ((dir == 2 ? d.jmx : d.kmx) + 6);
+    k_vjp_ghost_nodes<<<nblocks(n), TPB_ADJ, 0, L.s>>>(d, bar_nodes, dir);
+    ++*L.count;
+  }
 }
 
 }  // namespace fest

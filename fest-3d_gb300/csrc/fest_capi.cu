@@ -661,6 +661,42 @@ int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const 
   return finish(h);
 }
 
+int fest_residual_vjp_nodes(fest_handle* h, const double* qp, int current_iter, const double* lambda,
+                            const double* Ifaces_bar, const double* Jfaces_bar,
+                            const double* Kfaces_bar, double* dq, double* dnodes) {
+  if (!h || !dnodes) return FEST_ERR_ARG;
+  if (!vjp_supported(h->p) || h->p.interp == FEST_INTERP_WENO_NM) return FEST_ERR_ARG;
+  RET(sync_fused(h));
+  Sizes z = sizes_of(h->p.d, h->p.n_grad);
+  if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
+  if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
+  const size_t n0 = h->allocs.size();
+  double *bf[3] = {nullptr, nullptr, nullptr}, *bn = nullptr;
+  int rc = FEST_OK;
+  for (int dir = 0; dir < 3 && !rc; ++dir) rc = dalloc(h, &bf[dir], z.faces[dir]);
+  if (!rc) rc = dalloc(h, &bn, z.nodes);
+  const double* fin[3] = {Ifaces_bar, Jfaces_bar, Kfaces_bar};
+  for (int dir = 0; dir < 3 && !rc; ++dir)
+    if (fin[dir]) rc = up(h, bf[dir], fin[dir], z.faces[dir]);
+  if (!rc && qp) rc = up(h, h->d.qp, qp, z.qp);
+  if (!rc && lambda) rc = up(h, h->d_vjp_lam, lambda, z.res);
+  else if (!rc) rc = cuda_status(cudaMemsetAsync(h->d_vjp_lam, 0, sizeof(double) * z.res, h->s));
+  if (!rc) {
+    launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
+    launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), bf);
+    launch_geometry_vjp(h->p, h->d, bf, bn, h->L());
+    rc = down(h, dnodes, bn, z.nodes);
+  }
+  if (!rc && dq) rc = down(h, dq, h->d_vjp_bar, z.qp);
+  if (!rc) rc = finish(h);
+  cudaStreamSynchronize(h->s);
+  while (h->allocs.size() > n0) {
+    cudaFree(h->allocs.back());
+    h->allocs.pop_back();
+  }
+  return rc;
+}
+
 int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_iters, double tol,
                        double* psi, int* n_done, double* drop) {
   if (!h || !dJdq || max_iters < 0) return FEST_ERR_ARG;

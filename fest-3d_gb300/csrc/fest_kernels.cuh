@@ -65,8 +65,14 @@ void launch_wall_dist(const Params& p, const DevBlock& b, const double* d_wall, 
 // adjoint of the inviscid residual: bar (padded qp layout) = (dR/dq)^T lam
 // (residue layout), ghost cells filled for iteration iter beforehand
 bool vjp_supported(const Params& p);
+// bar_faces (null, or three face-layout arrays, zeroed by the caller) also
+// receive (dR/dfaces)^T lam
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
-                         double* bar, const Launcher& L);
+                         double* bar, const Launcher& L, double* const* bar_faces = nullptr);
+// nodes-layout bar_nodes = (dfaces/dnodes)^T bar_faces, through the face
+// vectors and the ghost-node extrapolation (interior nodes carry the result)
+void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_faces, double* bar_nodes,
+                         const Launcher& L);
 // work arrays of the fixed-point adjoint: phi, dJ, a, b, c, bar in the qp
 // layout, mu in the residue layout, sq one double
 struct AdjointWork {

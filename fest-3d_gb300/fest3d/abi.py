@@ -203,6 +203,7 @@ _SIGS = {
     "fest_profile": [C.c_void_p, C.c_int],
     "fest_profile_read": [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)],
     "fest_residual_vjp": [C.c_void_p, _DP, C.c_int, _DP, _DP],
+    "fest_residual_vjp_nodes": [C.c_void_p, _DP, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP],
     "fest_adjoint_solve": [C.c_void_p, _DP, C.c_double, C.c_int, C.c_double, _DP,
                            C.POINTER(C.c_int), _DP],
     "fest_find_resnorm_noalloc": [C.POINTER(Extent), C.POINTER(Flow), C.c_void_p, C.c_void_p,

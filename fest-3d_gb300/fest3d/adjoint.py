@@ -104,14 +104,49 @@ def residual_param_derivative(case, q, it, param, h_rel=1e-6, lib=None):
     return (out[0] - out[1]) / (2 * step)
 
 
-def sensitivities(case, q, it, params=("mach", "angle"), tol=1e-10, max_iters=200000, lib=None):
-    """dJ/dalpha for each parameter from one adjoint solve at the converged
-    state q; returns ({param: dJ/dalpha}, J, adjoint iterations, drop)."""
+def wall_force_faces_bar(q, ext, Jfaces):
+    """dJ/dJfaces of J = sum p nx A (J-face layout, zero elsewhere)."""
+    bar = np.zeros_like(Jfaces)
+    p = q[3:ext.imx + 2, 3, 3:ext.kmx + 2, 4]
+    bar[0, 3:ext.imx + 2, 3, 3:ext.kmx + 2] = p * Jfaces[1, 3:ext.imx + 2, 3, 3:ext.kmx + 2]
+    bar[1, 3:ext.imx + 2, 3, 3:ext.kmx + 2] = p * Jfaces[0, 3:ext.imx + 2, 3, 3:ext.kmx + 2]
+    return bar
+
+
+def wall_blend(ext):
+    """Weight (1 - t_j) of a lower-wall node displacement at node row j
+    (linear blending to the fixed top wall in the bump grid's j spacing)."""
+    r = 1.02 ** np.arange(ext.jmx - 1)
+    t = np.concatenate([[0.0], np.cumsum(r)])
+    return 1.0 - t / t[-1]
+
+
+def displaced_nodes(case, i, delta):
+    """The bump grid with lower-wall node i (1..imx) moved by delta in y,
+    blended linearly to the top wall."""
+    ext = case["ext"]
+    nodes = np.array(case["nodes"], order="F")
+    nodes[1, i + 2, 3:ext.jmx + 3, 3:ext.kmx + 3] += delta * wall_blend(ext)[:, None]
+    return nodes
+
+
+def sensitivities(case, q, it, params=("mach", "angle"), wall_nodes=(), tol=1e-10,
+                  max_iters=200000, lib=None):
+    """dJ/dalpha for each flow parameter and dJ/d(delta_i) for each listed
+    lower-wall node i from one adjoint solve at the converged state q;
+    returns ({name: derivative}, J, adjoint iterations, drop)."""
     h = make_handle(case, lib=lib)
     h.upload_state(q)
-    J, dJ = wall_force(q, case["ext"], h.get("Jfaces"))
+    Jf = h.get("Jfaces")
+    J, dJ = wall_force(q, case["ext"], Jf)
     psi, n, drop = h.adjoint_solve(dJ, case["CFL"], max_iters, tol)
     grads = {pname: float(np.sum(psi * residual_param_derivative(case, q, it, pname, lib=lib)))
              for pname in params}
+    if len(wall_nodes):
+        ext = case["ext"]
+        dn = h.residual_vjp_nodes(q, it, psi, (None, wall_force_faces_bar(q, ext, Jf), None))
+        wgt = wall_blend(ext)
+        for i in wall_nodes:
+            grads[f"wall_node_{i}"] = float(np.sum(dn[1, i + 2, 3:ext.jmx + 3, 3:ext.kmx + 3] * wgt[:, None]))
     h.close()
     return grads, J, n, drop

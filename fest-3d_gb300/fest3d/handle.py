@@ -122,6 +122,16 @@ class Handle:
         self._call("fest_residual_vjp", abi.ptr(q), int(it), abi.ptr(lam), abi.ptr(dq))
         return dq
 
+    def residual_vjp_nodes(self, qp, it, lam=None, faces_bar=(None, None, None)):
+        """(dR/dnodes)^T lam + (dfaces/dnodes)^T faces_bar (nodes layout)."""
+        q = None if qp is None else np.array(qp, order="F")
+        lam = None if lam is None else np.asfortranarray(lam, dtype=np.float64)
+        fb = [None if f is None else np.asfortranarray(f, dtype=np.float64) for f in faces_bar]
+        dn = np.empty(self.shape["nodes"], order="F")
+        self._call("fest_residual_vjp_nodes", abi.ptr(q), int(it), abi.ptr(lam), abi.ptr(fb[0]),
+                   abi.ptr(fb[1]), abi.ptr(fb[2]), None, abi.ptr(dn))
+        return dn
+
     def adjoint_solve(self, dJdq, CFL, max_iters, tol):
         """psi with (dR/dq)^T psi = -dJ/dq at the device state; returns
         (psi, iterations, drop)."""

@@ -255,6 +255,19 @@ int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
  * FEST_ERR_ARG otherwise. */
 int fest_residual_vjp(fest_handle *h, const double *qp, int current_iter,
                       const double *lambda, double *dq);
+/* No counterpart in the reference.  The same product with respect to the
+ * grid nodes: dnodes = (dR/dnodes)^T lambda + (dfaces/dnodes)^T faces_bar,
+ * through the face metrics of the fluxes and of the BCs (tangency normals,
+ * Riemann normals), the face vectors and the ghost-node extrapolation
+ * (grid.f90:137-236, geometry.f90).  dnodes in the nodes layout (interior
+ * nodes carry the result, ghost nodes zero); lambda and the three
+ * face-layout adjoints *_bar (an objective's explicit metric dependence)
+ * are nullable; dq (nullable) receives fest_residual_vjp's result.  Same
+ * restrictions as fest_residual_vjp, and no WENO_NM (volume weights). */
+int fest_residual_vjp_nodes(fest_handle *h, const double *qp, int current_iter,
+                            const double *lambda, const double *Ifaces_bar,
+                            const double *Jfaces_bar, const double *Kfaces_bar,
+                            double *dq, double *dnodes);
 /* No counterpart in the reference.  Adjoint of the steady residual at the
  * device state (a converged primal, local time steps at CFL): solves
  * (dR/dq)^T psi = -dJ/dq for psi (residue layout) as the fixed point

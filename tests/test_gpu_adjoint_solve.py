@@ -6,8 +6,10 @@ Reduced grid (64x24x4 cells) and the first-order scheme, whose explicit
 iteration converges to a 1e-10 drop within seconds (the second-order
 scheme's explicit iteration needs far longer on this case; its residual
 Jacobian is checked against finite differences in test_gpu_adjoint.py).
-Five primal solves and one adjoint solve, each to a 1e-10 drop; agreement
-to 1e-4 relative."""
+Nine primal solves and one adjoint solve, each to a 1e-10 drop; agreement
+to 1e-4 relative for the inflow Mach number, the inflow angle and two
+lower-wall node displacements (grid deformed by linear blending to the top
+wall)."""
 import numpy as np
 import pytest
 
@@ -21,7 +23,8 @@ def test_bump_wall_force_sensitivities(gpu_lib):
     h = A.make_handle(case, lib=gpu_lib)
     q, it, drop, ref = A.converge(h, case["qp"], case["CFL"], tol=1e-10)
     assert drop <= 1e-10
-    grads, J, n, adrop = A.sensitivities(case, q, it, tol=1e-10, lib=gpu_lib)
+    wall_nodes = (20, 33)  # on the bump's flank and near its crest
+    grads, J, n, adrop = A.sensitivities(case, q, it, wall_nodes=wall_nodes, tol=1e-10, lib=gpu_lib)
     assert adrop <= 1e-10, (n, adrop)
     Jf = h.get("Jfaces")
     for param, step in (("mach", 1e-4), ("angle", 1e-2)):
@@ -38,3 +41,18 @@ def test_bump_wall_force_sensitivities(gpu_lib):
             hp.close()
         fd = (vals[0] - vals[1]) / (2 * step)
         assert abs(fd - grads[param]) <= 1e-4 * max(abs(fd), 1e-6 * abs(J)), (param, fd, grads[param])
+    # lower-wall node displacements (grid deformed by linear blending)
+    for i in wall_nodes:
+        step = 1e-6
+        vals = []
+        for sgn in (1, -1):
+            c2 = dict(case)
+            c2["nodes"] = A.displaced_nodes(case, i, sgn * step)
+            hp = A.make_handle(c2, lib=gpu_lib)
+            qs, _, d2, _ = A.converge(hp, q, case["CFL"], first_iter=it, tol=1e-10, ref=ref)
+            assert d2 <= 1e-10
+            vals.append(A.wall_force(qs, case["ext"], hp.get("Jfaces"))[0])
+            hp.close()
+        fd = (vals[0] - vals[1]) / (2 * step)
+        g = grads[f"wall_node_{i}"]
+        assert abs(fd - g) <= 1e-4 * max(abs(fd), 1e-3 * abs(J)), (i, fd, g)
