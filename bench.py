@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="bump", choices=["bump"])
+    ap.add_argument("--converged", type=int, default=0, metavar="ITERS",
+                    help="instead of the bench line: run FP64 for ITERS iterations, then mixed "
+                         "until its wall Cp is within 1e-5 of FP64's (at most ITERS), and report "
+                         "both wall times")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the 1024x384x64-cell roofline measurement")
     return ap.parse_args()
@@ -243,6 +247,38 @@ def large_block_roofline(lib, abi, cases, Handle, peak, flush, nc=(1024, 384, 64
         return {"error": str(e)}
 
 
+def adjoint_cost(lib, reps=20):
+    """Adjoint/primal cost on the adjoint workload (bump 128x48x4, Euler,
+    unlimited MUSCL + SLAU, FP64): one fest_residual_vjp against one
+    fest_get_total_conservative_residue, both through the C ABI with their
+    host arrays (state in; residual out / lambda in, dq out), wall clock."""
+    import numpy as np
+    from fest3d import adjoint as A
+    try:
+        case = A.adjoint_case()
+        h = A.make_handle(case, lib=lib)
+        q = np.array(case["qp"], order="F")
+        ext = case["ext"]
+        lam = np.asfortranarray(np.random.default_rng(0).standard_normal(
+            (ext.imx - 1, ext.jmx - 1, ext.kmx - 1, 5)))
+        h.residual(q, 3)
+        h.residual_vjp(q, 3, lam)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            h.residual(q, 3)
+        tp = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            h.residual_vjp(q, 3, lam)
+        ta = (time.perf_counter() - t0) / reps
+        h.close()
+        return {"workload": "bump 128x48x4, Euler, MUSCL (unlimited) + SLAU, FP64",
+                "primal_residual_ms": tp * 1e3, "vjp_ms": ta * 1e3, "adjoint_over_primal": ta / tp,
+                "timing": "wall clock per C-ABI call incl. host transfers, mean of %d" % reps}
+    except Exception as e:
+        return {"error": str(e)}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -388,6 +424,8 @@ def run_ours(args):
     e2e_rate = ws * N * STAGES * e2e_steps / tot_e2e / 1e6
     nbytes = int(qhost.nbytes)
 
+    adj = adjoint_cost(lib) if rank == 0 else None
+
     cpu = None
     if rank == 0 and ws == 1:
         v, n_it, threads = cpu_rate(case, seconds=10.0)
@@ -415,6 +453,7 @@ def run_ours(args):
                          "peak_source": peak_kind, "launches_timed": int(nl.value),
                          "avg_launch_us": avg_s * 1e6, "bytes_per_launch": bytes_launch},
             "roofline_large_block": large,
+            "adjoint": adj,
             "clocks": mixed["clocks"],
             "e2e": {"value": e2e_rate, "unit": "Mcell-residuals/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes,
@@ -427,8 +466,65 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_converged(args):
+    """Wall time for the mixed-precision solver to reach, on the bump, the
+    wall Cp of an FP64 run of args.converged iterations to within 1e-5."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    from fest3d import abi, build, cases
+    from fest3d.handle import Handle
+    if not os.path.exists(abi.LIB_PATH):
+        build.build()
+    lib = abi.load()
+    case = cases.bump_case()
+    ext, flow, CFL = case["ext"], case["flow"], case["CFL"]
+    total = args.converged
+
+    def make(prec):
+        h = Handle(ext, flow, case["scheme"], case["bc"], lib=lib)
+        h.setup_geometry(case["nodes"])
+        h.upload_state(case["qp"])
+        h.set_precision(prec)
+        return h
+
+    out = {"mode": "converged wall Cp", "workload": case["name"], "fp64_iters": total}
+    h = make(abi.FEST_FP64)
+    it, t64, hist = 1, 0.0, []
+    while it <= total:
+        n = min(20000, total - it + 1)
+        t0 = time.perf_counter()
+        norm = h.step(n, it, CFL)
+        t64 += time.perf_counter() - t0
+        it += n
+        hist.append([it - 1, float(norm[1])])
+    cp64 = wall_cp(h.download_state(), ext, flow)
+    out.update(fp64_seconds=t64, fp64_residual=hist)
+    h.close()
+    h = make(abi.FEST_MIXED)
+    it, t32, hist, reached = 1, 0.0, [], None
+    while it <= total:
+        n = min(10000, total - it + 1)
+        t0 = time.perf_counter()
+        norm = h.step(n, it, CFL)
+        t32 += time.perf_counter() - t0
+        it += n
+        d = float(np.abs(wall_cp(h.download_state(), ext, flow) - cp64).max())
+        hist.append([it - 1, float(norm[1]), d])
+        if reached is None and d <= 1e-5:
+            reached = {"iters": it - 1, "seconds": t32}
+            break
+    out.update(mixed_residual_and_cp_diff=hist, mixed_reached=reached,
+               mixed_seconds_run=t32,
+               speedup_to_fp64_cp=(t64 / reached["seconds"]) if reached else None)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.converged:
+        run_converged(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
