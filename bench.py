@@ -48,11 +48,16 @@ def parse():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="bump", choices=["bump"])
+    ap.add_argument("--workload", default="bump", choices=["bump", "bump-512x192x16"],
+                    help="bump: the headline 256x96x4 block; bump-512x192x16: the same case on a "
+                         "1.6M-cell block (for profiling the sweep at a size that streams HBM)")
     ap.add_argument("--converged", type=int, default=0, metavar="ITERS",
                     help="instead of the bench line: run FP64 for ITERS iterations, then mixed "
                          "until its wall Cp is within 1e-5 of FP64's (at most ITERS), and report "
                          "both wall times")
+    ap.add_argument("--batch", action="store_true",
+                    help="instead of the bench line: the 96-block batched case, one launch per "
+                         "stage for all blocks against a loop over the blocks' own steps")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the 1024x384x64-cell roofline measurement")
     return ap.parse_args()
@@ -300,7 +305,7 @@ def run_ours(args):
     if not os.path.exists(abi.LIB_PATH):
         build.build()
     lib = abi.load()
-    case = cases.bump_case()
+    case = cases.bump_case() if args.workload == "bump" else cases.bump_case(nc=(512, 192, 16))
     ext, flow, CFL = case["ext"], case["flow"], case["CFL"]
     N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
     STAGES = 3
@@ -520,8 +525,99 @@ def run_converged(args):
     print(json.dumps(out), flush=True)
 
 
+def run_batch(args):
+    """96 seeded blocks (cell dims uniform in [16,160]x[16,96]x[2,16]),
+    inviscid MUSCL + AUSM+, TVD-RK3, mixed precision: Mcell-residuals/s of
+    the batched step (one ghost and one sweep launch per stage for all
+    blocks) against stepping each block through its own handle."""
+    import ctypes as C
+    import torch
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    from fest3d import abi, build, cases
+    from fest3d.handle import Handle
+    if not os.path.exists(abi.LIB_PATH):
+        build.build()
+    lib = abi.load()
+    blocks = cases.batch_blocks()
+    cells = sum(c["cells"] for c in blocks)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def handles():
+        hs = []
+        for c in blocks:
+            h = Handle(c["ext"], c["flow"], c["scheme"], c["bc"], lib=lib)
+            h.setup_geometry(c["nodes"])
+            h.upload_state(c["qp"])
+            h.set_precision(abi.FEST_MIXED)
+            abi.check(lib.fest_set_stream(h.h, C.c_void_p(stream.cuda_stream)), "set_stream")
+            hs.append(h)
+        return hs
+
+    def timed(step, steps, it0):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        torch.cuda.synchronize()
+        it = it0
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            step(it)
+            e1.record(stream)
+            it += 1
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs) / 1e3
+
+    steps, warm = args.steps if args.steps != 2000 else 200, max(args.warmup, 3)
+    out = {"mode": "batched multiblock", "blocks": len(blocks), "cells": cells,
+           "workload": "96 blocks, dims uniform in [16,160]x[16,96]x[2,16] (seed 0), inviscid "
+                       "MUSCL+AUSM+, TVD-RK3, CFL 0.5, periodic/extrapolated faces",
+           "steps": steps, "warmup": warm, "dtype": "f32 stencil / f64 state"}
+    hs = handles()
+    arr = (C.c_void_p * len(hs))(*[h.h.value for h in hs])
+    b = C.c_void_p()
+    abi.check(lib.fest_batch_create(arr, len(hs), C.byref(b)), "batch_create")
+    for it in range(1, warm + 1):
+        abi.check(lib.fest_batch_step_async(b, 1, it, 0.5), "batch warmup")
+    torch.cuda.synchronize()
+    n0 = hs[0].launches
+    tb = timed(lambda it: abi.check(lib.fest_batch_step_async(b, 1, it, 0.5), "batch step"),
+               steps, warm + 1)
+    nb_launch = (hs[0].launches - n0) / steps
+    for h in hs:
+        abi.check(lib.fest_last_device_error(h.h), "device error")
+    out["batched"] = {"mcell_residuals_per_s": 3 * cells * steps / tb / 1e6, "ms_per_step": tb / steps * 1e3,
+                      "launches_per_step": nb_launch}
+    lib.fest_batch_destroy(b)
+    for h in hs:
+        h.close()
+    hs = handles()
+    for it in range(1, warm + 1):
+        for h in hs:
+            abi.check(lib.fest_step_async(h.h, 1, it, 0.5), "loop warmup")
+    torch.cuda.synchronize()
+    n1 = sum(h.launches for h in hs)
+
+    def loop(it):
+        for h in hs:
+            abi.check(lib.fest_step_async(h.h, 1, it, 0.5), "loop step")
+
+    tl = timed(loop, steps, warm + 1)
+    out["per_block_loop"] = {"mcell_residuals_per_s": 3 * cells * steps / tl / 1e6,
+                             "ms_per_step": tl / steps * 1e3,
+                             "launches_per_step": (sum(h.launches for h in hs) - n1) / steps}
+    out["batched_over_loop"] = tl / tb
+    for h in hs:
+        h.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.batch:
+        run_batch(args)
+        return
     if args.converged:
         run_converged(args)
         return

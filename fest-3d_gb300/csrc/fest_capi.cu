@@ -386,6 +386,7 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
 int fest_destroy(fest_handle* h) {
   if (!h) return FEST_OK;
   if (h->s) cudaStreamSynchronize(h->s);
+  cudaGetLastError();  // nothing of this handle's may linger for the next call
   if (h->fused) fused_destroy(h->fused);
   for (void* p : h->allocs) cudaFree(p);
   if (h->own) cudaStreamDestroy(h->own);
@@ -808,6 +809,70 @@ int fest_step(fest_handle* h, int n_iters, int first_iter, double CFL, double* r
 
 int fest_step_async(fest_handle* h, int n_iters, int first_iter, double CFL) {
   return step_enqueue(h, n_iters, first_iter, CFL);
+}
+
+struct fest_batch {
+  std::vector<fest_handle*> h;
+  std::vector<cudaStream_t> prev;  // each handle's stream before the batch
+  FusedBatch* fb = nullptr;
+};
+
+int fest_batch_create(fest_handle* const* blocks, int n_blocks, fest_batch** out) {
+  if (!out) return FEST_ERR_ARG;
+  *out = nullptr;
+  if (!blocks || n_blocks < 1) return FEST_ERR_ARG;
+  fest_handle* h0 = blocks[0];
+  for (int n = 0; n < n_blocks; ++n) {
+    fest_handle* h = blocks[n];
+    if (!h || h->precision != FEST_MIXED || !fused_supported(h->p, FEST_MIXED)) return FEST_ERR_ARG;
+  }
+  std::vector<FusedState*> f;
+  std::vector<Params> p;
+  std::vector<DevBlock> d;
+  fest_batch* b = new fest_batch();
+  int rc = FEST_OK;
+  for (int n = 0; n < n_blocks && !rc; ++n) {
+    fest_handle* h = blocks[n];
+    // one stream for the whole batch: the first block's current one
+    rc = cuda_status(cudaStreamSynchronize(h->s));
+    b->h.push_back(h);
+    b->prev.push_back(h->s);
+    h->s = h0->s;
+    if (!rc && !h->fused) rc = fused_create(h->p, h->d, h->d_table, h->s, &h->fused);
+    f.push_back(h->fused);
+    p.push_back(h->p);
+    d.push_back(h->d);
+  }
+  if (!rc) rc = fused_batch_create(f, p, d, &b->fb);
+  if (rc) {
+    fest_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return FEST_OK;
+}
+
+int fest_batch_destroy(fest_batch* b) {
+  if (!b) return FEST_OK;
+  if (!b->h.empty()) cudaStreamSynchronize(b->h[0]->s);
+  fused_batch_destroy(b->fb);
+  for (size_t n = 0; n < b->h.size(); ++n) b->h[n]->s = b->prev[n];  // handles get their streams back
+  delete b;
+  return FEST_OK;
+}
+
+int fest_batch_step_async(fest_batch* b, int n_iters, int first_iter, double CFL) {
+  if (!b || n_iters < 0) return FEST_ERR_ARG;
+  fest_handle* h0 = b->h[0];
+  for (fest_handle* h : b->h)
+    if (h->s != h0->s || h->precision != FEST_MIXED) return FEST_ERR_ARG;
+  return fused_batch_run(b->fb, n_iters, first_iter, CFL, h0->s, &h0->launches);
+}
+
+int fest_batch_step(fest_batch* b, int n_iters, int first_iter, double CFL) {
+  RET(fest_batch_step_async(b, n_iters, first_iter, CFL));
+  for (fest_handle* h : b->h) RET(finish(h));
+  return FEST_OK;
 }
 
 int fest_set_stream(fest_handle* h, void* stream) {

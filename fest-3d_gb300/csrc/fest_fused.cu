@@ -100,17 +100,10 @@ __device__ __forceinline__ void icell(const Dims& d, int f, int m, int ta, int t
   }
 }
 
-__global__ void __launch_bounds__(128) k_ghosts_mirror(Params p, Mirror M, GhostPlan plan,
-                                                       const float4* F0, const float4* F1,
-                                                       const float4* F2) {
+__device__ __forceinline__ void ghost_mirror_column(const Params& p, const Mirror& M, int f, int ta, int tb,
+                                                    const float4* F0, const float4* F1,
+                                                    const float4* F2) {
   const Dims& d = p.d;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= plan.start[plan.nf]) return;
-  int n = 0;
-  while (t >= plan.start[n + 1]) ++n;
-  const int f = plan.face[n];
-  const long long u = t - plan.start[n];
-  const int ta = 1 + (int)(u % plan.na[n]), tb = 1 + (int)(u / plan.na[n]);
   const int id = p.id[f];
   auto G = [&](int L, int l) -> float& { int i, j, k; gcell(d, f, L, ta, tb, i, j, k); return M.at(i, j, k, l); };
   auto I = [&](int m, int l) -> float { int i, j, k; icell(d, f, m, ta, tb, i, j, k); return M.at(i, j, k, l); };
@@ -220,6 +213,40 @@ __global__ void __launch_bounds__(128) k_ghosts_mirror(Params p, Mirror M, Ghost
   }
 }
 
+__global__ void __launch_bounds__(128) k_ghosts_mirror(Params p, Mirror M, GhostPlan plan,
+                                                       const float4* F0, const float4* F1,
+                                                       const float4* F2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= plan.start[plan.nf]) return;
+  int n = 0;
+  while (t >= plan.start[n + 1]) ++n;
+  const long long u = t - plan.start[n];
+  ghost_mirror_column(p, M, plan.face[n], 1 + (int)(u % plan.na[n]), 1 + (int)(u / plan.na[n]), F0, F1, F2);
+}
+
+// one (block, face) segment of a batched mirror ghost fill
+struct GhostSeg {
+  long long start;  // first thread of the segment
+  int block, face, na;
+  Mirror M;
+  const float4* F[3];
+};
+__global__ void __launch_bounds__(128) k_ghosts_mirror_batch(const Params* ps, const GhostSeg* seg, int nseg,
+                                                             long long total) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  int lo = 0, hi = nseg - 1;  // last segment with start <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (seg[mid].start <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const GhostSeg& g = seg[lo];
+  const long long u = t - g.start;
+  ghost_mirror_column(ps[g.block], g.M, g.face, 1 + (int)(u % g.na), 1 + (int)(u / g.na), g.F[0], g.F[1],
+                      g.F[2]);
+}
+
 unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
@@ -262,12 +289,12 @@ struct FusedState {
 bool fused_supported(const Params& p, int precision) {
   (void)precision;
   // ping-pong buffers keep each stage's ghosts in its own input buffer; BC
-  // sets that read another face's ghosts (thin blocks, -9, two Riemann
-  // faces) need the in-place module path
+  // sets that read another face's ghosts (blocks thinner than a BC's read
+  // depth, -9) need the in-place module path
   // the sweep addresses one plane's stencil with 32-bit offsets
   const bool small_enough = (long long)p.d.P * p.d.nv < (1ll << 31);
   return p.mu_ref == 0.0 && p.turb == FEST_TURB_NONE && p.d.nv == 5 && p.tstep == 'l' &&
-         !ghosts_need_sequential(p) && small_enough;
+         ghost_depth_ok(p) && small_enough;
 }
 
 int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cudaStream_t s,
@@ -444,6 +471,33 @@ static int tune_chunk(FusedState* f, const Params& p, int prec, StageArgs a, con
   return best;
 }
 
+// the arguments of one stage sweep of block f
+static StageArgs stage_args(FusedState* f, const DevBlock& b, bool mixed, int in, int out, int base,
+                            double bA, double bB, double TF, double SF, int TU, int use_rn,
+                            int compute_dt, double CFL, bool last) {
+  StageArgs a;
+  a.qin = f->Q[in];
+  a.qout = f->Q[out];
+  a.qbase = f->Q[base];
+  a.qU = f->Q[f->cur];
+  a.bA = bA; a.bB = bB; a.TF = TF; a.SF = SF; a.TU = TU; a.use_rn = use_rn;
+  a.Rn = b.Rstore; a.dt = b.dt; a.compute_dt = compute_dt; a.CFL = CFL;
+  a.res_out = last ? b.res : nullptr;
+  for (int dir = 0; dir < 3; ++dir) {
+    a.mflux[dir] = last ? b.flux[dir] : nullptr;
+    a.faces[dir] = b.faces[dir];
+  }
+  a.cells = b.cells;
+  a.err = b.err;
+  a.qin32 = mixed ? f->Q32[in] : nullptr;
+  a.qout32 = mixed ? f->Q32[out] : nullptr;
+  for (int dir = 0; dir < 3; ++dir) a.faces32[dir] = mixed ? f->F32[dir] : nullptr;
+  a.vol32 = mixed ? f->V32 : nullptr;
+  a.mpitch = f->mpitch;
+  a.k_chunk = 1;
+  return a;
+}
+
 static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int prec, int in, int out,
                   int base, double bA, double bB, double TF, double SF, int TU, int use_rn,
                   int compute_dt, double CFL, int iter, bool last, cudaStream_t s, long long* cnt) {
@@ -477,25 +531,7 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
     // edge/corner ghosts are never read by an interior update: no averaging
     launch_ghosts(p, bb, f->table[in], iter, L, false);
   }
-  StageArgs a;
-  a.qin = f->Q[in];
-  a.qout = f->Q[out];
-  a.qbase = f->Q[base];
-  a.qU = f->Q[f->cur];
-  a.bA = bA; a.bB = bB; a.TF = TF; a.SF = SF; a.TU = TU; a.use_rn = use_rn;
-  a.Rn = b.Rstore; a.dt = b.dt; a.compute_dt = compute_dt; a.CFL = CFL;
-  a.res_out = last ? b.res : nullptr;
-  for (int dir = 0; dir < 3; ++dir) {
-    a.mflux[dir] = last ? b.flux[dir] : nullptr;
-    a.faces[dir] = b.faces[dir];
-  }
-  a.cells = b.cells;
-  a.err = b.err;
-  a.qin32 = mixed ? f->Q32[in] : nullptr;
-  a.qout32 = mixed ? f->Q32[out] : nullptr;
-  for (int dir = 0; dir < 3; ++dir) a.faces32[dir] = mixed ? f->F32[dir] : nullptr;
-  a.vol32 = mixed ? f->V32 : nullptr;
-  a.mpitch = f->mpitch;
+  StageArgs a = stage_args(f, b, mixed, in, out, base, bA, bB, TF, SF, TU, use_rn, compute_dt, CFL, last);
   const CUtensorMap& tm = mixed ? f->tm[in] : f->tm_none;
   const int nk = p.d.kmx - 1;
   int& kc = f->kc[mixed ? 1 : 0];
@@ -520,11 +556,60 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   ++*cnt;
 }
 
-// one iteration of the integrator (update.f90:129-226) on the stream
+// The stages of one iteration of the integrator (update.f90:129-226) with
+// the current state in buffer U: input, output and base buffers, blend and
+// update factors.  *zero_rn: RK2/RK4 clear their accumulator first.
+struct StageSpec {
+  int in, out, base;
+  double bA, bB, TF, SF;
+  int TU, use_rn, cdt;
+  bool last;
+};
+static int schedule(int integ, int U, bool lastit, StageSpec* st, int* next_cur, bool* zero_rn) {
+  const int A = (U + 1) % 3, B = (U + 2) % 3;
+  *next_cur = U;
+  *zero_rn = false;
+  switch (integ) {
+    case FEST_TIME_NONE:
+      st[0] = {U, A, U, 0, 1, 1., 1., 0, 0, 1, lastit};
+      *next_cur = A;
+      return 1;
+    case FEST_TIME_TVDRK2:
+      st[0] = {U, A, U, 0, 1, 1., 1., 0, 0, 1, false};
+      st[1] = {A, U, A, 0.5, 0.5, 1., 1., 0, 0, 0, lastit};
+      return 2;
+    case FEST_TIME_TVDRK3:
+      st[0] = {U, A, U, 0, 1, 1., 1., 0, 0, 1, false};
+      st[1] = {A, B, A, 0.75, 0.25, 1., 1., 0, 0, 0, false};
+      st[2] = {B, U, B, 1. / 3., 2. / 3., 1., 1., 0, 0, 0, lastit};
+      return 3;
+    case FEST_TIME_RK2:
+      *zero_rn = true;
+      st[0] = {U, A, U, 0, 1, 0.5, 1., 0, 1, 1, false};
+      st[1] = {A, U, U, 0, 1, 0.5, 1., 1, 1, 0, lastit};
+      return 2;
+    case FEST_TIME_RK4:
+      *zero_rn = true;
+      st[0] = {U, A, U, 0, 1, 0.5, 1., 0, 1, 1, false};
+      st[1] = {A, B, U, 0, 1, 0.5, 2., 0, 1, 0, false};
+      st[2] = {B, A, U, 0, 1, 1.0, 2., 0, 1, 0, false};
+      st[3] = {A, U, U, 0, 1, 1. / 6., 1., 1, 1, 0, lastit};
+      return 4;
+    default:
+      return 0;
+  }
+}
+
+// one iteration of the integrator on the stream
 static int enqueue_iteration(FusedState* f, const Params& p, const DevBlock& b, int prec, int it,
                              bool lastit, double CFL, cudaStream_t s, long long* cnt) {
   const bool mixed = prec == FEST_MIXED;
-  const int U = f->cur, A = (U + 1) % 3, B = (U + 2) % 3;
+  const int U = f->cur;
+  StageSpec st[4];
+  int next = U;
+  bool zero_rn = false;
+  const int ns = schedule(p.integ, U, lastit, st, &next, &zero_rn);
+  if (ns == 0) return FEST_ERR_ARG;
   if (it <= 2) {
     // fix() ghosts are written only while current_iter <= 2
     // (bc_primitive.f90:236,318,366) and persist afterwards: every
@@ -541,56 +626,28 @@ static int enqueue_iteration(FusedState* f, const Params& p, const DevBlock& b, 
   const size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
   const bool tvd_early = it <= 2 && (p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3);
   if (tvd_early) cudaMemcpyAsync(f->Us, f->Q[U], bytes, cudaMemcpyDeviceToDevice, s);
-  switch (p.integ) {
-    case FEST_TIME_NONE:
-      run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, lastit, s, cnt);
-      f->cur = A;
-      break;
-    case FEST_TIME_TVDRK2:
-      run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, false, s, cnt);
-      run_stage(f, p, b, prec, A, U, A, 0.5, 0.5, 1., 1., 0, 0, 0, CFL, it, lastit, s, cnt);
-      if (tvd_early) {
-        long long n = p.d.P * p.d.nv;
-        k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
-                                                                 f->mpitch, f->Us, f->Q[A], 0.5, 0.5);
-        ++*cnt;
-      }
-      break;
-    case FEST_TIME_TVDRK3:
-      run_stage(f, p, b, prec, U, A, U, 0, 1, 1., 1., 0, 0, 1, CFL, it, false, s, cnt);
-      run_stage(f, p, b, prec, A, B, A, 0.75, 0.25, 1., 1., 0, 0, 0, CFL, it, false, s, cnt);
-      run_stage(f, p, b, prec, B, U, B, 1. / 3., 2. / 3., 1., 1., 0, 0, 0, CFL, it, lastit, s, cnt);
-      if (tvd_early) {
-        long long n = p.d.P * p.d.nv;
-        k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
-                                                                 f->mpitch, f->Us, f->Q[B], 1. / 3., 2. / 3.);
-        ++*cnt;
-      }
-      break;
-    case FEST_TIME_RK2:
-      cudaMemsetAsync(b.Rstore, 0, sizeof(double) * ncells(p.d) * p.d.nv, s);
-      run_stage(f, p, b, prec, U, A, U, 0, 1, 0.5, 1., 0, 1, 1, CFL, it, false, s, cnt);
-      run_stage(f, p, b, prec, A, U, U, 0, 1, 0.5, 1., 1, 1, 0, CFL, it, lastit, s, cnt);
-      break;
-    case FEST_TIME_RK4:
-      cudaMemsetAsync(b.Rstore, 0, sizeof(double) * ncells(p.d) * p.d.nv, s);
-      run_stage(f, p, b, prec, U, A, U, 0, 1, 0.5, 1., 0, 1, 1, CFL, it, false, s, cnt);
-      run_stage(f, p, b, prec, A, B, U, 0, 1, 0.5, 2., 0, 1, 0, CFL, it, false, s, cnt);
-      run_stage(f, p, b, prec, B, A, U, 0, 1, 1.0, 2., 0, 1, 0, CFL, it, false, s, cnt);
-      run_stage(f, p, b, prec, A, U, U, 0, 1, 1. / 6., 1., 1, 1, 0, CFL, it, lastit, s, cnt);
-      break;
-    default:
-      return FEST_ERR_ARG;
-  }
-  // the blended ghosts must persist in every buffer once fix() stops
-  if (tvd_early)
-    for (int n = 0; n < 3; ++n)
-      if (n != f->cur) {
-        cudaMemcpyAsync(f->Q[n], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
+  if (zero_rn) cudaMemsetAsync(b.Rstore, 0, sizeof(double) * ncells(p.d) * p.d.nv, s);
+  for (int n = 0; n < ns; ++n)
+    run_stage(f, p, b, prec, st[n].in, st[n].out, st[n].base, st[n].bA, st[n].bB, st[n].TF, st[n].SF,
+              st[n].TU, st[n].use_rn, st[n].cdt, CFL, it, st[n].last, s, cnt);
+  f->cur = next;
+  if (tvd_early) {
+    // TVD blends run over the ghosts too (update.f90:203-206): the last
+    // stage's input X, q = bA*Us + bB*X on non-interior cells
+    const StageSpec& z = st[ns - 1];
+    long long n = p.d.P * p.d.nv;
+    k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
+                                                             f->mpitch, f->Us, f->Q[z.in], z.bA, z.bB);
+    ++*cnt;
+    // the blended ghosts must persist in every buffer once fix() stops
+    for (int m = 0; m < 3; ++m)
+      if (m != f->cur) {
+        cudaMemcpyAsync(f->Q[m], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
         if (mixed)
-          cudaMemcpyAsync(f->Q32[n], f->Q32[f->cur], sizeof(float) * (size_t)f->m_elems,
+          cudaMemcpyAsync(f->Q32[m], f->Q32[f->cur], sizeof(float) * (size_t)f->m_elems,
                           cudaMemcpyDeviceToDevice, s);
       }
+  }
   return FEST_OK;
 }
 
@@ -706,4 +763,303 @@ int fused_profile_read(FusedState* f, long long* launches, double* total_ms) {
 
 int fused_export_residual(FusedState* f, const DevBlock&, cudaStream_t) { return f ? FEST_OK : FEST_ERR_ARG; }
 
+
+// ---- batches: every block of a multiblock case in one launch per stage ----
+
+struct FusedBatch {
+  std::vector<FusedState*> f;
+  std::vector<Params> p;
+  std::vector<DevBlock> b;
+  int nb = 0, interp = 0, flux = 0, integ = 0;
+  Params* d_params = nullptr;
+  int kcap = 0;  // k-chunk cap, tuned on the first batched stage
+  struct Table {
+    int stage, cur;
+    bool last;
+    double CFL;
+    int kcap;
+    BatchEntry* d;
+    int ctas;
+  };
+  std::vector<Table> tables;
+  struct GTable {
+    int buf;
+    GhostSeg* d;
+    int nseg;
+    long long total;
+  };
+  std::vector<GTable> gtables;
+  struct Graph {
+    double CFL;
+    bool last;
+    int cur;
+    cudaGraphExec_t exec;
+    int kernels;
+  };
+  std::vector<Graph> graphs;
+  bool use_graphs = true;
+};
+
+static int chunk_of(const Params& p, int kcap) { return std::max(1, std::min(p.d.kmx - 1, kcap)); }
+
+// device table of one stage for every block (built once per key)
+static FusedBatch::Table* batch_table(FusedBatch* B, int stage, const StageSpec& sp, int cur, double CFL,
+                                      int kcap, bool tuning) {
+  if (!tuning)
+    for (auto& t : B->tables)
+      if (t.stage == stage && t.cur == cur && t.last == sp.last && t.CFL == CFL && t.kcap == kcap) return &t;
+  std::vector<BatchEntry> h(B->nb);
+  int cta = 0;
+  for (int n = 0; n < B->nb; ++n) {
+    FusedState* f = B->f[n];
+    const Params& p = B->p[n];
+    BatchEntry& e = h[n];
+    e.tm = f->tm[sp.in];
+    e.p = p;
+    e.a = stage_args(f, B->b[n], true, sp.in, sp.out, sp.base, sp.bA, sp.bB, sp.TF, sp.SF, sp.TU,
+                     sp.use_rn, sp.cdt, CFL, sp.last);
+    e.a.qU = f->Q[cur];
+    const int kc = chunk_of(p, kcap), nk = p.d.kmx - 1;
+    e.a.k_chunk = kc;
+    if (tuning) {  // trial launches: private error word, no accumulator, no norms
+      e.a.use_rn = 0; e.a.TU = 0; e.a.res_out = nullptr;
+      for (int dir = 0; dir < 3; ++dir) e.a.mflux[dir] = nullptr;
+      e.a.err = f->tune_err;
+    }
+    e.tx = (p.d.imx - 1 + IX - 1) / IX;
+    e.ty = (p.d.jmx - 1 + IY - 1) / IY;
+    e.cta0 = cta;
+    cta += e.tx * e.ty * ((nk + kc - 1) / kc);
+  }
+  FusedBatch::Table t{stage, cur, sp.last, CFL, kcap, nullptr, cta};
+  if (cudaMalloc((void**)&t.d, sizeof(BatchEntry) * B->nb) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(t.d, h.data(), sizeof(BatchEntry) * B->nb, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(t.d);
+    return nullptr;
+  }
+  if (tuning) {  // the caller frees it
+    static thread_local FusedBatch::Table tmp;
+    tmp = t;
+    return &tmp;
+  }
+  B->tables.push_back(t);
+  return &B->tables.back();
+}
+
+static FusedBatch::GTable* batch_ghosts(FusedBatch* B, int buf) {
+  for (auto& g : B->gtables)
+    if (g.buf == buf) return &g;
+  std::vector<GhostSeg> h;
+  long long start = 0;
+  for (int n = 0; n < B->nb; ++n) {
+    FusedState* f = B->f[n];
+    const Params& p = B->p[n];
+    for (int fc = 0; fc < 6; ++fc) {
+      if (p.id[fc] == -1) continue;  // fix() only
+      const int dir = fc / 2;
+      const int na = (dir == 0 ? p.d.jmx : p.d.imx) - 1, nb = (dir == 2 ? p.d.jmx : p.d.kmx) - 1;
+      GhostSeg g;
+      g.start = start;
+      g.block = n;
+      g.face = fc;
+      g.na = na;
+      g.M = Mirror{f->Q32[buf], f->mpitch, p.d.nj, p.d.nk, (long long)f->mpitch * p.d.nj * p.d.nk};
+      for (int m = 0; m < 3; ++m) g.F[m] = f->F32[m];
+      h.push_back(g);
+      start += (long long)na * nb;
+    }
+  }
+  FusedBatch::GTable g{buf, nullptr, (int)h.size(), start};
+  if (!h.empty()) {
+    if (cudaMalloc((void**)&g.d, sizeof(GhostSeg) * h.size()) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(g.d, h.data(), sizeof(GhostSeg) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      return nullptr;
+  }
+  B->gtables.push_back(g);
+  return &B->gtables.back();
+}
+
+static int launch_batch(const FusedBatch* B, int ctas, const BatchEntry* e, cudaStream_t s) {
+  switch (B->interp) {
+    case FEST_INTERP_NONE: return launch_batch_none(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+    case FEST_INTERP_MUSCL: return launch_batch_muscl(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+    case FEST_INTERP_PPM: return launch_batch_ppm(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+    case FEST_INTERP_WENO: return launch_batch_weno(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+    default: return launch_batch_weno_nm(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+  }
+}
+
+// The project's tile tuner for batches: the k-chunk cap (planes per CTA)
+// timed on the first batched stage; short chunks give more CTAs, long ones
+// re-read fewer halo planes.  Results do not depend on it.
+static int tune_batch(FusedBatch* B, const StageSpec& sp, int cur, double CFL, cudaStream_t s,
+                      long long* cnt) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = 64;
+  float best_ms = 1e30f;
+  for (int cap : {1, 2, 4, 8, 16, 64}) {
+    FusedBatch::Table* t = batch_table(B, 0, sp, cur, CFL, cap, true);
+    if (!t) break;
+    BatchEntry* d = t->d;
+    const int ctas = t->ctas;
+    launch_batch(B, ctas, d, s);
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; ++r) launch_batch(B, ctas, d, s);
+    cudaEventRecord(e1, s);
+    *cnt += 4;
+    float ms = 0.f;
+    const bool ok = cudaEventSynchronize(e1) == cudaSuccess;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaFree(d);
+    if (!ok) break;
+    if (ms < best_ms) { best_ms = ms; best = cap; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (FusedState* f : B->f) cudaMemsetAsync(f->tune_err, 0, sizeof(int), s);
+  return best;
+}
+
+static int batch_iteration(FusedBatch* B, bool lastit, double CFL, cudaStream_t s, long long* cnt) {
+  const int U = B->f[0]->cur;
+  StageSpec st[4];
+  int next = U;
+  bool zero_rn = false;
+  const int ns = schedule(B->integ, U, lastit, st, &next, &zero_rn);
+  if (ns == 0) return FEST_ERR_ARG;
+  if (zero_rn)
+    for (int n = 0; n < B->nb; ++n)
+      cudaMemsetAsync(B->b[n].Rstore, 0, sizeof(double) * ncells(B->p[n].d) * B->p[n].d.nv, s);
+  for (int k = 0; k < ns; ++k) {
+    FusedBatch::GTable* g = batch_ghosts(B, st[k].in);
+    if (!g) return FEST_ERR_NOMEM;
+    if (g->total > 0) {
+      k_ghosts_mirror_batch<<<(unsigned)((g->total + 127) / 128), 128, 0, s>>>(B->d_params, g->d, g->nseg,
+                                                                                g->total);
+      ++*cnt;
+    }
+    FusedBatch::Table* t = batch_table(B, k, st[k], U, CFL, B->kcap, false);
+    if (!t) return FEST_ERR_NOMEM;
+    int rc = launch_batch(B, t->ctas, t->d, s);
+    if (rc) return rc;
+    ++*cnt;
+  }
+  for (FusedState* f : B->f) f->cur = next;
+  return FEST_OK;
+}
+
+int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Params>& p,
+                       const std::vector<DevBlock>& b, FusedBatch** out) {
+  *out = nullptr;
+  if (f.empty() || f.size() != p.size() || f.size() != b.size()) return FEST_ERR_ARG;
+  for (size_t n = 0; n < f.size(); ++n) {
+    if (!f[n] || !fused_supported(p[n], FEST_MIXED)) return FEST_ERR_ARG;
+    if (p[n].interp != p[0].interp || p[n].flux != p[0].flux || p[n].integ != p[0].integ) return FEST_ERR_ARG;
+  }
+  FusedBatch* B = new FusedBatch();
+  B->f = f;
+  B->p = p;
+  B->b = b;
+  B->nb = (int)f.size();
+  B->interp = p[0].interp;
+  B->flux = p[0].flux;
+  B->integ = p[0].integ;
+  if (cudaMalloc((void**)&B->d_params, sizeof(Params) * B->nb) != cudaSuccess ||
+      cudaMemcpy(B->d_params, p.data(), sizeof(Params) * B->nb, cudaMemcpyHostToDevice) != cudaSuccess) {
+    fused_batch_destroy(B);
+    return FEST_ERR_NOMEM;
+  }
+  *out = B;
+  return FEST_OK;
+}
+
+void fused_batch_destroy(FusedBatch* B) {
+  if (!B) return;
+  for (auto& g : B->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto& t : B->tables) cudaFree(t.d);
+  for (auto& g : B->gtables) cudaFree(g.d);
+  cudaFree(B->d_params);
+  delete B;
+}
+
+int fused_batch_run(FusedBatch* B, int n_iters, int first_iter, double CFL, cudaStream_t s, long long* cnt) {
+  if (!B) return FEST_ERR_ARG;
+  // every block starts from its own state, in the same buffer
+  bool same = true;
+  for (FusedState* f : B->f) same = same && f->seeded && f->cur == B->f[0]->cur;
+  for (int n = 0; n < B->nb; ++n) {
+    FusedState* f = B->f[n];
+    if (!same && f->seeded) fused_export_state(f, B->b[n].qp, s);
+    if (!f->seeded) seed(f, s);
+    int rc = ensure_mirrors(f, B->b[n], s, cnt);
+    if (rc) return rc;
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cap);
+  for (int n = 0; n < n_iters; ++n) {
+    const int it = first_iter + n;
+    const bool lastit = (n == n_iters - 1);
+    if (it <= 2) {  // the early iterations' special ghost handling, block by block
+      for (int m = 0; m < B->nb; ++m) {
+        int rc = enqueue_iteration(B->f[m], B->p[m], B->b[m], FEST_MIXED, it, lastit, CFL, s, cnt);
+        if (rc) return rc;
+      }
+      continue;
+    }
+    if (B->kcap == 0) {
+      if (cap != cudaStreamCaptureStatusNone) return FEST_ERR_ARG;  // tuning synchronises
+      StageSpec st[4];
+      int next;
+      bool z;
+      schedule(B->integ, B->f[0]->cur, false, st, &next, &z);
+      B->kcap = tune_batch(B, st[0], B->f[0]->cur, CFL, s, cnt);
+    }
+    {  // device tables of this iteration exist before any capture (they copy from the host)
+      StageSpec st[4];
+      int next;
+      bool z;
+      const int ns = schedule(B->integ, B->f[0]->cur, lastit, st, &next, &z);
+      for (int k = 0; k < ns; ++k)
+        if (!batch_ghosts(B, st[k].in) || !batch_table(B, k, st[k], B->f[0]->cur, CFL, B->kcap, false))
+          return FEST_ERR_NOMEM;
+    }
+    if (B->use_graphs && cap == cudaStreamCaptureStatusNone) {
+      cudaGraphExec_t exec = nullptr;
+      int kernels = 0;
+      const int cur0 = B->f[0]->cur;
+      for (const auto& g : B->graphs)
+        if (g.CFL == CFL && g.last == lastit && g.cur == cur0) { exec = g.exec; kernels = g.kernels; }
+      if (!exec) {
+        long long k = 0;
+        cudaGraph_t graph = nullptr;
+        bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        int rc = ok ? batch_iteration(B, lastit, CFL, s, &k) : FEST_ERR_CUDA;
+        if (ok) ok = cudaStreamEndCapture(s, &graph) == cudaSuccess && graph && rc == FEST_OK;
+        for (FusedState* f : B->f) f->cur = cur0;
+        if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+        if (graph) cudaGraphDestroy(graph);
+        if (ok) {
+          B->graphs.push_back(FusedBatch::Graph{CFL, lastit, cur0, exec, (int)k});
+          kernels = (int)k;
+        } else {
+          cudaGetLastError();
+          B->use_graphs = false;
+          exec = nullptr;
+        }
+      }
+      if (exec) {
+        if (cudaGraphLaunch(exec, s) != cudaSuccess) return FEST_ERR_CUDA;
+        *cnt += kernels;
+        if (B->integ == FEST_TIME_NONE)
+          for (FusedState* f : B->f) f->cur = (f->cur + 1) % 3;
+        continue;
+      }
+    }
+    int rc = batch_iteration(B, lastit, CFL, s, cnt);
+    if (rc) return rc;
+  }
+  return FEST_OK;
+}
 }  // namespace fest

@@ -2,6 +2,8 @@
 // reconstructs, evaluates fluxes, sums the residual and updates the state,
 // in FP32 (FEST_MIXED) or FP64 arithmetic.
 #pragma once
+#include <vector>
+
 #include "fest_kernels.cuh"
 
 namespace fest {
@@ -23,5 +25,14 @@ void fused_profile(FusedState* f, bool enable);
 int fused_profile_read(FusedState* f, long long* launches, double* total_ms);
 // materialise the last stage's residual and boundary fluxes for find_resnorm
 int fused_export_residual(FusedState* f, const DevBlock& b, cudaStream_t s);
+
+// Blocks of one multiblock case (same reconstruction, flux scheme and
+// integrator, mixed precision) advanced together: per stage one ghost
+// launch and one sweep launch for all blocks.
+struct FusedBatch;
+int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Params>& p,
+                       const std::vector<DevBlock>& b, FusedBatch** out);
+void fused_batch_destroy(FusedBatch* B);
+int fused_batch_run(FusedBatch* B, int n_iters, int first_iter, double CFL, cudaStream_t s, long long* cnt);
 
 }  // namespace fest

@@ -1054,6 +1054,26 @@ bool ghosts_need_sequential(const Params& p) {
   return false;
 }
 
+bool ghost_depth_ok(const Params& p) {
+  // interior layers each face's BC reads at an interior column
+  // (bc_primitive.f90:160-206): copies 1, symmetric copies and tangency 3
+  // (4 with the higher-order ghost term c3), interfaces 3, Riemann 1
+  const int symm = p.c3 != 0.0 ? 4 : 3;
+  for (int f = 0; f < 6; ++f) {
+    const int id = p.id[f];
+    int depth;
+    switch (id) {
+      case -1: depth = 0; break;
+      case -2: case -3: case -4: case -7: case -8: case -11: depth = 1; break;
+      case -5: case -6: depth = symm; break;
+      case -9: return false;
+      default: depth = 3;  // interfaces
+    }
+    if (extent_of(p.d, f / 2) - 1 < depth) return false;
+  }
+  return true;
+}
+
 void launch_ghosts(const Params& p, const DevBlock& b, const BlockRef* tab, int iter,
                    const Launcher& L, bool corners) {
   const Dims& d = p.d;

@@ -57,6 +57,16 @@ struct StageArgs {
   int mpitch;           // row pitch of the state mirror (imx+5 rounded up to 4)
 };
 
+// one block of a batched stage launch (device memory, 64-byte aligned for
+// the tensor map)
+struct BatchEntry {
+  CUtensorMap tm;  // the block's stencil mirror (FP32)
+  Params p;
+  StageArgs a;
+  int cta0;        // first CTA of this block in the batched grid
+  int tx, ty;      // tiles in i and j; k-chunks = CTAs / (tx*ty)
+};
+
 namespace stage {
 
 constexpr int TX = 32, TY = 8;        // threads per CTA
@@ -278,9 +288,12 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
   return true;
 }
 
+// The sweep of one CTA: tile (bx, by) of the block, k-chunk bz.  The
+// single-block kernel passes its block indices; the batched kernel maps its
+// CTA to a block of the batch and a tile of that block.
 template <typename T, int INTERP, int FLUX>
-__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
-    k_stage(Params p, StageArgs a, const __grid_constant__ CUtensorMap tm) {
+__device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, const CUtensorMap* tmp,
+                                           int bx, int by, int bz) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   constexpr int NV = 5;
   constexpr int RW = RingGeom<T>::W, NR = RingGeom<T>::N;
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
   __shared__ int abort_flag;
   const Dims& d = p.d;
   const int lane = threadIdx.x, w = threadIdx.y, tid = w * TX + lane;
-  const int ib = 1 + IX * blockIdx.x, jb = 1 + IY * blockIdx.y;
+  const int ib = 1 + IX * bx, jb = 1 + IY * by;
   const int i = ib - 1 + lane, j = jb - 1 + w;
   const int i0 = ib - 3, j0 = jb - 3;  // stencil plane origin (col 0, row 0)
   const bool in_i = lane >= 1 && lane <= IX && i <= d.imx - 1;
@@ -301,13 +314,13 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
   const int plane = NV * SH * RW;
   const T gm = (T)p.gm;
   // FP32: the TMA box starts ox columns left of the tile's stencil origin
-  const int ox = kTma ? ((IX * (int)blockIdx.x) & 3) : 0;
+  const int ox = kTma ? ((IX * bx) & 3) : 0;
   const bool thin = d.kmx == 2;
 
   // clamp to the padded block so halo lanes past the edge stay finite
   auto clampi = [&](int x, int hi) { return x < -2 ? -2 : (x > hi + 2 ? hi + 2 : x); };
 
-  const int k0 = 1 + a.k_chunk * blockIdx.z;
+  const int k0 = 1 + a.k_chunk * bz;
   const int k1 = min(k0 + a.k_chunk - 1, d.kmx - 1);
   const int base = k0 - 3;                 // first plane of the chunk's march
   const int nplanes = (k1 + 3) - base + 1;
@@ -343,7 +356,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
   constexpr uint32_t kPlaneBytes = (uint32_t)(NV * SH * RW * sizeof(T));
   auto issue = [&](int c) {
     fence_proxy_async();  // earlier generic reads of the slot come first
-    tma_load_4d(ring + slot(c) * plane, &tm, IX * (int)blockIdx.x - ox, IY * (int)blockIdx.y, c + 2, 0,
+    tma_load_4d(ring + slot(c) * plane, tmp, IX * bx - ox, IY * by, c + 2, 0,
                 bars + slot(c), kPlaneBytes);
   };
   if constexpr (kTma) {
@@ -530,6 +543,45 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
   }
 }
 
+template <typename T, int INTERP, int FLUX>
+__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
+    k_stage(Params p, StageArgs a, const __grid_constant__ CUtensorMap tm) {
+  stage_body<T, INTERP, FLUX>(p, a, &tm, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// One launch for every block of a batch: block b owns CTAs
+// [cta0, cta0 + tx*ty*nz) of the 1-D grid.
+template <typename T, int INTERP, int FLUX>
+__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
+    k_stage_batch(const BatchEntry* e, int nb) {
+  __shared__ Params sp;
+  __shared__ StageArgs sa;
+  __shared__ int sb;
+  const int tid = threadIdx.y * TX + threadIdx.x;
+  if (tid == 0) {
+    int lo = 0, hi = nb - 1;  // last entry with cta0 <= blockIdx.x
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (e[mid].cta0 <= (int)blockIdx.x) lo = mid;
+      else hi = mid - 1;
+    }
+    sb = lo;
+  }
+  __syncthreads();
+  const BatchEntry& E = e[sb];
+  {
+    const int* src = reinterpret_cast<const int*>(&E.p);
+    int* dst = reinterpret_cast<int*>(&sp);
+    for (int n = tid; n < (int)(sizeof(Params) / 4); n += TX * TY) dst[n] = src[n];
+    src = reinterpret_cast<const int*>(&E.a);
+    dst = reinterpret_cast<int*>(&sa);
+    for (int n = tid; n < (int)(sizeof(StageArgs) / 4); n += TX * TY) dst[n] = src[n];
+  }
+  __syncthreads();
+  const int local = (int)blockIdx.x - E.cta0;
+  stage_body<T, INTERP, FLUX>(sp, sa, &E.tm, local % E.tx, (local / E.tx) % E.ty, local / (E.tx * E.ty));
+}
+
 template <typename T> inline size_t stage_smem() {
   return sizeof(T) * ((size_t)RingGeom<T>::N * 5 * SH * RingGeom<T>::W + 2 * 5 * TY * TX + TY * TX) +
          sizeof(uint64_t) * RingGeom<T>::N + 16;
@@ -547,6 +599,14 @@ FEST_STAGE_LAUNCHER(launch_stage_muscl);
 FEST_STAGE_LAUNCHER(launch_stage_ppm);
 FEST_STAGE_LAUNCHER(launch_stage_weno);
 FEST_STAGE_LAUNCHER(launch_stage_weno_nm);
+// batched: every block of the batch in one launch of `ctas` CTAs
+#define FEST_BATCH_LAUNCHER(name) \
+  int name(int prec, int flux, int ctas, cudaStream_t s, const BatchEntry* e, int nb)
+FEST_BATCH_LAUNCHER(launch_batch_none);
+FEST_BATCH_LAUNCHER(launch_batch_muscl);
+FEST_BATCH_LAUNCHER(launch_batch_ppm);
+FEST_BATCH_LAUNCHER(launch_batch_weno);
+FEST_BATCH_LAUNCHER(launch_batch_weno_nm);
 
 template <int INTERP>
 int launch_stage_t(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a,
@@ -586,6 +646,35 @@ int launch_stage_t(int prec, int flux, dim3 grid, cudaStream_t s, const Params& 
       case 5: FEST_GO(double, 5); break;
       default: return FEST_ERR_ARG;
     }
+  }
+#undef FEST_GO
+  return FEST_OK;
+}
+
+template <int INTERP>
+int launch_batch_t(int prec, int flux, int ctas, cudaStream_t s, const BatchEntry* e, int nb) {
+  using namespace stage;
+  const dim3 blk(TX, TY);
+  static bool attrs = false;
+#define FEST_SET(T, F)                                                                           \
+  cudaFuncSetAttribute(k_stage_batch<T, INTERP, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)stage_smem<T>())
+  if (!attrs) {
+    FEST_SET(float, 0); FEST_SET(float, 1); FEST_SET(float, 2);
+    FEST_SET(float, 3); FEST_SET(float, 4); FEST_SET(float, 5);
+    attrs = true;
+  }
+#undef FEST_SET
+  if (prec != FEST_MIXED) return FEST_ERR_ARG;  // batches run the FP32 sweep
+#define FEST_GO(F) k_stage_batch<float, INTERP, F><<<ctas, blk, stage_smem<float>(), s>>>(e, nb)
+  switch (flux) {
+    case 0: FEST_GO(0); break;
+    case 1: FEST_GO(1); break;
+    case 2: FEST_GO(2); break;
+    case 3: FEST_GO(3); break;
+    case 4: FEST_GO(4); break;
+    case 5: FEST_GO(5); break;
+    default: return FEST_ERR_ARG;
   }
 #undef FEST_GO
   return FEST_OK;

@@ -202,6 +202,10 @@ _SIGS = {
     "fest_set_stream": [C.c_void_p, C.c_void_p],
     "fest_profile": [C.c_void_p, C.c_int],
     "fest_profile_read": [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)],
+    "fest_batch_create": [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)],
+    "fest_batch_destroy": [C.c_void_p],
+    "fest_batch_step": [C.c_void_p, C.c_int, C.c_int, C.c_double],
+    "fest_batch_step_async": [C.c_void_p, C.c_int, C.c_int, C.c_double],
     "fest_residual_vjp": [C.c_void_p, _DP, C.c_int, _DP, _DP],
     "fest_residual_vjp_nodes": [C.c_void_p, _DP, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP],
     "fest_adjoint_solve": [C.c_void_p, _DP, C.c_double, C.c_int, C.c_double, _DP,

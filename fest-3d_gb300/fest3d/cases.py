@@ -93,7 +93,8 @@ def uniform_state(ext, flow, tk=0.0, tw=0.0):
     return qp
 
 
-def random_state(ext, seed=0, mach=0.3, amp=0.1, p0=101325.0, rho0=1.2, tk=1.0, tw=1000.0):
+def random_state(ext, seed=0, mach=0.3, amp=0.1, p0=101325.0, rho0=1.2, tk=1.0, tw=1000.0,
+                 rho_amp=None):
     """Smooth 3-mode Fourier field over the padded block: rho in
     rho0*(1 +- amp), |u| up to mach*c, p0*(1 +- amp), positive tk/tw."""
     rng = np.random.default_rng(seed)
@@ -112,7 +113,7 @@ def random_state(ext, seed=0, mach=0.3, amp=0.1, p0=101325.0, rho0=1.2, tk=1.0, 
 
     c = np.sqrt(1.4 * p0 / rho0)
     qp = abi.farray(ext, "qp")
-    qp[..., 0] = rho0 * (1 + amp * field())
+    qp[..., 0] = rho0 * (1 + (amp if rho_amp is None else rho_amp) * field())
     for l in (1, 2, 3):
         qp[..., l] = mach * c * field()
     qp[..., 4] = p0 * (1 + amp * field())
@@ -163,7 +164,7 @@ def bump_case(nc=(256, 96, 4), mach=0.5):
     bc = abi.make_bc([-11, -4, -6, -6, -10, -10], partners={4: (0, 5), 5: (0, 4)}, **fixed)
     nodes = bump_nodes(ext)
     qp = uniform_state(ext, flow)
-    return dict(name="smooth bump 256x96x4, WENO5+SLAU, inviscid, TVD-RK3", ext=ext, flow=flow,
+    return dict(name=f"smooth bump {nc[0]}x{nc[1]}x{nc[2]}, WENO5+SLAU, inviscid, TVD-RK3", ext=ext, flow=flow,
                 scheme=scheme, bc=bc, nodes=nodes, qp=qp, CFL=0.8)
 
 
@@ -216,3 +217,38 @@ def wall_nodes_of(nodes, ext, bc):
                 for i in range(i0, i1 + 1):
                     pts.append(nodes[:, i + 2, j + 2, k + 2])
     return np.array(pts, dtype=np.float64)
+
+
+def batch_blocks(n=96, seed=0, dims_lo=(16, 16, 2), dims_hi=(160, 96, 16), mach=0.8,
+                 scheme_name="ausmP", interpolant="muscl", integrator="TVDRK3"):
+    """Independent blocks of a batched multiblock case: cell dimensions drawn
+    uniformly from [16,160]x[16,96]x[2,16] (numpy default_rng(seed)),
+    Cartesian grids with a sinusoidal node perturbation of 5% of the local
+    spacing, smooth random fields (rho in [0.9,1.3], velocity components up
+    to Mach 0.8 from 3 Fourier modes, p = 101325 +- 10%).  Each direction is
+    periodic (a self-paired interface, when the block has >= 4 cells there)
+    or extrapolated (-2: ghost = first interior cell), by a fair coin.
+    Inviscid MUSCL + AUSM+ with TVD-RK3, CFL 0.5."""
+    rng = np.random.default_rng(seed)
+    out = []
+    c = np.sqrt(1.4 * 101325.0 / 1.1)
+    for b in range(n):
+        nc = [int(rng.integers(lo, hi + 1)) for lo, hi in zip(dims_lo, dims_hi)]
+        ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 5)
+        ids, partners = [], {}
+        for d in range(3):
+            periodic = nc[d] >= 4 and rng.random() < 0.5
+            ids += [-10, -10] if periodic else [-2, -2]
+            if periodic:
+                partners[2 * d] = (0, 2 * d + 1)
+                partners[2 * d + 1] = (0, 2 * d)
+        bc = abi.make_bc(ids, partners=partners)
+        flow = abi.make_flow(density_inf=1.1, x_speed_inf=0.3 * c, pressure_inf=101325.0, mu_ref=0.0)
+        scheme = abi.make_scheme(scheme_name=scheme_name, interpolant=interpolant,
+                                 time_step_accuracy=integrator, time_stepping_method="l")
+        h = 1.0 / 64
+        nodes = box_nodes(ext, L=(nc[0] * h, nc[1] * h, nc[2] * h), perturb=0.05, seed=seed * 1000 + b)
+        qp = random_state(ext, seed=seed * 1000 + b + 7, mach=mach, amp=0.1, p0=101325.0, rho0=1.1,
+                          rho_amp=0.2 / 1.1)
+        out.append(dict(ext=ext, flow=flow, scheme=scheme, bc=bc, nodes=nodes, qp=qp, CFL=0.5, cells=int(np.prod(nc))))
+    return out

@@ -243,6 +243,24 @@ int fest_set_stream(fest_handle *h, void *cuda_stream);
 int fest_profile(fest_handle *h, int enable);
 int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
 
+/* ---- batches ------------------------------------------------------------- */
+/* No counterpart in the reference (its blocks advance one MPI rank each).
+ * The blocks of a multiblock case advanced together: per RK stage one ghost
+ * launch and one sweep launch cover every block.  All handles must use
+ * FEST_MIXED and the fused path's schemes, with the same reconstruction,
+ * flux scheme and integrator; their geometry and state are set through the
+ * handles as usual.  fest_batch_create moves every handle onto the first
+ * handle's current stream and fest_batch_destroy gives each its own stream
+ * back: destroy the batch before any of its handles.  Each handle still
+ * answers fest_find_resnorm, fest_download_state etc. for its block. */
+typedef struct fest_batch fest_batch;
+int fest_batch_create(fest_handle *const *blocks, int n_blocks, fest_batch **out);
+int fest_batch_destroy(fest_batch *b);
+/* n_iters iterations of every block from iteration number first_iter;
+ * _async returns after enqueueing on the batch's stream */
+int fest_batch_step(fest_batch *b, int n_iters, int first_iter, double CFL);
+int fest_batch_step_async(fest_batch *b, int n_iters, int first_iter, double CFL);
+
 /* ---- adjoint ------------------------------------------------------------- */
 /* No counterpart in the reference.  Reverse-mode product with the
  * transposed Jacobian of the residual that fest_get_total_conservative_residue
