@@ -264,6 +264,7 @@ struct FusedState {
   float* V32 = nullptr;
   bool mirror_valid = false;  // Q32 interiors match Q
   int kc[2] = {0, 0};         // tuned k-chunk per precision (0: not tuned yet)
+  int occ[2] = {1, 2};        // tuned register budget (CTAs per SM) per precision
   int mpitch = 0;             // row pitch of Q32
   long long m_elems = 0;      // floats per Q32 buffer
   CUtensorMap tm[3];          // TMA descriptors of Q32[0..2]
@@ -417,14 +418,14 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
   return FEST_OK;
 }
 
-static void launch_sweep(const Params& p, int prec, dim3 grid, cudaStream_t s, const StageArgs& a,
+static void launch_sweep(const Params& p, int prec, int occ, dim3 grid, cudaStream_t s, const StageArgs& a,
                          const CUtensorMap& tm) {
   switch (p.interp) {
-    case FEST_INTERP_NONE: launch_stage_none(prec, p.flux, grid, s, p, a, tm); break;
-    case FEST_INTERP_MUSCL: launch_stage_muscl(prec, p.flux, grid, s, p, a, tm); break;
-    case FEST_INTERP_PPM: launch_stage_ppm(prec, p.flux, grid, s, p, a, tm); break;
-    case FEST_INTERP_WENO: launch_stage_weno(prec, p.flux, grid, s, p, a, tm); break;
-    default: launch_stage_weno_nm(prec, p.flux, grid, s, p, a, tm); break;
+    case FEST_INTERP_NONE: launch_stage_none(prec, p.flux, occ, grid, s, p, a, tm); break;
+    case FEST_INTERP_MUSCL: launch_stage_muscl(prec, p.flux, occ, grid, s, p, a, tm); break;
+    case FEST_INTERP_PPM: launch_stage_ppm(prec, p.flux, occ, grid, s, p, a, tm); break;
+    case FEST_INTERP_WENO: launch_stage_weno(prec, p.flux, occ, grid, s, p, a, tm); break;
+    default: launch_stage_weno_nm(prec, p.flux, occ, grid, s, p, a, tm); break;
   }
 }
 
@@ -434,7 +435,7 @@ static void launch_sweep(const Params& p, int prec, dim3 grid, cudaStream_t s, c
 // (rewritten by the real launch) and a private error word; the RK
 // accumulator is left alone.  Chunking does not change any result.
 static int tune_chunk(FusedState* f, const Params& p, int prec, StageArgs a, const CUtensorMap& tm,
-                      cudaStream_t s, long long* cnt) {
+                      cudaStream_t s, long long* cnt, int* occ_out) {
   const int nk = p.d.kmx - 1;
   const dim3 g0((p.d.imx - 1 + IX - 1) / IX, (p.d.jmx - 1 + IY - 1) / IY, 1);
   a.use_rn = 0; a.TU = 0; a.res_out = nullptr;
@@ -444,27 +445,32 @@ static int tune_chunk(FusedState* f, const Params& p, int prec, StageArgs a, con
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  int best = nk, last_chunks = -1;
+  int best = nk, best_occ = prec == FEST_MIXED ? 2 : 1;
   float best_ms = 1e30f;
-  for (int kc : cand) {
-    if (kc > nk) kc = nk;
-    const int chunks = (nk + kc - 1) / kc;
-    if (chunks == last_chunks) continue;
-    last_chunks = chunks;
-    a.k_chunk = (nk + chunks - 1) / chunks;
-    dim3 g = g0;
-    g.z = chunks;
-    launch_sweep(p, prec, g, s, a, tm);  // warm-up
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < 3; ++r) launch_sweep(p, prec, g, s, a, tm);
-    cudaEventRecord(e1, s);
-    *cnt += 4;
-    float ms = 0.f;
-    if (cudaEventSynchronize(e1) != cudaSuccess) break;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best_ms) { best_ms = ms; best = a.k_chunk; }
-    if (chunks == 1) break;
+  for (int occ : {2, 3}) {
+    if (prec != FEST_MIXED && occ == 3) break;  // FP64 has one variant
+    int last_chunks = -1;
+    for (int kc : cand) {
+      if (kc > nk) kc = nk;
+      const int chunks = (nk + kc - 1) / kc;
+      if (chunks == last_chunks) continue;
+      last_chunks = chunks;
+      a.k_chunk = (nk + chunks - 1) / chunks;
+      dim3 g = g0;
+      g.z = chunks;
+      launch_sweep(p, prec, occ, g, s, a, tm);  // warm-up
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < 3; ++r) launch_sweep(p, prec, occ, g, s, a, tm);
+      cudaEventRecord(e1, s);
+      *cnt += 4;
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess) break;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best_ms) { best_ms = ms; best = a.k_chunk; best_occ = occ; }
+      if (chunks == 1) break;
+    }
   }
+  *occ_out = best_occ;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaMemsetAsync(f->tune_err, 0, sizeof(int), s);
@@ -535,7 +541,8 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   const CUtensorMap& tm = mixed ? f->tm[in] : f->tm_none;
   const int nk = p.d.kmx - 1;
   int& kc = f->kc[mixed ? 1 : 0];
-  if (kc == 0) kc = tune_chunk(f, p, prec, a, tm, s, cnt);
+  int& occ = f->occ[mixed ? 1 : 0];
+  if (kc == 0) kc = tune_chunk(f, p, prec, a, tm, s, cnt, &occ);
   a.k_chunk = kc;
   const int chunks = (nk + kc - 1) / kc;
   dim3 grid((p.d.imx - 1 + IX - 1) / IX, (p.d.jmx - 1 + IY - 1) / IY, chunks);
@@ -548,7 +555,7 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
       }
     cudaEventRecord(f->ev[f->nev], s);
   }
-  launch_sweep(p, prec, grid, s, a, tm);
+  launch_sweep(p, prec, occ, grid, s, a, tm);
   if (f->profiling) {
     cudaEventRecord(f->ev[f->nev + 1], s);
     f->nev += 2;

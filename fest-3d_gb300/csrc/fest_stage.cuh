@@ -543,8 +543,11 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
   }
 }
 
-template <typename T, int INTERP, int FLUX>
-__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
+// MB: CTAs per SM the registers are budgeted for (FP32: 2 = 115 registers,
+// no spills, fewer instructions; 3 = 80 registers, more warps to hide
+// latency on large blocks; the tuner picks per block)
+template <typename T, int INTERP, int FLUX, int MB>
+__global__ void __launch_bounds__(TX* TY, MB)
     k_stage(Params p, StageArgs a, const __grid_constant__ CUtensorMap tm) {
   stage_body<T, INTERP, FLUX>(p, a, &tm, blockIdx.x, blockIdx.y, blockIdx.z);
 }
@@ -552,7 +555,7 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
 // One launch for every block of a batch: block b owns CTAs
 // [cta0, cta0 + tx*ty*nz) of the 1-D grid.
 template <typename T, int INTERP, int FLUX>
-__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 3 : 1)
     k_stage_batch(const BatchEntry* e, int nb) {
   __shared__ Params sp;
   __shared__ StageArgs sa;
@@ -592,7 +595,7 @@ template <typename T> inline size_t stage_smem() {
 
 // one host launcher per reconstruction (fest_stage_<method>.cu)
 #define FEST_STAGE_LAUNCHER(name)                                                         \
-  int name(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a, \
+  int name(int prec, int flux, int occ, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a, \
            const CUtensorMap& tm)
 FEST_STAGE_LAUNCHER(launch_stage_none);
 FEST_STAGE_LAUNCHER(launch_stage_muscl);
@@ -609,44 +612,42 @@ FEST_BATCH_LAUNCHER(launch_batch_weno);
 FEST_BATCH_LAUNCHER(launch_batch_weno_nm);
 
 template <int INTERP>
-int launch_stage_t(int prec, int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a,
-                   const CUtensorMap& tm) {
+int launch_stage_t(int prec, int flux, int occ, dim3 grid, cudaStream_t s, const Params& p,
+                   const StageArgs& a, const CUtensorMap& tm) {
   using namespace stage;
   const dim3 blk(TX, TY);
   static bool attrs = false;
-#define FEST_SET(T, F)                                                                     \
-  cudaFuncSetAttribute(k_stage<T, INTERP, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+#define FEST_SET(T, F, MB)                                                                     \
+  cudaFuncSetAttribute(k_stage<T, INTERP, F, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                        (int)stage_smem<T>())
   if (!attrs) {
-    FEST_SET(float, 0); FEST_SET(float, 1); FEST_SET(float, 2);
-    FEST_SET(float, 3); FEST_SET(float, 4); FEST_SET(float, 5);
-    FEST_SET(double, 0); FEST_SET(double, 1); FEST_SET(double, 2);
-    FEST_SET(double, 3); FEST_SET(double, 4); FEST_SET(double, 5);
+    FEST_SET(float, 0, 2); FEST_SET(float, 1, 2); FEST_SET(float, 2, 2);
+    FEST_SET(float, 3, 2); FEST_SET(float, 4, 2); FEST_SET(float, 5, 2);
+    FEST_SET(float, 0, 3); FEST_SET(float, 1, 3); FEST_SET(float, 2, 3);
+    FEST_SET(float, 3, 3); FEST_SET(float, 4, 3); FEST_SET(float, 5, 3);
+    FEST_SET(double, 0, 1); FEST_SET(double, 1, 1); FEST_SET(double, 2, 1);
+    FEST_SET(double, 3, 1); FEST_SET(double, 4, 1); FEST_SET(double, 5, 1);
     attrs = true;
   }
 #undef FEST_SET
-#define FEST_GO(T, F) k_stage<T, INTERP, F><<<grid, blk, stage_smem<T>(), s>>>(p, a, tm)
-  if (prec == FEST_MIXED) {
-    switch (flux) {
-      case 0: FEST_GO(float, 0); break;
-      case 1: FEST_GO(float, 1); break;
-      case 2: FEST_GO(float, 2); break;
-      case 3: FEST_GO(float, 3); break;
-      case 4: FEST_GO(float, 4); break;
-      case 5: FEST_GO(float, 5); break;
-      default: return FEST_ERR_ARG;
-    }
-  } else {
-    switch (flux) {
-      case 0: FEST_GO(double, 0); break;
-      case 1: FEST_GO(double, 1); break;
-      case 2: FEST_GO(double, 2); break;
-      case 3: FEST_GO(double, 3); break;
-      case 4: FEST_GO(double, 4); break;
-      case 5: FEST_GO(double, 5); break;
-      default: return FEST_ERR_ARG;
-    }
+#define FEST_GO(T, F, MB) k_stage<T, INTERP, F, MB><<<grid, blk, stage_smem<T>(), s>>>(p, a, tm)
+#define FEST_FLUXES(T, MB)                 \
+  switch (flux) {                          \
+    case 0: FEST_GO(T, 0, MB); break;      \
+    case 1: FEST_GO(T, 1, MB); break;      \
+    case 2: FEST_GO(T, 2, MB); break;      \
+    case 3: FEST_GO(T, 3, MB); break;      \
+    case 4: FEST_GO(T, 4, MB); break;      \
+    case 5: FEST_GO(T, 5, MB); break;      \
+    default: return FEST_ERR_ARG;          \
   }
+  if (prec == FEST_MIXED) {
+    if (occ >= 3) { FEST_FLUXES(float, 3) }
+    else { FEST_FLUXES(float, 2) }
+  } else {
+    FEST_FLUXES(double, 1)
+  }
+#undef FEST_FLUXES
 #undef FEST_GO
   return FEST_OK;
 }

@@ -3,6 +3,6 @@
 #include "fest_stage.cuh"
 
 namespace fest {
-FEST_STAGE_LAUNCHER(launch_stage_weno) { return launch_stage_t<FEST_INTERP_WENO>(prec, flux, grid, s, p, a, tm); }
+FEST_STAGE_LAUNCHER(launch_stage_weno) { return launch_stage_t<FEST_INTERP_WENO>(prec, flux, occ, grid, s, p, a, tm); }
 FEST_BATCH_LAUNCHER(launch_batch_weno) { return launch_batch_t<FEST_INTERP_WENO>(prec, flux, ctas, s, e, nb); }
 }  // namespace fest

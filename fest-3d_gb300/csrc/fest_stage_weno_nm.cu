@@ -3,6 +3,6 @@
 #include "fest_stage.cuh"
 
 namespace fest {
-FEST_STAGE_LAUNCHER(launch_stage_weno_nm) { return launch_stage_t<FEST_INTERP_WENO_NM>(prec, flux, grid, s, p, a, tm); }
+FEST_STAGE_LAUNCHER(launch_stage_weno_nm) { return launch_stage_t<FEST_INTERP_WENO_NM>(prec, flux, occ, grid, s, p, a, tm); }
 FEST_BATCH_LAUNCHER(launch_batch_weno_nm) { return launch_batch_t<FEST_INTERP_WENO_NM>(prec, flux, ctas, s, e, nb); }
 }  // namespace fest
