@@ -272,12 +272,13 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
   const float u2 = u + du, v2 = v + dv, w2 = w + dw;
   const float dp = gm1 * (-dE + 0.5f * dr * (u2 * u2 + v2 * v2 + w2 * w2) -
                           0.5f * rho * (2.0f * (u * du + v * dv + w * dw) + du * du + dv * dv + dw * dw));
-  double out[5] = {b64[0] - (double)dr, b64[1] + (double)du, b64[2] + (double)dv, b64[3] + (double)dw,
-                   b64[4] + (double)dp};
-  bool bad = (out[0] < 0.) || (out[4] < 0.);
-#pragma unroll
-  for (int l = 0; l < 5; ++l) bad |= (out[l] != out[l]);
-  if (bad) return false;
+  // negative or NaN density/pressure after the update (update.f90:448),
+  // judged in FP32 (a NaN anywhere in the increments reaches rn or pn)
+  const float p0 = own ? qc[4] : (float)b64[4];
+  const float rn = rho - dr, pn = p0 + dp;
+  if (!(rn >= 0.0f) || !(pn >= 0.0f) || du != du || dv != dv || dw != dw) return false;
+  const double out[5] = {b64[0] - (double)dr, b64[1] + (double)du, b64[2] + (double)dv,
+                         b64[3] + (double)dw, b64[4] + (double)dp};
 #pragma unroll
   for (int l = 0; l < 5; ++l) {
     double val = out[l];
@@ -519,10 +520,10 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
 #pragma unroll
             for (int l = 0; l < NV; ++l) a.res_out[ci + ncells(d) * l] = (double)R[l];
           // the finished cell's own stencil values (plane k-1 of the ring)
-          T qo[4];
+          T qo[5];
           const T* own1 = ring + slot(kc) * plane + r * RW + cc;
 #pragma unroll
-          for (int l = 0; l < 4; ++l) qo[l] = own1[l * SH * RW];
+          for (int l = 0; l < 5; ++l) qo[l] = own1[l * SH * RW];
           const long long m0 = (long long)(i + 2) + (long long)a.mpitch * ((j + 2) + (long long)d.nj * (kc + 2));
           if (!update_cell(p, a, c0, ci, R, dtc, vol_c, qo, m0))
             raise_error(a.err, FEST_ERR_NEGATIVE_STATE);

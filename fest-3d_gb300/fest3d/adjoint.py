@@ -150,3 +150,158 @@ def sensitivities(case, q, it, params=("mach", "angle"), wall_nodes=(), tol=1e-1
             grads[f"wall_node_{i}"] = float(np.sum(dn[1, i + 2, 3:ext.jmx + 3, 3:ext.kmx + 3] * wgt[:, None]))
     h.close()
     return grads, J, n, drop
+
+
+# ---- unsteady adjoint with checkpointing -------------------------------------
+# N time-accurate TVD-RK3 steps with a fixed global time step (schemetype
+# 'g' with global_time_step > 0, time.f90:248-289) on the FP64 module path
+# (fest_get_next_solution).  One step: q1 = M(q0), q2 = 3/4 q0 + 1/4 M(q1),
+# q3 = 1/3 q0 + 2/3 M(q2) (update.f90:196-206) with the stage update
+# M(q) = prim(cons(q) - (dt/V) R(q)) (update.f90:367-485).  The adjoint runs
+# the steps backwards: M'(q)^T v = C'(q)^T w - (dR/dq)^T ((dt/V) w),
+# w = P'(M(q))^T v, C = cons, P = prim, the residual part by
+# fest_residual_vjp.  States are kept at every `every`-th step and each
+# segment is recomputed forwards before it is reversed.
+
+GM = 1.4
+
+
+def _interior(ext):
+    return (slice(3, ext.imx + 2), slice(3, ext.jmx + 2), slice(3, ext.kmx + 2))
+
+
+def _cons_T(q, w, gm=GM):
+    """C'(q)^T w for U = (rho, rho u, rho v, rho w, E) of q = (rho,u,v,w,p)."""
+    r, u, v, x = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
+    out = np.empty_like(w)
+    out[..., 0] = w[..., 0] + u * w[..., 1] + v * w[..., 2] + x * w[..., 3] + 0.5 * (u * u + v * v + x * x) * w[..., 4]
+    out[..., 1] = r * w[..., 1] + r * u * w[..., 4]
+    out[..., 2] = r * w[..., 2] + r * v * w[..., 4]
+    out[..., 3] = r * w[..., 3] + r * x * w[..., 4]
+    out[..., 4] = w[..., 4] / (gm - 1.0)
+    return out
+
+
+def _prim_T(q, v, gm=GM):
+    """P'(U)^T v at the primitive state q = P(U)."""
+    r, u, vv, x = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
+    g1 = gm - 1.0
+    out = np.empty_like(v)
+    out[..., 0] = v[..., 0] - (u * v[..., 1] + vv * v[..., 2] + x * v[..., 3]) / r + 0.5 * g1 * (u * u + vv * vv + x * x) * v[..., 4]
+    out[..., 1] = v[..., 1] / r - g1 * u * v[..., 4]
+    out[..., 2] = v[..., 2] / r - g1 * vv * v[..., 4]
+    out[..., 3] = v[..., 3] / r - g1 * x * v[..., 4]
+    out[..., 4] = g1 * v[..., 4]
+    return out
+
+
+def _stage_update(q, R, dtv, gm=GM):
+    """M(q) on interior cells: prim(cons(q) - dt/V R), FP64."""
+    r, u, v, x, p = (q[..., l] for l in range(5))
+    U = np.stack([r, r * u, r * v, r * x, p / (gm - 1.0) + 0.5 * r * (u * u + v * v + x * x)], axis=-1)
+    U = U - R * dtv[..., None]
+    rn = U[..., 0]
+    un, vn, xn = U[..., 1] / rn, U[..., 2] / rn, U[..., 3] / rn
+    pn = (gm - 1.0) * (U[..., 4] - 0.5 * rn * (un * un + vn * vn + xn * xn))
+    return np.stack([rn, un, vn, xn, pn], axis=-1)
+
+
+def _stages(h, q0, it, dtv, ext):
+    """The three stage inputs of one step from q0 (padded, ghosts as the
+    step starts) and the step's result; each with its ghosts as filled by
+    its own residual evaluation."""
+    sl = _interior(ext)
+    qs, Rs = [], []
+    q = np.array(q0, order="F")
+    for k in range(3):
+        qf, R = h.residual(q, it)
+        qs.append(qf)
+        Rs.append(R)
+        m = _stage_update(qf[sl], R, dtv)
+        nxt = np.array(qf, order="F")
+        if k == 0:
+            nxt[sl] = m
+        elif k == 1:
+            nxt[sl] = 0.75 * qs[0][sl] + 0.25 * m
+        else:
+            nxt[sl] = qs[0][sl] / 3.0 + 2.0 / 3.0 * m
+        q = nxt
+    return qs, Rs, q
+
+
+def _stage_vjp(h, qf, R, it, dtv, v, ext):
+    """M'(q)^T v on interior cells (v and the result: (nI,nJ,nK,5))."""
+    sl = _interior(ext)
+    qn = _stage_update(qf[sl], R, dtv)
+    w = _prim_T(qn, v)
+    lam = np.asfortranarray(w * dtv[..., None])
+    dq = h.residual_vjp(qf, it, lam)[sl]
+    return _cons_T(qf[sl], w) - dq
+
+
+def unsteady_case(nc=(64, 24, 4), dt=2e-5, steps=100, mach=0.5):
+    """The bump run time-accurately: unlimited MUSCL + SLAU, TVD-RK3 with a
+    fixed global time step dt, from the uniform inflow plus a pressure pulse
+    (the perturbation direction dq0, 1000 Pa Gaussian in the channel)."""
+    ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 5)
+    scheme = abi.make_scheme(scheme_name="slau", interpolant="muscl", time_step_accuracy="TVDRK3",
+                             time_stepping_method="g", global_time_step=dt, ilimiter_switch=0,
+                             jlimiter_switch=0, klimiter_switch=0)
+    flow = bump_flow(mach)
+    nodes = cases.bump_nodes(ext)
+    qp = cases.uniform_state(ext, flow)
+    X = 0.125 * (nodes[0, 3:ext.imx + 2, 3:ext.jmx + 2, 3:ext.kmx + 2] + nodes[0, 4:ext.imx + 3, 3:ext.jmx + 2, 3:ext.kmx + 2]
+                 + nodes[0, 3:ext.imx + 2, 4:ext.jmx + 3, 3:ext.kmx + 2] + nodes[0, 4:ext.imx + 3, 4:ext.jmx + 3, 3:ext.kmx + 2]) * 2
+    Y = 0.125 * (nodes[1, 3:ext.imx + 2, 3:ext.jmx + 2, 3:ext.kmx + 2] + nodes[1, 4:ext.imx + 3, 3:ext.jmx + 2, 3:ext.kmx + 2]
+                 + nodes[1, 3:ext.imx + 2, 4:ext.jmx + 3, 3:ext.kmx + 2] + nodes[1, 4:ext.imx + 3, 4:ext.jmx + 3, 3:ext.kmx + 2]) * 2
+    dq0 = np.zeros_like(qp)
+    dq0[3:ext.imx + 2, 3:ext.jmx + 2, 3:ext.kmx + 2, 4] = 1000.0 * np.exp(-((X + 0.5) ** 2 + (Y - 0.4) ** 2) / 0.02)
+    return dict(ext=ext, flow=flow, scheme=scheme, bc=bump_bc(mach), nodes=nodes, qp=qp, dq0=dq0,
+                dt=dt, steps=steps, CFL=0.8, mach=mach, angle=0.0)
+
+
+def run_primal(h, q0, steps, first_iter=1, keep_every=0):
+    """`steps` steps of fest_get_next_solution from q0; returns the final
+    state and, with keep_every, the states at steps 0, keep_every, ..."""
+    q = np.array(q0, order="F")
+    kept = {}
+    for n in range(steps):
+        if keep_every and n % keep_every == 0:
+            kept[n] = q.copy(order="F")
+        q = h.get_next_solution(q, first_iter + n, 0.8)
+    return q, kept
+
+
+def unsteady_sensitivity(case, eps=0.0, every=10, lib=None):
+    """dJ/d(eps) of J = wall_force(q_N) for q_0 = qp + eps dq0 by the
+    discrete adjoint of the N steps, states checkpointed every `every`
+    steps and recomputed segment by segment.  Returns (J, dJ/deps,
+    residual-VJP calls)."""
+    ext = case["ext"]
+    sl = _interior(ext)
+    h = make_handle(case, lib=lib)
+    vol = h.get("cells")[0][sl]
+    dtv = case["dt"] / vol
+    q0 = case["qp"] + eps * case["dq0"]
+    N = case["steps"]
+    qN, ckpt = run_primal(h, q0, N, keep_every=every)
+    J, dJ = wall_force(qN, ext, h.get("Jfaces"))
+    lam = np.array(dJ[sl])
+    calls = 0
+    for seg in range(((N - 1) // every) * every, -1, -every):
+        # recompute the segment's step-start states
+        states = [ckpt[seg]]
+        for n in range(seg, min(seg + every, N) - 1):
+            states.append(h.get_next_solution(states[-1], n + 1, 0.8))
+        for n in range(min(seg + every, N) - 1, seg - 1, -1):
+            it = n + 1
+            qs, Rs, _ = _stages(h, states[n - seg], it, dtv, ext)
+            # q3 = q0/3 + 2/3 M(q2); q2 = 3/4 q0 + 1/4 M(q1); q1 = M(q0)
+            l2 = _stage_vjp(h, qs[2], Rs[2], it, dtv, (2.0 / 3.0) * lam, ext)
+            l0 = lam / 3.0 + 0.75 * l2
+            l1 = _stage_vjp(h, qs[1], Rs[1], it, dtv, 0.25 * l2, ext)
+            l0 = l0 + _stage_vjp(h, qs[0], Rs[0], it, dtv, l1, ext)
+            lam = l0
+            calls += 3
+    h.close()
+    return J, float(np.sum(lam * case["dq0"][sl])), calls
