@@ -63,6 +63,23 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x, dist, device):
+    """The largest value of x over all ranks (the job's time is its slowest
+    rank's); x itself when not distributed."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(cells_per_rank_step, steps, world, seconds):
+    """Whole-job Mcell-residuals/s of `world` replicas, each advancing its
+    own block, timed by the slowest rank."""
+    return world * cells_per_rank_step * steps / seconds / 1e6
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -339,11 +356,7 @@ def run_ours(args):
             it += 1
         barrier()
         abi.check(lib.fest_last_device_error(h.h), "device error")
-        ms = sum(a.elapsed_time(b) for a, b in evs)
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), dist, "cuda")
         return ms, it
 
     results = {}
@@ -362,7 +375,7 @@ def run_ours(args):
         launches = h.launches - n0
         results[prec] = dict(h=h, ms=ms, steps=steps, it=it, launches=launches, clocks=ck.summary())
     mixed, fp64 = results[abi.FEST_MIXED], results[abi.FEST_FP64]
-    rate = lambda r: ws * N * STAGES * r["steps"] / (r["ms"] / 1e3) / 1e6
+    rate = lambda r: replica_rate(N * STAGES, r["steps"], ws, r["ms"] / 1e3)
 
     # roofline of the dominant kernel: event-timed stage-sweep launches
     h = mixed["h"]
@@ -422,11 +435,8 @@ def run_ours(args):
         abi.check(lib.fest_download_state(he.h, ptr), "download")
         tot_e2e += time.perf_counter() - t0
         it += 1
-    if dist:
-        t = torch.tensor([tot_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_e2e = float(t.item())
-    e2e_rate = ws * N * STAGES * e2e_steps / tot_e2e / 1e6
+    tot_e2e = max_over_ranks(tot_e2e, dist, "cuda")
+    e2e_rate = replica_rate(N * STAGES, e2e_steps, ws, tot_e2e)
     nbytes = int(qhost.nbytes)
 
     adj = adjoint_cost(lib) if rank == 0 else None
