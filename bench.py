@@ -537,7 +537,7 @@ def run_converged(args):
 
 def run_batch(args):
     """96 seeded blocks (cell dims uniform in [16,160]x[16,96]x[2,16]),
-    inviscid MUSCL + AUSM+, TVD-RK3, mixed precision: Mcell-residuals/s of
+    laminar (Sutherland) MUSCL + AUSM+, TVD-RK3, mixed precision: Mcell-residuals/s of
     the batched step (one ghost and one sweep launch per stage for all
     blocks) against stepping each block through its own handle."""
     import ctypes as C
@@ -581,8 +581,8 @@ def run_batch(args):
 
     steps, warm = args.steps if args.steps != 2000 else 200, max(args.warmup, 3)
     out = {"mode": "batched multiblock", "blocks": len(blocks), "cells": cells,
-           "workload": "96 blocks, dims uniform in [16,160]x[16,96]x[2,16] (seed 0), inviscid "
-                       "MUSCL+AUSM+, TVD-RK3, CFL 0.5, periodic/extrapolated faces",
+           "workload": "96 blocks, dims uniform in [16,160]x[16,96]x[2,16] (seed 0), laminar "
+                       "(Sutherland) MUSCL+AUSM+, TVD-RK3, CFL 0.5, periodic/extrapolated faces",
            "steps": steps, "warmup": warm, "dtype": "f32 stencil / f64 state"}
     hs = handles()
     arr = (C.c_void_p * len(hs))(*[h.h.value for h in hs])

@@ -49,6 +49,13 @@ __global__ void k_faces_to_f32(const double* faces, float4* dst, long long n) {
     dst[t] = make_float4((float)f[0], (float)f[1], (float)f[2], (float)f[3]);
   }
 }
+__global__ void k_cells_to_f32(const double* cells, float4* dst, long long n) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double* c = cells + 4 * t;
+    dst[t] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
+  }
+}
 __global__ void k_vol_to_f32(const double* cells, float* dst, long long n) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x)
@@ -262,6 +269,8 @@ struct FusedState {
   float* Q32[3] = {nullptr, nullptr, nullptr};
   float4* F32[3] = {nullptr, nullptr, nullptr};
   float* V32 = nullptr;
+  float4* C32 = nullptr;  // {volume, cx, cy, cz} for the viscous sweep
+  bool visc = false;
   bool mirror_valid = false;  // Q32 interiors match Q
   int kc[2] = {0, 0};         // tuned k-chunk per precision (0: not tuned yet)
   int occ[2] = {1, 2};        // tuned register budget (CTAs per SM) per precision
@@ -288,14 +297,16 @@ struct FusedState {
 };
 
 bool fused_supported(const Params& p, int precision) {
-  (void)precision;
   // ping-pong buffers keep each stage's ghosts in its own input buffer; BC
   // sets that read another face's ghosts (blocks thinner than a BC's read
   // depth, -9) need the in-place module path
   // the sweep addresses one plane's stencil with 32-bit offsets
   const bool small_enough = (long long)p.d.P * p.d.nv < (1ll << 31);
-  return p.mu_ref == 0.0 && p.turb == FEST_TURB_NONE && p.d.nv == 5 && p.tstep == 'l' &&
-         ghost_depth_ok(p) && small_enough;
+  // laminar viscous terms are in the FP32 sweep only (FP64 viscous blocks
+  // take the module path, which keeps the reference's temperature timing)
+  const bool physics = p.mu_ref == 0.0 || precision == FEST_MIXED;
+  return physics && p.turb == FEST_TURB_NONE && p.d.nv == 5 && p.tstep == 'l' && ghost_depth_ok(p) &&
+         small_enough;
 }
 
 int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cudaStream_t s,
@@ -305,6 +316,7 @@ int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cuda
   if (!fused_supported(p, FEST_MIXED)) return FEST_ERR_ARG;
   FusedState* f = new FusedState();
   f->d = p.d;
+  f->visc = p.mu_ref != 0.0;
   f->Q[0] = b.qp;
   size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
   for (int n = 1; n < 3; ++n) {
@@ -403,6 +415,12 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
     f->allocs.push_back(f->V32);
     k_vol_to_f32<<<grid_for(d.P), 256, 0, s>>>(b.cells, f->V32, d.P);
     ++*cnt;
+    if (f->visc) {
+      if (cudaMalloc((void**)&f->C32, sizeof(float4) * (size_t)d.P) != cudaSuccess) return FEST_ERR_NOMEM;
+      f->allocs.push_back(f->C32);
+      k_cells_to_f32<<<grid_for(d.P), 256, 0, s>>>(b.cells, f->C32, d.P);
+      ++*cnt;
+    }
     f->mirror_valid = false;
   }
   if (!f->mirror_valid) {
@@ -420,6 +438,16 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
 
 static void launch_sweep(const Params& p, int prec, int occ, dim3 grid, cudaStream_t s, const StageArgs& a,
                          const CUtensorMap& tm) {
+  if (prec == FEST_MIXED && p.mu_ref != 0.0) {
+    switch (p.interp) {
+      case FEST_INTERP_NONE: launch_stage_none_visc(prec, p.flux, occ, grid, s, p, a, tm); break;
+      case FEST_INTERP_MUSCL: launch_stage_muscl_visc(prec, p.flux, occ, grid, s, p, a, tm); break;
+      case FEST_INTERP_PPM: launch_stage_ppm_visc(prec, p.flux, occ, grid, s, p, a, tm); break;
+      case FEST_INTERP_WENO: launch_stage_weno_visc(prec, p.flux, occ, grid, s, p, a, tm); break;
+      default: launch_stage_weno_nm_visc(prec, p.flux, occ, grid, s, p, a, tm); break;
+    }
+    return;
+  }
   switch (p.interp) {
     case FEST_INTERP_NONE: launch_stage_none(prec, p.flux, occ, grid, s, p, a, tm); break;
     case FEST_INTERP_MUSCL: launch_stage_muscl(prec, p.flux, occ, grid, s, p, a, tm); break;
@@ -500,6 +528,7 @@ static StageArgs stage_args(FusedState* f, const DevBlock& b, bool mixed, int in
   for (int dir = 0; dir < 3; ++dir) a.faces32[dir] = mixed ? f->F32[dir] : nullptr;
   a.vol32 = mixed ? f->V32 : nullptr;
   a.mpitch = f->mpitch;
+  a.cells32 = mixed ? f->C32 : nullptr;
   a.k_chunk = 1;
   return a;
 }
@@ -887,6 +916,15 @@ static FusedBatch::GTable* batch_ghosts(FusedBatch* B, int buf) {
 }
 
 static int launch_batch(const FusedBatch* B, int ctas, const BatchEntry* e, cudaStream_t s) {
+  if (B->p[0].mu_ref != 0.0) {
+    switch (B->interp) {
+      case FEST_INTERP_NONE: return launch_batch_none_visc(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+      case FEST_INTERP_MUSCL: return launch_batch_muscl_visc(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+      case FEST_INTERP_PPM: return launch_batch_ppm_visc(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+      case FEST_INTERP_WENO: return launch_batch_weno_visc(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+      default: return launch_batch_weno_nm_visc(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+    }
+  }
   switch (B->interp) {
     case FEST_INTERP_NONE: return launch_batch_none(FEST_MIXED, B->flux, ctas, s, e, B->nb);
     case FEST_INTERP_MUSCL: return launch_batch_muscl(FEST_MIXED, B->flux, ctas, s, e, B->nb);
@@ -963,7 +1001,9 @@ int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Para
   if (f.empty() || f.size() != p.size() || f.size() != b.size()) return FEST_ERR_ARG;
   for (size_t n = 0; n < f.size(); ++n) {
     if (!f[n] || !fused_supported(p[n], FEST_MIXED)) return FEST_ERR_ARG;
-    if (p[n].interp != p[0].interp || p[n].flux != p[0].flux || p[n].integ != p[0].integ) return FEST_ERR_ARG;
+    if (p[n].interp != p[0].interp || p[n].flux != p[0].flux || p[n].integ != p[0].integ ||
+        (p[n].mu_ref != 0.0) != (p[0].mu_ref != 0.0))
+      return FEST_ERR_ARG;
   }
   FusedBatch* B = new FusedBatch();
   B->f = f;

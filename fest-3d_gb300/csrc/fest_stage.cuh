@@ -55,6 +55,7 @@ struct StageArgs {
   const float4* faces32[3];  // {A,nx,ny,nz} per face
   const float* vol32;   // cell volumes (padded)
   int mpitch;           // row pitch of the state mirror (imx+5 rounded up to 4)
+  const float4* cells32;  // {volume, cx, cy, cz} (FP32, padded layout): viscous sweeps
 };
 
 // one block of a batched stage launch (device memory, 64-byte aligned for
@@ -289,12 +290,147 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
   return true;
 }
 
+
+// ---- laminar viscous terms of the FP32 sweep --------------------------------
+// Cell data the viscous terms read: FP32 copies of the cell records
+// {volume, cx, cy, cz} (float4, padded layout).
+struct ViscCell {
+  float u, v, w, T, rho;  // primitive velocity, temperature p/(rho R), density
+};
+__device__ __forceinline__ ViscCell visc_cell(const float* q, int vs, float R) {
+  ViscCell c;
+  c.rho = q[0];
+  c.u = q[vs];
+  c.v = q[2 * vs];
+  c.w = q[3 * vs];
+  c.T = dv(q[4 * vs], c.rho * R);
+  return c;
+}
+// dynamic viscosity at a cell: constant mu_ref, or Sutherland's law from the
+// cell temperature (viscosity.f90:109-136)
+__device__ __forceinline__ float visc_mu(const Params& p, float T) {
+  const float mu_ref = (float)p.mu_ref;
+  if (p.mu_var != FEST_MU_SUTHERLAND) return mu_ref;
+  const float Tr = (float)p.T_ref, S = (float)p.S;
+  const float t = dv(T, Tr);
+  return mu_ref * (t * sq(t)) * dv(Tr + S, T + S);
+}
+// Green-Gauss gradient of (u, v, w, T) at a cell (gradients.f90:276-482):
+// grad = sum over faces of +-(phi_nb + phi_c) n A / (2V), low faces of
+// i, j, k first; z components zero on a single-plane block.
+// nb[0..5] = i-1, j-1, k-1, i+1, j+1, k+1; f[0..5] the matching faces.
+__device__ __forceinline__ void visc_gg(const ViscCell& c, const ViscCell* nb, const float4* f, float vol,
+                                        bool thin, float* G) {
+  const float iv2 = dv(1.0f, 2.0f * vol);
+  const float vc[4] = {c.u, c.v, c.w, c.T};
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    float vn[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) vn[m] = l == 0 ? nb[m].u : l == 1 ? nb[m].v : l == 2 ? nb[m].w : nb[m].T;
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) {
+      float g = 0.0f;
+      if (!(thin && comp == 2)) {
+        const float n0 = comp == 0 ? f[0].y : comp == 1 ? f[0].z : f[0].w;
+        const float n1 = comp == 0 ? f[1].y : comp == 1 ? f[1].z : f[1].w;
+        const float n2 = comp == 0 ? f[2].y : comp == 1 ? f[2].z : f[2].w;
+        const float n3 = comp == 0 ? f[3].y : comp == 1 ? f[3].z : f[3].w;
+        const float n4 = comp == 0 ? f[4].y : comp == 1 ? f[4].z : f[4].w;
+        const float n5 = comp == 0 ? f[5].y : comp == 1 ? f[5].z : f[5].w;
+        float s = -((vn[0] + vc[l]) * n0 * f[0].x);
+        s = s - (vn[1] + vc[l]) * n1 * f[1].x;
+        s = s - (vn[2] + vc[l]) * n2 * f[2].x;
+        s = s + (vn[3] + vc[l]) * n3 * f[3].x;
+        s = s + (vn[4] + vc[l]) * n4 * f[4].x;
+        s = s + (vn[5] + vc[l]) * n5 * f[5].x;
+        g = s * iv2;
+      }
+      G[3 * l + comp] = g;
+    }
+  }
+}
+// gradient of a ghost cell from its interior neighbour (apply_gradient_bc,
+// gradients.f90:486-676): normal jump over the boundary face, adiabatic
+// walls flip the temperature gradient, plus the interior tangential part
+__device__ __forceinline__ void visc_gbc(const Params& p, int f, const float* GI, const ViscCell& cI,
+                                         const ViscCell& cG, float volI, float4 fc, float* GG) {
+  const float sig = (f % 2) ? -1.0f : 1.0f;
+  const float av = dv(fc.x, volI);
+  const float ccx = av * fc.y, ccy = av * fc.z, ccz = av * fc.w;
+  const float diff[4] = {cI.u - cG.u, cI.v - cG.v, cI.w - cG.w, cI.T - cG.T};
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    GG[3 * l + 0] = sig * diff[l] * ccx;
+    GG[3 * l + 1] = sig * diff[l] * ccy;
+    GG[3 * l + 2] = sig * diff[l] * ccz;
+  }
+  const double Tw = p.Tw[f];
+  if (p.id[f] == -5 && Tw < 1.0 && Tw >= 0.0) {
+    GG[9] = -GI[9]; GG[10] = -GI[10]; GG[11] = -GI[11];
+  }
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const float gx = GI[3 * l], gy = GI[3 * l + 1], gz = GI[3 * l + 2];
+    const float dot = gx * fc.y + gy * fc.z + gz * fc.w;
+    GG[3 * l + 0] += gx - dot * fc.y;
+    GG[3 * l + 1] += gy - dot * fc.z;
+    GG[3 * l + 2] += gz - dot * fc.w;
+  }
+}
+// laminar viscous flux of a face between cells L and R
+// (viscous.f90:144-325): face gradient = mean of the cell gradients,
+// corrected along the centre-to-centre vector; returns the terms that the
+// reference subtracts from F(2:5)
+__device__ __forceinline__ void visc_flux(const Params& p, const float* GL, const float* GR, const ViscCell& L,
+                                          const ViscCell& Rc, float4 cL, float4 cR, float muL, float muR,
+                                          float4 fc, float* Fv) {
+  float G[3][4];
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp)
+#pragma unroll
+    for (int l = 0; l < 4; ++l) G[comp][l] = 0.5f * (GL[3 * l + comp] + GR[3 * l + comp]);
+  const float dx = cR.y - cL.y, dy = cR.z - cL.z, dz = cR.w - cL.w;
+  const float dLR = sq(dx * dx + dy * dy + dz * dz);
+  const float idLR = dv(1.0f, dLR);
+  const float del[4] = {Rc.u - L.u, Rc.v - L.v, Rc.w - L.w, Rc.T - L.T};
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const float nc = (del[l] - (G[0][l] * dx + G[1][l] * dy + G[2][l] * dz)) * idLR;
+    G[0][l] = G[0][l] + (nc * dx * idLR);
+    G[1][l] = G[1][l] + (nc * dy * idLR);
+    G[2][l] = G[2][l] + (nc * dz * idLR);
+  }
+  const float tm = 0.5f * (muL + muR);
+  const float div3 = (G[0][0] + G[1][1] + G[2][2]) * (1.0f / 3.0f);
+  const float Txx = 2.0f * tm * (G[0][0] - div3), Tyy = 2.0f * tm * (G[1][1] - div3),
+              Tzz = 2.0f * tm * (G[2][2] - div3);
+  const float Txy = tm * (G[0][1] + G[1][0]), Txz = tm * (G[0][2] + G[2][0]), Tyz = tm * (G[1][2] + G[2][1]);
+  const float gm = (float)p.gm;
+  const float Kh = dv(tm, (float)p.Pr) * gm * (float)p.R * dv(1.0f, gm - 1.0f);
+  const float Qx = Kh * G[0][3], Qy = Kh * G[1][3], Qz = Kh * G[2][3];
+  const float uf = 0.5f * (L.u + Rc.u), vf = 0.5f * (L.v + Rc.v), wf = 0.5f * (L.w + Rc.w);
+  const float A = fc.x, nx = fc.y, ny = fc.z, nz = fc.w;
+  Fv[0] = (Txx * nx + Txy * ny + Txz * nz) * A;
+  Fv[1] = (Txy * nx + Tyy * ny + Tyz * nz) * A;
+  Fv[2] = (Txz * nx + Tyz * ny + Tzz * nz) * A;
+  Fv[3] = A * (((Txx * uf + Txy * vf + Txz * wf + Qx) * nx) + ((Txy * uf + Tyy * vf + Tyz * wf + Qy) * ny) +
+               ((Txz * uf + Tyz * vf + Tzz * wf + Qz) * nz));
+}
+// viscous time-step term of a face (add_viscous_time, time.f90:366-448):
+// A mu/(rho |(c_L - c_R).n|) with mu and rho of the face's high-side cell
+__device__ __forceinline__ float visc_lambda(float4 fc, float4 cL, float4 cR, float muR, float rhoR) {
+  const float d = fabsf((cL.y - cR.y) * fc.y + (cL.z - cR.z) * fc.z + (cL.w - cR.w) * fc.w);
+  return fc.x * dv(muR, rhoR * d);
+}
+
 // The sweep of one CTA: tile (bx, by) of the block, k-chunk bz.  The
 // single-block kernel passes its block indices; the batched kernel maps its
 // CTA to a block of the batch and a tile of that block.
-template <typename T, int INTERP, int FLUX>
+template <typename T, int INTERP, int FLUX, bool VISC = false>
 __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, const CUtensorMap* tmp,
                                            int bx, int by, int bz) {
+  static_assert(!VISC || sizeof(T) == 4, "viscous terms are in the FP32 sweep only");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   constexpr int NV = 5;
   constexpr int RW = RingGeom<T>::W, NR = RingGeom<T>::N;
@@ -303,7 +439,10 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
   T* xch = ring + NR * NV * SH * RW;                      // [NV][TY][TX] j-face left states
   T* gfl = xch + NV * TY * TX;                            // [NV][TY][TX] j-face fluxes
   T* lam = gfl + NV * TY * TX;                            // [TY][TX]    j-face dt terms
-  uint64_t* bars = reinterpret_cast<uint64_t*>(lam + TY * TX);  // [NR] ring-slot barriers
+  // viscous: [12][TY][TX] cell gradients and [TY][TX] viscous j-face dt terms
+  float* gxch = reinterpret_cast<float*>(lam + TY * TX);
+  float* lamv = gxch + 12 * TY * TX;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(lam + TY * TX + (VISC ? 13 * TY * TX : 0));  // [NR]
   __shared__ int abort_flag;
   const Dims& d = p.d;
   const int lane = threadIdx.x, w = threadIdx.y, tid = w * TX + lane;
@@ -376,6 +515,13 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
   T lamk_prev = 0, lami_lo_prev = 0, lami_hi_prev = 0, lamj_lo_prev = 0, lamj_hi_prev = 0;
 #pragma unroll
   for (int l = 0; l < NV; ++l) { Lp_prev[l] = 0; H_prev[l] = 0; dF_prev[l] = 0; dG_prev[l] = 0; }
+  // viscous march state: raw gradient of cell (i, j, k-1), viscous dt terms
+  float Gprev[VISC ? 12 : 1];
+#pragma unroll
+  for (int m = 0; m < (VISC ? 12 : 1); ++m) Gprev[m] = 0.0f;
+  float lvk_prev = 0, lvi_lo_prev = 0, lvi_hi_prev = 0, lvj_lo_prev = 0, lvj_hi_prev = 0;
+  const float Rg = (float)p.R;
+  const int VS = SH * RW;  // variable stride in a ring plane
 
   const long long sj = d.ni, sk = (long long)d.ni * d.nj;
   for (int n = 0; n < nplanes; ++n) {
@@ -406,6 +552,35 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
     T qc[NV];
 #pragma unroll
     for (int l = 0; l < NV; ++l) qc[l] = own[l * SH * RW];
+    // viscous: this cell's values, centre, viscosity and raw Green-Gauss
+    // gradient (every thread, halo included)
+    ViscCell Vc{};
+    float4 cown = make_float4(1.f, 0.f, 0.f, 0.f);
+    float muc = 0.f, Gc[VISC ? 12 : 1];
+    float lvi_lo = 0, lvi_hi = 0, lvj_lo = 0, lvj_hi = 0;
+    const int ci_ = clampi(i, d.imx), cj_ = clampi(j, d.jmx);
+    if constexpr (VISC) {
+      const float* o = reinterpret_cast<const float*>(own);
+      Vc = visc_cell(o, VS, Rg);
+      ViscCell nb[6];
+      nb[0] = visc_cell(o - 1, VS, Rg);
+      nb[1] = visc_cell(o - RW, VS, Rg);
+      nb[2] = visc_cell(reinterpret_cast<const float*>(ring + slot(k - 1) * plane + r * RW + cc), VS, Rg);
+      nb[3] = visc_cell(o + 1, VS, Rg);
+      nb[4] = visc_cell(o + RW, VS, Rg);
+      nb[5] = visc_cell(reinterpret_cast<const float*>(ring + slot(k + 1) * plane + r * RW + cc), VS, Rg);
+      const int ci1 = clampi(i + 1, d.imx + 1), cj1 = clampi(j + 1, d.jmx + 1);
+      float4 fgg[6];
+      fgg[0] = __ldg(a.faces32[0] + fidx(d, 0, ci_, cj_, k));
+      fgg[1] = __ldg(a.faces32[1] + fidx(d, 1, ci_, cj_, k));
+      fgg[2] = __ldg(a.faces32[2] + fidx(d, 2, ci_, cj_, k));
+      fgg[3] = __ldg(a.faces32[0] + fidx(d, 0, ci1, cj_, k));
+      fgg[4] = __ldg(a.faces32[1] + fidx(d, 1, ci_, cj1, k));
+      fgg[5] = __ldg(a.faces32[2] + fidx(d, 2, ci_, cj_, k + 1));
+      cown = __ldg(a.cells32 + pidx(d, ci_, cj_, k));
+      visc_gg(Vc, nb, fgg, cown.x, thin, Gc);
+      muc = visc_mu(p, Vc.T);
+    }
     // ---------------- i-faces (warp shuffles) ----------------
     if (kin && in_j) {  // warp-uniform
       T Rm[NV], Lp[NV];
@@ -425,6 +600,23 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       face_flux<T, FLUX>(p, L, Rm, A, nx, ny, nz, (T)wall_mask(p, 0, i), F);
       if (a.compute_dt) lami_lo = lambda_face<T>(gm, L, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
       lami_hi = __shfl_down_sync(0xffffffffu, lami_lo, 1);
+      if constexpr (VISC) {  // viscous flux of the low i-face (cells i-1, i)
+        float Gl[12], GL[12], GR[12], Fv[4];
+#pragma unroll
+        for (int m = 0; m < 12; ++m) Gl[m] = __shfl_up_sync(0xffffffffu, Gc[m], 1);
+        const ViscCell VL = visc_cell(reinterpret_cast<const float*>(own) - 1, VS, Rg);
+        const float4 cL = __ldg(a.cells32 + pidx(d, clampi(i - 1, d.imx), cj_, k));
+        const float4 fc = make_float4(A, nx, ny, nz);
+#pragma unroll
+        for (int m = 0; m < 12; ++m) { GL[m] = Gl[m]; GR[m] = Gc[m]; }
+        if (i - 1 == 0 && p.id[0] < 0) visc_gbc(p, 0, Gc, Vc, VL, cown.x, fc, GL);
+        if (i == d.imx && p.id[1] < 0) visc_gbc(p, 1, Gl, VL, Vc, cL.x, fc, GR);
+        visc_flux(p, GL, GR, VL, Vc, cL, cown, visc_mu(p, VL.T), muc, fc, Fv);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) F[1 + l] -= Fv[l];
+        if (a.compute_dt) lvi_lo = visc_lambda(fc, cL, cown, muc, Vc.rho);
+        lvi_hi = __shfl_down_sync(0xffffffffu, lvi_lo, 1);
+      }
 #pragma unroll
       for (int l = 0; l < NV; ++l) {
         T Fh = __shfl_down_sync(0xffffffffu, F[l], 1);
@@ -446,6 +638,9 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       }
 #pragma unroll
       for (int l = 0; l < NV; ++l) xch[(l * TY + w) * TX + lane] = Lp[l];
+      if constexpr (VISC)
+#pragma unroll
+        for (int m = 0; m < 12; ++m) gxch[(m * TY + w) * TX + lane] = Gc[m];
       __syncthreads();
       T F[NV];
 #pragma unroll
@@ -457,6 +652,25 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         T A, nx, ny, nz;
         load_face(a, 1, fidx(d, 1, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
         face_flux<T, FLUX>(p, L, Rm, A, nx, ny, nz, (T)wall_mask(p, 1, j), F);
+        if constexpr (VISC) {  // viscous flux of the low j-face (cells j-1, j)
+          float Gd[12], GL[12], GR[12], Fv[4];
+#pragma unroll
+          for (int m = 0; m < 12; ++m) Gd[m] = gxch[(m * TY + w - 1) * TX + lane];
+          const ViscCell VD = visc_cell(reinterpret_cast<const float*>(own) - RW, VS, Rg);
+          const float4 cD = __ldg(a.cells32 + pidx(d, ci_, clampi(j - 1, d.jmx), k));
+          const float4 fc = make_float4(A, nx, ny, nz);
+#pragma unroll
+          for (int m = 0; m < 12; ++m) { GL[m] = Gd[m]; GR[m] = Gc[m]; }
+          if (j - 1 == 0 && p.id[2] < 0) visc_gbc(p, 2, Gc, Vc, VD, cown.x, fc, GL);
+          if (j == d.jmx && p.id[3] < 0) visc_gbc(p, 3, Gd, VD, Vc, cD.x, fc, GR);
+          visc_flux(p, GL, GR, VD, Vc, cD, cown, visc_mu(p, VD.T), muc, fc, Fv);
+#pragma unroll
+          for (int l = 0; l < 4; ++l) F[1 + l] -= Fv[l];
+          if (a.compute_dt) {
+            lvj_lo = visc_lambda(fc, cD, cown, muc, Vc.rho);
+            lamv[w * TX + lane] = lvj_lo;
+          }
+        }
 #pragma unroll
         for (int l = 0; l < NV; ++l) gfl[(l * TY + w) * TX + lane] = F[l];
         if (a.compute_dt) {
@@ -471,6 +685,8 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
 #pragma unroll
         for (int l = 0; l < NV; ++l) dG[l] = gfl[(l * TY + w + 1) * TX + lane] - F[l];
         if (a.compute_dt) lamj_hi = lam[(w + 1) * TX + lane];
+        if constexpr (VISC)
+          if (a.compute_dt) lvj_hi = lamv[(w + 1) * TX + lane];
       }
     } else {
       __syncthreads();
@@ -489,6 +705,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       }
       T H[NV];
       T lamk = 0;
+      float lvk = 0;
       if (k >= k0) {
         T A, nx, ny, nz;
         load_face(a, 2, fidx(d, 2, i, j, k), A, nx, ny, nz);
@@ -499,6 +716,21 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
           face_flux<T, FLUX>(p, Lp_prev, Rm, A, nx, ny, nz, (T)wall_mask(p, 2, k), H);
         }
         if (a.compute_dt) lamk = lambda_face<T>(gm, Lp_prev, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
+        if constexpr (VISC) {  // viscous flux of the low k-face (cells k-1, k)
+          float GL[12], GR[12], Fv[4];
+          const ViscCell VK = visc_cell(reinterpret_cast<const float*>(ring + slot(k - 1) * plane + r * RW + cc),
+                                        VS, Rg);
+          const float4 cK = __ldg(a.cells32 + pidx(d, i, j, k - 1));
+          const float4 fc = make_float4(A, nx, ny, nz);
+#pragma unroll
+          for (int m = 0; m < 12; ++m) { GL[m] = Gprev[m]; GR[m] = Gc[m]; }
+          if (k - 1 == 0 && p.id[4] < 0) visc_gbc(p, 4, Gc, Vc, VK, cown.x, fc, GL);
+          if (k == d.kmx && p.id[5] < 0) visc_gbc(p, 5, Gprev, VK, Vc, cK.x, fc, GR);
+          visc_flux(p, GL, GR, VK, Vc, cK, cown, visc_mu(p, VK.T), muc, fc, Fv);
+#pragma unroll
+          for (int l = 0; l < 4; ++l) H[1 + l] -= Fv[l];
+          if (a.compute_dt) lvk = visc_lambda(fc, cK, cown, muc, Vc.rho);
+        }
         if (a.mflux[2] && (k == 1 || k == d.kmx)) a.mflux[2][flidx(fldim(d, 2), i, j, k)] = (double)H[0];
         if (k >= k0 + 1) {
           // cell (i, j, k-1) is complete: residual (scheme.f90:133-135)
@@ -512,6 +744,12 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
           if (a.compute_dt) {
             T s = lami_lo_prev + lamj_lo_prev + lamk_prev + lami_hi_prev + lamj_hi_prev + lamk;
             dtc = (T(1) / s) * vol_c * (T)a.CFL;
+            if constexpr (VISC) {  // add_viscous_time (time.f90:366-448)
+              float sv = lvi_lo_prev + lvj_lo_prev + lvk_prev + lvi_hi_prev + lvj_hi_prev + lvk;
+              sv = (float)p.gm * sv / (float)p.Pr;
+              sv = 2.0f / (sv + (2.0f * (float)a.CFL * vol_c / dtc));
+              dtc = (float)a.CFL * (sv * vol_c);
+            }
             a.dt[ci] = (double)dtc;
           } else {
             dtc = (T)a.dt[ci];
@@ -540,6 +778,15 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         lami_lo_prev = lami_lo; lami_hi_prev = lami_hi;
         lamj_lo_prev = lamj_lo; lamj_hi_prev = lamj_hi;
       }
+      if constexpr (VISC) {
+#pragma unroll
+        for (int m = 0; m < 12; ++m) Gprev[m] = Gc[m];
+        if (k >= k0) lvk_prev = lvk;
+        if (kin) {
+          lvi_lo_prev = lvi_lo; lvi_hi_prev = lvi_hi;
+          lvj_lo_prev = lvj_lo; lvj_hi_prev = lvj_hi;
+        }
+      }
     }
   }
 }
@@ -547,16 +794,16 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
 // MB: CTAs per SM the registers are budgeted for (FP32: 2 = 115 registers,
 // no spills, fewer instructions; 3 = 80 registers, more warps to hide
 // latency on large blocks; the tuner picks per block)
-template <typename T, int INTERP, int FLUX, int MB>
+template <typename T, int INTERP, int FLUX, int MB, bool VISC = false>
 __global__ void __launch_bounds__(TX* TY, MB)
     k_stage(Params p, StageArgs a, const __grid_constant__ CUtensorMap tm) {
-  stage_body<T, INTERP, FLUX>(p, a, &tm, blockIdx.x, blockIdx.y, blockIdx.z);
+  stage_body<T, INTERP, FLUX, VISC>(p, a, &tm, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // One launch for every block of a batch: block b owns CTAs
 // [cta0, cta0 + tx*ty*nz) of the 1-D grid.
-template <typename T, int INTERP, int FLUX>
-__global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 3 : 1)
+template <typename T, int INTERP, int FLUX, bool VISC = false>
+__global__ void __launch_bounds__(TX* TY, VISC ? 2 : (sizeof(T) == 4 ? 3 : 1))
     k_stage_batch(const BatchEntry* e, int nb) {
   __shared__ Params sp;
   __shared__ StageArgs sa;
@@ -583,12 +830,12 @@ __global__ void __launch_bounds__(TX* TY, sizeof(T) == 4 ? 3 : 1)
   }
   __syncthreads();
   const int local = (int)blockIdx.x - E.cta0;
-  stage_body<T, INTERP, FLUX>(sp, sa, &E.tm, local % E.tx, (local / E.tx) % E.ty, local / (E.tx * E.ty));
+  stage_body<T, INTERP, FLUX, VISC>(sp, sa, &E.tm, local % E.tx, (local / E.tx) % E.ty, local / (E.tx * E.ty));
 }
 
-template <typename T> inline size_t stage_smem() {
+template <typename T, bool VISC = false> inline size_t stage_smem() {
   return sizeof(T) * ((size_t)RingGeom<T>::N * 5 * SH * RingGeom<T>::W + 2 * 5 * TY * TX + TY * TX) +
-         sizeof(uint64_t) * RingGeom<T>::N + 16;
+         (VISC ? sizeof(float) * 13 * TY * TX : 0) + sizeof(uint64_t) * RingGeom<T>::N + 16;
 }
 
 
@@ -598,6 +845,12 @@ template <typename T> inline size_t stage_smem() {
 #define FEST_STAGE_LAUNCHER(name)                                                         \
   int name(int prec, int flux, int occ, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a, \
            const CUtensorMap& tm)
+// the laminar-viscous FP32 sweeps (fest_stage_<method>_visc.cu)
+FEST_STAGE_LAUNCHER(launch_stage_none_visc);
+FEST_STAGE_LAUNCHER(launch_stage_muscl_visc);
+FEST_STAGE_LAUNCHER(launch_stage_ppm_visc);
+FEST_STAGE_LAUNCHER(launch_stage_weno_visc);
+FEST_STAGE_LAUNCHER(launch_stage_weno_nm_visc);
 FEST_STAGE_LAUNCHER(launch_stage_none);
 FEST_STAGE_LAUNCHER(launch_stage_muscl);
 FEST_STAGE_LAUNCHER(launch_stage_ppm);
@@ -611,6 +864,11 @@ FEST_BATCH_LAUNCHER(launch_batch_muscl);
 FEST_BATCH_LAUNCHER(launch_batch_ppm);
 FEST_BATCH_LAUNCHER(launch_batch_weno);
 FEST_BATCH_LAUNCHER(launch_batch_weno_nm);
+FEST_BATCH_LAUNCHER(launch_batch_none_visc);
+FEST_BATCH_LAUNCHER(launch_batch_muscl_visc);
+FEST_BATCH_LAUNCHER(launch_batch_ppm_visc);
+FEST_BATCH_LAUNCHER(launch_batch_weno_visc);
+FEST_BATCH_LAUNCHER(launch_batch_weno_nm_visc);
 
 template <int INTERP>
 int launch_stage_t(int prec, int flux, int occ, dim3 grid, cudaStream_t s, const Params& p,
@@ -649,6 +907,63 @@ int launch_stage_t(int prec, int flux, int occ, dim3 grid, cudaStream_t s, const
     FEST_FLUXES(double, 1)
   }
 #undef FEST_FLUXES
+#undef FEST_GO
+  return FEST_OK;
+}
+
+// the laminar-viscous FP32 sweep (one register budget: 1 CTA of 256 threads
+// per 64K registers would waste the SM, so MB = 2 with what spills)
+template <int INTERP>
+int launch_stage_visc_t(int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a,
+                        const CUtensorMap& tm) {
+  using namespace stage;
+  const dim3 blk(TX, TY);
+  static bool attrs = false;
+  const size_t smem = stage_smem<float, true>();
+#define FEST_SET(F) \
+  cudaFuncSetAttribute(k_stage<float, INTERP, F, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+  if (!attrs) {
+    FEST_SET(0); FEST_SET(1); FEST_SET(2); FEST_SET(3); FEST_SET(4); FEST_SET(5);
+    attrs = true;
+  }
+#undef FEST_SET
+#define FEST_GO(F) k_stage<float, INTERP, F, 2, true><<<grid, blk, smem, s>>>(p, a, tm)
+  switch (flux) {
+    case 0: FEST_GO(0); break;
+    case 1: FEST_GO(1); break;
+    case 2: FEST_GO(2); break;
+    case 3: FEST_GO(3); break;
+    case 4: FEST_GO(4); break;
+    case 5: FEST_GO(5); break;
+    default: return FEST_ERR_ARG;
+  }
+#undef FEST_GO
+  return FEST_OK;
+}
+
+template <int INTERP>
+int launch_batch_visc_t(int flux, int ctas, cudaStream_t s, const BatchEntry* e, int nb) {
+  using namespace stage;
+  const dim3 blk(TX, TY);
+  static bool attrs = false;
+  const size_t smem = stage_smem<float, true>();
+#define FEST_SET(F) \
+  cudaFuncSetAttribute(k_stage_batch<float, INTERP, F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+  if (!attrs) {
+    FEST_SET(0); FEST_SET(1); FEST_SET(2); FEST_SET(3); FEST_SET(4); FEST_SET(5);
+    attrs = true;
+  }
+#undef FEST_SET
+#define FEST_GO(F) k_stage_batch<float, INTERP, F, true><<<ctas, blk, smem, s>>>(e, nb)
+  switch (flux) {
+    case 0: FEST_GO(0); break;
+    case 1: FEST_GO(1); break;
+    case 2: FEST_GO(2); break;
+    case 3: FEST_GO(3); break;
+    case 4: FEST_GO(4); break;
+    case 5: FEST_GO(5); break;
+    default: return FEST_ERR_ARG;
+  }
 #undef FEST_GO
   return FEST_OK;
 }

@@ -1,0 +1,16 @@
+// fest_stage_weno_nm_visc.cu - laminar-viscous FP32 stage sweeps with the weno_nm
+// reconstruction (all six flux schemes, single-block and batched); see
+// fest_stage.cuh.
+#include "fest_stage.cuh"
+
+namespace fest {
+FEST_STAGE_LAUNCHER(launch_stage_weno_nm_visc) {
+  (void)prec;
+  (void)occ;
+  return launch_stage_visc_t<FEST_INTERP_WENO_NM>(flux, grid, s, p, a, tm);
+}
+FEST_BATCH_LAUNCHER(launch_batch_weno_nm_visc) {
+  (void)prec;
+  return launch_batch_visc_t<FEST_INTERP_WENO_NM>(flux, ctas, s, e, nb);
+}
+}  // namespace fest

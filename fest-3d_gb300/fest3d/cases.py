@@ -220,7 +220,7 @@ def wall_nodes_of(nodes, ext, bc):
 
 
 def batch_blocks(n=96, seed=0, dims_lo=(16, 16, 2), dims_hi=(160, 96, 16), mach=0.8,
-                 scheme_name="ausmP", interpolant="muscl", integrator="TVDRK3"):
+                 scheme_name="ausmP", interpolant="muscl", integrator="TVDRK3", viscous=True):
     """Independent blocks of a batched multiblock case: cell dimensions drawn
     uniformly from [16,160]x[16,96]x[2,16] (numpy default_rng(seed)),
     Cartesian grids with a sinusoidal node perturbation of 5% of the local
@@ -228,7 +228,8 @@ def batch_blocks(n=96, seed=0, dims_lo=(16, 16, 2), dims_hi=(160, 96, 16), mach=
     to Mach 0.8 from 3 Fourier modes, p = 101325 +- 10%).  Each direction is
     periodic (a self-paired interface, when the block has >= 4 cells there)
     or extrapolated (-2: ghost = first interior cell), by a fair coin.
-    Inviscid MUSCL + AUSM+ with TVD-RK3, CFL 0.5."""
+    Laminar Navier-Stokes with Sutherland viscosity (viscous=False: Euler),
+    MUSCL + AUSM+ with TVD-RK3, CFL 0.5."""
     rng = np.random.default_rng(seed)
     out = []
     c = np.sqrt(1.4 * 101325.0 / 1.1)
@@ -243,7 +244,8 @@ def batch_blocks(n=96, seed=0, dims_lo=(16, 16, 2), dims_hi=(160, 96, 16), mach=
                 partners[2 * d] = (0, 2 * d + 1)
                 partners[2 * d + 1] = (0, 2 * d)
         bc = abi.make_bc(ids, partners=partners)
-        flow = abi.make_flow(density_inf=1.1, x_speed_inf=0.3 * c, pressure_inf=101325.0, mu_ref=0.0)
+        flow = abi.make_flow(density_inf=1.1, x_speed_inf=0.3 * c, pressure_inf=101325.0,
+                             mu_ref=1.716e-5 if viscous else 0.0, mu_variation="sutherland_law")
         scheme = abi.make_scheme(scheme_name=scheme_name, interpolant=interpolant,
                                  time_step_accuracy=integrator, time_stepping_method="l")
         h = 1.0 / 64

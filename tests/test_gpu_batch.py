@@ -18,8 +18,8 @@ from fest3d.handle import Handle
 pytestmark = pytest.mark.gpu
 
 
-def small_blocks(n=6, seed=3):
-    return cases.batch_blocks(n=n, seed=seed, dims_lo=(8, 8, 1), dims_hi=(40, 30, 8))
+def small_blocks(n=6, seed=3, viscous=True):
+    return cases.batch_blocks(n=n, seed=seed, dims_lo=(8, 8, 1), dims_hi=(40, 30, 8), viscous=viscous)
 
 
 def handle_of(c, lib):
@@ -37,8 +37,9 @@ def make_batch(lib, handles):
     return b
 
 
-def test_batch_equals_single_blocks(gpu_lib):
-    blocks = small_blocks()
+@pytest.mark.parametrize("viscous", [False, True])
+def test_batch_equals_single_blocks(gpu_lib, viscous):
+    blocks = small_blocks(viscous=viscous)
     single = [handle_of(c, gpu_lib) for c in blocks]
     batched = [handle_of(c, gpu_lib) for c in blocks]
     b = make_batch(gpu_lib, batched)
@@ -58,8 +59,9 @@ def test_batch_equals_single_blocks(gpu_lib):
         gpu_lib.fest_batch_destroy(b)
 
 
-def test_batch_follows_oracle(gpu_lib):
-    blocks = small_blocks(n=4, seed=5)
+@pytest.mark.parametrize("viscous", [False, True])
+def test_batch_follows_oracle(gpu_lib, viscous):
+    blocks = small_blocks(n=4, seed=5, viscous=viscous)
     hs = [handle_of(c, gpu_lib) for c in blocks]
     b = make_batch(gpu_lib, hs)
     try:

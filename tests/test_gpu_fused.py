@@ -5,8 +5,8 @@ magnitude (ghost layers of the returned state are those of the last BC
 application, not the reference's blended copies; the next iteration's BCs
 rewrite them, so only interior cells are compared).
 FEST_MIXED: FP32 stencil arithmetic (ghost cells in FP32 from iteration 3 on)
-with FP64 accumulation; the interior state stays within 2e-5 of each
-variable's magnitude over six iterations."""
+with FP64 accumulation, inviscid and laminar viscous; the interior state
+stays within 2e-5 of each variable's magnitude over six iterations."""
 import ctypes as C
 
 import numpy as np
@@ -35,12 +35,32 @@ COMBOS = {
 }
 
 
+# laminar viscous terms run in the FP32 sweep only (FP64 viscous blocks take
+# the module path); the FP32 sweep evaluates the temperature gradient from the
+# current stage's state where the reference uses the iteration's first
+VISC_COMBOS = {
+    "lam-muscl-ausm-cavity": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ausm"),
+                                  ids=(-5, -5, -5, -3, -10, -10),
+                                  flow_kw=dict(mu_ref=5e-2, mu_variation="constant")),
+    "suth-weno-slau": dict(scheme_kw=dict(interpolant="weno", scheme_name="slau"),
+                           ids=(-3, -4, -5, -6, -10, -10),
+                           flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law")),
+    "suth-ppm-ausmP-slip": dict(scheme_kw=dict(interpolant="ppm", scheme_name="ausmP"),
+                                ids=(-3, -4, -5, -6, -6, -6),
+                                flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law")),
+    "lam-none-vanleer": dict(scheme_kw=dict(interpolant="none", scheme_name="van_leer"),
+                             ids=(-1, -4, -5, -6, -10, -10),
+                             flow_kw=dict(mu_ref=5e-2, mu_variation="constant")),
+}
+COMBOS_ALL = dict(COMBOS, **VISC_COMBOS)
+
+
 def interior(q, ext):
     return q[3:ext.imx + 2, 3:ext.jmx + 2, 3:ext.kmx + 2, :]
 
 
 def run_pair(name, acc, precision, iters=3, nc=(37, 14, 5)):
-    kw = dict(COMBOS[name])
+    kw = dict(COMBOS_ALL[name])
     sk = dict(kw.pop("scheme_kw"))
     sk["time_step_accuracy"] = acc
     kw.setdefault("nc", nc)
@@ -71,6 +91,20 @@ def test_fused_mixed(gpu_lib, name, acc):
     assert e <= 2e-5, f"mixed interior state differs by {e:.3e}"
     ref = O.find_resnorm([blk])
     assert np.allclose(norm[1:], ref[1:], rtol=2e-2), (norm, ref)
+
+
+@pytest.mark.parametrize("name", list(VISC_COMBOS))
+@pytest.mark.parametrize("acc", ["none", "TVDRK3", "RK4"])
+def test_fused_mixed_viscous(gpu_lib, name, acc):
+    ext, blk, h, q, norm = run_pair(name, acc, abi.FEST_MIXED, iters=6)
+    e = rel_err(interior(q, ext), interior(blk["qp"], ext))
+    assert e <= 2e-5, f"mixed viscous interior state differs by {e:.3e}"
+
+
+def test_fp64_viscous_takes_module_path(gpu_lib):
+    """FP64 viscous blocks step through the module kernels: exact."""
+    ext, blk, h, q, norm = run_pair("suth-weno-slau", "TVDRK3", abi.FEST_FP64)
+    assert rel_err(q, blk["qp"]) <= 1e-11
 
 
 @pytest.mark.parametrize("nc,ids", [((40, 9, 1), (-3, -4, -6, -5, -6, -6)),
