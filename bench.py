@@ -55,6 +55,9 @@ def parse():
                     help="instead of the bench line: run FP64 for ITERS iterations, then mixed "
                          "until its wall Cp is within 1e-5 of FP64's (at most ITERS), and report "
                          "both wall times")
+    ap.add_argument("--cavity", type=int, default=0, metavar="ITERS",
+                    help="instead of the bench line: the laminar lid-driven cavity 64x64x4 for ITERS "
+                         "iterations in mixed precision (fused sweep) and FP64 (module path)")
     ap.add_argument("--batch", action="store_true",
                     help="instead of the bench line: the 96-block batched case, one launch per "
                          "stage for all blocks against a loop over the blocks' own steps")
@@ -623,8 +626,52 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_cavity(args):
+    """Laminar lid-driven cavity (64x64x4 cells, MUSCL + AUSM, forward Euler,
+    local dt, CFL 0.5, constant mu for Re 100): ITERS iterations in mixed
+    precision (the fused FP32 sweep with its viscous terms) and in FP64 (the
+    module kernels), wall times and the u-velocity difference along the
+    vertical centre line, relative to the lid speed."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    from fest3d import abi, build, cases
+    from fest3d.handle import Handle
+    if not os.path.exists(abi.LIB_PATH):
+        build.build()
+    lib = abi.load()
+    case = cases.ldc_case()
+    ext = case["ext"]
+    out = {"mode": "lid-driven cavity", "workload": case["name"], "iters": args.cavity}
+    prof = {}
+    for prec, name in ((abi.FEST_MIXED, "mixed"), (abi.FEST_FP64, "fp64")):
+        h = Handle(ext, case["flow"], case["scheme"], case["bc"], lib=lib)
+        h.setup_geometry(case["nodes"])
+        h.upload_state(case["qp"])
+        h.set_precision(prec)
+        h.step(2, 1, case["CFL"], with_norm=False)  # first-use setup, fix() iterations
+        torch.cuda.synchronize()
+        n = args.cavity - 2
+        t0 = time.perf_counter()
+        norm = h.step(n, 3, case["CFL"])
+        t = time.perf_counter() - t0
+        q = h.download_state()
+        prof[name] = q[3 + (ext.imx - 1) // 2, 3:ext.jmx + 2, 3, 1] / 34.7
+        N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
+        # find_resnorm scales by the free-stream speed, zero in the cavity
+        # (resnorm.f90:128-169): the norm itself is not finite here
+        out[name] = {"seconds": t, "mcell_residuals_per_s": N * n / t / 1e6}
+        h.close()
+    out["centreline_u_max_abs_diff_over_lid_speed"] = float(np.abs(prof["mixed"] - prof["fp64"]).max())
+    out["mixed_over_fp64_time"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.cavity:
+        run_cavity(args)
+        return
     if args.batch:
         run_batch(args)
         return

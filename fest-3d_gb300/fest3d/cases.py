@@ -130,12 +130,13 @@ def ldc_case(nc=(64, 64, 4)):
     gamma 1.4, R 287, rho 1.2, p 101325, lid at jmax moving +x at 34.7 m/s
     (id -3, FIX_DENSITY/X_SPEED, COPY_PRESSURE), other x/y faces adiabatic
     no-slip walls (-5), z faces periodic (-10, kmin<->kmax); constant mu for
-    Re=100 on the lid; MUSCL + AUSM, local time step, forward Euler, CFL 0.5."""
+    Re=100 on the lid; MUSCL (van Albada limiter) + AUSM, local time step,
+    forward Euler, CFL 0.5."""
     ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 5)
     flow = abi.make_flow(density_inf=1.2, x_speed_inf=0.0, pressure_inf=101325.0,
                          mu_ref=1.2 * 34.7 * 1.0 / 100.0, mu_variation="constant")
     scheme = abi.make_scheme(scheme_name="ausm", interpolant="muscl", time_step_accuracy="none",
-                             time_stepping_method="l")
+                             time_stepping_method="l", limiter="van_albada")
     fixed = {k: [0.0] * 6 for k in ("fixed_density", "fixed_x_speed", "fixed_y_speed",
                                     "fixed_z_speed", "fixed_wall_temperature")}
     fixed["fixed_density"][3] = 1.2
