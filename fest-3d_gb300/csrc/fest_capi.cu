@@ -467,6 +467,7 @@ int fest_set_metrics(fest_handle* h, const double* cells, const double* Ifaces,
 
 int fest_find_wall_dist(fest_handle* h, const double* wall_xyz, int n_wall, double* dist) {
   if (!h || !wall_xyz || n_wall <= 0) return FEST_ERR_ARG;
+  RET(drop_fused(h));  // the SST sweep keeps an FP32 copy of the distances
   const Dims& d = h->p.d;
   if (n_wall > h->n_wall_cap) {
     if (h->d_wall) cudaFree(h->d_wall);
@@ -486,6 +487,7 @@ int fest_find_wall_dist(fest_handle* h, const double* wall_xyz, int n_wall, doub
 
 int fest_set_wall_dist(fest_handle* h, const double* dist) {
   if (!h || !dist) return FEST_ERR_ARG;
+  RET(drop_fused(h));
   RET(up(h, h->d.dist, dist, h->p.d.P));
   return finish(h);
 }

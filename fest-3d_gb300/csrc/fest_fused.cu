@@ -56,6 +56,11 @@ __global__ void k_cells_to_f32(const double* cells, float4* dst, long long n) {
     dst[t] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
   }
 }
+__global__ void k_dist_to_f32(const double* src, float* dst, long long n) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    dst[t] = (float)src[t];
+}
 __global__ void k_vol_to_f32(const double* cells, float* dst, long long n) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x)
@@ -107,11 +112,67 @@ __device__ __forceinline__ void icell(const Dims& d, int f, int m, int ta, int t
   }
 }
 
+// Riemann-invariant ghost state of column (ta, tb) of face f
+// (bc_primitive.f90:1237-1776 for -11, the far-field form for -8); returns
+// the boundary normal velocity Unb
+__device__ __forceinline__ float riemann_mirror(const Params& p, const Mirror& M, int f, int ta, int tb,
+                                                const float4* Fd, float& rg, float& ug, float& vg, float& wg,
+                                                float& pg) {
+  const Dims& d = p.d;
+  const bool tp = p.id[f] == -11;
+  auto I = [&](int m, int l) -> float { int i, j, k; icell(d, f, m, ta, tb, i, j, k); return M.at(i, j, k, l); };
+  int fi, fj, fk;
+  {
+    const int c = (f % 2 == 0) ? 1 : extent_of(d, f / 2);
+    if (f / 2 == 0) { fi = c; fj = ta; fk = tb; }
+    else if (f / 2 == 1) { fi = ta; fj = c; fk = tb; }
+    else { fi = ta; fj = tb; fk = c; }
+  }
+  const float gm = (float)p.gm;
+  const float4 fc = __ldg(Fd + fidx(d, f / 2, fi, fj, fk));
+  const float sg = (f % 2 == 0) ? -1.f : 1.f;
+  const float nx = sg * fc.y, ny = sg * fc.z, nz = sg * fc.w;
+  const float uu = I(1, 1), vv = I(1, 2), ww = I(1, 3), pI = I(1, 4), rI = I(1, 0);
+  const float uinf = (float)p.u_inf, vinf = (float)p.v_inf, winf = (float)p.w_inf;
+  const float pinf = (float)p.p_inf, rinf = (float)p.rho_inf;
+  const float cexp = sqrtf(gm * pI / rI), cinf = sqrtf(gm * pinf / rinf);
+  const float Unexp = uu * nx + vv * ny + ww * nz, Uninf = uinf * nx + vinf * ny + winf * nz;
+  const float Rinf = Uninf - 2.f * cinf / (gm - 1.f), Rexp = Unexp + 2.f * cexp / (gm - 1.f);
+  const float Unb = 0.5f * (Rexp + Rinf), Cb = 0.25f * (gm - 1.f) * (Rexp - Rinf);
+  rg = 0.f;
+  pg = 0.f;
+  if (Unb > 0.f) {
+    const float vd = Unb - Unexp;
+    ug = uu + vd * nx; vg = vv + vd * ny; wg = ww + vd * nz;
+    if (!tp) {
+      const float sv = pI / powf(rI, gm);
+      rg = powf(Cb * Cb / (gm * sv), 1.f / (gm - 1.f));
+      pg = rg * Cb * Cb / gm;
+    }
+  } else {
+    const float vd = Unb - Uninf;
+    ug = uinf + vd * nx; vg = vinf + vd * ny; wg = winf + vd * nz;
+    if (!tp) {
+      const float sv = pinf / powf(rinf, gm);
+      rg = powf(Cb * Cb / (gm * sv), 1.f / (gm - 1.f));
+      pg = rg * Cb * Cb / gm;
+    }
+  }
+  if (tp) {
+    const float Mb = sqrtf(ug * ug + vg * vg + wg * wg) / Cb;
+    pg = (float)p.Tp[f] / powf((1.f + 0.5f * (gm - 1.f) * Mb * Mb), gm / (gm - 1.f));
+    rg = gm * pg / (Cb * Cb);
+  }
+  return Unb;
+}
+
+// dist: the FP64 wall distance (padded), read by the SST wall's omega
 __device__ __forceinline__ void ghost_mirror_column(const Params& p, const Mirror& M, int f, int ta, int tb,
                                                     const float4* F0, const float4* F1,
-                                                    const float4* F2) {
+                                                    const float4* F2, const double* dist) {
   const Dims& d = p.d;
   const int id = p.id[f];
+  const bool sst = d.nv == 7;
   auto G = [&](int L, int l) -> float& { int i, j, k; gcell(d, f, L, ta, tb, i, j, k); return M.at(i, j, k, l); };
   auto I = [&](int m, int l) -> float { int i, j, k; icell(d, f, m, ta, tb, i, j, k); return M.at(i, j, k, l); };
   const float c1 = (float)p.c1, c2 = (float)p.c2, c3 = (float)p.c3;
@@ -135,8 +196,9 @@ __device__ __forceinline__ void ghost_mirror_column(const Params& p, const Mirro
       for (int l = 0; l < d.nv; ++l) flat(l);
       break;
     case -3: flat(4); break;      // subsonic inlet: pressure copied (fix() for the rest)
-    case -4:                      // subsonic outlet: rho,u,v,w copied (fix() for p)
+    case -4:                      // subsonic outlet: rho,u,v,w (and k, omega) copied (fix() for p)
       for (int l = 0; l < 4; ++l) flat(l);
+      if (sst) { flat(5); flat(6); }
       break;
     case -5: {  // wall (bc_primitive.f90:392-402)
       symm(4);
@@ -154,9 +216,25 @@ __device__ __forceinline__ void ghost_mirror_column(const Params& p, const Mirro
         symm(0);
       }
       anti(1); anti(2); anti(3);
+      if (sst) {
+        anti(5);
+        // set_omega_at_wall (bc_primitive.f90:564-643): omega from the
+        // Sutherland viscosity at the face temperature and twice the first
+        // cell's wall distance
+        int i1, j1, k1;
+        icell(d, f, 1, ta, tb, i1, j1, k1);
+        const float Tf = 0.5f * ((G(1, 4) / G(1, 0)) + (I(1, 4) / I(1, 0))) / R;
+        const float Tr = (float)p.T_ref, S = (float)p.S;
+        const float mu = (float)p.mu_ref * powf(Tf / Tr, 1.5f) * ((Tr + S) / (Tf + S));
+        const float rho = 0.5f * (G(1, 0) + I(1, 0));
+        const float dd = 2.f * (float)dist[pidx(d, i1, j1, k1)];
+        const float om = 120.f * mu / (rho * 0.075f * (dd * dd));
+        for (int L = 1; L <= 3; ++L) G(L, 6) = om - I(L, 6);
+      }
     } break;
     case -6: {  // slip wall + flow tangency with I-face normals (FT_bc.f90:67-69)
       symm(0); symm(4);
+      if (sst) { symm(5); symm(6); }
       const float4 fn = __ldg(Fd + fidx(d, f / 2, fi, fj, fk));
       const float4 fr = __ldg(F0 + fidx(d, 0, fi, fj, fk));
       for (int L = 1; L <= 3; ++L) {
@@ -169,42 +247,22 @@ __device__ __forceinline__ void ghost_mirror_column(const Params& p, const Mirro
     } break;
     case -8:
     case -11: {  // Riemann invariants on layer 1, copied to layers 2-3
-      const bool tp = id == -11;
-      const float4 fc = __ldg(Fd + fidx(d, f / 2, fi, fj, fk));
-      const float sg = (f % 2 == 0) ? -1.f : 1.f;
-      const float nx = sg * fc.y, ny = sg * fc.z, nz = sg * fc.w;
-      const float uu = I(1, 1), vv = I(1, 2), ww = I(1, 3), pI = I(1, 4), rI = I(1, 0);
-      const float uinf = (float)p.u_inf, vinf = (float)p.v_inf, winf = (float)p.w_inf;
-      const float pinf = (float)p.p_inf, rinf = (float)p.rho_inf;
-      const float cexp = sqrtf(gm * pI / rI), cinf = sqrtf(gm * pinf / rinf);
-      const float Unexp = uu * nx + vv * ny + ww * nz, Uninf = uinf * nx + vinf * ny + winf * nz;
-      const float Rinf = Uninf - 2.f * cinf / (gm - 1.f), Rexp = Unexp + 2.f * cexp / (gm - 1.f);
-      const float Unb = 0.5f * (Rexp + Rinf), Cb = 0.25f * (gm - 1.f) * (Rexp - Rinf);
-      float ug, vg, wg, rg = 0.f, pg = 0.f;
-      if (Unb > 0.f) {
-        const float vd = Unb - Unexp;
-        ug = uu + vd * nx; vg = vv + vd * ny; wg = ww + vd * nz;
-        if (!tp) {
-          const float sv = pI / powf(rI, gm);
-          rg = powf(Cb * Cb / (gm * sv), 1.f / (gm - 1.f));
-          pg = rg * Cb * Cb / gm;
-        }
-      } else {
-        const float vd = Unb - Uninf;
-        ug = uinf + vd * nx; vg = vinf + vd * ny; wg = winf + vd * nz;
-        if (!tp) {
-          const float sv = pinf / powf(rinf, gm);
-          rg = powf(Cb * Cb / (gm * sv), 1.f / (gm - 1.f));
-          pg = rg * Cb * Cb / gm;
-        }
-      }
-      if (tp) {
-        const float Mb = sqrtf(ug * ug + vg * vg + wg * wg) / Cb;
-        pg = (float)p.Tp[f] / powf((1.f + 0.5f * (gm - 1.f) * Mb * Mb), gm / (gm - 1.f));
-        rg = gm * pg / (Cb * Cb);
-      }
+      float rg, ug, vg, wg, pg;
+      riemann_mirror(p, M, f, ta, tb, Fd, rg, ug, vg, wg, pg);
       for (int L = 1; L <= 3; ++L) {
         G(L, 0) = rg; G(L, 1) = ug; G(L, 2) = vg; G(L, 3) = wg; G(L, 4) = pg;
+      }
+      if (sst) {
+        // k and omega follow the direction of the face's last column
+        // (the loop variable the reference tests after its loop)
+        const int na = (f / 2 == 0 ? d.jmx : d.imx) - 1, nb = (f / 2 == 2 ? d.jmx : d.kmx) - 1;
+        float r2, u2, v2, w2, p2;
+        const float Ulast = riemann_mirror(p, M, f, na, nb, Fd, r2, u2, v2, w2, p2);
+        if (Ulast > 0.f) {
+          flat(5); flat(6);
+        } else {
+          for (int L = 1; L <= 3; ++L) { G(L, 5) = (float)p.fix_tk[f]; G(L, 6) = (float)p.fix_tw[f]; }
+        }
       }
     } break;
     default:
@@ -222,13 +280,14 @@ __device__ __forceinline__ void ghost_mirror_column(const Params& p, const Mirro
 
 __global__ void __launch_bounds__(128) k_ghosts_mirror(Params p, Mirror M, GhostPlan plan,
                                                        const float4* F0, const float4* F1,
-                                                       const float4* F2) {
+                                                       const float4* F2, const double* dist) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= plan.start[plan.nf]) return;
   int n = 0;
   while (t >= plan.start[n + 1]) ++n;
   const long long u = t - plan.start[n];
-  ghost_mirror_column(p, M, plan.face[n], 1 + (int)(u % plan.na[n]), 1 + (int)(u / plan.na[n]), F0, F1, F2);
+  ghost_mirror_column(p, M, plan.face[n], 1 + (int)(u % plan.na[n]), 1 + (int)(u / plan.na[n]), F0, F1, F2,
+                      dist);
 }
 
 // one (block, face) segment of a batched mirror ghost fill
@@ -237,6 +296,7 @@ struct GhostSeg {
   int block, face, na;
   Mirror M;
   const float4* F[3];
+  const double* dist;
 };
 __global__ void __launch_bounds__(128) k_ghosts_mirror_batch(const Params* ps, const GhostSeg* seg, int nseg,
                                                              long long total) {
@@ -251,7 +311,27 @@ __global__ void __launch_bounds__(128) k_ghosts_mirror_batch(const Params* ps, c
   const GhostSeg& g = seg[lo];
   const long long u = t - g.start;
   ghost_mirror_column(ps[g.block], g.M, g.face, 1 + (int)(u % g.na), 1 + (int)(u / g.na), g.F[0], g.F[1],
-                      g.F[2]);
+                      g.F[2], g.dist);
+}
+
+// copy ghost layers 1-3 of face f (interior columns, every variable) from
+// one mirror (and FP64 buffer, when q is given) to the two others
+__global__ void k_ghost_bcast(Dims d, int f, int na, int nb, Mirror src, Mirror d1, Mirror d2, const double* q,
+                              double* q1, double* q2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nb * 3 * d.nv) return;
+  const int ta = 1 + (int)(t % na), tb = 1 + (int)((t / na) % nb);
+  const int L = 1 + (int)((t / ((long long)na * nb)) % 3), l = (int)(t / (3ll * na * nb));
+  int i, j, k;
+  gcell(d, f, L, ta, tb, i, j, k);
+  const float v = src.at(i, j, k, l);
+  d1.at(i, j, k, l) = v;
+  d2.at(i, j, k, l) = v;
+  if (q) {
+    const long long c = pidx(d, i, j, k) + d.P * l;
+    q1[c] = q[c];
+    q2[c] = q[c];
+  }
 }
 
 unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152 * 16); }
@@ -270,7 +350,9 @@ struct FusedState {
   float4* F32[3] = {nullptr, nullptr, nullptr};
   float* V32 = nullptr;
   float4* C32 = nullptr;  // {volume, cx, cy, cz} for the viscous sweep
+  float* D32 = nullptr;   // wall distance for the SST sweep
   bool visc = false;
+  bool turb = false;
   bool mirror_valid = false;  // Q32 interiors match Q
   int kc[2] = {0, 0};         // tuned k-chunk per precision (0: not tuned yet)
   int occ[2] = {1, 2};        // tuned register budget (CTAs per SM) per precision
@@ -296,17 +378,48 @@ struct FusedState {
   size_t nev = 0;               // events in use
 };
 
+// Directions whose ghost fill depends on the order of the faces: a single
+// interior layer under a symmetric face (-5, -6) with the higher-order term
+// c3, whose ghost layer 1 then reads the opposite face's ghost layer 1.  The
+// reference fills its faces in place, low face first: the low face reads
+// the high face's previous fill, the high face the low face's new one.
+static int order_dirs(const Params& p) {
+  if (p.c3 == 0.0) return 0;
+  int m = 0;
+  for (int dir = 0; dir < 3; ++dir) {
+    if (extent_of(p.d, dir) - 1 != 1) continue;
+    for (int s = 0; s < 2; ++s) {
+      const int id = p.id[2 * dir + s];
+      if (id == -5 || id == -6) m |= 1 << dir;
+    }
+  }
+  return m;
+}
+
+static Mirror mirror_of(FusedState* f, int buf) {
+  const Dims& d = f->d;
+  return Mirror{f->Q32[buf], f->mpitch, d.nj, d.nk, (long long)f->mpitch * d.nj * d.nk};
+}
+
 bool fused_supported(const Params& p, int precision) {
   // ping-pong buffers keep each stage's ghosts in its own input buffer; BC
   // sets that read another face's ghosts (blocks thinner than a BC's read
-  // depth, -9) need the in-place module path
+  // depth, -9) need the in-place module path.  FP64 keeps every ghost layer
+  // equal to the reference's; the mixed sweep needs the layers that the
+  // interior updates read (ghost_depth_ok).
   // the sweep addresses one plane's stencil with 32-bit offsets
+  const bool mixed = precision == FEST_MIXED;
   const bool small_enough = (long long)p.d.P * p.d.nv < (1ll << 31);
-  // laminar viscous terms are in the FP32 sweep only (FP64 viscous blocks
+  // viscous and SST terms are in the FP32 sweep only (FP64 viscous blocks
   // take the module path, which keeps the reference's temperature timing)
-  const bool physics = p.mu_ref == 0.0 || precision == FEST_MIXED;
-  return physics && p.turb == FEST_TURB_NONE && p.d.nv == 5 && p.tstep == 'l' && ghost_depth_ok(p) &&
-         small_enough;
+  const bool physics = p.mu_ref == 0.0 || mixed;
+  const bool sst = p.turb == FEST_TURB_SST || p.turb == FEST_TURB_SST2003;
+  const bool model = p.turb == FEST_TURB_NONE ? p.d.nv == 5 : (sst && mixed && p.mu_ref != 0.0 && p.d.nv == 7);
+  // the TVD integrators blend ghosts between fills, which order-dependent
+  // directions would read; they take the module path
+  const bool tvd = p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3;
+  const bool order_ok = !mixed || order_dirs(p) == 0 || !tvd;
+  return physics && model && p.tstep == 'l' && ghost_depth_ok(p, mixed) && order_ok && small_enough;
 }
 
 int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cudaStream_t s,
@@ -317,6 +430,7 @@ int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cuda
   FusedState* f = new FusedState();
   f->d = p.d;
   f->visc = p.mu_ref != 0.0;
+  f->turb = p.turb != FEST_TURB_NONE;
   f->Q[0] = b.qp;
   size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
   for (int n = 1; n < 3; ++n) {
@@ -371,7 +485,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 // 4-D view (i, j, k, variable) of one FP32 state mirror; box = one stencil
-// plane of a tile (40 x 12 x 1 x 5).  Out-of-range elements read as zero.
+// plane of a tile (40 x 12 x 1 x n_var).  Out-of-range elements read as zero.
 static int encode_mirror_map(CUtensorMap* tm, float* base, const Dims& d, int pitch) {
   static EncodeTiledFn encode = nullptr;
   if (!encode) {
@@ -386,7 +500,7 @@ static int encode_mirror_map(CUtensorMap* tm, float* base, const Dims& d, int pi
   const cuuint64_t dims[4] = {(cuuint64_t)d.ni, (cuuint64_t)d.nj, (cuuint64_t)d.nk, (cuuint64_t)d.nv};
   const cuuint64_t strides[3] = {(cuuint64_t)pitch * 4, (cuuint64_t)pitch * d.nj * 4,
                                  (cuuint64_t)pitch * d.nj * d.nk * 4};
-  const cuuint32_t box[4] = {(cuuint32_t)RingGeom<float>::W, (cuuint32_t)SH, 1, 5};
+  const cuuint32_t box[4] = {(cuuint32_t)RingGeom<float>::W, (cuuint32_t)SH, 1, (cuuint32_t)d.nv};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, estr,
                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -421,6 +535,12 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
       k_cells_to_f32<<<grid_for(d.P), 256, 0, s>>>(b.cells, f->C32, d.P);
       ++*cnt;
     }
+    if (f->turb) {
+      if (cudaMalloc((void**)&f->D32, sizeof(float) * (size_t)d.P) != cudaSuccess) return FEST_ERR_NOMEM;
+      f->allocs.push_back(f->D32);
+      k_dist_to_f32<<<grid_for(d.P), 256, 0, s>>>(b.dist, f->D32, d.P);
+      ++*cnt;
+    }
     f->mirror_valid = false;
   }
   if (!f->mirror_valid) {
@@ -438,6 +558,16 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
 
 static void launch_sweep(const Params& p, int prec, int occ, dim3 grid, cudaStream_t s, const StageArgs& a,
                          const CUtensorMap& tm) {
+  if (prec == FEST_MIXED && p.turb != FEST_TURB_NONE) {
+    switch (p.interp) {
+      case FEST_INTERP_NONE: launch_stage_none_sst(prec, p.flux, occ, grid, s, p, a, tm); break;
+      case FEST_INTERP_MUSCL: launch_stage_muscl_sst(prec, p.flux, occ, grid, s, p, a, tm); break;
+      case FEST_INTERP_PPM: launch_stage_ppm_sst(prec, p.flux, occ, grid, s, p, a, tm); break;
+      case FEST_INTERP_WENO: launch_stage_weno_sst(prec, p.flux, occ, grid, s, p, a, tm); break;
+      default: launch_stage_weno_nm_sst(prec, p.flux, occ, grid, s, p, a, tm); break;
+    }
+    return;
+  }
   if (prec == FEST_MIXED && p.mu_ref != 0.0) {
     switch (p.interp) {
       case FEST_INTERP_NONE: launch_stage_none_visc(prec, p.flux, occ, grid, s, p, a, tm); break;
@@ -476,7 +606,8 @@ static int tune_chunk(FusedState* f, const Params& p, int prec, StageArgs a, con
   int best = nk, best_occ = prec == FEST_MIXED ? 2 : 1;
   float best_ms = 1e30f;
   for (int occ : {2, 3}) {
-    if (prec != FEST_MIXED && occ == 3) break;  // FP64 has one variant
+    // FP64 and the viscous and SST sweeps have one register budget
+    if ((prec != FEST_MIXED || p.mu_ref != 0.0) && occ == 3) break;
     int last_chunks = -1;
     for (int kc : cand) {
       if (kc > nk) kc = nk;
@@ -529,6 +660,7 @@ static StageArgs stage_args(FusedState* f, const DevBlock& b, bool mixed, int in
   a.vol32 = mixed ? f->V32 : nullptr;
   a.mpitch = f->mpitch;
   a.cells32 = mixed ? f->C32 : nullptr;
+  a.dist32 = mixed ? f->D32 : nullptr;
   a.k_chunk = 1;
   return a;
 }
@@ -542,29 +674,50 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   bb.qp32 = mixed ? f->Q32[in] : nullptr;
   bb.qp32_pitch = f->mpitch;
   Launcher L{s, cnt};
+  const int od = mixed ? order_dirs(p) : 0;
   if (mixed && iter > 2) {
     // FP32 ghost fill of the stencil mirror (the FP64 ghosts of Q[in] are
-    // read by nothing on this path after iteration 2)
-    GhostPlan plan{};
-    for (int fc = 0; fc < 6; ++fc) {
-      if (p.id[fc] == -1) continue;  // fix() only
-      const int dir = fc / 2;
-      const int na = (dir == 0 ? p.d.jmx : p.d.imx) - 1, nb = (dir == 2 ? p.d.jmx : p.d.kmx) - 1;
-      plan.face[plan.nf] = fc;
-      plan.na[plan.nf] = na;
-      plan.start[plan.nf + 1] = plan.start[plan.nf] + (long long)na * nb;
-      ++plan.nf;
-    }
-    const long long work = plan.start[plan.nf];
-    if (work > 0) {
-      Mirror M{f->Q32[in], f->mpitch, p.d.nj, p.d.nk, (long long)f->mpitch * p.d.nj * p.d.nk};
-      k_ghosts_mirror<<<(unsigned)((work + 127) / 128), 128, 0, s>>>(p, M, plan, f->F32[0], f->F32[1],
-                                                                       f->F32[2]);
-      ++*cnt;
+    // read by nothing on this path after iteration 2); the high faces of
+    // order-dependent directions go second
+    Mirror M = mirror_of(f, in);
+    for (int pass = 0; pass < (od ? 2 : 1); ++pass) {
+      GhostPlan plan{};
+      for (int fc = 0; fc < 6; ++fc) {
+        if (p.id[fc] == -1) continue;  // fix() only
+        const bool second = (fc % 2 == 1) && ((od >> (fc / 2)) & 1);
+        if (second != (pass == 1)) continue;
+        const int dir = fc / 2;
+        const int na = (dir == 0 ? p.d.jmx : p.d.imx) - 1, nb = (dir == 2 ? p.d.jmx : p.d.kmx) - 1;
+        plan.face[plan.nf] = fc;
+        plan.na[plan.nf] = na;
+        plan.start[plan.nf + 1] = plan.start[plan.nf] + (long long)na * nb;
+        ++plan.nf;
+      }
+      const long long work = plan.start[plan.nf];
+      if (work > 0) {
+        k_ghosts_mirror<<<(unsigned)((work + 127) / 128), 128, 0, s>>>(p, M, plan, f->F32[0], f->F32[1],
+                                                                         f->F32[2], b.dist);
+        ++*cnt;
+      }
     }
   } else {
     // edge/corner ghosts are never read by an interior update: no averaging
+    // (order-dependent blocks are thin, so the faces run one by one)
     launch_ghosts(p, bb, f->table[in], iter, L, false);
+  }
+  // order-dependent directions: the next fill's low face reads this fill's
+  // high-face ghosts, in whichever buffer serves as its input
+  for (int dir = 0; dir < 3; ++dir) {
+    if (!((od >> dir) & 1)) continue;
+    const int fc = 2 * dir + 1;
+    const int na = (dir == 0 ? p.d.jmx : p.d.imx) - 1, nb = (dir == 2 ? p.d.jmx : p.d.kmx) - 1;
+    const long long n = (long long)na * nb * 3 * p.d.nv;
+    const int o1 = (in + 1) % 3, o2 = (in + 2) % 3;
+    const bool fp64 = iter <= 2;  // the FP64 fill of iterations 1-2 reads the FP64 buffers
+    k_ghost_bcast<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+        p.d, fc, na, nb, mirror_of(f, in), mirror_of(f, o1), mirror_of(f, o2), fp64 ? f->Q[in] : nullptr,
+        f->Q[o1], f->Q[o2]);
+    ++*cnt;
   }
   StageArgs a = stage_args(f, b, mixed, in, out, base, bA, bB, TF, SF, TU, use_rn, compute_dt, CFL, last);
   const CUtensorMap& tm = mixed ? f->tm[in] : f->tm_none;
@@ -901,6 +1054,7 @@ static FusedBatch::GTable* batch_ghosts(FusedBatch* B, int buf) {
       g.na = na;
       g.M = Mirror{f->Q32[buf], f->mpitch, p.d.nj, p.d.nk, (long long)f->mpitch * p.d.nj * p.d.nk};
       for (int m = 0; m < 3; ++m) g.F[m] = f->F32[m];
+      g.dist = B->b[n].dist;
       h.push_back(g);
       start += (long long)na * nb;
     }
@@ -1000,7 +1154,9 @@ int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Para
   *out = nullptr;
   if (f.empty() || f.size() != p.size() || f.size() != b.size()) return FEST_ERR_ARG;
   for (size_t n = 0; n < f.size(); ++n) {
-    if (!f[n] || !fused_supported(p[n], FEST_MIXED)) return FEST_ERR_ARG;
+    // the batched sweep covers Euler and laminar blocks (SST blocks step alone)
+    if (!f[n] || !fused_supported(p[n], FEST_MIXED) || p[n].turb != FEST_TURB_NONE || order_dirs(p[n]))
+      return FEST_ERR_ARG;
     if (p[n].interp != p[0].interp || p[n].flux != p[0].flux || p[n].integ != p[0].integ ||
         (p[n].mu_ref != 0.0) != (p[0].mu_ref != 0.0))
       return FEST_ERR_ARG;

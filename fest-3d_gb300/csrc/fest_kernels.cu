@@ -1054,11 +1054,20 @@ bool ghosts_need_sequential(const Params& p) {
   return false;
 }
 
-bool ghost_depth_ok(const Params& p) {
+bool ghost_depth_ok(const Params& p, bool stencil_only) {
   // interior layers each face's BC reads at an interior column
   // (bc_primitive.f90:160-206): copies 1, symmetric copies and tangency 3
-  // (4 with the higher-order ghost term c3), interfaces 3, Riemann 1
-  const int symm = p.c3 != 0.0 ? 4 : 3;
+  // (4 with the higher-order ghost term c3), interfaces 3, Riemann 1.
+  // stencil_only: only ghost layer 1 of a face with a negative id other
+  // than -10 reaches an interior update (the boundary face states are
+  // overridden, boundary_state_reconstruction.f90:28-412, and ppm/weno
+  // switch to MUSCL on the first interior cell), and symmetric layer 1
+  // reads interior layers 1 (and 2 with c3)
+  // A single interior layer under such a face (depth 2) is allowed there:
+  // the face then reads the opposite face's ghost layer 1, which the mixed
+  // path provides in the reference's order (low face from the previous
+  // fill, high face after the low one).
+  const int symm = stencil_only ? (p.c3 != 0.0 ? 2 : 1) : (p.c3 != 0.0 ? 4 : 3);
   for (int f = 0; f < 6; ++f) {
     const int id = p.id[f];
     int depth;
@@ -1069,7 +1078,8 @@ bool ghost_depth_ok(const Params& p) {
       case -9: return false;
       default: depth = 3;  // interfaces
     }
-    if (extent_of(p.d, f / 2) - 1 < depth) return false;
+    const int n = extent_of(p.d, f / 2) - 1;
+    if (n < depth && !(stencil_only && depth == 2 && n == 1)) return false;
   }
   return true;
 }

@@ -45,7 +45,7 @@ void launch_ghosts(const Params& p, const DevBlock& b, const BlockRef* d_table, 
 bool ghosts_need_sequential(const Params& p);
 // true when no face's BC reads beyond the block's interior cells (the
 // faces may then fill their ghosts concurrently, in any buffer)
-bool ghost_depth_ok(const Params& p);
+bool ghost_depth_ok(const Params& p, bool stencil_only = false);
 void launch_temperature(const Params& p, const DevBlock& b, const Launcher& L);
 // mode 0: compute_face_interpolant only; 1: + reconstruct_boundary_state;
 // 2: reconstruct_boundary_state alone on the held face states

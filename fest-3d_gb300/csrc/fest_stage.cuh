@@ -56,6 +56,7 @@ struct StageArgs {
   const float* vol32;   // cell volumes (padded)
   int mpitch;           // row pitch of the state mirror (imx+5 rounded up to 4)
   const float4* cells32;  // {volume, cx, cy, cz} (FP32, padded layout): viscous sweeps
+  const float* dist32;    // wall distance (FP32, padded layout): SST sweeps
 };
 
 // one block of a batched stage launch (device memory, 64-byte aligned for
@@ -239,26 +240,36 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
 
 // FP32 arithmetic, FP64 accumulation: the conservative increment
 // dU = R*TF*dt/V is turned into primitive increments exactly (no
-// linearisation) in FP32 and added to the FP64 state.
-__device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
-                                            long long ci, const float* R_in, float dtc, float vol,
-                                            const float* qc, long long m0) {
+// linearisation) in FP32 and added to the FP64 state.  SST (NV = 7): the
+// point-implicit destruction of update.f90:395-398 divides the k and omega
+// residuals first (F1: the cell's blending function), and k, omega are
+// written only where they stay non-negative (update.f90:479-480).
+template <int NV>
+__device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs& a, long long c0,
+                                                long long ci, const float* R_in, float dtc, float vol,
+                                                const float* qc, long long m0, float F1) {
   const long long P = p.d.P, N = ncells(p.d);
   const float gm1 = (float)(p.gm - 1.0);
-  float R[5];
+  float R[NV];
 #pragma unroll
-  for (int l = 0; l < 5; ++l) R[l] = R_in[l];
+  for (int l = 0; l < NV; ++l) R[l] = R_in[l];
+  if constexpr (NV == 7) {
+    const float beta = 0.075f * F1 + (1.0f - F1) * 0.0828f;
+    const float wv = qc[6];  // omega of the stage's input state
+    R[5] = R[5] / (1.0f + (beta * wv * dtc));
+    R[6] = R[6] / (1.0f + (2.0f * beta * wv * dtc));
+  }
   if (a.use_rn) {
 #pragma unroll
-    for (int l = 0; l < 5; ++l) {
+    for (int l = 0; l < NV; ++l) {
       double rn = a.Rn[ci + N * l] + a.SF * (double)R[l];
       a.Rn[ci + N * l] = rn;
       if (a.TU) R[l] = (float)rn;
     }
   }
-  double b64[5];
+  double b64[NV];
 #pragma unroll
-  for (int l = 0; l < 5; ++l) b64[l] = a.qbase[c0 + P * l];
+  for (int l = 0; l < NV; ++l) b64[l] = a.qbase[c0 + P * l];
   const long long mvar = (long long)a.mpitch * p.d.nj * p.d.nk;  // mirror variable stride
   // FP32 copies of the base state: the stencil's own cell when the update
   // starts from the stencil state (bit-identical to converting b64)
@@ -278,10 +289,22 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
   const float p0 = own ? qc[4] : (float)b64[4];
   const float rn = rho - dr, pn = p0 + dp;
   if (!(rn >= 0.0f) || !(pn >= 0.0f) || du != du || dv != dv || dw != dw) return false;
-  const double out[5] = {b64[0] - (double)dr, b64[1] + (double)du, b64[2] + (double)dv,
-                         b64[3] + (double)dw, b64[4] + (double)dp};
+  double out[NV];
+  out[0] = b64[0] - (double)dr;
+  out[1] = b64[1] + (double)du;
+  out[2] = b64[2] + (double)dv;
+  out[3] = b64[3] + (double)dw;
+  out[4] = b64[4] + (double)dp;
+  if constexpr (NV == 7) {
+    const float tk = own ? qc[5] : (float)b64[5], tw = own ? qc[6] : (float)b64[6];
+    const float dk = (tk * dr - R[5] * fac) * ir2, dom = (tw * dr - R[6] * fac) * ir2;
+    if (dk != dk || dom != dom) return false;
+    const double k2 = b64[5] + (double)dk, w2o = b64[6] + (double)dom;
+    out[5] = k2 >= 0.0 ? k2 : a.qin[c0 + P * 5];
+    out[6] = w2o >= 0.0 ? w2o : a.qin[c0 + P * 6];
+  }
 #pragma unroll
-  for (int l = 0; l < 5; ++l) {
+  for (int l = 0; l < NV; ++l) {
     double val = out[l];
     if (a.bA != 0.0) val = a.bA * a.qU[c0 + P * l] + a.bB * val;
     a.qout[c0 + P * l] = val;
@@ -291,12 +314,15 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
 }
 
 
-// ---- laminar viscous terms of the FP32 sweep --------------------------------
+// ---- viscous and SST terms of the FP32 sweep -------------------------------
 // Cell data the viscous terms read: FP32 copies of the cell records
-// {volume, cx, cy, cz} (float4, padded layout).
+// {volume, cx, cy, cz} (float4, padded layout) and, for SST, of the wall
+// distance.
 struct ViscCell {
   float u, v, w, T, rho;  // primitive velocity, temperature p/(rho R), density
+  float k, om;            // SST: turbulent kinetic energy, specific dissipation
 };
+template <bool TURB = false>
 __device__ __forceinline__ ViscCell visc_cell(const float* q, int vs, float R) {
   ViscCell c;
   c.rho = q[0];
@@ -304,7 +330,19 @@ __device__ __forceinline__ ViscCell visc_cell(const float* q, int vs, float R) {
   c.v = q[2 * vs];
   c.w = q[3 * vs];
   c.T = dv(q[4 * vs], c.rho * R);
+  if constexpr (TURB) {
+    c.k = q[5 * vs];
+    c.om = q[6 * vs];
+  } else {
+    c.k = 0.0f;
+    c.om = 0.0f;
+  }
   return c;
+}
+// gradient variable l of a cell: u, v, w, T (+ k, omega for SST), the
+// reference's gradient order (gradients.f90:276-482)
+__device__ __forceinline__ float gvar(const ViscCell& c, int l) {
+  return l == 0 ? c.u : l == 1 ? c.v : l == 2 ? c.w : l == 3 ? c.T : l == 4 ? c.k : c.om;
 }
 // dynamic viscosity at a cell: constant mu_ref, or Sutherland's law from the
 // cell temperature (viscosity.f90:109-136)
@@ -315,19 +353,21 @@ __device__ __forceinline__ float visc_mu(const Params& p, float T) {
   const float t = dv(T, Tr);
   return mu_ref * (t * sq(t)) * dv(Tr + S, T + S);
 }
-// Green-Gauss gradient of (u, v, w, T) at a cell (gradients.f90:276-482):
-// grad = sum over faces of +-(phi_nb + phi_c) n A / (2V), low faces of
-// i, j, k first; z components zero on a single-plane block.
-// nb[0..5] = i-1, j-1, k-1, i+1, j+1, k+1; f[0..5] the matching faces.
+// Green-Gauss gradient of the NGV gradient variables at a cell
+// (gradients.f90:276-482): grad = sum over faces of +-(phi_nb + phi_c) n A
+// / (2V), low faces of i, j, k first; z components zero on a single-plane
+// block.  nb[0..5] = i-1, j-1, k-1, i+1, j+1, k+1; f[0..5] the matching
+// faces; G[3*l + component].
+template <int NGV>
 __device__ __forceinline__ void visc_gg(const ViscCell& c, const ViscCell* nb, const float4* f, float vol,
                                         bool thin, float* G) {
   const float iv2 = dv(1.0f, 2.0f * vol);
-  const float vc[4] = {c.u, c.v, c.w, c.T};
 #pragma unroll
-  for (int l = 0; l < 4; ++l) {
+  for (int l = 0; l < NGV; ++l) {
+    const float vc = gvar(c, l);
     float vn[6];
 #pragma unroll
-    for (int m = 0; m < 6; ++m) vn[m] = l == 0 ? nb[m].u : l == 1 ? nb[m].v : l == 2 ? nb[m].w : nb[m].T;
+    for (int m = 0; m < 6; ++m) vn[m] = gvar(nb[m], l);
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
       float g = 0.0f;
@@ -338,12 +378,12 @@ __device__ __forceinline__ void visc_gg(const ViscCell& c, const ViscCell* nb, c
         const float n3 = comp == 0 ? f[3].y : comp == 1 ? f[3].z : f[3].w;
         const float n4 = comp == 0 ? f[4].y : comp == 1 ? f[4].z : f[4].w;
         const float n5 = comp == 0 ? f[5].y : comp == 1 ? f[5].z : f[5].w;
-        float s = -((vn[0] + vc[l]) * n0 * f[0].x);
-        s = s - (vn[1] + vc[l]) * n1 * f[1].x;
-        s = s - (vn[2] + vc[l]) * n2 * f[2].x;
-        s = s + (vn[3] + vc[l]) * n3 * f[3].x;
-        s = s + (vn[4] + vc[l]) * n4 * f[4].x;
-        s = s + (vn[5] + vc[l]) * n5 * f[5].x;
+        float s = -((vn[0] + vc) * n0 * f[0].x);
+        s = s - (vn[1] + vc) * n1 * f[1].x;
+        s = s - (vn[2] + vc) * n2 * f[2].x;
+        s = s + (vn[3] + vc) * n3 * f[3].x;
+        s = s + (vn[4] + vc) * n4 * f[4].x;
+        s = s + (vn[5] + vc) * n5 * f[5].x;
         g = s * iv2;
       }
       G[3 * l + comp] = g;
@@ -353,24 +393,25 @@ __device__ __forceinline__ void visc_gg(const ViscCell& c, const ViscCell* nb, c
 // gradient of a ghost cell from its interior neighbour (apply_gradient_bc,
 // gradients.f90:486-676): normal jump over the boundary face, adiabatic
 // walls flip the temperature gradient, plus the interior tangential part
+template <int NGV>
 __device__ __forceinline__ void visc_gbc(const Params& p, int f, const float* GI, const ViscCell& cI,
                                          const ViscCell& cG, float volI, float4 fc, float* GG) {
   const float sig = (f % 2) ? -1.0f : 1.0f;
   const float av = dv(fc.x, volI);
   const float ccx = av * fc.y, ccy = av * fc.z, ccz = av * fc.w;
-  const float diff[4] = {cI.u - cG.u, cI.v - cG.v, cI.w - cG.w, cI.T - cG.T};
 #pragma unroll
-  for (int l = 0; l < 4; ++l) {
-    GG[3 * l + 0] = sig * diff[l] * ccx;
-    GG[3 * l + 1] = sig * diff[l] * ccy;
-    GG[3 * l + 2] = sig * diff[l] * ccz;
+  for (int l = 0; l < NGV; ++l) {
+    const float diff = gvar(cI, l) - gvar(cG, l);
+    GG[3 * l + 0] = sig * diff * ccx;
+    GG[3 * l + 1] = sig * diff * ccy;
+    GG[3 * l + 2] = sig * diff * ccz;
   }
   const double Tw = p.Tw[f];
   if (p.id[f] == -5 && Tw < 1.0 && Tw >= 0.0) {
     GG[9] = -GI[9]; GG[10] = -GI[10]; GG[11] = -GI[11];
   }
 #pragma unroll
-  for (int l = 0; l < 4; ++l) {
+  for (int l = 0; l < NGV; ++l) {
     const float gx = GI[3 * l], gy = GI[3 * l + 1], gz = GI[3 * l + 2];
     const float dot = gx * fc.y + gy * fc.z + gz * fc.w;
     GG[3 * l + 0] += gx - dot * fc.y;
@@ -378,36 +419,45 @@ __device__ __forceinline__ void visc_gbc(const Params& p, int f, const float* GI
     GG[3 * l + 2] += gz - dot * fc.w;
   }
 }
-// laminar viscous flux of a face between cells L and R
-// (viscous.f90:144-325): face gradient = mean of the cell gradients,
-// corrected along the centre-to-centre vector; returns the terms that the
-// reference subtracts from F(2:5)
+// Viscous flux of a face between cells L and R (viscous.f90:144-325):
+// face gradient = mean of the cell gradients, corrected along the
+// centre-to-centre vector; Fv holds the terms that the reference subtracts
+// from F(2:5) (and, for SST, from F(6:7)).  SST (viscous.f90:328-447): eddy
+// viscosity added to the stresses and the heat flux, the -2/3 rho k normal
+// stress and the k and omega diffusion with F1-blended sigmas, all skipped
+// on the k faces of a single-plane block (sst_face false).
+template <bool TURB = false>
 __device__ __forceinline__ void visc_flux(const Params& p, const float* GL, const float* GR, const ViscCell& L,
                                           const ViscCell& Rc, float4 cL, float4 cR, float muL, float muR,
-                                          float4 fc, float* Fv) {
-  float G[3][4];
+                                          float mutL, float mutR, float F1L, float F1R, float4 fc,
+                                          bool sst_face, float* Fv) {
+  constexpr int NGV = TURB ? 6 : 4;
+  float G[3][NGV];
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp)
 #pragma unroll
-    for (int l = 0; l < 4; ++l) G[comp][l] = 0.5f * (GL[3 * l + comp] + GR[3 * l + comp]);
+    for (int l = 0; l < NGV; ++l) G[comp][l] = 0.5f * (GL[3 * l + comp] + GR[3 * l + comp]);
   const float dx = cR.y - cL.y, dy = cR.z - cL.z, dz = cR.w - cL.w;
   const float dLR = sq(dx * dx + dy * dy + dz * dz);
   const float idLR = dv(1.0f, dLR);
-  const float del[4] = {Rc.u - L.u, Rc.v - L.v, Rc.w - L.w, Rc.T - L.T};
 #pragma unroll
-  for (int l = 0; l < 4; ++l) {
-    const float nc = (del[l] - (G[0][l] * dx + G[1][l] * dy + G[2][l] * dz)) * idLR;
+  for (int l = 0; l < NGV; ++l) {
+    const float del = gvar(Rc, l) - gvar(L, l);
+    const float nc = (del - (G[0][l] * dx + G[1][l] * dy + G[2][l] * dz)) * idLR;
     G[0][l] = G[0][l] + (nc * dx * idLR);
     G[1][l] = G[1][l] + (nc * dy * idLR);
     G[2][l] = G[2][l] + (nc * dz * idLR);
   }
-  const float tm = 0.5f * (muL + muR);
+  const float mu_f = 0.5f * (muL + muR);
+  const float mut_f = TURB ? 0.5f * (mutL + mutR) : 0.0f;
+  const float tm = TURB ? mu_f + mut_f : mu_f;
   const float div3 = (G[0][0] + G[1][1] + G[2][2]) * (1.0f / 3.0f);
   const float Txx = 2.0f * tm * (G[0][0] - div3), Tyy = 2.0f * tm * (G[1][1] - div3),
               Tzz = 2.0f * tm * (G[2][2] - div3);
   const float Txy = tm * (G[0][1] + G[1][0]), Txz = tm * (G[0][2] + G[2][0]), Tyz = tm * (G[1][2] + G[2][1]);
   const float gm = (float)p.gm;
-  const float Kh = dv(tm, (float)p.Pr) * gm * (float)p.R * dv(1.0f, gm - 1.0f);
+  const float kd = TURB ? dv(mu_f, (float)p.Pr) + dv(mut_f, (float)p.tPr) : dv(tm, (float)p.Pr);
+  const float Kh = kd * gm * (float)p.R * dv(1.0f, gm - 1.0f);
   const float Qx = Kh * G[0][3], Qy = Kh * G[1][3], Qz = Kh * G[2][3];
   const float uf = 0.5f * (L.u + Rc.u), vf = 0.5f * (L.v + Rc.v), wf = 0.5f * (L.w + Rc.w);
   const float A = fc.x, nx = fc.y, ny = fc.z, nz = fc.w;
@@ -416,33 +466,143 @@ __device__ __forceinline__ void visc_flux(const Params& p, const float* GL, cons
   Fv[2] = (Txz * nx + Tyz * ny + Tzz * nz) * A;
   Fv[3] = A * (((Txx * uf + Txy * vf + Txz * wf + Qx) * nx) + ((Txy * uf + Tyy * vf + Tyz * wf + Qy) * ny) +
                ((Txz * uf + Tyz * vf + Tzz * wf + Qz) * nz));
+  if constexpr (TURB) {
+    Fv[4] = 0.0f;
+    Fv[5] = 0.0f;
+    if (sst_face) {
+      const float F1f = 0.5f * (F1L + F1R);
+      const float skf = 0.85f * F1f + 1.0f * (1.0f - F1f);
+      const float swf = 0.5f * F1f + 0.856f * (1.0f - F1f);
+      const float rhof = 0.5f * (L.rho + Rc.rho), tkf = 0.5f * (L.k + Rc.k);
+      const float Tk = -2.0f * rhof * tkf * (1.0f / 3.0f);
+      const float dk = G[0][4] * nx + G[1][4] * ny + G[2][4] * nz;
+      const float dw = G[0][5] * nx + G[1][5] * ny + G[2][5] * nz;
+      Fv[0] += Tk * nx * A;
+      Fv[1] += Tk * ny * A;
+      Fv[2] += Tk * nz * A;
+      const float kdiff = A * ((mu_f + skf * mut_f) * dk);
+      Fv[3] += kdiff;
+      Fv[4] = kdiff;
+      Fv[5] = A * ((mu_f + swf * mut_f) * dw);
+    }
+  }
 }
-// viscous time-step term of a face (add_viscous_time, time.f90:366-448):
-// A mu/(rho |(c_L - c_R).n|) with mu and rho of the face's high-side cell
+// viscous time-step term of a face (add_viscous_time, time.f90:366-448;
+// add_turbulent_time, time.f90:450-531, with mu_t): A mu/(rho |(c_L -
+// c_R).n|) with mu and rho of the face's high-side cell
 __device__ __forceinline__ float visc_lambda(float4 fc, float4 cL, float4 cR, float muR, float rhoR) {
   const float d = fabsf((cL.y - cR.y) * fc.y + (cL.z - cR.z) * fc.z + (cL.w - cR.w) * fc.w);
   return fc.x * dv(muR, rhoR * d);
 }
 
+// SST quantities of a cell (viscosity.f90:52-546, source.f90:158-270): eddy
+// viscosity, blending function F1, cross-diffusion CD (clamped) and the
+// vorticity magnitude.  G: the cell's gradients of u, v, w, T, k, omega.
+struct SstCell {
+  float mut, F1, CD, vort;
+};
+__device__ __forceinline__ SstCell sst_cell(const Params& p, const ViscCell& c, float mu, float dd, const float* G) {
+  const float bstar = 0.09f, a1 = 0.31f, sw2 = 0.856f;
+  const bool s2003 = p.turb == FEST_TURB_SST2003;
+  SstCell s;
+  const float var1 = dv(sq(c.k), bstar * c.om * dd);
+  const float var2 = dv(500.0f * dv(mu, c.rho), (dd * dd) * c.om);
+  const float arg2 = fmax2(2.0f * var1, var2);
+  const float F2 = tanhf(arg2 * arg2);
+  const float NUM = c.rho * a1 * c.k;
+  // G(component, variable) of the reference = G[3*(variable-1) + component]
+  const float wx = G[7] - G[5], wy = G[2] - G[6], wz = G[3] - G[1];
+  s.vort = sq(wx * wx + wy * wy + wz * wz);
+  float DENOM;
+  if (s2003) {
+    const float sxx = G[0], syy = G[4], szz = G[8];
+    const float syz = G[7] + G[5], szx = G[2] + G[6], sxy = G[3] + G[1];
+    const float SijSij = (2.0f * (sxx * sxx)) + (2.0f * (syy * syy)) + (2.0f * (szz * szz)) + syz * syz +
+                         szx * szx + sxy * sxy;
+    DENOM = fmax2(fmax2(a1 * c.om, sq(SijSij) * F2), 1.0e-10f);
+  } else {
+    DENOM = fmax2(fmax2(a1 * c.om, s.vort * F2), 1.0e-20f);
+  }
+  s.mut = dv(NUM, DENOM);
+  float CD = dv(2.0f * c.rho * sw2 * (G[12] * G[15] + G[13] * G[16] + G[14] * G[17]), c.om);
+  s.CD = fmax2(CD, s2003 ? 1.0e-10f : 1.0e-20f);
+  const float right = dv(4.0f * (c.rho * sw2 * c.k), s.CD * (dd * dd));
+  const float arg1 = fmin2(fmax2(var1, var2), right);
+  const float a2 = arg1 * arg1;
+  s.F1 = tanhf(a2 * a2);
+  return s;
+}
+// SST source of an interior cell (add_sst_source, source.f90:158-270):
+// production limited by 20 (sst) or 10 (sst2003) times the destruction;
+// the residual of k and omega loses Sk, Sw
+__device__ __forceinline__ void sst_source(const Params& p, const ViscCell& c, const SstCell& s, const float* G,
+                                           float vol, float& Sk, float& Sw) {
+  constexpr double kBeta1 = 0.075, kBeta2 = 0.0828, kBstar = 0.09, kSw1 = 0.5, kSw2 = 0.856, kKap = 0.41;
+  // gamma_{1,2} = beta_{1,2}/beta* - sigma_w{1,2} kappa^2 / sqrt(beta*), sqrt(0.09) = 0.3
+  constexpr float kG1 = (float)((kBeta1 / kBstar) - ((kSw1 * (kKap * kKap)) / 0.3));
+  constexpr float kG2 = (float)((kBeta2 / kBstar) - ((kSw2 * (kKap * kKap)) / 0.3));
+  const bool s2003 = p.turb == FEST_TURB_SST2003;
+  const float lim = s2003 ? 10.0f : 20.0f;
+  const float gama1 = s2003 ? 5.0f / 9.0f : kG1, gama2 = s2003 ? 0.44f : kG2;
+  const float F1 = s.F1;
+  const float gama = gama1 * F1 + gama2 * (1.0f - F1);
+  const float beta = (float)kBeta1 * F1 + (float)kBeta2 * (1.0f - F1);
+  const float Dk = (float)kBstar * c.rho * c.om * c.k;
+  const float Dw = beta * c.rho * (c.om * c.om);
+  const float divergence = G[0] + G[4] + G[8];
+  float Pk = s.mut * (s.vort * s.vort) - ((2.0f / 3.0f) * c.rho * c.k * divergence);
+  Pk = fmin2(Pk, lim * Dk);
+  const float Pw = dv(c.rho * gama, s.mut) * Pk;
+  Sk = (Pk - Dk) * vol;
+  Sw = (Pw - Dw + (1.0f - F1) * s.CD) * vol;
+}
+// eddy viscosity and F1 of a ghost cell next to a boundary face with a
+// negative id: faces -1..-9 copy the interior values, the wall negating
+// mu_t (viscosity.f90:287-340); other faces keep what calculate_viscosity
+// computed there from the ghost's own state and boundary gradient
+__device__ __forceinline__ void sst_ghost(const Params& p, int f, const ViscCell& cG, float muG, const float* GG,
+                                          float ddG, float mutI, float F1I, float& mutG, float& F1G) {
+  const int id = p.id[f];
+  if (id <= -1 && id >= -9) {
+    mutG = id == -5 ? -mutI : mutI;
+    F1G = F1I;
+  } else {
+    const SstCell s = sst_cell(p, cG, muG, ddG, GG);
+    mutG = s.mut;
+    F1G = s.F1;
+  }
+}
+
 // The sweep of one CTA: tile (bx, by) of the block, k-chunk bz.  The
 // single-block kernel passes its block indices; the batched kernel maps its
 // CTA to a block of the batch and a tile of that block.
-template <typename T, int INTERP, int FLUX, bool VISC = false>
+// VISC adds the laminar viscous terms, TURB (with VISC) the k-omega SST
+// model: seven variables, six gradient variables, eddy viscosity and F1 per
+// cell, the SST face terms, source and time-step terms and the update's
+// point-implicit destruction.
+template <typename T, int INTERP, int FLUX, bool VISC = false, bool TURB = false>
 __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, const CUtensorMap* tmp,
                                            int bx, int by, int bz) {
   static_assert(!VISC || sizeof(T) == 4, "viscous terms are in the FP32 sweep only");
+  static_assert(!TURB || VISC, "the SST terms come with the viscous terms");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  constexpr int NV = 5;
+  constexpr int NV = TURB ? 7 : 5;
+  constexpr int NGV = TURB ? 6 : 4, NGC = 3 * NGV;  // gradient variables, gradient floats per cell
+  constexpr int NXV = VISC ? NGC + (TURB ? 4 : 1) : 0;  // viscous j-exchange floats per thread
   constexpr int RW = RingGeom<T>::W, NR = RingGeom<T>::N;
   constexpr bool kTma = sizeof(T) == 4;
   T* ring = reinterpret_cast<T*>(smem_raw);               // [NR][NV][SH][RW]
   T* xch = ring + NR * NV * SH * RW;                      // [NV][TY][TX] j-face left states
   T* gfl = xch + NV * TY * TX;                            // [NV][TY][TX] j-face fluxes
   T* lam = gfl + NV * TY * TX;                            // [TY][TX]    j-face dt terms
-  // viscous: [12][TY][TX] cell gradients and [TY][TX] viscous j-face dt terms
+  // viscous: [NGC][TY][TX] cell gradients, [TY][TX] viscous j-face dt
+  // terms; SST: [TY][TX] each of mu_t, F1 and turbulent j-face dt terms
   float* gxch = reinterpret_cast<float*>(lam + TY * TX);
-  float* lamv = gxch + 12 * TY * TX;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(lam + TY * TX + (VISC ? 13 * TY * TX : 0));  // [NR]
+  float* lamv = gxch + NGC * TY * TX;
+  float* mutx = lamv + TY * TX;
+  float* f1x = mutx + TY * TX;
+  float* lamt = f1x + TY * TX;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(lam + TY * TX + NXV * TY * TX);  // [NR]
   __shared__ int abort_flag;
   const Dims& d = p.d;
   const int lane = threadIdx.x, w = threadIdx.y, tid = w * TX + lane;
@@ -490,7 +650,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       if (e < NV * SH * SW) dst[e] = __ldg(src + off[m]);
     }
   };
-  // FP32 path: plane c of the mirror -> ring slot, box (40 x 12 x 1 x 5)
+  // FP32 path: plane c of the mirror -> ring slot, box (40 x 12 x 1 x NV)
   // at array coordinates (30*bx - ox, 6*by, c+2, 0); columns or rows past
   // the array are zero-filled and feed only discarded halo lanes
   constexpr uint32_t kPlaneBytes = (uint32_t)(NV * SH * RW * sizeof(T));
@@ -516,10 +676,13 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
 #pragma unroll
   for (int l = 0; l < NV; ++l) { Lp_prev[l] = 0; H_prev[l] = 0; dF_prev[l] = 0; dG_prev[l] = 0; }
   // viscous march state: raw gradient of cell (i, j, k-1), viscous dt terms
-  float Gprev[VISC ? 12 : 1];
+  float Gprev[VISC ? NGC : 1];
 #pragma unroll
-  for (int m = 0; m < (VISC ? 12 : 1); ++m) Gprev[m] = 0.0f;
+  for (int m = 0; m < (VISC ? NGC : 1); ++m) Gprev[m] = 0.0f;
   float lvk_prev = 0, lvi_lo_prev = 0, lvi_hi_prev = 0, lvj_lo_prev = 0, lvj_hi_prev = 0;
+  // SST march state: mu_t, F1 and source of cell (i, j, k-1), turbulent dt terms
+  float mut_prev = 0, F1_prev = 0, Sk_prev = 0, Sw_prev = 0;
+  float ltk_prev = 0, lti_lo_prev = 0, lti_hi_prev = 0, ltj_lo_prev = 0, ltj_hi_prev = 0;
   const float Rg = (float)p.R;
   const int VS = SH * RW;  // variable stride in a ring plane
 
@@ -553,22 +716,25 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
 #pragma unroll
     for (int l = 0; l < NV; ++l) qc[l] = own[l * SH * RW];
     // viscous: this cell's values, centre, viscosity and raw Green-Gauss
-    // gradient (every thread, halo included)
+    // gradient (every thread, halo included); SST: its mu_t, F1 and source
     ViscCell Vc{};
     float4 cown = make_float4(1.f, 0.f, 0.f, 0.f);
-    float muc = 0.f, Gc[VISC ? 12 : 1];
+    float muc = 0.f, Gc[VISC ? NGC : 1];
     float lvi_lo = 0, lvi_hi = 0, lvj_lo = 0, lvj_hi = 0;
+    SstCell Sc{0.f, 0.f, 0.f, 0.f};
+    float ddc = 1.f, Skc = 0.f, Swc = 0.f;
+    float lti_lo = 0, lti_hi = 0, ltj_lo = 0, ltj_hi = 0;
     const int ci_ = clampi(i, d.imx), cj_ = clampi(j, d.jmx);
     if constexpr (VISC) {
       const float* o = reinterpret_cast<const float*>(own);
-      Vc = visc_cell(o, VS, Rg);
+      Vc = visc_cell<TURB>(o, VS, Rg);
       ViscCell nb[6];
-      nb[0] = visc_cell(o - 1, VS, Rg);
-      nb[1] = visc_cell(o - RW, VS, Rg);
-      nb[2] = visc_cell(reinterpret_cast<const float*>(ring + slot(k - 1) * plane + r * RW + cc), VS, Rg);
-      nb[3] = visc_cell(o + 1, VS, Rg);
-      nb[4] = visc_cell(o + RW, VS, Rg);
-      nb[5] = visc_cell(reinterpret_cast<const float*>(ring + slot(k + 1) * plane + r * RW + cc), VS, Rg);
+      nb[0] = visc_cell<TURB>(o - 1, VS, Rg);
+      nb[1] = visc_cell<TURB>(o - RW, VS, Rg);
+      nb[2] = visc_cell<TURB>(reinterpret_cast<const float*>(ring + slot(k - 1) * plane + r * RW + cc), VS, Rg);
+      nb[3] = visc_cell<TURB>(o + 1, VS, Rg);
+      nb[4] = visc_cell<TURB>(o + RW, VS, Rg);
+      nb[5] = visc_cell<TURB>(reinterpret_cast<const float*>(ring + slot(k + 1) * plane + r * RW + cc), VS, Rg);
       const int ci1 = clampi(i + 1, d.imx + 1), cj1 = clampi(j + 1, d.jmx + 1);
       float4 fgg[6];
       fgg[0] = __ldg(a.faces32[0] + fidx(d, 0, ci_, cj_, k));
@@ -578,8 +744,13 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       fgg[4] = __ldg(a.faces32[1] + fidx(d, 1, ci_, cj1, k));
       fgg[5] = __ldg(a.faces32[2] + fidx(d, 2, ci_, cj_, k + 1));
       cown = __ldg(a.cells32 + pidx(d, ci_, cj_, k));
-      visc_gg(Vc, nb, fgg, cown.x, thin, Gc);
+      visc_gg<NGV>(Vc, nb, fgg, cown.x, thin, Gc);
       muc = visc_mu(p, Vc.T);
+      if constexpr (TURB) {
+        ddc = __ldg(a.dist32 + pidx(d, ci_, cj_, k));
+        Sc = sst_cell(p, Vc, muc, ddc, Gc);
+        if (kin && in_i && in_j) sst_source(p, Vc, Sc, Gc, cown.x, Skc, Swc);
+      }
     }
     // ---------------- i-faces (warp shuffles) ----------------
     if (kin && in_j) {  // warp-uniform
@@ -601,21 +772,41 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       if (a.compute_dt) lami_lo = lambda_face<T>(gm, L, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
       lami_hi = __shfl_down_sync(0xffffffffu, lami_lo, 1);
       if constexpr (VISC) {  // viscous flux of the low i-face (cells i-1, i)
-        float Gl[12], GL[12], GR[12], Fv[4];
+        float Gl[NGC], GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
 #pragma unroll
-        for (int m = 0; m < 12; ++m) Gl[m] = __shfl_up_sync(0xffffffffu, Gc[m], 1);
-        const ViscCell VL = visc_cell(reinterpret_cast<const float*>(own) - 1, VS, Rg);
+        for (int m = 0; m < NGC; ++m) Gl[m] = __shfl_up_sync(0xffffffffu, Gc[m], 1);
+#pragma unroll
+        for (int m = 0; m < NGC; ++m) { GL[m] = Gl[m]; GR[m] = Gc[m]; }
+        const ViscCell VL = visc_cell<TURB>(reinterpret_cast<const float*>(own) - 1, VS, Rg);
         const float4 cL = __ldg(a.cells32 + pidx(d, clampi(i - 1, d.imx), cj_, k));
         const float4 fc = make_float4(A, nx, ny, nz);
-#pragma unroll
-        for (int m = 0; m < 12; ++m) { GL[m] = Gl[m]; GR[m] = Gc[m]; }
-        if (i - 1 == 0 && p.id[0] < 0) visc_gbc(p, 0, Gc, Vc, VL, cown.x, fc, GL);
-        if (i == d.imx && p.id[1] < 0) visc_gbc(p, 1, Gl, VL, Vc, cL.x, fc, GR);
-        visc_flux(p, GL, GR, VL, Vc, cL, cown, visc_mu(p, VL.T), muc, fc, Fv);
+        const float muL = visc_mu(p, VL.T);
+        float mutL = 0.f, F1L = 0.f, mutR = Sc.mut, F1R = Sc.F1;
+        if constexpr (TURB) {
+          mutL = __shfl_up_sync(0xffffffffu, Sc.mut, 1);
+          F1L = __shfl_up_sync(0xffffffffu, Sc.F1, 1);
+        }
+        const float mutLi = mutL, F1Li = F1L;
+        if (i - 1 == 0 && p.id[0] < 0) {
+          visc_gbc<NGV>(p, 0, Gc, Vc, VL, cown.x, fc, GL);
+          if constexpr (TURB)
+            sst_ghost(p, 0, VL, muL, GL, __ldg(a.dist32 + pidx(d, clampi(i - 1, d.imx), cj_, k)), Sc.mut, Sc.F1,
+                      mutL, F1L);
+        }
+        if (i == d.imx && p.id[1] < 0) {
+          visc_gbc<NGV>(p, 1, Gl, VL, Vc, cL.x, fc, GR);
+          if constexpr (TURB) sst_ghost(p, 1, Vc, muc, GR, ddc, mutLi, F1Li, mutR, F1R);
+        }
+        visc_flux<TURB>(p, GL, GR, VL, Vc, cL, cown, muL, muc, mutL, mutR, F1L, F1R, fc, true, Fv);
 #pragma unroll
         for (int l = 0; l < 4; ++l) F[1 + l] -= Fv[l];
-        if (a.compute_dt) lvi_lo = visc_lambda(fc, cL, cown, muc, Vc.rho);
+        if constexpr (TURB) { F[5] -= Fv[4]; F[6] -= Fv[5]; }
+        if (a.compute_dt) {
+          lvi_lo = visc_lambda(fc, cL, cown, muc, Vc.rho);
+          if constexpr (TURB) lti_lo = visc_lambda(fc, cL, cown, mutR, Vc.rho);
+        }
         lvi_hi = __shfl_down_sync(0xffffffffu, lvi_lo, 1);
+        if constexpr (TURB) lti_hi = __shfl_down_sync(0xffffffffu, lti_lo, 1);
       }
 #pragma unroll
       for (int l = 0; l < NV; ++l) {
@@ -638,9 +829,14 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       }
 #pragma unroll
       for (int l = 0; l < NV; ++l) xch[(l * TY + w) * TX + lane] = Lp[l];
-      if constexpr (VISC)
+      if constexpr (VISC) {
 #pragma unroll
-        for (int m = 0; m < 12; ++m) gxch[(m * TY + w) * TX + lane] = Gc[m];
+        for (int m = 0; m < NGC; ++m) gxch[(m * TY + w) * TX + lane] = Gc[m];
+        if constexpr (TURB) {
+          mutx[w * TX + lane] = Sc.mut;
+          f1x[w * TX + lane] = Sc.F1;
+        }
+      }
       __syncthreads();
       T F[NV];
 #pragma unroll
@@ -653,22 +849,42 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         load_face(a, 1, fidx(d, 1, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
         face_flux<T, FLUX>(p, L, Rm, A, nx, ny, nz, (T)wall_mask(p, 1, j), F);
         if constexpr (VISC) {  // viscous flux of the low j-face (cells j-1, j)
-          float Gd[12], GL[12], GR[12], Fv[4];
+          float Gd[NGC], GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
 #pragma unroll
-          for (int m = 0; m < 12; ++m) Gd[m] = gxch[(m * TY + w - 1) * TX + lane];
-          const ViscCell VD = visc_cell(reinterpret_cast<const float*>(own) - RW, VS, Rg);
+          for (int m = 0; m < NGC; ++m) Gd[m] = gxch[(m * TY + w - 1) * TX + lane];
+          const ViscCell VD = visc_cell<TURB>(reinterpret_cast<const float*>(own) - RW, VS, Rg);
           const float4 cD = __ldg(a.cells32 + pidx(d, ci_, clampi(j - 1, d.jmx), k));
           const float4 fc = make_float4(A, nx, ny, nz);
+          const float muD = visc_mu(p, VD.T);
+          float mutD = 0.f, F1D = 0.f, mutR = Sc.mut, F1R = Sc.F1;
+          if constexpr (TURB) {
+            mutD = mutx[(w - 1) * TX + lane];
+            F1D = f1x[(w - 1) * TX + lane];
+          }
+          const float mutDi = mutD, F1Di = F1D;
 #pragma unroll
-          for (int m = 0; m < 12; ++m) { GL[m] = Gd[m]; GR[m] = Gc[m]; }
-          if (j - 1 == 0 && p.id[2] < 0) visc_gbc(p, 2, Gc, Vc, VD, cown.x, fc, GL);
-          if (j == d.jmx && p.id[3] < 0) visc_gbc(p, 3, Gd, VD, Vc, cD.x, fc, GR);
-          visc_flux(p, GL, GR, VD, Vc, cD, cown, visc_mu(p, VD.T), muc, fc, Fv);
+          for (int m = 0; m < NGC; ++m) { GL[m] = Gd[m]; GR[m] = Gc[m]; }
+          if (j - 1 == 0 && p.id[2] < 0) {
+            visc_gbc<NGV>(p, 2, Gc, Vc, VD, cown.x, fc, GL);
+            if constexpr (TURB)
+              sst_ghost(p, 2, VD, muD, GL, __ldg(a.dist32 + pidx(d, ci_, clampi(j - 1, d.jmx), k)), Sc.mut,
+                        Sc.F1, mutD, F1D);
+          }
+          if (j == d.jmx && p.id[3] < 0) {
+            visc_gbc<NGV>(p, 3, Gd, VD, Vc, cD.x, fc, GR);
+            if constexpr (TURB) sst_ghost(p, 3, Vc, muc, GR, ddc, mutDi, F1Di, mutR, F1R);
+          }
+          visc_flux<TURB>(p, GL, GR, VD, Vc, cD, cown, muD, muc, mutD, mutR, F1D, F1R, fc, true, Fv);
 #pragma unroll
           for (int l = 0; l < 4; ++l) F[1 + l] -= Fv[l];
+          if constexpr (TURB) { F[5] -= Fv[4]; F[6] -= Fv[5]; }
           if (a.compute_dt) {
             lvj_lo = visc_lambda(fc, cD, cown, muc, Vc.rho);
             lamv[w * TX + lane] = lvj_lo;
+            if constexpr (TURB) {
+              ltj_lo = visc_lambda(fc, cD, cown, mutR, Vc.rho);
+              lamt[w * TX + lane] = ltj_lo;
+            }
           }
         }
 #pragma unroll
@@ -686,7 +902,10 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         for (int l = 0; l < NV; ++l) dG[l] = gfl[(l * TY + w + 1) * TX + lane] - F[l];
         if (a.compute_dt) lamj_hi = lam[(w + 1) * TX + lane];
         if constexpr (VISC)
-          if (a.compute_dt) lvj_hi = lamv[(w + 1) * TX + lane];
+          if (a.compute_dt) {
+            lvj_hi = lamv[(w + 1) * TX + lane];
+            if constexpr (TURB) ltj_hi = lamt[(w + 1) * TX + lane];
+          }
       }
     } else {
       __syncthreads();
@@ -705,7 +924,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       }
       T H[NV];
       T lamk = 0;
-      float lvk = 0;
+      float lvk = 0, ltk = 0;
       if (k >= k0) {
         T A, nx, ny, nz;
         load_face(a, 2, fidx(d, 2, i, j, k), A, nx, ny, nz);
@@ -717,19 +936,32 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         }
         if (a.compute_dt) lamk = lambda_face<T>(gm, Lp_prev, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
         if constexpr (VISC) {  // viscous flux of the low k-face (cells k-1, k)
-          float GL[12], GR[12], Fv[4];
-          const ViscCell VK = visc_cell(reinterpret_cast<const float*>(ring + slot(k - 1) * plane + r * RW + cc),
-                                        VS, Rg);
+          float GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
+          const ViscCell VK = visc_cell<TURB>(
+              reinterpret_cast<const float*>(ring + slot(k - 1) * plane + r * RW + cc), VS, Rg);
           const float4 cK = __ldg(a.cells32 + pidx(d, i, j, k - 1));
           const float4 fc = make_float4(A, nx, ny, nz);
+          const float muK = visc_mu(p, VK.T);
+          float mutK = mut_prev, F1K = F1_prev, mutR = Sc.mut, F1R = Sc.F1;
 #pragma unroll
-          for (int m = 0; m < 12; ++m) { GL[m] = Gprev[m]; GR[m] = Gc[m]; }
-          if (k - 1 == 0 && p.id[4] < 0) visc_gbc(p, 4, Gc, Vc, VK, cown.x, fc, GL);
-          if (k == d.kmx && p.id[5] < 0) visc_gbc(p, 5, Gprev, VK, Vc, cK.x, fc, GR);
-          visc_flux(p, GL, GR, VK, Vc, cK, cown, visc_mu(p, VK.T), muc, fc, Fv);
+          for (int m = 0; m < NGC; ++m) { GL[m] = Gprev[m]; GR[m] = Gc[m]; }
+          if (k - 1 == 0 && p.id[4] < 0) {
+            visc_gbc<NGV>(p, 4, Gc, Vc, VK, cown.x, fc, GL);
+            if constexpr (TURB)
+              sst_ghost(p, 4, VK, muK, GL, __ldg(a.dist32 + pidx(d, i, j, k - 1)), Sc.mut, Sc.F1, mutK, F1K);
+          }
+          if (k == d.kmx && p.id[5] < 0) {
+            visc_gbc<NGV>(p, 5, Gprev, VK, Vc, cK.x, fc, GR);
+            if constexpr (TURB) sst_ghost(p, 5, Vc, muc, GR, ddc, mut_prev, F1_prev, mutR, F1R);
+          }
+          visc_flux<TURB>(p, GL, GR, VK, Vc, cK, cown, muK, muc, mutK, mutR, F1K, F1R, fc, !thin, Fv);
 #pragma unroll
           for (int l = 0; l < 4; ++l) H[1 + l] -= Fv[l];
-          if (a.compute_dt) lvk = visc_lambda(fc, cK, cown, muc, Vc.rho);
+          if constexpr (TURB) { H[5] -= Fv[4]; H[6] -= Fv[5]; }
+          if (a.compute_dt) {
+            lvk = visc_lambda(fc, cK, cown, muc, Vc.rho);
+            if constexpr (TURB) ltk = visc_lambda(fc, cK, cown, mutR, Vc.rho);
+          }
         }
         if (a.mflux[2] && (k == 1 || k == d.kmx)) a.mflux[2][flidx(fldim(d, 2), i, j, k)] = (double)H[0];
         if (k >= k0 + 1) {
@@ -739,6 +971,10 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
           T R[NV];
 #pragma unroll
           for (int l = 0; l < NV; ++l) R[l] = (dF_prev[l] + dG_prev[l]) + (H[l] - H_prev[l]);
+          if constexpr (TURB) {  // add_sst_source (source.f90:265-266)
+            R[5] = R[5] - Sk_prev;
+            R[6] = R[6] - Sw_prev;
+          }
           const T vol_c = cell_vol(a, T(0), c0);
           T dtc;
           if (a.compute_dt) {
@@ -750,6 +986,12 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
               sv = 2.0f / (sv + (2.0f * (float)a.CFL * vol_c / dtc));
               dtc = (float)a.CFL * (sv * vol_c);
             }
+            if constexpr (TURB) {  // add_turbulent_time (time.f90:450-531)
+              float st = lti_lo_prev + ltj_lo_prev + ltk_prev + lti_hi_prev + ltj_hi_prev + ltk;
+              st = (float)p.gm * st / (float)p.tPr;
+              st = 2.0f / (st + (2.0f * (float)a.CFL * vol_c / dtc));
+              dtc = (float)a.CFL * (st * vol_c);
+            }
             a.dt[ci] = (double)dtc;
           } else {
             dtc = (T)a.dt[ci];
@@ -758,13 +1000,15 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
 #pragma unroll
             for (int l = 0; l < NV; ++l) a.res_out[ci + ncells(d) * l] = (double)R[l];
           // the finished cell's own stencil values (plane k-1 of the ring)
-          T qo[5];
+          T qo[NV];
           const T* own1 = ring + slot(kc) * plane + r * RW + cc;
 #pragma unroll
-          for (int l = 0; l < 5; ++l) qo[l] = own1[l * SH * RW];
+          for (int l = 0; l < NV; ++l) qo[l] = own1[l * SH * RW];
           const long long m0 = (long long)(i + 2) + (long long)a.mpitch * ((j + 2) + (long long)d.nj * (kc + 2));
-          if (!update_cell(p, a, c0, ci, R, dtc, vol_c, qo, m0))
-            raise_error(a.err, FEST_ERR_NEGATIVE_STATE);
+          bool ok;
+          if constexpr (kTma) ok = update_cell_f32<NV>(p, a, c0, ci, R, dtc, vol_c, qo, m0, F1_prev);
+          else ok = update_cell(p, a, c0, ci, R, dtc, vol_c, qo, m0);
+          if (!ok) raise_error(a.err, FEST_ERR_NEGATIVE_STATE);
         }
       }
 #pragma unroll
@@ -780,11 +1024,22 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       }
       if constexpr (VISC) {
 #pragma unroll
-        for (int m = 0; m < 12; ++m) Gprev[m] = Gc[m];
+        for (int m = 0; m < NGC; ++m) Gprev[m] = Gc[m];
         if (k >= k0) lvk_prev = lvk;
         if (kin) {
           lvi_lo_prev = lvi_lo; lvi_hi_prev = lvi_hi;
           lvj_lo_prev = lvj_lo; lvj_hi_prev = lvj_hi;
+        }
+      }
+      if constexpr (TURB) {
+        mut_prev = Sc.mut;
+        F1_prev = Sc.F1;
+        Sk_prev = Skc;
+        Sw_prev = Swc;
+        if (k >= k0) ltk_prev = ltk;
+        if (kin) {
+          lti_lo_prev = lti_lo; lti_hi_prev = lti_hi;
+          ltj_lo_prev = ltj_lo; ltj_hi_prev = ltj_hi;
         }
       }
     }
@@ -794,10 +1049,10 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
 // MB: CTAs per SM the registers are budgeted for (FP32: 2 = 115 registers,
 // no spills, fewer instructions; 3 = 80 registers, more warps to hide
 // latency on large blocks; the tuner picks per block)
-template <typename T, int INTERP, int FLUX, int MB, bool VISC = false>
+template <typename T, int INTERP, int FLUX, int MB, bool VISC = false, bool TURB = false>
 __global__ void __launch_bounds__(TX* TY, MB)
     k_stage(Params p, StageArgs a, const __grid_constant__ CUtensorMap tm) {
-  stage_body<T, INTERP, FLUX, VISC>(p, a, &tm, blockIdx.x, blockIdx.y, blockIdx.z);
+  stage_body<T, INTERP, FLUX, VISC, TURB>(p, a, &tm, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // One launch for every block of a batch: block b owns CTAs
@@ -833,9 +1088,10 @@ __global__ void __launch_bounds__(TX* TY, VISC ? 2 : (sizeof(T) == 4 ? 3 : 1))
   stage_body<T, INTERP, FLUX, VISC>(sp, sa, &E.tm, local % E.tx, (local / E.tx) % E.ty, local / (E.tx * E.ty));
 }
 
-template <typename T, bool VISC = false> inline size_t stage_smem() {
-  return sizeof(T) * ((size_t)RingGeom<T>::N * 5 * SH * RingGeom<T>::W + 2 * 5 * TY * TX + TY * TX) +
-         (VISC ? sizeof(float) * 13 * TY * TX : 0) + sizeof(uint64_t) * RingGeom<T>::N + 16;
+template <typename T, bool VISC = false, bool TURB = false> inline size_t stage_smem() {
+  constexpr size_t NV = TURB ? 7 : 5, NXV = VISC ? (TURB ? 18 + 4 : 12 + 1) : 0;
+  return sizeof(T) * ((size_t)RingGeom<T>::N * NV * SH * RingGeom<T>::W + 2 * NV * TY * TX + TY * TX) +
+         sizeof(float) * NXV * TY * TX + sizeof(uint64_t) * RingGeom<T>::N + 16;
 }
 
 
@@ -845,6 +1101,12 @@ template <typename T, bool VISC = false> inline size_t stage_smem() {
 #define FEST_STAGE_LAUNCHER(name)                                                         \
   int name(int prec, int flux, int occ, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a, \
            const CUtensorMap& tm)
+// the SST FP32 sweeps (fest_stage_<method>_sst.cu)
+FEST_STAGE_LAUNCHER(launch_stage_none_sst);
+FEST_STAGE_LAUNCHER(launch_stage_muscl_sst);
+FEST_STAGE_LAUNCHER(launch_stage_ppm_sst);
+FEST_STAGE_LAUNCHER(launch_stage_weno_sst);
+FEST_STAGE_LAUNCHER(launch_stage_weno_nm_sst);
 // the laminar-viscous FP32 sweeps (fest_stage_<method>_visc.cu)
 FEST_STAGE_LAUNCHER(launch_stage_none_visc);
 FEST_STAGE_LAUNCHER(launch_stage_muscl_visc);
@@ -928,6 +1190,37 @@ int launch_stage_visc_t(int flux, dim3 grid, cudaStream_t s, const Params& p, co
   }
 #undef FEST_SET
 #define FEST_GO(F) k_stage<float, INTERP, F, 2, true><<<grid, blk, smem, s>>>(p, a, tm)
+  switch (flux) {
+    case 0: FEST_GO(0); break;
+    case 1: FEST_GO(1); break;
+    case 2: FEST_GO(2); break;
+    case 3: FEST_GO(3); break;
+    case 4: FEST_GO(4); break;
+    case 5: FEST_GO(5); break;
+    default: return FEST_ERR_ARG;
+  }
+#undef FEST_GO
+  return FEST_OK;
+}
+
+// the SST FP32 sweep: seven variables and the SST exchange need ~118 KB
+// of shared memory, so one CTA per SM with the whole register file
+template <int INTERP>
+int launch_stage_sst_t(int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a,
+                       const CUtensorMap& tm) {
+  using namespace stage;
+  const dim3 blk(TX, TY);
+  static bool attrs = false;
+  const size_t smem = stage_smem<float, true, true>();
+#define FEST_SET(F)                                                                                          \
+  cudaFuncSetAttribute(k_stage<float, INTERP, F, 1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)smem)
+  if (!attrs) {
+    FEST_SET(0); FEST_SET(1); FEST_SET(2); FEST_SET(3); FEST_SET(4); FEST_SET(5);
+    attrs = true;
+  }
+#undef FEST_SET
+#define FEST_GO(F) k_stage<float, INTERP, F, 1, true, true><<<grid, blk, smem, s>>>(p, a, tm)
   switch (flux) {
     case 0: FEST_GO(0); break;
     case 1: FEST_GO(1); break;

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from fest3d import abi
+from fest3d import abi, cases
 from parity import make_pair, rel_err, small_case
 
 pytestmark = pytest.mark.gpu
@@ -51,6 +51,26 @@ VISC_COMBOS = {
     "lam-none-vanleer": dict(scheme_kw=dict(interpolant="none", scheme_name="van_leer"),
                              ids=(-1, -4, -5, -6, -10, -10),
                              flow_kw=dict(mu_ref=5e-2, mu_variation="constant")),
+}
+# k-omega SST in the FP32 sweep: seven variables, eddy viscosity and F1 per
+# cell, SST face, source and time-step terms, point-implicit destruction;
+# wall distances from the -5 faces' nodes
+SST_COMBOS = {
+    "sst-muscl-ausmUP": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ausmUP"),
+                             ids=(-3, -4, -5, -4, -10, -10),
+                             flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law", MInf=0.2)),
+    "sst2003-weno-slau": dict(scheme_kw=dict(interpolant="weno", scheme_name="slau", turbulence="sst2003"),
+                              ids=(-11, -4, -5, -6, -10, -10),
+                              flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law")),
+    "sst-ppm-ausmP-slip": dict(scheme_kw=dict(interpolant="ppm", scheme_name="ausmP"),
+                               ids=(-3, -4, -5, -6, -6, -6),
+                               flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law")),
+    "sst-none-vanleer-farfield": dict(scheme_kw=dict(interpolant="none", scheme_name="van_leer"),
+                                      ids=(-8, -4, -5, -6, -10, -10),
+                                      flow_kw=dict(mu_ref=5e-2, mu_variation="constant")),
+    "sst-wenoNM-ldfss-walls": dict(scheme_kw=dict(interpolant="weno_NM", scheme_name="ldfss0"),
+                                   ids=(-5, -4, -5, -5, -10, -10),
+                                   flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law")),
 }
 COMBOS_ALL = dict(COMBOS, **VISC_COMBOS)
 
@@ -101,28 +121,80 @@ def test_fused_mixed_viscous(gpu_lib, name, acc):
     assert e <= 2e-5, f"mixed viscous interior state differs by {e:.3e}"
 
 
+def run_sst_pair(name, acc, precision, iters=6, nc=(37, 14, 5), ids=None):
+    kw = dict(SST_COMBOS[name])
+    sk = dict(kw.pop("scheme_kw"))
+    sk["time_step_accuracy"] = acc
+    if ids is not None:
+        kw["ids"] = ids
+    ext, flow, scheme, bc, nodes, qp = small_case(scheme_kw=sk, turb=True, nc=nc, **kw)
+    wall = cases.wall_nodes_of(nodes, ext, bc)
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp, wall=wall)
+    h.set_precision(precision)
+    norm = h.step(iters, 1, 0.5)
+    for it in range(1, iters + 1):
+        assert O.get_next_solution([blk], it, 0.5) == 0
+    return ext, blk, h, h.download_state(), norm
+
+
+@pytest.mark.parametrize("name", list(SST_COMBOS))
+@pytest.mark.parametrize("acc", ["none", "TVDRK3", "RK4"])
+def test_fused_mixed_sst(gpu_lib, name, acc):
+    ext, blk, h, q, norm = run_sst_pair(name, acc, abi.FEST_MIXED)
+    e = rel_err(interior(q, ext), interior(blk["qp"], ext))
+    assert e <= 2e-5, f"mixed SST interior state differs by {e:.3e}"
+    ref = O.find_resnorm([blk])
+    assert np.allclose(norm[1:], ref[1:], rtol=2e-2), (norm, ref)
+
+
+def test_fused_mixed_sst_single_plane(gpu_lib):
+    """a flat-plate-like single-plane block (kmx = 2, slip k faces): the
+    mixed sweep reads ghost layer 1 only, so it runs where the FP64 fused
+    path needs the in-place module path"""
+    ext, blk, h, q, norm = run_sst_pair("sst-muscl-ausmUP", "RK4", abi.FEST_MIXED, nc=(40, 9, 1),
+                                        ids=(-3, -4, -5, -4, -6, -6))
+    e = rel_err(interior(q, ext), interior(blk["qp"], ext))
+    assert e <= 2e-5, f"mixed SST single-plane interior state differs by {e:.3e}"
+
+
+def test_fp64_sst_takes_module_path(gpu_lib):
+    """FP64 SST blocks step through the module kernels: exact."""
+    ext, blk, h, q, norm = run_sst_pair("sst-muscl-ausmUP", "RK4", abi.FEST_FP64, iters=3)
+    assert rel_err(q, blk["qp"]) <= 1e-11
+
+
 def test_fp64_viscous_takes_module_path(gpu_lib):
     """FP64 viscous blocks step through the module kernels: exact."""
     ext, blk, h, q, norm = run_pair("suth-weno-slau", "TVDRK3", abi.FEST_FP64)
     assert rel_err(q, blk["qp"]) <= 1e-11
 
 
-@pytest.mark.parametrize("nc,ids", [((40, 9, 1), (-3, -4, -6, -5, -6, -6)),
-                                    ((37, 14, 5), (-1, -4, -6, -6, -9, -9))])
-def test_in_place_cases_use_module_path(gpu_lib, nc, ids):
+@pytest.mark.parametrize("nc,ids,acc,mixed_runs", [((40, 9, 1), (-3, -4, -6, -5, -6, -6), "RK4", True),
+                                                   ((40, 9, 1), (-3, -4, -6, -5, -6, -6), "TVDRK3", False),
+                                                   ((37, 14, 5), (-1, -4, -6, -6, -9, -9), "TVDRK3", False)])
+def test_in_place_cases_use_module_path(gpu_lib, nc, ids, acc, mixed_runs):
     """thin blocks and -9 faces read other faces' ghosts: FP64 fest_step
-    runs the in-place module path (exact), FEST_MIXED refuses them."""
+    runs the in-place module path (exact).  FEST_MIXED runs the thin block
+    with the reference's face order (its interior updates read ghost layer
+    1 only, the symmetric faces the opposite face's layer 1) unless a TVD
+    integrator blends those ghosts between fills; it refuses -9."""
     ext, flow, scheme, bc, nodes, qp = small_case(
         nc=nc, ids=ids, scheme_kw=dict(interpolant="muscl", scheme_name="ausm",
-                                       time_step_accuracy="TVDRK3"))
+                                       time_step_accuracy=acc))
     blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
     h.step(3, 1, 0.5)
     for it in (1, 2, 3):
         assert O.get_next_solution([blk], it, 0.5) == 0
     assert rel_err(h.download_state(), blk["qp"]) <= 1e-11
     h.set_precision(abi.FEST_MIXED)
-    with pytest.raises(abi.FestError):
-        h.step(1, 4, 0.5)
+    if mixed_runs:
+        h.step(3, 4, 0.5)
+        for it in (4, 5, 6):
+            assert O.get_next_solution([blk], it, 0.5) == 0
+        assert rel_err(interior(h.download_state(), ext), interior(blk["qp"], ext)) <= 2e-5
+    else:
+        with pytest.raises(abi.FestError):
+            h.step(1, 4, 0.5)
 
 
 def test_fused_state_roundtrip_and_module_interplay(gpu_lib):
