@@ -32,6 +32,7 @@ struct fest_handle {
   FusedState* fused = nullptr;
   double* d_vjp_bar = nullptr;  // adjoint work arrays, allocated on first use
   double* d_vjp_lam = nullptr;
+  int* h_err = nullptr;          // pinned host copy of the device error word
   std::vector<void*> allocs;
   Launcher L() { return Launcher{s, &launches}; }
 };
@@ -93,9 +94,15 @@ int down(fest_handle* h, double* dst, const double* src, long long n) {
 // wait for the stream; report CUDA errors, then the device error word
 int finish(fest_handle* h) {
   CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(h->s));
   int err = 0;
-  CK(cudaMemcpy(&err, h->d.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h->h_err) {  // the error word rides on the stream: one synchronisation
+    CK(cudaMemcpyAsync(h->h_err, h->d.err, sizeof(int), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    err = *h->h_err;
+  } else {
+    CK(cudaStreamSynchronize(h->s));
+    CK(cudaMemcpy(&err, h->d.err, sizeof(int), cudaMemcpyDeviceToHost));
+  }
   if (err) {
     CK(cudaMemset(h->d.err, 0, sizeof(int)));
     return err;
@@ -362,6 +369,12 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
       h->allocs.push_back(b.err);
       cudaMemsetAsync(b.err, 0, sizeof(int), h->s);
     }
+    // pinned host word for the error check (without it finish() reads the
+    // device word synchronously)
+    if (cudaMallocHost((void**)&h->h_err, sizeof(int)) != cudaSuccess) {
+      h->h_err = nullptr;
+      cudaGetLastError();
+    }
   }
   if (rc == FEST_OK) {
     // setup_viscosity: mu = mu_ref everywhere (viscosity.f90:562-566)
@@ -390,6 +403,7 @@ int fest_destroy(fest_handle* h) {
   if (h->fused) fused_destroy(h->fused);
   for (void* p : h->allocs) cudaFree(p);
   if (h->own) cudaStreamDestroy(h->own);
+  if (h->h_err) cudaFreeHost(h->h_err);
   delete h;
   return FEST_OK;
 }
@@ -501,8 +515,10 @@ int fest_upload_state(fest_handle* h, const double* qp) {
 
 int fest_download_state(fest_handle* h, double* qp) {
   if (!h || !qp) return FEST_ERR_ARG;
-  RET(sync_fused(h));
-  RET(down(h, qp, h->d.qp, h->p.d.P * h->p.d.nv));
+  // reading leaves the fused path's buffers as they are (no re-seeding at
+  // the next step)
+  const double* cur = fused_current_state(h->fused);
+  RET(down(h, qp, cur ? cur : h->d.qp, h->p.d.P * h->p.d.nv));
   return finish(h);
 }
 

@@ -36,11 +36,12 @@ __global__ void k_ghost_blend(Dims d, double* q, float* q32, int pitch, const do
 // FP32 mirrors for the mixed sweep: state (whole padded array), face
 // records {A,nx,ny,nz} and cell volumes.  Rounding to nearest, as a
 // conversion on load would do.
+// one row (j, k, variable) of the padded array per blockIdx.y
 __global__ void k_to_mirror(Dims d, int pitch, const double* src, float* dst) {
-  const long long n = d.P * d.nv;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x)
-    dst[mirror_index(d, pitch, t % d.P, (int)(t / d.P))] = (float)src[t];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ni) return;
+  const long long row = blockIdx.y;  // (j + 2) + nj*((k + 2) + nk*l)
+  dst[row * pitch + i] = (float)src[row * d.ni + i];
 }
 __global__ void k_faces_to_f32(const double* faces, float4* dst, long long n) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
@@ -354,6 +355,7 @@ struct FusedState {
   bool visc = false;
   bool turb = false;
   bool mirror_valid = false;  // Q32 interiors match Q
+  bool buffers_equal = false;  // Q[0..2] hold the same state (just seeded)
   int kc[2] = {0, 0};         // tuned k-chunk per precision (0: not tuned yet)
   int occ[2] = {1, 2};        // tuned register budget (CTAs per SM) per precision
   int mpitch = 0;             // row pitch of Q32
@@ -475,6 +477,7 @@ static void seed(FusedState* f, cudaStream_t s) {
     if (n != f->cur) cudaMemcpyAsync(f->Q[n], f->Q[f->cur], bytes, cudaMemcpyDeviceToDevice, s);
   f->seeded = true;
   f->mirror_valid = false;
+  f->buffers_equal = true;
 }
 
 // allocate and fill the FP32 mirrors the mixed sweep reads (once per
@@ -546,9 +549,15 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
   if (!f->mirror_valid) {
     // whole padded arrays, so that the edge and corner cells the halo lanes
     // read (results discarded) hold finite values
+    // (pitch padding columns are outside the tensor map: never read); equal
+    // FP64 buffers share one conversion
+    const dim3 g((d.ni + 127) / 128, (unsigned)((long long)d.nj * d.nk * d.nv));
     for (int m = 0; m < 3; ++m) {
-      // pitch padding columns are outside the tensor map: never read
-      k_to_mirror<<<grid_for(d.P * d.nv), 256, 0, s>>>(d, f->mpitch, f->Q[m], f->Q32[m]);
+      if (m > 0 && f->buffers_equal) {
+        cudaMemcpyAsync(f->Q32[m], f->Q32[0], sizeof(float) * (size_t)f->m_elems, cudaMemcpyDeviceToDevice, s);
+        continue;
+      }
+      k_to_mirror<<<g, 128, 0, s>>>(d, f->mpitch, f->Q[m], f->Q32[m]);
       ++*cnt;
     }
     f->mirror_valid = true;
@@ -893,6 +902,7 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
   } else {
     f->mirror_valid = false;  // FP64 stages do not maintain the mirror
   }
+  if (n_iters > 0) f->buffers_equal = false;
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(s, &cap);
   for (int n = 0; n < n_iters; ++n) {
@@ -918,6 +928,8 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
   }
   return FEST_OK;
 }
+
+const double* fused_current_state(const FusedState* f) { return f && f->seeded ? f->Q[f->cur] : nullptr; }
 
 int fused_export_state(FusedState* f, double* qp, cudaStream_t s) {
   if (!f) return FEST_ERR_ARG;
@@ -1198,6 +1210,7 @@ int fused_batch_run(FusedBatch* B, int n_iters, int first_iter, double CFL, cuda
     if (!f->seeded) seed(f, s);
     int rc = ensure_mirrors(f, B->b[n], s, cnt);
     if (rc) return rc;
+    if (n_iters > 0) f->buffers_equal = false;
   }
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(s, &cap);

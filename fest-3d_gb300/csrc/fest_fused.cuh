@@ -20,6 +20,9 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int precision, 
               int first_iter, double CFL, cudaStream_t s, long long* launches);
 // copy the fused path's FP64 state into qp (the reference layout)
 int fused_export_state(FusedState* f, double* qp, cudaStream_t s);
+// the buffer holding the current state (reference layout), nullptr before
+// the first run or after an invalidation; reading it keeps the fused state
+const double* fused_current_state(const FusedState* f);
 // event timing of the stage-sweep launches
 void fused_profile(FusedState* f, bool enable);
 int fused_profile_read(FusedState* f, long long* launches, double* total_ms);
