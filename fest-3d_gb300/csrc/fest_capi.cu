@@ -154,6 +154,7 @@ void fill_params(fest_handle* h) {
     p.fix_tk[i] = b.fixed_tk[i]; p.fix_tw[i] = b.fixed_tw[i];
     p.Tw[i] = b.fixed_wall_temperature[i]; p.Tp[i] = b.fixed_Tpressure[i];
   }
+  params_f32(p);
 }
 
 double* arr_ptr(fest_handle* h, int which) {

@@ -31,7 +31,28 @@ struct Params {
   double c1, c2, c3;
   double fix_rho[6], fix_p[6], fix_u[6], fix_v[6], fix_w[6], fix_tk[6], fix_tw[6];
   double Tw[6], Tp[6];
+  // FP32 copies of the constants the FP32 sweep uses (rounded on the host,
+  // so the device does no FP64 conversions for them)
+  float f_gm, f_gm1, f_R, f_MInf, f_p_inf, f_rho_inf, f_u_inf, f_v_inf, f_w_inf;
+  float f_mu_ref, f_T_ref, f_S, f_Pr, f_tPr, f_c1, f_c2, f_c3;
+  float f_Tw[6], f_Tp[6];
 };
+
+// fill the FP32 copies in a Params from its FP64 fields
+inline void params_f32(Params& p) {
+  p.f_gm = (float)p.gm; p.f_gm1 = (float)(p.gm - 1.0); p.f_R = (float)p.R; p.f_MInf = (float)p.MInf;
+  p.f_p_inf = (float)p.p_inf; p.f_rho_inf = (float)p.rho_inf;
+  p.f_u_inf = (float)p.u_inf; p.f_v_inf = (float)p.v_inf; p.f_w_inf = (float)p.w_inf;
+  p.f_mu_ref = (float)p.mu_ref; p.f_T_ref = (float)p.T_ref; p.f_S = (float)p.S;
+  p.f_Pr = (float)p.Pr; p.f_tPr = (float)p.tPr;
+  p.f_c1 = (float)p.c1; p.f_c2 = (float)p.c2; p.f_c3 = (float)p.c3;
+  for (int f = 0; f < 6; ++f) { p.f_Tw[f] = (float)p.Tw[f]; p.f_Tp[f] = (float)p.Tp[f]; }
+}
+
+// a Params constant in the arithmetic type T: the FP64 field (FP64 and dual
+// numbers), or its FP32 copy
+template <typename T> __host__ __device__ __forceinline__ T pv(double d, float) { return T(d); }
+template <> __host__ __device__ __forceinline__ float pv<float>(double, float f) { return f; }
 
 // ---- index maps (Fortran column-major, lower bounds as in the reference) ----
 __host__ __device__ __forceinline__ long long pidx(const Dims& d, int i, int j, int k) {
@@ -288,7 +309,7 @@ __device__ __forceinline__ void recon_interior(const Params& p, int dir, int c, 
   }
   if ((interp == FEST_INTERP_MUSCL || interp == FEST_INTERP_PPM) && p.pb[dir] == 1) {
     T qc = q(c);
-    T pd = pdif_cell<T>(pres, c, n, T(p.p_inf));
+    T pd = pdif_cell<T>(pres, c, n, pv<T>(p.p_inf, p.f_p_inf));
     if (c <= n - 1) Lp = qc + (pd * (Lp - qc));
     if (c >= 1) Rm = qc - (pd * (qc - Rm));
   }
@@ -477,9 +498,10 @@ __device__ __forceinline__ void face_flux(const Params& p, const T* qL, const T*
                                           T ny, T nz, T mask, T* Fo) {
   const int kind = FLUX >= 0 ? FLUX : p.flux;
   if (kind == FEST_FLUX_AUSM || kind == FEST_FLUX_VAN_LEER || kind == FEST_FLUX_LDFSS0)
-    flux_ausm_family<T>(kind, p.d.nv, T(p.gm), qL, qR, A, nx, ny, nz, mask, Fo);
+    flux_ausm_family<T>(kind, p.d.nv, pv<T>(p.gm, p.f_gm), qL, qR, A, nx, ny, nz, mask, Fo);
   else
-    flux_mass_family<T>(kind, p.d.nv, T(p.gm), T(p.MInf), qL, qR, A, nx, ny, nz, mask, Fo);
+    flux_mass_family<T>(kind, p.d.nv, pv<T>(p.gm, p.f_gm), pv<T>(p.MInf, p.f_MInf), qL, qR, A, nx, ny, nz, mask,
+                        Fo);
 }
 
 // wall mass-flux mask of a face (bc.f90:57-66): 0 at the first/last face of a

@@ -113,14 +113,12 @@ __device__ __forceinline__ void icell(const Dims& d, int f, int m, int ta, int t
   }
 }
 
-// Riemann-invariant ghost state of column (ta, tb) of face f
-// (bc_primitive.f90:1237-1776 for -11, the far-field form for -8); returns
-// the boundary normal velocity Unb
+// Riemann-invariant ghost state of column (ta, tb) of face f from its
+// interior layer 1; returns the boundary normal velocity Unb
 __device__ __forceinline__ float riemann_mirror(const Params& p, const Mirror& M, int f, int ta, int tb,
                                                 const float4* Fd, float& rg, float& ug, float& vg, float& wg,
                                                 float& pg) {
   const Dims& d = p.d;
-  const bool tp = p.id[f] == -11;
   auto I = [&](int m, int l) -> float { int i, j, k; icell(d, f, m, ta, tb, i, j, k); return M.at(i, j, k, l); };
   int fi, fj, fk;
   {
@@ -129,42 +127,8 @@ __device__ __forceinline__ float riemann_mirror(const Params& p, const Mirror& M
     else if (f / 2 == 1) { fi = ta; fj = c; fk = tb; }
     else { fi = ta; fj = tb; fk = c; }
   }
-  const float gm = (float)p.gm;
   const float4 fc = __ldg(Fd + fidx(d, f / 2, fi, fj, fk));
-  const float sg = (f % 2 == 0) ? -1.f : 1.f;
-  const float nx = sg * fc.y, ny = sg * fc.z, nz = sg * fc.w;
-  const float uu = I(1, 1), vv = I(1, 2), ww = I(1, 3), pI = I(1, 4), rI = I(1, 0);
-  const float uinf = (float)p.u_inf, vinf = (float)p.v_inf, winf = (float)p.w_inf;
-  const float pinf = (float)p.p_inf, rinf = (float)p.rho_inf;
-  const float cexp = sqrtf(gm * pI / rI), cinf = sqrtf(gm * pinf / rinf);
-  const float Unexp = uu * nx + vv * ny + ww * nz, Uninf = uinf * nx + vinf * ny + winf * nz;
-  const float Rinf = Uninf - 2.f * cinf / (gm - 1.f), Rexp = Unexp + 2.f * cexp / (gm - 1.f);
-  const float Unb = 0.5f * (Rexp + Rinf), Cb = 0.25f * (gm - 1.f) * (Rexp - Rinf);
-  rg = 0.f;
-  pg = 0.f;
-  if (Unb > 0.f) {
-    const float vd = Unb - Unexp;
-    ug = uu + vd * nx; vg = vv + vd * ny; wg = ww + vd * nz;
-    if (!tp) {
-      const float sv = pI / powf(rI, gm);
-      rg = powf(Cb * Cb / (gm * sv), 1.f / (gm - 1.f));
-      pg = rg * Cb * Cb / gm;
-    }
-  } else {
-    const float vd = Unb - Uninf;
-    ug = uinf + vd * nx; vg = vinf + vd * ny; wg = winf + vd * nz;
-    if (!tp) {
-      const float sv = pinf / powf(rinf, gm);
-      rg = powf(Cb * Cb / (gm * sv), 1.f / (gm - 1.f));
-      pg = rg * Cb * Cb / gm;
-    }
-  }
-  if (tp) {
-    const float Mb = sqrtf(ug * ug + vg * vg + wg * wg) / Cb;
-    pg = (float)p.Tp[f] / powf((1.f + 0.5f * (gm - 1.f) * Mb * Mb), gm / (gm - 1.f));
-    rg = gm * pg / (Cb * Cb);
-  }
-  return Unb;
+  return riemann_ghost_f32(p, f, fc, I(1, 1), I(1, 2), I(1, 3), I(1, 4), I(1, 0), rg, ug, vg, wg, pg);
 }
 
 // dist: the FP64 wall distance (padded), read by the SST wall's omega
@@ -401,6 +365,31 @@ static int order_dirs(const Params& p) {
 static Mirror mirror_of(FusedState* f, int buf) {
   const Dims& d = f->d;
   return Mirror{f->Q32[buf], f->mpitch, d.nj, d.nk, (long long)f->mpitch * d.nj * d.nk};
+}
+
+// Faces whose ghosts the FP32 sweep makes itself after iteration 2 (bit f
+// of the result: ghost layer 1 from the staged interior cells, the only
+// layer an interior update reads for these faces) and k-interfaces served
+// by remapped TMA planes (*kper bit 0: kmin, bit 1: kmax).  The rest (i/j
+// interfaces, order-dependent directions, SST far-field faces) keep the
+// FP32 ghost-fill kernel; -1 faces need nothing after iteration 2.
+static int ring_faces(const Params& p, int* kper) {
+  const int od = order_dirs(p);
+  const bool sst = p.turb != FEST_TURB_NONE;
+  int m = 0;
+  *kper = 0;
+  for (int f = 0; f < 6; ++f) {
+    const int id = p.id[f];
+    if ((od >> (f / 2)) & 1) continue;
+    switch (id) {
+      case -2: case -3: case -4: case -5: case -6: case -7: m |= 1 << f; break;
+      case -8: case -11: if (!sst) m |= 1 << f; break;
+      default:
+        if ((id == -10 || id >= 0) && f / 2 == 2 && p.part_face[4] == 5 && p.part_face[5] == 4)
+          *kper |= 1 << (f - 4);
+    }
+  }
+  return m;
 }
 
 bool fused_supported(const Params& p, int precision) {
@@ -656,6 +645,7 @@ static StageArgs stage_args(FusedState* f, const DevBlock& b, bool mixed, int in
   a.qU = f->Q[f->cur];
   a.bA = bA; a.bB = bB; a.TF = TF; a.SF = SF; a.TU = TU; a.use_rn = use_rn;
   a.Rn = b.Rstore; a.dt = b.dt; a.compute_dt = compute_dt; a.CFL = CFL;
+  a.f_TF = (float)TF; a.f_CFL = (float)CFL; a.blend = bA != 0.0;
   a.res_out = last ? b.res : nullptr;
   for (int dir = 0; dir < 3; ++dir) {
     a.mflux[dir] = last ? b.flux[dir] : nullptr;
@@ -670,6 +660,8 @@ static StageArgs stage_args(FusedState* f, const DevBlock& b, bool mixed, int in
   a.mpitch = f->mpitch;
   a.cells32 = mixed ? f->C32 : nullptr;
   a.dist32 = mixed ? f->D32 : nullptr;
+  a.ring_ghosts = 0;
+  a.kper = 0;
   a.k_chunk = 1;
   return a;
 }
@@ -684,15 +676,19 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
   bb.qp32_pitch = f->mpitch;
   Launcher L{s, cnt};
   const int od = mixed ? order_dirs(p) : 0;
+  int ring = 0, kper = 0;
   if (mixed && iter > 2) {
-    // FP32 ghost fill of the stencil mirror (the FP64 ghosts of Q[in] are
-    // read by nothing on this path after iteration 2); the high faces of
-    // order-dependent directions go second
+    // the sweep makes the ghosts of most faces itself; the FP32 ghost fill
+    // of the stencil mirror covers the rest (the FP64 ghosts of Q[in] are
+    // read by nothing on this path after iteration 2), the high faces of
+    // order-dependent directions second
+    ring = ring_faces(p, &kper);
+    const int skip = ring | (kper << 4);
     Mirror M = mirror_of(f, in);
     for (int pass = 0; pass < (od ? 2 : 1); ++pass) {
       GhostPlan plan{};
       for (int fc = 0; fc < 6; ++fc) {
-        if (p.id[fc] == -1) continue;  // fix() only
+        if (p.id[fc] == -1 || ((skip >> fc) & 1)) continue;  // fix() only, or made by the sweep
         const bool second = (fc % 2 == 1) && ((od >> (fc / 2)) & 1);
         if (second != (pass == 1)) continue;
         const int dir = fc / 2;
@@ -729,6 +725,8 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
     ++*cnt;
   }
   StageArgs a = stage_args(f, b, mixed, in, out, base, bA, bB, TF, SF, TU, use_rn, compute_dt, CFL, last);
+  a.ring_ghosts = ring;
+  a.kper = kper;
   const CUtensorMap& tm = mixed ? f->tm[in] : f->tm_none;
   const int nk = p.d.kmx - 1;
   int& kc = f->kc[mixed ? 1 : 0];
@@ -1020,6 +1018,7 @@ static FusedBatch::Table* batch_table(FusedBatch* B, int stage, const StageSpec&
     e.a = stage_args(f, B->b[n], true, sp.in, sp.out, sp.base, sp.bA, sp.bB, sp.TF, sp.SF, sp.TU,
                      sp.use_rn, sp.cdt, CFL, sp.last);
     e.a.qU = f->Q[cur];
+    e.a.ring_ghosts = ring_faces(p, &e.a.kper);  // batched stages run after iteration 2
     const int kc = chunk_of(p, kcap), nk = p.d.kmx - 1;
     e.a.k_chunk = kc;
     if (tuning) {  // trial launches: private error word, no accumulator, no norms
@@ -1055,8 +1054,10 @@ static FusedBatch::GTable* batch_ghosts(FusedBatch* B, int buf) {
   for (int n = 0; n < B->nb; ++n) {
     FusedState* f = B->f[n];
     const Params& p = B->p[n];
+    int kper = 0;
+    const int skip = ring_faces(p, &kper) | (kper << 4);
     for (int fc = 0; fc < 6; ++fc) {
-      if (p.id[fc] == -1) continue;  // fix() only
+      if (p.id[fc] == -1 || ((skip >> fc) & 1)) continue;  // fix() only, or made by the sweep
       const int dir = fc / 2;
       const int na = (dir == 0 ? p.d.jmx : p.d.imx) - 1, nb = (dir == 2 ? p.d.jmx : p.d.kmx) - 1;
       GhostSeg g;

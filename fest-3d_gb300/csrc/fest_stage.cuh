@@ -57,6 +57,14 @@ struct StageArgs {
   int mpitch;           // row pitch of the state mirror (imx+5 rounded up to 4)
   const float4* cells32;  // {volume, cx, cy, cz} (FP32, padded layout): viscous sweeps
   const float* dist32;    // wall distance (FP32, padded layout): SST sweeps
+  float f_TF, f_CFL;      // FP32 copies of TF and CFL
+  int blend;              // bA != 0
+  // FP32 sweeps after iteration 2: faces (bit f) whose ghost layer 1 the
+  // sweep computes in shared memory from the staged interior cells, and
+  // k-interfaces (bit 0: kmin, bit 1: kmax) whose ghost planes the TMA
+  // fetches from the partner face's interior planes
+  int ring_ghosts;
+  int kper;
 };
 
 // one block of a batched stage launch (device memory, 64-byte aligned for
@@ -232,7 +240,7 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
 #pragma unroll
   for (int l = 0; l < 5; ++l) {
     double v = u2[l];
-    if (a.bA != 0.0) v = a.bA * a.qU[c0 + P * l] + a.bB * v;
+    if (a.blend) v = a.bA * a.qU[c0 + P * l] + a.bB * v;
     a.qout[c0 + P * l] = v;
   }
   return true;
@@ -249,7 +257,7 @@ __device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs
                                                 long long ci, const float* R_in, float dtc, float vol,
                                                 const float* qc, long long m0, float F1) {
   const long long P = p.d.P, N = ncells(p.d);
-  const float gm1 = (float)(p.gm - 1.0);
+  const float gm1 = p.f_gm1;
   float R[NV];
 #pragma unroll
   for (int l = 0; l < NV; ++l) R[l] = R_in[l];
@@ -276,7 +284,7 @@ __device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs
   const bool own = a.qbase == a.qin;
   const float rho = own ? qc[0] : (float)b64[0], u = own ? qc[1] : (float)b64[1],
               v = own ? qc[2] : (float)b64[2], w = own ? qc[3] : (float)b64[3];
-  const float fac = (float)a.TF * dtc / vol;
+  const float fac = a.f_TF * dtc / vol;
   const float dr = R[0] * fac, dmx = R[1] * fac, dmy = R[2] * fac, dmz = R[3] * fac, dE = R[4] * fac;
   const float r2 = rho - dr;
   const float ir2 = 1.0f / r2;
@@ -306,7 +314,7 @@ __device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs
 #pragma unroll
   for (int l = 0; l < NV; ++l) {
     double val = out[l];
-    if (a.bA != 0.0) val = a.bA * a.qU[c0 + P * l] + a.bB * val;
+    if (a.blend) val = a.bA * a.qU[c0 + P * l] + a.bB * val;
     a.qout[c0 + P * l] = val;
     a.qout32[m0 + mvar * l] = (float)val;
   }
@@ -347,9 +355,9 @@ __device__ __forceinline__ float gvar(const ViscCell& c, int l) {
 // dynamic viscosity at a cell: constant mu_ref, or Sutherland's law from the
 // cell temperature (viscosity.f90:109-136)
 __device__ __forceinline__ float visc_mu(const Params& p, float T) {
-  const float mu_ref = (float)p.mu_ref;
+  const float mu_ref = p.f_mu_ref;
   if (p.mu_var != FEST_MU_SUTHERLAND) return mu_ref;
-  const float Tr = (float)p.T_ref, S = (float)p.S;
+  const float Tr = p.f_T_ref, S = p.f_S;
   const float t = dv(T, Tr);
   return mu_ref * (t * sq(t)) * dv(Tr + S, T + S);
 }
@@ -455,9 +463,9 @@ __device__ __forceinline__ void visc_flux(const Params& p, const float* GL, cons
   const float Txx = 2.0f * tm * (G[0][0] - div3), Tyy = 2.0f * tm * (G[1][1] - div3),
               Tzz = 2.0f * tm * (G[2][2] - div3);
   const float Txy = tm * (G[0][1] + G[1][0]), Txz = tm * (G[0][2] + G[2][0]), Tyz = tm * (G[1][2] + G[2][1]);
-  const float gm = (float)p.gm;
-  const float kd = TURB ? dv(mu_f, (float)p.Pr) + dv(mut_f, (float)p.tPr) : dv(tm, (float)p.Pr);
-  const float Kh = kd * gm * (float)p.R * dv(1.0f, gm - 1.0f);
+  const float gm = p.f_gm;
+  const float kd = TURB ? dv(mu_f, p.f_Pr) + dv(mut_f, p.f_tPr) : dv(tm, p.f_Pr);
+  const float Kh = kd * gm * p.f_R * dv(1.0f, gm - 1.0f);
   const float Qx = Kh * G[0][3], Qy = Kh * G[1][3], Qz = Kh * G[2][3];
   const float uf = 0.5f * (L.u + Rc.u), vf = 0.5f * (L.v + Rc.v), wf = 0.5f * (L.w + Rc.w);
   const float A = fc.x, nx = fc.y, ny = fc.z, nz = fc.w;
@@ -573,6 +581,122 @@ __device__ __forceinline__ void sst_ghost(const Params& p, int f, const ViscCell
   }
 }
 
+// ---- ghost layer 1 of a boundary face in FP32 -------------------------------
+// Riemann-invariant ghost state (bc_primitive.f90:1237-1776 for -11, the
+// far-field form for -8) from the interior cell's primitive values; fc: the
+// boundary face record (normals of low faces flipped to point outwards).
+// Returns the boundary normal velocity.  Fast FP32 division, square root
+// and power, as everywhere in the mixed sweep.
+__device__ __forceinline__ float riemann_ghost_f32(const Params& p, int f, float4 fc, float uu, float vv, float ww,
+                                                   float pI, float rI, float& rg, float& ug, float& vg, float& wg,
+                                                   float& pg) {
+  const bool tp = p.id[f] == -11;
+  const float gm = p.f_gm;
+  const float sg = (f % 2 == 0) ? -1.f : 1.f;
+  const float nx = sg * fc.y, ny = sg * fc.z, nz = sg * fc.w;
+  const float uinf = p.f_u_inf, vinf = p.f_v_inf, winf = p.f_w_inf;
+  const float pinf = p.f_p_inf, rinf = p.f_rho_inf;
+  const float cexp = sq(dv(gm * pI, rI)), cinf = sq(dv(gm * pinf, rinf));
+  const float Unexp = uu * nx + vv * ny + ww * nz, Uninf = uinf * nx + vinf * ny + winf * nz;
+  const float Rinf = Uninf - dv(2.f * cinf, gm - 1.f), Rexp = Unexp + dv(2.f * cexp, gm - 1.f);
+  const float Unb = 0.5f * (Rexp + Rinf), Cb = 0.25f * (gm - 1.f) * (Rexp - Rinf);
+  rg = 0.f;
+  pg = 0.f;
+  if (Unb > 0.f) {
+    const float vd = Unb - Unexp;
+    ug = uu + vd * nx; vg = vv + vd * ny; wg = ww + vd * nz;
+    if (!tp) {
+      const float sv = dv(pI, __powf(rI, gm));
+      rg = __powf(dv(Cb * Cb, gm * sv), dv(1.f, gm - 1.f));
+      pg = dv(rg * Cb * Cb, gm);
+    }
+  } else {
+    const float vd = Unb - Uninf;
+    ug = uinf + vd * nx; vg = vinf + vd * ny; wg = winf + vd * nz;
+    if (!tp) {
+      const float sv = dv(pinf, __powf(rinf, gm));
+      rg = __powf(dv(Cb * Cb, gm * sv), dv(1.f, gm - 1.f));
+      pg = dv(rg * Cb * Cb, gm);
+    }
+  }
+  if (tp) {
+    const float Mb = dv(sq(ug * ug + vg * vg + wg * wg), Cb);
+    pg = dv(p.f_Tp[f], __powf((1.f + 0.5f * (gm - 1.f) * Mb * Mb), dv(gm, gm - 1.f)));
+    rg = dv(gm * pg, Cb * Cb);
+  }
+  return Unb;
+}
+
+// Ghost layer 1 of face f at one column from its interior layers 1 and 2:
+// the face procedures of the FP32 ghost fill (bc_primitive.f90:160-206,
+// copy_bc.f90, FT_bc.f90:15-107, bc_primitive.f90:392-402,564-643,
+// 1237-1945) at layer 1, after iteration 2 (no fix() writes).  G, I1, I2
+// address variable 0, variables vs apart.  fn: the face's own record, fr:
+// the I-face record at the same index (flow tangency's normals,
+// FT_bc.f90:67-69), dd1: the interior cell's wall distance (SST walls).
+// Faces -8/-11 with SST (k, omega follow the face's last column) are not
+// handled here.
+template <int NV>
+__device__ __forceinline__ void ghost_layer1(const Params& p, int f, float* G, const float* I1, const float* I2,
+                                             int vs, float4 fn, float4 fr, float dd1) {
+  const float c1 = p.f_c1, c2 = p.f_c2, c3 = p.f_c3;
+  const float gm = p.f_gm, R = p.f_R;
+  auto symm = [&](int l) { G[l * vs] = dv(c2 * I1[l * vs] - c3 * I2[l * vs], c1); };
+  switch (p.id[f]) {
+    case -2:
+    case -7:
+#pragma unroll
+      for (int l = 0; l < NV; ++l) G[l * vs] = I1[l * vs];
+      break;
+    case -3: G[4 * vs] = I1[4 * vs]; break;
+    case -4:
+#pragma unroll
+      for (int l = 0; l < 4; ++l) G[l * vs] = I1[l * vs];
+      if constexpr (NV == 7) { G[5 * vs] = I1[5 * vs]; G[6 * vs] = I1[6 * vs]; }
+      break;
+    case -5: {
+      symm(4);
+      const float Tw = p.f_Tw[f];
+      if (Tw < 0.f) {
+        const float pp = I1[4 * vs], rho = I1[0];
+        const float stag = dv(pp, R * rho) * (1.f + dv(0.5f * (gm - 1.f) * gm * pp, rho));
+        G[0] = dv(G[4 * vs], R * stag);
+      } else if (Tw > 1.f) {
+        const float Ti = dv(I1[4 * vs], R * I1[0]);
+        G[0] = dv(G[4 * vs], R * (2.f * Tw - Ti));
+      } else {
+        symm(0);
+      }
+      G[vs] = -I1[vs]; G[2 * vs] = -I1[2 * vs]; G[3 * vs] = -I1[3 * vs];
+      if constexpr (NV == 7) {
+        G[5 * vs] = -I1[5 * vs];
+        const float Tf = 0.5f * ((G[4 * vs] / G[0]) + (I1[4 * vs] / I1[0])) / R;
+        const float Tr = p.f_T_ref, S = p.f_S;
+        const float mu = p.f_mu_ref * powf(Tf / Tr, 1.5f) * ((Tr + S) / (Tf + S));
+        const float rho = 0.5f * (G[0] + I1[0]);
+        const float dd = 2.f * dd1;
+        G[6 * vs] = 120.f * mu / (rho * 0.075f * (dd * dd)) - I1[6 * vs];
+      }
+    } break;
+    case -6: {
+      symm(0); symm(4);
+      if constexpr (NV == 7) { symm(5); symm(6); }
+      const float uu = I1[vs], vv = I1[2 * vs], ww = I1[3 * vs];
+      const float dot = uu * fn.y + vv * fn.z + ww * fn.w;
+      G[vs] = uu - (2.f * dot * fr.y);
+      G[2 * vs] = vv - (2.f * dot * fr.z);
+      G[3 * vs] = ww - (2.f * dot * fr.w);
+    } break;
+    case -8:
+    case -11: {
+      float rg, ug, vg, wg, pg;
+      riemann_ghost_f32(p, f, fn, I1[vs], I1[2 * vs], I1[3 * vs], I1[4 * vs], I1[0], rg, ug, vg, wg, pg);
+      G[0] = rg; G[vs] = ug; G[2 * vs] = vg; G[3 * vs] = wg; G[4 * vs] = pg;
+    } break;
+    default: break;  // -1: fix() only
+  }
+}
+
 // The sweep of one CTA: tile (bx, by) of the block, k-chunk bz.  The
 // single-block kernel passes its block indices; the batched kernel maps its
 // CTA to a block of the batch and a tile of that block.
@@ -612,7 +736,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
   const bool in_i = lane >= 1 && lane <= IX && i <= d.imx - 1;
   const bool in_j = w >= 1 && w <= IY && j <= d.jmx - 1;
   const int plane = NV * SH * RW;
-  const T gm = (T)p.gm;
+  const T gm = pv<T>(p.gm, p.f_gm);
   // FP32: the TMA box starts ox columns left of the tile's stencil origin
   const int ox = kTma ? ((IX * bx) & 3) : 0;
   const bool thin = d.kmx == 2;
@@ -655,9 +779,78 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
   // the array are zero-filled and feed only discarded halo lanes
   constexpr uint32_t kPlaneBytes = (uint32_t)(NV * SH * RW * sizeof(T));
   auto issue = [&](int c) {
-    fence_proxy_async();  // earlier generic reads of the slot come first
-    tma_load_4d(ring + slot(c) * plane, tmp, IX * bx - ox, IY * by, c + 2, 0,
+    fence_proxy_async();  // earlier generic accesses of the slot come first
+    // k-interfaces: ghost plane 1-L <- partner plane kmx-L, kmx+L-1 <- L
+    int src = c;
+    if ((a.kper & 1) && c <= 0) src = c + d.kmx - 1;
+    else if ((a.kper & 2) && c >= d.kmx) src = c - d.kmx + 1;
+    tma_load_4d(ring + slot(c) * plane, tmp, IX * bx - ox, IY * by, src + 2, 0,
                 bars + slot(c), kPlaneBytes);
+  };
+  // in-ring ghost layer 1 of the faces in a.ring_ghosts (FP32 sweep): ring
+  // column of array index i = i - (ib-3) + ox, ring row of j = j - (jb-3)
+  const int rgm = kTma ? a.ring_ghosts : 0;
+  const int col_ilo = 3 - ib + ox, col_ihi = d.imx - ib + 3 + ox;
+  const int row_jlo = 3 - jb, row_jhi = d.jmx - jb + 3;
+  const bool g_ilo = (rgm & 1) && col_ilo >= 0, g_ihi = (rgm & 2) && col_ihi < RW;
+  const bool g_jlo = (rgm & 4) && row_jlo >= 0, g_jhi = (rgm & 8) && row_jhi < SH;
+  const bool g_ij = g_ilo || g_ihi || g_jlo || g_jhi;
+  // In-ring i/j ghost tasks, done by the halo warps 0 and TY-1 (idle while
+  // the interior warps do the k faces): q = 0..RW-1 the j-face ghost of
+  // ring column q (the low face; the high one too, second, in a block of
+  // at most IY interior rows), q = RW..RW+2*SH-1 the i-face ghost of a ring
+  // row (low face, then high).  Per task: ring offset, face record (own
+  // face, I-face) and wall-distance indices at k = 0 (32-bit: the fused
+  // path takes blocks with P*n_var < 2^31).
+  const int VS = SH * RW;  // variable stride in a ring plane
+  const int gq = w == 0 ? lane : (w == TY - 1 ? TX + lane : -1);
+  auto ghost_task = [&](int q, bool second, int& face, int& off, int& fn, int& fr, int& dd) -> bool {
+    if (q < RW) {
+      const bool hi = second || !g_jlo;
+      const int ii = q + ib - 3 - ox;
+      if (!(hi ? g_jhi : g_jlo) || ii < 1 || ii > d.imx - 1) return false;
+      face = 2 + hi;
+      off = (hi ? row_jhi : row_jlo) * RW + q;
+      fn = (int)fidx(d, 1, ii, hi ? d.jmx : 1, 0);
+      fr = (int)fidx(d, 0, ii, hi ? d.jmx : 1, 0);
+      dd = (int)pidx(d, ii, hi ? d.jmx - 1 : 1, 0);
+      return true;
+    }
+    const int r2 = q - RW, hi = r2 >= SH, r = r2 - hi * SH, jj = jb - 3 + r;
+    if (r2 >= 2 * SH || !(hi ? g_ihi : g_ilo) || jj < 1 || jj > d.jmx - 1) return false;
+    face = hi;
+    off = r * RW + (hi ? col_ihi : col_ilo);
+    fn = fr = (int)fidx(d, 0, hi ? d.imx : 1, jj, 0);
+    dd = (int)pidx(d, hi ? d.imx - 1 : 1, jj, 0);
+    return true;
+  };
+  int gt_face = -1, gt_off = 0, gt_fn = 0, gt_fr = 0, gt_dd = 0;
+  bool gt_second = false;
+  if (g_ij && gq >= 0) {
+    if (!ghost_task(gq, false, gt_face, gt_off, gt_fn, gt_fr, gt_dd)) gt_face = -1;
+    gt_second = gq < RW && g_jlo && g_jhi;
+  }
+  // k strides of the I-face, J-face and cell arrays
+  const int sI = d.nj * (d.ni + 1), sJ = (d.nj + 1) * d.ni, sC = d.ni * d.nj;
+  // apply this thread's tasks to plane kp (fn0/fr0/dd0: the first task's
+  // records on that plane)
+  auto ij_ghosts = [&](int kp, float4 fn0, float4 fr0, float dd0) {
+    float* P = reinterpret_cast<float*>(ring) + slot(kp) * plane;
+    auto apply = [&](int face, int off, float4 fn, float4 fr, float dd) {
+      float* G = P + off;
+      const int st = face == 0 ? 1 : (face == 1 ? -1 : (face == 2 ? RW : -RW));  // inwards
+      ghost_layer1<NV>(p, face, G, G + st, G + 2 * st, VS, fn, fr, dd);
+    };
+    if (gt_face >= 0) apply(gt_face, gt_off, fn0, fr0, dd0);
+    if (gt_second) {
+      int face, off, fn, fr, dd;
+      if (ghost_task(gq, true, face, off, fn, fr, dd)) {
+        const float4 fnv = __ldg(a.faces32[1] + (fn + sJ * kp)), frv = __ldg(a.faces32[0] + (fr + sI * kp));
+        float ddv = 0.f;
+        if constexpr (TURB) ddv = __ldg(a.dist32 + (dd + sC * kp));
+        apply(face, off, fnv, frv, ddv);
+      }
+    }
   };
   if constexpr (kTma) {
     if (tid == 0) {
@@ -683,13 +876,21 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
   // SST march state: mu_t, F1 and source of cell (i, j, k-1), turbulent dt terms
   float mut_prev = 0, F1_prev = 0, Sk_prev = 0, Sw_prev = 0;
   float ltk_prev = 0, lti_lo_prev = 0, lti_hi_prev = 0, ltj_lo_prev = 0, ltj_hi_prev = 0;
-  const float Rg = (float)p.R;
-  const int VS = SH * RW;  // variable stride in a ring plane
+  const float Rg = p.f_R;
 
   const long long sj = d.ni, sk = (long long)d.ni * d.nj;
   for (int n = 0; n < nplanes; ++n) {
     const int kl = base + n;  // plane arriving now
     __syncthreads();
+    // ghost tasks on plane kl (FP32): face records fetched while it is in flight
+    const bool gij_now = (gt_face >= 0 || gt_second) && kl >= 1 && kl <= d.kmx - 1;
+    float4 g_fn = make_float4(0.f, 0.f, 0.f, 0.f), g_fr = g_fn;
+    float g_dd = 0.f;
+    if (gt_face >= 0 && gij_now) {
+      g_fn = __ldg(a.faces32[gt_face / 2] + (gt_fn + (gt_face < 2 ? sI : sJ) * kl));
+      g_fr = gt_face < 2 ? g_fn : __ldg(a.faces32[0] + (gt_fr + sI * kl));
+      if constexpr (TURB) g_dd = __ldg(a.dist32 + (gt_dd + sC * kl));
+    }
     if constexpr (kTma) {
       if (abort_flag) return;  // uniform: read after the barrier
       // the slot of plane n+1 last held plane n+1-NR, read up to iteration n-1
@@ -698,12 +899,50 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         raise_error(a.err, FEST_ERR_TIMEOUT);
         abort_flag = 1;
       }
+      if (rgm) {
+        float* ringf = reinterpret_cast<float*>(ring);
+        // k ghost planes: read in this very step, so computed by all
+        // threads and published by a barrier (uniform over the CTA)
+        const bool fix_klo = (rgm & 16) && kl == 2 && base <= 0;  // plane 0 from planes 1, 2
+        const bool fix_khi = (rgm & 32) && kl == d.kmx;           // plane kmx from kmx-1, kmx-2
+        if (fix_klo || fix_khi) {
+          auto fix_kplane = [&](int f, int kg, int ka, int kb) {
+            float* G0 = ringf + slot(kg) * plane;
+            const float* A1 = ringf + slot(ka) * plane;
+            const float* A2 = ringf + slot(kb) * plane;
+            const int fk = f == 4 ? 1 : d.kmx;
+            for (int e = tid; e < SH * RW; e += TX * TY) {
+              const int r = e / RW, c = e - r * RW;
+              const int ii = c + ib - 3 - ox, jj = jb - 3 + r;
+              if (ii < 1 || ii > d.imx - 1 || jj < 1 || jj > d.jmx - 1) continue;
+              const float4 fn = __ldg(a.faces32[2] + fidx(d, 2, ii, jj, fk));
+              const float4 fr = __ldg(a.faces32[0] + fidx(d, 0, ii, jj, fk));
+              float dd1 = 0.f;
+              if constexpr (TURB) dd1 = __ldg(a.dist32 + pidx(d, ii, jj, ka));
+              ghost_layer1<NV>(p, f, G0 + e, A1 + e, A2 + e, VS, fn, fr, dd1);
+            }
+          };
+          if (fix_klo) fix_kplane(4, 0, 1, 2);
+          if (fix_khi) {
+            if (fix_klo) __syncthreads();  // a single interior plane: kmin's ghosts first
+            fix_kplane(5, d.kmx, d.kmx - 1, d.kmx - 2);
+          }
+          __syncthreads();
+        }
+      }
     } else {
       load_plane(kl);
       __syncthreads();
     }
     const int k = kl - 2;  // plane processed now
-    if (k < k0 - 1) continue;
+    // i/j ghost cells of plane kl are first read two steps later, as the
+    // own plane's i/j stencils (this step reads plane kl at interior
+    // columns only): the halo warps make them at the end of the step, or
+    // now when the step has nothing else to do
+    if (k < k0 - 1) {
+      if (gij_now) ij_ghosts(kl, g_fn, g_fr, g_dd);
+      continue;
+    }
     const bool kin = k >= k0 && k <= k1;
     T dF[NV], dG[NV];
 #pragma unroll
@@ -979,18 +1218,18 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
           T dtc;
           if (a.compute_dt) {
             T s = lami_lo_prev + lamj_lo_prev + lamk_prev + lami_hi_prev + lamj_hi_prev + lamk;
-            dtc = (T(1) / s) * vol_c * (T)a.CFL;
+            dtc = (T(1) / s) * vol_c * pv<T>(a.CFL, a.f_CFL);
             if constexpr (VISC) {  // add_viscous_time (time.f90:366-448)
               float sv = lvi_lo_prev + lvj_lo_prev + lvk_prev + lvi_hi_prev + lvj_hi_prev + lvk;
-              sv = (float)p.gm * sv / (float)p.Pr;
-              sv = 2.0f / (sv + (2.0f * (float)a.CFL * vol_c / dtc));
-              dtc = (float)a.CFL * (sv * vol_c);
+              sv = p.f_gm * sv / p.f_Pr;
+              sv = 2.0f / (sv + (2.0f * a.f_CFL * vol_c / dtc));
+              dtc = a.f_CFL * (sv * vol_c);
             }
             if constexpr (TURB) {  // add_turbulent_time (time.f90:450-531)
               float st = lti_lo_prev + ltj_lo_prev + ltk_prev + lti_hi_prev + ltj_hi_prev + ltk;
-              st = (float)p.gm * st / (float)p.tPr;
-              st = 2.0f / (st + (2.0f * (float)a.CFL * vol_c / dtc));
-              dtc = (float)a.CFL * (st * vol_c);
+              st = p.f_gm * st / p.f_tPr;
+              st = 2.0f / (st + (2.0f * a.f_CFL * vol_c / dtc));
+              dtc = a.f_CFL * (st * vol_c);
             }
             a.dt[ci] = (double)dtc;
           } else {
@@ -1043,6 +1282,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         }
       }
     }
+    if (gij_now) ij_ghosts(kl, g_fn, g_fr, g_dd);  // halo warps, published by the next barrier
   }
 }
 
