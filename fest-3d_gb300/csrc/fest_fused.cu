@@ -645,7 +645,7 @@ static StageArgs stage_args(FusedState* f, const DevBlock& b, bool mixed, int in
   a.qU = f->Q[f->cur];
   a.bA = bA; a.bB = bB; a.TF = TF; a.SF = SF; a.TU = TU; a.use_rn = use_rn;
   a.Rn = b.Rstore; a.dt = b.dt; a.compute_dt = compute_dt; a.CFL = CFL;
-  a.f_TF = (float)TF; a.f_CFL = (float)CFL; a.blend = bA != 0.0;
+  a.f_TF = (float)TF; a.f_CFL = (float)CFL; a.f_bB = (float)bB; a.blend = bA != 0.0;
   a.res_out = last ? b.res : nullptr;
   for (int dir = 0; dir < 3; ++dir) {
     a.mflux[dir] = last ? b.flux[dir] : nullptr;

@@ -57,7 +57,7 @@ struct StageArgs {
   int mpitch;           // row pitch of the state mirror (imx+5 rounded up to 4)
   const float4* cells32;  // {volume, cx, cy, cz} (FP32, padded layout): viscous sweeps
   const float* dist32;    // wall distance (FP32, padded layout): SST sweeps
-  float f_TF, f_CFL;      // FP32 copies of TF and CFL
+  float f_TF, f_CFL, f_bB;  // FP32 copies of TF, CFL and bB
   int blend;              // bA != 0
   // FP32 sweeps after iteration 2: faces (bit f) whose ghost layer 1 the
   // sweep computes in shared memory from the staged interior cells, and
@@ -203,6 +203,39 @@ __device__ __forceinline__ T lambda_face(T gm, const T* L, const T* R, T A, T nx
   return A * (fabs((u * nx) + (v * ny) + (w * nz)) + c);
 }
 
+// ---- FP32 <-> FP64 conversions in integer arithmetic -------------------------
+// GB300 converts between FP32 and FP64 in its FP64 unit, which runs at a
+// small fraction of the FP32 rate; the mixed sweep's conversions are done
+// with integer operations instead.  f2d is exact for normal numbers, zero,
+// infinities and NaN (FP32 subnormals, below 1.2e-38, become zero); d2f
+// rounds to nearest even like a conversion instruction for results in the
+// normal FP32 range (results below it become signed zero).
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu, s = u & 0x80000000u, m = u & 0x7fffffu;
+  unsigned hi = s, lo = 0u;
+  if (e == 0xffu) { hi = s | 0x7ff00000u | (m >> 3); lo = m << 29; }
+  else if (e != 0u) { hi = s | ((e + 896u) << 20) | (m >> 3); lo = m << 29; }
+  return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned s = hi & 0x80000000u, ed = (hi >> 20) & 0x7ffu;
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rest = lo & 0x1fffffffu;  // the 29 bits dropped
+  if (ed == 0x7ffu) return __uint_as_float(s | 0x7f800000u | (mant != 0u || rest != 0u ? 0x400000u : 0u));
+  const int e = (int)ed - 896;  // FP32 biased exponent
+  if (e <= 0) return __uint_as_float(s);
+  if (e >= 255) return __uint_as_float(s | 0x7f800000u);
+  unsigned bits = s | ((unsigned)e << 23) | mant;
+  bits += (rest > 0x10000000u || (rest == 0x10000000u && (mant & 1u))) ? 1u : 0u;  // may carry into inf
+  return __uint_as_float(bits);
+}
+__device__ __forceinline__ double to_f64(float x) { return f2d(x); }
+__device__ __forceinline__ double to_f64(double x) { return x; }
+__device__ __forceinline__ float from_f64(double x, float) { return d2f(x); }
+__device__ __forceinline__ double from_f64(double x, double) { return x; }
+
 // ---- the update of one cell -------------------------------------------------
 // FP64: update_with(...,'conservative',...) (update.f90:367-485) verbatim.
 __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
@@ -270,9 +303,9 @@ __device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs
   if (a.use_rn) {
 #pragma unroll
     for (int l = 0; l < NV; ++l) {
-      double rn = a.Rn[ci + N * l] + a.SF * (double)R[l];
+      double rn = fma(a.SF, f2d(R[l]), a.Rn[ci + N * l]);
       a.Rn[ci + N * l] = rn;
-      if (a.TU) R[l] = (float)rn;
+      if (a.TU) R[l] = d2f(rn);
     }
   }
   double b64[NV];
@@ -282,8 +315,8 @@ __device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs
   // FP32 copies of the base state: the stencil's own cell when the update
   // starts from the stencil state (bit-identical to converting b64)
   const bool own = a.qbase == a.qin;
-  const float rho = own ? qc[0] : (float)b64[0], u = own ? qc[1] : (float)b64[1],
-              v = own ? qc[2] : (float)b64[2], w = own ? qc[3] : (float)b64[3];
+  const float rho = own ? qc[0] : d2f(b64[0]), u = own ? qc[1] : d2f(b64[1]),
+              v = own ? qc[2] : d2f(b64[2]), w = own ? qc[3] : d2f(b64[3]);
   const float fac = a.f_TF * dtc / vol;
   const float dr = R[0] * fac, dmx = R[1] * fac, dmy = R[2] * fac, dmz = R[3] * fac, dE = R[4] * fac;
   const float r2 = rho - dr;
@@ -294,29 +327,39 @@ __device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs
                           0.5f * rho * (2.0f * (u * du + v * dv + w * dw) + du * du + dv * dv + dw * dw));
   // negative or NaN density/pressure after the update (update.f90:448),
   // judged in FP32 (a NaN anywhere in the increments reaches rn or pn)
-  const float p0 = own ? qc[4] : (float)b64[4];
+  const float p0 = own ? qc[4] : d2f(b64[4]);
   const float rn = rho - dr, pn = p0 + dp;
   if (!(rn >= 0.0f) || !(pn >= 0.0f) || du != du || dv != dv || dw != dw) return false;
-  double out[NV];
-  out[0] = b64[0] - (double)dr;
-  out[1] = b64[1] + (double)du;
-  out[2] = b64[2] + (double)dv;
-  out[3] = b64[3] + (double)dw;
-  out[4] = b64[4] + (double)dp;
+  // new state = base + increment; the TVD blends bA*U + bB*(base + inc)
+  // as two FMAs, fma(bB, base, fma(bA, U, bB*inc))
+  float inc[NV];
+  inc[0] = -dr; inc[1] = du; inc[2] = dv; inc[3] = dw; inc[4] = dp;
+  bool keep[NV];
+#pragma unroll
+  for (int l = 0; l < NV; ++l) keep[l] = false;
   if constexpr (NV == 7) {
-    const float tk = own ? qc[5] : (float)b64[5], tw = own ? qc[6] : (float)b64[6];
+    const float tk = own ? qc[5] : d2f(b64[5]), tw = own ? qc[6] : d2f(b64[6]);
     const float dk = (tk * dr - R[5] * fac) * ir2, dom = (tw * dr - R[6] * fac) * ir2;
     if (dk != dk || dom != dom) return false;
-    const double k2 = b64[5] + (double)dk, w2o = b64[6] + (double)dom;
-    out[5] = k2 >= 0.0 ? k2 : a.qin[c0 + P * 5];
-    out[6] = w2o >= 0.0 ? w2o : a.qin[c0 + P * 6];
+    inc[5] = dk;
+    inc[6] = dom;
+    keep[5] = b64[5] + f2d(dk) < 0.0;
+    keep[6] = b64[6] + f2d(dom) < 0.0;
   }
+  const float bBf = a.f_bB;
 #pragma unroll
   for (int l = 0; l < NV; ++l) {
-    double val = out[l];
-    if (a.blend) val = a.bA * a.qU[c0 + P * l] + a.bB * val;
+    double val;
+    if (keep[l]) {
+      val = a.qin[c0 + P * l];  // k, omega that would turn negative keep the stage input
+      if (a.blend) val = fma(a.bA, a.qU[c0 + P * l], a.bB * val);
+    } else if (a.blend) {
+      val = fma(a.bB, b64[l], fma(a.bA, a.qU[c0 + P * l], f2d(bBf * inc[l])));
+    } else {
+      val = b64[l] + f2d(inc[l]);
+    }
     a.qout[c0 + P * l] = val;
-    a.qout32[m0 + mvar * l] = (float)val;
+    a.qout32[m0 + mvar * l] = d2f(val);
   }
   return true;
 }
@@ -1231,13 +1274,13 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
               st = 2.0f / (st + (2.0f * a.f_CFL * vol_c / dtc));
               dtc = a.f_CFL * (st * vol_c);
             }
-            a.dt[ci] = (double)dtc;
+            a.dt[ci] = to_f64(dtc);
           } else {
-            dtc = (T)a.dt[ci];
+            dtc = from_f64(a.dt[ci], T(0));
           }
           if (a.res_out)
 #pragma unroll
-            for (int l = 0; l < NV; ++l) a.res_out[ci + ncells(d) * l] = (double)R[l];
+            for (int l = 0; l < NV; ++l) a.res_out[ci + ncells(d) * l] = to_f64(R[l]);
           // the finished cell's own stencil values (plane k-1 of the ring)
           T qo[NV];
           const T* own1 = ring + slot(kc) * plane + r * RW + cc;
