@@ -164,6 +164,224 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
     }
 }
 
+// ---- laminar viscous terms (gradients.f90, viscosity.f90, viscous.f90) -----
+// The viscous flux of a face (viscous.f90:144-325, laminar: mu_t = 0) as a
+// function of its 21 inputs x: the mean of the two cells' gradients
+// x[4c+l] (component c, variable l of u, v, w, T), the left and right cells'
+// u, v, w, T (x[12..15], x[16..19]) and the face viscosity x[20]; the
+// geometry enters as constants.  Returns the four terms the reference
+// subtracts from F(2:5).
+template <typename D>
+__device__ __forceinline__ void visc_flux_d(const Params& p, const D* x, const double* C0, const double* C1,
+                                            const double* fc, D* Fv) {
+  D G[3][4];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int l = 0; l < 4; ++l) G[c][l] = x[4 * c + l];
+  const double dx0 = C1[1] - C0[1], dy0 = C1[2] - C0[2], dz0 = C1[3] - C0[3];
+  const D delx(dx0), dely(dy0), delz(dz0), dLR(::sqrt(dx0 * dx0 + dy0 * dy0 + dz0 * dz0));
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const D del = x[16 + l] - x[12 + l];
+    const D nc = (del - (G[0][l] * delx + G[1][l] * dely + G[2][l] * delz)) / dLR;
+    G[0][l] = G[0][l] + (nc * delx / dLR);
+    G[1][l] = G[1][l] + (nc * dely / dLR);
+    G[2][l] = G[2][l] + (nc * delz / dLR);
+  }
+  const D two(2.), three(3.), half(0.5);
+  const D tm = x[20];
+  const D dudx = G[0][0], dudy = G[1][0], dudz = G[2][0];
+  const D dvdx = G[0][1], dvdy = G[1][1], dvdz = G[2][1];
+  const D dwdx = G[0][2], dwdy = G[1][2], dwdz = G[2][2];
+  const D Txx = two * tm * (dudx - ((dudx + dvdy + dwdz) / three));
+  const D Tyy = two * tm * (dvdy - ((dudx + dvdy + dwdz) / three));
+  const D Tzz = two * tm * (dwdz - ((dudx + dvdy + dwdz) / three));
+  const D Txy = tm * (dvdx + dudy), Txz = tm * (dwdx + dudz), Tyz = tm * (dwdy + dvdz);
+  const D Kh = (tm / D(p.Pr)) * D(p.gm) * D(p.R) / D(p.gm - 1);
+  const D Qx = Kh * G[0][3], Qy = Kh * G[1][3], Qz = Kh * G[2][3];
+  const D A(fc[0]), nx(fc[1]), ny(fc[2]), nz(fc[3]);
+  const D uf = half * (x[12] + x[16]), vf = half * (x[13] + x[17]), wf = half * (x[14] + x[18]);
+  Fv[0] = (Txx * nx + Txy * ny + Txz * nz) * A;
+  Fv[1] = (Txy * nx + Tyy * ny + Tyz * nz) * A;
+  Fv[2] = (Txz * nx + Tyz * ny + Tzz * nz) * A;
+  Fv[3] = A * (((Txx * uf + Txy * vf + Txz * wf + Qx) * nx) + ((Txy * uf + Tyy * vf + Tyz * wf + Qy) * ny) +
+               ((Txz * uf + Tyz * vf + Tzz * wf + Qz) * nz));
+}
+
+// d mu / d T of calculate_viscosity (viscosity.f90:109-136; constant mu: 0)
+__device__ __forceinline__ double dmu_dT(const Params& p, double T) {
+  if (p.mu_var != FEST_MU_SUTHERLAND) return 0.0;
+  const double mu = p.mu_ref * (::pow(T / p.T_ref, 1.5)) * ((p.T_ref + p.S) / (T + p.S));
+  return mu * (1.5 / T - 1.0 / (T + p.S));
+}
+
+// adjoints of a cell's u, v, w, T into its primitive state (T = p/(rho R),
+// the temperature of update.f90:170 at this state)
+__device__ __forceinline__ void give_uvwT(const Params& p, const DevBlock& b, double* bar, long long c,
+                                          const double* g) {
+  const long long P = p.d.P;
+  const double rho = b.qp[c], pr = b.qp[c + 4 * P];
+  if (g[0] != 0.0) atomicAdd(bar + c + P, g[0]);
+  if (g[1] != 0.0) atomicAdd(bar + c + 2 * P, g[1]);
+  if (g[2] != 0.0) atomicAdd(bar + c + 3 * P, g[2]);
+  if (g[3] != 0.0) {
+    atomicAdd(bar + c + 4 * P, g[3] / (rho * p.R));
+    atomicAdd(bar + c, -g[3] * pr / (rho * rho * p.R));
+  }
+}
+
+// one thread per face of direction dir: the transposed viscous flux onto
+// mu = lambda(left) - lambda(right) (the flux enters the residual with a
+// minus sign).  Gradient adjoints go to barG (interior cells, 12 per cell
+// as [component][variable]); a ghost cell's gradient is its face's
+// gradient BC (gradients.f90:486-676) of the interior cell, transposed here.
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_viscous(Params p, DevBlock b, const double* lam, double* bar,
+                                                         double* barG, int dir) {
+  using D = Dual<double, 21>;
+  const Dims& d = p.d;
+  const int n = extent_of(d, dir);
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * na * nb) return;
+  const int c = 1 + (int)(t % n);
+  const long long r = t / n;
+  const int ta = 1 + (int)(r % na), tb = 1 + (int)(r / na);
+  const long long P = d.P, N = ncells(d), NG = ngrad(d);
+  double mu[4] = {0, 0, 0, 0};
+  int i, j, k;
+  if (c - 1 >= 1) {
+    cell_of(dir, c - 1, ta, tb, i, j, k);
+    for (int l = 0; l < 4; ++l) mu[l] += lam[cidx(d, i, j, k) + N * (l + 1)];
+  }
+  if (c <= n - 1) {
+    cell_of(dir, c, ta, tb, i, j, k);
+    for (int l = 0; l < 4; ++l) mu[l] -= lam[cidx(d, i, j, k) + N * (l + 1)];
+  }
+  if (mu[0] == 0.0 && mu[1] == 0.0 && mu[2] == 0.0 && mu[3] == 0.0) return;
+  int il, jl, kl, ir, jr, kr;
+  cell_of(dir, c - 1, ta, tb, il, jl, kl);
+  cell_of(dir, c, ta, tb, ir, jr, kr);
+  const long long cL = pidx(d, il, jl, kl), cR = pidx(d, ir, jr, kr);
+  const long long gL = gidx(d, il, jl, kl), gR = gidx(d, ir, jr, kr);
+  D x[21], Fv[4];
+#pragma unroll
+  for (int cc = 0; cc < 3; ++cc)
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+      x[4 * cc + l] = D::var(0.5 * (b.grad[cc][gL + NG * l] + b.grad[cc][gR + NG * l]), 4 * cc + l);
+  const double TL = b.qp[cL + 4 * P] / (b.qp[cL] * p.R), TR = b.qp[cR + 4 * P] / (b.qp[cR] * p.R);
+  for (int l = 0; l < 3; ++l) {
+    x[12 + l] = D::var(b.qp[cL + P * (l + 1)], 12 + l);
+    x[16 + l] = D::var(b.qp[cR + P * (l + 1)], 16 + l);
+  }
+  x[15] = D::var(TL, 15);
+  x[19] = D::var(TR, 19);
+  x[20] = D::var(0.5 * (b.mu[cL] + b.mu[cR]), 20);
+  const long long fi = fidx(d, dir, ir, jr, kr);
+  visc_flux_d<D>(p, x, b.cells + 4 * cL, b.cells + 4 * cR, b.faces[dir] + 4 * fi, Fv);
+  double bx[21];
+#pragma unroll
+  for (int m = 0; m < 21; ++m) {
+    double s = 0.0;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) s -= mu[l] * Fv[l].d[m];
+    bx[m] = s;
+  }
+  // cell values and the face viscosity
+  double gLv[4] = {bx[12], bx[13], bx[14], bx[15]}, gRv[4] = {bx[16], bx[17], bx[18], bx[19]};
+  gLv[3] += 0.5 * bx[20] * dmu_dT(p, TL);
+  gRv[3] += 0.5 * bx[20] * dmu_dT(p, TR);
+  // gradients: half of the mean to each side; ghost sides through the BC
+  double gG[2][12];
+#pragma unroll
+  for (int m = 0; m < 12; ++m) gG[0][m] = gG[1][m] = 0.5 * bx[m];
+  for (int side = 0; side < 2; ++side) {
+    const bool ghost = side == 0 ? (c == 1 && p.id[2 * dir] < 0) : (c == n && p.id[2 * dir + 1] < 0);
+    double* gv = side == 0 ? gLv : gRv;
+    if (!ghost) {
+      const int ci = side == 0 ? (int)cidx(d, il, jl, kl) : (int)cidx(d, ir, jr, kr);
+      for (int m = 0; m < 12; ++m)
+        if (gG[side][m] != 0.0) atomicAdd(barG + (long long)ci * 12 + m, gG[side][m]);
+      continue;
+    }
+    // G_ghost = jump(cI - cG) + tangential(G_I) (adiabatic walls: -G_I for T)
+    const int f = 2 * dir + side;  // the low face has the ghost on the left
+    const double* fc = b.faces[dir] + 4 * fi;
+    const double nx = fc[1], ny = fc[2], nz = fc[3];
+    const long long cI = side == 0 ? cR : cL;
+    const double vI = b.cells[4 * cI];
+    const double cc3[3] = {fc[0] * nx / vI, fc[0] * ny / vI, fc[0] * nz / vI};
+    const double nn[3] = {nx, ny, nz};
+    const double sig = side ? -1.0 : 1.0;
+    const bool adiab = p.id[f] == -5 && (p.Tw[f] < 1. && p.Tw[f] >= 0.);
+    double gI[12], jI[4], jG[4];
+    for (int l = 0; l < 4; ++l) {
+      double dot = 0.0;
+      for (int q = 0; q < 3; ++q) dot += gG[side][4 * q + l] * nn[q];
+      for (int q = 0; q < 3; ++q) gI[4 * q + l] = gG[side][4 * q + l] - nn[q] * dot;
+      double s = 0.0;
+      for (int q = 0; q < 3; ++q) s += gG[side][4 * q + l] * cc3[q];
+      jI[l] = sig * s;
+      jG[l] = -sig * s;
+    }
+    if (adiab) {
+      for (int q = 0; q < 3; ++q) gI[4 * q + 3] -= gG[side][4 * q + 3];
+      jI[3] = 0.0;
+      jG[3] = 0.0;
+    }
+    const int ci = side == 0 ? (int)cidx(d, ir, jr, kr) : (int)cidx(d, il, jl, kl);
+    for (int m = 0; m < 12; ++m)
+      if (gI[m] != 0.0) atomicAdd(barG + (long long)ci * 12 + m, gI[m]);
+    double* gInt = side == 0 ? gRv : gLv;  // the interior cell's u, v, w, T
+    for (int l = 0; l < 4; ++l) {
+      gInt[l] += jI[l];
+      gv[l] += jG[l];
+    }
+  }
+  give_uvwT(p, b, bar, cL, gLv);
+  give_uvwT(p, b, bar, cR, gRv);
+}
+
+// one thread per interior cell: its gradient adjoint through the
+// Green-Gauss sum (gradients.f90:405-482) onto u, v, w, T of the cell and
+// its six neighbours
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_grad(Params p, DevBlock b, const double* barG, double* bar) {
+  const Dims& d = p.d;
+  const long long N = ncells(d);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= N) return;
+  const int i = 1 + (int)(t % (d.imx - 1));
+  const long long r = t / (d.imx - 1);
+  const int j = 1 + (int)(r % (d.jmx - 1)), k = 1 + (int)(r / (d.jmx - 1));
+  const double* g = barG + t * 12;  // [component][variable]
+  bool any = false;
+  for (int m = 0; m < 12; ++m) any |= g[m] != 0.0;
+  if (!any) return;
+  const int ncomp = d.kmx > 2 ? 3 : 2;
+  const long long c0 = pidx(d, i, j, k);
+  const double vol2 = 2 * b.cells[4 * c0];
+  // faces i, j, k (low, sign -1) and i+1, j+1, k+1 (high, +1) with their neighbours
+  const double* fr[6] = {b.faces[0] + 4 * fidx(d, 0, i, j, k), b.faces[1] + 4 * fidx(d, 1, i, j, k),
+                         b.faces[2] + 4 * fidx(d, 2, i, j, k), b.faces[0] + 4 * fidx(d, 0, i + 1, j, k),
+                         b.faces[1] + 4 * fidx(d, 1, i, j + 1, k), b.faces[2] + 4 * fidx(d, 2, i, j, k + 1)};
+  const long long nbc[6] = {pidx(d, i - 1, j, k), pidx(d, i, j - 1, k), pidx(d, i, j, k - 1),
+                            pidx(d, i + 1, j, k), pidx(d, i, j + 1, k), pidx(d, i, j, k + 1)};
+  double own[4] = {0, 0, 0, 0};
+  for (int f = 0; f < 6; ++f) {
+    const double sg = f < 3 ? -1.0 : 1.0;
+    double gn[4];
+    for (int l = 0; l < 4; ++l) {
+      double s = 0.0;
+      for (int q = 0; q < ncomp; ++q) s += g[4 * q + l] * fr[f][1 + q];
+      gn[l] = sg * s * fr[f][0] / vol2;
+      own[l] += gn[l];
+    }
+    give_uvwT(p, b, bar, nbc[f], gn);
+  }
+  give_uvwT(p, b, bar, c0, own);
+}
+
 // ghost (layer L) / interior (layer m) cell of face f at (ta, tb)
 __device__ __forceinline__ long long gcell_p(const Dims& d, int f, int L, int ta, int tb) {
   switch (f) {
@@ -366,13 +584,14 @@ __global__ void k_adj_psi(Dims d, const double* mu, double* psi) {  // psi = -mu
 }  // namespace
 
 bool vjp_supported(const Params& p) {
-  if (p.mu_ref != 0.0 || p.turb != FEST_TURB_NONE || p.d.nv != 5) return false;
+  if (p.turb != FEST_TURB_NONE || p.d.nv != 5) return false;
   if (p.pb[0] || p.pb[1] || p.pb[2]) return false;  // pressure switch couples variables
   if (ghosts_need_sequential(p) || p.d.kmx == 2) return false;
   for (int f = 0; f < 6; ++f) {
     const int id = p.id[f];
     if (id == -9) return false;
     if (id == -5 && (p.Tw[f] < 0.0 || p.Tw[f] > 1.0)) return false;
+    if (p.mu_ref != 0.0 && id >= 0) return false;  // a raw ghost gradient would reach past the ghosts
   }
   return true;
 }
@@ -383,7 +602,7 @@ static void apply_ST(const Params& p, const DevBlock& b, const double* v, double
                      const Launcher& L) {
   const long long N = ncells(p.d);
   k_adj_precond<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p, b, v, w.mu);
-  launch_residual_vjp(p, b, 3, w.mu, w.bar, L);
+  launch_residual_vjp(p, b, 3, w.mu, w.bar, L, nullptr, w.grad);
   k_adj_combine<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p.d, out, 1.0, v, -1.0, w.bar, 0.0, nullptr, 0.0,
                                                  nullptr, nullptr);
   *L.count += 2;
@@ -429,14 +648,24 @@ void launch_adjoint_psi(const Params& p, const DevBlock& b, AdjointWork& w, doub
 }
 
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
-                         double* bar, const Launcher& L, double* const* bar_faces) {
+                         double* bar, const Launcher& L, double* const* bar_faces, double* bar_grad) {
   const Dims& d = p.d;
+  const bool visc = p.mu_ref != 0.0;
   cudaMemsetAsync(bar, 0, sizeof(double) * (size_t)d.P * d.nv, L.s);
+  if (visc) cudaMemsetAsync(bar_grad, 0, sizeof(double) * 12 * (size_t)ncells(d), L.s);
   for (int dir = 0; dir < 3; ++dir) {
     const int n = extent_of(d, dir);
     const long long nf = (long long)n * ((dir == 0 ? d.jmx : d.imx) - 1) * ((dir == 2 ? d.jmx : d.kmx) - 1);
     k_vjp_faces<double><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar,
                                                           bar_faces ? bar_faces[dir] : nullptr, dir);
+    ++*L.count;
+    if (visc) {
+      k_vjp_viscous<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bar_grad, dir);
+      ++*L.count;
+    }
+  }
+  if (visc) {
+    k_vjp_grad<<<nblocks(ncells(d)), TPB_ADJ, 0, L.s>>>(p, b, bar_grad, bar);
     ++*L.count;
   }
   long long wmax = 0;

@@ -32,6 +32,7 @@ struct fest_handle {
   FusedState* fused = nullptr;
   double* d_vjp_bar = nullptr;  // adjoint work arrays, allocated on first use
   double* d_vjp_lam = nullptr;
+  double* d_vjp_grad = nullptr;  // laminar adjoint: 12 per interior cell
   int* h_err = nullptr;          // pinned host copy of the device error word
   std::vector<void*> allocs;
   Launcher L() { return Launcher{s, &launches}; }
@@ -665,6 +666,17 @@ int fest_get_total_conservative_residue(fest_handle* h, double* qp, int current_
   return finish(h);
 }
 
+// laminar blocks: the primal's temperature, gradients (with their BCs) and
+// viscosity at the resident state, which the residual's VJP reads
+static int viscous_prep(fest_handle* h) {
+  if (h->p.mu_ref == 0.0) return FEST_OK;
+  if (!h->d_vjp_grad) RET(dalloc(h, &h->d_vjp_grad, 12 * ncells(h->p.d)));
+  launch_temperature(h->p, h->d, h->L());
+  launch_gradients(h->p, h->d, h->L());
+  launch_viscosity(h->p, h->d, h->L());
+  return FEST_OK;
+}
+
 int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const double* lambda,
                       double* dq) {
   if (!h || !lambda || !dq) return FEST_ERR_ARG;
@@ -676,7 +688,8 @@ int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const 
   if (qp) RET(up(h, h->d.qp, qp, z.qp));
   RET(up(h, h->d_vjp_lam, lambda, z.res));
   launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
-  launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L());
+  RET(viscous_prep(h));
+  launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), nullptr, h->d_vjp_grad);
   RET(down(h, dq, h->d_vjp_bar, z.qp));
   return finish(h);
 }
@@ -685,7 +698,8 @@ int fest_residual_vjp_nodes(fest_handle* h, const double* qp, int current_iter, 
                             const double* Ifaces_bar, const double* Jfaces_bar,
                             const double* Kfaces_bar, double* dq, double* dnodes) {
   if (!h || !dnodes) return FEST_ERR_ARG;
-  if (!vjp_supported(h->p) || h->p.interp == FEST_INTERP_WENO_NM) return FEST_ERR_ARG;
+  // metric adjoints of the inviscid residual only
+  if (!vjp_supported(h->p) || h->p.interp == FEST_INTERP_WENO_NM || h->p.mu_ref != 0.0) return FEST_ERR_ARG;
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
@@ -726,6 +740,9 @@ int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_i
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
   if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
+  // the handle keeps this one: allocated before the solve's own work arrays,
+  // which release() frees
+  if (h->p.mu_ref != 0.0 && !h->d_vjp_grad) RET(dalloc(h, &h->d_vjp_grad, 12 * ncells(h->p.d)));
   AdjointWork w{};
   w.bar = h->d_vjp_bar;
   w.mu = h->d_vjp_lam;
@@ -742,8 +759,11 @@ int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_i
     }
   };
   if (!rc) rc = up(h, w.dJ, dJdq, z.qp);
-  // the frozen primal: ghost cells, face states and the local time step
+  // the frozen primal: ghost cells, face states, (laminar) temperature,
+  // gradients and viscosity, and the local time step
   if (!rc) rc = residual_fp64(h, 3);
+  if (!rc) rc = viscous_prep(h);
+  w.grad = h->d_vjp_grad;
   if (!rc) launch_time_step(h->p, h->d, CFL, h->L());
   Launcher L = h->L();
   double first = -1.0, last = 0.0;

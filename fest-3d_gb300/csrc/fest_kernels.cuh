@@ -65,13 +65,17 @@ void launch_resnorm(const Params& p, const DevBlock& b, double* d_out, const Lau
 void launch_geometry(const Params& p, const DevBlock& b, const Launcher& L);
 void launch_wall_dist(const Params& p, const DevBlock& b, const double* d_wall, int n_wall,
                       double* d_node_dist, const Launcher& L);
-// adjoint of the inviscid residual: bar (padded qp layout) = (dR/dq)^T lam
-// (residue layout), ghost cells filled for iteration iter beforehand
+// adjoint of the residual (inviscid or laminar): bar (padded qp layout) =
+// (dR/dq)^T lam (residue layout), ghost cells filled for iteration iter
+// beforehand and, for laminar blocks, the temperature, gradients and
+// viscosity of the state computed (launch_viscous_prep)
 bool vjp_supported(const Params& p);
 // bar_faces (null, or three face-layout arrays, zeroed by the caller) also
-// receive (dR/dfaces)^T lam
+// receive (dR/dfaces)^T lam (inviscid blocks); bar_grad: 12 doubles per
+// interior cell of work space for laminar blocks
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
-                         double* bar, const Launcher& L, double* const* bar_faces = nullptr);
+                         double* bar, const Launcher& L, double* const* bar_faces = nullptr,
+                         double* bar_grad = nullptr);
 // nodes-layout bar_nodes = (dfaces/dnodes)^T bar_faces, through the face
 // vectors and the ghost-node extrapolation (interior nodes carry the result)
 void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_faces, double* bar_nodes,
@@ -80,6 +84,7 @@ void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_
 // layout, mu in the residue layout, sq one double
 struct AdjointWork {
   double *phi, *dJ, *a, *b, *c, *bar, *mu, *sq;
+  double* grad;  // 12 per interior cell (laminar blocks)
 };
 // one step phi <- G^T phi + dJ/dq (G the integrator's map linearised at the
 // fixed point: forward Euler or TVD-RK3); sq += |change of phi|^2

@@ -17,36 +17,45 @@ from . import abi, cases
 from .handle import Handle
 
 
-def bump_flow(mach, angle_deg=0.0, p0=101325.0, rho0=1.2, gm=1.4):
+def bump_flow(mach, angle_deg=0.0, p0=101325.0, rho0=1.2, gm=1.4, mu_ref=0.0):
+    """Free stream of the bump channel; mu_ref > 0: laminar, constant
+    viscosity."""
     c = np.sqrt(gm * p0 / rho0)
     a = np.deg2rad(angle_deg)
     return abi.make_flow(density_inf=rho0, x_speed_inf=mach * c * np.cos(a),
-                         y_speed_inf=mach * c * np.sin(a), pressure_inf=p0, mu_ref=0.0)
+                         y_speed_inf=mach * c * np.sin(a), pressure_inf=p0, mu_ref=mu_ref,
+                         mu_variation="constant")
 
 
-def bump_bc(mach, p0=101325.0, gm=1.4):
+def bump_bc(mach, p0=101325.0, gm=1.4, wall=-6):
+    """Total-pressure inlet, pressure outlet, lower and upper walls of type
+    wall (-6 slip, -5 no-slip adiabatic), periodic k faces."""
     pt = p0 * (1 + 0.5 * (gm - 1) * mach * mach) ** (gm / (gm - 1))
     fixed = {k: [0.0] * 6 for k in ("fixed_pressure", "fixed_Tpressure")}
     fixed["fixed_pressure"][1] = p0
     fixed["fixed_Tpressure"][0] = pt
-    return abi.make_bc([-11, -4, -6, -6, -10, -10], partners={4: (0, 5), 5: (0, 4)}, **fixed)
+    return abi.make_bc([-11, -4, wall, wall, -10, -10], partners={4: (0, 5), 5: (0, 4)}, **fixed)
 
 
-def adjoint_case(nc=(128, 48, 4), mach=0.5, angle_deg=0.0, interpolant="muscl"):
+def adjoint_case(nc=(128, 48, 4), mach=0.5, angle_deg=0.0, interpolant="muscl", mu_ref=0.0,
+                 integrator="TVDRK3", CFL=0.8):
     """The bump at 128x48x4 cells, Euler, unlimited MUSCL (kappa 1/3) + SLAU,
     TVD-RK3 with local time steps at CFL 0.8 (the smooth subsonic flow needs
     no limiter, which keeps the residual differentiable; forward Euler is
     unstable with unlimited MUSCL).  interpolant="none" gives the
     first-order scheme, whose explicit iteration converges to round-off
     within a few 10^4 iterations (the second-order one drops by only ~20
-    in 4*10^4 on this grid, identically in the oracle)."""
+    in 4*10^4 on this grid, identically in the oracle).  mu_ref > 0: laminar
+    with no-slip adiabatic walls."""
     ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 5)
-    scheme = abi.make_scheme(scheme_name="slau", interpolant=interpolant, time_step_accuracy="TVDRK3",
+    scheme = abi.make_scheme(scheme_name="slau", interpolant=interpolant, time_step_accuracy=integrator,
                              time_stepping_method="l", ilimiter_switch=0, jlimiter_switch=0,
                              klimiter_switch=0)
-    flow = bump_flow(mach, angle_deg)
-    return dict(ext=ext, flow=flow, scheme=scheme, bc=bump_bc(mach), nodes=cases.bump_nodes(ext),
-                qp=cases.uniform_state(ext, flow), CFL=0.8, mach=mach, angle=angle_deg)
+    flow = bump_flow(mach, angle_deg, mu_ref=mu_ref)
+    wall = -5 if mu_ref > 0 else -6
+    return dict(ext=ext, flow=flow, scheme=scheme, bc=bump_bc(mach, wall=wall), nodes=cases.bump_nodes(ext),
+                qp=cases.uniform_state(ext, flow), CFL=CFL, mach=mach, angle=angle_deg, mu_ref=mu_ref,
+                wall=wall)
 
 
 def make_handle(case, flow=None, bc=None, lib=None):
@@ -97,7 +106,8 @@ def residual_param_derivative(case, q, it, param, h_rel=1e-6, lib=None):
     for a in (a0 + step, a0 - step):
         mach = a if param == "mach" else case["mach"]
         ang = a if param == "angle" else case["angle"]
-        hp = make_handle(case, flow=bump_flow(mach, ang), bc=bump_bc(mach), lib=lib)
+        hp = make_handle(case, flow=bump_flow(mach, ang, mu_ref=case.get("mu_ref", 0.0)),
+                         bc=bump_bc(mach, wall=case.get("wall", -6)), lib=lib)
         _, r = hp.residual(q, it)
         out.append(r)
         hp.close()

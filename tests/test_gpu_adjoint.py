@@ -1,5 +1,5 @@
-"""fest_residual_vjp: the transposed-Jacobian product of the inviscid
-residual, checked against central finite differences of the oracle's FP64
+"""fest_residual_vjp: the transposed-Jacobian product of the inviscid and
+laminar residual, checked against central finite differences of the oracle's FP64
 residual (get_total_conservative_Residue, update.f90:495-547, at iteration 3
 so that no fix() BC writes), and wrapped in a torch.autograd.Function for
 torch.autograd.gradcheck.
@@ -87,14 +87,78 @@ def test_vjp_matches_oracle_finite_differences(gpu_lib, name):
     assert usable >= 3, f"{name}: only {usable} kink-free directions"
 
 
-def test_vjp_rejects_viscous_blocks(gpu_lib):
+# laminar blocks: the viscous face terms (viscous.f90:144-325) through the
+# Green-Gauss gradients and their BCs (gradients.f90:276-676) and the
+# viscosity (viscosity.f90:109-136), with the temperature p/(rho R) of the
+# state; viscosities large enough that the viscous terms are a sizeable
+# part of the residual
+VISC_CASES = {
+    "lam-muscl-ausm-walls": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ausm"),
+                                 ids=(-3, -4, -5, -6, -10, -10),
+                                 flow_kw=dict(mu_ref=1.0, mu_variation="constant")),
+    "suth-weno-slau-riemann": dict(scheme_kw=dict(interpolant="weno", scheme_name="slau"),
+                                   ids=(-11, -4, -5, -5, -10, -10),
+                                   flow_kw=dict(mu_ref=0.5, mu_variation="sutherland_law")),
+    "suth-none-vanleer-farfield": dict(scheme_kw=dict(interpolant="none", scheme_name="van_leer"),
+                                       ids=(-8, -2, -6, -5, -6, -6),
+                                       flow_kw=dict(mu_ref=0.5, mu_variation="sutherland_law")),
+}
+
+
+@pytest.mark.parametrize("name", list(VISC_CASES))
+def test_viscous_vjp_matches_oracle_finite_differences(gpu_lib, name):
+    ext, flow, scheme, bc, nodes, qp = small_case(nc=(10, 8, 6), **VISC_CASES[name])
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
+    rng = np.random.default_rng(13)
+    lam = np.asfortranarray(rng.standard_normal((ext.imx - 1, ext.jmx - 1, ext.kmx - 1, ext.n_var)))
+    dq = h.residual_vjp(qp, IT, lam)
+    mask = interior_mask(ext)
+    assert np.all(dq * (1 - mask) == 0), "ghost entries of dq must be zero"
+    scale = var_scale(qp, ext)
+
+    def phi(q):
+        # ghosts of this state first, then its temperature, then the residual
+        blk["qp"] = np.asfortranarray(q)
+        assert O.get_total_conservative_residue([blk], IT) == 0
+        blk.compute_temperature()
+        assert O.get_total_conservative_residue([blk], IT) == 0
+        return float(np.sum(lam * blk["residue"]))
+
+    def fd(v, e):
+        return (8 * (phi(qp + e * v) - phi(qp - e * v)) - (phi(qp + 2 * e * v) - phi(qp - 2 * e * v))) / (12 * e)
+
+    inner = np.argwhere(mask[..., 0] > 0)
+    usable = 0
+    for trial in range(6):
+        v = np.zeros(qp.shape)
+        for i, j, k in inner[rng.choice(len(inner), 24, replace=False)]:
+            v[i, j, k] = rng.standard_normal(ext.n_var) * scale
+        f1, f2 = fd(v, 1e-6), fd(v, 2e-7)
+        if abs(f1 - f2) > 1e-6 * max(abs(f1), abs(f2)):
+            continue  # a limiter kink inside the step
+        ad = float(np.sum(dq * v))
+        assert abs(f1 - ad) <= 1e-5 * max(abs(f1), abs(ad)), (name, trial, f1, f2, ad)
+        usable += 1
+    assert usable >= 3, f"{name}: only {usable} kink-free directions"
+
+
+def test_vjp_rejects_unsupported_blocks(gpu_lib):
+    """SST blocks have no residual VJP; laminar blocks no metric VJP."""
+    ext, flow, scheme, bc, nodes, qp = small_case(
+        nc=(12, 9, 7), ids=(-3, -4, -5, -6, -10, -10), turb=True,
+        flow_kw=dict(mu_ref=1e-2, mu_variation="constant"))
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
+    lam = np.zeros((ext.imx - 1, ext.jmx - 1, ext.kmx - 1, ext.n_var), order="F")
+    with pytest.raises(abi.FestError) as e:
+        h.residual_vjp(qp, IT, lam)
+    assert e.value.code == abi.FEST_ERR_ARG
     ext, flow, scheme, bc, nodes, qp = small_case(
         nc=(12, 9, 7), ids=(-3, -4, -5, -6, -10, -10),
         flow_kw=dict(mu_ref=1e-2, mu_variation="constant"))
     blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
     lam = np.zeros((ext.imx - 1, ext.jmx - 1, ext.kmx - 1, ext.n_var), order="F")
     with pytest.raises(abi.FestError) as e:
-        h.residual_vjp(qp, IT, lam)
+        h.residual_vjp_nodes(qp, IT, lam)
     assert e.value.code == abi.FEST_ERR_ARG
 
 

@@ -56,3 +56,25 @@ def test_bump_wall_force_sensitivities(gpu_lib):
         fd = (vals[0] - vals[1]) / (2 * step)
         g = grads[f"wall_node_{i}"]
         assert abs(fd - g) <= 1e-4 * max(abs(fd), 1e-3 * abs(J)), (i, fd, g)
+
+
+def test_laminar_adjoint_solve_satisfies_the_adjoint_equation(gpu_lib):
+    """fest_adjoint_solve on a laminar bump (no-slip adiabatic walls,
+    Reynolds number ~ 2000 on the channel height, first-order SLAU, forward
+    Euler) after 3000 primal iterations: the fixed point psi satisfies
+    (dR/dq)^T psi = -dJ/dq, checked with fest_residual_vjp on every
+    interior cell (the iteration needs a contractive linearised step, not a
+    converged primal)."""
+    case = A.adjoint_case(nc=(48, 16, 4), interpolant="none", mu_ref=0.1, integrator="none", CFL=0.5)
+    h = A.make_handle(case, lib=gpu_lib)
+    h.upload_state(case["qp"])
+    h.step(3000, 1, case["CFL"], with_norm=False)
+    q = h.download_state()
+    ext = case["ext"]
+    J, dJ = A.wall_force(q, ext, h.get("Jfaces"))
+    psi, n, drop = h.adjoint_solve(dJ, case["CFL"], max_iters=100000, tol=1e-10)
+    assert drop <= 1e-10, (n, drop)
+    back = h.residual_vjp(q, 3, psi)
+    sl = (slice(3, ext.imx + 2), slice(3, ext.jmx + 2), slice(3, ext.kmx + 2))
+    err = np.abs(back[sl] + dJ[sl]).max() / np.abs(dJ[sl]).max()
+    assert err <= 1e-6, (err, n)
