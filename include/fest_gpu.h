@@ -268,9 +268,11 @@ int fest_batch_step_async(fest_batch *b, int n_iters, int first_iter, double CFL
  * state (ghost cells follow it through the BCs of the iteration), lambda in
  * the residue layout, dq in the qp layout (ghost entries zero).  qp
  * (nullable: the device state) is uploaded and its ghosts filled first.
- * FP64.  Inviscid blocks of the fused-path kind (n_var 5, >= 4 interior
- * cells per direction, no -9 face, no pressure switch, adiabatic -5 walls);
- * FEST_ERR_ARG otherwise. */
+ * FP64.  Inviscid and laminar blocks of the fused-path kind (n_var 5,
+ * >= 4 interior cells per direction, no -9 face, no pressure switch,
+ * adiabatic -5 walls; laminar: no interface ids >= 0), the laminar terms
+ * with the temperature p/(rho R) of the state; FEST_ERR_ARG otherwise
+ * (SST blocks). */
 int fest_residual_vjp(fest_handle *h, const double *qp, int current_iter,
                       const double *lambda, double *dq);
 /* No counterpart in the reference.  The same product with respect to the
@@ -281,7 +283,8 @@ int fest_residual_vjp(fest_handle *h, const double *qp, int current_iter,
  * nodes carry the result, ghost nodes zero); lambda and the three
  * face-layout adjoints *_bar (an objective's explicit metric dependence)
  * are nullable; dq (nullable) receives fest_residual_vjp's result.  Same
- * restrictions as fest_residual_vjp, and no WENO_NM (volume weights). */
+ * restrictions as fest_residual_vjp, inviscid blocks only, and no WENO_NM
+ * (volume weights). */
 int fest_residual_vjp_nodes(fest_handle *h, const double *qp, int current_iter,
                             const double *lambda, const double *Ifaces_bar,
                             const double *Jfaces_bar, const double *Kfaces_bar,
