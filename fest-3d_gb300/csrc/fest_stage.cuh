@@ -1040,7 +1040,9 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       const T* rowp = ring + slot(k) * plane + r * RW;
       const auto vol = vol_line(a, T(0), pidx(d, 0, clampi(j, d.jmx), k), 1, d.imx);
       SmemLine<T> pres{rowp + 4 * SH * RW + cc, i, 1};
-#pragma unroll
+      // not unrolled: the sweep's code outgrows the instruction cache
+      // (stalls on instruction fetch were the largest before this)
+#pragma unroll 1
       for (int l = 0; l < NV; ++l) {
         SmemLine<T> q{rowp + l * SH * RW + cc, i, 1};
         recon_cell<T, INTERP>(p, 0, i, l + 1, q, pres, vol, Rm[l], Lp[l]);
@@ -1104,7 +1106,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       const T* colp = ring + slot(k) * plane + cc;
       const auto vol = vol_line(a, T(0), pidx(d, clampi(i, d.imx), 0, k), sj, d.jmx);
       SmemLine<T> pres{colp + 4 * SH * RW + r * RW, j, RW};
-#pragma unroll
+#pragma unroll 1
       for (int l = 0; l < NV; ++l) {
         SmemLine<T> q{colp + l * SH * RW + r * RW, j, RW};
         recon_cell<T, INTERP>(p, 1, j, l + 1, q, pres, vol, Rm[l], Lp[l]);
