@@ -36,12 +36,11 @@ __global__ void k_ghost_blend(Dims d, double* q, float* q32, int pitch, const do
 // FP32 mirrors for the mixed sweep: state (whole padded array), face
 // records {A,nx,ny,nz} and cell volumes.  Rounding to nearest, as a
 // conversion on load would do.
-// one row (j, k, variable) of the padded array per blockIdx.y
+// one row (j, k, variable) of the padded array per block (rows in the x
+// dimension of the grid, which has no 65535 limit)
 __global__ void k_to_mirror(Dims d, int pitch, const double* src, float* dst) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ni) return;
-  const long long row = blockIdx.y;  // (j + 2) + nj*((k + 2) + nk*l)
-  dst[row * pitch + i] = (float)src[row * d.ni + i];
+  const long long row = blockIdx.x;  // (j + 2) + nj*((k + 2) + nk*l)
+  for (int i = threadIdx.x; i < d.ni; i += blockDim.x) dst[row * pitch + i] = (float)src[row * d.ni + i];
 }
 __global__ void k_faces_to_f32(const double* faces, float4* dst, long long n) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
@@ -540,7 +539,7 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
     // read (results discarded) hold finite values
     // (pitch padding columns are outside the tensor map: never read); equal
     // FP64 buffers share one conversion
-    const dim3 g((d.ni + 127) / 128, (unsigned)((long long)d.nj * d.nk * d.nv));
+    const unsigned g = (unsigned)((long long)d.nj * d.nk * d.nv);
     for (int m = 0; m < 3; ++m) {
       if (m > 0 && f->buffers_equal) {
         cudaMemcpyAsync(f->Q32[m], f->Q32[0], sizeof(float) * (size_t)f->m_elems, cudaMemcpyDeviceToDevice, s);

@@ -219,3 +219,19 @@ def test_profile_counts_stage_launches(gpu_lib):
     ms = C.c_double()
     abi.check(L.fest_profile_read(h.h, C.byref(n), C.byref(ms)), "profile_read")
     assert n.value == 12 and ms.value > 0
+
+
+def test_mixed_block_with_many_rows(gpu_lib):
+    """a block whose padded rows (j, k, variable) outnumber 65535: the FP32
+    mirror's conversion covers every row"""
+    ext, flow, scheme, bc, nodes, qp = small_case(
+        nc=(16, 200, 64), ids=(-3, -4, -6, -6, -10, -10),
+        scheme_kw=dict(interpolant="muscl", scheme_name="ausm", time_step_accuracy="TVDRK3"))
+    assert (ext.jmx + 5) * (ext.kmx + 5) * ext.n_var > 65535
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
+    h.set_precision(abi.FEST_MIXED)
+    h.step(3, 1, 0.5, with_norm=False)
+    for it in (1, 2, 3):
+        assert O.get_next_solution([blk], it, 0.5) == 0
+    e = rel_err(interior(h.download_state(), ext), interior(blk["qp"], ext))
+    assert e <= 2e-5, f"mixed interior state differs by {e:.3e}"
