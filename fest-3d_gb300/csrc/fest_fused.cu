@@ -1082,6 +1082,15 @@ static FusedBatch::GTable* batch_ghosts(FusedBatch* B, int buf) {
 }
 
 static int launch_batch(const FusedBatch* B, int ctas, const BatchEntry* e, cudaStream_t s) {
+  if (B->p[0].turb != FEST_TURB_NONE) {
+    switch (B->interp) {
+      case FEST_INTERP_NONE: return launch_batch_none_sst(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+      case FEST_INTERP_MUSCL: return launch_batch_muscl_sst(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+      case FEST_INTERP_PPM: return launch_batch_ppm_sst(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+      case FEST_INTERP_WENO: return launch_batch_weno_sst(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+      default: return launch_batch_weno_nm_sst(FEST_MIXED, B->flux, ctas, s, e, B->nb);
+    }
+  }
   if (B->p[0].mu_ref != 0.0) {
     switch (B->interp) {
       case FEST_INTERP_NONE: return launch_batch_none_visc(FEST_MIXED, B->flux, ctas, s, e, B->nb);
@@ -1166,11 +1175,11 @@ int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Para
   *out = nullptr;
   if (f.empty() || f.size() != p.size() || f.size() != b.size()) return FEST_ERR_ARG;
   for (size_t n = 0; n < f.size(); ++n) {
-    // the batched sweep covers Euler and laminar blocks (SST blocks step alone)
-    if (!f[n] || !fused_supported(p[n], FEST_MIXED) || p[n].turb != FEST_TURB_NONE || order_dirs(p[n]))
-      return FEST_ERR_ARG;
+    // one sweep kernel for all: the same reconstruction, flux scheme,
+    // integrator and physics (Euler, laminar, or SST)
+    if (!f[n] || !fused_supported(p[n], FEST_MIXED) || order_dirs(p[n])) return FEST_ERR_ARG;
     if (p[n].interp != p[0].interp || p[n].flux != p[0].flux || p[n].integ != p[0].integ ||
-        (p[n].mu_ref != 0.0) != (p[0].mu_ref != 0.0))
+        (p[n].mu_ref != 0.0) != (p[0].mu_ref != 0.0) || (p[n].turb != FEST_TURB_NONE) != (p[0].turb != FEST_TURB_NONE))
       return FEST_ERR_ARG;
   }
   FusedBatch* B = new FusedBatch();

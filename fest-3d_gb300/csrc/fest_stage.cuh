@@ -1342,8 +1342,8 @@ __global__ void __launch_bounds__(TX* TY, MB)
 
 // One launch for every block of a batch: block b owns CTAs
 // [cta0, cta0 + tx*ty*nz) of the 1-D grid.
-template <typename T, int INTERP, int FLUX, bool VISC = false>
-__global__ void __launch_bounds__(TX* TY, VISC ? 2 : (sizeof(T) == 4 ? 3 : 1))
+template <typename T, int INTERP, int FLUX, bool VISC = false, bool TURB = false>
+__global__ void __launch_bounds__(TX* TY, TURB ? 1 : (VISC ? 2 : (sizeof(T) == 4 ? 3 : 1)))
     k_stage_batch(const BatchEntry* e, int nb) {
   __shared__ Params sp;
   __shared__ StageArgs sa;
@@ -1370,7 +1370,8 @@ __global__ void __launch_bounds__(TX* TY, VISC ? 2 : (sizeof(T) == 4 ? 3 : 1))
   }
   __syncthreads();
   const int local = (int)blockIdx.x - E.cta0;
-  stage_body<T, INTERP, FLUX, VISC>(sp, sa, &E.tm, local % E.tx, (local / E.tx) % E.ty, local / (E.tx * E.ty));
+  stage_body<T, INTERP, FLUX, VISC, TURB>(sp, sa, &E.tm, local % E.tx, (local / E.tx) % E.ty,
+                                         local / (E.tx * E.ty));
 }
 
 template <typename T, bool VISC = false, bool TURB = false> inline size_t stage_smem() {
@@ -1411,6 +1412,11 @@ FEST_BATCH_LAUNCHER(launch_batch_muscl);
 FEST_BATCH_LAUNCHER(launch_batch_ppm);
 FEST_BATCH_LAUNCHER(launch_batch_weno);
 FEST_BATCH_LAUNCHER(launch_batch_weno_nm);
+FEST_BATCH_LAUNCHER(launch_batch_none_sst);
+FEST_BATCH_LAUNCHER(launch_batch_muscl_sst);
+FEST_BATCH_LAUNCHER(launch_batch_ppm_sst);
+FEST_BATCH_LAUNCHER(launch_batch_weno_sst);
+FEST_BATCH_LAUNCHER(launch_batch_weno_nm_sst);
 FEST_BATCH_LAUNCHER(launch_batch_none_visc);
 FEST_BATCH_LAUNCHER(launch_batch_muscl_visc);
 FEST_BATCH_LAUNCHER(launch_batch_ppm_visc);
@@ -1506,6 +1512,34 @@ int launch_stage_sst_t(int flux, dim3 grid, cudaStream_t s, const Params& p, con
   }
 #undef FEST_SET
 #define FEST_GO(F) k_stage<float, INTERP, F, 1, true, true><<<grid, blk, smem, s>>>(p, a, tm)
+  switch (flux) {
+    case 0: FEST_GO(0); break;
+    case 1: FEST_GO(1); break;
+    case 2: FEST_GO(2); break;
+    case 3: FEST_GO(3); break;
+    case 4: FEST_GO(4); break;
+    case 5: FEST_GO(5); break;
+    default: return FEST_ERR_ARG;
+  }
+#undef FEST_GO
+  return FEST_OK;
+}
+
+template <int INTERP>
+int launch_batch_sst_t(int flux, int ctas, cudaStream_t s, const BatchEntry* e, int nb) {
+  using namespace stage;
+  const dim3 blk(TX, TY);
+  static bool attrs = false;
+  const size_t smem = stage_smem<float, true, true>();
+#define FEST_SET(F)                                                                                          \
+  cudaFuncSetAttribute(k_stage_batch<float, INTERP, F, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)smem)
+  if (!attrs) {
+    FEST_SET(0); FEST_SET(1); FEST_SET(2); FEST_SET(3); FEST_SET(4); FEST_SET(5);
+    attrs = true;
+  }
+#undef FEST_SET
+#define FEST_GO(F) k_stage_batch<float, INTERP, F, true, true><<<ctas, blk, smem, s>>>(e, nb)
   switch (flux) {
     case 0: FEST_GO(0); break;
     case 1: FEST_GO(1); break;

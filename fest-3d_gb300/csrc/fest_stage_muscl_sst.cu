@@ -1,5 +1,5 @@
 // fest_stage_muscl_sst.cu - k-omega SST FP32 stage sweeps with the muscl
-// reconstruction (all six flux schemes, single block); see fest_stage.cuh.
+// reconstruction (all six flux schemes, single-block and batched); see fest_stage.cuh.
 #include "fest_stage.cuh"
 
 namespace fest {
@@ -7,5 +7,9 @@ FEST_STAGE_LAUNCHER(launch_stage_muscl_sst) {
   (void)prec;
   (void)occ;
   return launch_stage_sst_t<FEST_INTERP_MUSCL>(flux, grid, s, p, a, tm);
+}
+FEST_BATCH_LAUNCHER(launch_batch_muscl_sst) {
+  (void)prec;
+  return launch_batch_sst_t<FEST_INTERP_MUSCL>(flux, ctas, s, e, nb);
 }
 }  // namespace fest

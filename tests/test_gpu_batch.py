@@ -91,3 +91,58 @@ def test_batch_rejects_mixed_schemes(gpu_lib):
     arr = (C.c_void_p * 2)(*[h.h.value for h in hs])
     b = C.c_void_p()
     assert gpu_lib.fest_batch_create(arr, 2, C.byref(b)) == abi.FEST_ERR_ARG
+
+
+def sst_blocks():
+    """three k-omega SST blocks of different sizes and walls (wall distances
+    from their -5 faces' nodes)"""
+    from parity import small_case
+    out = []
+    for nc, ids in (((14, 9, 5), (-3, -4, -5, -4, -10, -10)),
+                    ((21, 7, 6), (-3, -4, -5, -6, -10, -10)),
+                    ((9, 12, 4), (-2, -4, -5, -5, -6, -6))):
+        ext, flow, scheme, bc, nodes, qp = small_case(
+            nc=nc, ids=ids, turb=True, scheme_kw=dict(interpolant="muscl", scheme_name="ausmUP",
+                                                      time_step_accuracy="RK4"),
+            flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law", MInf=0.2))
+        out.append(dict(ext=ext, flow=flow, scheme=scheme, bc=bc, nodes=nodes, qp=qp, CFL=0.5,
+                        wall=cases.wall_nodes_of(nodes, ext, bc)))
+    return out
+
+
+def sst_handle(c, lib):
+    h = Handle(c["ext"], c["flow"], c["scheme"], c["bc"], lib=lib)
+    h.setup_geometry(c["nodes"])
+    h.find_wall_dist(c["wall"])
+    h.upload_state(c["qp"])
+    h.set_precision(abi.FEST_MIXED)
+    return h
+
+
+def test_sst_batch_equals_single_blocks_and_follows_oracle(gpu_lib):
+    blocks = sst_blocks()
+    single = [sst_handle(c, gpu_lib) for c in blocks]
+    batched = [sst_handle(c, gpu_lib) for c in blocks]
+    b = make_batch(gpu_lib, batched)
+    try:
+        for h, c in zip(single, blocks):
+            h.step(6, 1, c["CFL"], with_norm=False)
+        abi.check(gpu_lib.fest_batch_step(b, 6, 1, 0.5), "fest_batch_step")
+    finally:
+        gpu_lib.fest_batch_destroy(b)
+    for n, (hs, hb, c) in enumerate(zip(single, batched, blocks)):
+        ext = c["ext"]
+        sl = (slice(3, ext.imx + 2), slice(3, ext.jmx + 2), slice(3, ext.kmx + 2))
+        qb = hb.download_state()
+        assert np.array_equal(hs.download_state()[sl], qb[sl]), f"block {n} differs"
+        blk = O.Block(ext, c["flow"], c["scheme"], c["bc"])
+        blk["nodes"] = c["nodes"]
+        blk.setup_geometry()
+        blk.find_wall_dist(c["wall"])
+        blk["qp"] = c["qp"]
+        for it in range(1, 7):
+            assert O.get_next_solution([blk], it, c["CFL"]) == 0
+        ref = blk["qp"][sl]
+        for l in range(ext.n_var):
+            e = np.abs(qb[sl][..., l] - ref[..., l]).max() / np.abs(ref[..., l]).max()
+            assert e <= 2e-5, (n, l, e)
