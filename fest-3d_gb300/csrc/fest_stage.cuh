@@ -326,7 +326,7 @@ __device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs
   const float dp = gm1 * (-dE + 0.5f * dr * (u2 * u2 + v2 * v2 + w2 * w2) -
                           0.5f * rho * (2.0f * (u * du + v * dv + w * dw) + du * du + dv * dv + dw * dw));
   // negative or NaN density/pressure after the update (update.f90:448),
-  // judged in FP32 (a NaN anywhere in the increments reaches rn or pn)
+  // decided in FP32 (a NaN anywhere in the increments reaches rn or pn)
   const float p0 = own ? qc[4] : d2f(b64[4]);
   const float rn = rho - dr, pn = p0 + dp;
   if (!(rn >= 0.0f) || !(pn >= 0.0f) || du != du || dv != dv || dw != dw) return false;
