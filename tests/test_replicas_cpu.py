@@ -44,3 +44,24 @@ def test_reference_arm_silent_off_rank_zero():
                         "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True,
                        timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_reference_arm_line_on_rank_zero():
+    """rank 0 of the reference arm times the oracle on the host cores and
+    prints one JSON line with the contract's keys: every requested warm-up
+    iteration run, no host<->device bytes, the cpu_baseline describing the
+    run itself"""
+    import json
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "3"], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["warmup"] == 3 and d["steps"] == 1
+    assert d["value"] > 0 and d["unit"] == "Mcell-residuals/s" and d["higher_is_better"] is True
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
+    assert d["config"]["workload"].startswith("smooth bump 256x96x4")
