@@ -28,6 +28,7 @@
 #include <cuda.h>  // CUtensorMap
 
 #include "fest_common.cuh"
+#include "fest_convert.cuh"
 
 namespace fest {
 
@@ -203,34 +204,7 @@ __device__ __forceinline__ T lambda_face(T gm, const T* L, const T* R, T A, T nx
   return A * (fabs((u * nx) + (v * ny) + (w * nz)) + c);
 }
 
-// ---- FP32 <-> FP64 conversions in integer arithmetic -------------------------
-// GB300 converts between FP32 and FP64 in its FP64 unit, which runs at a
-// small fraction of the FP32 rate; the mixed sweep's conversions are done
-// with integer operations instead.  f2d is exact for normal numbers, zero,
-// infinities and NaN (FP32 subnormals, below 1.2e-38, become zero); d2f
-// rounds to nearest even like a conversion instruction for results in the
-// normal FP32 range (results below it become signed zero).
-__device__ __forceinline__ double f2d(float x) {
-  const unsigned u = __float_as_uint(x);
-  const unsigned e = (u >> 23) & 0xffu, s = u & 0x80000000u, m = u & 0x7fffffu;
-  unsigned hi = s, lo = 0u;
-  if (e == 0xffu) { hi = s | 0x7ff00000u | (m >> 3); lo = m << 29; }
-  else if (e != 0u) { hi = s | ((e + 896u) << 20) | (m >> 3); lo = m << 29; }
-  return __hiloint2double((int)hi, (int)lo);
-}
-__device__ __forceinline__ float d2f(double x) {
-  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const unsigned s = hi & 0x80000000u, ed = (hi >> 20) & 0x7ffu;
-  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const unsigned rest = lo & 0x1fffffffu;  // the 29 bits dropped
-  if (ed == 0x7ffu) return __uint_as_float(s | 0x7f800000u | (mant != 0u || rest != 0u ? 0x400000u : 0u));
-  const int e = (int)ed - 896;  // FP32 biased exponent
-  if (e <= 0) return __uint_as_float(s);
-  if (e >= 255) return __uint_as_float(s | 0x7f800000u);
-  unsigned bits = s | ((unsigned)e << 23) | mant;
-  bits += (rest > 0x10000000u || (rest == 0x10000000u && (mant & 1u))) ? 1u : 0u;  // may carry into inf
-  return __uint_as_float(bits);
-}
+// ---- FP32 <-> FP64 conversions (integer arithmetic, fest_convert.cuh) -------
 __device__ __forceinline__ double to_f64(float x) { return f2d(x); }
 __device__ __forceinline__ double to_f64(double x) { return x; }
 __device__ __forceinline__ float from_f64(double x, float) { return d2f(x); }
