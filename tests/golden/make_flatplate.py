@@ -1,0 +1,79 @@
+"""Make tests/golden/flatplate_laminar.npz from the reference's laminar
+flat-plate test case (tests/Lfp of FEST-3D): its two blocks (grid_00.txt,
+21x41x2 nodes, the run-in with a slip floor; grid_01.txt, 37x41x2 nodes, the
+no-slip adiabatic plate from x = 0 to 1), joined at an interface (layout.md,
+mapping.txt), and the oracle's steady state on them after N RK4 iterations
+(CFL 1.5, local time steps) from the free stream, with the case's scheme,
+flow and BCs (system/fvscheme.md, flow.md, bc_0{0,1}.md): AUSM, MUSCL
+without limiter or pressure switch, first-order ghost cells, constant
+viscosity 2.12653e-4 (Re 10^6 on the plate), far field (-8) at the inlet,
+subsonic outlet (-4, pressure 105472.5), slip (-6) and wall (-5) faces.
+Saved: both blocks' nodes and interior states.  Run in the container that
+holds the reference:
+
+    python tests/golden/make_flatplate.py /root/reference/tests/Lfp --converge 60000
+"""
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+from make_smoothbump import read_grid  # noqa: E402
+
+U_INF, RHO_INF, P_INF, MU = 173.5943, 1.225, 105472.5, 2.12653e-4
+
+
+def flatplate_case(grids):
+    """The reference laminar flat-plate configuration on its two blocks:
+    (ext, flow, scheme, bc, nodes, qp) per block."""
+    sys.path.insert(0, os.path.join(ROOT, "fest-3d_gb300"))
+    from fest3d import abi, cases
+    flow = abi.make_flow(density_inf=RHO_INF, x_speed_inf=U_INF, pressure_inf=P_INF, mu_ref=MU,
+                         mu_variation="constant", T_ref=300.0, Sutherland_temp=110.5, Pr=0.72, tPr=0.9,
+                         gm=1.4, R_gas=287.0)
+    scheme = abi.make_scheme(scheme_name="ausm", interpolant="muscl", time_step_accuracy="RK4",
+                             time_stepping_method="l", ilimiter_switch=0, jlimiter_switch=0,
+                             klimiter_switch=0, accur=0)
+    fixed = dict(fixed_pressure=[P_INF] * 6, fixed_wall_temperature=[0.0] * 6)
+    bcs = [abi.make_bc([-8, 1, -6, -6, -6, -6], partners={1: (1, 0)}, **fixed),
+           abi.make_bc([0, -4, -5, -6, -6, -6], partners={0: (0, 1)}, **fixed)]
+    out = []
+    for n, bc in zip(grids, bcs):
+        ext = abi.Extent(*n.shape[:3], 5)
+        nodes = cases.set_interior_nodes(cases.empty_nodes(ext), n[..., 0], n[..., 1], n[..., 2])
+        out.append((ext, flow, scheme, bc, nodes, cases.uniform_state(ext, flow)))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case_dir", nargs="?", default="/root/reference/tests/Lfp")
+    ap.add_argument("--converge", type=int, default=60000, metavar="N")
+    args = ap.parse_args()
+    g = os.path.join(args.case_dir, "system", "mesh", "gridfiles")
+    grids = [read_grid(os.path.join(g, f"grid_0{b}.txt")) for b in (0, 1)]
+    assert np.array_equal(grids[0][-1], grids[1][0]), "blocks must share their interface node plane"
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    blocks = []
+    for ext, flow, scheme, bc, nodes, qp in flatplate_case(grids):
+        blk = O.Block(ext, flow, scheme, bc)
+        blk["nodes"] = nodes
+        blk.setup_geometry()
+        blk["qp"] = qp
+        blocks.append(blk)
+    O.set_threads(os.cpu_count() or 1)
+    for it in range(1, args.converge + 1):
+        assert O.get_next_solution(blocks, it, 1.5) == 0
+    qs = [b["qp"][3:b.ext.imx + 2, 3:b.ext.jmx + 2, 3:b.ext.kmx + 2, :] for b in blocks]
+    np.savez_compressed(os.path.join(HERE, "flatplate_laminar.npz"), nodes0=grids[0], nodes1=grids[1],
+                        q0=qs[0], q1=qs[1], iterations=args.converge, resnorm=O.find_resnorm(blocks))
+    print("flatplate_laminar.npz", [q.shape for q in qs])
+
+
+if __name__ == "__main__":
+    main()
