@@ -1814,6 +1814,217 @@ int fo_get_next_solution(fo_block **bl, int nb, int it, double CFL) {
   return err;
 }
 
+/* ======================================================================== */
+/* Implicit LU-SGS (lusgs.f90:186-683 laminar, 686-1196 k-omega SST).  Not
+ * part of the explicit path: the reference runs its flat-plate test cases
+ * with this integrator ("implicit", update.f90:215-218), and the oracle
+ * restates it only to replay those runs iteration for iteration. */
+
+/* one face seen from the cell being updated: area, outward normal, and the
+ * means over the two cells of volume, laminar and eddy viscosity and the
+ * SST blending F1 (lusgs.f90:278-324, 783-835) */
+typedef struct { double A, nx, ny, nz, vol, mu, mut, F1; } lu_face;
+
+/* lusgs.f90:491-630 Flux and 1027-1196 SSTFlux: the inviscid flux of the
+ * neighbour state ql advanced by the conservative change du (k and omega
+ * kept at ql's values where the advanced ones turn negative), less the
+ * thin-layer viscous flux between that state and the cell state qr, times
+ * the area; n = 5 (laminar) or 7 (SST) */
+static void lu_flux(const fest_flow *fl, int n, const double *ql, const double *qr, const double *du,
+                    const lu_face *f, double *out) {
+  const double gm = fl->gm, R = fl->R_gas;
+  double U[7], W[7];
+  U[0] = ql[0];
+  U[1] = ql[0] * ql[1];
+  U[2] = ql[0] * ql[2];
+  U[3] = ql[0] * ql[3];
+  U[4] = (ql[4] / (gm - 1.0)) + (0.5 * ql[0] * (ql[1] * ql[1] + ql[2] * ql[2] + ql[3] * ql[3]));
+  for (int l = 5; l < n; ++l) U[l] = ql[0] * ql[l];
+  for (int l = 0; l < n; ++l) U[l] = U[l] + du[l];
+  W[0] = U[0];
+  W[1] = U[1] / U[0];
+  W[2] = U[2] / U[0];
+  W[3] = U[3] / U[0];
+  W[4] = (gm - 1.0) * (U[4] - (0.5 * (U[1] * U[1] + U[2] * U[2] + U[3] * U[3]) / U[0]));
+  for (int l = 5; l < n; ++l) {
+    W[l] = U[l] / U[0];
+    W[l] = W[l] + 0.5 * (1. - fsign(1., W[l])) * (ql[l] - W[l]);
+  }
+  const double nx = f->nx, ny = f->ny, nz = f->nz;
+  double vn = (W[1] * nx) + (W[2] * ny) + (W[3] * nz);
+  double uf = 0.5 * (W[1] + qr[1]), vf = 0.5 * (W[2] + qr[2]), wf = 0.5 * (W[3] + qr[3]);
+  out[0] = W[0] * vn;
+  out[1] = (W[1] * out[0]) + (W[4] * nx);
+  out[2] = (W[2] * out[0]) + (W[4] * ny);
+  out[3] = (W[3] * out[0]) + (W[4] * nz);
+  double half_rho_u2 = 0.5 * W[0] * (W[1] * W[1] + W[2] * W[2] + W[3] * W[3]);
+  out[4] = (((gm / (gm - 1.0)) * W[4]) + half_rho_u2) * vn;
+  for (int l = 5; l < n; ++l) out[l] = W[l] * out[0];
+  /* differences across the face as the only gradient */
+  const double mu = f->mu + f->mut, s = f->A;
+  double T1 = W[4] / (W[0] * R), T2 = qr[4] / (qr[0] * R);
+  double dT[3] = {(T2 - T1) * nx * s / f->vol, (T2 - T1) * ny * s / f->vol, (T2 - T1) * nz * s / f->vol};
+  double g[5][3]; /* g[c][d]: d(u, v, w, k, omega)/d(x_d) */
+  for (int c = 0; c < 3 + (n - 5); ++c) {
+    double dv = qr[c < 3 ? 1 + c : 2 + c] - W[c < 3 ? 1 + c : 2 + c];
+    g[c][0] = dv * nx * s / f->vol;
+    g[c][1] = dv * ny * s / f->vol;
+    g[c][2] = dv * nz * s / f->vol;
+  }
+  double tr = g[0][0] + g[1][1] + g[2][2];
+  double txx = 2. * mu * (g[0][0] - tr / 3.0), tyy = 2. * mu * (g[1][1] - tr / 3.0),
+         tzz = 2. * mu * (g[2][2] - tr / 3.0);
+  double txy = mu * (g[1][0] + g[0][1]), txz = mu * (g[2][0] + g[0][2]), tyz = mu * (g[2][1] + g[1][2]);
+  double kh = (f->mu / fl->Pr + f->mut / fl->tPr) * gm * R / (gm - 1.0);
+  out[1] = out[1] - (txx * nx + txy * ny + txz * nz);
+  out[2] = out[2] - (txy * nx + tyy * ny + tyz * nz);
+  out[3] = out[3] - (txz * nx + tyz * ny + tzz * nz);
+  out[4] = out[4] - (txx * uf + txy * vf + txz * wf + kh * dT[0]) * nx;
+  out[4] = out[4] - (txy * uf + tyy * vf + tyz * wf + kh * dT[1]) * ny;
+  out[4] = out[4] - (txz * uf + tyz * vf + tzz * wf + kh * dT[2]) * nz;
+  if (n == 7) {
+    double sk = sigma_k1 * f->F1 + sigma_k2 * (1.0 - f->F1), sw = sigma_w1 * f->F1 + sigma_w2 * (1.0 - f->F1);
+    /* added, as lusgs.f90:1190-1191 has it */
+    out[5] = out[5] + (f->mu + sk * f->mut) * (g[3][0] * nx + g[3][1] * ny + g[3][2] * nz);
+    out[6] = out[6] + (f->mu + sw * f->mut) * (g[4][0] * nx + g[4][1] * ny + g[4][2] * nz);
+  }
+  for (int l = 0; l < n; ++l) out[l] = out[l] * s;
+}
+
+/* lusgs.f90:633-683 SpectralRadius: convective plus viscous spectral
+ * radius of the face, times its area; ca, cb the two cell centres */
+static double lu_radius(const fest_flow *fl, const double *qa, const double *qb, const lu_face *f,
+                        const double *ca, const double *cb) {
+  const double gm = fl->gm;
+  double vn = fabs(0.5 * (((qa[1] + qb[1]) * f->nx) + ((qa[2] + qb[2]) * f->ny) + ((qa[3] + qb[3]) * f->nz)));
+  double c = 0.5 * (sqrt(gm * qa[4] / qa[0]) + sqrt(gm * qb[4] / qb[0]));
+  double rho = 0.5 * (qa[0] + qb[0]);
+  double dx = ca[0] - cb[0], dy = ca[1] - cb[1], dz = ca[2] - cb[2];
+  double dist = sqrt(dx * dx + dy * dy + dz * dz);
+  double vis = gm * (f->mu / fl->Pr + f->mut / fl->tPr) / (rho * dist);
+  return (vn + c + vis) * f->A;
+}
+
+/* lusgs.f90:186-488 update_laminar_variables, 686-1024
+ * update_SST_variables: forward sweep for dQ*, back sweep for dQ, then the
+ * conservative update of the interior cells (k and omega only where they
+ * stay positive).  dQ is zero outside the block, so neighbouring blocks do
+ * not couple. */
+static void lu_sgs(fo_block *b) {
+  const fest_flow *fl = &b->flow;
+  const int imx = IMX, jmx = JMX, kmx = KMX, n = NV, sst = is_sst(b);
+  V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), F1 = vpad(b, FO_F1), r = vres(b), dt = vdt(b);
+  R4 cl = vcells(b), fa[3] = {vfaces(b, 0), vfaces(b, 1), vfaces(b, 2)};
+  size_t cnt = (size_t)(imx + 1) * (jmx + 1) * (kmx + 1) * n;
+  V dqs = mkv((double *)calloc(cnt, sizeof(double)), 0, 0, 0, imx + 1, jmx + 1, kmx + 1);
+  V dq = mkv((double *)calloc(cnt, sizeof(double)), 0, 0, 0, imx + 1, jmx + 1, kmx + 1);
+  static const int off[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int pass = 0; pass < 2; ++pass) {
+    /* forward: k, j, i ascending; back: i, j, k descending (lusgs.f90:363-365) */
+    int ncell = (imx - 1) * (jmx - 1) * (kmx - 1);
+    for (int c = 0; c < ncell; ++c) {
+      int i, j, k;
+      if (pass == 0) {
+        i = 1 + c % (imx - 1);
+        j = 1 + (c / (imx - 1)) % (jmx - 1);
+        k = 1 + c / ((imx - 1) * (jmx - 1));
+      } else {
+        k = kmx - 1 - c % (kmx - 1);
+        j = jmx - 1 - (c / (kmx - 1)) % (jmx - 1);
+        i = imx - 1 - c / ((kmx - 1) * (jmx - 1));
+      }
+      double q0[7], qn[6][7], lam[6], sumlam = 0.;
+      lu_face fc[6];
+      const double *c0 = r4(cl, i, j, k) + 1;
+      for (int l = 0; l < n; ++l) q0[l] = *at(q, i, j, k, l + 1);
+      for (int s = 0; s < 6; ++s) { /* 0..2 low i/j/k neighbour, 3..5 high */
+        int d = s % 3, hi = s / 3;
+        int ni = i + (hi ? off[d][0] : -off[d][0]), nj = j + (hi ? off[d][1] : -off[d][1]),
+            nk = k + (hi ? off[d][2] : -off[d][2]);
+        const double *f = r4(fa[d], i + hi * off[d][0], j + hi * off[d][1], k + hi * off[d][2]);
+        double sg = hi ? 1.0 : -1.0;
+        fc[s].A = f[0];
+        fc[s].nx = sg * f[1];
+        fc[s].ny = sg * f[2];
+        fc[s].nz = sg * f[3];
+        fc[s].vol = 0.5 * (r4(cl, ni, nj, nk)[0] + r4(cl, i, j, k)[0]);
+        fc[s].mu = 0.5 * (*at(mu, ni, nj, nk, 1) + *at(mu, i, j, k, 1));
+        fc[s].mut = sst ? 0.5 * (*at(mut, ni, nj, nk, 1) + *at(mut, i, j, k, 1)) : 0.0;
+        fc[s].F1 = sst ? 0.5 * (*at(F1, ni, nj, nk, 1) + *at(F1, i, j, k, 1)) : 0.0;
+        for (int l = 0; l < n; ++l) qn[s][l] = *at(q, ni, nj, nk, l + 1);
+        lam[s] = lu_radius(fl, qn[s], q0, &fc[s], r4(cl, ni, nj, nk) + 1, c0);
+      }
+      for (int s = 0; s < 6; ++s) sumlam = sumlam + lam[s];
+      const double vol = r4(cl, i, j, k)[0];
+      double D[7];
+      for (int l = 0; l < n; ++l) D[l] = (vol / *at(dt, i, j, k, 1)) + 0.5 * sumlam;
+      if (sst) { /* lusgs.f90:860-862: the destruction terms of k and omega */
+        double f1 = *at(F1, i, j, k, 1), beta = f1 * beta1 + (1.0 - f1) * beta2, w = q0[6];
+        D[5] = (D[5] + (bstar * w) * vol);
+        D[6] = (D[6] + 2.0 * beta * w * vol);
+      }
+      double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+      for (int d = 0; d < 3; ++d) {
+        int s = pass == 0 ? d : 3 + d;
+        int ni = i + (pass ? off[d][0] : -off[d][0]), nj = j + (pass ? off[d][1] : -off[d][1]),
+            nk = k + (pass ? off[d][2] : -off[d][2]);
+        V src = pass == 0 ? dqs : dq;
+        double dn[7], zero[7] = {0, 0, 0, 0, 0, 0, 0}, fnew[7], fold[7];
+        for (int l = 0; l < n; ++l) dn[l] = *at(src, ni, nj, nk, l + 1);
+        lu_flux(fl, n, qn[s], q0, dn, &fc[s], fnew);
+        lu_flux(fl, n, qn[s], q0, zero, &fc[s], fold);
+        for (int l = 0; l < n; ++l) acc[l] = acc[l] + ((fnew[l] - fold[l]) - lam[s] * dn[l]);
+      }
+      for (int l = 0; l < n; ++l) {
+        if (pass == 0)
+          *at(dqs, i, j, k, l + 1) = (-*at(r, i, j, k, l + 1) - 0.5 * acc[l]) / D[l];
+        else
+          *at(dq, i, j, k, l + 1) = *at(dqs, i, j, k, l + 1) - 0.5 * acc[l] / D[l];
+      }
+    }
+  }
+  const double gm = fl->gm;
+  for (int k = 1; k <= kmx - 1; ++k)
+    for (int j = 1; j <= jmx - 1; ++j)
+      for (int i = 1; i <= imx - 1; ++i) {
+        double *p[7], U[7];
+        for (int l = 0; l < n; ++l) p[l] = at(q, i, j, k, l + 1);
+        U[0] = *p[0];
+        U[1] = *p[0] * *p[1];
+        U[2] = *p[0] * *p[2];
+        U[3] = *p[0] * *p[3];
+        U[4] = (*p[4] / (gm - 1.0)) + (0.5 * *p[0] * (*p[1] * *p[1] + *p[2] * *p[2] + *p[3] * *p[3]));
+        for (int l = 5; l < n; ++l) U[l] = *p[0] * *p[l];
+        for (int l = 0; l < n; ++l) U[l] = U[l] + *at(dq, i, j, k, l + 1);
+        *p[0] = U[0];
+        *p[1] = U[1] / U[0];
+        *p[2] = U[2] / U[0];
+        *p[3] = U[3] / U[0];
+        *p[4] = (gm - 1.0) * (U[4] - (0.5 * (U[1] * U[1] + U[2] * U[2] + U[3] * U[3]) / U[0]));
+        for (int l = 5; l < n; ++l)
+          if (U[l] > 0) *p[l] = U[l] / U[0];
+      }
+  free(dqs.p);
+  free(dq.p);
+}
+
+/* update.f90:215-218: one implicit iteration; laminar and k-omega SST
+ * blocks (lusgs.f90:158-164) */
+int fo_lusgs_next_solution(fo_block **bl, int nb, int it, double CFL) {
+  for (int n = 0; n < nb; ++n) {
+    int t = bl[n]->sc.turbulence;
+    if (!((t == FEST_TURB_NONE && bl[n]->d.n_var == 5) || ((t == FEST_TURB_SST || t == FEST_TURB_SST2003) && bl[n]->d.n_var == 7)))
+      return FEST_ERR_ARG;
+  }
+  for (int n = 0; n < nb; ++n) fo_compute_temperature(bl[n]);
+  int err = fo_get_total_conservative_residue(bl, nb, it);
+  for (int n = 0; n < nb; ++n) {
+    fo_compute_time_step(bl[n], CFL);
+    lu_sgs(bl[n]);
+  }
+  return err;
+}
+
 /* resnorm.f90:128-225 */
 void fo_find_resnorm(fo_block **bl, int nb, double *out) {
   int n = bl[0]->d.n_var;

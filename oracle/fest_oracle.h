@@ -66,6 +66,11 @@ int  fo_update_with(fo_block *b, double TF, double SF, int TU, int use_store);
 /* drivers over a set of blocks (the MPI ranks of the reference) */
 int fo_get_total_conservative_residue(fo_block **blocks, int nb, int current_iter);
 int fo_get_next_solution(fo_block **blocks, int nb, int current_iter, double CFL);
+/* one iteration of the reference's implicit integrator (update.f90:215-218,
+ * LU-SGS of lusgs.f90:186-1196), laminar and k-omega SST blocks
+ * (FEST_ERR_ARG otherwise): kept to replay the reference's own implicit
+ * test runs */
+int fo_lusgs_next_solution(fo_block **blocks, int nb, int current_iter, double CFL);
 /* res_abs[0..n_var] (resnorm.f90:171-225) */
 void fo_find_resnorm(fo_block **blocks, int nb, double *res_abs);
 

@@ -85,6 +85,7 @@ def lib():
         L.fo_apply_interface.restype = None
         L.fo_get_total_conservative_residue.argtypes = [pvp, ip, ip]
         L.fo_get_next_solution.argtypes = [pvp, ip, ip, C.c_double]
+        L.fo_lusgs_next_solution.argtypes = [pvp, ip, ip, C.c_double]
         L.fo_find_resnorm.argtypes = [pvp, ip, dp]
         L.fo_find_resnorm.restype = None
         _lib = L
@@ -195,6 +196,12 @@ def get_total_conservative_residue(blocks, it):
 
 def get_next_solution(blocks, it, CFL):
     return lib().fo_get_next_solution(_arr(blocks), len(blocks), int(it), float(CFL))
+
+
+def lusgs_next_solution(blocks, it, CFL):
+    """one iteration of the reference's implicit LU-SGS integrator (laminar
+    blocks), for replaying the reference's implicit test runs"""
+    return lib().fo_lusgs_next_solution(_arr(blocks), len(blocks), int(it), float(CFL))
 
 
 def find_resnorm(blocks):

@@ -4,7 +4,11 @@ paths.
 
 Turbulent (k-omega SST): the report expects 2.900E-03 within 2 % (the
 reference computed 2.872E-03); the oracle's steady state on the case's two
-blocks gives 2.880E-03 (0.3 % above the reference's figure).
+blocks gives 2.880E-03 (0.3 % above the reference's figure).  Unlike the
+laminar case this is not explained by the case's fixed implicit run: the
+LU-SGS restatement run as the case runs (10000 iterations at CFL 3000)
+gives 2.952E-03 and converges from above to the same 2.880E-03, below which
+the reported figure lies.
 
 Laminar:
 
@@ -15,8 +19,11 @@ two blocks and the oracle's steady state on them; the drag coefficient is
 evaluated as the reference's post-processing does (Lfp/pp/Surface.py: wall
 shear from the first cells' Green-Gauss velocity gradients and viscosity on
 the wall faces, divided by the dynamic pressure and the span 0.05).  The
-oracle's value, 1.3195E-03, passes the report's 1 % band; it is 0.7 % below
-the reference's own figure, a difference not yet explained.  No GPU."""
+oracle's steady-state value, 1.3194E-03, passes the report's 1 % band; it
+is 0.75 % below the reference's own figure because that figure is not a
+steady state but the state after the case's 5000 implicit iterations,
+which the oracle's restatement of the reference's LU-SGS integrator
+replays to 1.4e-5 relative.  No GPU."""
 import os
 import sys
 
@@ -31,15 +38,18 @@ import make_flatplate as MF  # noqa: E402
 BLASIUS_CD = 1.330e-03  # tests/Report.txt, "Expected drag coeffcient", allowed tolerance 1 %
 
 
-def drag_coefficient(blk, length_span=0.05, rho=None, u=None, mu=None):
+def drag_coefficient(blk, length_span=0.05, rho=None, u=None, mu=None, recompute=True):
     """Lfp/pp/Surface.py (Tfp/pp/Surface.py: length x span 2 x 0.04) on the
     wall (j = 1) faces of the plate block; mu: the first cells' laminar
-    viscosity (default the laminar case's constant)."""
+    viscosity (default the laminar case's constant).  recompute=False uses
+    the gradients held from the last residual evaluation, as the reference's
+    output files hold them (update.f90:540 is their only evaluation)."""
     ext = blk.ext
     rho = MF.RHO_INF if rho is None else rho
     u = MF.U_INF if u is None else u
-    blk.compute_temperature()
-    blk.evaluate_all_gradients()
+    if recompute:
+        blk.compute_temperature()
+        blk.evaluate_all_gradients()
     gx, gy, gz = blk["gradqp_x"], blk["gradqp_y"], blk["gradqp_z"]
     c = (slice(1, ext.imx), 1, 1)  # first cell row, (0:imx, 0:jmx, 0:kmx) layout
     dudx, dudy, dudz = gx[c + (0,)], gy[c + (0,)], gz[c + (0,)]
@@ -79,6 +89,76 @@ def test_oracle_flat_plate_drag_passes_the_reference_test():
     assert r[2] < 1e-3 * r0[2], (r, r0)
     cd = drag_coefficient(blocks[1])
     assert abs(cd - BLASIUS_CD) <= 0.01 * BLASIUS_CD, cd
+
+
+# Report.txt, laminar case: "Difference 5.001E-02 %" from the expected
+# 1.330E-03, i.e. the reference computed 1.330e-3 * (1 - 5.001e-4)
+REFERENCE_RUN_CD = BLASIUS_CD * (1.0 - 5.001e-4)
+
+
+def test_oracle_replays_the_reference_implicit_run():
+    """The reference's own figure is not a steady state: its case runs the
+    implicit LU-SGS integrator (Lfp/system/fvscheme.md "implicit") for 5000
+    iterations at CFL 2000 from the free stream (control.md) and stops
+    there.  The oracle's restatement of that integrator, run the same way
+    on the same two blocks, gives the reference's drag coefficient to
+    1.4e-5 relative (the reference's value lies between the oracle's
+    iterations 5001 and 5002, where the drag still falls by 7e-6 relative
+    per iteration), while its converged value is 0.75 % lower."""
+    fx = np.load(os.path.join(HERE, "golden", "flatplate_laminar.npz"))
+    blocks = []
+    for ext, flow, scheme, bc, nodes, qp in MF.flatplate_case([fx["nodes0"], fx["nodes1"]]):
+        blk = O.Block(ext, flow, scheme, bc)
+        blk["nodes"] = nodes
+        blk.setup_geometry()
+        blk["qp"] = qp  # the free stream, as the reference starts (restart level 0)
+        blocks.append(blk)
+    O.set_threads(min(4, os.cpu_count() or 1))
+    for it in range(1, 5001):
+        assert O.lusgs_next_solution(blocks, it, 2000.0) == 0
+    # the gradients of the last residual evaluation, as the reference writes them
+    cd = drag_coefficient(blocks[1], recompute=False)
+    assert abs(cd - REFERENCE_RUN_CD) <= 3e-5 * REFERENCE_RUN_CD, (cd, REFERENCE_RUN_CD)
+
+
+def _sst_blocks(fx, steady):
+    case = MF.flatplate_sst_case([fx["nodes0"], fx["nodes1"]])
+    wall = MF.wall_nodes(case)
+    blocks = []
+    for n, (ext, flow, scheme, bc, nodes, qp) in enumerate(case):
+        blk = O.Block(ext, flow, scheme, bc)
+        blk["nodes"] = nodes
+        blk.setup_geometry()
+        blk.find_wall_dist(wall)
+        if steady:
+            qp = np.array(qp, order="F")
+            qp[3:ext.imx + 2, 3:ext.jmx + 2, 3:ext.kmx + 2] = fx["q%d" % n]
+        blk["qp"] = qp
+        blocks.append(blk)
+    return blocks
+
+
+def test_lusgs_sst_holds_the_explicit_steady_state():
+    """The SST branch of the LU-SGS restatement (lusgs.f90:686-1196) solves
+    the same residual: started on the explicit integrator's steady state it
+    stays there (drag within 2e-4, the fixture's own convergence level: run
+    from the free stream it settles at 2.8801e-3 against the fixture's
+    2.8805e-3; x-momentum residual not growing)."""
+    fx = np.load(os.path.join(HERE, "golden", "flatplate_sst.npz"))
+    blocks = _sst_blocks(fx, steady=True)
+    plate = blocks[1]
+
+    def cd():
+        mu = plate["mu"][3:plate.ext.imx + 2, 3, 3]
+        return drag_coefficient(plate, length_span=2 * 0.04, rho=MF.T_RHO, u=MF.T_U, mu=mu,
+                                recompute=False)
+
+    assert O.lusgs_next_solution(blocks, 1, 3000.0) == 0
+    cd0, r0 = cd(), O.find_resnorm(blocks)[2]
+    for it in range(2, 201):
+        assert O.lusgs_next_solution(blocks, it, 3000.0) == 0
+    assert abs(cd() - cd0) <= 2e-4 * cd0, (cd(), cd0)
+    assert O.find_resnorm(blocks)[2] <= r0, (O.find_resnorm(blocks)[2], r0)
 
 
 SST_CD = 2.900e-03  # tests/Report.txt, turbulent case, "Expected drag coeffcient", tolerance 2 %
