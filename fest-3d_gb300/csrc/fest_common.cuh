@@ -144,11 +144,11 @@ template <typename T, typename S> struct Line {
 
 template <typename T> __device__ __forceinline__ T limiter_fn(T r, int lim) {
   if (lim == FEST_LIMITER_VAN_ALBADA) return dv(((r * r) + r), ((r * r) + T(1)));
-  const T alpha = T(2) / T(3);  // Koren alpha family, muscl.f90:258,283
+  const T alpha = T(2) / T(3);  // Koren alpha family, muscl.f90:151,176
   return fmax2(T(0), fmin2(fmin2(T(2) * r, alpha * (r - T(1)) + T(1)), T(2)));
 }
 
-// MUSCL kappa=1/3 (muscl.f90:268-304) for cell c: Rm = state at its low face,
+// MUSCL kappa=1/3 (muscl.f90:115-200) for cell c: Rm = state at its low face,
 // Lp = state at its high face.
 template <typename T, class Lq>
 __device__ __forceinline__ void muscl_cell(const Lq& q, int c, T sw, int lim, T& Rm, T& Lp) {
@@ -214,7 +214,7 @@ __device__ __forceinline__ void weno_cell(const Lq& q, int c, T& Rm, T& Lp) {
   Rm = dv((w0 * P0 + w1 * P1 + w2 * P2), (w0 + w1 + w2));
 }
 
-// WENO on non-uniform cells (weno_NM.f90:191-235); v(c) are cell volumes
+// WENO on non-uniform cells (weno_NM.f90:82-116); v(c) are cell volumes
 template <typename T, class Lq, class Lv>
 __device__ __forceinline__ void weno_nm_cell(const Lq& q, const Lv& v, int c, T& Rm, T& Lp) {
   const T eps = T(1e-6);
@@ -259,7 +259,7 @@ __device__ __forceinline__ void weno_nm_cell(const Lq& q, const Lv& v, int c, T&
   Rm = dv((w0 * P0 + w1 * P1 + w2 * P2), (w0 + w1 + w2));
 }
 
-// PPM face estimate (ppm.f90:317-319) and extremum removal (ppm.f90:356-371)
+// PPM face estimate (ppm.f90:47-49) and extremum removal (ppm.f90:86-101)
 template <typename T, class Lq> __device__ __forceinline__ T ppm_estimate(const Lq& q, int f) {
   return dvc((T(7) * (q(f) + q(f - 1)) - (q(f + 1) + q(f - 2))), T(12));
 }

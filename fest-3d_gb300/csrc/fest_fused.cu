@@ -68,7 +68,7 @@ __global__ void k_vol_to_f32(const double* cells, float* dst, long long n) {
 }
 // ---- ghost cells on the FP32 mirror (mixed sweep, iterations > 2) ----------
 // The same face procedures as the FP64 ghost fill (bc_primitive.f90:160-206,
-// copy_bc.f90:129-202, FT_bc.f90:15-107, bc_primitive.f90:1237-1776,
+// copy_bc.f90:58-131, FT_bc.f90:15-107, bc_primitive.f90:1237-1776,
 // interface1.f90:496-700), evaluated in FP32 on the mirror that the mixed
 // sweep reads.  After iteration 2 no fix() BC writes anything
 // (bc_primitive.f90:236,318,366), so only the copy, wall, tangency, Riemann

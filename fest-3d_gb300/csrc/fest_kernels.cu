@@ -68,7 +68,7 @@ __device__ __forceinline__ void bface_ijk(const Dims& d, int f, int ta, int tb, 
 
 enum { CP_ANTI, CP_FLAT, CP_SYMM };
 
-// copy_bc.f90:129-202 for one column of a face
+// copy_bc.f90:58-131 for one column of a face
 __device__ void copy3_col(const Params& p, double* q, int f, int ta, int tb, int l, int type) {
   double a1, a2, a3;
   int il0, il1, il2;

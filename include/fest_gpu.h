@@ -62,7 +62,7 @@ enum { FEST_TIME_NONE = 0, FEST_TIME_RK2 = 1, FEST_TIME_RK4 = 2,
 enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2 };
 enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
 /* MUSCL limiter: the reference hard-codes Koren's alpha family
- * (muscl.f90:258,283); van Albada (muscl.f90:285, commented out there) is an
+ * (muscl.f90:151,176); van Albada (muscl.f90:178, commented out there) is an
  * extension selectable here. */
 enum { FEST_LIMITER_KOREN = 0, FEST_LIMITER_VAN_ALBADA = 1 };
 /* arithmetic of the hot path */

@@ -398,7 +398,7 @@ static void tang_range(const fo_block *b, int f, int *na, int *nb) {
 static double *Qp(fo_block *b, int i, int j, int k, int l) { return at(vqp(b), i, j, k, l); }
 
 enum { CP_ANTI, CP_FLAT, CP_SYMM };
-/* copy_bc.f90:129-202 copy3 */
+/* copy_bc.f90:58-131 copy3 */
 static void copy3(fo_block *b, int l, int type, int f) {
   double a1, a2, a3;
   int il[3];
@@ -782,7 +782,7 @@ static inline double limiter(const fo_block *b, double r) {
   return fmax2(0., fmin2(fmin2(2 * r, alpha * (r - 1.0) + 1.0), 2.));
 }
 
-/* muscl.f90:222-307 compute_face_state */
+/* muscl.f90:115-200 compute_face_state */
 static void muscl_dir(fo_block *b, int dir, int lam, int turb) {
   V q = vqp(b), L = vfs(b, FO_XL + 2 * dir, dir), R = vfs(b, FO_XR + 2 * dir, dir);
   int ii = dir == 0, jj = dir == 1, kk = dir == 2;
@@ -808,7 +808,7 @@ static void muscl_dir(fo_block *b, int dir, int lam, int turb) {
   }
 }
 
-/* muscl.f90:144-219 / ppm.f90:379-456 pressure_based_switching */
+/* muscl.f90:37-112 / ppm.f90:109-186 pressure_based_switching */
 static void pressure_switch(fo_block *b, int dir) {
   V q = vqp(b), L = vfs(b, FO_XL + 2 * dir, dir), R = vfs(b, FO_XR + 2 * dir, dir);
   V pd = mkv(b->a[FO_PDIF], 0, 0, 0, IMX + 1, JMX + 1, KMX + 1);
@@ -845,7 +845,7 @@ static void pressure_switch(fo_block *b, int dir) {
         }
 }
 
-/* weno.f90:24-93 and weno_NM.f90:142-241 compute_face_states */
+/* weno.f90:24-93 and weno_NM.f90:21-120 compute_face_states */
 static void weno_dir(fo_block *b, int dir, int nm) {
   V q = vqp(b), L = vfs(b, FO_XL + 2 * dir, dir), R = vfs(b, FO_XR + 2 * dir, dir);
   R4 cl = vcells(b);
@@ -924,7 +924,7 @@ static void weno_dir(fo_block *b, int dir, int nm) {
   }
 }
 
-/* ppm.f90:291-377 compute_face_estimates + remove_extrema */
+/* ppm.f90:21-107 compute_face_estimates + remove_extrema */
 static void ppm_dir(fo_block *b, int dir, int lim) {
   V q = vqp(b), L = vfs(b, FO_XL + 2 * dir, dir), R = vfs(b, FO_XR + 2 * dir, dir);
   int i_f = dir == 0, j_f = dir == 1, k_f = dir == 2;

@@ -60,7 +60,7 @@ def test_flux_known_answer(scheme, band):
     assert band[0] < F[1, 0, 0, 1] < band[1]
 
 
-RAMP = [-2.0, -1.0, 0.0, 1.0, 2.0, 3.0, 5.0, 7.0, 7.0, 7.0]  # tests/test_muscl.f90:87-96
+RAMP = [-2.0, -1.0, 0.0, 1.0, 2.0, 3.0, 5.0, 7.0, 7.0, 7.0]  # tests/test_muscl.f90:27-36
 
 
 def ramp_block(**kw):
@@ -78,7 +78,7 @@ def x_states(blk):
 
 
 def test_muscl_limiter_off_exact():
-    """tests/test_muscl.f90:81-103 (limiters off)."""
+    """tests/test_muscl.f90:17-50 (limiters off)."""
     blk = ramp_block(interpolant="muscl", ilimiter_switch=0, jlimiter_switch=0, klimiter_switch=0)
     blk.compute_face_interpolant()
     s = x_states(blk)
