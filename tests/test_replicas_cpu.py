@@ -32,7 +32,7 @@ def _rank(rank, world, port, out):
 
 def test_two_rank_max_and_rate():
     port = _free_port()
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()  # no fork of a threaded process
     mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
     assert out[0][0] == out[1][0] == 11.0
     assert out[0][1] == pytest.approx(2 * 1000 * 10 / 11.0 / 1e6)
