@@ -20,6 +20,11 @@ holds the reference:
 
     python tests/golden/make_flatplate.py /root/reference/tests/Lfp --converge 60000
     python tests/golden/make_flatplate.py /root/reference/tests/Tfp --turbulent --converge 150000
+    python tests/golden/make_flatplate.py /root/reference/tests/Tfp --restart
+
+The last writes tests/golden/flatplate_sst_restart.npz: the turbulent
+case's own starting state, which its run restarts from (see
+restart_states).
 """
 import argparse
 import os
@@ -96,15 +101,65 @@ def wall_nodes(case):
     return cases.wall_nodes_of(nodes, ext, bc)
 
 
+def read_tecplot_block(path, nodes_shape, n_cell_vars):
+    """A block-packed Tecplot dump as the reference writes it
+    (write_output_tec.f90): x, y, z at the nodes, then n_cell_vars
+    cell-centred scalars over the interior cells, one value per line after
+    a header of variable names and zone records."""
+    vals, started = [], False
+    for line in open(path):
+        t = line.split()
+        if not t:
+            continue
+        if not started:
+            try:
+                float(t[0])
+                started = True
+            except ValueError:
+                continue
+        vals.extend(float(x) for x in t)
+    v = np.array(vals)
+    ni, nj, nk = nodes_shape
+    nn, nc = ni * nj * nk, (ni - 1) * (nj - 1) * (nk - 1)
+    assert v.size == 3 * nn + n_cell_vars * nc, (path, v.size)
+    xyz = np.stack([v[m * nn:(m + 1) * nn].reshape(nodes_shape, order="F") for m in range(3)], axis=-1)
+    cc = [v[3 * nn + m * nc:3 * nn + (m + 1) * nc].reshape((ni - 1, nj - 1, nk - 1), order="F")
+          for m in range(n_cell_vars)]
+    return xyz, cc
+
+
+def restart_states(case_dir, grids):
+    """The turbulent case's starting state (control.md "Restart level 2"):
+    its dumps time_directories/0002/process_0{0,1}.dat hold u, v, w,
+    density, pressure and Mu; the reference reads velocity, density and
+    pressure (output_control.md read list) into the interior cells over a
+    free-stream state (state.f90:181-187), so k and omega start at their
+    free-stream values.  Returns per block the interior (rho, u, v, w, p)."""
+    out = []
+    for b, g in enumerate(grids):
+        path = os.path.join(case_dir, "time_directories", "0002", f"process_0{b}.dat")
+        xyz, (u, v, w, rho, p, _mu) = read_tecplot_block(path, g.shape[:3], 6)
+        assert np.array_equal(xyz, g), "the restart dump must be on the case's grid"
+        out.append(np.stack([rho, u, v, w, p], axis=-1))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("case_dir", nargs="?", default="/root/reference/tests/Lfp")
     ap.add_argument("--converge", type=int, default=60000, metavar="N")
     ap.add_argument("--turbulent", action="store_true")
+    ap.add_argument("--restart", action="store_true",
+                    help="write the turbulent case's restart state (flatplate_sst_restart.npz) and stop")
     args = ap.parse_args()
     g = os.path.join(args.case_dir, "system", "mesh", "gridfiles")
     grids = [read_grid(os.path.join(g, f"grid_0{b}.txt")) for b in (0, 1)]
     assert np.array_equal(grids[0][-1], grids[1][0]), "blocks must share their interface node plane"
+    if args.restart:
+        qs = restart_states(args.case_dir, grids)
+        np.savez_compressed(os.path.join(HERE, "flatplate_sst_restart.npz"), q0=qs[0], q1=qs[1])
+        print("flatplate_sst_restart.npz", [q.shape for q in qs])
+        return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     case = flatplate_sst_case(grids) if args.turbulent else flatplate_case(grids)

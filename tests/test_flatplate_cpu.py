@@ -4,11 +4,10 @@ paths.
 
 Turbulent (k-omega SST): the report expects 2.900E-03 within 2 % (the
 reference computed 2.872E-03); the oracle's steady state on the case's two
-blocks gives 2.880E-03 (0.3 % above the reference's figure).  Unlike the
-laminar case this is not explained by the case's fixed implicit run: the
-LU-SGS restatement run as the case runs (10000 iterations at CFL 3000)
-gives 2.952E-03 and converges from above to the same 2.880E-03, below which
-the reported figure lies.
+blocks gives 2.880E-03 (0.3 % above the reference's figure).  That figure
+too is the state after a fixed implicit run, one that restarts from the
+case's stored solution: replayed from it, the oracle's LU-SGS gives
+2.8686E-03 (0.13 % below it).
 
 Laminar:
 
@@ -162,6 +161,37 @@ def test_lusgs_sst_holds_the_explicit_steady_state():
 
 
 SST_CD = 2.900e-03  # tests/Report.txt, turbulent case, "Expected drag coeffcient", tolerance 2 %
+# Report.txt, turbulent case: "Difference 9.586E-01 %" from the expected 2.900E-03
+REFERENCE_SST_RUN_CD = SST_CD * (1.0 - 9.586e-3)
+
+
+def test_oracle_replays_the_reference_turbulent_restart_run():
+    """The turbulent case's figure is not a steady state either: the case
+    restarts (control.md "Restart level 2") from its stored solution
+    (density, velocity, pressure; k and omega at free stream), runs 10000
+    LU-SGS iterations at CFL 3000 and writes what it has.  Replayed from
+    that state (tests/golden/flatplate_sst_restart.npz) the oracle's LU-SGS
+    gives 2.8686e-3, 0.13 % below the reported 2.8722e-3 and approaching
+    it from below, the way the reported figure lies below the steady state
+    (2.8801e-3); from the free stream instead it gives 2.952e-3.  The
+    remaining 0.13 % (about 700 iterations of progress at that point) is
+    not explained; the replay is insensitive to 1e-12 perturbations of the
+    start, so it is not rounding."""
+    fx = np.load(os.path.join(HERE, "golden", "flatplate_sst.npz"))
+    rs = np.load(os.path.join(HERE, "golden", "flatplate_sst_restart.npz"))
+    blocks = _sst_blocks(fx, steady=False)
+    for n, blk in enumerate(blocks):
+        ext = blk.ext
+        qp = np.array(blk["qp"], order="F")  # the free stream, ghosts included
+        qp[3:ext.imx + 2, 3:ext.jmx + 2, 3:ext.kmx + 2, :5] = rs["q%d" % n]
+        blk["qp"] = qp
+    O.set_threads(min(4, os.cpu_count() or 1))
+    for it in range(1, 10001):
+        assert O.lusgs_next_solution(blocks, it, 3000.0) == 0
+    plate = blocks[1]
+    mu = plate["mu"][3:plate.ext.imx + 2, 3, 3]
+    cd = drag_coefficient(plate, length_span=2 * 0.04, rho=MF.T_RHO, u=MF.T_U, mu=mu, recompute=False)
+    assert cd < REFERENCE_SST_RUN_CD and abs(cd - REFERENCE_SST_RUN_CD) <= 2e-3 * REFERENCE_SST_RUN_CD, cd
 
 
 def test_oracle_sst_flat_plate_drag_passes_the_reference_test():
