@@ -48,13 +48,23 @@ class Handle:
     def _call(self, name, *args):
         return abi.check(getattr(self.lib, name)(self.h, *args), name)
 
+    def _input(self, a, name, copy=True):
+        """a as a Fortran-ordered float64 array for an argument in the
+        layout of array `name`; ValueError if it holds fewer values than the
+        C call reads (which would read past the end of it)."""
+        a = np.array(a, order="F", dtype=np.float64) if copy else np.asfortranarray(a, dtype=np.float64)
+        need = int(np.prod(self.shape[name]))
+        if a.size < need:
+            raise ValueError(f"{name} argument of shape {a.shape}: {a.size} values, the call reads {need}")
+        return a
+
     def get(self, name):
         a = np.empty(self.shape[name], order="F")
         self._call("fest_get_array", ARR[name], abi.ptr(a))
         return a
 
     def set(self, name, a):
-        a = np.asfortranarray(a, dtype=np.float64)
+        a = self._input(a, name, copy=False)
         self._call("fest_set_array", ARR[name], abi.ptr(a))
 
     @property
@@ -65,7 +75,7 @@ class Handle:
         self._call("fest_set_precision", int(p))
 
     def setup_geometry(self, nodes):
-        nodes = np.array(nodes, order="F", dtype=np.float64)
+        nodes = self._input(nodes, "nodes")
         self._call("fest_setup_geometry", abi.ptr(nodes), None, None, None, None)
         return nodes
 
@@ -80,7 +90,7 @@ class Handle:
         return d
 
     def upload_state(self, qp):
-        self._call("fest_upload_state", abi.ptr(np.asfortranarray(qp)))
+        self._call("fest_upload_state", abi.ptr(self._input(qp, "qp", copy=False)))
 
     def download_state(self):
         q = np.empty(self.shape["qp"], order="F")
@@ -88,7 +98,7 @@ class Handle:
         return q
 
     def populate_ghost_primitive(self, qp, it):
-        q = np.array(qp, order="F")
+        q = self._input(qp, "qp")
         self._call("fest_populate_ghost_primitive", abi.ptr(q), int(it))
         return q
 
@@ -98,12 +108,12 @@ class Handle:
         return T
 
     def get_next_solution(self, qp, it, CFL):
-        q = np.array(qp, order="F")
+        q = self._input(qp, "qp")
         self._call("fest_get_next_solution", abi.ptr(q), int(it), float(CFL), None, None)
         return q
 
     def residual(self, qp, it):
-        q = np.array(qp, order="F")
+        q = self._input(qp, "qp")
         r = np.empty(self.shape["residue"], order="F")
         self._call("fest_get_total_conservative_residue", abi.ptr(q), int(it), abi.ptr(r))
         return q, r
@@ -116,17 +126,18 @@ class Handle:
 
     def residual_vjp(self, qp, it, lam):
         """(dR/dq)^T lam for the residual of iteration it at state qp."""
-        q = None if qp is None else np.array(qp, order="F")
-        lam = np.asfortranarray(lam, dtype=np.float64)
+        q = None if qp is None else self._input(qp, "qp")
+        lam = self._input(lam, "residue", copy=False)
         dq = np.empty(self.shape["qp"], order="F")
         self._call("fest_residual_vjp", abi.ptr(q), int(it), abi.ptr(lam), abi.ptr(dq))
         return dq
 
     def residual_vjp_nodes(self, qp, it, lam=None, faces_bar=(None, None, None)):
         """(dR/dnodes)^T lam + (dfaces/dnodes)^T faces_bar (nodes layout)."""
-        q = None if qp is None else np.array(qp, order="F")
-        lam = None if lam is None else np.asfortranarray(lam, dtype=np.float64)
-        fb = [None if f is None else np.asfortranarray(f, dtype=np.float64) for f in faces_bar]
+        q = None if qp is None else self._input(qp, "qp")
+        lam = None if lam is None else self._input(lam, "residue", copy=False)
+        fb = [None if f is None else self._input(f, n, copy=False)
+              for f, n in zip(faces_bar, ("Ifaces", "Jfaces", "Kfaces"))]
         dn = np.empty(self.shape["nodes"], order="F")
         self._call("fest_residual_vjp_nodes", abi.ptr(q), int(it), abi.ptr(lam), abi.ptr(fb[0]),
                    abi.ptr(fb[1]), abi.ptr(fb[2]), None, abi.ptr(dn))
@@ -135,7 +146,7 @@ class Handle:
     def adjoint_solve(self, dJdq, CFL, max_iters, tol):
         """psi with (dR/dq)^T psi = -dJ/dq at the device state; returns
         (psi, iterations, drop)."""
-        dj = np.asfortranarray(dJdq, dtype=np.float64)
+        dj = self._input(dJdq, "qp", copy=False)
         psi = np.empty(self.shape["residue"], order="F")
         n = C.c_int()
         drop = C.c_double()

@@ -52,3 +52,21 @@ def test_argument_validation_without_device(lib):
     for fn in ("fest_destroy", "fest_find_resnorm", "fest_step"):
         assert getattr(L, fn)(None, *([None] if fn == "fest_find_resnorm" else
                                        [0, 0, 0.5, None] if fn == "fest_step" else [])) in (0, 1)
+
+
+def test_handle_refuses_short_host_arrays():
+    """Host arrays shorter than what a C call reads are refused before the
+    call (no device needed: the object is built without fest_create)."""
+    import numpy as np
+    from fest3d.handle import Handle
+    ext = abi.Extent(9, 7, 5, 5)
+    sh = abi.shapes(ext)
+    h = Handle.__new__(Handle)
+    h.h = None
+    h.shape = {"qp": sh["qp"], "residue": sh["residue"]}
+    ok = h._input(np.zeros(sh["qp"], order="C"), "qp")
+    assert ok.flags.f_contiguous and ok.dtype == np.float64 and ok.shape == sh["qp"]
+    with pytest.raises(ValueError):
+        h._input(np.zeros(sh["qp"])[..., :4], "qp")
+    with pytest.raises(ValueError):
+        h._input(np.zeros(sh["residue"][:3]), "residue", copy=False)
