@@ -333,7 +333,8 @@ def run_ours(args):
     N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
     STAGES = 3
     stream = torch.cuda.current_stream()
-    assert stream.cuda_stream != 0
+    if stream.cuda_stream == 0:  # the library is bound to this stream; events must see it
+        raise RuntimeError("bench needs a non-default current CUDA stream")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def barrier():

@@ -164,7 +164,8 @@ def ptr(a):
     """double* of a Fortran-ordered float64 array (None -> NULL)."""
     if a is None:
         return None
-    assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1), "need F-contiguous f64"
+    if not (a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1)):
+        raise TypeError(f"need an F-contiguous float64 array, got {a.dtype} {a.shape}")
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
