@@ -200,3 +200,40 @@ def test_geometry_unit_faces_and_cube():
     assert np.allclose(blk["cells"][1:, 3, 3, 3], [0.5, 0.5, 0.5])
     # ghost nodes are linear extrapolations (grid.f90:137-236)
     assert nd[0, 0, 3, 3] == -3.0 and nd[0, 7, 3, 3] == 4.0
+
+
+@pytest.mark.parametrize("scheme", ["ausm", "slau", "ausmP", "ausmUP", "ldfss0", "van_leer"])
+def test_wall_faces_carry_no_mass_flux(scheme):
+    """tests/test_bc.f90: setup_bc with a wall at jmin gives
+    make_G_flux_zero(1) == 0 (bc.f90:53-66): wall (-5), slip (-6) and pole
+    (-7) faces get a zero mass flux in every scheme (ausm.f90:103-108,
+    slau.f90:166-168, ausmP.f90:160-162, ausmUP.f90:178-180,
+    ldfss0.f90:110-115, van_leer.f90:95-100), hence a zero energy flux;
+    other faces keep theirs.  Random face states, unit normals."""
+    ext = abi.Extent(5, 5, 5, 5)
+    ids = [-3, -6, -5, -4, -7, -11]  # imin, imax (slip), jmin (wall), jmax, kmin (pole), kmax
+    blk = O.Block(ext, abi.make_flow(), abi.make_scheme(scheme_name=scheme), abi.make_bc(ids))
+    unit_faces(blk)
+    rng = np.random.default_rng(7)
+    for n in ("x_qp_left", "x_qp_right", "y_qp_left", "y_qp_right", "z_qp_left", "z_qp_right"):
+        a = blk[n]
+        a[..., 0] = rng.uniform(0.8, 1.4, a.shape[:-1])
+        a[..., 1:4] = rng.uniform(-0.5, 0.5, a.shape[:-1] + (3,))
+        a[..., 4] = rng.uniform(0.6, 1.2, a.shape[:-1])
+    assert blk.compute_fluxes() == 0
+    F, G, H = blk["F"], blk["G"], blk["H"]  # face index 1 at position 0
+    for masked, normal in ((F[ext.imx - 1], 1), (G[:, 0], 2), (H[:, :, 0], 3)):
+        assert np.all(masked[..., 0] == 0.0) and np.all(masked[..., 4] == 0.0)
+        # only the pressure force remains: along the normal, none tangentially
+        assert np.all(masked[..., normal] != 0.0)
+        assert np.all(np.delete(masked[..., 1:4], normal - 1, axis=-1) == 0.0)
+    for open_face in (F[0], G[:, ext.jmx - 1], H[:, :, ext.kmx - 1]):
+        assert np.all(open_face[..., 0] != 0.0)
+    # control: the same face states without walls carry mass through those faces
+    ctl = O.Block(ext, abi.make_flow(), abi.make_scheme(scheme_name=scheme), abi.make_bc([-3] * 6))
+    for n in ("Ifaces", "Jfaces", "Kfaces", "x_qp_left", "x_qp_right", "y_qp_left", "y_qp_right",
+              "z_qp_left", "z_qp_right"):
+        ctl[n] = blk[n]
+    assert ctl.compute_fluxes() == 0
+    for face in (ctl["F"][ext.imx - 1], ctl["G"][:, 0], ctl["H"][:, :, 0]):
+        assert np.all(face[..., 0] != 0.0)
