@@ -93,6 +93,17 @@ def make_flow(**kw):
     return f
 
 
+def sst_free_stream(flow, tu_inf=1.0, mu_ratio_inf=1.0):
+    """Free-stream k and omega of the SST models from the turbulence
+    intensity tu_inf (percent) and the eddy-to-laminar viscosity ratio, as
+    init_infinity_values derives them (state.f90:90, 98-99; defaults of
+    vartypes.f90:256, 266): returns (tk_inf, tw_inf) for make_flow."""
+    intensity = tu_inf / 100
+    tk = 1.5 * ((flow.vel_mag * intensity) ** 2)
+    tw = flow.density_inf * tk / (flow.mu_ref * mu_ratio_inf)
+    return tk, tw
+
+
 def make_scheme(**kw):
     """schemetype with the reference defaults (vartypes.f90:198-231)."""
     d = dict(scheme_name="ausm", interpolant="muscl", time_stepping_method="l",

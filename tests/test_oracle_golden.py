@@ -237,3 +237,21 @@ def test_wall_faces_carry_no_mass_flux(scheme):
     assert ctl.compute_fluxes() == 0
     for face in (ctl["F"][ext.imx - 1], ctl["G"][:, 0], ctl["H"][:, :, 0]):
         assert np.all(face[..., 0] != 0.0)
+
+
+def test_sst_free_stream_values():
+    """tests/test_state.f90: with the flow defaults, SST and mu_ref = 1,
+    init_infinity_values gives Turb_intensity_inf 0.01, tk_inf 1.5 (and a
+    7-variable state, which fest_create requires for SST blocks)."""
+    flow = abi.make_flow(mu_ref=1.0)
+    tk, tw = abi.sst_free_stream(flow)
+    assert tk == 1.5
+    assert tw == flow.density_inf * 1.5 / 1.0
+    # the turbulent flat plate's free stream (tests/Tfp/system/flow.md)
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_flatplate as MF
+    f = abi.make_flow(density_inf=MF.T_RHO, x_speed_inf=MF.T_U, mu_ref=MF.T_MU)
+    tk, tw = abi.sst_free_stream(f, tu_inf=0.03873, mu_ratio_inf=0.01)
+    assert tk == pytest.approx(MF.T_TK, rel=1e-15) and tw == pytest.approx(MF.T_TW, rel=1e-15)
