@@ -1,7 +1,8 @@
-"""The reference's case files on the host: grid files, Tecplot block output,
-restart logs and residual-norm lines, byte for byte in the formats FEST-3D's
-own readers and writers use, so that a run of this library starts from, and
-leaves behind, files the reference's driver and post-processing read.
+"""The reference's case files on the host: grid files, Tecplot and legacy
+VTK block output, restart logs and residual-norm lines, in the formats
+FEST-3D's own readers and writers use, so that a run of this library starts
+from, and leaves behind, files the reference's driver and post-processing
+read.
 
 Arrays are in the C ABI's layouts (fest_gpu.h): the state ``qp`` is
 Fortran-ordered ``(imx+5, jmx+5, kmx+5, n_var)`` with Fortran index -2 at
@@ -11,8 +12,10 @@ Fortran-ordered ``(imx+5, jmx+5, kmx+5, n_var)`` with Fortran index -2 at
 Number formats follow the Fortran edit descriptors the reference writes
 with (ES28.15E4, Ew.dE2, F0.16, I0): the decimal digits are the correctly
 rounded digits of the binary value (round half to even, as the C library's
-printf that gfortran formats through), checked byte for byte against output
-files the reference wrote.
+printf that gfortran formats through).  Grid files, Tecplot output and
+restart logs are checked byte for byte against files the reference wrote;
+the legacy VTK format, of which the reference ships no sample, against
+known answers.
 """
 import math
 import os
@@ -228,6 +231,115 @@ def read_tecplot(path, qp, variables=("Velocity", "Density", "Pressure"), turbul
             pos += nc
             if l is not None:
                 qp[cells + (l,)] = field
+    return qp
+
+
+# ---- legacy VTK output (write_output_vtk.f90, read_output_vtk.f90) ---------
+# scalar names in the file (write_output_vtk.f90:131-199); trailing blanks
+# of the gradient names are trimmed by the writer
+_VTK_SCALAR = {"Density": "Density", "Pressure": "Pressure", "Mu": "Mu", "Mu_t": "Mu_t",
+               "TKE": "TKE", "Omega": "Omega", "Kl": "Kl", "tv": "tv", "tgm": "tgm",
+               "Dissipation": "Dissipation", "Wall_distance": "dist", "F1": "F1"}
+for _g in ("u", "v", "w", "T", "tk", "tw"):
+    for _c in "xyz":
+        _VTK_SCALAR["D%sd%s" % (_g, _c)] = "d%sd%s" % (_g, _c)
+
+
+def vtk_text(qp, nodes, variables=("Velocity", "Density", "Pressure"), turbulence="none",
+             extra=None, data_format="ASCII"):
+    """The text write_file (write_output_vtk.f90:46-163) writes for one
+    block: the header (write_header), the nodes as F0.16 triples
+    (write_grid), the velocity as ES27.16E4 triples (write_velocity) and
+    each scalar as one ES25.16E4 value per line (write_scalar), every
+    section closed by an empty record.  Arguments as tecplot_text.  The
+    reference ships no VTK output of its own, so this format is restated
+    from the writer's edit descriptors and checked by known answers and
+    round trips, not against reference bytes."""
+    qp = np.asarray(qp)
+    imx, jmx, kmx = qp.shape[0] - 5, qp.shape[1] - 5, qp.shape[2] - 5
+    if nodes.shape != (3, imx + 6, jmx + 6, kmx + 6):
+        raise ValueError(f"nodes {nodes.shape} do not match a {imx}x{jmx}x{kmx} block")
+    extra = extra or {}
+    nc = (imx - 1) * (jmx - 1) * (kmx - 1)
+    out = ["# vtk DataFile Version 3.1", "cfd-iitm output", data_format, "DATASET STRUCTURED_GRID",
+           "DIMENSIONS %d %d %d" % (imx, jmx, kmx), "POINTS %d DOUBLE" % (imx * jmx * kmx)]
+    xyz = [nodes[c, 3:3 + imx, 3:3 + jmx, 3:3 + kmx].ravel(order="F") for c in range(3)]
+    out += ["%s %s %s" % (fortran_f0(x), fortran_f0(y), fortran_f0(z)) for x, y, z in zip(*xyz)]
+    out.append("")
+    cells = (slice(3, imx + 2), slice(3, jmx + 2), slice(3, kmx + 2))
+    k_omega = turbulence in _TURB_WITH_K_OMEGA
+    for v in variables:
+        if v == "do not write":
+            continue
+        if v == "Velocity":
+            out += ["CELL_DATA %d" % nc, "VECTORS Velocity FLOAT"]
+            uvw = [qp[cells + (l,)].ravel(order="F") for l in (1, 2, 3)]
+            out += ["%s %s %s" % (fortran_es(u, 27, 16), fortran_es(vv, 27, 16), fortran_es(w, 27, 16))
+                    for u, vv, w in zip(*uvw)]
+        elif v in _VTK_SCALAR:
+            if v in ("Density", "Pressure"):
+                a = qp[cells + (0 if v == "Density" else 4,)]
+            elif v in ("TKE", "Omega"):
+                if not k_omega:
+                    raise ValueError(f"{v} needs a k-omega turbulence model, not {turbulence!r}")
+                a = qp[cells + (5 if v == "TKE" else 6,)]
+            elif v in extra:
+                e = np.asarray(extra[v])
+                off = 3 if e.shape[0] == imx + 5 else 1
+                a = e[off:off + imx - 1, off:off + jmx - 1, off:off + kmx - 1]
+            else:
+                raise ValueError(f"no data for output variable {v!r}")
+            out += ["SCALARS %s FLOAT" % _VTK_SCALAR[v], "LOOKUP_TABLE default"]
+            out += [fortran_es(x, 25, 16) for x in np.asarray(a).ravel(order="F")]
+        else:
+            continue  # the reference prints a message and writes nothing
+        out.append("")
+    return "\n".join(out) + "\n"
+
+
+def write_vtk(path, qp, nodes, **kw):
+    """vtk_text(qp, nodes, **kw) written to `path`."""
+    with open(path, "w") as f:
+        f.write(vtk_text(qp, nodes, **kw))
+
+
+def read_vtk(path, qp, variables=("Velocity", "Density", "Pressure"), turbulence="none"):
+    """Fill the interior cells of qp (in place; also returned) from a
+    legacy VTK block file as read_file (read_output_vtk.f90:24-92) reads
+    it, one record per line: header, grid, then each listed variable
+    (Velocity as one vector field, Density, Pressure, TKE, Omega); 'do not
+    read' skips a scalar field and other names read nothing."""
+    imx, jmx, kmx = qp.shape[0] - 5, qp.shape[1] - 5, qp.shape[2] - 5
+    nc, nn = (imx - 1) * (jmx - 1) * (kmx - 1), imx * jmx * kmx
+    with open(path) as f:
+        lines = f.read().split("\n")
+    pos = 4 + 2 + nn + 1  # header, DIMENSIONS/POINTS, the points, the empty record
+    cells = (slice(3, imx + 2), slice(3, jmx + 2), slice(3, kmx + 2))
+    shape = (imx - 1, jmx - 1, kmx - 1)
+
+    def block(n_cols):
+        nonlocal pos
+        rows = lines[pos + 2:pos + 2 + nc]
+        if len(rows) < nc:
+            raise ValueError(f"{path}: the file ends inside a field of {nc} cells")
+        pos += 2 + nc + 1
+        a = np.array(" ".join(rows).split(), dtype=np.float64)
+        if a.size != nc * n_cols:
+            raise ValueError(f"{path}: {a.size} values where {nc * n_cols} belong")
+        return a.reshape(nc, n_cols)
+
+    for v in variables:
+        if v in ("TKE", "Omega") and turbulence not in _TURB_WITH_K_OMEGA:
+            raise ValueError(f"{v} needs a k-omega turbulence model, not {turbulence!r}")
+        if v == "Velocity":
+            a = block(3)
+            for c, l in enumerate((1, 2, 3)):
+                qp[cells + (l,)] = a[:, c].reshape(shape, order="F")
+        elif v in ("Density", "Pressure", "TKE", "Omega"):
+            l = {"Density": 0, "Pressure": 4, "TKE": 5, "Omega": 6}[v]
+            qp[cells + (l,)] = block(1)[:, 0].reshape(shape, order="F")
+        elif v == "do not read":
+            pos += 2 + nc + 1
     return qp
 
 

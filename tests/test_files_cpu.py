@@ -170,3 +170,39 @@ def test_resnorm_log(tmp_path):
     log.close()
     assert rr[1] == 0.5
     assert p.read_text().splitlines()[-1].split()[0] == "9"
+
+
+def test_vtk_output_format_and_round_trip(tmp_path):
+    """write_file/read_file of the legacy VTK format (write_output_vtk.f90,
+    read_output_vtk.f90): known answers for the records the writer's edit
+    descriptors give, and the SST state (with TKE and Omega) read back to
+    within 17 significant digits of rounding."""
+    ext = abi.Extent(6, 5, 3, 7)
+    nodes = cases.box_nodes(ext, perturb=0.05)
+    qp = np.asfortranarray(cases.random_state(ext, seed=5, tk=1.5, tw=800.0))
+    qp[3, 3, 3, 1:4] = (-1.5, 0.25, 0.0)
+    qp[3, 3, 3, 0] = 1.225
+    mu = np.full(qp.shape[:3], 1.8e-5, order="F")
+    names = ("Velocity", "Density", "Pressure", "TKE", "Omega", "Mu")
+    txt = FI.vtk_text(qp, nodes, variables=names, turbulence="sst", extra={"Mu": mu})
+    rows = txt.split("\n")
+    assert rows[:6] == ["# vtk DataFile Version 3.1", "cfd-iitm output", "ASCII",
+                        "DATASET STRUCTURED_GRID", "DIMENSIONS 6 5 3", "POINTS 90 DOUBLE"]
+    assert rows[6] == "%s %s %s" % tuple(FI.fortran_f0(nodes[c, 3, 3, 3]) for c in range(3))
+    v = rows.index("VECTORS Velocity FLOAT")
+    assert rows[v - 1] == "CELL_DATA 40" and rows[v - 2] == "" and rows[v - 3] != ""
+    assert rows[v + 1] == "  -1.5000000000000000E+0000    2.5000000000000000E-0001    0.0000000000000000E+0000"
+    d = rows.index("SCALARS Density FLOAT")
+    assert rows[d + 1] == "LOOKUP_TABLE default"
+    assert rows[d + 2] == " 1.2250000000000001E+0000"  # 17 significant digits of the double 1.225
+    assert "SCALARS Mu FLOAT" in rows and txt.endswith("\n\n")
+    p = tmp_path / "process_00.vtk"
+    p.write_text(txt)
+    back = np.zeros_like(qp)
+    FI.read_vtk(p, back, ("Velocity", "Density", "Pressure", "TKE", "Omega", "Mu"), turbulence="sst")
+    c = (slice(3, 8), slice(3, 7), slice(3, 5))
+    assert np.array_equal(back[c], qp[c])  # 17 digits round-trip every double
+    # 'do not read' skips a scalar field
+    back2 = np.zeros_like(qp)
+    FI.read_vtk(p, back2, ("Velocity", "do not read", "Pressure"), turbulence="sst")
+    assert np.array_equal(back2[c + (4,)], qp[c + (4,)]) and np.all(back2[c + (0,)] == 0)
