@@ -61,7 +61,8 @@ def fortran_es(x, w=28, d=15, e=4):
 def fortran_e(x, w, d, e=2):
     """x under Ew.dEe: mantissa 0.ddd (d digits), exponent of e digits,
     right-justified in w (gfortran prints the optional leading zero when
-    the width leaves room for it)."""
+    the width leaves room for it).  e=None is Ew.d: a two-digit exponent
+    after 'E', or a sign and three digits without the 'E' beyond 99."""
     x = float(x)
     if not math.isfinite(x):
         return _nonfinite(x).rjust(w)
@@ -71,9 +72,15 @@ def fortran_e(x, w, d, e=2):
         s = "%.*e" % (d - 1, abs(x))  # d significant digits, correctly rounded
         mant, ex = s.split("e")
         digits, ex, neg = mant.replace(".", ""), int(ex) + 1, x < 0
-    if len(str(abs(ex))) > e:
+    sign = "-" if ex < 0 else "+"
+    if e is None:
+        if abs(ex) > 999:
+            return "*" * w
+        body = "0.%s%s%s%0*d" % (digits, "E" if abs(ex) <= 99 else "", sign, 2 if abs(ex) <= 99 else 3, abs(ex))
+    elif len(str(abs(ex))) > e:
         return "*" * w
-    body = "0.%sE%s%0*d" % (digits, "-" if ex < 0 else "+", e, abs(ex))
+    else:
+        body = "0.%sE%s%0*d" % (digits, sign, e, abs(ex))
     if neg:
         body = "-" + body
     if len(body) > w:
@@ -188,6 +195,57 @@ def tecplot_text(qp, nodes, variables=("Velocity", "Density", "Pressure"), block
             a = np.asarray(extra[v])
             off = 3 if a.shape[0] == imx + 5 else 1  # padded (-2:) or gradient (0:) lower bound
             out += column(a[off:off + imx - 1, off:off + jmx - 1, off:off + kmx - 1])
+        else:
+            raise ValueError(f"no data for output variable {v!r}")
+    return "\n".join(out) + "\n"
+
+
+def tecplot_nodal_text(qp, nodes, variables=("Velocity", "Density", "Pressure"), block=0,
+                       solution_time=0, turbulence="none", extra=None):
+    """The text of the 'tecplot_nodal' output (write_output_tec_node.f90):
+    every field at the nodes i = 1..imx, j = 1..jmx of the node planes
+    k = 1..kmx-1, a node's value the mean 0.25*(v(i,j)+v(i-1,j)+v(i,j-1)+
+    v(i-1,j-1)) of the four cells around it in its i-j plane (ghost cells
+    included, summed in that order), written 35 values per record under
+    E25.15.  Arguments as tecplot_text."""
+    qp = np.asarray(qp)
+    imx, jmx, kmx = qp.shape[0] - 5, qp.shape[1] - 5, qp.shape[2] - 5
+    if nodes.shape != (3, imx + 6, jmx + 6, kmx + 6):
+        raise ValueError(f"nodes {nodes.shape} do not match a {imx}x{jmx}x{kmx} block")
+    extra = extra or {}
+    k_omega = turbulence in _TURB_WITH_K_OMEGA
+    labels = _tec_labels(variables, turbulence)
+    total = 3 + sum(len(lb.split()) for lb in labels)
+    out = ["variables = x y z "] + labels
+    out.append("zone T=block%04d  i=%05d j=%05d k=%05d Datapacking=Block" % (block, imx, jmx, kmx - 1))
+    out.append(" Varlocation=([1-3]=Nodal)")
+    out.append("Varlocation=([4-%02d]=Nodal)" % total)
+    out.append("STRANDID=%04d" % 1)
+    out.append("SOLUTIONTIME=%04d" % solution_time)
+
+    def records(a):  # one write statement: 35 values per record
+        v = [fortran_e(x, 25, 15, None) for x in np.asarray(a).ravel(order="F")]
+        return ["".join(v[n:n + 35]) for n in range(0, len(v), 35)]
+
+    def at_nodes(a, off):  # a over cells, Fortran index -off at 0
+        i0, j0 = off + 1, off + 1  # cell 1 (the cell after node 1)
+        k = slice(off + 1, off + kmx)  # k = 1..kmx-1
+        return 0.25 * (a[i0:i0 + imx, j0:j0 + jmx, k] + a[i0 - 1:i0 - 1 + imx, j0:j0 + jmx, k]
+                       + a[i0:i0 + imx, j0 - 1:j0 - 1 + jmx, k] + a[i0 - 1:i0 - 1 + imx, j0 - 1:j0 - 1 + jmx, k])
+
+    for c in range(3):
+        out += records(nodes[c, 3:3 + imx, 3:3 + jmx, 3:3 + kmx - 1])
+    for v in variables:
+        if v == "do not write":
+            continue
+        if v in _STATE_VARS:
+            if v in ("TKE", "Omega") and not k_omega:
+                raise ValueError(f"{v} needs a k-omega turbulence model, not {turbulence!r}")
+            for l in _STATE_VARS[v][1]:
+                out += records(at_nodes(qp[..., l], 2))
+        elif v in extra:
+            a = np.asarray(extra[v])
+            out += records(at_nodes(a, 2 if a.shape[0] == imx + 5 else 0))
         else:
             raise ValueError(f"no data for output variable {v!r}")
     return "\n".join(out) + "\n"

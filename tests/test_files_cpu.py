@@ -206,3 +206,36 @@ def test_vtk_output_format_and_round_trip(tmp_path):
     back2 = np.zeros_like(qp)
     FI.read_vtk(p, back2, ("Velocity", "do not read", "Pressure"), turbulence="sst")
     assert np.array_equal(back2[c + (4,)], qp[c + (4,)]) and np.all(back2[c + (0,)] == 0)
+
+
+def test_tecplot_nodal_output():
+    """'tecplot_nodal' output (write_output_tec_node.f90): header with
+    k = kmx-1 node planes and nodal data, node coordinates of those planes,
+    each field the four-cell mean around a node (ghost cells included, the
+    reference's summation order), 35 E25.15 values per record."""
+    ext = abi.Extent(5, 4, 3, 5)
+    nodes = cases.box_nodes(ext, perturb=0.05)
+    qp = np.asfortranarray(cases.random_state(ext, seed=7))
+    txt = FI.tecplot_nodal_text(qp, nodes, block=2, solution_time=4)
+    rows = txt.split("\n")
+    assert rows[:9] == ["variables = x y z ", " u v w ", "Density ", "Pressure ",
+                        "zone T=block0002  i=00005 j=00004 k=00002 Datapacking=Block",
+                        " Varlocation=([1-3]=Nodal)", "Varlocation=([4-08]=Nodal)",
+                        "STRANDID=0001", "SOLUTIONTIME=0004"]
+    n = 5 * 4 * 2  # values per field: 40 -> records of 35 and 5
+    body = rows[9:-1]
+    assert len(body) == 8 * 2 and all(len(r) == 25 * 35 for r in body[0::2])
+    assert all(len(r) == 25 * 5 for r in body[1::2])
+    vals = np.array([float(r[m:m + 25]) for r in body for m in range(0, len(r), 25)]).reshape(8, n)
+    x = [nodes[0, i + 2, j + 2, k + 2] for k in (1, 2) for j in range(1, 5) for i in range(1, 6)]
+    assert np.allclose(vals[0], x, rtol=1e-14, atol=0)  # 15 significant digits
+    expect = []
+    for l in (1, 2, 3, 0, 4):
+        q = qp[..., l]
+        expect.append([0.25 * (q[i + 2, j + 2, k + 2] + q[i + 1, j + 2, k + 2] + q[i + 2, j + 1, k + 2]
+                               + q[i + 1, j + 1, k + 2])
+                       for k in (1, 2) for j in range(1, 5) for i in range(1, 6)])
+    first = [FI.fortran_e(v, 25, 15, None) for v in expect[0]]
+    assert body[6] == "".join(first[:35]) and body[7] == "".join(first[35:])
+    assert np.allclose(vals[3:], expect, rtol=1e-14, atol=0)
+    assert FI.fortran_e(-2e-120, 25, 15, None) == "   -0.200000000000000-119"
