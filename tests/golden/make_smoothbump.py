@@ -30,13 +30,10 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 
 
 def read_grid(path):
-    """FEST-3D grid file (grid.f90:110-127): 'imx jmx kmx' then one node
-    per line, i fastest."""
-    with open(path) as f:
-        imx, jmx, kmx = (int(x) for x in f.readline().split())
-        xyz = np.loadtxt(f)
-    assert xyz.shape == (imx * jmx * kmx, 3)
-    return xyz.reshape(kmx, jmx, imx, 3).transpose(2, 1, 0, 3)  # (i, j, k, xyz)
+    """FEST-3D grid file as (imx, jmx, kmx, 3) nodes (fest3d.files)."""
+    sys.path.insert(0, os.path.join(ROOT, "fest-3d_gb300"))
+    from fest3d.files import read_grid as read
+    return read(path)
 
 
 def smoothbump_case(nodes_ijk):
