@@ -450,10 +450,12 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and ws == 1:
+        v1, n1, _ = cpu_rate(case, seconds=3.0, threads=1)
         v, n_it, threads = cpu_rate(case, seconds=10.0)
         cpu = {"value": v, "unit": "Mcell-residuals/s", "cores": threads, "kind": "port",
                "sample": f"{n_it} TVD-RK3 iterations of the full 256x96x4 block (~10 s), "
-                         f"C restatement of the reference path, OpenMP {threads} threads"}
+                         f"C restatement of the reference path, OpenMP {threads} threads",
+               "single_thread": {"value": v1, "sample": f"{n1} iterations (~3 s), 1 thread"}}
 
     if rank == 0:
         line = {
