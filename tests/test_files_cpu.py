@@ -239,3 +239,23 @@ def test_tecplot_nodal_output():
     assert body[6] == "".join(first[:35]) and body[7] == "".join(first[35:])
     assert np.allclose(vals[3:], expect, rtol=1e-14, atol=0)
     assert FI.fortran_e(-2e-120, 25, 15, None) == "   -0.200000000000000-119"
+
+
+def test_tecplot_sst_state_round_trip(tmp_path):
+    """An SST state written with TKE and Omega (write_output_tec.f90's tk/tw
+    fields, header 'TKE ' and 'Omega ', 10 variables) reads back into
+    variables 6 and 7; asking for them without a k-omega model is refused."""
+    ext = abi.Extent(7, 6, 3, 7)
+    nodes = cases.box_nodes(ext)
+    qp = np.asfortranarray(cases.random_state(ext, seed=11, tk=2.0, tw=900.0))
+    names = ("Velocity", "Density", "Pressure", "TKE", "Omega")
+    p = tmp_path / "sst.dat"
+    FI.write_tecplot(p, qp, nodes, variables=names, turbulence="sst")
+    rows = p.read_text().split("\n")
+    assert rows[4:6] == ["TKE ", "Omega "] and rows[8] == "Varlocation=([4-10]=CELLCENTERED)"
+    back = np.zeros_like(qp)
+    FI.read_tecplot(p, back, names, turbulence="sst")
+    c = (slice(3, 9), slice(3, 8), slice(3, 5))
+    assert np.allclose(back[c], qp[c], rtol=6e-16, atol=0)
+    with pytest.raises(ValueError):
+        FI.tecplot_text(qp, nodes, variables=names, turbulence="none")
