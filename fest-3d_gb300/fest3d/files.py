@@ -141,7 +141,7 @@ def nodes_from_grid(nodes_ijk):
 
 
 # ---- Tecplot block output (write_output_tec.f90, read_output_tec.f90) ------
-def _tec_labels(variables, turbulence):
+def _tec_labels(variables):
     labels = []
     for v in variables:
         if v == "do not write":
@@ -167,7 +167,7 @@ def tecplot_text(qp, nodes, variables=("Velocity", "Density", "Pressure"), block
         raise ValueError(f"nodes {nodes.shape} do not match a {imx}x{jmx}x{kmx} block")
     extra = extra or {}
     k_omega = turbulence in _TURB_WITH_K_OMEGA
-    labels = _tec_labels(variables, turbulence)
+    labels = _tec_labels(variables)
     total = 3 + sum(len(lb.split()) for lb in labels)
     out = ["variables = x y z "]
     out += [lb for lb in labels]
@@ -214,7 +214,7 @@ def tecplot_nodal_text(qp, nodes, variables=("Velocity", "Density", "Pressure"),
         raise ValueError(f"nodes {nodes.shape} do not match a {imx}x{jmx}x{kmx} block")
     extra = extra or {}
     k_omega = turbulence in _TURB_WITH_K_OMEGA
-    labels = _tec_labels(variables, turbulence)
+    labels = _tec_labels(variables)
     total = 3 + sum(len(lb.split()) for lb in labels)
     out = ["variables = x y z "] + labels
     out.append("zone T=block%04d  i=%05d j=%05d k=%05d Datapacking=Block" % (block, imx, jmx, kmx - 1))
