@@ -135,6 +135,10 @@ extern "C" int fest_find_resnorm_noalloc(const fest_extent* ext, const fest_flow
   if (ext->imx < 2 || ext->jmx < 2 || ext->kmx < 2 || ext->n_var < 1) return FEST_ERR_ARG;
   // the fixed scratch holds kNaSlots sums per CTA: n_var + 1 must fit
   if (ext->n_var + 1 > kNaSlots) return FEST_ERR_SCRATCH;
+  // the scales below are those of the laminar/Euler (5) and k-omega SST (7)
+  // variable sets (resnorm.f90:128-169); other counts (SA's 6, k-kL's 7 with
+  // other free-stream scales) are models this library does not build
+  if (ext->n_var != 5 && ext->n_var != 7) return FEST_ERR_ARG;
   int dev = -1;
   int rc = status_of(cudaGetDevice(&dev));
   if (rc) return rc;

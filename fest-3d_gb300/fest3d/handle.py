@@ -80,7 +80,9 @@ class Handle:
         return nodes
 
     def set_metrics(self, cells, If, Jf, Kf):
-        self._call("fest_set_metrics", abi.ptr(cells), abi.ptr(If), abi.ptr(Jf), abi.ptr(Kf))
+        args = [self._input(a, n, copy=False) for a, n in
+                ((cells, "cells"), (If, "Ifaces"), (Jf, "Jfaces"), (Kf, "Kfaces"))]
+        self._call("fest_set_metrics", *[abi.ptr(a) for a in args])
 
     def find_wall_dist(self, wall_xyz):
         w = np.ascontiguousarray(wall_xyz, dtype=np.float64)

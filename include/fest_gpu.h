@@ -312,7 +312,8 @@ int fest_adjoint_solve(fest_handle *h, const double *dJdq, double CFL,
  * (memory held by their own pool, or an asynchronous loop that a
  * cudaMalloc/cudaFree pair would synchronise).  It allocates nothing: its
  * scratch is a fixed 32 KiB area per device, so n_var may be at most 7
- * (FEST_ERR_SCRATCH otherwise).  Calls that overlap in time on one device
+ * (FEST_ERR_SCRATCH otherwise); n_var must be 5 (Euler, laminar) or 7
+ * (k-omega SST, scaled by tk_inf and tw_inf), FEST_ERR_ARG otherwise.  Calls that overlap in time on one device
  * race on that area and must be serialised by the caller.  The first call
  * on each device (with that device current) does the setup and should come
  * before any stream capture.  Runs on cuda_stream (NULL: the legacy default

@@ -63,10 +63,18 @@ def test_handle_refuses_short_host_arrays():
     sh = abi.shapes(ext)
     h = Handle.__new__(Handle)
     h.h = None
-    h.shape = {"qp": sh["qp"], "residue": sh["residue"]}
+    h.shape = {"qp": sh["qp"], "residue": sh["residue"], "cells": sh["cells"],
+               "Ifaces": sh["Ifaces"], "Jfaces": sh["Jfaces"], "Kfaces": sh["Kfaces"]}
     ok = h._input(np.zeros(sh["qp"], order="C"), "qp")
     assert ok.flags.f_contiguous and ok.dtype == np.float64 and ok.shape == sh["qp"]
     with pytest.raises(ValueError):
         h._input(np.zeros(sh["qp"])[..., :4], "qp")
     with pytest.raises(ValueError):
         h._input(np.zeros(sh["residue"][:3]), "residue", copy=False)
+    # set_metrics checks each of its four arrays before the call
+    full = [np.zeros(sh[n], order="F") for n in ("cells", "Ifaces", "Jfaces", "Kfaces")]
+    for bad in range(4):
+        args = list(full)
+        args[bad] = args[bad].ravel(order="F")[:-1]
+        with pytest.raises(ValueError):
+            h.set_metrics(*args)

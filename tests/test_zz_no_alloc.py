@@ -27,6 +27,8 @@ def test_noalloc_rejects_before_device_work():
     flow = abi.make_flow()
     assert _call_noalloc(L, abi.Extent(10, 8, 6, 8), flow, ptrs, out) == abi.FEST_ERR_SCRATCH
     assert _call_noalloc(L, abi.Extent(1, 8, 6, 5), flow, ptrs, out) == abi.FEST_ERR_ARG
+    for nv in (1, 4, 6):  # only the Euler/laminar and SST variable sets have scales here
+        assert _call_noalloc(L, abi.Extent(10, 8, 6, nv), flow, ptrs, out) == abi.FEST_ERR_ARG
     assert _call_noalloc(L, abi.Extent(10, 8, 6, 5), flow, [0] + ptrs[1:], out) == abi.FEST_ERR_ARG
 
 
