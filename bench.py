@@ -34,12 +34,17 @@ sys.path.insert(0, os.path.join(ROOT, "fest-3d_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 METRIC = "Mcell-residuals/s (mixed precision; FP64 and mixed-vs-FP64 wall-Cp error reported)"
-# algorithmic bytes per cell-residual of the mixed sweep, each array once at
-# its stored precision: stage 1 reads the FP32 stencil mirror (20 B), the
-# FP64 base state (40), FP32 I/J/K face records (48) and volume (4), writes
-# the FP64 state (40), its FP32 mirror (20) and dt (8) = 180 B; stages 2-3
-# also read U_store (40) and dt (8) but write no dt = 220 B
-BYTES_STAGE = (180.0, 220.0, 220.0)
+# algorithmic bytes per cell-residual of a fused mixed-precision stage, each
+# array once, the grid metrics at the precision the grid is stored in (FP64):
+# the FP32 stencil state (20 B), the FP64 state the update starts from (40),
+# one I, J and K face record {A,nx,ny,nz} (96) and the volume (8) in; the FP64
+# state (40) and its FP32 copy (20) out = 224 B in stage 1; stages 2-3 of
+# TVD-RK3 also read U_store (40) = 264 B.  (The sweep reads FP32 copies of
+# the metrics, 52 B fewer, and the time step, 8 B more; the FP64 figures are
+# the compulsory traffic of the method.)
+BYTES_STAGE = (224.0, 264.0, 264.0)
+# iterations of the bump configuration's mixed-vs-FP64 report (its stated count)
+C2_ITERS = 10000
 
 
 def parse():
@@ -66,7 +71,20 @@ def parse():
                          "stage for all blocks against a loop over the blocks' own steps")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the 1024x384x64-cell roofline measurement")
+    ap.add_argument("--c2-iters", type=int, default=C2_ITERS, metavar="ITERS",
+                    help="iterations of the mixed-vs-FP64 bump report (wall Cp, entropy, residual "
+                         "drop); 0 skips it")
     return ap.parse_args()
+
+
+def bench_config(case, ws):
+    """The config dict of both arms' lines: the workload and what the timed
+    region does between steps."""
+    ext = case["ext"]
+    N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
+    return {"workload": case["name"], "cells": N, "cell_residuals_per_step": 3 * N,
+            "l2": "GPU arm: flushed (256 MiB write) before every timed step; CPU arm: none",
+            "parallelism": "replicas" if ws > 1 else "single device"}
 
 
 def max_over_ranks(x, dist, device):
@@ -224,8 +242,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
             "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": case["name"], "cells": N, "cell_residuals_per_step": 3 * N,
-                       "parallelism": "cpu"},
+            "config": bench_config(case, ws),
             "cpu_baseline": {"value": v, "unit": "Mcell-residuals/s", "cores": threads, "kind": "port",
                              "sample": f"{steps} TVD-RK3 iterations of the full block (bounded to "
                                        f"{budget:.0f} s), C restatement of the reference path, "
@@ -304,6 +321,47 @@ def adjoint_cost(lib, reps=20):
                 "primal_residual_ms": tp * 1e3, "vjp_ms": ta * 1e3, "adjoint_over_primal": ta / tp,
                 "timing": "wall clock per C-ABI call incl. host transfers, mean of %d" % reps}
     except Exception as e:
+        return {"error": str(e)}
+
+
+def c2_report(lib, abi, cases, Handle, iters):
+    """The bump configuration's own report after `iters` iterations from the
+    uniform start, FP64 and mixed precision: continuity-residual drop
+    (last/first iteration), relative entropy change (SmoothBump/pp/entropy.py),
+    the mixed-vs-FP64 differences of wall Cp and of the entropy field, and
+    each run's wall time (fest_step through the C ABI, state on the device)."""
+    import numpy as np
+    from fest3d import post
+    try:
+        case = cases.bump_case()
+        ext, flow, CFL = case["ext"], case["flow"], case["CFL"]
+        out = {"iters": iters, "workload": case["name"]}
+        q = {}
+        for prec, name in ((abi.FEST_FP64, "fp64"), (abi.FEST_MIXED, "mixed")):
+            h = Handle(ext, flow, case["scheme"], case["bc"], lib=lib)
+            h.setup_geometry(case["nodes"])
+            h.upload_state(case["qp"])
+            h.set_precision(prec)
+            t0 = time.perf_counter()
+            n1 = h.step(1, 1, CFL)
+            nN = h.step(iters - 1, 2, CFL)
+            t = time.perf_counter() - t0
+            q[name] = post.interior(h.download_state(), ext)
+            vol = post.interior(h.get("cells")[0], ext)
+            out[name] = {"seconds": t, "l2_drop_continuity": float(nN[1] / n1[1]),
+                         "resnorm_first": [float(x) for x in n1], "resnorm_last": [float(x) for x in nN],
+                         "entropy_change": post.entropy_change(q[name], vol, flow.pressure_inf,
+                                                               flow.density_inf)}
+            h.close()
+        cp = {n: (q[n][:, 0, 0, 4] - flow.pressure_inf) / (0.5 * flow.density_inf * flow.vel_mag ** 2)
+              for n in q}
+        ef = {n: post.entropy_field(q[n], flow.pressure_inf, flow.density_inf) for n in q}
+        out["wall_cp_abs_err_mixed_vs_fp64"] = float(np.abs(cp["mixed"] - cp["fp64"]).max())
+        out["entropy_field_abs_err_mixed_vs_fp64"] = float(np.abs(ef["mixed"] - ef["fp64"]).max())
+        out["entropy_field_max_abs_fp64"] = float(np.abs(ef["fp64"]).max())
+        out["fp64_over_mixed_time"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+        return out
+    except Exception as e:  # report, do not lose the main line
         return {"error": str(e)}
 
 
@@ -397,9 +455,14 @@ def run_ours(args):
     nl, tot = C.c_longlong(), C.c_double()
     abi.check(lib.fest_profile_read(h.h, C.byref(nl), C.byref(tot)), "profile_read")
     abi.check(lib.fest_profile(h.h, 0), "profile off")
-    avg_s = tot.value / 1e3 / max(nl.value, 1)
+    iso_s = tot.value / 1e3 / max(nl.value, 1)  # event pair around each launch, no graph
     bytes_launch = N * sum(BYTES_STAGE) / len(BYTES_STAGE)
-    achieved = bytes_launch / avg_s / 1e9
+    # in-step duration: the timed region's time per step over its sweep
+    # launches (graph replay; a mixed bump step after iteration 2 launches
+    # the three stage sweeps and nothing else)
+    per_step = mixed["launches"] / max(mixed["steps"], 1)
+    step_launch_s = mixed["ms"] / mixed["steps"] / 1e3 / max(per_step, 1)
+    achieved = bytes_launch / step_launch_s / 1e9
     peak, peak_kind = measured_peak()
     tr = committed_traffic()
     traffic = tr.get("bytes_per_launch") if tr else None
@@ -447,6 +510,7 @@ def run_ours(args):
     nbytes = int(qhost.nbytes)
 
     adj = adjoint_cost(lib) if rank == 0 else None
+    c2 = c2_report(lib, abi, cases, Handle, args.c2_iters) if rank == 0 and args.c2_iters > 1 else None
 
     cpu = None
     if rank == 0 and ws == 1:
@@ -464,9 +528,7 @@ def run_ours(args):
             "ms_per_step": mixed["ms"] / mixed["steps"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 stencil / f64 state",
             "data": "synthetic (analytic bump grid, uniform Mach 0.5 start)",
-            "config": {"workload": case["name"], "cells": N, "cell_residuals_per_step": STAGES * N,
-                       "l2": "flushed (256 MiB write) before every timed step",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": bench_config(case, ws),
             "fp64": {"value": rate(fp64), "unit": "Mcell-residuals/s", "steps": fp64["steps"],
                      "ms_per_step": fp64["ms"] / fp64["steps"]},
             "mixed_over_fp64": rate(mixed) / rate(fp64),
@@ -474,9 +536,15 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_stage<float> (fused WENO5+SLAU sweep + update)",
-                         "peak_source": peak_kind, "launches_timed": int(nl.value),
-                         "avg_launch_us": avg_s * 1e6, "bytes_per_launch": bytes_launch},
+                         "peak_source": peak_kind, "launches_per_step": per_step,
+                         "avg_launch_us": step_launch_s * 1e6,
+                         "duration": "timed region's ms_per_step / sweep launches per step (graph "
+                                     "replay, inter-launch gaps included)",
+                         "isolated_launch_us": iso_s * 1e6, "isolated_launches": int(nl.value),
+                         "bytes_per_cell_residual": list(BYTES_STAGE),
+                         "bytes_per_launch": bytes_launch},
             "roofline_large_block": large,
+            "bump_report": c2,
             "adjoint": adj,
             "clocks": mixed["clocks"],
             "e2e": {"value": e2e_rate, "unit": "Mcell-residuals/s", "h2d_bytes_per_step": nbytes,

@@ -146,7 +146,7 @@ def restart_states(case_dir, grids):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case_dir", nargs="?", default="/root/reference/tests/Lfp")
+    ap.add_argument("case_dir", help="the reference's Lfp or Tfp case directory")
     ap.add_argument("--converge", type=int, default=60000, metavar="N")
     ap.add_argument("--turbulent", action="store_true")
     ap.add_argument("--restart", action="store_true",

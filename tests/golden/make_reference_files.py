@@ -58,7 +58,7 @@ def parse_tecplot(path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("tests_dir", nargs="?", default="/root/reference/tests")
+    ap.add_argument("tests_dir", help="the reference's tests directory")
     a = ap.parse_args()
     out = {}
     for key, (rel, t) in TEC.items():

@@ -55,7 +55,7 @@ def smoothbump_case(nodes_ijk):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case_dir", nargs="?", default="/root/reference/tests/SmoothBump")
+    ap.add_argument("case_dir", help="the reference's SmoothBump case directory")
     ap.add_argument("--converge", type=int, default=0, metavar="N")
     args = ap.parse_args()
     g = os.path.join(args.case_dir, "system", "mesh", "gridfiles")

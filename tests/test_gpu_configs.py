@@ -1,0 +1,93 @@
+"""Parity at the benchmark configurations' own sizes, on the GPU, against the
+oracle on the same inputs.
+
+* Smooth bump, 256x96x4 cells, WENO5 + SLAU, TVD-RK3, CFL 0.8 (the workload
+  bench.py times, built by the same function): FP64 through the fused sweep,
+  three iterations, residual of the last stage within 1e-12 flux-scaled
+  (and in global L2) and the interior state within 1e-11 of each variable's
+  magnitude; mixed precision, twenty iterations, interior state within 2e-5.
+* Lid-driven cavity, 64x64x4 cells, MUSCL (van Albada) + AUSM, laminar,
+  forward Euler, CFL 0.5: all 2000 iterations of the configuration,
+  field-wise (every interior cell, every variable) against the oracle's
+  2000 iterations, FP64 within 1e-9 and mixed precision within 2e-5 of
+  each variable's magnitude.  The cavity starts at rest, so its velocities
+  are judged against the lid speed."""
+import numpy as np
+import pytest
+
+import oracle as O
+from fest3d import abi, cases, post
+from parity import assert_residual, make_pair
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_run(blk, first, n, CFL):
+    for it in range(first, first + n):
+        assert O.get_next_solution([blk], it, CFL) == 0
+
+
+def _field_err(q, ref, ext, scale=None):
+    """max over variables of max|q - ref| / scale_l over interior cells
+    (scale_l: max|ref_l| unless given)."""
+    a, b = post.interior(q, ext), post.interior(ref, ext)
+    errs = []
+    for l in range(ext.n_var):
+        s = scale[l] if scale is not None else np.abs(b[..., l]).max()
+        errs.append(np.abs(a[..., l] - b[..., l]).max() / s)
+    return max(errs), errs
+
+
+def test_bump_256x96x4_fp64_residual_and_state(gpu_lib):
+    case = cases.bump_case()
+    ext = case["ext"]
+    blk, h = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    h.set_precision(abi.FEST_FP64)
+    h.step(3, 1, case["CFL"])
+    q = h.download_state()
+    res = h.get("residue")  # the last stage's residual, kept by the fused sweep
+    _oracle_run(blk, 1, 3, case["CFL"])
+    assert_residual(res, blk, rtol=1e-12, what="bump 256x96x4 FP64 residual, iteration 3 stage 3")
+    e, errs = _field_err(q, blk["qp"], ext)
+    assert e <= 1e-11, f"bump FP64 interior state after 3 iterations differs by {errs}"
+    h.close()
+
+
+def test_bump_256x96x4_mixed_twenty_iterations(gpu_lib):
+    case = cases.bump_case()
+    ext = case["ext"]
+    blk, h = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    h.set_precision(abi.FEST_MIXED)
+    norm = h.step(20, 1, case["CFL"])
+    q = h.download_state()
+    _oracle_run(blk, 1, 20, case["CFL"])
+    # the flow has left the uniform start: compare the departure from it too
+    dep = np.abs(post.interior(blk["qp"], ext)[..., 4] - case["flow"].pressure_inf).max()
+    assert dep > 10.0, dep
+    e, errs = _field_err(q, blk["qp"], ext)
+    assert e <= 2e-5, f"bump mixed interior state after 20 iterations differs by {errs}"
+    ref = O.find_resnorm([blk])
+    assert np.allclose(norm[1:], ref[1:], rtol=2e-2), (norm, ref)
+    h.close()
+
+
+@pytest.mark.parametrize("precision", [abi.FEST_FP64, abi.FEST_MIXED], ids=["fp64", "mixed"])
+def test_cavity_64x64x4_all_2000_iterations(gpu_lib, precision):
+    case = cases.ldc_case()
+    ext = case["ext"]
+    iters = 2000
+    blk, h = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    h.set_precision(precision)
+    h.step(iters, 1, case["CFL"], with_norm=False)
+    q = h.download_state()
+    _oracle_run(blk, 1, iters, case["CFL"])
+    ref = blk["qp"]
+    lid = 34.7
+    rho_s, p_s = np.abs(post.interior(ref, ext)[..., 0]).max(), np.abs(post.interior(ref, ext)[..., 4]).max()
+    scale = [rho_s, lid, lid, lid, p_s]
+    # the lid has set the cavity in motion
+    assert np.abs(post.interior(ref, ext)[..., 1]).max() > 0.05 * lid
+    tol = 1e-9 if precision == abi.FEST_FP64 else 2e-5
+    e, errs = _field_err(q, ref, ext, scale)
+    assert e <= tol, f"cavity after {iters} iterations differs by {errs} (tolerance {tol})"
+    h.close()
