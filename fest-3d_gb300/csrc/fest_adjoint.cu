@@ -505,10 +505,13 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_ghosts(Params p, DevBlock b, do
     default:
       if (id == -10 || id >= 0) {  // ghost L <- layer L of the partner face (same block)
         const int pf = p.part_face[f];
+        int na, nb, pa, pb;
+        face_columns(d, f, na, nb);
+        interface_map(p.part_orient[f], na, nb, ta, tb, pa, pb);
         for (int l = 0; l < 5; ++l)
           for (int L = 1; L <= 3; ++L) {
             const double g = take(L, l);
-            if (g != 0.0) atomicAdd(bar + icell_p(d, pf, L, ta, tb) + P * l, g);
+            if (g != 0.0) atomicAdd(bar + icell_p(d, pf, L, pa, pb) + P * l, g);
           }
       } else {
         for (int l = 0; l < 5; ++l) none(l);

@@ -145,11 +145,15 @@ void fill_params(fest_handle* h) {
   // ppm_flag (boundary_state_reconstruction.f90:45-47)
   p.ppm_flag = (s.interpolant == FEST_INTERP_PPM || s.interpolant == FEST_INTERP_WENO ||
                 s.interpolant == FEST_INTERP_WENO_NM);
+  p.self_block = 0;
   for (int i = 0; i < 6; ++i) {
     p.id[i] = b.id[i];
     if (b.id[i] == -7) p.ppm_flag = 1;
-    p.part_block[i] = b.partner_block[i];
+    // a pair with this same block resolves to entry 0 of the handle's own
+    // block table; pairs with other blocks resolve inside a batch
+    p.part_block[i] = b.partner_block[i] == b.block_id ? 0 : -1;
     p.part_face[i] = b.partner_face[i];
+    p.part_orient[i] = b.partner_orient[i];
     p.fix_rho[i] = b.fixed_density[i]; p.fix_p[i] = b.fixed_pressure[i];
     p.fix_u[i] = b.fixed_x_speed[i]; p.fix_v[i] = b.fixed_y_speed[i]; p.fix_w[i] = b.fixed_z_speed[i];
     p.fix_tk[i] = b.fixed_tk[i]; p.fix_tw[i] = b.fixed_tw[i];
@@ -212,6 +216,14 @@ long long arr_size(const fest_handle* h, int which) {
     case FEST_ARR_DELTA_T: return z.dt;
     default: return 0;
   }
+}
+
+// a handle whose interface faces pair with other blocks fills its ghosts
+// only inside a batch (fest_batch_create resolves the partners)
+bool needs_batch(const fest_handle* h) {
+  for (int f = 0; f < 6; ++f)
+    if ((h->p.id[f] == -10 || h->p.id[f] >= 0) && h->p.part_block[f] < 0) return true;
+  return false;
 }
 
 // the fused path may hold the current state in one of its own buffers:
@@ -322,16 +334,20 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
   for (int f = 0; f < 6; ++f) {
     if (!valid_id(bc->id[f])) return FEST_ERR_ARG;
     if (bc->id[f] == -10 || bc->id[f] >= 0) {
-      if (bc->partner_block[f] != 0 || bc->partner_face[f] < 0 || bc->partner_face[f] > 5)
+      if (bc->partner_block[f] < 0 || bc->partner_face[f] < 0 || bc->partner_face[f] > 5 ||
+          bc->partner_orient[f] < 0 || bc->partner_orient[f] > 7)
         return FEST_ERR_ARG;
+      // the exchange copies interior layers 1..3 of the partner face
+      int n = f / 2 == 0 ? dims->imx : f / 2 == 1 ? dims->jmx : dims->kmx;
+      if (n - 1 < 3) return FEST_ERR_ARG;
+      if (bc->partner_block[f] != bc->block_id) continue;  // another block: checked by the batch
       int pf = bc->partner_face[f];
       int na = (f / 2 == 0 ? dims->jmx : dims->imx), nb = (f / 2 == 2 ? dims->jmx : dims->kmx);
       int pa = (pf / 2 == 0 ? dims->jmx : dims->imx), pb = (pf / 2 == 2 ? dims->jmx : dims->kmx);
+      if (bc->partner_orient[f] & 4) std::swap(pa, pb);
       if (na != pa || nb != pb) return FEST_ERR_ARG;
-      // the exchange copies interior layers 1..3 of the partner face
-      int n = f / 2 == 0 ? dims->imx : f / 2 == 1 ? dims->jmx : dims->kmx;
       int pn = pf / 2 == 0 ? dims->imx : pf / 2 == 1 ? dims->jmx : dims->kmx;
-      if (n - 1 < 3 || pn - 1 < 3) return FEST_ERR_ARG;
+      if (pn - 1 < 3) return FEST_ERR_ARG;
     }
   }
   int ndev = 0;
@@ -525,7 +541,7 @@ int fest_download_state(fest_handle* h, double* qp) {
 }
 
 int fest_populate_ghost_primitive(fest_handle* h, double* qp, int current_iter) {
-  if (!h) return FEST_ERR_ARG;
+  if (!h || needs_batch(h)) return FEST_ERR_ARG;
   RET(sync_fused(h));
   long long n = h->p.d.P * h->p.d.nv;
   RET(up(h, h->d.qp, qp, n));
@@ -656,7 +672,7 @@ int fest_compute_time_step(fest_handle* h, const double* qp, double CFL, double*
 
 int fest_get_total_conservative_residue(fest_handle* h, double* qp, int current_iter,
                                         double* residue) {
-  if (!h) return FEST_ERR_ARG;
+  if (!h || needs_batch(h)) return FEST_ERR_ARG;
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
@@ -680,7 +696,7 @@ static int viscous_prep(fest_handle* h) {
 int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const double* lambda,
                       double* dq) {
   if (!h || !lambda || !dq) return FEST_ERR_ARG;
-  if (!vjp_supported(h->p)) return FEST_ERR_ARG;
+  if (!vjp_supported(h->p) || needs_batch(h)) return FEST_ERR_ARG;
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
@@ -697,7 +713,7 @@ int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const 
 int fest_residual_vjp_nodes(fest_handle* h, const double* qp, int current_iter, const double* lambda,
                             const double* Ifaces_bar, const double* Jfaces_bar,
                             const double* Kfaces_bar, double* dq, double* dnodes) {
-  if (!h || !dnodes) return FEST_ERR_ARG;
+  if (!h || !dnodes || needs_batch(h)) return FEST_ERR_ARG;
   // metric adjoints of the inviscid residual only
   if (!vjp_supported(h->p) || h->p.interp == FEST_INTERP_WENO_NM || h->p.mu_ref != 0.0) return FEST_ERR_ARG;
   RET(sync_fused(h));
@@ -734,7 +750,7 @@ int fest_residual_vjp_nodes(fest_handle* h, const double* qp, int current_iter, 
 int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_iters, double tol,
                        double* psi, int* n_done, double* drop) {
   if (!h || !dJdq || max_iters < 0) return FEST_ERR_ARG;
-  if (!vjp_supported(h->p) || h->p.tstep != 'l') return FEST_ERR_ARG;
+  if (!vjp_supported(h->p) || h->p.tstep != 'l' || needs_batch(h)) return FEST_ERR_ARG;
   if (h->p.integ != FEST_TIME_NONE && h->p.integ != FEST_TIME_TVDRK3) return FEST_ERR_ARG;
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
@@ -795,7 +811,7 @@ int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_i
 
 int fest_get_next_solution(fest_handle* h, double* qp, int current_iter, double CFL,
                            double* residue, double* delta_t) {
-  if (!h) return FEST_ERR_ARG;
+  if (!h || needs_batch(h)) return FEST_ERR_ARG;
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
@@ -828,7 +844,7 @@ int fest_find_resnorm(fest_handle* h, double* res_abs) {
 }
 
 static int step_enqueue(fest_handle* h, int n_iters, int first_iter, double CFL) {
-  if (!h || n_iters < 0) return FEST_ERR_ARG;
+  if (!h || n_iters < 0 || needs_batch(h)) return FEST_ERR_ARG;
   if (fused_supported(h->p, h->precision)) {
     if (!h->fused) RET(fused_create(h->p, h->d, h->d_table, h->s, &h->fused));
     return fused_run(h->fused, h->p, h->d, h->precision, n_iters, first_iter, CFL, h->s,
@@ -861,12 +877,45 @@ int fest_batch_create(fest_handle* const* blocks, int n_blocks, fest_batch** out
   *out = nullptr;
   if (!blocks || n_blocks < 1) return FEST_ERR_ARG;
   fest_handle* h0 = blocks[0];
+  if (!h0) return FEST_ERR_ARG;
+  const int prec = h0->precision;
   for (int n = 0; n < n_blocks; ++n) {
     fest_handle* h = blocks[n];
-    if (!h || h->precision != FEST_MIXED || !fused_supported(h->p, FEST_MIXED)) return FEST_ERR_ARG;
+    if (!h || h->precision != prec || !fused_supported(h->p, prec)) return FEST_ERR_ARG;
+  }
+  // interface partners as batch indices: the block itself, or the one
+  // other handle whose block_id is the face's partner_block
+  std::vector<Params> p(n_blocks);
+  for (int n = 0; n < n_blocks; ++n) {
+    const fest_handle* h = blocks[n];
+    p[n] = h->p;
+    p[n].self_block = n;
+    for (int f = 0; f < 6; ++f) {
+      if (!(h->bc.id[f] == -10 || h->bc.id[f] >= 0)) continue;
+      const int pb = h->bc.partner_block[f];
+      if (pb == h->bc.block_id) {
+        p[n].part_block[f] = n;
+        continue;
+      }
+      int m = -1;
+      for (int k = 0; k < n_blocks; ++k)
+        if (k != n && blocks[k]->bc.block_id == pb) {
+          if (m >= 0) return FEST_ERR_ARG;  // two blocks with that number
+          m = k;
+        }
+      if (m < 0) return FEST_ERR_ARG;
+      // the partner face has this face's columns (swapped with dir_switch)
+      // and the three interior layers the exchange copies
+      int na, nb, pa, pc;
+      face_columns(h->p.d, f, na, nb);
+      const int pf = h->bc.partner_face[f];
+      face_columns(blocks[m]->p.d, pf, pa, pc);
+      if (h->bc.partner_orient[f] & 4) std::swap(pa, pc);
+      if (na != pa || nb != pc || extent_of(blocks[m]->p.d, pf / 2) - 1 < 3) return FEST_ERR_ARG;
+      p[n].part_block[f] = m;
+    }
   }
   std::vector<FusedState*> f;
-  std::vector<Params> p;
   std::vector<DevBlock> d;
   fest_batch* b = new fest_batch();
   int rc = FEST_OK;
@@ -879,10 +928,9 @@ int fest_batch_create(fest_handle* const* blocks, int n_blocks, fest_batch** out
     h->s = h0->s;
     if (!rc && !h->fused) rc = fused_create(h->p, h->d, h->d_table, h->s, &h->fused);
     f.push_back(h->fused);
-    p.push_back(h->p);
     d.push_back(h->d);
   }
-  if (!rc) rc = fused_batch_create(f, p, d, &b->fb);
+  if (!rc) rc = fused_batch_create(f, p, d, prec, &b->fb);
   if (rc) {
     fest_batch_destroy(b);
     return rc;
@@ -904,7 +952,7 @@ int fest_batch_step_async(fest_batch* b, int n_iters, int first_iter, double CFL
   if (!b || n_iters < 0) return FEST_ERR_ARG;
   fest_handle* h0 = b->h[0];
   for (fest_handle* h : b->h)
-    if (h->s != h0->s || h->precision != FEST_MIXED) return FEST_ERR_ARG;
+    if (h->s != h0->s || h->precision != h0->precision) return FEST_ERR_ARG;
   return fused_batch_run(b->fb, n_iters, first_iter, CFL, h0->s, &h0->launches);
 }
 
@@ -922,7 +970,7 @@ int fest_set_stream(fest_handle* h, void* stream) {
 }
 
 int fest_profile(fest_handle* h, int enable) {
-  if (!h) return FEST_ERR_ARG;
+  if (!h || needs_batch(h)) return FEST_ERR_ARG;
   if (!h->fused && fused_supported(h->p, h->precision))
     RET(fused_create(h->p, h->d, h->d_table, h->s, &h->fused));
   fused_profile(h->fused, enable != 0);

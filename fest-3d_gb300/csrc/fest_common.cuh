@@ -27,7 +27,12 @@ struct Params {
   int integ;   // schemetype%time_step_accuracy (FEST_TIME_*)
   int lam[3], tlim[3], pb[3];
   int id[6];
-  int part_block[6], part_face[6];
+  // interface partners: block (index into the ghost fill's block table,
+  // -1 while unresolved), face, orientation (bit 0/1: first/second
+  // tangential direction reversed, bit 2: swapped); self_block: this
+  // block's own index in that table
+  int part_block[6], part_face[6], part_orient[6];
+  int self_block;
   double c1, c2, c3;
   double fix_rho[6], fix_p[6], fix_u[6], fix_v[6], fix_w[6], fix_tk[6], fix_tw[6];
   double Tw[6], Tp[6];
@@ -109,6 +114,24 @@ __host__ __device__ __forceinline__ int extent_of(const Dims& d, int dir) {
 }
 __host__ __device__ __forceinline__ long long pstride(const Dims& d, int dir) {
   return dir == 0 ? 1 : dir == 1 ? (long long)d.ni : (long long)d.ni * d.nj;
+}
+
+// Tangential position (pa, pb) on the partner face of ghost column (ta, tb)
+// of an interface face with na x nb interior columns: the receive loops of
+// apply_interface (interface1.f90:96-464) over the index ranges of
+// change_map_to_particular_range (mapping.f90:159-236).  orient bit 0/1
+// reverses the first/second tangential direction, bit 2 swaps them.
+__host__ __device__ __forceinline__ void interface_map(int orient, int na, int nb, int ta, int tb, int& pa,
+                                                       int& pb) {
+  const int a = (orient & 1) ? na - ta : ta - 1;
+  const int b = (orient & 2) ? nb - tb : tb - 1;
+  if (orient & 4) { pa = 1 + b; pb = 1 + a; }
+  else { pa = 1 + a; pb = 1 + b; }
+}
+// interior columns of face f (its two tangential extents)
+__host__ __device__ __forceinline__ void face_columns(const Dims& d, int f, int& na, int& nb) {
+  na = (f / 2 == 0 ? d.jmx : d.imx) - 1;
+  nb = (f / 2 == 2 ? d.jmx : d.kmx) - 1;
 }
 
 // ---- Fortran intrinsics with the reference's semantics ----------------------
@@ -212,6 +235,62 @@ __device__ __forceinline__ void weno_cell(const Lq& q, int c, T& Rm, T& Lp) {
   P2 = dvc((T(2) * u0 + T(5) * um1 - T(1) * um2), T(6));
   w0 = dv(g0, (e2 * e2)); w1 = dv(g1, (e1 * e1)); w2 = dv(g2, (e0 * e0));
   Rm = dv((w0 * P0 + w1 * P1 + w2 * P2), (w0 + w1 + w2));
+}
+
+// ---- packed FP32 pairs -------------------------------------------------------
+// Blackwell executes two FP32 adds, multiplies or FMAs in one instruction
+// (FADD2/FMUL2/FFMA2 on float2): the FP32 sweep reconstructs two variables
+// per instruction stream.  Same rounding per element as the scalar forms.
+__device__ __forceinline__ float2 pk(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 prcp(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
+
+// WENO5-JS (weno.f90:59-87) of two variables at once: qa, qb are their
+// lines.  The weights' reciprocals 1/(eps+B_k)^2 serve both faces, and the
+// 1/6 of the candidate-stencil estimates moves into the normalisation.
+template <class Lq>
+__device__ __forceinline__ void weno_pair(const Lq& qa, const Lq& qb, int c, float2& Rm, float2& Lp) {
+  const float2 um2 = make_float2(qa(c - 2), qb(c - 2)), um1 = make_float2(qa(c - 1), qb(c - 1)),
+               u0 = make_float2(qa(c), qb(c)), up1 = make_float2(qa(c + 1), qb(c + 1)),
+               up2 = make_float2(qa(c + 2), qb(c + 2));
+  const float2 k1312 = pk(13.0f / 12.0f), k14 = pk(0.25f), eps = pk(1e-6f);
+  float2 t1, t2;
+  t1 = padd(psub(um2, padd(um1, um1)), u0);
+  t2 = pfma(pk(3.0f), u0, pfma(pk(-4.0f), um1, um2));
+  const float2 B0 = pfma(k1312, pmul(t1, t1), pmul(k14, pmul(t2, t2)));
+  t1 = padd(psub(um1, padd(u0, u0)), up1);
+  t2 = psub(um1, up1);
+  const float2 B1 = pfma(k1312, pmul(t1, t1), pmul(k14, pmul(t2, t2)));
+  t1 = padd(psub(u0, padd(up1, up1)), up2);
+  t2 = padd(pfma(pk(-4.0f), up1, pmul(pk(3.0f), u0)), up2);
+  const float2 B2 = pfma(k1312, pmul(t1, t1), pmul(k14, pmul(t2, t2)));
+  float2 e = padd(eps, B0);
+  const float2 r0 = prcp(pmul(e, e));
+  e = padd(eps, B1);
+  const float2 r1 = prcp(pmul(e, e));
+  e = padd(eps, B2);
+  const float2 r2 = prcp(pmul(e, e));
+  const float2 w1 = pmul(pk(0.6f), r1);
+  // high face: linear weights 0.1, 0.6, 0.3 on stencils (c-2..c), (c-1..c+1), (c..c+2)
+  float2 w0 = pmul(pk(0.1f), r0), w2 = pmul(pk(0.3f), r2);
+  float2 P0 = pfma(pk(11.0f), u0, pfma(pk(-7.0f), um1, padd(um2, um2)));
+  float2 P1 = psub(pfma(pk(2.0f), up1, pmul(pk(5.0f), u0)), um1);
+  float2 P2 = psub(pfma(pk(5.0f), up1, padd(u0, u0)), up2);
+  float2 num = pfma(w2, P2, pfma(w1, P1, pmul(w0, P0)));
+  float2 den = pmul(pk(6.0f), padd(padd(w0, w1), w2));
+  Lp = pmul(num, prcp(den));
+  // low face: the mirrored stencils, weights 0.1 on (c..c+2), 0.3 on (c-2..c)
+  w0 = pmul(pk(0.1f), r2);
+  w2 = pmul(pk(0.3f), r0);
+  P0 = pfma(pk(11.0f), u0, pfma(pk(-7.0f), up1, padd(up2, up2)));
+  P1 = psub(pfma(pk(2.0f), um1, pmul(pk(5.0f), u0)), up1);
+  P2 = psub(pfma(pk(5.0f), um1, padd(u0, u0)), um2);
+  num = pfma(w2, P2, pfma(w1, P1, pmul(w0, P0)));
+  den = pmul(pk(6.0f), padd(padd(w0, w1), w2));
+  Rm = pmul(num, prcp(den));
 }
 
 // WENO on non-uniform cells (weno_NM.f90:82-116); v(c) are cell volumes

@@ -130,10 +130,13 @@ __device__ __forceinline__ float riemann_mirror(const Params& p, const Mirror& M
   return riemann_ghost_f32(p, f, fc, I(1, 1), I(1, 2), I(1, 3), I(1, 4), I(1, 0), rg, ug, vg, wg, pg);
 }
 
-// dist: the FP64 wall distance (padded), read by the SST wall's omega
+// dist: the FP64 wall distance (padded), read by the SST wall's omega;
+// PM, pd: the mirror and extents of the block an interface face pairs with
+// (this block's own for a face paired with the block itself)
 __device__ __forceinline__ void ghost_mirror_column(const Params& p, const Mirror& M, int f, int ta, int tb,
                                                     const float4* F0, const float4* F1,
-                                                    const float4* F2, const double* dist) {
+                                                    const float4* F2, const double* dist, const Mirror& PM,
+                                                    const Dims& pd) {
   const Dims& d = p.d;
   const int id = p.id[f];
   const bool sst = d.nv == 7;
@@ -230,28 +233,41 @@ __device__ __forceinline__ void ghost_mirror_column(const Params& p, const Mirro
       }
     } break;
     default:
-      if (id == -10 || id >= 0) {  // interface of a single block: ghost L <- partner layer L
+      if (id == -10 || id >= 0) {  // interface: ghost L <- layer L of the partner face
         const int pf = p.part_face[f];
+        int na, nb, pa, pb;
+        face_columns(d, f, na, nb);
+        interface_map(p.part_orient[f], na, nb, ta, tb, pa, pb);
         for (int l = 0; l < d.nv; ++l)
           for (int L = 1; L <= 3; ++L) {
             int i, j, k;
-            icell(d, pf, L, ta, tb, i, j, k);
-            G(L, l) = M.at(i, j, k, l);
+            icell(pd, pf, L, pa, pb, i, j, k);
+            G(L, l) = PM.at(i, j, k, l);
           }
       }
   }
 }
 
+// tab: the block table of the stage's input buffer (interface partners in
+// other blocks of a batch, read through their FP32 mirrors)
 __global__ void __launch_bounds__(128) k_ghosts_mirror(Params p, Mirror M, GhostPlan plan,
                                                        const float4* F0, const float4* F1,
-                                                       const float4* F2, const double* dist) {
+                                                       const float4* F2, const double* dist,
+                                                       const BlockRef* tab) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= plan.start[plan.nf]) return;
   int n = 0;
   while (t >= plan.start[n + 1]) ++n;
   const long long u = t - plan.start[n];
-  ghost_mirror_column(p, M, plan.face[n], 1 + (int)(u % plan.na[n]), 1 + (int)(u / plan.na[n]), F0, F1, F2,
-                      dist);
+  const int f = plan.face[n];
+  Mirror PM = M;
+  Dims pd = p.d;
+  if ((p.id[f] == -10 || p.id[f] >= 0) && p.part_block[f] != p.self_block) {
+    const BlockRef& r = tab[p.part_block[f]];
+    PM = Mirror{r.b.qp32, r.b.qp32_pitch, r.d.nj, r.d.nk, (long long)r.b.qp32_pitch * r.d.nj * r.d.nk};
+    pd = r.d;
+  }
+  ghost_mirror_column(p, M, f, 1 + (int)(u % plan.na[n]), 1 + (int)(u / plan.na[n]), F0, F1, F2, dist, PM, pd);
 }
 
 // one (block, face) segment of a batched mirror ghost fill
@@ -261,6 +277,8 @@ struct GhostSeg {
   Mirror M;
   const float4* F[3];
   const double* dist;
+  Mirror PM;        // the interface partner's mirror (interface faces)
+  Dims pd;          // and its extents
 };
 __global__ void __launch_bounds__(128) k_ghosts_mirror_batch(const Params* ps, const GhostSeg* seg, int nseg,
                                                              long long total) {
@@ -275,7 +293,7 @@ __global__ void __launch_bounds__(128) k_ghosts_mirror_batch(const Params* ps, c
   const GhostSeg& g = seg[lo];
   const long long u = t - g.start;
   ghost_mirror_column(ps[g.block], g.M, g.face, 1 + (int)(u % g.na), 1 + (int)(u / g.na), g.F[0], g.F[1],
-                      g.F[2], g.dist);
+                      g.F[2], g.dist, g.PM, g.pd);
 }
 
 // copy ghost layers 1-3 of face f (interior columns, every variable) from
@@ -384,7 +402,9 @@ static int ring_faces(const Params& p, int* kper) {
       case -2: case -3: case -4: case -5: case -6: case -7: m |= 1 << f; break;
       case -8: case -11: if (!sst) m |= 1 << f; break;
       default:
-        if ((id == -10 || id >= 0) && f / 2 == 2 && p.part_face[4] == 5 && p.part_face[5] == 4)
+        if ((id == -10 || id >= 0) && f / 2 == 2 && p.part_face[4] == 5 && p.part_face[5] == 4 &&
+            p.part_block[4] == p.self_block && p.part_block[5] == p.self_block && p.part_orient[4] == 0 &&
+            p.part_orient[5] == 0)
           *kper |= 1 << (f - 4);
     }
   }
@@ -665,9 +685,12 @@ static StageArgs stage_args(FusedState* f, const DevBlock& b, bool mixed, int in
   return a;
 }
 
+// tabs[n]: the block table (this block and its interface partners, each
+// with its buffer n) the ghost fill of a stage reading buffer n uses
 static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int prec, int in, int out,
                   int base, double bA, double bB, double TF, double SF, int TU, int use_rn,
-                  int compute_dt, double CFL, int iter, bool last, cudaStream_t s, long long* cnt) {
+                  int compute_dt, double CFL, int iter, bool last, BlockRef* const* tabs, cudaStream_t s,
+                  long long* cnt) {
   const bool mixed = prec == FEST_MIXED;
   DevBlock bb = b;
   bb.qp = f->Q[in];
@@ -700,14 +723,14 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
       const long long work = plan.start[plan.nf];
       if (work > 0) {
         k_ghosts_mirror<<<(unsigned)((work + 127) / 128), 128, 0, s>>>(p, M, plan, f->F32[0], f->F32[1],
-                                                                         f->F32[2], b.dist);
+                                                                         f->F32[2], b.dist, tabs[in]);
         ++*cnt;
       }
     }
   } else {
     // edge/corner ghosts are never read by an interior update: no averaging
     // (order-dependent blocks are thin, so the faces run one by one)
-    launch_ghosts(p, bb, f->table[in], iter, L, false);
+    launch_ghosts(p, bb, tabs[in], iter, L, false);
   }
   // order-dependent directions: the next fill's low face reads this fill's
   // high-face ghosts, in whichever buffer serves as its input
@@ -795,16 +818,23 @@ static int schedule(int integ, int U, bool lastit, StageSpec* st, int* next_cur,
   }
 }
 
-// one iteration of the integrator on the stream
-static int enqueue_iteration(FusedState* f, const Params& p, const DevBlock& b, int prec, int it,
-                             bool lastit, double CFL, cudaStream_t s, long long* cnt) {
+// One iteration of the integrator on the stream, in three parts so that
+// the blocks of a batch can advance stage by stage together (their ghost
+// fills read each other's stage inputs): iter_begin (schedule, fix()
+// ghosts of the early iterations, TVD snapshot, accumulator reset), the
+// stages (run_stage), iter_end (buffer rotation, TVD ghost blends).
+struct IterPlan {
+  StageSpec st[4];
+  int ns = 0, next = 0;
+  bool tvd_early = false;
+};
+static int iter_begin(FusedState* f, const Params& p, const DevBlock& b, int prec, int it, bool lastit,
+                      BlockRef* const* tabs, cudaStream_t s, long long* cnt, IterPlan& ip) {
   const bool mixed = prec == FEST_MIXED;
   const int U = f->cur;
-  StageSpec st[4];
-  int next = U;
   bool zero_rn = false;
-  const int ns = schedule(p.integ, U, lastit, st, &next, &zero_rn);
-  if (ns == 0) return FEST_ERR_ARG;
+  ip.ns = schedule(p.integ, U, lastit, ip.st, &ip.next, &zero_rn);
+  if (ip.ns == 0) return FEST_ERR_ARG;
   if (it <= 2) {
     // fix() ghosts are written only while current_iter <= 2
     // (bc_primitive.f90:236,318,366) and persist afterwards: every
@@ -815,21 +845,31 @@ static int enqueue_iteration(FusedState* f, const Params& p, const DevBlock& b, 
       bb.qp = f->Q[n];
       bb.qp32 = mixed ? f->Q32[n] : nullptr;
       bb.qp32_pitch = f->mpitch;
-      launch_ghosts(p, bb, f->table[n], it, Launcher{s, cnt}, false);
+      launch_ghosts(p, bb, tabs[n], it, Launcher{s, cnt}, false);
     }
   }
   const size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
-  const bool tvd_early = it <= 2 && (p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3);
-  if (tvd_early) cudaMemcpyAsync(f->Us, f->Q[U], bytes, cudaMemcpyDeviceToDevice, s);
+  ip.tvd_early = it <= 2 && (p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3);
+  if (ip.tvd_early) cudaMemcpyAsync(f->Us, f->Q[U], bytes, cudaMemcpyDeviceToDevice, s);
   if (zero_rn) cudaMemsetAsync(b.Rstore, 0, sizeof(double) * ncells(p.d) * p.d.nv, s);
-  for (int n = 0; n < ns; ++n)
-    run_stage(f, p, b, prec, st[n].in, st[n].out, st[n].base, st[n].bA, st[n].bB, st[n].TF, st[n].SF,
-              st[n].TU, st[n].use_rn, st[n].cdt, CFL, it, st[n].last, s, cnt);
-  f->cur = next;
-  if (tvd_early) {
+  return FEST_OK;
+}
+static void iter_stage(FusedState* f, const Params& p, const DevBlock& b, int prec, int it, double CFL,
+                       const IterPlan& ip, int n, BlockRef* const* tabs, cudaStream_t s, long long* cnt) {
+  const StageSpec& z = ip.st[n];
+  run_stage(f, p, b, prec, z.in, z.out, z.base, z.bA, z.bB, z.TF, z.SF, z.TU, z.use_rn, z.cdt, CFL, it, z.last,
+            tabs, s, cnt);
+}
+static void iter_end(FusedState* f, const Params& p, int prec, const IterPlan& ip, cudaStream_t s,
+                     long long* cnt) {
+  const bool mixed = prec == FEST_MIXED;
+  const int U = f->cur;
+  f->cur = ip.next;
+  if (ip.tvd_early) {
     // TVD blends run over the ghosts too (update.f90:203-206): the last
     // stage's input X, q = bA*Us + bB*X on non-interior cells
-    const StageSpec& z = st[ns - 1];
+    const size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
+    const StageSpec& z = ip.st[ip.ns - 1];
     long long n = p.d.P * p.d.nv;
     k_ghost_blend<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Q[U], mixed ? f->Q32[U] : nullptr,
                                                              f->mpitch, f->Us, f->Q[z.in], z.bA, z.bB);
@@ -843,6 +883,14 @@ static int enqueue_iteration(FusedState* f, const Params& p, const DevBlock& b, 
                           cudaMemcpyDeviceToDevice, s);
       }
   }
+}
+static int enqueue_iteration(FusedState* f, const Params& p, const DevBlock& b, int prec, int it,
+                             bool lastit, double CFL, cudaStream_t s, long long* cnt) {
+  IterPlan ip;
+  int rc = iter_begin(f, p, b, prec, it, lastit, f->table, s, cnt, ip);
+  if (rc) return rc;
+  for (int n = 0; n < ip.ns; ++n) iter_stage(f, p, b, prec, it, CFL, ip, n, f->table, s, cnt);
+  iter_end(f, p, prec, ip, s, cnt);
   return FEST_OK;
 }
 
@@ -966,9 +1014,14 @@ int fused_export_residual(FusedState* f, const DevBlock&, cudaStream_t) { return
 
 struct FusedBatch {
   std::vector<FusedState*> f;
-  std::vector<Params> p;
+  std::vector<Params> p;  // part_block: batch indices, self_block: the block's own
   std::vector<DevBlock> b;
-  int nb = 0, interp = 0, flux = 0, integ = 0;
+  int nb = 0, interp = 0, flux = 0, integ = 0, prec = FEST_MIXED;
+  // one batched sweep launch per stage (mixed, one kernel for all blocks);
+  // otherwise every block's own launches, stage by stage
+  bool batched = false;
+  BlockRef* tabs[3] = {nullptr, nullptr, nullptr};  // every block with its buffer n (FP64 and FP32)
+  bool tabs_ready = false;
   Params* d_params = nullptr;
   int kcap = 0;  // k-chunk cap, tuned on the first batched stage
   struct Table {
@@ -1067,6 +1120,14 @@ static FusedBatch::GTable* batch_ghosts(FusedBatch* B, int buf) {
       g.M = Mirror{f->Q32[buf], f->mpitch, p.d.nj, p.d.nk, (long long)f->mpitch * p.d.nj * p.d.nk};
       for (int m = 0; m < 3; ++m) g.F[m] = f->F32[m];
       g.dist = B->b[n].dist;
+      g.PM = g.M;
+      g.pd = p.d;
+      if ((p.id[fc] == -10 || p.id[fc] >= 0) && p.part_block[fc] != n) {  // another block of the batch
+        const FusedState* q = B->f[p.part_block[fc]];
+        const Dims& qd = B->p[p.part_block[fc]].d;
+        g.PM = Mirror{q->Q32[buf], q->mpitch, qd.nj, qd.nk, (long long)q->mpitch * qd.nj * qd.nk};
+        g.pd = qd;
+      }
       h.push_back(g);
       start += (long long)na * nb;
     }
@@ -1171,16 +1232,20 @@ static int batch_iteration(FusedBatch* B, bool lastit, double CFL, cudaStream_t 
 }
 
 int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Params>& p,
-                       const std::vector<DevBlock>& b, FusedBatch** out) {
+                       const std::vector<DevBlock>& b, int prec, FusedBatch** out) {
   *out = nullptr;
   if (f.empty() || f.size() != p.size() || f.size() != b.size()) return FEST_ERR_ARG;
+  if (prec != FEST_MIXED && prec != FEST_FP64) return FEST_ERR_ARG;
+  // the blocks advance stage by stage together: one integrator; a batched
+  // mixed sweep also needs one kernel for all (the same reconstruction, flux
+  // scheme and physics: Euler, laminar, or SST) and no direction whose
+  // ghosts depend on the face order
+  bool batched = prec == FEST_MIXED;
   for (size_t n = 0; n < f.size(); ++n) {
-    // one sweep kernel for all: the same reconstruction, flux scheme,
-    // integrator and physics (Euler, laminar, or SST)
-    if (!f[n] || !fused_supported(p[n], FEST_MIXED) || order_dirs(p[n])) return FEST_ERR_ARG;
-    if (p[n].interp != p[0].interp || p[n].flux != p[0].flux || p[n].integ != p[0].integ ||
+    if (!f[n] || !fused_supported(p[n], prec) || p[n].integ != p[0].integ) return FEST_ERR_ARG;
+    if (order_dirs(p[n]) || p[n].interp != p[0].interp || p[n].flux != p[0].flux ||
         (p[n].mu_ref != 0.0) != (p[0].mu_ref != 0.0) || (p[n].turb != FEST_TURB_NONE) != (p[0].turb != FEST_TURB_NONE))
-      return FEST_ERR_ARG;
+      batched = false;
   }
   FusedBatch* B = new FusedBatch();
   B->f = f;
@@ -1190,12 +1255,51 @@ int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Para
   B->interp = p[0].interp;
   B->flux = p[0].flux;
   B->integ = p[0].integ;
-  if (cudaMalloc((void**)&B->d_params, sizeof(Params) * B->nb) != cudaSuccess ||
-      cudaMemcpy(B->d_params, p.data(), sizeof(Params) * B->nb, cudaMemcpyHostToDevice) != cudaSuccess) {
+  B->prec = prec;
+  B->batched = batched;
+  bool ok = cudaMalloc((void**)&B->d_params, sizeof(Params) * B->nb) == cudaSuccess &&
+            cudaMemcpy(B->d_params, p.data(), sizeof(Params) * B->nb, cudaMemcpyHostToDevice) == cudaSuccess;
+  for (int n = 0; n < 3 && ok; ++n) ok = cudaMalloc((void**)&B->tabs[n], sizeof(BlockRef) * B->nb) == cudaSuccess;
+  if (!ok) {
     fused_batch_destroy(B);
     return FEST_ERR_NOMEM;
   }
   *out = B;
+  return FEST_OK;
+}
+
+// the block tables of the three buffers: every block's FP64 buffer and FP32
+// mirror n (the mirrors exist once the first run has made them)
+static int batch_tables(FusedBatch* B, cudaStream_t s) {
+  if (B->tabs_ready) return FEST_OK;
+  for (int n = 0; n < 3; ++n) {
+    std::vector<BlockRef> t(B->nb);
+    for (int m = 0; m < B->nb; ++m) {
+      t[m].b = B->b[m];
+      t[m].b.qp = B->f[m]->Q[n];
+      t[m].b.qp32 = B->f[m]->Q32[n];
+      t[m].b.qp32_pitch = B->f[m]->mpitch;
+      t[m].d = B->p[m].d;
+    }
+    if (cudaMemcpyAsync(B->tabs[n], t.data(), sizeof(BlockRef) * B->nb, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return FEST_ERR_CUDA;
+  }
+  B->tabs_ready = B->prec == FEST_FP64 || B->f[0]->Q32[0] != nullptr;
+  return FEST_OK;
+}
+
+// one iteration of every block, stage by stage (each block's launches of a
+// stage follow the ghost fills that read the other blocks' stage inputs)
+static int batch_lockstep(FusedBatch* B, int it, bool lastit, double CFL, cudaStream_t s, long long* cnt) {
+  std::vector<IterPlan> ip(B->nb);
+  for (int m = 0; m < B->nb; ++m) {
+    int rc = iter_begin(B->f[m], B->p[m], B->b[m], B->prec, it, lastit, B->tabs, s, cnt, ip[m]);
+    if (rc) return rc;
+  }
+  for (int k = 0; k < ip[0].ns; ++k)
+    for (int m = 0; m < B->nb; ++m) iter_stage(B->f[m], B->p[m], B->b[m], B->prec, it, CFL, ip[m], k, B->tabs, s, cnt);
+  for (int m = 0; m < B->nb; ++m) iter_end(B->f[m], B->p[m], B->prec, ip[m], s, cnt);
   return FEST_OK;
 }
 
@@ -1204,6 +1308,7 @@ void fused_batch_destroy(FusedBatch* B) {
   for (auto& g : B->graphs) cudaGraphExecDestroy(g.exec);
   for (auto& t : B->tables) cudaFree(t.d);
   for (auto& g : B->gtables) cudaFree(g.d);
+  for (int n = 0; n < 3; ++n) cudaFree(B->tabs[n]);
   cudaFree(B->d_params);
   delete B;
 }
@@ -1217,20 +1322,29 @@ int fused_batch_run(FusedBatch* B, int n_iters, int first_iter, double CFL, cuda
     FusedState* f = B->f[n];
     if (!same && f->seeded) fused_export_state(f, B->b[n].qp, s);
     if (!f->seeded) seed(f, s);
-    int rc = ensure_mirrors(f, B->b[n], s, cnt);
-    if (rc) return rc;
+    if (B->prec == FEST_MIXED) {
+      int rc = ensure_mirrors(f, B->b[n], s, cnt);
+      if (rc) return rc;
+    } else {
+      f->mirror_valid = false;  // FP64 stages do not maintain the mirror
+    }
     if (n_iters > 0) f->buffers_equal = false;
   }
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(s, &cap);
+  if (!B->tabs_ready) {
+    if (cap != cudaStreamCaptureStatusNone) return FEST_ERR_ARG;  // the tables copy from the host
+    int rc = batch_tables(B, s);
+    if (rc) return rc;
+  }
   for (int n = 0; n < n_iters; ++n) {
     const int it = first_iter + n;
     const bool lastit = (n == n_iters - 1);
-    if (it <= 2) {  // the early iterations' special ghost handling, block by block
-      for (int m = 0; m < B->nb; ++m) {
-        int rc = enqueue_iteration(B->f[m], B->p[m], B->b[m], FEST_MIXED, it, lastit, CFL, s, cnt);
-        if (rc) return rc;
-      }
+    if (it <= 2 || !B->batched) {
+      // the early iterations' special ghost handling, and FP64 batches (no
+      // batched FP64 sweep): each block's own launches, stage by stage
+      int rc = batch_lockstep(B, it, lastit, CFL, s, cnt);
+      if (rc) return rc;
       continue;
     }
     if (B->kcap == 0) {

@@ -29,12 +29,15 @@ int fused_profile_read(FusedState* f, long long* launches, double* total_ms);
 // materialise the last stage's residual and boundary fluxes for find_resnorm
 int fused_export_residual(FusedState* f, const DevBlock& b, cudaStream_t s);
 
-// Blocks of one multiblock case (same reconstruction, flux scheme and
-// integrator, mixed precision) advanced together: per stage one ghost
-// launch and one sweep launch for all blocks.
+// Blocks of one multiblock case advanced together, stage by stage, their
+// interface ghosts read from each other: mixed precision (same
+// reconstruction, flux scheme, integrator and physics) with one ghost launch
+// and one sweep launch per stage for all blocks after iteration 2; FP64
+// with each block's own launches.  p: the blocks' parameters with
+// part_block set to batch indices and self_block to the block's own.
 struct FusedBatch;
 int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Params>& p,
-                       const std::vector<DevBlock>& b, FusedBatch** out);
+                       const std::vector<DevBlock>& b, int precision, FusedBatch** out);
 void fused_batch_destroy(FusedBatch* B);
 int fused_batch_run(FusedBatch* B, int n_iters, int first_iter, double CFL, cudaStream_t s, long long* cnt);
 

@@ -247,13 +247,16 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       }
     } break;
     default:
-      if (id == -10 || id >= 0) {  // interface / periodic exchange (interface1.f90:496-700)
+      if (id == -10 || id >= 0) {  // interface / periodic exchange (interface1.f90:96-700)
         const BlockRef& pr = blocks[p.part_block[f]];
-        int pf = p.part_face[f];
+        const int pf = p.part_face[f];
+        int na, nb, pa, pb;
+        face_columns(d, f, na, nb);
+        interface_map(p.part_orient[f], na, nb, ta, tb, pa, pb);
         for (int l = 1; l <= d.nv; ++l)
           for (int L = 1; L <= 3; ++L)
             q[ghost_p(d, f, L, ta, tb) + P * (l - 1)] =
-                pr.b.qp[inner_p(pr.d, pf, L, ta, tb) + pr.d.P * (l - 1)];
+                pr.b.qp[inner_p(pr.d, pf, L, pa, pb) + pr.d.P * (l - 1)];
       }
       break;
   }

@@ -106,6 +106,52 @@ template <typename T> struct RingLine {
   }
 };
 
+// Face states of NV variables of one cell along a line: WENO5 in the FP32
+// sweep two variables per instruction stream (weno_pair), every other
+// method and FP64 one variable at a time (recon_cell); the boundary
+// overrides of the cells next to a boundary face follow per variable.
+// ROLL keeps the loop over the variables rolled (instruction-cache size).
+template <typename T, int INTERP, int NV, bool ROLL, class MakeLine, class Lpres, class Lvol>
+__device__ __forceinline__ void recon_vars(const Params& p, int dir, int c, const MakeLine& line, const Lpres& pres,
+                                           const Lvol& vol, T* Rm, T* Lp) {
+  if constexpr (sizeof(T) == 4 && INTERP == FEST_INTERP_WENO) {
+    const bool nb = near_boundary(p, dir, c);
+    if constexpr (ROLL) {
+#pragma unroll 1
+      for (int l = 0; l < NV; l += 2) {
+        const int l2 = l + 1 < NV ? l + 1 : l;
+        const auto qa = line(l), qb = line(l2);
+        float2 rm, lp;
+        weno_pair(qa, qb, c, rm, lp);
+        Rm[l] = rm.x; Lp[l] = lp.x; Rm[l2] = rm.y; Lp[l2] = lp.y;
+        if (nb) {
+          boundary_override<T, INTERP>(p, dir, c, l + 1, qa, Rm[l], Lp[l]);
+          if (l2 != l) boundary_override<T, INTERP>(p, dir, c, l2 + 1, qb, Rm[l2], Lp[l2]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int l = 0; l < NV; l += 2) {
+        const int l2 = l + 1 < NV ? l + 1 : l;
+        const auto qa = line(l), qb = line(l2);
+        float2 rm, lp;
+        weno_pair(qa, qb, c, rm, lp);
+        Rm[l] = rm.x; Lp[l] = lp.x; Rm[l2] = rm.y; Lp[l2] = lp.y;
+        if (nb) {
+          boundary_override<T, INTERP>(p, dir, c, l + 1, qa, Rm[l], Lp[l]);
+          if (l2 != l) boundary_override<T, INTERP>(p, dir, c, l2 + 1, qb, Rm[l2], Lp[l2]);
+        }
+      }
+    }
+  } else if constexpr (ROLL) {
+#pragma unroll 1
+    for (int l = 0; l < NV; ++l) recon_cell<T, INTERP>(p, dir, c, l + 1, line(l), pres, vol, Rm[l], Lp[l]);
+  } else {
+#pragma unroll
+    for (int l = 0; l < NV; ++l) recon_cell<T, INTERP>(p, dir, c, l + 1, line(l), pres, vol, Rm[l], Lp[l]);
+  }
+}
+
 // ---- TMA and mbarrier (PTX) -------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -1016,11 +1062,8 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       SmemLine<T> pres{rowp + 4 * SH * RW + cc, i, 1};
       // not unrolled: the sweep's code outgrows the instruction cache
       // (stalls on instruction fetch were the largest before this)
-#pragma unroll 1
-      for (int l = 0; l < NV; ++l) {
-        SmemLine<T> q{rowp + l * SH * RW + cc, i, 1};
-        recon_cell<T, INTERP>(p, 0, i, l + 1, q, pres, vol, Rm[l], Lp[l]);
-      }
+      auto iline = [&](int l) { return SmemLine<T>{rowp + l * SH * RW + cc, i, 1}; };
+      recon_vars<T, INTERP, NV, true>(p, 0, i, iline, pres, vol, Rm, Lp);
       T L[NV], F[NV];
 #pragma unroll
       for (int l = 0; l < NV; ++l) L[l] = __shfl_up_sync(0xffffffffu, Lp[l], 1);
@@ -1080,11 +1123,8 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       const T* colp = ring + slot(k) * plane + cc;
       const auto vol = vol_line(a, T(0), pidx(d, clampi(i, d.imx), 0, k), sj, d.jmx);
       SmemLine<T> pres{colp + 4 * SH * RW + r * RW, j, RW};
-#pragma unroll 1
-      for (int l = 0; l < NV; ++l) {
-        SmemLine<T> q{colp + l * SH * RW + r * RW, j, RW};
-        recon_cell<T, INTERP>(p, 1, j, l + 1, q, pres, vol, Rm[l], Lp[l]);
-      }
+      auto jline = [&](int l) { return SmemLine<T>{colp + l * SH * RW + r * RW, j, RW}; };
+      recon_vars<T, INTERP, NV, true>(p, 1, j, jline, pres, vol, Rm, Lp);
 #pragma unroll
       for (int l = 0; l < NV; ++l) xch[(l * TY + w) * TX + lane] = Lp[l];
       if constexpr (VISC) {
@@ -1175,11 +1215,8 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       const T* cp = ring + r * RW + cc;
       const auto vol = vol_line(a, T(0), pidx(d, i, j, 0), sk, d.kmx);
       RingLine<T> pres{cp + 4 * SH * RW, plane, base};
-#pragma unroll
-      for (int l = 0; l < NV; ++l) {
-        RingLine<T> q{cp + l * SH * RW, plane, base};
-        recon_cell<T, INTERP>(p, 2, k, l + 1, q, pres, vol, Rm[l], Lp[l]);
-      }
+      auto kline = [&](int l) { return RingLine<T>{cp + l * SH * RW, plane, base}; };
+      recon_vars<T, INTERP, NV, false>(p, 2, k, kline, pres, vol, Rm, Lp);
       T H[NV];
       T lamk = 0;
       float lvk = 0, ltk = 0;

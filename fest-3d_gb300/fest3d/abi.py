@@ -65,7 +65,8 @@ I6 = C.c_int * 6
 class BC(C.Structure):
     _fields_ = [("id", I6), ("partner_block", I6), ("partner_face", I6)] + [(n, D6) for n in (
         "fixed_density", "fixed_pressure", "fixed_x_speed", "fixed_y_speed", "fixed_z_speed",
-        "fixed_tk", "fixed_tw", "fixed_wall_temperature", "fixed_Tpressure", "fixed_Ttemperature")]
+        "fixed_tk", "fixed_tw", "fixed_wall_temperature", "fixed_Tpressure", "fixed_Ttemperature")] + [
+        ("block_id", C.c_int), ("partner_orient", I6)]
 
 
 def make_flow(**kw):
@@ -127,17 +128,23 @@ def make_scheme(**kw):
     return s
 
 
-def make_bc(ids, partners=None, **fixed):
+def make_bc(ids, partners=None, block_id=0, **fixed):
     """boundarytype: ids per face (imin..kmax); partners maps face index ->
-    (block, face) for interface faces; fixed_* arrays of 6 values."""
+    (block, face) or (block, face, orient) for interface faces (orient:
+    bit 0/1 the partner's first/second tangential range reversed, bit 2 the
+    two swapped); block_id: this block's number in its case; fixed_* arrays
+    of 6 values."""
     b = BC()
+    b.block_id = int(block_id)
     for f in range(6):
         b.id[f] = int(ids[f])
-        b.partner_block[f] = 0
+        b.partner_block[f] = int(block_id)
         b.partner_face[f] = f
-    for f, (pb, pf) in (partners or {}).items():
-        b.partner_block[f] = int(pb)
-        b.partner_face[f] = int(pf)
+        b.partner_orient[f] = 0
+    for f, v in (partners or {}).items():
+        b.partner_block[f] = int(v[0])
+        b.partner_face[f] = int(v[1])
+        b.partner_orient[f] = int(v[2]) if len(v) > 2 else 0
     for k, v in fixed.items():
         arr = getattr(b, k)
         for f in range(6):
@@ -259,3 +266,12 @@ def check(code, where):
     if code != FEST_OK:
         raise FestError(code, where)
     return code
+
+
+def orient_from_mapping(f1, s21, e21, s22, e22, dir_switch):
+    """partner_orient of face f1 (1..6) from its line of the reference's
+    mapping file (b1 f1 s11 e11 s12 e12 b2 f2 s21 e21 s22 e22 dir_switch):
+    the partner's ranges along this face's tangential directions, reversed
+    where they run backwards (mapping.f90:159-236)."""
+    del f1  # the same two columns describe every face's tangential directions
+    return (1 if s21 > e21 else 0) | (2 if s22 > e22 else 0) | (4 if dir_switch else 0)

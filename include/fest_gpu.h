@@ -106,9 +106,12 @@ typedef struct {            /* boundarytype, vartypes.f90:289-367 */
   int id[6];                /* imin,imax,jmin,jmax,kmin,kmax */
   /* interface partner of a face whose id is -10 (or >= 0): the ghost layer
    * l of this face receives interior layer l of face partner_face[f] of
-   * block partner_block[f] (interface1.f90:496-700).  For a single-block
-   * handle partner_block must be 0.  A face paired with itself reproduces
-   * what MPI_SENDRECV to the own rank does in the reference (a mirror). */
+   * block partner_block[f] (interface1.f90:96-700), at the tangential
+   * position partner_orient[f] maps it to.  A handle stepped on its own
+   * pairs only with itself (partner_block == block_id); pairs between
+   * blocks are exchanged inside a batch.  A face paired with itself
+   * reproduces what MPI_SENDRECV to the own rank does in the reference (a
+   * mirror). */
   int partner_block[6];
   int partner_face[6];
   double fixed_density[6], fixed_pressure[6];
@@ -116,6 +119,19 @@ typedef struct {            /* boundarytype, vartypes.f90:289-367 */
   double fixed_tk[6], fixed_tw[6];
   double fixed_wall_temperature[6];
   double fixed_Tpressure[6], fixed_Ttemperature[6];
+  /* this block's number in its case (the reference's process_id): a face
+   * whose partner_block equals it pairs with this same block; any other
+   * partner_block names another handle of a batch (fest_batch_create),
+   * matched by that handle's block_id.  Default 0. */
+  int block_id;
+  /* orientation of each interface face relative to its partner face, from
+   * the face's line of the reference's mapping file (mapping.f90:64-236,
+   * interface1.f90:96-464): bit 0 set when the partner's range along this
+   * face's first tangential direction runs backwards (s > e), bit 1 the
+   * same for the second direction, bit 2 the dir_switch column (the two
+   * tangential directions swapped).  Tangential directions: (j, k) on i
+   * faces, (i, k) on j faces, (i, j) on k faces.  Default 0 (aligned). */
+  int partner_orient[6];
 } fest_bc;
 
 typedef struct fest_handle fest_handle;
@@ -244,15 +260,22 @@ int fest_profile(fest_handle *h, int enable);
 int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
 
 /* ---- batches ------------------------------------------------------------- */
-/* No counterpart in the reference (its blocks advance one MPI rank each).
- * The blocks of a multiblock case advanced together: per RK stage one ghost
- * launch and one sweep launch cover every block.  All handles must use
- * FEST_MIXED and the fused path's schemes, with the same reconstruction,
- * flux scheme and integrator; their geometry and state are set through the
- * handles as usual.  fest_batch_create moves every handle onto the first
- * handle's current stream and fest_batch_destroy gives each its own stream
- * back: destroy the batch before any of its handles.  Each handle still
- * answers fest_find_resnorm, fest_download_state etc. for its block. */
+/* No counterpart in the reference (its blocks advance one MPI rank each,
+ * exchanging interface ghosts with MPI_SENDRECV, interface1.f90:96-464).
+ * The blocks of a multiblock case advanced together, stage by stage, each
+ * interface face's ghost layers copied on the device from its partner
+ * block's interior (fest_bc.partner_block names the partner's block_id,
+ * partner_orient its orientation).  All handles must use one precision and
+ * the fused path's schemes with one integrator.  FEST_MIXED batches (one
+ * reconstruction, flux scheme and physics) run one ghost launch and one
+ * sweep launch per RK stage for every block from iteration 3 on; FP64
+ * batches launch each block's own sweep.  Geometry and state are set
+ * through the handles as usual.  fest_batch_create moves every handle onto
+ * the first handle's current stream and fest_batch_destroy gives each its
+ * own stream back: destroy the batch before any of its handles.  Each
+ * handle still answers fest_find_resnorm, fest_download_state etc. for its
+ * block; a handle with partners in other blocks steps only in its batch
+ * (its own step and residual entry points return FEST_ERR_ARG). */
 typedef struct fest_batch fest_batch;
 int fest_batch_create(fest_handle *const *blocks, int n_blocks, fest_batch **out);
 int fest_batch_destroy(fest_batch *b);

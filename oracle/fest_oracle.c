@@ -627,8 +627,34 @@ static void periodic_bc(fo_block *b, int f) {
     }
 }
 
-/* interface1.f90:496-700 apply_periodic_bc and the interface exchange:
- * every receiving face is packed from a snapshot of its partner's interior
+/* the block a face's interface pairs with: itself when partner_block is the
+ * block's own number (the reference's process_id), else the one block of
+ * the list with that number (NULL if there is none or more than one) */
+static fo_block *partner_of(fo_block **blocks, int nblocks, fo_block *b, int f) {
+  const int pb = b->bc.partner_block[f];
+  if (pb == b->bc.block_id) return b;
+  fo_block *found = NULL;
+  for (int m = 0; m < nblocks; ++m)
+    if (blocks[m] != b && blocks[m]->bc.block_id == pb) {
+      if (found) return NULL;
+      found = blocks[m];
+    }
+  return found;
+}
+/* apply_interface's receive loops (interface1.f90:96-464): the sender packs
+ * its layer l with j fastest over its own ranges; the receiver unpacks it
+ * over the ranges of change_map_to_particular_range (mapping.f90:159-236),
+ * each direction forwards or backwards, the two loops swapped by
+ * dir_switch.  Returns the partner's position (pa, pb) of column (ta, tb). */
+static void interface_pos(int orient, int na, int nb, int ta, int tb, int *pa, int *pb) {
+  const int a = (orient & 1) ? na - ta : ta - 1;
+  const int c = (orient & 2) ? nb - tb : tb - 1;
+  if (orient & 4) { *pa = 1 + c; *pb = 1 + a; }
+  else { *pa = 1 + a; *pb = 1 + c; }
+}
+
+/* interface1.f90:96-700 apply_interface / apply_periodic_bc: every
+ * receiving face is packed from a snapshot of its partner's interior
  * layers 1..3 taken before any ghost is written. */
 void fo_apply_interface(fo_block **blocks, int nblocks) {
   int cnt = 0;
@@ -638,11 +664,14 @@ void fo_apply_interface(fo_block **blocks, int nblocks) {
     for (int f = 0; f < 6; ++f) {
       int id = b->bc.id[f];
       if (!(id == -10 || id >= 0)) continue;
-      fo_block *p = blocks[b->bc.partner_block[f]];
+      fo_block *p = partner_of(blocks, nblocks, b, f);
+      if (!p) continue;
       int pf = b->bc.partner_face[f];
+      int orient = b->bc.partner_orient[f];
       int na, nb, pa, pb;
       tang_range(b, f, &na, &nb);
       tang_range(p, pf, &pa, &pb);
+      if (orient & 4) { int t = pa; pa = pb; pb = t; }
       if (na != pa || nb != pb) continue;
       double *s = (double *)malloc(sizeof(double) * (size_t)3 * (na > 0 ? na : 1) * (nb > 0 ? nb : 1) * b->d.n_var);
       size_t c = 0;
@@ -650,8 +679,9 @@ void fo_apply_interface(fo_block **blocks, int nblocks) {
         for (int L = 1; L <= 3; ++L)
           for (int tb = 1; tb <= nb; ++tb)
             for (int ta = 1; ta <= na; ++ta) {
-              int ii, ij, ik;
-              inner_ijk(p, pf, L, ta, tb, &ii, &ij, &ik);
+              int ii, ij, ik, qa, qb;
+              interface_pos(orient, na, nb, ta, tb, &qa, &qb);
+              inner_ijk(p, pf, L, qa, qb, &ii, &ij, &ik);
               s[c++] = *Qp(p, ii, ij, ik, l);
             }
       buf[bi * 6 + f] = s;

@@ -53,7 +53,7 @@ def flatplate_case(grids):
                              klimiter_switch=0, accur=0)
     fixed = dict(fixed_pressure=[P_INF] * 6, fixed_wall_temperature=[0.0] * 6)
     bcs = [abi.make_bc([-8, 1, -6, -6, -6, -6], partners={1: (1, 0)}, **fixed),
-           abi.make_bc([0, -4, -5, -6, -6, -6], partners={0: (0, 1)}, **fixed)]
+           abi.make_bc([0, -4, -5, -6, -6, -6], partners={0: (0, 1)}, block_id=1, **fixed)]
     out = []
     for n, bc in zip(grids, bcs):
         ext = abi.Extent(*n.shape[:3], 5)
@@ -84,7 +84,7 @@ def flatplate_sst_case(grids):
                  fixed_tw=[T_TW] * 6, fixed_density=[T_RHO] * 6, fixed_x_speed=[T_U] * 6,
                  fixed_y_speed=[0.0] * 6, fixed_z_speed=[0.0] * 6)
     bcs = [abi.make_bc([-8, 1, -6, -6, -6, -6], partners={1: (1, 0)}, **fixed),
-           abi.make_bc([0, -4, -5, -6, -6, -6], partners={0: (0, 1)}, **fixed)]
+           abi.make_bc([0, -4, -5, -6, -6, -6], partners={0: (0, 1)}, block_id=1, **fixed)]
     out = []
     for n, bc in zip(grids, bcs):
         ext = abi.Extent(*n.shape[:3], 7)

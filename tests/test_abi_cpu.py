@@ -44,11 +44,15 @@ def test_argument_validation_without_device(lib):
     rc = L.fest_create(C.byref(ext), C.byref(abi.make_flow()), C.byref(abi.make_scheme()),
                        C.byref(abi.make_bc([-5] * 6)), C.byref(h))
     assert rc == abi.FEST_ERR_ARG
-    ext = abi.Extent(9, 9, 9, 5)
-    bc = abi.make_bc([-10, -10, -5, -5, -5, -5], partners={0: (1, 1), 1: (0, 0)})
-    rc = L.fest_create(C.byref(ext), C.byref(abi.make_flow()), C.byref(abi.make_scheme()),
-                       C.byref(bc), C.byref(h))
-    assert rc == abi.FEST_ERR_ARG  # a single-block handle cannot pair with block 1
+    ext = abi.Extent(9, 7, 6, 5)
+    # interface partners: a face number outside 0..5, a negative block, an
+    # orientation outside 0..7, a self pair whose columns do not match
+    for partners in ({0: (1, 6), 1: (0, 0)}, {0: (-1, 1), 1: (0, 0)}, {0: (0, 1, 8), 1: (0, 0)},
+                     {0: (0, 2), 1: (0, 0)}):
+        bc = abi.make_bc([-10, -10, -5, -5, -5, -5], partners=partners)
+        rc = L.fest_create(C.byref(ext), C.byref(abi.make_flow()), C.byref(abi.make_scheme()),
+                           C.byref(bc), C.byref(h))
+        assert rc == abi.FEST_ERR_ARG, partners
     for fn in ("fest_destroy", "fest_find_resnorm", "fest_step"):
         assert getattr(L, fn)(None, *([None] if fn == "fest_find_resnorm" else
                                        [0, 0, 0.5, None] if fn == "fest_step" else [])) in (0, 1)
