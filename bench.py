@@ -61,11 +61,11 @@ def parse():
                          "until its wall Cp is within 1e-5 of FP64's (at most ITERS), and report "
                          "both wall times")
     ap.add_argument("--plate", type=int, default=0, metavar="ITERS",
-                    help="instead of the bench line: the SST flat plate 192x128x1 for ITERS iterations "
-                         "in mixed precision and FP64, with the skin-friction difference")
+                    help="instead of the bench line: the two-block SST flat plate 192x128x2 for ITERS "
+                         "iterations in mixed precision and FP64, with the skin-friction difference")
     ap.add_argument("--cavity", type=int, default=0, metavar="ITERS",
                     help="instead of the bench line: the laminar lid-driven cavity 64x64x4 for ITERS "
-                         "iterations in mixed precision (fused sweep) and FP64 (module path)")
+                         "iterations in mixed precision and FP64 (both fused sweeps)")
     ap.add_argument("--batch", action="store_true",
                     help="instead of the bench line: the 96-block batched case, one launch per "
                          "stage for all blocks against a loop over the blocks' own steps")
@@ -742,14 +742,14 @@ def run_cavity(args):
 
 
 def run_plate(args):
-    """Turbulent flat plate with k-omega SST (192x128x1 cells, MUSCL +
-    AUSM-UP, RK4, local dt, CFL 1.0, M 0.2, Re 5e6 per metre): ITERS
-    iterations in mixed precision (the fused FP32 sweep with its SST terms)
-    and in FP64 (the module kernels); wall times, rates, residual norms and
-    the skin friction along the plate.  Cf = tau_w / (1/2 rho_inf U_inf^2)
-    with tau_w = mu(T_1) u_1 / d_1 from the first cell row (u_1 its
-    x-velocity, d_1 its wall distance, mu by Sutherland's law at its
-    temperature)."""
+    """Turbulent flat plate with k-omega SST, 192x128x2 cells as the
+    reference's two-block layout (0.33 m symmetry run-in + 2 m plate joined
+    by an interface; MUSCL + AUSM-UP, RK4, local dt, CFL 1.0, M 0.2, Re 5e6
+    per metre): ITERS iterations of both blocks in one batch, in mixed
+    precision and in FP64; wall times, rates, residual norms and the skin
+    friction along the plate.  Cf = tau_w / (1/2 rho_inf U_inf^2) with tau_w
+    = mu(T_1) u_1 / d_1 from the first cell row (u_1 its x-velocity, d_1 its
+    wall distance, mu by Sutherland's law at its temperature)."""
     import numpy as np
     import torch
     torch.cuda.set_device(0)
@@ -759,25 +759,35 @@ def run_plate(args):
         build.build()
     lib = abi.load()
     case = cases.plate_case()
-    ext, flow = case["ext"], case["flow"]
-    wall = cases.wall_nodes_of(case["nodes"], ext, case["bc"])
+    flow = case["flow"]
     out = {"mode": "SST flat plate", "workload": case["name"], "iters": args.plate}
     cf = {}
-    N = (ext.imx - 1) * (ext.jmx - 1) * (ext.kmx - 1)
+    N = sum((b["ext"].imx - 1) * (b["ext"].jmx - 1) * (b["ext"].kmx - 1) for b in case["blocks"])
     U, rho_inf = flow.x_speed_inf, flow.density_inf
     for prec, name in ((abi.FEST_MIXED, "mixed"), (abi.FEST_FP64, "fp64")):
-        h = Handle(ext, flow, case["scheme"], case["bc"], lib=lib)
-        h.setup_geometry(case["nodes"])
-        dist = h.find_wall_dist(wall)
-        h.upload_state(case["qp"])
-        h.set_precision(prec)
-        h.step(2, 1, case["CFL"], with_norm=False)  # first-use setup, fix() iterations
+        hs = []
+        for blk in case["blocks"]:
+            h = Handle(blk["ext"], blk["flow"], blk["scheme"], blk["bc"], lib=lib)
+            h.setup_geometry(blk["nodes"])
+            h.find_wall_dist(case["wall"])
+            h.upload_state(blk["qp"])
+            h.set_precision(prec)
+            hs.append(h)
+        arr = (C.c_void_p * len(hs))(*[h.h.value for h in hs])
+        b = C.c_void_p()
+        abi.check(lib.fest_batch_create(arr, len(hs), C.byref(b)), "fest_batch_create")
+        abi.check(lib.fest_batch_step(b, 2, 1, case["CFL"]), "batch step")  # first-use setup, fix() iterations
         torch.cuda.synchronize()
         n = args.plate - 2
         t0 = time.perf_counter()
-        norm = h.step(n, 3, case["CFL"])
+        abi.check(lib.fest_batch_step(b, n, 3, case["CFL"]), "batch step")
         t = time.perf_counter() - t0
-        q = h.download_state()
+        lib.fest_batch_destroy(b)
+        plate = hs[1]
+        ext = plate.ext
+        q = plate.download_state()
+        dist = plate.get("dist")
+        norm = [list(h.resnorm()) for h in hs]
         rho1, u1, p1 = q[3:ext.imx + 2, 3, 3, 0], q[3:ext.imx + 2, 3, 3, 1], q[3:ext.imx + 2, 3, 3, 4]
         T1 = p1 / (rho1 * flow.R_gas)
         mu = flow.mu_ref * (T1 / flow.T_ref) ** 1.5 * (flow.T_ref + flow.Sutherland_temp) / (T1 + flow.Sutherland_temp)
@@ -785,8 +795,9 @@ def run_plate(args):
         cf[name] = mu * u1 / d1 / (0.5 * rho_inf * U * U)
         out[name] = {"seconds": t, "mcell_residuals_per_s": 4 * N * n / t / 1e6,
                      "finite": bool(np.all(np.isfinite(q))),
-                     "resnorm": [float(x) for x in norm]}
-        h.close()
+                     "resnorm_per_block": [[float(x) for x in r] for r in norm]}
+        for h in hs:
+            h.close()
     out["cf_max_abs_diff"] = float(np.abs(cf["mixed"] - cf["fp64"]).max())
     out["cf_max_abs"] = float(np.abs(cf["fp64"]).max())
     out["cf_fp64_sample"] = [float(x) for x in cf["fp64"][:: max(1, len(cf["fp64"]) // 8)]]

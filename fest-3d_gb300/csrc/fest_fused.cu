@@ -318,12 +318,41 @@ __global__ void k_ghost_bcast(Dims d, int f, int na, int nb, Mirror src, Mirror 
 
 unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152 * 16); }
 
+__device__ __forceinline__ bool is_interior(const Dims& d, long long t) {
+  const int i = (int)(t % d.ni) - 2, j = (int)((t / d.ni) % d.nj) - 2, k = (int)(t / ((long long)d.ni * d.nj)) - 2;
+  return i >= 1 && i <= d.imx - 1 && j >= 1 && j <= d.jmx - 1 && k >= 1 && k <= d.kmx - 1;
+}
+// The temperature the reference's gradients use in an iteration
+// (update.f90:170: p/(R rho) of its state at the iteration's start): the
+// interior from the current buffer q; the ghost cells from G, the ghost
+// values the reference's state carries then (the previous iteration's last
+// BC fill, TVD-blended like the whole array, update.f90:196-214)
+__global__ void k_temp_start(Dims d, double R, const double* q, const double* G, double* Temp) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.P) return;
+  const double* s = is_interior(d, t) ? q : G;
+  Temp[t] = s[t + 4 * d.P] / (R * s[t]);
+}
+// the reference's ghost values after an iteration: X, the last stage's
+// input with that stage's BC fill, blended with the previous ones by the
+// TVD integrators (G = bA G + bB X), taken as they are by the others
+__global__ void k_gref(Dims d, double* G, const double* X, double bA, double bB, int blend) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.P * d.nv) return;
+  if (is_interior(d, t % d.P)) return;
+  G[t] = blend ? bA * G[t] + bB * X[t] : X[t];
+}
+
 }  // namespace
 
 struct FusedState {
   Dims d;
   double* Q[3] = {nullptr, nullptr, nullptr};  // Q[0] is the handle's qp
   double* Us = nullptr;  // state at the start of a TVD iteration (<= 2)
+  // FP64 viscous sweeps: the ghost values of the reference's state at the
+  // iteration's start, for the temperature of its gradients
+  double* Gref = nullptr;
+  bool gref_valid = false;
   BlockRef* table[3] = {nullptr, nullptr, nullptr};
   int cur = 0;       // buffer holding the current state
   bool seeded = false;
@@ -414,22 +443,20 @@ static int ring_faces(const Params& p, int* kper) {
 bool fused_supported(const Params& p, int precision) {
   // ping-pong buffers keep each stage's ghosts in its own input buffer; BC
   // sets that read another face's ghosts (blocks thinner than a BC's read
-  // depth, -9) need the in-place module path.  FP64 keeps every ghost layer
-  // equal to the reference's; the mixed sweep needs the layers that the
-  // interior updates read (ghost_depth_ok).
+  // depth, -9) need the in-place module path.  Only ghost layer 1 of a
+  // boundary face (and layers 1-3 of an interface) reaches an interior
+  // update (ghost_depth_ok with stencil_only); directions whose layer-1 fill
+  // depends on the face order are reproduced by the mixed path only.
   // the sweep addresses one plane's stencil with 32-bit offsets
   const bool mixed = precision == FEST_MIXED;
   const bool small_enough = (long long)p.d.P * p.d.nv < (1ll << 31);
-  // viscous and SST terms are in the FP32 sweep only (FP64 viscous blocks
-  // take the module path, which keeps the reference's temperature timing)
-  const bool physics = p.mu_ref == 0.0 || mixed;
   const bool sst = p.turb == FEST_TURB_SST || p.turb == FEST_TURB_SST2003;
-  const bool model = p.turb == FEST_TURB_NONE ? p.d.nv == 5 : (sst && mixed && p.mu_ref != 0.0 && p.d.nv == 7);
+  const bool model = p.turb == FEST_TURB_NONE ? p.d.nv == 5 : (sst && p.mu_ref != 0.0 && p.d.nv == 7);
   // the TVD integrators blend ghosts between fills, which order-dependent
   // directions would read; they take the module path
   const bool tvd = p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3;
-  const bool order_ok = !mixed || order_dirs(p) == 0 || !tvd;
-  return physics && model && p.tstep == 'l' && ghost_depth_ok(p, mixed) && order_ok && small_enough;
+  const bool order_ok = mixed ? (order_dirs(p) == 0 || !tvd) : order_dirs(p) == 0;
+  return model && p.tstep == 'l' && ghost_depth_ok(p, true) && order_ok && small_enough;
 }
 
 int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cudaStream_t s,
@@ -450,6 +477,10 @@ int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cuda
   if (p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3) {
     if (cudaMalloc((void**)&f->Us, bytes) != cudaSuccess) { fused_destroy(f); return FEST_ERR_NOMEM; }
     f->allocs.push_back(f->Us);
+  }
+  if (p.mu_ref != 0.0) {
+    if (cudaMalloc((void**)&f->Gref, bytes) != cudaSuccess) { fused_destroy(f); return FEST_ERR_NOMEM; }
+    f->allocs.push_back(f->Gref);
   }
   if (cudaMalloc((void**)&f->tune_err, sizeof(int)) != cudaSuccess) { fused_destroy(f); return FEST_ERR_NOMEM; }
   f->allocs.push_back(f->tune_err);
@@ -474,7 +505,7 @@ void fused_destroy(FusedState* f) {
 }
 
 void fused_invalidate(FusedState* f) {
-  if (f) { f->cur = 0; f->seeded = false; }
+  if (f) { f->cur = 0; f->seeded = false; f->gref_valid = false; }
 }
 
 // copy the full padded state of buffer `from` into the others so ghost
@@ -575,7 +606,7 @@ static int ensure_mirrors(FusedState* f, const DevBlock& b, cudaStream_t s, long
 
 static void launch_sweep(const Params& p, int prec, int occ, dim3 grid, cudaStream_t s, const StageArgs& a,
                          const CUtensorMap& tm) {
-  if (prec == FEST_MIXED && p.turb != FEST_TURB_NONE) {
+  if (p.turb != FEST_TURB_NONE) {
     switch (p.interp) {
       case FEST_INTERP_NONE: launch_stage_none_sst(prec, p.flux, occ, grid, s, p, a, tm); break;
       case FEST_INTERP_MUSCL: launch_stage_muscl_sst(prec, p.flux, occ, grid, s, p, a, tm); break;
@@ -585,7 +616,7 @@ static void launch_sweep(const Params& p, int prec, int occ, dim3 grid, cudaStre
     }
     return;
   }
-  if (prec == FEST_MIXED && p.mu_ref != 0.0) {
+  if (p.mu_ref != 0.0) {
     switch (p.interp) {
       case FEST_INTERP_NONE: launch_stage_none_visc(prec, p.flux, occ, grid, s, p, a, tm); break;
       case FEST_INTERP_MUSCL: launch_stage_muscl_visc(prec, p.flux, occ, grid, s, p, a, tm); break;
@@ -679,6 +710,8 @@ static StageArgs stage_args(FusedState* f, const DevBlock& b, bool mixed, int in
   a.mpitch = f->mpitch;
   a.cells32 = mixed ? f->C32 : nullptr;
   a.dist32 = mixed ? f->D32 : nullptr;
+  a.Temp = b.Temp;
+  a.dist = b.dist;
   a.ring_ghosts = 0;
   a.kper = 0;
   a.k_chunk = 1;
@@ -848,6 +881,11 @@ static int iter_begin(FusedState* f, const Params& p, const DevBlock& b, int pre
       launch_ghosts(p, bb, tabs[n], it, Launcher{s, cnt}, false);
     }
   }
+  if (!mixed && p.mu_ref != 0.0) {
+    // the gradients' temperature of this iteration (the FP64 viscous sweep)
+    k_temp_start<<<(unsigned)((p.d.P + 255) / 256), 256, 0, s>>>(p.d, p.R, f->Q[U], f->Gref, b.Temp);
+    ++*cnt;
+  }
   const size_t bytes = sizeof(double) * (size_t)p.d.P * p.d.nv;
   ip.tvd_early = it <= 2 && (p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3);
   if (ip.tvd_early) cudaMemcpyAsync(f->Us, f->Q[U], bytes, cudaMemcpyDeviceToDevice, s);
@@ -864,6 +902,13 @@ static void iter_end(FusedState* f, const Params& p, int prec, const IterPlan& i
                      long long* cnt) {
   const bool mixed = prec == FEST_MIXED;
   const int U = f->cur;
+  if (!mixed && p.mu_ref != 0.0) {
+    const StageSpec& z = ip.st[ip.ns - 1];
+    const long long n = p.d.P * p.d.nv;
+    const bool tvd = p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3;
+    k_gref<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.d, f->Gref, f->Q[z.in], z.bA, z.bB, tvd ? 1 : 0);
+    ++*cnt;
+  }
   f->cur = ip.next;
   if (ip.tvd_early) {
     // TVD blends run over the ghosts too (update.f90:203-206): the last
@@ -936,6 +981,14 @@ static int graph_for(FusedState* f, const Params& p, const DevBlock& b, int prec
   return FEST_OK;
 }
 
+// the reference's ghost values start as those of the state the run starts
+// from (before any graph capture, which would replay the copy)
+static void gref_init(FusedState* f, const Params& p, int prec, cudaStream_t s) {
+  if (prec != FEST_FP64 || p.mu_ref == 0.0 || f->gref_valid || !f->Gref) return;
+  cudaMemcpyAsync(f->Gref, f->Q[f->cur], sizeof(double) * (size_t)p.d.P * p.d.nv, cudaMemcpyDeviceToDevice, s);
+  f->gref_valid = true;
+}
+
 int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n_iters,
               int first_iter, double CFL, cudaStream_t s, long long* cnt) {
   if (!f) return FEST_ERR_ARG;
@@ -950,6 +1003,7 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
   if (n_iters > 0) f->buffers_equal = false;
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(s, &cap);
+  gref_init(f, p, prec, s);
   for (int n = 0; n < n_iters; ++n) {
     const int it = first_iter + n;
     const bool lastit = (n == n_iters - 1);
@@ -1328,6 +1382,7 @@ int fused_batch_run(FusedBatch* B, int n_iters, int first_iter, double CFL, cuda
     } else {
       f->mirror_valid = false;  // FP64 stages do not maintain the mirror
     }
+    gref_init(f, B->p[n], B->prec, s);
     if (n_iters > 0) f->buffers_equal = false;
   }
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;

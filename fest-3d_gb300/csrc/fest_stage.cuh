@@ -58,6 +58,10 @@ struct StageArgs {
   int mpitch;           // row pitch of the state mirror (imx+5 rounded up to 4)
   const float4* cells32;  // {volume, cx, cy, cz} (FP32, padded layout): viscous sweeps
   const float* dist32;    // wall distance (FP32, padded layout): SST sweeps
+  // FP64 viscous sweeps: the temperature of the iteration's start (padded;
+  // the reference's gradients use it, update.f90:170) and the wall distance
+  const double* Temp;
+  const double* dist;
   float f_TF, f_CFL, f_bB;  // FP32 copies of TF, CFL and bB
   int blend;              // bA != 0
   // FP32 sweeps after iteration 2: faces (bit f) whose ghost layer 1 the
@@ -257,23 +261,33 @@ __device__ __forceinline__ float from_f64(double x, float) { return d2f(x); }
 __device__ __forceinline__ double from_f64(double x, double) { return x; }
 
 // ---- the update of one cell -------------------------------------------------
-// FP64: update_with(...,'conservative',...) (update.f90:367-485) verbatim.
+// FP64: update_with(...,'conservative',...) (update.f90:367-485) verbatim;
+// SST (NV = 7): the point-implicit destruction (update.f90:395-398, F1 the
+// cell's blending function, omega of the stage's input state) and k, omega
+// written only where they stay non-negative (update.f90:479-480).
+template <int NV>
 __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a, long long c0,
                                             long long ci, const double* R_in, double dtc,
-                                            double vol, const double*, long long) {
+                                            double vol, const double*, long long, double F1) {
   const long long P = p.d.P, N = ncells(p.d);
   const double gm = p.gm;
-  double R[5], u1[5], u2[5];
+  double R[NV], u1[NV], u2[NV];
 #pragma unroll
-  for (int l = 0; l < 5; ++l) R[l] = R_in[l];
+  for (int l = 0; l < NV; ++l) R[l] = R_in[l];
   u1[0] = a.qbase[c0];
 #pragma unroll
-  for (int l = 1; l < 5; ++l) u1[l] = a.qbase[c0 + P * l] * u1[0];
+  for (int l = 1; l < NV; ++l) u1[l] = a.qbase[c0 + P * l] * u1[0];
   double s1 = u1[1] * u1[1] + u1[2] * u1[2] + u1[3] * u1[3];
   u1[4] = (u1[4] / (gm - 1.) + 0.5 * s1) / u1[0];
+  if constexpr (NV == 7) {
+    const double beta = 0.075 * F1 + (1. - F1) * 0.0828;
+    const double wv = a.qin[c0 + 6 * P];
+    R[5] = R[5] / (1 + (beta * wv * dtc));
+    R[6] = R[6] / (1 + (2 * beta * wv * dtc));
+  }
   if (a.use_rn) {
 #pragma unroll
-    for (int l = 0; l < 5; ++l) {
+    for (int l = 0; l < NV; ++l) {
       double rn = a.Rn[ci + N * l] + a.SF * R[l];
       a.Rn[ci + N * l] = rn;
       if (a.TU) R[l] = rn;
@@ -281,18 +295,19 @@ __device__ __forceinline__ bool update_cell(const Params& p, const StageArgs& a,
   }
   const double fac = (a.TF * dtc / vol);
 #pragma unroll
-  for (int l = 0; l < 5; ++l) u2[l] = u1[l] - R[l] * fac;
+  for (int l = 0; l < NV; ++l) u2[l] = u1[l] - R[l] * fac;
 #pragma unroll
-  for (int l = 1; l < 5; ++l) u2[l] = u2[l] / u2[0];
+  for (int l = 1; l < NV; ++l) u2[l] = u2[l] / u2[0];
   double s2 = u2[1] * u2[1] + u2[2] * u2[2] + u2[3] * u2[3];
   u2[4] = (gm - 1.) * u2[0] * (u2[4] - (0.5 * s2));
   bool bad = (u2[0] < 0.) || (u2[4] < 0.);
 #pragma unroll
-  for (int l = 0; l < 5; ++l) bad |= (u2[l] != u2[l]);
+  for (int l = 0; l < NV; ++l) bad |= (u2[l] != u2[l]);
   if (bad) return false;
 #pragma unroll
-  for (int l = 0; l < 5; ++l) {
+  for (int l = 0; l < NV; ++l) {
     double v = u2[l];
+    if (l >= 5 && v < 0.) v = a.qin[c0 + P * l];  // k, omega that would turn negative keep the stage input
     if (a.blend) v = a.bA * a.qU[c0 + P * l] + a.bB * v;
     a.qout[c0 + P * l] = v;
   }
@@ -385,35 +400,75 @@ __device__ __forceinline__ bool update_cell_f32(const Params& p, const StageArgs
 }
 
 
-// ---- viscous and SST terms of the FP32 sweep -------------------------------
-// Cell data the viscous terms read: FP32 copies of the cell records
-// {volume, cx, cy, cz} (float4, padded layout) and, for SST, of the wall
-// distance.
-struct ViscCell {
-  float u, v, w, T, rho;  // primitive velocity, temperature p/(rho R), density
-  float k, om;            // SST: turbulent kinetic energy, specific dissipation
+// ---- viscous and SST terms of the sweep -------------------------------------
+// Templated on the arithmetic type: FP32 in the mixed sweep (fast division
+// and square root), FP64 in the FP64 sweep with the reference's operations.
+// Face and cell records: {A,nx,ny,nz} and {volume,cx,cy,cz}, float4 (FP32
+// copies) or D4 (the FP64 arrays).
+struct D4 {
+  double x, y, z, w;
 };
-template <bool TURB = false>
-__device__ __forceinline__ ViscCell visc_cell(const float* q, int vs, float R) {
-  ViscCell c;
+template <typename T> struct Rec4;
+template <> struct Rec4<float> { using type = float4; };
+template <> struct Rec4<double> { using type = D4; };
+template <typename T> using R4 = typename Rec4<T>::type;
+__device__ __forceinline__ float4 mk4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+__device__ __forceinline__ D4 mk4(double a, double b, double c, double d) { return D4{a, b, c, d}; }
+__device__ __forceinline__ float4 ld_face4(const StageArgs& a, int dir, long long idx, float) {
+  return __ldg(a.faces32[dir] + idx);
+}
+__device__ __forceinline__ D4 ld_face4(const StageArgs& a, int dir, long long idx, double) {
+  const double2* f2 = reinterpret_cast<const double2*>(a.faces[dir] + 4 * idx);
+  const double2 u = __ldg(f2), v = __ldg(f2 + 1);
+  return D4{u.x, u.y, v.x, v.y};
+}
+__device__ __forceinline__ float4 ld_cell4(const StageArgs& a, long long idx, float) { return __ldg(a.cells32 + idx); }
+__device__ __forceinline__ D4 ld_cell4(const StageArgs& a, long long idx, double) {
+  const double2* c2 = reinterpret_cast<const double2*>(a.cells + 4 * idx);
+  const double2 u = __ldg(c2), v = __ldg(c2 + 1);
+  return D4{u.x, u.y, v.x, v.y};
+}
+__device__ __forceinline__ float ld_dist(const StageArgs& a, long long idx, float) { return __ldg(a.dist32 + idx); }
+__device__ __forceinline__ double ld_dist(const StageArgs& a, long long idx, double) { return __ldg(a.dist + idx); }
+__device__ __forceinline__ float ex_tanh(float x) { return tanhf(x); }
+__device__ __forceinline__ double ex_tanh(double x) { return tanh(x); }
+__device__ __forceinline__ float ex_pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double ex_pow(double x, double y) { return pow(x, y); }
+
+template <typename T> struct ViscCell {
+  T u, v, w, rho;  // primitive velocity, density
+  T Tm;            // temperature p/(rho R) of the stage's state (viscosity, flux)
+  T Tg;            // temperature the gradients use (FP64: the iteration's start)
+  T k, om;         // SST: turbulent kinetic energy, specific dissipation
+};
+// Tg: the temperature of the gradient sums, or a negative value for the
+// stage's own (FP32 sweep)
+template <bool TURB, typename T>
+__device__ __forceinline__ ViscCell<T> visc_cell(const T* q, int vs, T R, T Tg) {
+  ViscCell<T> c;
   c.rho = q[0];
   c.u = q[vs];
   c.v = q[2 * vs];
   c.w = q[3 * vs];
-  c.T = dv(q[4 * vs], c.rho * R);
+  c.Tm = dv(q[4 * vs], c.rho * R);
+  c.Tg = Tg < T(0) ? c.Tm : Tg;
   if constexpr (TURB) {
     c.k = q[5 * vs];
     c.om = q[6 * vs];
   } else {
-    c.k = 0.0f;
-    c.om = 0.0f;
+    c.k = T(0);
+    c.om = T(0);
   }
   return c;
 }
 // gradient variable l of a cell: u, v, w, T (+ k, omega for SST), the
-// reference's gradient order (gradients.f90:276-482)
-__device__ __forceinline__ float gvar(const ViscCell& c, int l) {
-  return l == 0 ? c.u : l == 1 ? c.v : l == 2 ? c.w : l == 3 ? c.T : l == 4 ? c.k : c.om;
+// reference's gradient order (gradients.f90:276-482); gvar for the gradient
+// sums, fvar for the differences of the viscous face correction
+template <typename T> __device__ __forceinline__ T gvar(const ViscCell<T>& c, int l) {
+  return l == 0 ? c.u : l == 1 ? c.v : l == 2 ? c.w : l == 3 ? c.Tg : l == 4 ? c.k : c.om;
+}
+template <typename T> __device__ __forceinline__ T fvar(const ViscCell<T>& c, int l) {
+  return l == 3 ? c.Tm : gvar(c, l);
 }
 // dynamic viscosity at a cell: constant mu_ref, or Sutherland's law from the
 // cell temperature (viscosity.f90:109-136)
@@ -424,38 +479,43 @@ __device__ __forceinline__ float visc_mu(const Params& p, float T) {
   const float t = dv(T, Tr);
   return mu_ref * (t * sq(t)) * dv(Tr + S, T + S);
 }
+__device__ __forceinline__ double visc_mu(const Params& p, double T) {
+  if (p.mu_var != FEST_MU_SUTHERLAND) return p.mu_ref;
+  return p.mu_ref * (pow(T / p.T_ref, 1.5)) * ((p.T_ref + p.S) / (T + p.S));
+}
 // Green-Gauss gradient of the NGV gradient variables at a cell
 // (gradients.f90:276-482): grad = sum over faces of +-(phi_nb + phi_c) n A
 // / (2V), low faces of i, j, k first; z components zero on a single-plane
 // block.  nb[0..5] = i-1, j-1, k-1, i+1, j+1, k+1; f[0..5] the matching
 // faces; G[3*l + component].
-template <int NGV>
-__device__ __forceinline__ void visc_gg(const ViscCell& c, const ViscCell* nb, const float4* f, float vol,
-                                        bool thin, float* G) {
-  const float iv2 = dv(1.0f, 2.0f * vol);
+template <int NGV, typename T>
+__device__ __forceinline__ void visc_gg(const ViscCell<T>& c, const ViscCell<T>* nb, const R4<T>* f, T vol,
+                                        bool thin, T* G) {
+  const T iv2 = dv(T(1), T(2) * vol);
 #pragma unroll
   for (int l = 0; l < NGV; ++l) {
-    const float vc = gvar(c, l);
-    float vn[6];
+    const T vc = gvar(c, l);
+    T vn[6];
 #pragma unroll
     for (int m = 0; m < 6; ++m) vn[m] = gvar(nb[m], l);
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-      float g = 0.0f;
+      T g = T(0);
       if (!(thin && comp == 2)) {
-        const float n0 = comp == 0 ? f[0].y : comp == 1 ? f[0].z : f[0].w;
-        const float n1 = comp == 0 ? f[1].y : comp == 1 ? f[1].z : f[1].w;
-        const float n2 = comp == 0 ? f[2].y : comp == 1 ? f[2].z : f[2].w;
-        const float n3 = comp == 0 ? f[3].y : comp == 1 ? f[3].z : f[3].w;
-        const float n4 = comp == 0 ? f[4].y : comp == 1 ? f[4].z : f[4].w;
-        const float n5 = comp == 0 ? f[5].y : comp == 1 ? f[5].z : f[5].w;
-        float s = -((vn[0] + vc) * n0 * f[0].x);
+        const T n0 = comp == 0 ? f[0].y : comp == 1 ? f[0].z : f[0].w;
+        const T n1 = comp == 0 ? f[1].y : comp == 1 ? f[1].z : f[1].w;
+        const T n2 = comp == 0 ? f[2].y : comp == 1 ? f[2].z : f[2].w;
+        const T n3 = comp == 0 ? f[3].y : comp == 1 ? f[3].z : f[3].w;
+        const T n4 = comp == 0 ? f[4].y : comp == 1 ? f[4].z : f[4].w;
+        const T n5 = comp == 0 ? f[5].y : comp == 1 ? f[5].z : f[5].w;
+        T s = -((vn[0] + vc) * n0 * f[0].x);
         s = s - (vn[1] + vc) * n1 * f[1].x;
         s = s - (vn[2] + vc) * n2 * f[2].x;
         s = s + (vn[3] + vc) * n3 * f[3].x;
         s = s + (vn[4] + vc) * n4 * f[4].x;
         s = s + (vn[5] + vc) * n5 * f[5].x;
-        g = s * iv2;
+        if constexpr (sizeof(T) == 8) g = s / (T(2) * vol);
+        else g = s * iv2;
       }
       G[3 * l + comp] = g;
     }
@@ -464,15 +524,20 @@ __device__ __forceinline__ void visc_gg(const ViscCell& c, const ViscCell* nb, c
 // gradient of a ghost cell from its interior neighbour (apply_gradient_bc,
 // gradients.f90:486-676): normal jump over the boundary face, adiabatic
 // walls flip the temperature gradient, plus the interior tangential part
-template <int NGV>
-__device__ __forceinline__ void visc_gbc(const Params& p, int f, const float* GI, const ViscCell& cI,
-                                         const ViscCell& cG, float volI, float4 fc, float* GG) {
-  const float sig = (f % 2) ? -1.0f : 1.0f;
-  const float av = dv(fc.x, volI);
-  const float ccx = av * fc.y, ccy = av * fc.z, ccz = av * fc.w;
+template <int NGV, typename T>
+__device__ __forceinline__ void visc_gbc(const Params& p, int f, const T* GI, const ViscCell<T>& cI,
+                                         const ViscCell<T>& cG, T volI, R4<T> fc, T* GG) {
+  const T sig = (f % 2) ? T(-1) : T(1);
+  T ccx, ccy, ccz;
+  if constexpr (sizeof(T) == 8) {
+    ccx = fc.x * fc.y / volI; ccy = fc.x * fc.z / volI; ccz = fc.x * fc.w / volI;
+  } else {
+    const T av = dv(fc.x, volI);
+    ccx = av * fc.y; ccy = av * fc.z; ccz = av * fc.w;
+  }
 #pragma unroll
   for (int l = 0; l < NGV; ++l) {
-    const float diff = gvar(cI, l) - gvar(cG, l);
+    const T diff = gvar(cI, l) - gvar(cG, l);
     GG[3 * l + 0] = sig * diff * ccx;
     GG[3 * l + 1] = sig * diff * ccy;
     GG[3 * l + 2] = sig * diff * ccz;
@@ -483,11 +548,11 @@ __device__ __forceinline__ void visc_gbc(const Params& p, int f, const float* GI
   }
 #pragma unroll
   for (int l = 0; l < NGV; ++l) {
-    const float gx = GI[3 * l], gy = GI[3 * l + 1], gz = GI[3 * l + 2];
-    const float dot = gx * fc.y + gy * fc.z + gz * fc.w;
-    GG[3 * l + 0] += gx - dot * fc.y;
-    GG[3 * l + 1] += gy - dot * fc.z;
-    GG[3 * l + 2] += gz - dot * fc.w;
+    const T gx = GI[3 * l], gy = GI[3 * l + 1], gz = GI[3 * l + 2];
+    const T dot = (gx * fc.y) + (gy * fc.z) + (gz * fc.w);
+    GG[3 * l + 0] = GG[3 * l + 0] + (gx - dot * fc.y);
+    GG[3 * l + 1] = GG[3 * l + 1] + (gy - dot * fc.z);
+    GG[3 * l + 2] = GG[3 * l + 2] + (gz - dot * fc.w);
   }
 }
 // Viscous flux of a face between cells L and R (viscous.f90:144-325):
@@ -497,61 +562,67 @@ __device__ __forceinline__ void visc_gbc(const Params& p, int f, const float* GI
 // viscosity added to the stresses and the heat flux, the -2/3 rho k normal
 // stress and the k and omega diffusion with F1-blended sigmas, all skipped
 // on the k faces of a single-plane block (sst_face false).
-template <bool TURB = false>
-__device__ __forceinline__ void visc_flux(const Params& p, const float* GL, const float* GR, const ViscCell& L,
-                                          const ViscCell& Rc, float4 cL, float4 cR, float muL, float muR,
-                                          float mutL, float mutR, float F1L, float F1R, float4 fc,
-                                          bool sst_face, float* Fv) {
+template <bool TURB = false, typename T>
+__device__ __forceinline__ void visc_flux(const Params& p, const T* GL, const T* GR, const ViscCell<T>& L,
+                                          const ViscCell<T>& Rc, R4<T> cL, R4<T> cR, T muL, T muR, T mutL,
+                                          T mutR, T F1L, T F1R, R4<T> fc, bool sst_face, T* Fv) {
   constexpr int NGV = TURB ? 6 : 4;
-  float G[3][NGV];
+  T G[3][NGV];
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp)
 #pragma unroll
-    for (int l = 0; l < NGV; ++l) G[comp][l] = 0.5f * (GL[3 * l + comp] + GR[3 * l + comp]);
-  const float dx = cR.y - cL.y, dy = cR.z - cL.z, dz = cR.w - cL.w;
-  const float dLR = sq(dx * dx + dy * dy + dz * dz);
-  const float idLR = dv(1.0f, dLR);
+    for (int l = 0; l < NGV; ++l) G[comp][l] = T(0.5) * (GL[3 * l + comp] + GR[3 * l + comp]);
+  const T dx = cR.y - cL.y, dy = cR.z - cL.z, dz = cR.w - cL.w;
+  const T dLR = sq(dx * dx + dy * dy + dz * dz);
 #pragma unroll
   for (int l = 0; l < NGV; ++l) {
-    const float del = gvar(Rc, l) - gvar(L, l);
-    const float nc = (del - (G[0][l] * dx + G[1][l] * dy + G[2][l] * dz)) * idLR;
-    G[0][l] = G[0][l] + (nc * dx * idLR);
-    G[1][l] = G[1][l] + (nc * dy * idLR);
-    G[2][l] = G[2][l] + (nc * dz * idLR);
+    const T del = fvar(Rc, l) - fvar(L, l);
+    if constexpr (sizeof(T) == 8) {
+      const T nc = (del - (G[0][l] * dx + G[1][l] * dy + G[2][l] * dz)) / dLR;
+      G[0][l] = G[0][l] + (nc * dx / dLR);
+      G[1][l] = G[1][l] + (nc * dy / dLR);
+      G[2][l] = G[2][l] + (nc * dz / dLR);
+    } else {
+      const T idLR = dv(T(1), dLR);
+      const T nc = (del - (G[0][l] * dx + G[1][l] * dy + G[2][l] * dz)) * idLR;
+      G[0][l] = G[0][l] + (nc * dx * idLR);
+      G[1][l] = G[1][l] + (nc * dy * idLR);
+      G[2][l] = G[2][l] + (nc * dz * idLR);
+    }
   }
-  const float mu_f = 0.5f * (muL + muR);
-  const float mut_f = TURB ? 0.5f * (mutL + mutR) : 0.0f;
-  const float tm = TURB ? mu_f + mut_f : mu_f;
-  const float div3 = (G[0][0] + G[1][1] + G[2][2]) * (1.0f / 3.0f);
-  const float Txx = 2.0f * tm * (G[0][0] - div3), Tyy = 2.0f * tm * (G[1][1] - div3),
-              Tzz = 2.0f * tm * (G[2][2] - div3);
-  const float Txy = tm * (G[0][1] + G[1][0]), Txz = tm * (G[0][2] + G[2][0]), Tyz = tm * (G[1][2] + G[2][1]);
-  const float gm = p.f_gm;
-  const float kd = TURB ? dv(mu_f, p.f_Pr) + dv(mut_f, p.f_tPr) : dv(tm, p.f_Pr);
-  const float Kh = kd * gm * p.f_R * dv(1.0f, gm - 1.0f);
-  const float Qx = Kh * G[0][3], Qy = Kh * G[1][3], Qz = Kh * G[2][3];
-  const float uf = 0.5f * (L.u + Rc.u), vf = 0.5f * (L.v + Rc.v), wf = 0.5f * (L.w + Rc.w);
-  const float A = fc.x, nx = fc.y, ny = fc.z, nz = fc.w;
+  const T mu_f = T(0.5) * (muL + muR);
+  const T mut_f = TURB ? T(0.5) * (mutL + mutR) : T(0);
+  const T tm = TURB ? mu_f + mut_f : mu_f;
+  const T div3 = dvc(G[0][0] + G[1][1] + G[2][2], T(3));
+  const T Txx = T(2) * tm * (G[0][0] - div3), Tyy = T(2) * tm * (G[1][1] - div3),
+          Tzz = T(2) * tm * (G[2][2] - div3);
+  const T Txy = tm * (G[0][1] + G[1][0]), Txz = tm * (G[0][2] + G[2][0]), Tyz = tm * (G[1][2] + G[2][1]);
+  const T gm = pv<T>(p.gm, p.f_gm), Rg = pv<T>(p.R, p.f_R);
+  const T kd = TURB ? dv(mu_f, pv<T>(p.Pr, p.f_Pr)) + dv(mut_f, pv<T>(p.tPr, p.f_tPr)) : dv(tm, pv<T>(p.Pr, p.f_Pr));
+  const T Kh = sizeof(T) == 8 ? kd * gm * Rg / (gm - T(1)) : kd * gm * Rg * dv(T(1), gm - T(1));
+  const T Qx = Kh * G[0][3], Qy = Kh * G[1][3], Qz = Kh * G[2][3];
+  const T uf = T(0.5) * (L.u + Rc.u), vf = T(0.5) * (L.v + Rc.v), wf = T(0.5) * (L.w + Rc.w);
+  const T A = fc.x, nx = fc.y, ny = fc.z, nz = fc.w;
   Fv[0] = (Txx * nx + Txy * ny + Txz * nz) * A;
   Fv[1] = (Txy * nx + Tyy * ny + Tyz * nz) * A;
   Fv[2] = (Txz * nx + Tyz * ny + Tzz * nz) * A;
   Fv[3] = A * (((Txx * uf + Txy * vf + Txz * wf + Qx) * nx) + ((Txy * uf + Tyy * vf + Tyz * wf + Qy) * ny) +
                ((Txz * uf + Tyz * vf + Tzz * wf + Qz) * nz));
   if constexpr (TURB) {
-    Fv[4] = 0.0f;
-    Fv[5] = 0.0f;
+    Fv[4] = T(0);
+    Fv[5] = T(0);
     if (sst_face) {
-      const float F1f = 0.5f * (F1L + F1R);
-      const float skf = 0.85f * F1f + 1.0f * (1.0f - F1f);
-      const float swf = 0.5f * F1f + 0.856f * (1.0f - F1f);
-      const float rhof = 0.5f * (L.rho + Rc.rho), tkf = 0.5f * (L.k + Rc.k);
-      const float Tk = -2.0f * rhof * tkf * (1.0f / 3.0f);
-      const float dk = G[0][4] * nx + G[1][4] * ny + G[2][4] * nz;
-      const float dw = G[0][5] * nx + G[1][5] * ny + G[2][5] * nz;
+      const T F1f = T(0.5) * (F1L + F1R);
+      const T skf = T(0.85) * F1f + T(1.0) * (T(1) - F1f);
+      const T swf = T(0.5) * F1f + T(0.856) * (T(1) - F1f);
+      const T rhof = T(0.5) * (L.rho + Rc.rho), tkf = T(0.5) * (L.k + Rc.k);
+      const T Tk = dvc(T(-2) * rhof * tkf, T(3));
+      const T dk = G[0][4] * nx + G[1][4] * ny + G[2][4] * nz;
+      const T dw = G[0][5] * nx + G[1][5] * ny + G[2][5] * nz;
       Fv[0] += Tk * nx * A;
       Fv[1] += Tk * ny * A;
       Fv[2] += Tk * nz * A;
-      const float kdiff = A * ((mu_f + skf * mut_f) * dk);
+      const T kdiff = A * ((mu_f + skf * mut_f) * dk);
       Fv[3] += kdiff;
       Fv[4] = kdiff;
       Fv[5] = A * ((mu_f + swf * mut_f) * dw);
@@ -561,84 +632,89 @@ __device__ __forceinline__ void visc_flux(const Params& p, const float* GL, cons
 // viscous time-step term of a face (add_viscous_time, time.f90:366-448;
 // add_turbulent_time, time.f90:450-531, with mu_t): A mu/(rho |(c_L -
 // c_R).n|) with mu and rho of the face's high-side cell
-__device__ __forceinline__ float visc_lambda(float4 fc, float4 cL, float4 cR, float muR, float rhoR) {
-  const float d = fabsf((cL.y - cR.y) * fc.y + (cL.z - cR.z) * fc.z + (cL.w - cR.w) * fc.w);
-  return fc.x * dv(muR, rhoR * d);
+template <typename T>
+__device__ __forceinline__ T visc_lambda(R4<T> fc, R4<T> cL, R4<T> cR, T muR, T rhoR) {
+  const T d = fabs(((cL.y - cR.y) * fc.y) + ((cL.z - cR.z) * fc.z) + ((cL.w - cR.w) * fc.w));
+  if constexpr (sizeof(T) == 8) return fc.x * (muR / (rhoR * d));
+  else return fc.x * dv(muR, rhoR * d);
 }
 
 // SST quantities of a cell (viscosity.f90:52-546, source.f90:158-270): eddy
 // viscosity, blending function F1, cross-diffusion CD (clamped) and the
 // vorticity magnitude.  G: the cell's gradients of u, v, w, T, k, omega.
-struct SstCell {
-  float mut, F1, CD, vort;
+template <typename T> struct SstCell {
+  T mut, F1, CD, vort;
 };
-__device__ __forceinline__ SstCell sst_cell(const Params& p, const ViscCell& c, float mu, float dd, const float* G) {
-  const float bstar = 0.09f, a1 = 0.31f, sw2 = 0.856f;
+template <typename T>
+__device__ __forceinline__ SstCell<T> sst_cell(const Params& p, const ViscCell<T>& c, T mu, T dd, const T* G) {
+  const T bstar = T(0.09), a1 = T(0.31), sw2 = T(0.856);
   const bool s2003 = p.turb == FEST_TURB_SST2003;
-  SstCell s;
-  const float var1 = dv(sq(c.k), bstar * c.om * dd);
-  const float var2 = dv(500.0f * dv(mu, c.rho), (dd * dd) * c.om);
-  const float arg2 = fmax2(2.0f * var1, var2);
-  const float F2 = tanhf(arg2 * arg2);
-  const float NUM = c.rho * a1 * c.k;
+  SstCell<T> s;
+  const T var1 = dv(sq(c.k), bstar * c.om * dd);
+  const T var2 = dv(T(500) * dv(mu, c.rho), (dd * dd) * c.om);
+  const T arg2 = fmax2(T(2) * var1, var2);
+  const T F2 = ex_tanh(arg2 * arg2);
+  const T NUM = c.rho * a1 * c.k;
   // G(component, variable) of the reference = G[3*(variable-1) + component]
-  const float wx = G[7] - G[5], wy = G[2] - G[6], wz = G[3] - G[1];
+  const T wx = G[7] - G[5], wy = G[2] - G[6], wz = G[3] - G[1];
   s.vort = sq(wx * wx + wy * wy + wz * wz);
-  float DENOM;
+  T DENOM;
   if (s2003) {
-    const float sxx = G[0], syy = G[4], szz = G[8];
-    const float syz = G[7] + G[5], szx = G[2] + G[6], sxy = G[3] + G[1];
-    const float SijSij = (2.0f * (sxx * sxx)) + (2.0f * (syy * syy)) + (2.0f * (szz * szz)) + syz * syz +
-                         szx * szx + sxy * sxy;
-    DENOM = fmax2(fmax2(a1 * c.om, sq(SijSij) * F2), 1.0e-10f);
+    const T sxx = G[0], syy = G[4], szz = G[8];
+    const T syz = G[7] + G[5], szx = G[2] + G[6], sxy = G[3] + G[1];
+    const T SijSij = (T(2) * (sxx * sxx)) + (T(2) * (syy * syy)) + (T(2) * (szz * szz)) + syz * syz +
+                     szx * szx + sxy * sxy;
+    DENOM = fmax2(fmax2(a1 * c.om, sq(SijSij) * F2), T(1.0e-10));
   } else {
-    DENOM = fmax2(fmax2(a1 * c.om, s.vort * F2), 1.0e-20f);
+    DENOM = fmax2(fmax2(a1 * c.om, s.vort * F2), T(1.0e-20));
   }
   s.mut = dv(NUM, DENOM);
-  float CD = dv(2.0f * c.rho * sw2 * (G[12] * G[15] + G[13] * G[16] + G[14] * G[17]), c.om);
-  s.CD = fmax2(CD, s2003 ? 1.0e-10f : 1.0e-20f);
-  const float right = dv(4.0f * (c.rho * sw2 * c.k), s.CD * (dd * dd));
-  const float arg1 = fmin2(fmax2(var1, var2), right);
-  const float a2 = arg1 * arg1;
-  s.F1 = tanhf(a2 * a2);
+  T CD = dv(T(2) * c.rho * sw2 * (G[12] * G[15] + G[13] * G[16] + G[14] * G[17]), c.om);
+  s.CD = fmax2(CD, s2003 ? T(1.0e-10) : T(1.0e-20));
+  const T right = dv(T(4) * (c.rho * sw2 * c.k), s.CD * (dd * dd));
+  const T arg1 = fmin2(fmax2(var1, var2), right);
+  const T a2 = arg1 * arg1;
+  s.F1 = ex_tanh(a2 * a2);
   return s;
 }
 // SST source of an interior cell (add_sst_source, source.f90:158-270):
 // production limited by 20 (sst) or 10 (sst2003) times the destruction;
 // the residual of k and omega loses Sk, Sw
-__device__ __forceinline__ void sst_source(const Params& p, const ViscCell& c, const SstCell& s, const float* G,
-                                           float vol, float& Sk, float& Sw) {
+template <typename T>
+__device__ __forceinline__ void sst_source(const Params& p, const ViscCell<T>& c, const SstCell<T>& s, const T* G,
+                                           T vol, T& Sk, T& Sw) {
   constexpr double kBeta1 = 0.075, kBeta2 = 0.0828, kBstar = 0.09, kSw1 = 0.5, kSw2 = 0.856, kKap = 0.41;
   // gamma_{1,2} = beta_{1,2}/beta* - sigma_w{1,2} kappa^2 / sqrt(beta*), sqrt(0.09) = 0.3
-  constexpr float kG1 = (float)((kBeta1 / kBstar) - ((kSw1 * (kKap * kKap)) / 0.3));
-  constexpr float kG2 = (float)((kBeta2 / kBstar) - ((kSw2 * (kKap * kKap)) / 0.3));
+  constexpr T kG1 = (T)((kBeta1 / kBstar) - ((kSw1 * (kKap * kKap)) / 0.3));
+  constexpr T kG2 = (T)((kBeta2 / kBstar) - ((kSw2 * (kKap * kKap)) / 0.3));
   const bool s2003 = p.turb == FEST_TURB_SST2003;
-  const float lim = s2003 ? 10.0f : 20.0f;
-  const float gama1 = s2003 ? 5.0f / 9.0f : kG1, gama2 = s2003 ? 0.44f : kG2;
-  const float F1 = s.F1;
-  const float gama = gama1 * F1 + gama2 * (1.0f - F1);
-  const float beta = (float)kBeta1 * F1 + (float)kBeta2 * (1.0f - F1);
-  const float Dk = (float)kBstar * c.rho * c.om * c.k;
-  const float Dw = beta * c.rho * (c.om * c.om);
-  const float divergence = G[0] + G[4] + G[8];
-  float Pk = s.mut * (s.vort * s.vort) - ((2.0f / 3.0f) * c.rho * c.k * divergence);
+  const T lim = s2003 ? T(10) : T(20);
+  const T gama1 = s2003 ? T(5.0 / 9.0) : kG1, gama2 = s2003 ? T(0.44) : kG2;
+  const T F1 = s.F1;
+  const T gama = gama1 * F1 + gama2 * (T(1) - F1);
+  const T beta = (T)kBeta1 * F1 + (T)kBeta2 * (T(1) - F1);
+  const T Dk = (T)kBstar * c.rho * c.om * c.k;
+  const T Dw = beta * c.rho * (c.om * c.om);
+  const T divergence = G[0] + G[4] + G[8];
+  T Pk = s.mut * (s.vort * s.vort) - ((T(2) / T(3)) * c.rho * c.k * divergence);
   Pk = fmin2(Pk, lim * Dk);
-  const float Pw = dv(c.rho * gama, s.mut) * Pk;
+  const T Pw = dv(c.rho * gama, s.mut) * Pk;
   Sk = (Pk - Dk) * vol;
-  Sw = (Pw - Dw + (1.0f - F1) * s.CD) * vol;
+  Sw = (Pw - Dw + (T(1) - F1) * s.CD) * vol;
 }
 // eddy viscosity and F1 of a ghost cell next to a boundary face with a
 // negative id: faces -1..-9 copy the interior values, the wall negating
 // mu_t (viscosity.f90:287-340); other faces keep what calculate_viscosity
 // computed there from the ghost's own state and boundary gradient
-__device__ __forceinline__ void sst_ghost(const Params& p, int f, const ViscCell& cG, float muG, const float* GG,
-                                          float ddG, float mutI, float F1I, float& mutG, float& F1G) {
+template <typename T>
+__device__ __forceinline__ void sst_ghost(const Params& p, int f, const ViscCell<T>& cG, T muG, const T* GG,
+                                          T ddG, T mutI, T F1I, T& mutG, T& F1G) {
   const int id = p.id[f];
   if (id <= -1 && id >= -9) {
     mutG = id == -5 ? -mutI : mutI;
     F1G = F1I;
   } else {
-    const SstCell s = sst_cell(p, cG, muG, ddG, GG);
+    const SstCell<T> s = sst_cell(p, cG, muG, ddG, GG);
     mutG = s.mut;
     F1G = s.F1;
   }
@@ -770,7 +846,6 @@ __device__ __forceinline__ void ghost_layer1(const Params& p, int f, float* G, c
 template <typename T, int INTERP, int FLUX, bool VISC = false, bool TURB = false>
 __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, const CUtensorMap* tmp,
                                            int bx, int by, int bz) {
-  static_assert(!VISC || sizeof(T) == 4, "viscous terms are in the FP32 sweep only");
   static_assert(!TURB || VISC, "the SST terms come with the viscous terms");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   constexpr int NV = TURB ? 7 : 5;
@@ -784,11 +859,11 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
   T* lam = gfl + NV * TY * TX;                            // [TY][TX]    j-face dt terms
   // viscous: [NGC][TY][TX] cell gradients, [TY][TX] viscous j-face dt
   // terms; SST: [TY][TX] each of mu_t, F1 and turbulent j-face dt terms
-  float* gxch = reinterpret_cast<float*>(lam + TY * TX);
-  float* lamv = gxch + NGC * TY * TX;
-  float* mutx = lamv + TY * TX;
-  float* f1x = mutx + TY * TX;
-  float* lamt = f1x + TY * TX;
+  T* gxch = lam + TY * TX;
+  T* lamv = gxch + NGC * TY * TX;
+  T* mutx = lamv + TY * TX;
+  T* f1x = mutx + TY * TX;
+  T* lamt = f1x + TY * TX;
   uint64_t* bars = reinterpret_cast<uint64_t*>(lam + TY * TX + NXV * TY * TX);  // [NR]
   __shared__ int abort_flag;
   const Dims& d = p.d;
@@ -932,14 +1007,20 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
 #pragma unroll
   for (int l = 0; l < NV; ++l) { Lp_prev[l] = 0; H_prev[l] = 0; dF_prev[l] = 0; dG_prev[l] = 0; }
   // viscous march state: raw gradient of cell (i, j, k-1), viscous dt terms
-  float Gprev[VISC ? NGC : 1];
+  T Gprev[VISC ? NGC : 1];
 #pragma unroll
-  for (int m = 0; m < (VISC ? NGC : 1); ++m) Gprev[m] = 0.0f;
-  float lvk_prev = 0, lvi_lo_prev = 0, lvi_hi_prev = 0, lvj_lo_prev = 0, lvj_hi_prev = 0;
+  for (int m = 0; m < (VISC ? NGC : 1); ++m) Gprev[m] = T(0);
+  T lvk_prev = 0, lvi_lo_prev = 0, lvi_hi_prev = 0, lvj_lo_prev = 0, lvj_hi_prev = 0;
   // SST march state: mu_t, F1 and source of cell (i, j, k-1), turbulent dt terms
-  float mut_prev = 0, F1_prev = 0, Sk_prev = 0, Sw_prev = 0;
-  float ltk_prev = 0, lti_lo_prev = 0, lti_hi_prev = 0, ltj_lo_prev = 0, ltj_hi_prev = 0;
-  const float Rg = p.f_R;
+  T mut_prev = 0, F1_prev = 0, Sk_prev = 0, Sw_prev = 0;
+  T ltk_prev = 0, lti_lo_prev = 0, lti_hi_prev = 0, ltj_lo_prev = 0, ltj_hi_prev = 0;
+  const T Rg = pv<T>(p.R, p.f_R);
+  // the temperature of a cell's gradient sums: FP64 reads the iteration's
+  // start (a.Temp), FP32 takes its stage's own (a negative value)
+  auto tgrad = [&](int ii, int jj, int kk) -> T {
+    if constexpr (sizeof(T) == 8) return __ldg(a.Temp + pidx(d, clampi(ii, d.imx), clampi(jj, d.jmx), kk));
+    else return T(-1);
+  };
 
   const long long sj = d.ni, sk = (long long)d.ni * d.nj;
   for (int n = 0; n < nplanes; ++n) {
@@ -1019,37 +1100,37 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
     for (int l = 0; l < NV; ++l) qc[l] = own[l * SH * RW];
     // viscous: this cell's values, centre, viscosity and raw Green-Gauss
     // gradient (every thread, halo included); SST: its mu_t, F1 and source
-    ViscCell Vc{};
-    float4 cown = make_float4(1.f, 0.f, 0.f, 0.f);
-    float muc = 0.f, Gc[VISC ? NGC : 1];
-    float lvi_lo = 0, lvi_hi = 0, lvj_lo = 0, lvj_hi = 0;
-    SstCell Sc{0.f, 0.f, 0.f, 0.f};
-    float ddc = 1.f, Skc = 0.f, Swc = 0.f;
-    float lti_lo = 0, lti_hi = 0, ltj_lo = 0, ltj_hi = 0;
+    ViscCell<T> Vc{};
+    R4<T> cown = mk4(T(1), T(0), T(0), T(0));
+    T muc = T(0), Gc[VISC ? NGC : 1];
+    T lvi_lo = 0, lvi_hi = 0, lvj_lo = 0, lvj_hi = 0;
+    SstCell<T> Sc{T(0), T(0), T(0), T(0)};
+    T ddc = T(1), Skc = T(0), Swc = T(0);
+    T lti_lo = 0, lti_hi = 0, ltj_lo = 0, ltj_hi = 0;
     const int ci_ = clampi(i, d.imx), cj_ = clampi(j, d.jmx);
     if constexpr (VISC) {
-      const float* o = reinterpret_cast<const float*>(own);
-      Vc = visc_cell<TURB>(o, VS, Rg);
-      ViscCell nb[6];
-      nb[0] = visc_cell<TURB>(o - 1, VS, Rg);
-      nb[1] = visc_cell<TURB>(o - RW, VS, Rg);
-      nb[2] = visc_cell<TURB>(reinterpret_cast<const float*>(ring + slot(k - 1) * plane + r * RW + cc), VS, Rg);
-      nb[3] = visc_cell<TURB>(o + 1, VS, Rg);
-      nb[4] = visc_cell<TURB>(o + RW, VS, Rg);
-      nb[5] = visc_cell<TURB>(reinterpret_cast<const float*>(ring + slot(k + 1) * plane + r * RW + cc), VS, Rg);
+      const T* o = own;
+      Vc = visc_cell<TURB>(o, VS, Rg, tgrad(i, j, k));
+      ViscCell<T> nb[6];
+      nb[0] = visc_cell<TURB>(o - 1, VS, Rg, tgrad(i - 1, j, k));
+      nb[1] = visc_cell<TURB>(o - RW, VS, Rg, tgrad(i, j - 1, k));
+      nb[2] = visc_cell<TURB>(ring + slot(k - 1) * plane + r * RW + cc, VS, Rg, tgrad(i, j, k - 1));
+      nb[3] = visc_cell<TURB>(o + 1, VS, Rg, tgrad(i + 1, j, k));
+      nb[4] = visc_cell<TURB>(o + RW, VS, Rg, tgrad(i, j + 1, k));
+      nb[5] = visc_cell<TURB>(ring + slot(k + 1) * plane + r * RW + cc, VS, Rg, tgrad(i, j, k + 1));
       const int ci1 = clampi(i + 1, d.imx + 1), cj1 = clampi(j + 1, d.jmx + 1);
-      float4 fgg[6];
-      fgg[0] = __ldg(a.faces32[0] + fidx(d, 0, ci_, cj_, k));
-      fgg[1] = __ldg(a.faces32[1] + fidx(d, 1, ci_, cj_, k));
-      fgg[2] = __ldg(a.faces32[2] + fidx(d, 2, ci_, cj_, k));
-      fgg[3] = __ldg(a.faces32[0] + fidx(d, 0, ci1, cj_, k));
-      fgg[4] = __ldg(a.faces32[1] + fidx(d, 1, ci_, cj1, k));
-      fgg[5] = __ldg(a.faces32[2] + fidx(d, 2, ci_, cj_, k + 1));
-      cown = __ldg(a.cells32 + pidx(d, ci_, cj_, k));
+      R4<T> fgg[6];
+      fgg[0] = ld_face4(a, 0, fidx(d, 0, ci_, cj_, k), T(0));
+      fgg[1] = ld_face4(a, 1, fidx(d, 1, ci_, cj_, k), T(0));
+      fgg[2] = ld_face4(a, 2, fidx(d, 2, ci_, cj_, k), T(0));
+      fgg[3] = ld_face4(a, 0, fidx(d, 0, ci1, cj_, k), T(0));
+      fgg[4] = ld_face4(a, 1, fidx(d, 1, ci_, cj1, k), T(0));
+      fgg[5] = ld_face4(a, 2, fidx(d, 2, ci_, cj_, k + 1), T(0));
+      cown = ld_cell4(a, pidx(d, ci_, cj_, k), T(0));
       visc_gg<NGV>(Vc, nb, fgg, cown.x, thin, Gc);
-      muc = visc_mu(p, Vc.T);
+      muc = visc_mu(p, Vc.Tm);
       if constexpr (TURB) {
-        ddc = __ldg(a.dist32 + pidx(d, ci_, cj_, k));
+        ddc = ld_dist(a, pidx(d, ci_, cj_, k), T(0));
         Sc = sst_cell(p, Vc, muc, ddc, Gc);
         if (kin && in_i && in_j) sst_source(p, Vc, Sc, Gc, cown.x, Skc, Swc);
       }
@@ -1063,7 +1144,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       // not unrolled: the sweep's code outgrows the instruction cache
       // (stalls on instruction fetch were the largest before this)
       auto iline = [&](int l) { return SmemLine<T>{rowp + l * SH * RW + cc, i, 1}; };
-      recon_vars<T, INTERP, NV, true>(p, 0, i, iline, pres, vol, Rm, Lp);
+      recon_vars<T, INTERP, NV, !(sizeof(T) == 4 && INTERP == FEST_INTERP_WENO)>(p, 0, i, iline, pres, vol, Rm, Lp);
       T L[NV], F[NV];
 #pragma unroll
       for (int l = 0; l < NV; ++l) L[l] = __shfl_up_sync(0xffffffffu, Lp[l], 1);
@@ -1073,26 +1154,26 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       if (a.compute_dt) lami_lo = lambda_face<T>(gm, L, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
       lami_hi = __shfl_down_sync(0xffffffffu, lami_lo, 1);
       if constexpr (VISC) {  // viscous flux of the low i-face (cells i-1, i)
-        float Gl[NGC], GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
+        T Gl[NGC], GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
 #pragma unroll
         for (int m = 0; m < NGC; ++m) Gl[m] = __shfl_up_sync(0xffffffffu, Gc[m], 1);
 #pragma unroll
         for (int m = 0; m < NGC; ++m) { GL[m] = Gl[m]; GR[m] = Gc[m]; }
-        const ViscCell VL = visc_cell<TURB>(reinterpret_cast<const float*>(own) - 1, VS, Rg);
-        const float4 cL = __ldg(a.cells32 + pidx(d, clampi(i - 1, d.imx), cj_, k));
-        const float4 fc = make_float4(A, nx, ny, nz);
-        const float muL = visc_mu(p, VL.T);
-        float mutL = 0.f, F1L = 0.f, mutR = Sc.mut, F1R = Sc.F1;
+        const ViscCell<T> VL = visc_cell<TURB>(own - 1, VS, Rg, tgrad(i - 1, j, k));
+        const R4<T> cL = ld_cell4(a, pidx(d, clampi(i - 1, d.imx), cj_, k), T(0));
+        const R4<T> fc = mk4(A, nx, ny, nz);
+        const T muL = visc_mu(p, VL.Tm);
+        T mutL = T(0), F1L = T(0), mutR = Sc.mut, F1R = Sc.F1;
         if constexpr (TURB) {
           mutL = __shfl_up_sync(0xffffffffu, Sc.mut, 1);
           F1L = __shfl_up_sync(0xffffffffu, Sc.F1, 1);
         }
-        const float mutLi = mutL, F1Li = F1L;
+        const T mutLi = mutL, F1Li = F1L;
         if (i - 1 == 0 && p.id[0] < 0) {
           visc_gbc<NGV>(p, 0, Gc, Vc, VL, cown.x, fc, GL);
           if constexpr (TURB)
-            sst_ghost(p, 0, VL, muL, GL, __ldg(a.dist32 + pidx(d, clampi(i - 1, d.imx), cj_, k)), Sc.mut, Sc.F1,
-                      mutL, F1L);
+            sst_ghost(p, 0, VL, muL, GL, ld_dist(a, pidx(d, clampi(i - 1, d.imx), cj_, k), T(0)), Sc.mut,
+                      Sc.F1, mutL, F1L);
         }
         if (i == d.imx && p.id[1] < 0) {
           visc_gbc<NGV>(p, 1, Gl, VL, Vc, cL.x, fc, GR);
@@ -1124,7 +1205,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       const auto vol = vol_line(a, T(0), pidx(d, clampi(i, d.imx), 0, k), sj, d.jmx);
       SmemLine<T> pres{colp + 4 * SH * RW + r * RW, j, RW};
       auto jline = [&](int l) { return SmemLine<T>{colp + l * SH * RW + r * RW, j, RW}; };
-      recon_vars<T, INTERP, NV, true>(p, 1, j, jline, pres, vol, Rm, Lp);
+      recon_vars<T, INTERP, NV, !(sizeof(T) == 4 && INTERP == FEST_INTERP_WENO)>(p, 1, j, jline, pres, vol, Rm, Lp);
 #pragma unroll
       for (int l = 0; l < NV; ++l) xch[(l * TY + w) * TX + lane] = Lp[l];
       if constexpr (VISC) {
@@ -1147,25 +1228,25 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         load_face(a, 1, fidx(d, 1, clampi(i, d.imx), clampi(j, d.jmx), k), A, nx, ny, nz);
         face_flux<T, FLUX>(p, L, Rm, A, nx, ny, nz, (T)wall_mask(p, 1, j), F);
         if constexpr (VISC) {  // viscous flux of the low j-face (cells j-1, j)
-          float Gd[NGC], GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
+          T Gd[NGC], GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
 #pragma unroll
           for (int m = 0; m < NGC; ++m) Gd[m] = gxch[(m * TY + w - 1) * TX + lane];
-          const ViscCell VD = visc_cell<TURB>(reinterpret_cast<const float*>(own) - RW, VS, Rg);
-          const float4 cD = __ldg(a.cells32 + pidx(d, ci_, clampi(j - 1, d.jmx), k));
-          const float4 fc = make_float4(A, nx, ny, nz);
-          const float muD = visc_mu(p, VD.T);
-          float mutD = 0.f, F1D = 0.f, mutR = Sc.mut, F1R = Sc.F1;
+          const ViscCell<T> VD = visc_cell<TURB>(own - RW, VS, Rg, tgrad(i, j - 1, k));
+          const R4<T> cD = ld_cell4(a, pidx(d, ci_, clampi(j - 1, d.jmx), k), T(0));
+          const R4<T> fc = mk4(A, nx, ny, nz);
+          const T muD = visc_mu(p, VD.Tm);
+          T mutD = T(0), F1D = T(0), mutR = Sc.mut, F1R = Sc.F1;
           if constexpr (TURB) {
             mutD = mutx[(w - 1) * TX + lane];
             F1D = f1x[(w - 1) * TX + lane];
           }
-          const float mutDi = mutD, F1Di = F1D;
+          const T mutDi = mutD, F1Di = F1D;
 #pragma unroll
           for (int m = 0; m < NGC; ++m) { GL[m] = Gd[m]; GR[m] = Gc[m]; }
           if (j - 1 == 0 && p.id[2] < 0) {
             visc_gbc<NGV>(p, 2, Gc, Vc, VD, cown.x, fc, GL);
             if constexpr (TURB)
-              sst_ghost(p, 2, VD, muD, GL, __ldg(a.dist32 + pidx(d, ci_, clampi(j - 1, d.jmx), k)), Sc.mut,
+              sst_ghost(p, 2, VD, muD, GL, ld_dist(a, pidx(d, ci_, clampi(j - 1, d.jmx), k), T(0)), Sc.mut,
                         Sc.F1, mutD, F1D);
           }
           if (j == d.jmx && p.id[3] < 0) {
@@ -1219,7 +1300,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
       recon_vars<T, INTERP, NV, false>(p, 2, k, kline, pres, vol, Rm, Lp);
       T H[NV];
       T lamk = 0;
-      float lvk = 0, ltk = 0;
+      T lvk = 0, ltk = 0;
       if (k >= k0) {
         T A, nx, ny, nz;
         load_face(a, 2, fidx(d, 2, i, j, k), A, nx, ny, nz);
@@ -1231,19 +1312,18 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
         }
         if (a.compute_dt) lamk = lambda_face<T>(gm, Lp_prev, Rm, A, nx, ny, nz, qc[1], qc[2], qc[3]);
         if constexpr (VISC) {  // viscous flux of the low k-face (cells k-1, k)
-          float GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
-          const ViscCell VK = visc_cell<TURB>(
-              reinterpret_cast<const float*>(ring + slot(k - 1) * plane + r * RW + cc), VS, Rg);
-          const float4 cK = __ldg(a.cells32 + pidx(d, i, j, k - 1));
-          const float4 fc = make_float4(A, nx, ny, nz);
-          const float muK = visc_mu(p, VK.T);
-          float mutK = mut_prev, F1K = F1_prev, mutR = Sc.mut, F1R = Sc.F1;
+          T GL[NGC], GR[NGC], Fv[TURB ? 6 : 4];
+          const ViscCell<T> VK = visc_cell<TURB>(ring + slot(k - 1) * plane + r * RW + cc, VS, Rg, tgrad(i, j, k - 1));
+          const R4<T> cK = ld_cell4(a, pidx(d, i, j, k - 1), T(0));
+          const R4<T> fc = mk4(A, nx, ny, nz);
+          const T muK = visc_mu(p, VK.Tm);
+          T mutK = mut_prev, F1K = F1_prev, mutR = Sc.mut, F1R = Sc.F1;
 #pragma unroll
           for (int m = 0; m < NGC; ++m) { GL[m] = Gprev[m]; GR[m] = Gc[m]; }
           if (k - 1 == 0 && p.id[4] < 0) {
             visc_gbc<NGV>(p, 4, Gc, Vc, VK, cown.x, fc, GL);
             if constexpr (TURB)
-              sst_ghost(p, 4, VK, muK, GL, __ldg(a.dist32 + pidx(d, i, j, k - 1)), Sc.mut, Sc.F1, mutK, F1K);
+              sst_ghost(p, 4, VK, muK, GL, ld_dist(a, pidx(d, i, j, k - 1), T(0)), Sc.mut, Sc.F1, mutK, F1K);
           }
           if (k == d.kmx && p.id[5] < 0) {
             visc_gbc<NGV>(p, 5, Gprev, VK, Vc, cK.x, fc, GR);
@@ -1276,16 +1356,18 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
             T s = lami_lo_prev + lamj_lo_prev + lamk_prev + lami_hi_prev + lamj_hi_prev + lamk;
             dtc = (T(1) / s) * vol_c * pv<T>(a.CFL, a.f_CFL);
             if constexpr (VISC) {  // add_viscous_time (time.f90:366-448)
-              float sv = lvi_lo_prev + lvj_lo_prev + lvk_prev + lvi_hi_prev + lvj_hi_prev + lvk;
-              sv = p.f_gm * sv / p.f_Pr;
-              sv = 2.0f / (sv + (2.0f * a.f_CFL * vol_c / dtc));
-              dtc = a.f_CFL * (sv * vol_c);
+              const T cfl = pv<T>(a.CFL, a.f_CFL);
+              T sv = lvi_lo_prev + lvj_lo_prev + lvk_prev + lvi_hi_prev + lvj_hi_prev + lvk;
+              sv = pv<T>(p.gm, p.f_gm) * sv / pv<T>(p.Pr, p.f_Pr);
+              sv = T(2) / (sv + (T(2) * cfl * vol_c / dtc));
+              dtc = cfl * (sv * vol_c);
             }
             if constexpr (TURB) {  // add_turbulent_time (time.f90:450-531)
-              float st = lti_lo_prev + ltj_lo_prev + ltk_prev + lti_hi_prev + ltj_hi_prev + ltk;
-              st = p.f_gm * st / p.f_tPr;
-              st = 2.0f / (st + (2.0f * a.f_CFL * vol_c / dtc));
-              dtc = a.f_CFL * (st * vol_c);
+              const T cfl = pv<T>(a.CFL, a.f_CFL);
+              T st = lti_lo_prev + ltj_lo_prev + ltk_prev + lti_hi_prev + ltj_hi_prev + ltk;
+              st = pv<T>(p.gm, p.f_gm) * st / pv<T>(p.tPr, p.f_tPr);
+              st = T(2) / (st + (T(2) * cfl * vol_c / dtc));
+              dtc = cfl * (st * vol_c);
             }
             a.dt[ci] = to_f64(dtc);
           } else {
@@ -1302,7 +1384,7 @@ __device__ __forceinline__ void stage_body(const Params& p, const StageArgs& a, 
           const long long m0 = (long long)(i + 2) + (long long)a.mpitch * ((j + 2) + (long long)d.nj * (kc + 2));
           bool ok;
           if constexpr (kTma) ok = update_cell_f32<NV>(p, a, c0, ci, R, dtc, vol_c, qo, m0, F1_prev);
-          else ok = update_cell(p, a, c0, ci, R, dtc, vol_c, qo, m0);
+          else ok = update_cell<NV>(p, a, c0, ci, R, dtc, vol_c, qo, m0, F1_prev);
           if (!ok) raise_error(a.err, FEST_ERR_NEGATIVE_STATE);
         }
       }
@@ -1388,7 +1470,7 @@ __global__ void __launch_bounds__(TX* TY, TURB ? 1 : (VISC ? 2 : (sizeof(T) == 4
 template <typename T, bool VISC = false, bool TURB = false> inline size_t stage_smem() {
   constexpr size_t NV = TURB ? 7 : 5, NXV = VISC ? (TURB ? 18 + 4 : 12 + 1) : 0;
   return sizeof(T) * ((size_t)RingGeom<T>::N * NV * SH * RingGeom<T>::W + 2 * NV * TY * TX + TY * TX) +
-         sizeof(float) * NXV * TY * TX + sizeof(uint64_t) * RingGeom<T>::N + 16;
+         sizeof(T) * NXV * TY * TX + sizeof(uint64_t) * RingGeom<T>::N + 16;
 }
 
 
@@ -1398,6 +1480,17 @@ template <typename T, bool VISC = false, bool TURB = false> inline size_t stage_
 #define FEST_STAGE_LAUNCHER(name)                                                         \
   int name(int prec, int flux, int occ, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a, \
            const CUtensorMap& tm)
+// the FP64 viscous and SST sweeps (fest_stage_<method>_visc64.cu, _sst64.cu)
+FEST_STAGE_LAUNCHER(launch_stage_none_visc64);
+FEST_STAGE_LAUNCHER(launch_stage_muscl_visc64);
+FEST_STAGE_LAUNCHER(launch_stage_ppm_visc64);
+FEST_STAGE_LAUNCHER(launch_stage_weno_visc64);
+FEST_STAGE_LAUNCHER(launch_stage_weno_nm_visc64);
+FEST_STAGE_LAUNCHER(launch_stage_none_sst64);
+FEST_STAGE_LAUNCHER(launch_stage_muscl_sst64);
+FEST_STAGE_LAUNCHER(launch_stage_ppm_sst64);
+FEST_STAGE_LAUNCHER(launch_stage_weno_sst64);
+FEST_STAGE_LAUNCHER(launch_stage_weno_nm_sst64);
 // the SST FP32 sweeps (fest_stage_<method>_sst.cu)
 FEST_STAGE_LAUNCHER(launch_stage_none_sst);
 FEST_STAGE_LAUNCHER(launch_stage_muscl_sst);
@@ -1475,23 +1568,25 @@ int launch_stage_t(int prec, int flux, int occ, dim3 grid, cudaStream_t s, const
   return FEST_OK;
 }
 
-// the laminar-viscous FP32 sweep (one register budget: 1 CTA of 256 threads
-// per 64K registers would waste the SM, so MB = 2 with what spills)
-template <int INTERP>
+// the laminar-viscous sweep: FP32 with one register budget (1 CTA of 256
+// threads per 64K registers would waste the SM, so MB = 2 with what
+// spills); FP64 one CTA per SM
+template <int INTERP, typename T = float>
 int launch_stage_visc_t(int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a,
                         const CUtensorMap& tm) {
   using namespace stage;
+  constexpr int MB = sizeof(T) == 4 ? 2 : 1;
   const dim3 blk(TX, TY);
   static bool attrs = false;
-  const size_t smem = stage_smem<float, true>();
+  const size_t smem = stage_smem<T, true>();
 #define FEST_SET(F) \
-  cudaFuncSetAttribute(k_stage<float, INTERP, F, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+  cudaFuncSetAttribute(k_stage<T, INTERP, F, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
   if (!attrs) {
     FEST_SET(0); FEST_SET(1); FEST_SET(2); FEST_SET(3); FEST_SET(4); FEST_SET(5);
     attrs = true;
   }
 #undef FEST_SET
-#define FEST_GO(F) k_stage<float, INTERP, F, 2, true><<<grid, blk, smem, s>>>(p, a, tm)
+#define FEST_GO(F) k_stage<T, INTERP, F, MB, true><<<grid, blk, smem, s>>>(p, a, tm)
   switch (flux) {
     case 0: FEST_GO(0); break;
     case 1: FEST_GO(1); break;
@@ -1505,24 +1600,25 @@ int launch_stage_visc_t(int flux, dim3 grid, cudaStream_t s, const Params& p, co
   return FEST_OK;
 }
 
-// the SST FP32 sweep: seven variables and the SST exchange need ~118 KB
-// of shared memory, so one CTA per SM with the whole register file
-template <int INTERP>
+// the SST sweep: seven variables and the SST exchange need ~118 KB (FP32)
+// or ~197 KB (FP64) of shared memory, so one CTA per SM with the whole
+// register file
+template <int INTERP, typename T = float>
 int launch_stage_sst_t(int flux, dim3 grid, cudaStream_t s, const Params& p, const StageArgs& a,
                        const CUtensorMap& tm) {
   using namespace stage;
   const dim3 blk(TX, TY);
   static bool attrs = false;
-  const size_t smem = stage_smem<float, true, true>();
-#define FEST_SET(F)                                                                                          \
-  cudaFuncSetAttribute(k_stage<float, INTERP, F, 1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+  const size_t smem = stage_smem<T, true, true>();
+#define FEST_SET(F)                                                                                      \
+  cudaFuncSetAttribute(k_stage<T, INTERP, F, 1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                        (int)smem)
   if (!attrs) {
     FEST_SET(0); FEST_SET(1); FEST_SET(2); FEST_SET(3); FEST_SET(4); FEST_SET(5);
     attrs = true;
   }
 #undef FEST_SET
-#define FEST_GO(F) k_stage<float, INTERP, F, 1, true, true><<<grid, blk, smem, s>>>(p, a, tm)
+#define FEST_GO(F) k_stage<T, INTERP, F, 1, true, true><<<grid, blk, smem, s>>>(p, a, tm)
   switch (flux) {
     case 0: FEST_GO(0); break;
     case 1: FEST_GO(1); break;

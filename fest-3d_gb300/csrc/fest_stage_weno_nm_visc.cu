@@ -5,7 +5,7 @@
 
 namespace fest {
 FEST_STAGE_LAUNCHER(launch_stage_weno_nm_visc) {
-  (void)prec;
+  if (prec == FEST_FP64) return launch_stage_weno_nm_visc64(prec, flux, occ, grid, s, p, a, tm);
   (void)occ;
   return launch_stage_visc_t<FEST_INTERP_WENO_NM>(flux, grid, s, p, a, tm);
 }

@@ -4,7 +4,7 @@
 
 namespace fest {
 FEST_STAGE_LAUNCHER(launch_stage_weno_sst) {
-  (void)prec;
+  if (prec == FEST_FP64) return launch_stage_weno_sst64(prec, flux, occ, grid, s, p, a, tm);
   (void)occ;
   return launch_stage_sst_t<FEST_INTERP_WENO>(flux, grid, s, p, a, tm);
 }

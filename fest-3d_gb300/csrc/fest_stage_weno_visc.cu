@@ -5,7 +5,7 @@
 
 namespace fest {
 FEST_STAGE_LAUNCHER(launch_stage_weno_visc) {
-  (void)prec;
+  if (prec == FEST_FP64) return launch_stage_weno_visc64(prec, flux, occ, grid, s, p, a, tm);
   (void)occ;
   return launch_stage_visc_t<FEST_INTERP_WENO>(flux, grid, s, p, a, tm);
 }

@@ -66,16 +66,27 @@ def bump_nodes(ext, x0=-1.5, x1=1.5, top=0.8, stretch=1.02, depth=0.1):
     return set_interior_nodes(empty_nodes(ext), X, Y, Z)
 
 
-def plate_nodes(ext, length=2.0, dy1=1e-6, stretch=1.12, height=1.0, depth=0.01):
-    """Flat plate x in [0, length] clustered at the leading edge; wall-normal
-    first cell dy1 growing geometrically by stretch, capped at height."""
-    imx, jmx, kmx = ext.imx, ext.jmx, ext.kmx
-    x = length * np.linspace(0.0, 1.0, imx) ** 1.5
-    dy = dy1 * stretch ** np.arange(jmx - 1)
+def wall_spacing(n, dy1=1e-6, stretch=1.12, height=1.0):
+    """Wall-normal node coordinates of n cells: the first cell dy1, each next
+    one stretch times longer, the growth capped at the spacing that puts the
+    last node at height (geometric near the wall, uniform beyond)."""
+    def top(cap):
+        return np.minimum(dy1 * stretch ** np.arange(n), cap).sum()
+    lo, hi = dy1, height
+    for _ in range(200):  # bisection on the cap
+        mid = 0.5 * (lo + hi)
+        if top(mid) < height:
+            lo = mid
+        else:
+            hi = mid
+    dy = np.minimum(dy1 * stretch ** np.arange(n), 0.5 * (lo + hi))
     y = np.concatenate([[0.0], np.cumsum(dy)])
-    if y[-1] > height:
-        y = y * (height / y[-1])
-    z = np.linspace(0.0, depth, kmx)
+    return y * (height / y[-1])  # the cap's last bit; dy1 moves by ~1e-12 relative
+
+
+def plate_block_nodes(ext, x, y, depth):
+    """Cartesian block of node lines x, y and kmx nodes over depth in z."""
+    z = np.linspace(0.0, depth, ext.kmx)
     X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
     return set_interior_nodes(empty_nodes(ext), X, Y, Z)
 
@@ -169,12 +180,19 @@ def bump_case(nc=(256, 96, 4), mach=0.5):
                 scheme=scheme, bc=bc, nodes=nodes, qp=qp, CFL=0.8)
 
 
-def plate_case(nc=(192, 128, 1), mach=0.2, Re_per_m=5e6, Tu=0.1, mut_ratio=0.01):
-    """Turbulent flat plate with k-omega SST: 192x128x1 cells (kmx=2), one
-    block whose jmin face is the no-slip adiabatic plate (-5); subsonic inlet
-    (-3) with free-stream k/omega, outlets (-4) at imax and jmax, slip k
-    faces (-6); MUSCL + AUSM-UP, RK4, CFL 1.0."""
-    ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 7)
+def plate_case(n_run=32, n_plate=160, nj=128, nk=2, mach=0.2, Re_per_m=5e6, Tu=0.1, mut_ratio=0.01,
+               run_in=0.33, length=2.0, depth=0.01):
+    """Turbulent zero-pressure-gradient flat plate with k-omega SST, laid out
+    as the reference's own Tfp case (tests/Tfp/system/mesh/layout): block 0
+    the symmetry run-in x in [-0.33, 0] (far field -8 at imin, symmetry -6
+    below), block 1 the plate x in [0, 2] (no-slip adiabatic wall -5 below,
+    outlet -4 at imax), joined by an interface (block 0's imax = block 1's
+    imin), slip top and k faces (-6).  192x128x2 cells in all (32 + 160 in
+    i); first wall-normal cell 1e-6 m, stretched by 1.12 up to the spacing
+    that reaches the 1 m top; nodes clustered at the leading edge.  Mach
+    0.2, Re 5e6 per metre, Tu 0.1%, mu_t/mu 0.01; MUSCL + AUSM-UP, RK4,
+    local time steps, CFL 1.0.  Returns dict(name, blocks=[per-block dicts
+    of ext, flow, scheme, bc, nodes, qp], wall, CFL)."""
     p0, T0, gm, R = 101325.0, 300.0, 1.4, 287.0
     rho0 = p0 / (R * T0)
     c = np.sqrt(gm * p0 / rho0)
@@ -189,16 +207,28 @@ def plate_case(nc=(192, 128, 1), mach=0.2, Re_per_m=5e6, Tu=0.1, mut_ratio=0.01)
     fixed = {k: [0.0] * 6 for k in ("fixed_density", "fixed_x_speed", "fixed_y_speed",
                                     "fixed_z_speed", "fixed_pressure", "fixed_tk", "fixed_tw",
                                     "fixed_wall_temperature")}
-    fixed["fixed_density"][0] = rho0
-    fixed["fixed_x_speed"][0] = U
-    fixed["fixed_tk"][0] = tk
-    fixed["fixed_tw"][0] = tw
-    fixed["fixed_pressure"][1] = p0
-    bc = abi.make_bc([-3, -4, -5, -4, -6, -6], **fixed)
-    nodes = plate_nodes(ext)
-    qp = uniform_state(ext, flow, tk=tk, tw=tw)
-    return dict(name="SST flat plate 192x128x1, MUSCL+AUSM-UP, RK4", ext=ext, flow=flow,
-                scheme=scheme, bc=bc, nodes=nodes, qp=qp, CFL=1.0)
+    for f in range(6):
+        fixed["fixed_density"][f] = rho0
+        fixed["fixed_x_speed"][f] = U
+        fixed["fixed_pressure"][f] = p0
+        fixed["fixed_tk"][f] = tk
+        fixed["fixed_tw"][f] = tw
+    y = wall_spacing(nj, height=1.0)
+    s_run = np.linspace(0.0, 1.0, n_run + 1)
+    s_pl = np.linspace(0.0, 1.0, n_plate + 1)
+    x_run = -run_in * (1.0 - s_run) ** 1.5
+    x_pl = length * s_pl ** 1.5
+    blocks = []
+    for b, (x, ids, partners) in enumerate(((x_run, [-8, 1, -6, -6, -6, -6], {1: (1, 0)}),
+                                            (x_pl, [0, -4, -5, -6, -6, -6], {0: (0, 1)}))):
+        ext = abi.Extent(len(x), nj + 1, nk + 1, 7)
+        bc = abi.make_bc(ids, partners=partners, block_id=b, **fixed)
+        blocks.append(dict(ext=ext, flow=flow, scheme=scheme, bc=bc,
+                           nodes=plate_block_nodes(ext, x, y, depth),
+                           qp=uniform_state(ext, flow, tk=tk, tw=tw)))
+    wall = wall_nodes_of(blocks[1]["nodes"], blocks[1]["ext"], blocks[1]["bc"])
+    return dict(name=f"SST flat plate {n_run + n_plate}x{nj}x{nk} (run-in {n_run} + plate {n_plate}), "
+                     "MUSCL+AUSM-UP, RK4", blocks=blocks, wall=wall, CFL=1.0, flow=flow)
 
 
 def wall_nodes_of(nodes, ext, bc):

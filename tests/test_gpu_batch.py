@@ -1,5 +1,6 @@
 """Batched multiblock stepping (fest_batch_*): one ghost launch and one sweep
-launch per stage for all blocks.
+launch per stage for all blocks (or, when the blocks share no sweep kernel,
+each block's own launches stage by stage).
 
 The batched sweep runs the same per-CTA code as the single-block sweep, so
 every block's state must equal, bit for bit, the state its own handle
@@ -83,10 +84,29 @@ def test_batch_follows_oracle(gpu_lib, viscous):
             assert e <= 2e-5, (n, l, e, (ext.imx - 1, ext.jmx - 1, ext.kmx - 1))
 
 
-def test_batch_rejects_mixed_schemes(gpu_lib):
+def test_batch_of_different_schemes_steps_block_by_block(gpu_lib):
+    """blocks with different flux schemes share no sweep kernel: the batch
+    launches each block's own sweeps, stage by stage, which gives the states
+    stepping them alone gives; different integrators share no stages and are
+    refused"""
     blocks = small_blocks(n=2)
     blocks[1]["scheme"] = abi.make_scheme(scheme_name="slau", interpolant="muscl",
                                           time_step_accuracy="TVDRK3", time_stepping_method="l")
+    single = [handle_of(c, gpu_lib) for c in blocks]
+    batched = [handle_of(c, gpu_lib) for c in blocks]
+    b = make_batch(gpu_lib, batched)
+    try:
+        for h, c in zip(single, blocks):
+            h.step(6, 1, c["CFL"], with_norm=False)
+        abi.check(gpu_lib.fest_batch_step(b, 6, 1, 0.5), "fest_batch_step")
+        for n, (hs, hb) in enumerate(zip(single, batched)):
+            ext = blocks[n]["ext"]
+            sl = (slice(3, ext.imx + 2), slice(3, ext.jmx + 2), slice(3, ext.kmx + 2))
+            assert np.array_equal(hs.download_state()[sl], hb.download_state()[sl]), f"block {n} differs"
+    finally:
+        gpu_lib.fest_batch_destroy(b)
+    blocks[1]["scheme"] = abi.make_scheme(scheme_name="slau", interpolant="muscl",
+                                          time_step_accuracy="RK4", time_stepping_method="l")
     hs = [handle_of(c, gpu_lib) for c in blocks]
     arr = (C.c_void_p * 2)(*[h.h.value for h in hs])
     b = C.c_void_p()

@@ -15,7 +15,12 @@ oracle on the same inputs.
   field-wise (every interior cell, every variable) against the oracle's
   2000 iterations, FP64 within 1e-9 and mixed precision within 2e-5 of
   each variable's magnitude.  The cavity starts at rest, so its velocities
-  are judged against the lid speed."""
+  are judged against the lid speed.
+* Turbulent flat plate with k-omega SST, 192x128x2 cells as two blocks (the
+  0.33 m symmetry run-in and the 2 m plate, joined by an interface, the
+  reference's own Tfp layout), first cell 1e-6 m: both blocks in one batch,
+  FP64 within 1e-11 after three RK4 iterations and mixed precision within
+  2e-5 after six, against the oracle's two-block run."""
 import numpy as np
 import pytest
 
@@ -104,3 +109,57 @@ def test_cavity_64x64x4_all_2000_iterations(gpu_lib, precision):
     e, errs = _field_err(q, ref, ext, scale)
     assert e <= tol, f"cavity after {iters} iterations differs by {errs} (tolerance {tol})"
     h.close()
+
+
+def _plate_handles(lib, case, precision):
+    from fest3d.handle import Handle
+    hs = []
+    for b in case["blocks"]:
+        h = Handle(b["ext"], b["flow"], b["scheme"], b["bc"], lib=lib)
+        h.setup_geometry(b["nodes"])
+        h.find_wall_dist(case["wall"])
+        h.upload_state(b["qp"])
+        h.set_precision(precision)
+        hs.append(h)
+    return hs
+
+
+@pytest.mark.parametrize("precision", [abi.FEST_FP64, abi.FEST_MIXED], ids=["fp64", "mixed"])
+def test_sst_plate_two_blocks_192x128x2(gpu_lib, precision):
+    import ctypes as C
+    case = cases.plate_case()
+    iters = 3 if precision == abi.FEST_FP64 else 6
+    tol = 1e-11 if precision == abi.FEST_FP64 else 2e-5
+    hs = _plate_handles(gpu_lib, case, precision)
+    arr = (C.c_void_p * 2)(*[h.h.value for h in hs])
+    b = C.c_void_p()
+    abi.check(gpu_lib.fest_batch_create(arr, 2, C.byref(b)), "fest_batch_create")
+    try:
+        abi.check(gpu_lib.fest_batch_step(b, iters, 1, case["CFL"]), "fest_batch_step")
+        blks = []
+        for blk in case["blocks"]:
+            o = O.Block(blk["ext"], blk["flow"], blk["scheme"], blk["bc"])
+            o["nodes"] = blk["nodes"]
+            o.setup_geometry()
+            o.find_wall_dist(case["wall"])
+            o["qp"] = blk["qp"]
+            blks.append(o)
+        _oracle_run_blocks(blks, iters, case["CFL"])
+        flow = case["flow"]
+        for n, (h, o) in enumerate(zip(hs, blks)):
+            ext = h.ext
+            ref = post.interior(o["qp"], ext)
+            V = flow.vel_mag
+            scale = [np.abs(ref[..., 0]).max(), V, V, V, np.abs(ref[..., 4]).max(),
+                     np.abs(ref[..., 5]).max(), np.abs(ref[..., 6]).max()]
+            e, errs = _field_err(h.download_state(), o["qp"], ext, scale)
+            assert e <= tol, f"plate block {n} after {iters} iterations differs by {errs}"
+    finally:
+        gpu_lib.fest_batch_destroy(b)
+        for h in hs:
+            h.close()
+
+
+def _oracle_run_blocks(blocks, n, CFL):
+    for it in range(1, n + 1):
+        assert O.get_next_solution(blocks, it, CFL) == 0

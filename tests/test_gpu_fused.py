@@ -14,7 +14,7 @@ import pytest
 
 import oracle as O
 from fest3d import abi, cases
-from parity import make_pair, rel_err, small_case
+from parity import assert_residual, make_pair, rel_err, small_case
 
 pytestmark = pytest.mark.gpu
 
@@ -35,9 +35,9 @@ COMBOS = {
 }
 
 
-# laminar viscous terms run in the FP32 sweep only (FP64 viscous blocks take
-# the module path); the FP32 sweep evaluates the temperature gradient from the
-# current stage's state where the reference uses the iteration's first
+# laminar viscous terms: the FP32 sweep evaluates the temperature gradient
+# from the current stage's state where the reference (and the FP64 sweep)
+# uses the iteration's first
 VISC_COMBOS = {
     "lam-muscl-ausm-cavity": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ausm"),
                                   ids=(-5, -5, -5, -3, -10, -10),
@@ -149,24 +149,35 @@ def test_fused_mixed_sst(gpu_lib, name, acc):
 
 def test_fused_mixed_sst_single_plane(gpu_lib):
     """a flat-plate-like single-plane block (kmx = 2, slip k faces): the
-    mixed sweep reads ghost layer 1 only, so it runs where the FP64 fused
-    path needs the in-place module path"""
+    mixed sweep reads ghost layer 1 only, and makes the symmetric faces'
+    ghosts in the reference's face order"""
     ext, blk, h, q, norm = run_sst_pair("sst-muscl-ausmUP", "RK4", abi.FEST_MIXED, nc=(40, 9, 1),
                                         ids=(-3, -4, -5, -4, -6, -6))
     e = rel_err(interior(q, ext), interior(blk["qp"], ext))
     assert e <= 2e-5, f"mixed SST single-plane interior state differs by {e:.3e}"
 
 
-def test_fp64_sst_takes_module_path(gpu_lib):
-    """FP64 SST blocks step through the module kernels: exact."""
-    ext, blk, h, q, norm = run_sst_pair("sst-muscl-ausmUP", "RK4", abi.FEST_FP64, iters=3)
-    assert rel_err(q, blk["qp"]) <= 1e-11
+@pytest.mark.parametrize("name", list(VISC_COMBOS))
+@pytest.mark.parametrize("acc", ["none", "TVDRK3", "RK4"])
+def test_fused_fp64_viscous(gpu_lib, name, acc):
+    """FP64 laminar blocks in the fused sweep: the gradients take the
+    temperature of the iteration's start, as the reference's do"""
+    ext, blk, h, q, norm = run_pair(name, acc, abi.FEST_FP64, iters=3)
+    e = rel_err(interior(q, ext), interior(blk["qp"], ext))
+    assert e <= 1e-11, f"fused FP64 viscous interior state differs by {e:.3e}"
+    assert_residual(h.get("residue"), blk, rtol=1e-12, what="fused FP64 viscous residual")
+    ref = O.find_resnorm([blk])
+    assert np.allclose(norm, ref, rtol=1e-9, atol=1e-300), (norm, ref)
 
 
-def test_fp64_viscous_takes_module_path(gpu_lib):
-    """FP64 viscous blocks step through the module kernels: exact."""
-    ext, blk, h, q, norm = run_pair("suth-weno-slau", "TVDRK3", abi.FEST_FP64)
-    assert rel_err(q, blk["qp"]) <= 1e-11
+@pytest.mark.parametrize("name", list(SST_COMBOS))
+@pytest.mark.parametrize("acc", ["none", "TVDRK3", "RK4"])
+def test_fused_fp64_sst(gpu_lib, name, acc):
+    """FP64 k-omega SST blocks in the fused sweep"""
+    ext, blk, h, q, norm = run_sst_pair(name, acc, abi.FEST_FP64, iters=3)
+    e = rel_err(interior(q, ext), interior(blk["qp"], ext))
+    assert e <= 1e-11, f"fused FP64 SST interior state differs by {e:.3e}"
+    assert_residual(h.get("residue"), blk, rtol=1e-12, what="fused FP64 SST residual")
 
 
 @pytest.mark.parametrize("nc,ids,acc,mixed_runs", [((40, 9, 1), (-3, -4, -6, -5, -6, -6), "RK4", True),
