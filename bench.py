@@ -294,11 +294,15 @@ def large_block_roofline(lib, abi, cases, Handle, peak, flush, nc=(1024, 384, 64
 
 def adjoint_cost(lib, reps=20):
     """Adjoint/primal cost on the adjoint workload (bump 128x48x4, Euler,
-    unlimited MUSCL + SLAU, FP64): one fest_residual_vjp against one
-    fest_get_total_conservative_residue, both through the C ABI with their
-    host arrays (state in; residual out / lambda in, dq out), wall clock."""
+    unlimited MUSCL + SLAU, FP64): the device time (CUDA events around the
+    kernels of the call, fest_last_kernel_ms) of one fest_residual_vjp
+    against one primal residual evaluation: the reference's
+    get_total_conservative_Residue (fest_get_total_conservative_residue:
+    ghosts, face states, fluxes, residue) and, beside it, one stage of the
+    fused FP64 sweep (residual, time step and update in one kernel).  The
+    calls' wall clock with their host transfers is reported too."""
     import numpy as np
-    from fest3d import adjoint as A
+    from fest3d import abi, adjoint as A
     try:
         case = A.adjoint_case()
         h = A.make_handle(case, lib=lib)
@@ -306,20 +310,43 @@ def adjoint_cost(lib, reps=20):
         ext = case["ext"]
         lam = np.asfortranarray(np.random.default_rng(0).standard_normal(
             (ext.imx - 1, ext.jmx - 1, ext.kmx - 1, 5)))
+        ms = C.c_double()
+
+        def dev():
+            abi.check(lib.fest_last_kernel_ms(h.h, C.byref(ms)), "fest_last_kernel_ms")
+            return ms.value
+
         h.residual(q, 3)
         h.residual_vjp(q, 3, lam)
-        t0 = time.perf_counter()
+        tp = ta = dp = da = 0.0
         for _ in range(reps):
+            t0 = time.perf_counter()
             h.residual(q, 3)
-        tp = (time.perf_counter() - t0) / reps
-        t0 = time.perf_counter()
-        for _ in range(reps):
+            tp += time.perf_counter() - t0
+            dp += dev()
+            t0 = time.perf_counter()
             h.residual_vjp(q, 3, lam)
-        ta = (time.perf_counter() - t0) / reps
+            ta += time.perf_counter() - t0
+            da += dev()
+        tp, ta, dp, da = tp / reps, ta / reps, dp / reps, da / reps
+        # one stage of the fused FP64 sweep on the same state
+        h.upload_state(q)
+        h.set_precision(abi.FEST_FP64)
+        h.step(3, 1, case["CFL"], with_norm=False)
+        abi.check(lib.fest_profile(h.h, 1), "profile")
+        h.step(reps, 4, case["CFL"], with_norm=False)
+        nl, tot = C.c_longlong(), C.c_double()
+        abi.check(lib.fest_profile_read(h.h, C.byref(nl), C.byref(tot)), "profile_read")
+        abi.check(lib.fest_profile(h.h, 0), "profile off")
+        stage_ms = tot.value / max(nl.value, 1)
         h.close()
         return {"workload": "bump 128x48x4, Euler, MUSCL (unlimited) + SLAU, FP64",
-                "primal_residual_ms": tp * 1e3, "vjp_ms": ta * 1e3, "adjoint_over_primal": ta / tp,
-                "timing": "wall clock per C-ABI call incl. host transfers, mean of %d" % reps}
+                "vjp_device_ms": da, "primal_residual_device_ms": dp, "fused_stage_device_ms": stage_ms,
+                "adjoint_over_primal": da / dp, "adjoint_over_fused_stage": da / stage_ms,
+                "timing": "CUDA events around each call's kernels on the handle's stream (fest_last_kernel_ms), "
+                          "mean of %d; fused stage: event pair per sweep launch" % reps,
+                "wall_clock_ms": {"primal_residual": tp * 1e3, "vjp": ta * 1e3,
+                                  "note": "per C-ABI call, host transfers included"}}
     except Exception as e:
         return {"error": str(e)}
 
@@ -508,6 +535,17 @@ def run_ours(args):
     tot_e2e = max_over_ranks(tot_e2e, dist, "cuda")
     e2e_rate = replica_rate(N * STAGES, e2e_steps, ws, tot_e2e)
     nbytes = int(qhost.nbytes)
+    # the host link alone: upload and download of the state, each synchronous
+    tu = td = 0.0
+    for _ in range(10):
+        t0 = time.perf_counter()
+        abi.check(lib.fest_upload_state(he.h, ptr), "upload")
+        tu += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        abi.check(lib.fest_download_state(he.h, ptr), "download")
+        td += time.perf_counter() - t0
+    link = {"h2d_gbs": 10 * nbytes / tu / 1e9, "d2h_gbs": 10 * nbytes / td / 1e9,
+            "upload_us": tu / 10 * 1e6, "download_us": td / 10 * 1e6}
 
     adj = adjoint_cost(lib) if rank == 0 else None
     c2 = c2_report(lib, abi, cases, Handle, args.c2_iters) if rank == 0 and args.c2_iters > 1 else None
@@ -549,7 +587,8 @@ def run_ours(args):
             "clocks": mixed["clocks"],
             "e2e": {"value": e2e_rate, "unit": "Mcell-residuals/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes,
-                    "path": "fest_upload_state + fest_step + fest_download_state, pinned host buffer"},
+                    "path": "fest_upload_state + fest_step + fest_download_state, pinned host buffer",
+                    "host_link": link},
             "gpu_launches": int(mixed["launches"]),
             "cpu_baseline": cpu,
         }
@@ -703,9 +742,9 @@ def run_batch(args):
 def run_cavity(args):
     """Laminar lid-driven cavity (64x64x4 cells, MUSCL + AUSM, forward Euler,
     local dt, CFL 0.5, constant mu for Re 100): ITERS iterations in mixed
-    precision (the fused FP32 sweep with its viscous terms) and in FP64 (the
-    module kernels), wall times and the u-velocity difference along the
-    vertical centre line, relative to the lid speed."""
+    precision and in FP64 (the fused sweeps with their viscous terms), wall
+    times and the u-velocity difference along the vertical centre line,
+    relative to the lid speed."""
     import numpy as np
     import torch
     torch.cuda.set_device(0)

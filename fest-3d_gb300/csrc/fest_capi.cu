@@ -2,6 +2,7 @@
 // movement of the reference's Fortran-layout arrays, and the module-level
 // and integrator entry points built from the module kernels.
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -33,7 +34,11 @@ struct fest_handle {
   double* d_vjp_bar = nullptr;  // adjoint work arrays, allocated on first use
   double* d_vjp_lam = nullptr;
   double* d_vjp_grad = nullptr;  // laminar adjoint: 12 per interior cell
+  double* d_lu = nullptr;        // LU-SGS work arrays, allocated on first use
   int* h_err = nullptr;          // pinned host copy of the device error word
+  // events around the device work of the last timed call (after its inputs
+  // arrived, before its outputs leave): fest_last_kernel_ms
+  cudaEvent_t kev[2] = {nullptr, nullptr};
   std::vector<void*> allocs;
   Launcher L() { return Launcher{s, &launches}; }
 };
@@ -81,13 +86,53 @@ Sizes sizes_of(const Dims& d, int n_grad) {
   return z;
 }
 
+// Host arrays that are pinned and mapped (cudaHostAlloc, a framework's
+// pinned-memory pool): the GPU reads and writes them itself, every SM
+// streaming 16-byte words over the CPU-GPU link.  Other host memory, and
+// arrays below 1 MiB (where the copy engine's latency is shorter), go
+// through cudaMemcpyAsync.
+__global__ void k_link_copy(const double* __restrict__ src, double* __restrict__ dst, long long n) {
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+  if ((((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
+    const long long n2 = n / 2;
+    const double2* s2 = reinterpret_cast<const double2*>(src);
+    double2* d2 = reinterpret_cast<double2*>(dst);
+    for (long long t = t0; t < n2; t += st) d2[t] = s2[t];
+    if (t0 == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+  } else {
+    for (long long t = t0; t < n; t += st) dst[t] = src[t];
+  }
+}
+// the device address of a pinned, mapped host array, or null
+const void* mapped_alias(const void* host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+constexpr long long kLinkMin = 1 << 17;  // doubles
+int link_copy(fest_handle* h, const double* src, double* dst, long long n) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_link_copy<<<sms * 4, 256, 0, h->s>>>(src, dst, n);
+  ++h->launches;
+  CK(cudaGetLastError());
+  return FEST_OK;
+}
 int up(fest_handle* h, double* dst, const double* src, long long n) {
   if (!src) return FEST_OK;
+  if (n >= kLinkMin)
+    if (const void* a = mapped_alias(src)) return link_copy(h, static_cast<const double*>(a), dst, n);
   CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, h->s));
   return FEST_OK;
 }
 int down(fest_handle* h, double* dst, const double* src, long long n) {
   if (!dst) return FEST_OK;
+  if (n >= kLinkMin)
+    if (const void* a = mapped_alias(dst)) return link_copy(h, src, static_cast<double*>(const_cast<void*>(a)), n);
   CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->s));
   return FEST_OK;
 }
@@ -218,6 +263,11 @@ long long arr_size(const fest_handle* h, int which) {
   }
 }
 
+// mark the start (0) or end (1) of a call's device work on the handle's stream
+void kmark(fest_handle* h, int which) {
+  if (h->kev[which]) cudaEventRecord(h->kev[which], h->s);
+}
+
 // a handle whose interface faces pair with other blocks fills its ghosts
 // only inside a batch (fest_batch_create resolves the partners)
 bool needs_batch(const fest_handle* h) {
@@ -238,11 +288,12 @@ __global__ void k_fill(double* x, long long n, double v) {
   if (t < n) x[t] = v;
 }
 
-// get_total_conservative_Residue (update.f90:495-547) on the resident state
-int residual_fp64(fest_handle* h, int iter) {
-  const Params& p = h->p;
+// get_total_conservative_Residue (update.f90:495-547) on the resident state;
+// p and tab: the block's parameters and the block table its interface
+// faces read (a batch's, whose part_block indices p holds)
+int residual_module(fest_handle* h, int iter, const Params& p, const BlockRef* tab) {
   Launcher L = h->L();
-  launch_ghosts(p, h->d, h->d_table, iter, L);
+  launch_ghosts(p, h->d, tab, iter, L);
   launch_face_states(p, h->d, 1, L);
   launch_fluxes(p, h->d, L);
   if (p.mu_ref != 0.0) {
@@ -251,6 +302,14 @@ int residual_fp64(fest_handle* h, int iter) {
     launch_viscous_fluxes(p, h->d, L);
   }
   launch_residue(p, h->d, true, L);
+  return FEST_OK;
+}
+int residual_fp64(fest_handle* h, int iter) { return residual_module(h, iter, h->p, h->d_table); }
+
+// update_with_lusgs (lusgs.f90:134-183) on the residue and time step held
+int lusgs_update(fest_handle* h, const Params& p) {
+  if (!h->d_lu) RET(dalloc(h, &h->d_lu, lusgs_scratch_doubles(p.d)));
+  launch_lusgs(p, h->d, h->d_lu, h->L());
   return FEST_OK;
 }
 
@@ -308,6 +367,11 @@ int next_solution_fp64(fest_handle* h, int it, double CFL) {
       residual_fp64(h, it); launch_update(p, h->d, 1.0, 1., 0, 0, L);
       launch_blend(p, h->d, 0.5, 0.5, L);
       break;
+    case FEST_TIME_IMPLICIT:  // update.f90:215-218
+      residual_fp64(h, it);
+      launch_time_step(p, h->d, CFL, L);
+      RET(lusgs_update(h, p));
+      break;
     default:
       return FEST_ERR_ARG;
   }
@@ -329,7 +393,7 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
   if (scheme->scheme_name < 0 || scheme->scheme_name > 5) return FEST_ERR_ARG;
   if (scheme->interpolant < 0 || scheme->interpolant > 4) return FEST_ERR_ARG;
   if (scheme->turbulence < 0 || scheme->turbulence > 2) return FEST_ERR_ARG;
-  if (scheme->time_step_accuracy < 0 || scheme->time_step_accuracy > 4) return FEST_ERR_ARG;
+  if (scheme->time_step_accuracy < 0 || scheme->time_step_accuracy > FEST_TIME_IMPLICIT) return FEST_ERR_ARG;
   if (scheme->time_stepping_method != 'l' && scheme->time_stepping_method != 'g') return FEST_ERR_ARG;
   for (int f = 0; f < 6; ++f) {
     if (!valid_id(bc->id[f])) return FEST_ERR_ARG;
@@ -364,6 +428,10 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
     return FEST_ERR_CUDA;
   }
   h->own = h->s;
+  if (cudaEventCreate(&h->kev[0]) != cudaSuccess || cudaEventCreate(&h->kev[1]) != cudaSuccess) {
+    h->kev[0] = h->kev[1] = nullptr;
+    cudaGetLastError();
+  }
   const Dims& d = h->p.d;
   Sizes z = sizes_of(d, h->p.n_grad);
   DevBlock& b = h->d;
@@ -422,6 +490,8 @@ int fest_destroy(fest_handle* h) {
   for (void* p : h->allocs) cudaFree(p);
   if (h->own) cudaStreamDestroy(h->own);
   if (h->h_err) cudaFreeHost(h->h_err);
+  for (cudaEvent_t e : h->kev)
+    if (e) cudaEventDestroy(e);
   delete h;
   return FEST_OK;
 }
@@ -676,7 +746,9 @@ int fest_get_total_conservative_residue(fest_handle* h, double* qp, int current_
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   RET(up(h, h->d.qp, qp, z.qp));
+  kmark(h, 0);
   RET(residual_fp64(h, current_iter));
+  kmark(h, 1);
   RET(down(h, qp, h->d.qp, z.qp));
   RET(down(h, residue, h->d.res, z.res));
   return finish(h);
@@ -703,9 +775,11 @@ int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const 
   if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
   if (qp) RET(up(h, h->d.qp, qp, z.qp));
   RET(up(h, h->d_vjp_lam, lambda, z.res));
+  kmark(h, 0);
   launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
   RET(viscous_prep(h));
   launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), nullptr, h->d_vjp_grad);
+  kmark(h, 1);
   RET(down(h, dq, h->d_vjp_bar, z.qp));
   return finish(h);
 }
@@ -857,7 +931,9 @@ static int step_enqueue(fest_handle* h, int n_iters, int first_iter, double CFL)
 }
 
 int fest_step(fest_handle* h, int n_iters, int first_iter, double CFL, double* res_abs) {
+  if (h) kmark(h, 0);
   RET(step_enqueue(h, n_iters, first_iter, CFL));
+  kmark(h, 1);
   if (res_abs) return fest_find_resnorm(h, res_abs);
   return finish(h);
 }
@@ -870,6 +946,11 @@ struct fest_batch {
   std::vector<fest_handle*> h;
   std::vector<cudaStream_t> prev;  // each handle's stream before the batch
   FusedBatch* fb = nullptr;
+  // implicit batches (module path): the blocks' parameters with batch
+  // indices for their partners, and the table of every block's state
+  bool implicit = false;
+  std::vector<Params> p;
+  BlockRef* d_tab = nullptr;
 };
 
 int fest_batch_create(fest_handle* const* blocks, int n_blocks, fest_batch** out) {
@@ -879,9 +960,15 @@ int fest_batch_create(fest_handle* const* blocks, int n_blocks, fest_batch** out
   fest_handle* h0 = blocks[0];
   if (!h0) return FEST_ERR_ARG;
   const int prec = h0->precision;
+  const bool implicit = h0->sc.time_step_accuracy == FEST_TIME_IMPLICIT;
   for (int n = 0; n < n_blocks; ++n) {
     fest_handle* h = blocks[n];
-    if (!h || h->precision != prec || !fused_supported(h->p, prec)) return FEST_ERR_ARG;
+    if (!h || h->precision != prec) return FEST_ERR_ARG;
+    if (implicit) {  // LU-SGS: FP64 module path, every block implicit
+      if (prec != FEST_FP64 || h->sc.time_step_accuracy != FEST_TIME_IMPLICIT) return FEST_ERR_ARG;
+    } else if (!fused_supported(h->p, prec)) {
+      return FEST_ERR_ARG;
+    }
   }
   // interface partners as batch indices: the block itself, or the one
   // other handle whose block_id is the face's partner_block
@@ -926,11 +1013,20 @@ int fest_batch_create(fest_handle* const* blocks, int n_blocks, fest_batch** out
     b->h.push_back(h);
     b->prev.push_back(h->s);
     h->s = h0->s;
-    if (!rc && !h->fused) rc = fused_create(h->p, h->d, h->d_table, h->s, &h->fused);
+    if (!implicit && !rc && !h->fused) rc = fused_create(h->p, h->d, h->d_table, h->s, &h->fused);
     f.push_back(h->fused);
     d.push_back(h->d);
   }
-  if (!rc) rc = fused_batch_create(f, p, d, prec, &b->fb);
+  if (!rc && implicit) {
+    b->implicit = true;
+    b->p = p;
+    std::vector<BlockRef> t(n_blocks);
+    for (int n = 0; n < n_blocks; ++n) t[n] = BlockRef{d[n], p[n].d};
+    if (cudaMalloc((void**)&b->d_tab, sizeof(BlockRef) * n_blocks) != cudaSuccess) rc = FEST_ERR_NOMEM;
+    else rc = cuda_status(cudaMemcpy(b->d_tab, t.data(), sizeof(BlockRef) * n_blocks, cudaMemcpyHostToDevice));
+  } else if (!rc) {
+    rc = fused_batch_create(f, p, d, prec, &b->fb);
+  }
   if (rc) {
     fest_batch_destroy(b);
     return rc;
@@ -943,6 +1039,7 @@ int fest_batch_destroy(fest_batch* b) {
   if (!b) return FEST_OK;
   if (!b->h.empty()) cudaStreamSynchronize(b->h[0]->s);
   fused_batch_destroy(b->fb);
+  if (b->d_tab) cudaFree(b->d_tab);
   for (size_t n = 0; n < b->h.size(); ++n) b->h[n]->s = b->prev[n];  // handles get their streams back
   delete b;
   return FEST_OK;
@@ -953,6 +1050,22 @@ int fest_batch_step_async(fest_batch* b, int n_iters, int first_iter, double CFL
   fest_handle* h0 = b->h[0];
   for (fest_handle* h : b->h)
     if (h->s != h0->s || h->precision != h0->precision) return FEST_ERR_ARG;
+  if (b->implicit) {
+    // the blocks in lockstep: every residual (whose ghost fills read the
+    // other blocks' states) before any block's LU-SGS update changes its own
+    const size_t nb = b->h.size();
+    for (int n = 0; n < n_iters; ++n) {
+      const int it = first_iter + n;
+      for (size_t m = 0; m < nb; ++m) RET(sync_fused(b->h[m]));
+      for (size_t m = 0; m < nb; ++m) launch_temperature(b->p[m], b->h[m]->d, b->h[m]->L());
+      for (size_t m = 0; m < nb; ++m) {
+        RET(residual_module(b->h[m], it, b->p[m], b->d_tab));
+        launch_time_step(b->p[m], b->h[m]->d, CFL, b->h[m]->L());
+      }
+      for (size_t m = 0; m < nb; ++m) RET(lusgs_update(b->h[m], b->p[m]));
+    }
+    return FEST_OK;
+  }
   return fused_batch_run(b->fb, n_iters, first_iter, CFL, h0->s, &h0->launches);
 }
 
@@ -980,6 +1093,15 @@ int fest_profile(fest_handle* h, int enable) {
 int fest_profile_read(fest_handle* h, long long* launches, double* total_ms) {
   if (!h || !h->fused) return FEST_ERR_ARG;
   return fused_profile_read(h->fused, launches, total_ms);
+}
+
+int fest_last_kernel_ms(fest_handle* h, double* ms) {
+  if (!h || !ms || !h->kev[0] || !h->kev[1]) return FEST_ERR_ARG;
+  CK(cudaEventSynchronize(h->kev[1]));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, h->kev[0], h->kev[1]));
+  *ms = t;
+  return FEST_OK;
 }
 
 }  // extern "C"

@@ -593,6 +593,65 @@ __device__ __forceinline__ int wall_mask(const Params& p, int dir, int f) {
   return ((f == 1 && wlo) || (f == n && whi)) ? 0 : 1;
 }
 
+// bc_primitive.f90:209-224: the edge and corner ghosts as the mean (0.33
+// times the sum) of their three neighbours, in the reference's order: the
+// i-lines of the j/k edges, the k-lines of the i/j edges, the corners.  The
+// j-lines of the i/k edges are left as they are.  One CTA; q(i, j, k, l)
+// returns the cell of variable l (1-based).
+template <typename T, class Q>
+__device__ void corner_average(const Dims& d, const Q& q) {
+  const int imx = d.imx, jmx = d.jmx, kmx = d.kmx, nv = d.nv;
+  const T c = T(0.33);
+  const int tid = threadIdx.x;
+  const int ni = imx + 5, nk = kmx + 5;
+  for (int s = 0; s < 4; ++s) {
+    for (int t = tid; t < ni * nv; t += blockDim.x) {
+      const int i = -2 + t % ni, l = 1 + t / ni;
+      switch (s) {
+        case 0: q(i, 0, 0, l) = c * (q(i, 1, 1, l) + q(i, 0, 1, l) + q(i, 1, 0, l)); break;
+        case 1: q(i, 0, kmx, l) = c * (q(i, 1, kmx - 1, l) + q(i, 0, kmx - 1, l) + q(i, 1, kmx, l)); break;
+        case 2: q(i, jmx, 0, l) = c * (q(i, jmx - 1, 1, l) + q(i, jmx, 1, l) + q(i, jmx - 1, 0, l)); break;
+        default:
+          q(i, jmx, kmx, l) = c * (q(i, jmx - 1, kmx - 1, l) + q(i, jmx, kmx - 1, l) + q(i, jmx - 1, kmx, l));
+      }
+    }
+    __syncthreads();
+  }
+  for (int s = 0; s < 4; ++s) {
+    for (int t = tid; t < nk * nv; t += blockDim.x) {
+      const int k = -2 + t % nk, l = 1 + t / nk;
+      switch (s) {
+        case 0: q(imx, 0, k, l) = c * (q(imx - 1, 1, k, l) + q(imx - 1, 0, k, l) + q(imx, 1, k, l)); break;
+        case 1: q(0, 0, k, l) = c * (q(1, 1, k, l) + q(1, 0, k, l) + q(0, 1, k, l)); break;
+        case 2: q(0, jmx, k, l) = c * (q(1, jmx - 1, k, l) + q(1, jmx, k, l) + q(0, jmx - 1, k, l)); break;
+        default:
+          q(imx, jmx, k, l) = c * (q(imx - 1, jmx - 1, k, l) + q(imx - 1, jmx, k, l) + q(imx, jmx - 1, k, l));
+      }
+    }
+    __syncthreads();
+  }
+  for (int l = 1 + tid; l <= nv; l += blockDim.x) {
+    q(0, 0, 0, l) = c * (q(1, 0, 0, l) + q(0, 1, 0, l) + q(0, 0, 1, l));
+    q(imx, 0, 0, l) = c * (q(imx - 1, 0, 0, l) + q(imx, 1, 0, l) + q(imx, 0, 1, l));
+    q(0, jmx, 0, l) = c * (q(1, jmx, 0, l) + q(0, jmx - 1, 0, l) + q(0, jmx, 1, l));
+    q(0, 0, kmx, l) = c * (q(1, 0, kmx, l) + q(0, 1, kmx, l) + q(0, 0, kmx - 1, l));
+    q(imx, jmx, 0, l) = c * (q(imx - 1, jmx, 0, l) + q(imx, jmx - 1, 0, l) + q(imx, jmx, 1, l));
+    q(imx, 0, kmx, l) = c * (q(imx - 1, 0, kmx, l) + q(imx, 1, kmx, l) + q(imx, 0, kmx - 1, l));
+    q(0, jmx, kmx, l) = c * (q(1, jmx, kmx, l) + q(0, jmx - 1, kmx, l) + q(0, jmx, kmx - 1, l));
+    q(imx, jmx, kmx, l) = c * (q(imx - 1, jmx, kmx, l) + q(imx, jmx - 1, kmx, l) + q(imx, jmx, kmx - 1, l));
+  }
+}
+// An interface face carries no gradient BC (apply_gradient_bc treats the
+// negative ids only): the viscous terms take its ghost cells' own
+// Green-Gauss gradient, whose neighbours include the averaged edge ghosts.
+// Viscous blocks with such a face need the edge averaging on the fused path.
+__host__ __device__ __forceinline__ bool needs_edge_ghosts(const Params& p) {
+  if (p.mu_ref == 0.0) return false;
+  for (int f = 0; f < 6; ++f)
+    if (p.id[f] >= 0) return true;
+  return false;
+}
+
 // device error word: first error wins, later ones keep it
 __device__ __forceinline__ void raise_error(int* err, int code) { atomicCAS(err, 0, code); }
 

@@ -296,6 +296,11 @@ __global__ void __launch_bounds__(128) k_ghosts_mirror_batch(const Params* ps, c
                       g.F[2], g.dist, g.PM, g.pd);
 }
 
+// the edge and corner averaging of the reference on an FP32 mirror (one CTA)
+__global__ void k_corners_mirror(Dims d, Mirror M) {
+  corner_average<float>(d, [&](int i, int j, int k, int l) -> float& { return M.at(i, j, k, l - 1); });
+}
+
 // copy ghost layers 1-3 of face f (interior columns, every variable) from
 // one mirror (and FP64 buffer, when q is given) to the two others
 __global__ void k_ghost_bcast(Dims d, int f, int na, int nb, Mirror src, Mirror d1, Mirror d2, const double* q,
@@ -456,7 +461,9 @@ bool fused_supported(const Params& p, int precision) {
   // directions would read; they take the module path
   const bool tvd = p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3;
   const bool order_ok = mixed ? (order_dirs(p) == 0 || !tvd) : order_dirs(p) == 0;
-  return model && p.tstep == 'l' && ghost_depth_ok(p, true) && order_ok && small_enough;
+  // the implicit integrator runs on the module path
+  return p.integ <= FEST_TIME_TVDRK3 && model && p.tstep == 'l' && ghost_depth_ok(p, true) && order_ok &&
+         small_enough;
 }
 
 int fused_create(const Params& p, const DevBlock& b, const BlockRef* table, cudaStream_t s,
@@ -738,6 +745,7 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
     // read by nothing on this path after iteration 2), the high faces of
     // order-dependent directions second
     ring = ring_faces(p, &kper);
+    if (needs_edge_ghosts(p)) ring = kper = 0;  // every face's ghosts in the mirror, for the edges
     const int skip = ring | (kper << 4);
     Mirror M = mirror_of(f, in);
     for (int pass = 0; pass < (od ? 2 : 1); ++pass) {
@@ -761,9 +769,14 @@ static void run_stage(FusedState* f, const Params& p, const DevBlock& b, int pre
       }
     }
   } else {
-    // edge/corner ghosts are never read by an interior update: no averaging
+    // edge/corner ghosts reach an interior update only through the ghost
+    // gradient of an interface face of a viscous block: averaged then
     // (order-dependent blocks are thin, so the faces run one by one)
-    launch_ghosts(p, bb, tabs[in], iter, L, false);
+    launch_ghosts(p, bb, tabs[in], iter, L, needs_edge_ghosts(p));
+  }
+  if (mixed && needs_edge_ghosts(p)) {
+    k_corners_mirror<<<1, 256, 0, s>>>(p.d, mirror_of(f, in));
+    ++*cnt;
   }
   // order-dependent directions: the next fill's low face reads this fill's
   // high-face ghosts, in whichever buffer serves as its input
@@ -1297,7 +1310,7 @@ int fused_batch_create(const std::vector<FusedState*>& f, const std::vector<Para
   bool batched = prec == FEST_MIXED;
   for (size_t n = 0; n < f.size(); ++n) {
     if (!f[n] || !fused_supported(p[n], prec) || p[n].integ != p[0].integ) return FEST_ERR_ARG;
-    if (order_dirs(p[n]) || p[n].interp != p[0].interp || p[n].flux != p[0].flux ||
+    if (order_dirs(p[n]) || needs_edge_ghosts(p[n]) || p[n].interp != p[0].interp || p[n].flux != p[0].flux ||
         (p[n].mu_ref != 0.0) != (p[0].mu_ref != 0.0) || (p[n].turb != FEST_TURB_NONE) != (p[0].turb != FEST_TURB_NONE))
       batched = false;
   }

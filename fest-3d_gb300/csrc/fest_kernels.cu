@@ -310,46 +310,7 @@ __global__ void k_ghosts(Params p, DevBlock b, const BlockRef* blocks, int iter,
 // bc_primitive.f90:209-224 corner/edge averaging, 16 ordered statements
 __global__ void k_corners(Params p, double* q) {
   const Dims& d = p.d;
-  const int imx = d.imx, jmx = d.jmx, kmx = d.kmx, nv = d.nv;
-  auto Q = [&](int i, int j, int k, int l) -> double& { return q[pidx(d, i, j, k) + d.P * (l - 1)]; };
-  const int tid = threadIdx.x;
-  const int ni = imx + 5, nk = kmx + 5;
-  for (int s = 0; s < 4; ++s) {
-    for (int t = tid; t < ni * nv; t += blockDim.x) {
-      int i = -2 + t % ni, l = 1 + t / ni;
-      switch (s) {
-        case 0: Q(i, 0, 0, l) = 0.33 * (Q(i, 1, 1, l) + Q(i, 0, 1, l) + Q(i, 1, 0, l)); break;
-        case 1: Q(i, 0, kmx, l) = 0.33 * (Q(i, 1, kmx - 1, l) + Q(i, 0, kmx - 1, l) + Q(i, 1, kmx, l)); break;
-        case 2: Q(i, jmx, 0, l) = 0.33 * (Q(i, jmx - 1, 1, l) + Q(i, jmx, 1, l) + Q(i, jmx - 1, 0, l)); break;
-        default:
-          Q(i, jmx, kmx, l) = 0.33 * (Q(i, jmx - 1, kmx - 1, l) + Q(i, jmx, kmx - 1, l) + Q(i, jmx - 1, kmx, l));
-      }
-    }
-    __syncthreads();
-  }
-  for (int s = 0; s < 4; ++s) {
-    for (int t = tid; t < nk * nv; t += blockDim.x) {
-      int k = -2 + t % nk, l = 1 + t / nk;
-      switch (s) {
-        case 0: Q(imx, 0, k, l) = 0.33 * (Q(imx - 1, 1, k, l) + Q(imx - 1, 0, k, l) + Q(imx, 1, k, l)); break;
-        case 1: Q(0, 0, k, l) = 0.33 * (Q(1, 1, k, l) + Q(1, 0, k, l) + Q(0, 1, k, l)); break;
-        case 2: Q(0, jmx, k, l) = 0.33 * (Q(1, jmx - 1, k, l) + Q(1, jmx, k, l) + Q(0, jmx - 1, k, l)); break;
-        default:
-          Q(imx, jmx, k, l) = 0.33 * (Q(imx - 1, jmx - 1, k, l) + Q(imx - 1, jmx, k, l) + Q(imx, jmx - 1, k, l));
-      }
-    }
-    __syncthreads();
-  }
-  for (int l = 1 + tid; l <= nv; l += blockDim.x) {
-    Q(0, 0, 0, l) = 0.33 * (Q(1, 0, 0, l) + Q(0, 1, 0, l) + Q(0, 0, 1, l));
-    Q(imx, 0, 0, l) = 0.33 * (Q(imx - 1, 0, 0, l) + Q(imx, 1, 0, l) + Q(imx, 0, 1, l));
-    Q(0, jmx, 0, l) = 0.33 * (Q(1, jmx, 0, l) + Q(0, jmx - 1, 0, l) + Q(0, jmx, 1, l));
-    Q(0, 0, kmx, l) = 0.33 * (Q(1, 0, kmx, l) + Q(0, 1, kmx, l) + Q(0, 0, kmx - 1, l));
-    Q(imx, jmx, 0, l) = 0.33 * (Q(imx - 1, jmx, 0, l) + Q(imx, jmx - 1, 0, l) + Q(imx, jmx, 1, l));
-    Q(imx, 0, kmx, l) = 0.33 * (Q(imx - 1, 0, kmx, l) + Q(imx, 1, kmx, l) + Q(imx, 0, kmx - 1, l));
-    Q(0, jmx, kmx, l) = 0.33 * (Q(1, jmx, kmx, l) + Q(0, jmx - 1, kmx, l) + Q(0, jmx, kmx - 1, l));
-    Q(imx, jmx, kmx, l) = 0.33 * (Q(imx - 1, jmx, kmx, l) + Q(imx, jmx - 1, kmx, l) + Q(imx, jmx, kmx - 1, l));
-  }
+  corner_average<double>(d, [&](int i, int j, int k, int l) -> double& { return q[pidx(d, i, j, k) + d.P * (l - 1)]; });
 }
 
 __global__ void k_temperature(Params p, const double* qp, double* T) {

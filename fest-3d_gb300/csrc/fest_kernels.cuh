@@ -62,6 +62,10 @@ void launch_update(const Params& p, const DevBlock& b, double TF, double SF, int
 void launch_blend(const Params& p, const DevBlock& b, double a, double c, const Launcher& L);
 // res_abs partials of this block: out[0] mass imbalance, out[l] sum R_l^2
 void launch_resnorm(const Params& p, const DevBlock& b, double* d_out, const Launcher& L);
+// the LU-SGS update of the implicit integrator (fest_lusgs.cu) on the
+// residue and time step held by b; scratch: lusgs_scratch_doubles doubles
+long long lusgs_scratch_doubles(const Dims& d);
+void launch_lusgs(const Params& p, const DevBlock& b, double* scratch, const Launcher& L);
 void launch_geometry(const Params& p, const DevBlock& b, const Launcher& L);
 void launch_wall_dist(const Params& p, const DevBlock& b, const double* d_wall, int n_wall,
                       double* d_node_dist, const Launcher& L);

@@ -57,8 +57,11 @@ enum { FEST_FLUX_AUSM = 0, FEST_FLUX_AUSMP = 1, FEST_FLUX_AUSMUP = 2,
        FEST_FLUX_SLAU = 3, FEST_FLUX_LDFSS0 = 4, FEST_FLUX_VAN_LEER = 5 };
 enum { FEST_INTERP_NONE = 0, FEST_INTERP_MUSCL = 1, FEST_INTERP_PPM = 2,
        FEST_INTERP_WENO = 3, FEST_INTERP_WENO_NM = 4 };
+/* FEST_TIME_IMPLICIT: the reference's "implicit" (update.f90:215-218), one
+ * residual and time step, then the LU-SGS update of lusgs.f90:134-1196
+ * (laminar and k-omega SST, FP64, module path; batches of blocks too) */
 enum { FEST_TIME_NONE = 0, FEST_TIME_RK2 = 1, FEST_TIME_RK4 = 2,
-       FEST_TIME_TVDRK2 = 3, FEST_TIME_TVDRK3 = 4 };
+       FEST_TIME_TVDRK2 = 3, FEST_TIME_TVDRK3 = 4, FEST_TIME_IMPLICIT = 5 };
 enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2 };
 enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
 /* MUSCL limiter: the reference hard-codes Koren's alpha family
@@ -258,6 +261,10 @@ int fest_set_stream(fest_handle *h, void *cuda_stream);
  * and their summed device time */
 int fest_profile(fest_handle *h, int enable);
 int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
+/* device time (CUDA events on the handle's stream) of the kernels of the
+ * last fest_step, fest_get_total_conservative_residue or fest_residual_vjp
+ * call: from after its host inputs arrived to before its outputs left */
+int fest_last_kernel_ms(fest_handle *h, double *ms);
 
 /* ---- batches ------------------------------------------------------------- */
 /* No counterpart in the reference (its blocks advance one MPI rank each,
@@ -325,6 +332,13 @@ int fest_residual_vjp_nodes(fest_handle *h, const double *qp, int current_iter,
 int fest_adjoint_solve(fest_handle *h, const double *dJdq, double CFL,
                        int max_iters, double tol, double *psi, int *n_done,
                        double *drop);
+
+/* ---- measurement ---------------------------------------------------------- */
+/* No counterpart in the reference.  The arithmetic roof of the current
+ * device, measured with event-timed dependent FMA chains on every SM: kind 0
+ * FP64, 1 FP32; *tflops in TFLOP/s (two per fused multiply-add).  The FP64
+ * sweeps are bound by it on this hardware. */
+int fest_measure_peak(int kind, double *tflops);
 
 /* ---- allocation-free norm ------------------------------------------------ */
 /* No counterpart in the reference.  find_resnorm (resnorm.f90:62) without a
