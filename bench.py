@@ -71,6 +71,16 @@ def parse():
                          "stage for all blocks against a loop over the blocks' own steps")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the 1024x384x64-cell roofline measurement")
+    ap.add_argument("--adjoint-study", default="", metavar="JSON",
+                    help="instead of the bench line: the wall-force sensitivity study on the "
+                         "128x48x4 bump (primal to a 1e-12 drop, adjoint to 1e-10, Mach, angle and "
+                         "lower-wall nodes against central differences); writes JSON")
+    ap.add_argument("--study-nodes", default="1-128",
+                    help="lower-wall nodes of --adjoint-study: a range a-b or a comma list")
+    ap.add_argument("--sweep", default="", choices=["", "mixed", "fp64"],
+                    help="instead of the bench line: step the workload block --sweep-iters "
+                         "iterations at this precision and exit (a short run for profilers)")
+    ap.add_argument("--sweep-iters", type=int, default=6)
     ap.add_argument("--c2-iters", type=int, default=C2_ITERS, metavar="ITERS",
                     help="iterations of the mixed-vs-FP64 bump report (wall Cp, entropy, residual "
                          "drop); 0 skips it")
@@ -168,13 +178,49 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def committed_traffic():
-    p = os.path.join(ROOT, "profiles", "k_stage_traffic.json")
+def committed_traffic(name="k_stage_traffic.json"):
+    p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
             return json.load(f)
     except Exception:
         return None
+
+
+def fp64_roofline(lib, C, abi, h, it, CFL, cells, reps=30):
+    """The FP64 sweep against its own roof: the FP64 unit.  Flops per
+    cell-residual from the committed ncu count of the same sweep
+    (profiles/k_stage_fp64_flops.json: 2 x DFMA + DADD + DMUL thread
+    instructions of one launch over its cells); the launch time from an
+    event pair around each sweep launch of `reps` further iterations
+    (fest_profile); the peak from an event-timed FP64 FMA microkernel run
+    now (fest_measure_peak).  The HBM figure beside it uses the method's
+    compulsory bytes."""
+    fl = committed_traffic("k_stage_fp64_flops.json") or {}
+    flops = fl.get("flops_per_cell_residual")
+    abi.check(lib.fest_profile(h.h, 1), "profile")
+    h.step(reps, it, CFL, with_norm=False)
+    nl, tot = C.c_longlong(), C.c_double()
+    abi.check(lib.fest_profile_read(h.h, C.byref(nl), C.byref(tot)), "profile_read")
+    abi.check(lib.fest_profile(h.h, 0), "profile off")
+    launch_s = tot.value / 1e3 / max(nl.value, 1)
+    t = C.c_double()
+    rc = lib.fest_measure_peak(0, C.byref(t))
+    peak = t.value if rc == 0 else None
+    out = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak,
+           "peak_source": "measured now: dependent FP64 FMA chains on every SM (fest_measure_peak)",
+           "kernel": "k_stage<double> (fused WENO5+SLAU sweep + update, FP64)",
+           "avg_launch_us": launch_s * 1e6, "launches": int(nl.value),
+           "duration": "event pair around each sweep launch (fest_profile), mean",
+           "flops_per_cell_residual": flops, "flops_source": fl.get("source")}
+    if flops and peak:
+        out["achieved"] = flops * cells / launch_s / 1e12
+        out["frac"] = out["achieved"] / peak
+    hbm, _ = measured_peak()
+    bytes_launch = cells * sum(BYTES_STAGE) / len(BYTES_STAGE)
+    out["hbm"] = {"achieved_gbs": bytes_launch / launch_s / 1e9, "peak_gbs": hbm,
+                  "frac": bytes_launch / launch_s / 1e9 / hbm}
+    return out
 
 
 def wall_cp(q, ext, flow):
@@ -547,6 +593,8 @@ def run_ours(args):
     link = {"h2d_gbs": 10 * nbytes / tu / 1e9, "d2h_gbs": 10 * nbytes / td / 1e9,
             "upload_us": tu / 10 * 1e6, "download_us": td / 10 * 1e6}
 
+    fp64_roof = fp64_roofline(lib, C, abi, fp64["h"], fp64["it"], CFL, N)
+    fp64["it"] += 30
     adj = adjoint_cost(lib) if rank == 0 else None
     c2 = c2_report(lib, abi, cases, Handle, args.c2_iters) if rank == 0 and args.c2_iters > 1 else None
 
@@ -568,7 +616,8 @@ def run_ours(args):
             "data": "synthetic (analytic bump grid, uniform Mach 0.5 start)",
             "config": bench_config(case, ws),
             "fp64": {"value": rate(fp64), "unit": "Mcell-residuals/s", "steps": fp64["steps"],
-                     "ms_per_step": fp64["ms"] / fp64["steps"]},
+                     "ms_per_step": fp64["ms"] / fp64["steps"],
+                     "roofline": fp64_roof, "clocks": fp64["clocks"]},
             "mixed_over_fp64": rate(mixed) / rate(fp64),
             "wall_cp_abs_err_mixed_vs_fp64": cp_err,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -595,6 +644,47 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def run_adjoint_study(args):
+    """fest3d.adjoint.wall_force_study through the C ABI; the result as JSON
+    to args.adjoint_study and a one-line summary on stdout."""
+    from fest3d import abi, build, adjoint as A
+    if not os.path.exists(abi.LIB_PATH):
+        build.build()
+    lib = abi.load()
+    spec = args.study_nodes
+    if "-" in spec:
+        a, b = (int(x) for x in spec.split("-"))
+        nodes = tuple(range(a, b + 1))
+    else:
+        nodes = tuple(int(x) for x in spec.split(",") if x)
+    t0 = time.perf_counter()
+    out = A.wall_force_study(lib, wall_nodes=nodes, log=lambda *a: print(*a, file=sys.stderr, flush=True))
+    out["seconds"] = time.perf_counter() - t0
+    with open(args.adjoint_study, "w") as f:
+        json.dump(out, f, indent=1)
+    print(json.dumps({k: out[k] for k in ("primal", "adjoint", "max_rel_diff", "seconds")
+                      if k in out}), flush=True)
+
+
+def run_sweep(args):
+    """The workload block stepped --sweep-iters iterations at one precision
+    through fest_step, nothing else: the command profilers capture."""
+    from fest3d import abi, build, cases
+    from fest3d.handle import Handle
+    if not os.path.exists(abi.LIB_PATH):
+        build.build()
+    lib = abi.load()
+    case = cases.bump_case() if args.workload == "bump" else cases.bump_case(nc=(512, 192, 16))
+    h = Handle(case["ext"], case["flow"], case["scheme"], case["bc"], lib=lib)
+    h.setup_geometry(case["nodes"])
+    h.upload_state(case["qp"])
+    h.set_precision(abi.FEST_FP64 if args.sweep == "fp64" else abi.FEST_MIXED)
+    h.step(args.sweep_iters, 1, case["CFL"], with_norm=False)
+    print(json.dumps({"sweep": args.sweep, "workload": case["name"], "iters": args.sweep_iters,
+                      "launches": h.launches}), flush=True)
+    h.close()
 
 
 def run_converged(args):
@@ -857,6 +947,12 @@ def main():
         return
     if args.converged:
         run_converged(args)
+        return
+    if args.sweep:
+        run_sweep(args)
+        return
+    if args.adjoint_study:
+        run_adjoint_study(args)
         return
     if args.impl == "reference":
         run_reference(args)

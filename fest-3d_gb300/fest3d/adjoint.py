@@ -13,7 +13,7 @@ Everything runs through the C ABI (include/fest_gpu.h) in FP64.
 """
 import numpy as np
 
-from . import abi, cases
+from . import abi, cases, krylov
 from .handle import Handle
 
 
@@ -86,6 +86,94 @@ def converge(h, q, CFL, first_iter=1, tol=1e-12, max_iters=200000, chunk=500, re
     return h.download_state(), it, drop, ref
 
 
+def _flat(a, sl):
+    return np.asarray(a[sl]).reshape(-1, order="F")
+
+
+def state_scale(flow, ext):
+    """Per-entry weights of the interior state vector: the free-stream
+    density, speed (three components) and pressure."""
+    sc = np.array([flow.density_inf, flow.vel_mag, flow.vel_mag, flow.vel_mag, flow.pressure_inf])
+    shape = (ext.imx - 1, ext.jmx - 1, ext.kmx - 1, 5)
+    return np.broadcast_to(sc, shape).reshape(-1, order="F").copy()
+
+
+def converge_accelerated(h, q, CFL, first_iter=3, tol=1e-12, ref=None, k=50, m=20, max_maps=4000,
+                         flow=None):
+    """The steady state from q by Anderson acceleration (fest3d.krylov) of
+    k solver iterations (fest_step, the handle's own integrator and
+    precision) as the fixed-point map, until the mass-residual norm the
+    step reports has dropped by tol relative to ref (default: the norm
+    of the first map).  Returns (state, next iteration, drop, ref, maps,
+    iterations)."""
+    ext = h.ext
+    sl = _interior(ext)
+    shape = q[sl].shape
+    cur = np.array(q, order="F")
+    state = {"it": first_iter, "ref": ref}
+
+    def phi(x):
+        cur[sl] = x.reshape(shape, order="F")
+        h.upload_state(cur)
+        norm = h.step(k, state["it"], CFL)
+        state["it"] += k
+        r = float(norm[1])
+        if not np.isfinite(r):
+            raise FloatingPointError("primal diverged")
+        if state["ref"] is None:
+            state["ref"] = r
+        cur[...] = h.download_state()
+        return _flat(cur, sl), r / state["ref"] if state["ref"] > 0 else 0.0
+
+    scale = state_scale(flow or h.flow, ext)
+    x, drop, maps = krylov.anderson(phi, _flat(cur, sl), m=m, maxiter=max_maps,
+                                    done=lambda d, n: d <= tol, scale=scale)
+    cur[sl] = x.reshape(shape, order="F")
+    return cur, state["it"], drop, state["ref"], maps, maps * k
+
+
+def adjoint_krylov(h, dJ, CFL, tol=1e-10, k=20, restart=40, max_products=3000, it=3):
+    """psi with (dR/dq)^T psi = -dJ/dq at the device state by GMRES
+    (fest3d.krylov) on (I - G^k) psi = S_k(g): S_k is k steps of the
+    fixed-point adjoint iteration from zero (fest_adjoint_solve), G its
+    iteration matrix, and (I - G^k) v = -S_k((dR/dq)^T v), one residual VJP
+    and k adjoint steps per product.  Restarts until the true residual
+    ||(dR/dq)^T psi + dJ/dq|| / ||dJ/dq|| over the interior cells is at most
+    tol.  Returns (psi in the residue layout, GMRES products, drop,
+    residual-VJP calls)."""
+    ext = h.ext
+    sl = _interior(ext)
+    shape = (ext.imx - 1, ext.jmx - 1, ext.kmx - 1, 5)
+    pad = np.zeros(h.shape["qp"], order="F")
+    calls = [0]
+
+    def S(b):
+        pad[sl] = b.reshape(shape, order="F")
+        psi, _, _ = h.adjoint_solve(pad, CFL, k, 0.0)
+        calls[0] += 3 * k
+        return psi.reshape(-1, order="F")
+
+    def AT(v):
+        dq = h.residual_vjp(None, it, np.asfortranarray(v.reshape(shape, order="F")))
+        calls[0] += 1
+        return _flat(dq, sl)
+
+    g = _flat(dJ, sl)
+    gn = np.linalg.norm(g)
+    rhs = S(g)
+    x, products, drop = None, 0, np.inf
+    inner = tol
+    for _ in range(6):
+        x, n, _ = krylov.gmres(lambda v: -S(AT(v)), rhs, x0=x, tol=inner, restart=restart,
+                               maxiter=max_products - products)
+        products += n
+        drop = float(np.linalg.norm(AT(x) + g) / gn)
+        if drop <= tol or products >= max_products:
+            break
+        inner = inner * max(tol / drop, 1e-3)
+    return np.asfortranarray(x.reshape(shape, order="F")), products, drop, calls[0]
+
+
 def wall_force(q, ext, Jfaces):
     """J = sum_{i,k} p(i,1,k) nx A over the lower-wall J-faces, and dJ/dq
     in the qp layout."""
@@ -141,15 +229,20 @@ def displaced_nodes(case, i, delta):
 
 
 def sensitivities(case, q, it, params=("mach", "angle"), wall_nodes=(), tol=1e-10,
-                  max_iters=200000, lib=None):
+                  max_iters=200000, lib=None, krylov_solve=False):
     """dJ/dalpha for each flow parameter and dJ/d(delta_i) for each listed
-    lower-wall node i from one adjoint solve at the converged state q;
-    returns ({name: derivative}, J, adjoint iterations, drop)."""
+    lower-wall node i from one adjoint solve at the converged state q (the
+    fixed-point iteration, or with krylov_solve its GMRES acceleration,
+    adjoint_krylov); returns ({name: derivative}, J, adjoint iterations or
+    GMRES products, drop)."""
     h = make_handle(case, lib=lib)
     h.upload_state(q)
     Jf = h.get("Jfaces")
     J, dJ = wall_force(q, case["ext"], Jf)
-    psi, n, drop = h.adjoint_solve(dJ, case["CFL"], max_iters, tol)
+    if krylov_solve:
+        psi, n, drop, _ = adjoint_krylov(h, dJ, case["CFL"], tol=tol, max_products=max_iters)
+    else:
+        psi, n, drop = h.adjoint_solve(dJ, case["CFL"], max_iters, tol)
     grads = {pname: float(np.sum(psi * residual_param_derivative(case, q, it, pname, lib=lib)))
              for pname in params}
     if len(wall_nodes):
@@ -160,6 +253,100 @@ def sensitivities(case, q, it, params=("mach", "angle"), wall_nodes=(), tol=1e-1
             grads[f"wall_node_{i}"] = float(np.sum(dn[1, i + 2, 3:ext.jmx + 3, 3:ext.kmx + 3] * wgt[:, None]))
     h.close()
     return grads, J, n, drop
+
+
+def perturbed_case(case, param, delta):
+    """The case with flow parameter param ('mach', 'angle') moved by delta,
+    or with lower-wall node param (an int) moved by delta in y."""
+    c = dict(case)
+    if isinstance(param, str):
+        c[param] = case[param] + delta
+        c["flow"] = bump_flow(c["mach"], c["angle"], mu_ref=case.get("mu_ref", 0.0))
+        c["bc"] = bump_bc(c["mach"], wall=case.get("wall", -6))
+    else:
+        c["nodes"] = displaced_nodes(case, param, delta)
+    return c
+
+
+def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angle"), fd_step=1e-6,
+                     fd_steps=None, primal_tol=1e-12, adjoint_tol=1e-10, threads=4, log=None):
+    """The bump's wall-force sensitivities at 128x48x4 cells (Euler,
+    unlimited MUSCL + SLAU, FP64): the primal converged to a primal_tol
+    drop (Anderson-accelerated explicit iterations from the free stream),
+    one adjoint solve to an adjoint_tol drop (GMRES over the fixed-point
+    adjoint iteration), gradients with respect to the inflow Mach number and
+    angle and the y-displacements of the listed lower-wall nodes; each
+    checked by a central difference of two re-converged primal solutions
+    (step fd_step, or fd_steps[param]; each re-solve from the converged
+    state to the same drop), the re-solves spread over `threads` handles.
+    Returns a dict of everything measured."""
+    import time
+    from concurrent.futures import ThreadPoolExecutor
+    say = log or (lambda *a: None)
+    case = adjoint_case()
+    ext, CFL = case["ext"], case["CFL"]
+    out = {"workload": "smooth bump 128x48x4, Euler, MUSCL (unlimited) + SLAU, TVD-RK3 CFL 0.8, FP64",
+           "objective": "x-force of the first-cell pressure on the lower wall J-faces"}
+    t0 = time.perf_counter()
+    h = make_handle(case, lib=lib)
+    h.upload_state(case["qp"])
+    ref = float(h.step(1, 1, CFL)[1])
+    q, it, drop, ref, maps, iters = converge_accelerated(h, h.download_state(), CFL, first_iter=2,
+                                                         tol=primal_tol, ref=ref)
+    out["primal"] = {"drop": drop, "ref_norm": ref, "anderson_maps": maps, "iterations": iters + 1,
+                     "seconds": time.perf_counter() - t0}
+    say("primal", out["primal"])
+    t1 = time.perf_counter()
+    Jf = h.get("Jfaces")
+    J, dJ = wall_force(q, ext, Jf)
+    h.upload_state(q)
+    psi, products, adrop, vjps = adjoint_krylov(h, dJ, CFL, tol=adjoint_tol)
+    grads = {p: float(np.sum(psi * residual_param_derivative(case, q, it, p, lib=lib))) for p in params}
+    if len(wall_nodes):
+        dn = h.residual_vjp_nodes(q, it, psi, (None, wall_force_faces_bar(q, ext, Jf), None))
+        wgt = wall_blend(ext)
+        for i in wall_nodes:
+            grads[i] = float(np.sum(dn[1, i + 2, 3:ext.jmx + 3, 3:ext.kmx + 3] * wgt[:, None]))
+    h.close()
+    out["adjoint"] = {"drop": adrop, "gmres_products": products, "residual_vjp_calls": vjps,
+                      "seconds": time.perf_counter() - t1, "J": J}
+    say("adjoint", out["adjoint"])
+    steps = dict(fd_steps or {})
+
+    def fd(param):
+        step = steps.get(param, fd_step)
+        vals, info = [], []
+        for sgn in (1.0, -1.0):
+            c = perturbed_case(case, param, sgn * step)
+            hp = make_handle(c, lib=lib)
+            qs, _, d, _, m, n = converge_accelerated(hp, q, CFL, first_iter=it, tol=primal_tol, ref=ref)
+            vals.append(wall_force(qs, ext, hp.get("Jfaces"))[0])
+            info.append({"drop": d, "iterations": n})
+            hp.close()
+        return param, (vals[0] - vals[1]) / (2 * step), step, info
+
+    t2 = time.perf_counter()
+    rows = []
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for param, g_fd, step, info in ex.map(fd, list(params) + list(wall_nodes)):
+            g = grads[param]
+            rel = abs(g - g_fd) / max(abs(g_fd), 1e-300)
+            rows.append({"param": param if isinstance(param, str) else f"wall_node_{param}",
+                         "node": None if isinstance(param, str) else int(param),
+                         "adjoint": g, "fd": g_fd, "rel_diff": rel, "fd_step": step,
+                         "fd_drops": [i["drop"] for i in info],
+                         "fd_iterations": [i["iterations"] for i in info]})
+            say(rows[-1]["param"], g, g_fd, rel)
+    out["fd_seconds"] = time.perf_counter() - t2
+    out["rows"] = rows
+    out["max_rel_diff"] = max(r["rel_diff"] for r in rows) if rows else None
+    nodes = [r for r in rows if r["node"] is not None]
+    if nodes:
+        big = max(abs(r["fd"]) for r in nodes)
+        for r in nodes:
+            r["abs_diff_over_max_node_gradient"] = abs(r["adjoint"] - r["fd"]) / big
+        out["wall_nodes_max_abs_diff_over_max_gradient"] = max(r["abs_diff_over_max_node_gradient"] for r in nodes)
+    return out
 
 
 # ---- unsteady adjoint with checkpointing -------------------------------------
