@@ -52,15 +52,166 @@ template <typename T, int N> struct VolConst {
   }
 };
 
+// the same lines in plain arithmetic (the face-state values)
+template <typename T> struct ValLine {
+  const double* base;
+  long long stride;
+  __device__ __forceinline__ T operator()(int c) const { return (T)base[c * stride]; }
+};
+template <typename T> struct VolVal {
+  const double* p;
+  long long stride;
+  int n;
+  __device__ __forceinline__ T operator()(int c) const {
+    c = c < -2 ? -2 : (c > n + 2 ? n + 2 : c);
+    return (T)p[4 * c * stride];
+  }
+};
+
 __device__ __forceinline__ void cell_of(int dir, int c, int ta, int tb, int& i, int& j, int& k) {
   if (dir == 0) { i = c; j = ta; k = tb; }
   else if (dir == 1) { i = ta; j = c; k = tb; }
   else { i = ta; j = tb; k = c; }
 }
 
+// Reverse mode of the SLAU flux (slau.f90:85-196, flux_mass_family):
+// bx = mu^T dF/d(qL, qR) in one backward sweep over the forward values,
+// about four times the flux's own arithmetic where the ten forward
+// directions of Dual<T, 10> cost about twenty.  The derivative conventions
+// at the kinks are the dual numbers' (fest_dual.cuh): fabs takes the sign
+// of its argument (+1 at 0), fmax2/fmin2 the branch they return, floor
+// and copysign none, sqrt 1/(2 sqrt(x)) (0 at 0).  nv = 5.
+template <typename T>
+__device__ __forceinline__ void slau_vjp(T gm, const T* qL, const T* qR, T A, T nx, T ny, T nz, T mask,
+                                         const T* mu, T* bx) {
+  const T rL = qL[0], uL = qL[1], vL = qL[2], wL = qL[3], pL = qL[4];
+  const T rR = qR[0], uR = qR[1], vR = qR[2], wR = qR[3], pR = qR[4];
+  // forward, as flux_mass_family computes it
+  const T g1 = gm / (gm - T(1));
+  const T HL = (T(0.5) * (uL * uL + vL * vL + wL * wL)) + (g1 * pL) / rL;
+  const T HR = (T(0.5) * (uR * uR + vR * vR + wR * wR)) + (g1 * pR) / rR;
+  const T VnL = uL * nx + vL * ny + wL * nz;
+  const T VnR = uR * nx + vR * ny + wR * nz;
+  const T cL2 = (gm * pL) / rL, cR2 = (gm * pR) / rR;
+  const T sL = ::sqrt(cL2), sR = ::sqrt(cR2);
+  const T C = T(0.5) * (sL + sR);
+  const T iC = T(1) / C;
+  const T ML = VnL * iC, MR = VnR * iC;
+  const T aL = fmax2(T(0), T(1) - ::floor(::fabs(ML)));
+  const T aR = fmax2(T(0), T(1) - ::floor(::fabs(MR)));
+  const T betaL = (T(1) - aL) * T(0.5) * (T(1) + fsign1(ML)) +
+                  (aL) * T(0.25) * (T(2) - ML) * ((ML + T(1)) * (ML + T(1)));
+  const T betaR = (T(1) - aR) * T(0.5) * (T(1) - fsign1(MR)) +
+                  (aR) * T(0.25) * (T(2) + MR) * ((MR - T(1)) * (MR - T(1)));
+  const T S2 = T(0.5) * ((uL * uL) + (vL * vL) + (wL * wL) + (uR * uR) + (vR * vR) + (wR * wR));
+  const T vt = ::sqrt(S2);
+  const T x = vt * iC;
+  const bool capped = T(1) < x;  // fmin2(1, x) returns the constant
+  const T Mcap = capped ? T(1) : x;
+  const T Xi = (T(1) - Mcap) * (T(1) - Mcap);
+  const T aVL = ::fabs(VnL), aVR = ::fabs(VnR);
+  const T sgL = VnL < T(0) ? T(-1) : T(1), sgR = VnR < T(0) ? T(-1) : T(1);
+  const T Nv = rL * aVL + rR * aVR, Dv = rL + rR;
+  const T Vnabs = Nv / Dv;
+  const bool a1 = ML < T(0);                // fmin2(ML, 0) returns ML
+  const T fa1 = a1 ? ML : T(0);
+  const bool a2 = fa1 > T(-1);              // fmax2(., -1) returns it
+  const T fa = a2 ? fa1 : T(-1);
+  const bool b1 = MR > T(0);                // fmax2(MR, 0) returns MR
+  const T fb1 = b1 ? MR : T(0);
+  const bool b2 = fb1 < T(1);               // fmin2(., 1) returns it
+  const T fb = b2 ? fb1 : T(1);
+  const T fnG = -fa * fb;
+  const T pbar = T(0.5) * ((pL + pR) + (betaL - betaR) * (pL - pR) +
+                           (T(1) - Xi) * (betaL + betaR - T(1)) * (pL + pR));
+  const T VnabsL = (T(1) - fnG) * Vnabs + fnG * aVL;
+  const T VnabsR = (T(1) - fnG) * Vnabs + fnG * aVR;
+  const T mass0 = T(0.5) * ((rL * (VnL + VnabsL) + rR * (VnR - VnabsR)) - (Xi * (pR - pL) * iC));
+  const T mass = mass0 * mask;
+  const T Fp0 = T(0.5) * (mass + ::fabs(mass)), Fm0 = T(0.5) * (mass - ::fabs(mass));
+  // backward
+  const T m0 = mu[0] * A, m1 = mu[1] * A, m2 = mu[2] * A, m3 = mu[3] * A, m4 = mu[4] * A;
+  T b_rL = T(0), b_uL = m1 * Fp0, b_vL = m2 * Fp0, b_wL = m3 * Fp0, b_pL = T(0);
+  T b_rR = T(0), b_uR = m1 * Fm0, b_vR = m2 * Fm0, b_wR = m3 * Fm0, b_pR = T(0);
+  const T b_HL = m4 * Fp0, b_HR = m4 * Fm0;
+  const T b_Fp0 = m0 + m1 * uL + m2 * vL + m3 * wL + m4 * HL;
+  const T b_Fm0 = m0 + m1 * uR + m2 * vR + m3 * wR + m4 * HR;
+  const T b_pbar = m1 * nx + m2 * ny + m3 * nz;
+  const T sm = mass < T(0) ? T(-1) : T(1);
+  const T b_mass0 = (b_Fp0 * T(0.5) * (T(1) + sm) + b_Fm0 * T(0.5) * (T(1) - sm)) * mask;
+  // mass0
+  const T hm = T(0.5) * b_mass0;
+  b_rL += hm * (VnL + VnabsL);
+  b_rR += hm * (VnR - VnabsR);
+  T b_VnL = hm * rL, b_VnR = hm * rR;
+  const T b_VnabsL = hm * rL, b_VnabsR = -hm * rR;
+  T b_Xi = -hm * (pR - pL) * iC;
+  b_pR += -hm * Xi * iC;
+  b_pL += hm * Xi * iC;
+  T b_iC = -hm * Xi * (pR - pL);
+  // VnabsL, VnabsR
+  const T b_fnG = b_VnabsL * (aVL - Vnabs) + b_VnabsR * (aVR - Vnabs);
+  const T b_Vnabs = (b_VnabsL + b_VnabsR) * (T(1) - fnG);
+  b_VnL += b_VnabsL * fnG * sgL;
+  b_VnR += b_VnabsR * fnG * sgR;
+  // pbar
+  const T hp = T(0.5) * b_pbar;
+  const T cc = (T(1) - Xi) * (betaL + betaR - T(1));
+  b_pL += hp * (T(1) + (betaL - betaR) + cc);
+  b_pR += hp * (T(1) - (betaL - betaR) + cc);
+  const T b_betaL = hp * ((pL - pR) + (T(1) - Xi) * (pL + pR));
+  const T b_betaR = hp * (-(pL - pR) + (T(1) - Xi) * (pL + pR));
+  b_Xi += -hp * (betaL + betaR - T(1)) * (pL + pR);
+  // fnG = -fa * fb
+  T b_ML = T(0), b_MR = T(0);
+  if (a1 && a2) b_ML += -b_fnG * fb;
+  if (b1 && b2) b_MR += -b_fnG * fa;
+  // Vnabs = Nv / Dv
+  const T b_Nv = b_Vnabs / Dv, b_Dv = -b_Vnabs * Vnabs / Dv;
+  b_rL += b_Nv * aVL + b_Dv;
+  b_rR += b_Nv * aVR + b_Dv;
+  b_VnL += b_Nv * rL * sgL;
+  b_VnR += b_Nv * rR * sgR;
+  // Xi, Mcap = x = vt iC
+  const T b_Mcap = -T(2) * (T(1) - Mcap) * b_Xi;
+  if (!capped) {
+    const T hv = vt > T(0) ? b_Mcap * iC * (T(0.5) / vt) : T(0);  // through S2
+    b_iC += b_Mcap * vt;
+    b_uL += hv * uL; b_vL += hv * vL; b_wL += hv * wL;
+    b_uR += hv * uR; b_vR += hv * vR; b_wR += hv * wR;
+  }
+  // betaL, betaR (aL, aR piecewise constant)
+  b_ML += b_betaL * aL * T(0.25) * (-((ML + T(1)) * (ML + T(1))) + (T(2) - ML) * T(2) * (ML + T(1)));
+  b_MR += b_betaR * aR * T(0.25) * (((MR - T(1)) * (MR - T(1))) + (T(2) + MR) * T(2) * (MR - T(1)));
+  // ML = VnL iC, MR = VnR iC
+  b_VnL += b_ML * iC;
+  b_VnR += b_MR * iC;
+  b_iC += b_ML * VnL + b_MR * VnR;
+  // iC = 1 / C, C = (sL + sR) / 2
+  const T b_C = -b_iC * iC * iC;
+  const T b_cL2 = sL > T(0) ? T(0.5) * b_C * (T(0.5) / sL) : T(0);
+  const T b_cR2 = sR > T(0) ? T(0.5) * b_C * (T(0.5) / sR) : T(0);
+  b_pL += b_cL2 * gm / rL;
+  b_rL += -b_cL2 * cL2 / rL;
+  b_pR += b_cR2 * gm / rR;
+  b_rR += -b_cR2 * cR2 / rR;
+  // HL, HR
+  b_uL += b_HL * uL; b_vL += b_HL * vL; b_wL += b_HL * wL;
+  b_pL += b_HL * g1 / rL;
+  b_rL += -b_HL * (g1 * pL) / (rL * rL);
+  b_uR += b_HR * uR; b_vR += b_HR * vR; b_wR += b_HR * wR;
+  b_pR += b_HR * g1 / rR;
+  b_rR += -b_HR * (g1 * pR) / (rR * rR);
+  // VnL, VnR
+  b_uL += b_VnL * nx; b_vL += b_VnL * ny; b_wL += b_VnL * nz;
+  b_uR += b_VnR * nx; b_vR += b_VnR * ny; b_wR += b_VnR * nz;
+  bx[0] = b_rL; bx[1] = b_uL; bx[2] = b_vL; bx[3] = b_wL; bx[4] = b_pL;
+  bx[5] = b_rR; bx[6] = b_uR; bx[7] = b_vR; bx[8] = b_wR; bx[9] = b_pR;
+}
+
 // one thread per face of direction dir (faces 1..n along dir, interior
 // tangential positions)
-template <typename T>
+template <typename T, bool SLAU>
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, const double* lam,
                                                        double* bar, double* bar_face, int dir) {
   using D5 = Dual<T, 5>;
@@ -90,39 +241,41 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
 #pragma unroll
     for (int l = 0; l < 5; ++l) mu[l] -= (T)lam[cidx(d, i, j, k) + N * l];
   }
-  // face states with their stencil derivatives
+  // the face states' values (the reconstruction in plain arithmetic)
   cell_of(dir, 0, ta, tb, i, j, k);
   const long long c0 = pidx(d, i, j, k);
-  D5 qL[5], qR[5];
+  T qL[5], qR[5];
   {
-    VolConst<T, 5> vol{b.cells + 4 * c0, st, n};
-    ConstLine<T, 5> pres{b.qp + c0 + P * 4, st};
+    VolVal<T> vol{b.cells + 4 * c0, st, n};
+    ValLine<T> pres{b.qp + c0 + P * 4, st};
 #pragma unroll
     for (int l = 0; l < 5; ++l) {
-      D5 Rm, Lp;
-      DualLine<T, 5> qa{b.qp + c0 + P * l, st, c - 1};
-      recon_cell<D5>(p, dir, c - 1, l + 1, qa, pres, vol, Rm, Lp);
+      T Rm, Lp;
+      ValLine<T> q{b.qp + c0 + P * l, st};
+      recon_cell<T>(p, dir, c - 1, l + 1, q, pres, vol, Rm, Lp);
       qL[l] = Lp;
-      DualLine<T, 5> qb{b.qp + c0 + P * l, st, c};
-      recon_cell<D5>(p, dir, c, l + 1, qb, pres, vol, Rm, Lp);
+      recon_cell<T>(p, dir, c, l + 1, q, pres, vol, Rm, Lp);
       qR[l] = Rm;
     }
   }
-  // flux Jacobian, transposed onto mu
+  const long long fi = fidx(d, dir, i + (dir == 0 ? c : 0), j + (dir == 1 ? c : 0), k + (dir == 2 ? c : 0));
+  const double* fc = b.faces[dir] + 4 * fi;
+  const T mask_v = (T)wall_mask(p, dir, c);
+  // flux Jacobian, transposed onto mu: reverse mode for SLAU, forward
+  // duals over the ten face-state values for the other schemes
   T bx[10];
-  {
+  if constexpr (SLAU) {
+    slau_vjp<T>((T)p.gm, qL, qR, (T)fc[0], (T)fc[1], (T)fc[2], (T)fc[3], mask_v, mu, bx);
+  } else {
     D10 xl[5], xr[5], Fo[NVMAX];
 #pragma unroll
     for (int l = 0; l < 5; ++l) {
-      xl[l] = D10::var(qL[l].v, l);
-      xr[l] = D10::var(qR[l].v, 5 + l);
+      xl[l] = D10::var(qL[l], l);
+      xr[l] = D10::var(qR[l], 5 + l);
     }
-    const double* fc = b.faces[dir] + 4 * fidx(d, dir, i + (dir == 0 ? c : 0), j + (dir == 1 ? c : 0),
-                                               k + (dir == 2 ? c : 0));
     const D10 A = D10::cst((T)fc[0]), nx = D10::cst((T)fc[1]), ny = D10::cst((T)fc[2]),
               nz = D10::cst((T)fc[3]);
-    const D10 mask = D10::cst((T)wall_mask(p, dir, c));
-    face_flux<D10>(p, xl, xr, A, nx, ny, nz, mask, Fo);
+    face_flux<D10>(p, xl, xr, A, nx, ny, nz, D10::cst(mask_v), Fo);
 #pragma unroll
     for (int m = 0; m < 10; ++m) {
       T s = T(0);
@@ -137,14 +290,11 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
     D4 xl[5], xr[5], Fo[NVMAX];
 #pragma unroll
     for (int l = 0; l < 5; ++l) {
-      xl[l] = D4::cst(qL[l].v);
-      xr[l] = D4::cst(qR[l].v);
+      xl[l] = D4::cst(qL[l]);
+      xr[l] = D4::cst(qR[l]);
     }
-    const long long fi = fidx(d, dir, i + (dir == 0 ? c : 0), j + (dir == 1 ? c : 0), k + (dir == 2 ? c : 0));
-    const double* fc = b.faces[dir] + 4 * fi;
-    const D4 mask = D4::cst((T)wall_mask(p, dir, c));
     face_flux<D4>(p, xl, xr, D4::var((T)fc[0], 0), D4::var((T)fc[1], 1), D4::var((T)fc[2], 2),
-                  D4::var((T)fc[3], 3), mask, Fo);
+                  D4::var((T)fc[3], 3), D4::cst(mask_v), Fo);
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
       T s = T(0);
@@ -153,15 +303,28 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
       if (s != T(0)) atomicAdd(bar_face + 4 * fi + m, (double)s);
     }
   }
-  // face states -> stencil cells
+  // face states -> stencil cells, one variable at a time: qL (cell c-1)
+  // reaches cells c-3..c+1, qR (cell c) cells c-2..c+2; the six targets
+  // are summed in registers before one atomic add each
+  VolConst<T, 5> vol{b.cells + 4 * c0, st, n};
+  ConstLine<T, 5> pres{b.qp + c0 + P * 4, st};
+#pragma unroll 1
+  for (int l = 0; l < 5; ++l) {
+    T acc[6];
+    D5 Rm, Lp;
+    DualLine<T, 5> qa{b.qp + c0 + P * l, st, c - 1};
+    recon_cell<D5>(p, dir, c - 1, l + 1, qa, pres, vol, Rm, Lp);
 #pragma unroll
-  for (int l = 0; l < 5; ++l)
+    for (int s = 0; s < 5; ++s) acc[s] = bx[l] * Lp.d[s];
+    acc[5] = T(0);
+    DualLine<T, 5> qb{b.qp + c0 + P * l, st, c};
+    recon_cell<D5>(p, dir, c, l + 1, qb, pres, vol, Rm, Lp);
 #pragma unroll
-    for (int s = 0; s < 5; ++s) {
-      const T gL = bx[l] * qL[l].d[s], gR = bx[5 + l] * qR[l].d[s];
-      if (gL != T(0)) atomicAdd(bar + c0 + (c - 1 + s - 2) * st + P * l, (double)gL);
-      if (gR != T(0)) atomicAdd(bar + c0 + (c + s - 2) * st + P * l, (double)gR);
-    }
+    for (int s = 0; s < 5; ++s) acc[s + 1] += bx[5 + l] * Rm.d[s];
+#pragma unroll
+    for (int s = 0; s < 6; ++s)
+      if (acc[s] != T(0)) atomicAdd(bar + c0 + (c - 3 + s) * st + P * l, (double)acc[s]);
+  }
 }
 
 // ---- laminar viscous terms (gradients.f90, viscosity.f90, viscous.f90) -----
@@ -659,8 +822,11 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
   for (int dir = 0; dir < 3; ++dir) {
     const int n = extent_of(d, dir);
     const long long nf = (long long)n * ((dir == 0 ? d.jmx : d.imx) - 1) * ((dir == 2 ? d.jmx : d.kmx) - 1);
-    k_vjp_faces<double><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar,
-                                                          bar_faces ? bar_faces[dir] : nullptr, dir);
+    double* bf = bar_faces ? bar_faces[dir] : nullptr;
+    if (p.flux == FEST_FLUX_SLAU)
+      k_vjp_faces<double, true><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bf, dir);
+    else
+      k_vjp_faces<double, false><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bf, dir);
     ++*L.count;
     if (visc) {
       k_vjp_viscous<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bar_grad, dir);

@@ -35,6 +35,7 @@ struct fest_handle {
   double* d_vjp_lam = nullptr;
   double* d_vjp_grad = nullptr;  // laminar adjoint: 12 per interior cell
   double* d_lu = nullptr;        // LU-SGS work arrays, allocated on first use
+  double* d_stage = nullptr;     // interior-cell staging for pageable host arrays
   int* h_err = nullptr;          // pinned host copy of the device error word
   // events around the device work of the last timed call (after its inputs
   // arrived, before its outputs leave): fest_last_kernel_ms
@@ -56,6 +57,12 @@ int cuda_status(cudaError_t e) {
   do {                                         \
     cudaError_t e_ = (x);                      \
     if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+#define RET(x)                \
+  do {                        \
+    int r_ = (x);             \
+    if (r_) return r_;        \
   } while (0)
 
 int dalloc(fest_handle* h, double** p, long long n) {
@@ -86,23 +93,21 @@ Sizes sizes_of(const Dims& d, int n_grad) {
   return z;
 }
 
-// Host arrays that are pinned and mapped (cudaHostAlloc, a framework's
-// pinned-memory pool): the GPU reads and writes them itself, every SM
-// streaming 16-byte words over the CPU-GPU link.  Other host memory, and
-// arrays below 1 MiB (where the copy engine's latency is shorter), go
-// through cudaMemcpyAsync.
-__global__ void k_link_copy(const double* __restrict__ src, double* __restrict__ dst, long long n) {
-  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
-  if ((((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
-    const long long n2 = n / 2;
-    const double2* s2 = reinterpret_cast<const double2*>(src);
-    double2* d2 = reinterpret_cast<double2*>(dst);
-    for (long long t = t0; t < n2; t += st) d2[t] = s2[t];
-    if (t0 == 0 && (n & 1)) dst[n - 1] = src[n - 1];
-  } else {
-    for (long long t = t0; t < n; t += st) dst[t] = src[t];
-  }
+// Whole arrays cross the host link by the copy engines (cudaMemcpyAsync):
+// on this part they move pinned host memory at the link's rate (about
+// 200 GB/s each way, measured against SM copy kernels of every width and
+// grid, which reach the same or slightly less).
+int up(fest_handle* h, double* dst, const double* src, long long n) {
+  if (!src) return FEST_OK;
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, h->s));
+  return FEST_OK;
 }
+int down(fest_handle* h, double* dst, const double* src, long long n) {
+  if (!dst) return FEST_OK;
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->s));
+  return FEST_OK;
+}
+
 // the device address of a pinned, mapped host array, or null
 const void* mapped_alias(const void* host) {
   cudaPointerAttributes at;
@@ -112,28 +117,50 @@ const void* mapped_alias(const void* host) {
   }
   return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
-constexpr long long kLinkMin = 1 << 17;  // doubles
-int link_copy(fest_handle* h, const double* src, double* dst, long long n) {
+
+// interior cells (1..imx-1, 1..jmx-1, 1..kmx-1) of the padded state and a
+// dense (imx-1)(jmx-1)(kmx-1) x n_var array, i fastest: to_padded scatters
+// the dense array into the state, else gathers from it.  Either side may
+// be a pinned, mapped host array, which the threads then read or write
+// over the link directly.
+__global__ void k_interior_copy(Dims d, const double* __restrict__ src, double* __restrict__ dst, int to_padded) {
+  const long long nc = ncells(d), n = nc * d.nv;
+  const long long st = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += st) {
+    const long long l = t / nc, c = t % nc;
+    const int i = 1 + (int)(c % (d.imx - 1));
+    const long long r = c / (d.imx - 1);
+    const int j = 1 + (int)(r % (d.jmx - 1)), k = 1 + (int)(r / (d.jmx - 1));
+    const long long pp = pidx(d, i, j, k) + d.P * l;
+    if (to_padded) dst[pp] = src[t];
+    else dst[t] = src[pp];
+  }
+}
+int interior_copy(fest_handle* h, const double* src, double* dst, int to_padded) {
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_link_copy<<<sms * 4, 256, 0, h->s>>>(src, dst, n);
+  k_interior_copy<<<sms * 4, 256, 0, h->s>>>(h->p.d, src, dst, to_padded);
   ++h->launches;
   CK(cudaGetLastError());
   return FEST_OK;
 }
-int up(fest_handle* h, double* dst, const double* src, long long n) {
-  if (!src) return FEST_OK;
-  if (n >= kLinkMin)
-    if (const void* a = mapped_alias(src)) return link_copy(h, static_cast<const double*>(a), dst, n);
-  CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, h->s));
-  return FEST_OK;
+// host interior array -> the padded device state (ghost cells kept)
+int up_interior(fest_handle* h, double* qdev, const double* host) {
+  const long long n = ncells(h->p.d) * h->p.d.nv;
+  if (const void* a = mapped_alias(host)) return interior_copy(h, static_cast<const double*>(a), qdev, 1);
+  if (!h->d_stage) RET(dalloc(h, &h->d_stage, n));
+  CK(cudaMemcpyAsync(h->d_stage, host, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, h->s));
+  return interior_copy(h, h->d_stage, qdev, 1);
 }
-int down(fest_handle* h, double* dst, const double* src, long long n) {
-  if (!dst) return FEST_OK;
-  if (n >= kLinkMin)
-    if (const void* a = mapped_alias(dst)) return link_copy(h, src, static_cast<double*>(const_cast<void*>(a)), n);
-  CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->s));
+// the padded device state's interior cells -> a host interior array
+int down_interior(fest_handle* h, double* host, const double* qdev) {
+  const long long n = ncells(h->p.d) * h->p.d.nv;
+  if (const void* a = mapped_alias(host))
+    return interior_copy(h, qdev, static_cast<double*>(const_cast<void*>(a)), 0);
+  if (!h->d_stage) RET(dalloc(h, &h->d_stage, n));
+  RET(interior_copy(h, qdev, h->d_stage, 0));
+  CK(cudaMemcpyAsync(host, h->d_stage, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->s));
   return FEST_OK;
 }
 
@@ -156,11 +183,6 @@ int finish(fest_handle* h) {
   return FEST_OK;
 }
 
-#define RET(x)                \
-  do {                        \
-    int r_ = (x);             \
-    if (r_) return r_;        \
-  } while (0)
 
 bool valid_id(int id) { return id >= -11 && id <= -1 ? true : id >= 0; }
 
@@ -896,13 +918,9 @@ int fest_get_next_solution(fest_handle* h, double* qp, int current_iter, double 
   return finish(h);
 }
 
-int fest_find_resnorm(fest_handle* h, double* res_abs) {
-  if (!h || !res_abs) return FEST_ERR_ARG;
-  launch_resnorm(h->p, h->d, h->d_resnorm, h->L());
-  double sums[NVMAX + 1];
-  RET(down(h, sums, h->d_resnorm, h->p.d.nv + 1));
-  RET(finish(h));
-  // setup_scale (resnorm.f90:128-169) and assemble (resnorm.f90:211-225)
+// setup_scale (resnorm.f90:128-169) and assemble (resnorm.f90:211-225)
+// from the device sums of find_resnorm
+static void resnorm_assemble(const fest_handle* h, const double* sums, double* res_abs) {
   const fest_flow& f = h->flow;
   double sc[NVMAX + 1];
   sc[0] = 1.;
@@ -914,6 +932,15 @@ int fest_find_resnorm(fest_handle* h, double* res_abs) {
   sc[7] = f.density_inf * f.vel_mag * f.tw_inf;
   res_abs[0] = fabs(sums[0] / sc[0]);
   for (int l = 1; l <= h->p.d.nv; ++l) res_abs[l] = sqrt(sums[l] / (sc[l] * sc[l]));
+}
+
+int fest_find_resnorm(fest_handle* h, double* res_abs) {
+  if (!h || !res_abs) return FEST_ERR_ARG;
+  launch_resnorm(h->p, h->d, h->d_resnorm, h->L());
+  double sums[NVMAX + 1];
+  RET(down(h, sums, h->d_resnorm, h->p.d.nv + 1));
+  RET(finish(h));
+  resnorm_assemble(h, sums, res_abs);
   return FEST_OK;
 }
 
@@ -940,6 +967,50 @@ int fest_step(fest_handle* h, int n_iters, int first_iter, double CFL, double* r
 
 int fest_step_async(fest_handle* h, int n_iters, int first_iter, double CFL) {
   return step_enqueue(h, n_iters, first_iter, CFL);
+}
+
+int fest_step_host_interior(fest_handle* h, double* q, int n_iters, int first_iter, double CFL,
+                            double* res_abs) {
+  if (!h || !q || n_iters < 0 || needs_batch(h)) return FEST_ERR_ARG;
+  // the interior goes into the state the next step reads: the primary
+  // state, whose ghost cells (the persistent fix() layers among them)
+  // are the handle's own
+  RET(sync_fused(h));
+  RET(up_interior(h, h->d.qp, q));
+  if (h->fused) fused_invalidate(h->fused);
+  kmark(h, 0);
+  RET(step_enqueue(h, n_iters, first_iter, CFL));
+  double sums[NVMAX + 1];
+  if (res_abs) {
+    launch_resnorm(h->p, h->d, h->d_resnorm, h->L());
+    RET(down(h, sums, h->d_resnorm, h->p.d.nv + 1));
+  }
+  kmark(h, 1);
+  const double* cur = fused_current_state(h->fused);
+  RET(down_interior(h, q, cur ? cur : h->d.qp));
+  RET(finish(h));
+  if (res_abs) resnorm_assemble(h, sums, res_abs);
+  return FEST_OK;
+}
+
+int fest_step_host(fest_handle* h, double* qp, int n_iters, int first_iter, double CFL, double* res_abs) {
+  if (!h || !qp || n_iters < 0 || needs_batch(h)) return FEST_ERR_ARG;
+  const long long n = h->p.d.P * h->p.d.nv;
+  RET(up(h, h->d.qp, qp, n));
+  if (h->fused) fused_invalidate(h->fused);
+  kmark(h, 0);
+  RET(step_enqueue(h, n_iters, first_iter, CFL));
+  double sums[NVMAX + 1];
+  if (res_abs) {
+    launch_resnorm(h->p, h->d, h->d_resnorm, h->L());
+    RET(down(h, sums, h->d_resnorm, h->p.d.nv + 1));
+  }
+  kmark(h, 1);
+  const double* cur = fused_current_state(h->fused);
+  RET(down(h, qp, cur ? cur : h->d.qp, n));
+  RET(finish(h));
+  if (res_abs) resnorm_assemble(h, sums, res_abs);
+  return FEST_OK;
 }
 
 struct fest_batch {

@@ -218,6 +218,8 @@ _SIGS = {
     "fest_find_resnorm": [C.c_void_p, _DP],
     "fest_step": [C.c_void_p, C.c_int, C.c_int, C.c_double, _DP],
     "fest_step_async": [C.c_void_p, C.c_int, C.c_int, C.c_double],
+    "fest_step_host": [C.c_void_p, _DP, C.c_int, C.c_int, C.c_double, _DP],
+    "fest_step_host_interior": [C.c_void_p, _DP, C.c_int, C.c_int, C.c_double, _DP],
     "fest_set_stream": [C.c_void_p, C.c_void_p],
     "fest_profile": [C.c_void_p, C.c_int],
     "fest_profile_read": [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)],

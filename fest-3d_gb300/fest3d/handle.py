@@ -126,6 +126,31 @@ class Handle:
                    out.ctypes.data_as(C.POINTER(C.c_double)) if with_norm else None)
         return out[:self.ext.n_var + 1] if with_norm else None
 
+    def step_host(self, qp, n, first_iter, CFL, with_norm=True):
+        """n iterations on the host state qp (padded, F-ordered float64),
+        updated in place; one synchronisation (fest_step_host)."""
+        if not (isinstance(qp, np.ndarray) and qp.dtype == np.float64 and qp.flags.f_contiguous
+                and qp.shape == self.shape["qp"]):
+            raise ValueError(f"qp must be an F-ordered float64 array of shape {self.shape['qp']}")
+        out = np.zeros(8) if with_norm else None
+        self._call("fest_step_host", abi.ptr(qp), int(n), int(first_iter), float(CFL),
+                   out.ctypes.data_as(C.POINTER(C.c_double)) if with_norm else None)
+        return out[:self.ext.n_var + 1] if with_norm else None
+
+    def step_host_interior(self, q, n, first_iter, CFL, with_norm=True):
+        """n iterations on the interior-cell state q ((imx-1, jmx-1, kmx-1,
+        n_var), F-ordered float64), updated in place; ghost cells stay on
+        the device (fest_step_host_interior)."""
+        e = self.ext
+        shape = (e.imx - 1, e.jmx - 1, e.kmx - 1, e.n_var)
+        if not (isinstance(q, np.ndarray) and q.dtype == np.float64 and q.flags.f_contiguous
+                and q.shape == shape):
+            raise ValueError(f"q must be an F-ordered float64 array of shape {shape}")
+        out = np.zeros(8) if with_norm else None
+        self._call("fest_step_host_interior", abi.ptr(q), int(n), int(first_iter), float(CFL),
+                   out.ctypes.data_as(C.POINTER(C.c_double)) if with_norm else None)
+        return out[:self.ext.n_var + 1] if with_norm else None
+
     def residual_vjp(self, qp, it, lam):
         """(dR/dq)^T lam for the residual of iteration it at state qp."""
         q = None if qp is None else self._input(qp, "qp")

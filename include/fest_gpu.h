@@ -250,6 +250,24 @@ int fest_find_resnorm(fest_handle *h, double *res_abs);
 int fest_step(fest_handle *h, int n_iters, int first_iter, double CFL,
               double *res_abs);
 
+/* fest_step on a host state: qp (the padded host array, as
+ * fest_upload_state takes it) goes to the device, n_iters iterations run,
+ * and the state comes back into qp, with one synchronisation for the
+ * whole call: get_next_solution (update.f90:129-226) n_iters times on the
+ * caller's array.  Pinned, mapped host arrays move over the host link by
+ * a copy kernel.  res_abs (nullable) receives the last norm. */
+int fest_step_host(fest_handle *h, double *qp, int n_iters, int first_iter, double CFL,
+                   double *res_abs);
+/* fest_step_host on the interior cells only: q is a dense
+ * (imx-1)(jmx-1)(kmx-1) x n_var array (i fastest, the cell-centred
+ * solution without ghost layers, as the reference's output files hold
+ * it).  The ghost cells stay the handle's own: every BC refills them from
+ * the interior at each stage, and the fix() layers written in iterations
+ * 1-2 persist on the device as they do in the reference's qp.  Pinned,
+ * mapped arrays are read and written by the GPU over the host link. */
+int fest_step_host_interior(fest_handle *h, double *q, int n_iters, int first_iter, double CFL,
+                            double *res_abs);
+
 /* enqueue fest_step's work on the handle's stream and return at once;
  * errors surface at the next synchronous call (fest_last_device_error) */
 int fest_step_async(fest_handle *h, int n_iters, int first_iter, double CFL);
@@ -262,8 +280,9 @@ int fest_set_stream(fest_handle *h, void *cuda_stream);
 int fest_profile(fest_handle *h, int enable);
 int fest_profile_read(fest_handle *h, long long *launches, double *total_ms);
 /* device time (CUDA events on the handle's stream) of the kernels of the
- * last fest_step, fest_get_total_conservative_residue or fest_residual_vjp
- * call: from after its host inputs arrived to before its outputs left */
+ * last fest_step, fest_step_host, fest_get_total_conservative_residue or
+ * fest_residual_vjp call: from after its host inputs arrived to before its
+ * outputs left */
 int fest_last_kernel_ms(fest_handle *h, double *ms);
 
 /* ---- batches ------------------------------------------------------------- */

@@ -85,7 +85,7 @@ def assert_residual(gpu_res, blk, rtol=RTOL, what="residue"):
 
 
 def small_case(nc=(9, 7, 6), ids=(-5, -5, -5, -3, -10, -10), scheme_kw=None, flow_kw=None,
-               turb=False, perturb=0.15, seed=1, partners=None, fixed=None):
+               turb=False, perturb=0.15, seed=1, partners=None, fixed=None, state_mach=0.3):
     ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 7 if turb else 5)
     fk = dict(density_inf=1.2, x_speed_inf=60.0, y_speed_inf=5.0, pressure_inf=101325.0)
     fk.update(flow_kw or {})
@@ -116,5 +116,5 @@ def small_case(nc=(9, 7, 6), ids=(-5, -5, -5, -3, -10, -10), scheme_kw=None, flo
                 partners[f] = (0, f ^ 1)
     bc = abi.make_bc(list(ids), partners=partners, **fx)
     nodes = cases.box_nodes(ext, L=(1.0, 0.8, 0.6), perturb=perturb, seed=seed)
-    qp = cases.random_state(ext, seed=seed + 7, mach=0.3)
+    qp = cases.random_state(ext, seed=seed + 7, mach=state_mach)
     return ext, flow, scheme, bc, nodes, qp

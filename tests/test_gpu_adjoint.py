@@ -25,6 +25,10 @@ CASES = {
                       ids=(-11, -4, -6, -6, -10, -10)),
     "muscl-slau": dict(scheme_kw=dict(interpolant="muscl", scheme_name="slau"),
                        ids=(-11, -4, -6, -6, -10, -10)),
+    # speeds up to 1.6 c: the capped Mach number and the supersonic
+    # branches of the SLAU reverse sweep
+    "muscl-slau-supersonic": dict(scheme_kw=dict(interpolant="muscl", scheme_name="slau"),
+                                  ids=(-1, -2, -6, -5, -10, -10), state_mach=1.6),
     "muscl-ausm-wall": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ausm"),
                             ids=(-3, -4, -5, -6, -10, -10)),
     "ppm-ausmP": dict(scheme_kw=dict(interpolant="ppm", scheme_name="ausmP"),

@@ -246,3 +246,67 @@ def test_mixed_block_with_many_rows(gpu_lib):
         assert O.get_next_solution([blk], it, 0.5) == 0
     e = rel_err(interior(h.download_state(), ext), interior(blk["qp"], ext))
     assert e <= 2e-5, f"mixed interior state differs by {e:.3e}"
+
+
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
+@pytest.mark.parametrize("precision", [abi.FEST_FP64, abi.FEST_MIXED], ids=["fp64", "mixed"])
+def test_step_host_equals_upload_step_download(gpu_lib, precision, pinned):
+    """fest_step_host (one synchronisation) leaves in the caller's array the
+    state that upload + fest_step + download leave, bit for bit, and the
+    same norm; pinned host memory moves through the host-link copy kernel
+    (the bump block's state is above its 1 MiB threshold)."""
+    import torch
+    case = cases.bump_case(nc=(64, 24, 4))
+    ext = case["ext"]
+    _, h1 = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    _, h2 = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    for h in (h1, h2):
+        h.set_precision(precision)
+    if pinned:
+        buf = torch.empty(abi.shapes(ext)["qp"][::-1], dtype=torch.float64, pin_memory=True)
+        q = buf.numpy().T
+    else:
+        q = np.zeros(abi.shapes(ext)["qp"], order="F")
+    q[...] = case["qp"]
+    it = 1
+    for _ in range(3):
+        n2 = h2.step_host(q, 2, it, case["CFL"])
+        h1.upload_state(h1.download_state())  # the same invalidation as an upload
+        n1 = h1.step(2, it, case["CFL"])
+        it += 2
+        ref = h1.download_state()
+        assert np.array_equal(q, ref)
+        assert np.allclose(n1, n2, rtol=1e-13, atol=0)
+    h1.close()
+    h2.close()
+
+
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
+def test_step_host_interior_equals_device_steps(gpu_lib, pinned):
+    """fest_step_host_interior on the interior cells (ghost cells kept on
+    the device) leaves the interior that fest_step leaves, bit for bit,
+    over calls that start in iterations 1-2 (fix() ghosts) and after."""
+    import torch
+    case = cases.bump_case(nc=(64, 24, 4))
+    ext = case["ext"]
+    _, h1 = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    _, h2 = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    for h in (h1, h2):
+        h.set_precision(abi.FEST_MIXED)
+    shape = (ext.imx - 1, ext.jmx - 1, ext.kmx - 1, ext.n_var)
+    if pinned:
+        buf = torch.empty(shape[::-1], dtype=torch.float64, pin_memory=True)
+        q = buf.numpy().T
+    else:
+        q = np.zeros(shape, order="F")
+    sl = (slice(3, ext.imx + 2), slice(3, ext.jmx + 2), slice(3, ext.kmx + 2))
+    q[...] = case["qp"][sl]
+    it = 1
+    for n in (1, 2, 3):
+        n2 = h2.step_host_interior(q, n, it, case["CFL"])
+        n1 = h1.step(n, it, case["CFL"])
+        it += n
+        assert np.array_equal(q, h1.download_state()[sl])
+        assert np.allclose(n1, n2, rtol=1e-13, atol=0)
+    h1.close()
+    h2.close()
