@@ -389,6 +389,7 @@ int next_solution_fp64(fest_handle* h, int it, double CFL) {
       residual_fp64(h, it); launch_update(p, h->d, 1.0, 1., 0, 0, L);
       launch_blend(p, h->d, 0.5, 0.5, L);
       break;
+    case FEST_TIME_PLUSGS:    // update.f90:219-222
     case FEST_TIME_IMPLICIT:  // update.f90:215-218
       residual_fp64(h, it);
       launch_time_step(p, h->d, CFL, L);
@@ -415,7 +416,7 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
   if (scheme->scheme_name < 0 || scheme->scheme_name > 5) return FEST_ERR_ARG;
   if (scheme->interpolant < 0 || scheme->interpolant > 4) return FEST_ERR_ARG;
   if (scheme->turbulence < 0 || scheme->turbulence > 2) return FEST_ERR_ARG;
-  if (scheme->time_step_accuracy < 0 || scheme->time_step_accuracy > FEST_TIME_IMPLICIT) return FEST_ERR_ARG;
+  if (scheme->time_step_accuracy < 0 || scheme->time_step_accuracy > FEST_TIME_PLUSGS) return FEST_ERR_ARG;
   if (scheme->time_stepping_method != 'l' && scheme->time_stepping_method != 'g') return FEST_ERR_ARG;
   for (int f = 0; f < 6; ++f) {
     if (!valid_id(bc->id[f])) return FEST_ERR_ARG;
@@ -1031,12 +1032,13 @@ int fest_batch_create(fest_handle* const* blocks, int n_blocks, fest_batch** out
   fest_handle* h0 = blocks[0];
   if (!h0) return FEST_ERR_ARG;
   const int prec = h0->precision;
-  const bool implicit = h0->sc.time_step_accuracy == FEST_TIME_IMPLICIT;
+  const int integ0 = h0->sc.time_step_accuracy;
+  const bool implicit = integ0 == FEST_TIME_IMPLICIT || integ0 == FEST_TIME_PLUSGS;
   for (int n = 0; n < n_blocks; ++n) {
     fest_handle* h = blocks[n];
     if (!h || h->precision != prec) return FEST_ERR_ARG;
     if (implicit) {  // LU-SGS: FP64 module path, every block implicit
-      if (prec != FEST_FP64 || h->sc.time_step_accuracy != FEST_TIME_IMPLICIT) return FEST_ERR_ARG;
+      if (prec != FEST_FP64 || h->sc.time_step_accuracy != integ0) return FEST_ERR_ARG;
     } else if (!fused_supported(h->p, prec)) {
       return FEST_ERR_ARG;
     }

@@ -1,6 +1,8 @@
-// fest_lusgs.cu - the implicit integrator of the reference: one residual,
+// fest_lusgs.cu - the implicit integrators of the reference: one residual,
 // the local time step, then update_with_lusgs (update.f90:215-218,
-// lusgs.f90:134-1196), for laminar and k-omega SST blocks, FP64.
+// lusgs.f90:134-1196) or its low-Mach preconditioned form
+// update_with_plusgs (update.f90:219-222, plusgs.f90:139-1431), for laminar
+// and k-omega SST blocks, FP64.
 //
 // The reference sweeps the interior cells forward (i fastest, then j, k)
 // computing dQ* from the dQ* of each cell's three lower neighbours, then
@@ -113,6 +115,60 @@ __device__ double lu_radius(const Params& p, const double* qa, const double* qb,
   return (vn + c + vis) * f.A;
 }
 
+// plusgs.f90:723-776 SpectralRadius of the preconditioned system: eps is
+// the cell's own min(1, max(M^2, Minf^2)), the viscous part twice LU-SGS's
+__device__ double plu_radius(const Params& p, const double* qa, const double* qb, const LuFace& f,
+                             const double* ca, const double* cb, double eps) {
+  const double gm = p.gm;
+  const double vn = fabs(0.5 * (((qa[1] + qb[1]) * f.nx) + ((qa[2] + qb[2]) * f.ny) + ((qa[3] + qb[3]) * f.nz)));
+  const double c = 0.5 * (sqrt(gm * qa[4] / qa[0]) + sqrt(gm * qb[4] / qb[0]));
+  const double rho = 0.5 * (qa[0] + qb[0]);
+  const double dx = ca[1] - cb[1], dy = ca[2] - cb[2], dz = ca[3] - cb[3];
+  const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+  const double vis = 2.0 * gm * (f.mu / p.Pr + f.mut / p.tPr) / (rho * dist);
+  return (0.5 * ((1.0 + eps) * vn + sqrt(((eps - 1.0) * (eps - 1.0)) * (vn * vn) + 4 * eps * (c * c))) + vis) * f.A;
+}
+
+// plusgs.f90:345-396 and 944-1014: the cell's inverse preconditioner
+// P = I - (factor x) c^T with x = (1, u, v, w, H[, k, omega]) and
+// c = (|V|^2/2, -u, -v, -w, 1[, -1, 0]); H as the reference has it, with
+// 0.5 |V| (not |V|^2)
+template <int N>
+struct PluP {
+  double fx[N], u, v, w, VMag, eps;
+  __device__ PluP(const Params& p, const double* q0) {
+    const double gm = p.gm, r = q0[0], pr = q0[4];
+    u = q0[1];
+    v = q0[2];
+    w = q0[3];
+    VMag = sqrt(u * u + v * v + w * w);
+    const double SoundMag = sqrt(gm * pr / r);
+    const double M = VMag / SoundMag;
+    const double H = (gm * pr / (r * (gm - 1.0))) + 0.5 * (VMag);
+    eps = fmin(1.0, fmax(M * M, p.MInf * p.MInf));
+    const double factor = (1.0 - eps) * (gm - 1.0) / (SoundMag * SoundMag);
+    const double x[7] = {1.0, u, v, w, H, N == 7 ? q0[5 % N] : 0.0, N == 7 ? q0[6 % N] : 0.0};
+#pragma unroll
+    for (int i = 0; i < N; ++i) fx[i] = factor * x[i];
+  }
+  // out = P y, each entry summed over the columns in order
+  __device__ void apply(const double* y, double* out) const {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      double s = ((i == 0 ? 1.0 : 0.0) - fx[i] * VMag * VMag / 2.0) * y[0];
+      s = s + ((i == 1 ? 1.0 : 0.0) - fx[i] * (-u)) * y[1];
+      s = s + ((i == 2 ? 1.0 : 0.0) - fx[i] * (-v)) * y[2];
+      s = s + ((i == 3 ? 1.0 : 0.0) - fx[i] * (-w)) * y[3];
+      s = s + ((i == 4 ? 1.0 : 0.0) - fx[i] * (1.)) * y[4];
+      if constexpr (N == 7) {
+        s = s + ((i == 5 ? 1.0 : 0.0) - fx[i] * (-1.)) * y[5];
+        s = s + ((i == 6 ? 1.0 : 0.0) - fx[i] * (0.)) * y[6];
+      }
+      out[i] = s;
+    }
+  }
+};
+
 struct LuDev {
   double *lam, *D, *Fold;  // per interior cell: 6, n and 6n values
   double *dqs, *dq;        // (0:imx, 0:jmx, 0:kmx, n), zero outside the interior
@@ -148,7 +204,7 @@ __host__ __device__ __forceinline__ long long lu_count(const Dims& d) {
 }
 
 // everything of a cell that the sweeps do not change
-template <int N>
+template <int N, bool PLUS>
 __global__ void k_lu_prep(Params p, DevBlock b, LuDev u) {
   const Dims& d = p.d;
   const long long nc = ncells(d);
@@ -160,7 +216,8 @@ __global__ void k_lu_prep(Params p, DevBlock b, LuDev u) {
   double q0[N];
 #pragma unroll
   for (int l = 0; l < N; ++l) q0[l] = b.qp[c0 + d.P * l];
-  double sumlam = 0.0, lam[6];
+  double sumlam = 0.0, lam[6], eps = 0.0;
+  if constexpr (PLUS) eps = PluP<N>(p, q0).eps;
   for (int s = 0; s < 6; ++s) {
     LuFace fc;
     long long nb;
@@ -171,7 +228,10 @@ __global__ void k_lu_prep(Params p, DevBlock b, LuDev u) {
       qn[l] = b.qp[nb + d.P * l];
       zero[l] = 0.0;
     }
-    lam[s] = lu_radius(p, qn, q0, fc, b.cells + 4 * nb, b.cells + 4 * c0);
+    if constexpr (PLUS)
+      lam[s] = plu_radius(p, qn, q0, fc, b.cells + 4 * nb, b.cells + 4 * c0, eps);
+    else
+      lam[s] = lu_radius(p, qn, q0, fc, b.cells + 4 * nb, b.cells + 4 * c0);
     lu_flux<N>(p, qn, q0, zero, fc, F);
 #pragma unroll
     for (int l = 0; l < N; ++l) u.Fold[t + nc * (s * N + l)] = F[l];
@@ -193,7 +253,7 @@ __global__ void k_lu_prep(Params p, DevBlock b, LuDev u) {
 
 // the cells of hyperplane i+j+k = s: one thread per (j, k), i = s - j - k;
 // pass 0 the forward sweep (dQ*), pass 1 the backward one (dQ)
-template <int N>
+template <int N, bool PLUS>
 __global__ void k_lu_plane(Params p, DevBlock b, LuDev u, int pass, int s) {
   const Dims& d = p.d;
   const int nj = d.jmx - 1, nk = d.kmx - 1;
@@ -225,14 +285,33 @@ __global__ void k_lu_plane(Params p, DevBlock b, LuDev u, int pass, int s) {
     lu_flux<N>(p, qn, q0, dn, fc, fnew);
     const double lam = u.lam[c + nc * sface];
 #pragma unroll
-    for (int l = 0; l < N; ++l) acc[l] = acc[l] + ((fnew[l] - u.Fold[c + nc * (sface * N + l)]) - lam * dn[l]);
+    for (int l = 0; l < N; ++l) fnew[l] = fnew[l] - u.Fold[c + nc * (sface * N + l)];
+    if constexpr (PLUS) {
+      double pf[N];
+      PluP<N>(p, q0).apply(fnew, pf);
+#pragma unroll
+      for (int l = 0; l < N; ++l) fnew[l] = pf[l];
+    }
+#pragma unroll
+    for (int l = 0; l < N; ++l) acc[l] = acc[l] + (fnew[l] - lam * dn[l]);
+  }
+  double rr[N];
+#pragma unroll
+  for (int l = 0; l < N; ++l) rr[l] = b.res[c + nc * l];
+  if constexpr (PLUS) {
+    if (pass == 0) {
+      double pr[N];
+      PluP<N>(p, q0).apply(rr, pr);
+#pragma unroll
+      for (int l = 0; l < N; ++l) rr[l] = pr[l];
+    }
   }
   const long long o = lu_idx(d, i, j, k);
 #pragma unroll
   for (int l = 0; l < N; ++l) {
     const double D = u.D[c + nc * l];
     if (pass == 0)
-      u.dqs[o + L * l] = (-b.res[c + nc * l] - 0.5 * acc[l]) / D;
+      u.dqs[o + L * l] = (-rr[l] - 0.5 * acc[l]) / D;
     else
       u.dq[o + L * l] = u.dqs[o + L * l] - 0.5 * acc[l] / D;
   }
@@ -277,12 +356,12 @@ __global__ void k_lu_apply(Params p, DevBlock b, LuDev u) {
   if (!(q[0] >= 0.0) || !(q[4] >= 0.0)) raise_error(b.err, FEST_ERR_NEGATIVE_STATE);
 }
 
-template <int N>
+template <int N, bool PLUS>
 void lusgs_t(const Params& p, const DevBlock& b, const LuDev& u, const Launcher& L) {
   const Dims& d = p.d;
   const long long nc = ncells(d);
   const unsigned g = (unsigned)((nc + 127) / 128);
-  k_lu_prep<N><<<g, 128, 0, L.s>>>(p, b, u);
+  k_lu_prep<N, PLUS><<<g, 128, 0, L.s>>>(p, b, u);
   ++*L.count;
   // dQ* and dQ are zero outside the interior (the layer the sweeps read)
   const size_t bytes = sizeof(double) * (size_t)lu_count(d) * N;
@@ -292,11 +371,11 @@ void lusgs_t(const Params& p, const DevBlock& b, const LuDev& u, const Launcher&
   const unsigned gp = (unsigned)((nt + 63) / 64);  // small CTAs: a plane spreads over the SMs
   const int smax = (d.imx - 1) + (d.jmx - 1) + (d.kmx - 1);
   for (int s = 3; s <= smax; ++s) {
-    k_lu_plane<N><<<gp, 64, 0, L.s>>>(p, b, u, 0, s);
+    k_lu_plane<N, PLUS><<<gp, 64, 0, L.s>>>(p, b, u, 0, s);
     ++*L.count;
   }
   for (int s = smax; s >= 3; --s) {
-    k_lu_plane<N><<<gp, 64, 0, L.s>>>(p, b, u, 1, s);
+    k_lu_plane<N, PLUS><<<gp, 64, 0, L.s>>>(p, b, u, 1, s);
     ++*L.count;
   }
   k_lu_apply<N><<<g, 128, 0, L.s>>>(p, b, u);
@@ -318,8 +397,9 @@ void launch_lusgs(const Params& p, const DevBlock& b, double* scratch, const Lau
   u.Fold = u.D + d.nv * nc;
   u.dqs = u.Fold + 6 * d.nv * nc;
   u.dq = u.dqs + lu_count(d) * d.nv;
-  if (d.nv == 7) lusgs_t<7>(p, b, u, L);
-  else lusgs_t<5>(p, b, u, L);
+  const bool plus = p.integ == FEST_TIME_PLUSGS;
+  if (d.nv == 7) plus ? lusgs_t<7, true>(p, b, u, L) : lusgs_t<7, false>(p, b, u, L);
+  else plus ? lusgs_t<5, true>(p, b, u, L) : lusgs_t<5, false>(p, b, u, L);
 }
 
 }  // namespace fest

@@ -30,7 +30,7 @@ ERR_NAMES = {0: "FEST_OK", 1: "FEST_ERR_ARG", 2: "FEST_ERR_CUDA", 3: "FEST_ERR_N
 
 FLUX = {"ausm": 0, "ausmP": 1, "ausmUP": 2, "slau": 3, "ldfss0": 4, "van_leer": 5}
 INTERP = {"none": 0, "muscl": 1, "ppm": 2, "weno": 3, "weno_NM": 4}
-TIME = {"none": 0, "RK2": 1, "RK4": 2, "TVDRK2": 3, "TVDRK3": 4, "implicit": 5}
+TIME = {"none": 0, "RK2": 1, "RK4": 2, "TVDRK2": 3, "TVDRK3": 4, "implicit": 5, "plusgs": 6}
 TURB = {"none": 0, "sst": 1, "sst2003": 2}
 MU = {"constant": 0, "sutherland_law": 1}
 LIMITER = {"koren": 0, "van_albada": 1}

@@ -59,9 +59,12 @@ enum { FEST_INTERP_NONE = 0, FEST_INTERP_MUSCL = 1, FEST_INTERP_PPM = 2,
        FEST_INTERP_WENO = 3, FEST_INTERP_WENO_NM = 4 };
 /* FEST_TIME_IMPLICIT: the reference's "implicit" (update.f90:215-218), one
  * residual and time step, then the LU-SGS update of lusgs.f90:134-1196
- * (laminar and k-omega SST, FP64, module path; batches of blocks too) */
+ * (laminar and k-omega SST, FP64, module path; batches of blocks too).
+ * FEST_TIME_PLUSGS: its "plusgs" (update.f90:219-222), the same with the
+ * low-Mach preconditioned update of plusgs.f90:139-1431. */
 enum { FEST_TIME_NONE = 0, FEST_TIME_RK2 = 1, FEST_TIME_RK4 = 2,
-       FEST_TIME_TVDRK2 = 3, FEST_TIME_TVDRK3 = 4, FEST_TIME_IMPLICIT = 5 };
+       FEST_TIME_TVDRK2 = 3, FEST_TIME_TVDRK3 = 4, FEST_TIME_IMPLICIT = 5,
+       FEST_TIME_PLUSGS = 6 };
 enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2 };
 enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
 /* MUSCL limiter: the reference hard-codes Koren's alpha family

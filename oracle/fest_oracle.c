@@ -1935,12 +1935,66 @@ static double lu_radius(const fest_flow *fl, const double *qa, const double *qb,
   return (vn + c + vis) * f->A;
 }
 
+/* plusgs.f90:723-776 SpectralRadius of the low-Mach preconditioned system:
+ * eps is the cell's own min(1, max(M^2, Minf^2)), and the viscous part is
+ * twice LU-SGS's */
+static double plu_radius(const fest_flow *fl, const double *qa, const double *qb, const lu_face *f,
+                         const double *ca, const double *cb, double eps) {
+  const double gm = fl->gm;
+  double vn = fabs(0.5 * (((qa[1] + qb[1]) * f->nx) + ((qa[2] + qb[2]) * f->ny) + ((qa[3] + qb[3]) * f->nz)));
+  double c = 0.5 * (sqrt(gm * qa[4] / qa[0]) + sqrt(gm * qb[4] / qb[0]));
+  double rho = 0.5 * (qa[0] + qb[0]);
+  double dx = ca[0] - cb[0], dy = ca[1] - cb[1], dz = ca[2] - cb[2];
+  double dist = sqrt(dx * dx + dy * dy + dz * dz);
+  double vis = 2.0 * gm * (f->mu / fl->Pr + f->mut / fl->tPr) / (rho * dist);
+  return (0.5 * ((1.0 + eps) * vn + sqrt(((eps - 1.0) * (eps - 1.0)) * (vn * vn) + 4 * eps * (c * c))) + vis) * f->A;
+}
+
+/* plusgs.f90:345-396 (laminar), 944-1014 (SST): the cell's eps and the
+ * inverse preconditioner P = I - factor x c^T, x = (1, u, v, w, H[, k,
+ * omega]), c = (|V|^2/2, -u, -v, -w, 1[, -1, 0]), H with the reference's
+ * 0.5 |V| (not |V|^2), each entry in the reference's evaluation order */
+static double plu_precond(const fest_flow *fl, int n, const double *q0, double P[7][7]) {
+  const double gm = fl->gm;
+  double r = q0[0], u = q0[1], v = q0[2], w = q0[3], p = q0[4];
+  double VMag = sqrt(u * u + v * v + w * w);
+  double SoundMag = sqrt(gm * p / r);
+  double M = VMag / SoundMag;
+  double H = (gm * p / (r * (gm - 1.0))) + 0.5 * (VMag);
+  double eps = fmin(1.0, fmax(M * M, fl->MInf * fl->MInf));
+  double factor = (1.0 - eps) * (gm - 1.0) / (SoundMag * SoundMag);
+  double x[7] = {1, u, v, w, H, n == 7 ? q0[5] : 0, n == 7 ? q0[6] : 0};
+  for (int i = 0; i < n; ++i) {
+    double fx = factor * x[i];
+    P[i][0] = (i == 0 ? 1.0 : 0.0) - fx * VMag * VMag / 2.0;
+    P[i][1] = (i == 1 ? 1.0 : 0.0) - fx * (-u);
+    P[i][2] = (i == 2 ? 1.0 : 0.0) - fx * (-v);
+    P[i][3] = (i == 3 ? 1.0 : 0.0) - fx * (-w);
+    P[i][4] = (i == 4 ? 1.0 : 0.0) - fx * (1.);
+    if (n == 7) {
+      P[i][5] = (i == 5 ? 1.0 : 0.0) - fx * (-1.);
+      P[i][6] = (i == 6 ? 1.0 : 0.0) - fx * (0.);
+    }
+  }
+  return eps;
+}
+
+static void plu_apply(int n, double P[7][7], const double *y, double *out) {
+  for (int i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) s = s + P[i][j] * y[j];
+    out[i] = s;
+  }
+}
+
 /* lusgs.f90:186-488 update_laminar_variables, 686-1024
  * update_SST_variables: forward sweep for dQ*, back sweep for dQ, then the
  * conservative update of the interior cells (k and omega only where they
  * stay positive).  dQ is zero outside the block, so neighbouring blocks do
- * not couple. */
-static void lu_sgs(fo_block *b) {
+ * not couple.  With plus, the low-Mach preconditioned form of
+ * plusgs.f90:191-577 and 779-1256: P applied to the residual and to the
+ * flux differences, the preconditioned spectral radii. */
+static void lu_sgs(fo_block *b, int plus) {
   const fest_flow *fl = &b->flow;
   const int imx = IMX, jmx = JMX, kmx = KMX, n = NV, sst = is_sst(b);
   V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), F1 = vpad(b, FO_F1), r = vres(b), dt = vdt(b);
@@ -1963,10 +2017,11 @@ static void lu_sgs(fo_block *b) {
         j = jmx - 1 - (c / (kmx - 1)) % (jmx - 1);
         i = imx - 1 - c / ((kmx - 1) * (jmx - 1));
       }
-      double q0[7], qn[6][7], lam[6], sumlam = 0.;
+      double q0[7], qn[6][7], lam[6], sumlam = 0., P[7][7], eps = 0.0;
       lu_face fc[6];
       const double *c0 = r4(cl, i, j, k) + 1;
       for (int l = 0; l < n; ++l) q0[l] = *at(q, i, j, k, l + 1);
+      if (plus) eps = plu_precond(fl, n, q0, P);
       for (int s = 0; s < 6; ++s) { /* 0..2 low i/j/k neighbour, 3..5 high */
         int d = s % 3, hi = s / 3;
         int ni = i + (hi ? off[d][0] : -off[d][0]), nj = j + (hi ? off[d][1] : -off[d][1]),
@@ -1982,7 +2037,8 @@ static void lu_sgs(fo_block *b) {
         fc[s].mut = sst ? 0.5 * (*at(mut, ni, nj, nk, 1) + *at(mut, i, j, k, 1)) : 0.0;
         fc[s].F1 = sst ? 0.5 * (*at(F1, ni, nj, nk, 1) + *at(F1, i, j, k, 1)) : 0.0;
         for (int l = 0; l < n; ++l) qn[s][l] = *at(q, ni, nj, nk, l + 1);
-        lam[s] = lu_radius(fl, qn[s], q0, &fc[s], r4(cl, ni, nj, nk) + 1, c0);
+        lam[s] = plus ? plu_radius(fl, qn[s], q0, &fc[s], r4(cl, ni, nj, nk) + 1, c0, eps)
+                      : lu_radius(fl, qn[s], q0, &fc[s], r4(cl, ni, nj, nk) + 1, c0);
       }
       for (int s = 0; s < 6; ++s) sumlam = sumlam + lam[s];
       const double vol = r4(cl, i, j, k)[0];
@@ -2003,11 +2059,17 @@ static void lu_sgs(fo_block *b) {
         for (int l = 0; l < n; ++l) dn[l] = *at(src, ni, nj, nk, l + 1);
         lu_flux(fl, n, qn[s], q0, dn, &fc[s], fnew);
         lu_flux(fl, n, qn[s], q0, zero, &fc[s], fold);
-        for (int l = 0; l < n; ++l) acc[l] = acc[l] + ((fnew[l] - fold[l]) - lam[s] * dn[l]);
+        double df[7], pdf[7];
+        for (int l = 0; l < n; ++l) df[l] = fnew[l] - fold[l];
+        if (plus) plu_apply(n, P, df, pdf);
+        for (int l = 0; l < n; ++l) acc[l] = acc[l] + ((plus ? pdf[l] : df[l]) - lam[s] * dn[l]);
       }
+      double rr[7], pr[7];
+      for (int l = 0; l < n; ++l) rr[l] = *at(r, i, j, k, l + 1);
+      if (plus) plu_apply(n, P, rr, pr);
       for (int l = 0; l < n; ++l) {
         if (pass == 0)
-          *at(dqs, i, j, k, l + 1) = (-*at(r, i, j, k, l + 1) - 0.5 * acc[l]) / D[l];
+          *at(dqs, i, j, k, l + 1) = (-(plus ? pr[l] : rr[l]) - 0.5 * acc[l]) / D[l];
         else
           *at(dq, i, j, k, l + 1) = *at(dqs, i, j, k, l + 1) - 0.5 * acc[l] / D[l];
       }
@@ -2038,9 +2100,10 @@ static void lu_sgs(fo_block *b) {
   free(dq.p);
 }
 
-/* update.f90:215-218: one implicit iteration; laminar and k-omega SST
- * blocks (lusgs.f90:158-164) */
-int fo_lusgs_next_solution(fo_block **bl, int nb, int it, double CFL) {
+/* update.f90:215-218 (LU-SGS) and 219-222 (PLU-SGS): one implicit
+ * iteration; laminar and k-omega SST blocks (lusgs.f90:158-164,
+ * plusgs.f90:161-170) */
+static int implicit_next_solution(fo_block **bl, int nb, int it, double CFL, int plus) {
   for (int n = 0; n < nb; ++n) {
     int t = bl[n]->sc.turbulence;
     if (!((t == FEST_TURB_NONE && bl[n]->d.n_var == 5) || ((t == FEST_TURB_SST || t == FEST_TURB_SST2003) && bl[n]->d.n_var == 7)))
@@ -2050,9 +2113,17 @@ int fo_lusgs_next_solution(fo_block **bl, int nb, int it, double CFL) {
   int err = fo_get_total_conservative_residue(bl, nb, it);
   for (int n = 0; n < nb; ++n) {
     fo_compute_time_step(bl[n], CFL);
-    lu_sgs(bl[n]);
+    lu_sgs(bl[n], plus);
   }
   return err;
+}
+
+int fo_lusgs_next_solution(fo_block **bl, int nb, int it, double CFL) {
+  return implicit_next_solution(bl, nb, it, CFL, 0);
+}
+
+int fo_plusgs_next_solution(fo_block **bl, int nb, int it, double CFL) {
+  return implicit_next_solution(bl, nb, it, CFL, 1);
 }
 
 /* resnorm.f90:128-225 */

@@ -71,6 +71,7 @@ int fo_get_next_solution(fo_block **blocks, int nb, int current_iter, double CFL
  * (FEST_ERR_ARG otherwise): kept to replay the reference's own implicit
  * test runs */
 int fo_lusgs_next_solution(fo_block **blocks, int nb, int current_iter, double CFL);
+int fo_plusgs_next_solution(fo_block **blocks, int nb, int current_iter, double CFL);
 /* res_abs[0..n_var] (resnorm.f90:171-225) */
 void fo_find_resnorm(fo_block **blocks, int nb, double *res_abs);
 

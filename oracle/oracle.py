@@ -86,6 +86,7 @@ def lib():
         L.fo_get_total_conservative_residue.argtypes = [pvp, ip, ip]
         L.fo_get_next_solution.argtypes = [pvp, ip, ip, C.c_double]
         L.fo_lusgs_next_solution.argtypes = [pvp, ip, ip, C.c_double]
+        L.fo_plusgs_next_solution.argtypes = [pvp, ip, ip, C.c_double]
         L.fo_find_resnorm.argtypes = [pvp, ip, dp]
         L.fo_find_resnorm.restype = None
         _lib = L
@@ -202,6 +203,12 @@ def lusgs_next_solution(blocks, it, CFL):
     """one iteration of the reference's implicit LU-SGS integrator (laminar
     blocks), for replaying the reference's implicit test runs"""
     return lib().fo_lusgs_next_solution(_arr(blocks), len(blocks), int(it), float(CFL))
+
+
+def plusgs_next_solution(blocks, it, CFL):
+    """one iteration of the reference's low-Mach preconditioned PLU-SGS
+    integrator (plusgs.f90, laminar and k-omega SST blocks)"""
+    return lib().fo_plusgs_next_solution(_arr(blocks), len(blocks), int(it), float(CFL))
 
 
 def find_resnorm(blocks):

@@ -221,3 +221,35 @@ def test_oracle_sst_flat_plate_drag_passes_the_reference_test():
     mu = plate["mu"][3:plate.ext.imx + 2, 3, 3]  # the first cells' laminar viscosity
     cd = drag_coefficient(plate, length_span=2 * 0.04, rho=MF.T_RHO, u=MF.T_U, mu=mu)
     assert abs(cd - SST_CD) <= 0.02 * SST_CD, cd
+
+
+def test_plusgs_restatement_properties():
+    """The oracle's PLU-SGS (plusgs.f90:191-577, 779-1256) where its
+    preconditioner is the identity: with every cell's Mach number capped
+    from below by a free-stream Mach number of 1.2, eps = 1, P = I and the
+    preconditioned spectral radius (0.5 (2 |Vn| + sqrt(4 c^2))) equals
+    LU-SGS's |Vn| + c, so an inviscid block advances as LU-SGS advances it,
+    bit for bit; at Mach 0.2 the preconditioner acts and the iterates
+    differ."""
+    import numpy as np
+    from fest3d import post
+    from parity import small_case
+
+    def run(fn, n, CFL, mach):
+        kw = dict(nc=(9, 7, 6), ids=(-3, -4, -6, -6, -10, -10),
+                  scheme_kw=dict(interpolant="muscl", scheme_name="ausm"), flow_kw=dict(MInf=mach))
+        ext, flow, scheme, bc, nodes, qp = small_case(**kw)
+        b = O.Block(ext, flow, scheme, bc)
+        b["nodes"] = nodes
+        b.setup_geometry()
+        b["qp"] = qp
+        for it in range(1, n + 1):
+            assert fn([b], it, CFL) == 0
+        return np.array(b["qp"]), ext
+
+    a, ext = run(O.lusgs_next_solution, 3, 50.0, 1.2)
+    b, _ = run(O.plusgs_next_solution, 3, 50.0, 1.2)
+    assert np.array_equal(post.interior(a, ext), post.interior(b, ext))
+    a, _ = run(O.lusgs_next_solution, 3, 50.0, 0.2)
+    b, _ = run(O.plusgs_next_solution, 3, 50.0, 0.2)
+    assert np.abs(post.interior(a, ext) - post.interior(b, ext)).max() > 1e-3

@@ -1,14 +1,17 @@
-"""The implicit integrator (LU-SGS, lusgs.f90:134-1196) on the GPU against
-the oracle's restatement of it, and the reference's own laminar
-flat-plate run replayed on the GPU.
+"""The implicit integrators (LU-SGS, lusgs.f90:134-1196, and its low-Mach
+preconditioned form PLU-SGS, plusgs.f90:139-1431) on the GPU against the
+oracle's restatement of them, and the reference's own laminar flat-plate
+run replayed on the GPU.
 
-* Single blocks, laminar and k-omega SST, three implicit iterations at CFL
-  200: interior state within 1e-11 of each variable's magnitude.  The
-  hyperplane sweeps do per cell the reference's arithmetic in an order the
-  data dependencies allow, so the result is the sequential sweep's.
+* Single blocks, laminar and k-omega SST, both integrators, three implicit
+  iterations at CFL 200 (PLU-SGS at free-stream Mach 0.2, so that the
+  preconditioner acts): interior state within 1e-11 of each variable's
+  magnitude.  The hyperplane sweeps do per cell the reference's arithmetic
+  in an order the data dependencies allow, so the result is the
+  sequential sweep's.
 * The reference's laminar flat plate (tests/Lfp: two blocks joined by an
   interface) in one batch: three iterations within 1e-11 of the oracle's
-  two-block run; and the case's own run, 5000 iterations at CFL 2000 from
+  two-block run, with either integrator; and the case's own run, 5000 iterations at CFL 2000 from
   the free stream, whose drag coefficient (Lfp/pp/Surface.py on the
   gradients of the last residual evaluation) is the reference's reported
   1.32933e-3 (tests/Report.txt) to 3e-5, as the oracle's replay is."""
@@ -42,35 +45,36 @@ def _err(q, ref, ext, speed=None):
     return max(np.abs(a[..., l] - b[..., l]).max() / sc[l] for l in range(ext.n_var))
 
 
+@pytest.mark.parametrize("integ", ["implicit", "plusgs"])
 @pytest.mark.parametrize("turb", [False, True], ids=["laminar", "sst"])
-def test_lusgs_single_block_matches_oracle(gpu_lib, turb):
+def test_lusgs_single_block_matches_oracle(gpu_lib, turb, integ):
     kw = dict(nc=(19, 13, 6), ids=(-3, -4, -5, -4, -10, -10),
-              scheme_kw=dict(interpolant="muscl", scheme_name="ausm", time_step_accuracy="implicit"),
-              flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law"))
+              scheme_kw=dict(interpolant="muscl", scheme_name="ausm", time_step_accuracy=integ),
+              flow_kw=dict(mu_ref=2e-2, mu_variation="sutherland_law", MInf=0.2))
     if turb:
         kw["turb"] = True
         kw["scheme_kw"] = dict(kw["scheme_kw"], scheme_name="ausmUP")
-        kw["flow_kw"] = dict(kw["flow_kw"], MInf=0.2)
     ext, flow, scheme, bc, nodes, qp = small_case(**kw)
     wall = cases.wall_nodes_of(nodes, ext, bc) if turb else None
     blk, h = make_pair(ext, flow, scheme, bc, nodes, qp, wall=wall)
     h.step(3, 1, 200.0, with_norm=False)
+    step = O.plusgs_next_solution if integ == "plusgs" else O.lusgs_next_solution
     for it in (1, 2, 3):
-        assert O.lusgs_next_solution([blk], it, 200.0) == 0
+        assert step([blk], it, 200.0) == 0
     e = _err(h.download_state(), blk["qp"], ext)
     assert e <= 1e-11, f"LU-SGS interior state differs by {e:.3e}"
     assert np.abs(post.interior(blk["qp"], ext)[..., 4] - post.interior(qp, ext)[..., 4]).max() > 1.0
     h.close()
 
 
-def _lfp(lib):
+def _lfp(lib, integ="implicit"):
     fx = np.load(os.path.join(HERE, "golden", "flatplate_laminar.npz"))
     parts = MF.flatplate_case([fx["nodes0"], fx["nodes1"]])
     hs, blocks = [], []
     for ext, flow, scheme, bc, nodes, qp in parts:
         # the case's own integrator (Lfp/system/fvscheme.md: "implicit")
         scheme = abi.Scheme.from_buffer_copy(scheme)
-        scheme.time_step_accuracy = abi.TIME["implicit"]
+        scheme.time_step_accuracy = abi.TIME[integ]
         h = Handle(ext, flow, scheme, bc, lib=lib)
         h.setup_geometry(nodes)
         h.upload_state(qp)
@@ -86,12 +90,14 @@ def _lfp(lib):
     return hs, blocks, b
 
 
-def test_lusgs_two_block_flat_plate_matches_oracle(gpu_lib):
-    hs, blocks, b = _lfp(gpu_lib)
+@pytest.mark.parametrize("integ", ["implicit", "plusgs"])
+def test_lusgs_two_block_flat_plate_matches_oracle(gpu_lib, integ):
+    hs, blocks, b = _lfp(gpu_lib, integ)
+    step = O.plusgs_next_solution if integ == "plusgs" else O.lusgs_next_solution
     try:
         abi.check(gpu_lib.fest_batch_step(b, 3, 1, 2000.0), "fest_batch_step")
         for it in (1, 2, 3):
-            assert O.lusgs_next_solution(blocks, it, 2000.0) == 0
+            assert step(blocks, it, 2000.0) == 0
         for n, (h, blk) in enumerate(zip(hs, blocks)):
             e = _err(h.download_state(), blk["qp"], h.ext, speed=MF.U_INF)
             assert e <= 1e-11, f"block {n}: LU-SGS state differs by {e:.3e}"
