@@ -579,6 +579,9 @@ def run_ours(args):
         tot_e2e += time.perf_counter() - t0
         it += 1
     ibytes = int(qint.nbytes)
+    kms = C.c_double()
+    abi.check(lib.fest_last_kernel_ms(he.h, C.byref(kms)), "fest_last_kernel_ms")
+    e2e_step_device_us = kms.value * 1e3  # the last call's device work between its copies
     # the padded state (ghost layers included: 2.4x the interior for this
     # block), one synchronisation per call
     host = torch.empty(abi.shapes(ext)["qp"][::-1], dtype=torch.float64, pin_memory=True)
@@ -665,6 +668,7 @@ def run_ours(args):
                     "path": "fest_step_host_interior (interior cells up, one iteration, interior "
                             "cells down; one synchronisation), pinned host buffer",
                     "over_device_rate": e2e_rate / rate(mixed),
+                    "call_us": tot_e2e / e2e_steps * 1e6, "call_device_work_us": e2e_step_device_us,
                     "padded_state": {"value": replica_rate(N * STAGES, e2e_steps, ws, totp),
                                      "bytes_each_way": nbytes,
                                      "path": "fest_step_host (the padded qp with ghost layers)"},

@@ -145,13 +145,18 @@ int interior_copy(fest_handle* h, const double* src, double* dst, int to_padded)
   CK(cudaGetLastError());
   return FEST_OK;
 }
-// host interior array -> the padded device state (ghost cells kept)
-int up_interior(fest_handle* h, double* qdev, const double* host) {
+// a device-readable copy of a host interior array: the array itself when it
+// is pinned and mapped, else the staging buffer after a copy
+int interior_source(fest_handle* h, const double* host, const double** src) {
   const long long n = ncells(h->p.d) * h->p.d.nv;
-  if (const void* a = mapped_alias(host)) return interior_copy(h, static_cast<const double*>(a), qdev, 1);
+  if (const void* a = mapped_alias(host)) {
+    *src = static_cast<const double*>(a);
+    return FEST_OK;
+  }
   if (!h->d_stage) RET(dalloc(h, &h->d_stage, n));
   CK(cudaMemcpyAsync(h->d_stage, host, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, h->s));
-  return interior_copy(h, h->d_stage, qdev, 1);
+  *src = h->d_stage;
+  return FEST_OK;
 }
 // the padded device state's interior cells -> a host interior array
 int down_interior(fest_handle* h, double* host, const double* qdev) {
@@ -973,12 +978,17 @@ int fest_step_async(fest_handle* h, int n_iters, int first_iter, double CFL) {
 int fest_step_host_interior(fest_handle* h, double* q, int n_iters, int first_iter, double CFL,
                             double* res_abs) {
   if (!h || !q || n_iters < 0 || needs_batch(h)) return FEST_ERR_ARG;
-  // the interior goes into the state the next step reads: the primary
-  // state, whose ghost cells (the persistent fix() layers among them)
-  // are the handle's own
-  RET(sync_fused(h));
-  RET(up_interior(h, h->d.qp, q));
-  if (h->fused) fused_invalidate(h->fused);
+  // the interior goes into the state the next step reads, whose ghost
+  // cells (the persistent fix() layers among them) are the handle's own:
+  // the fused path's current buffer and FP32 mirror in place, or, before
+  // the fused path has a state, the primary state
+  const double* src = nullptr;
+  RET(interior_source(h, q, &src));
+  if (!(h->fused && fused_import_interior(h->fused, src, h->s, &h->launches) == FEST_OK)) {
+    RET(sync_fused(h));
+    RET(interior_copy(h, src, h->d.qp, 1));
+    if (h->fused) fused_invalidate(h->fused);
+  }
   kmark(h, 0);
   RET(step_enqueue(h, n_iters, first_iter, CFL));
   double sums[NVMAX + 1];

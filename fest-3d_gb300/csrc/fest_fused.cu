@@ -1043,6 +1043,36 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
 
 const double* fused_current_state(const FusedState* f) { return f && f->seeded ? f->Q[f->cur] : nullptr; }
 
+// dense interior cells -> the FP64 state and (q32 non-null) its mirror,
+// converted as k_to_mirror converts them
+__global__ void k_import_interior(Dims d, int pitch, const double* __restrict__ src, double* __restrict__ q64,
+                                  float* __restrict__ q32) {
+  const long long nc = ncells(d), n = nc * d.nv;
+  const long long st = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += st) {
+    const long long l = t / nc, c = t % nc;
+    const int i = 1 + (int)(c % (d.imx - 1));
+    const long long r = c / (d.imx - 1);
+    const int j = 1 + (int)(r % (d.jmx - 1)), k = 1 + (int)(r / (d.jmx - 1));
+    const long long pp = pidx(d, i, j, k) + d.P * l;
+    const double v = src[t];
+    q64[pp] = v;
+    if (q32) q32[(pp / d.ni) * pitch + pp % d.ni] = (float)v;
+  }
+}
+
+int fused_import_interior(FusedState* f, const double* src, cudaStream_t s, long long* cnt) {
+  if (!f || !f->seeded) return FEST_ERR_ARG;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  float* q32 = (f->V32 && f->mirror_valid) ? f->Q32[f->cur] : nullptr;
+  k_import_interior<<<sms * 4, 256, 0, s>>>(f->d, f->mpitch, src, f->Q[f->cur], q32);
+  ++*cnt;
+  f->buffers_equal = false;
+  return cudaGetLastError() == cudaSuccess ? FEST_OK : FEST_ERR_CUDA;
+}
+
 int fused_export_state(FusedState* f, double* qp, cudaStream_t s) {
   if (!f) return FEST_ERR_ARG;
   if (f->Q[f->cur] != qp)

@@ -23,6 +23,11 @@ int fused_export_state(FusedState* f, double* qp, cudaStream_t s);
 // the buffer holding the current state (reference layout), nullptr before
 // the first run or after an invalidation; reading it keeps the fused state
 const double* fused_current_state(const FusedState* f);
+// the interior cells of the current state, and of its FP32 mirror where the
+// mixed path keeps one, from a dense (imx-1)(jmx-1)(kmx-1) x n_var array in
+// device-readable memory; the buffers, ghost cells and captured graphs stay
+// as they are.  FEST_ERR_ARG if the state is not seeded (nothing written).
+int fused_import_interior(FusedState* f, const double* src, cudaStream_t s, long long* cnt);
 // event timing of the stage-sweep launches
 void fused_profile(FusedState* f, bool enable);
 int fused_profile_read(FusedState* f, long long* launches, double* total_ms);

@@ -285,7 +285,11 @@ def test_step_host_equals_upload_step_download(gpu_lib, precision, pinned):
 def test_step_host_interior_equals_device_steps(gpu_lib, pinned):
     """fest_step_host_interior on the interior cells (ghost cells kept on
     the device) leaves the interior that fest_step leaves, bit for bit,
-    over calls that start in iterations 1-2 (fix() ghosts) and after."""
+    over calls that start in iterations 1-2 (fix() ghosts) and after: once
+    the fused path holds a state, a call writes the interior into its
+    current buffer and FP32 mirror in place (the values the mirror already
+    holds, when the host array is unchanged), so the sweeps continue as if
+    no call had been made."""
     import torch
     case = cases.bump_case(nc=(64, 24, 4))
     ext = case["ext"]
