@@ -209,21 +209,33 @@ __device__ __forceinline__ void slau_vjp(T gm, const T* qL, const T* qR, T A, T 
   bx[5] = b_rR; bx[6] = b_uR; bx[7] = b_vR; bx[8] = b_wR; bx[9] = b_pR;
 }
 
-// one thread per face of direction dir (faces 1..n along dir, interior
-// tangential positions)
+// faces of direction dir: faces 1..n along dir at the interior tangential
+// positions, face t at c = 1 + t % n, (ta, tb) from t / n
+__device__ __forceinline__ void face_of(const Dims& d, int dir, long long t, int& c, int& ta, int& tb) {
+  const int n = extent_of(d, dir);
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1;
+  c = 1 + (int)(t % n);
+  const long long r = t / n;
+  ta = 1 + (int)(r % na);
+  tb = 1 + (int)(r / na);
+}
+
+// one thread per face of direction dir: mu = lambda(left) - lambda(right)
+// transposed through the flux onto the ten face-state values, stored as
+// bx[m * nf + t]; and, when bar_face is given, onto the face record.
+// Reverse mode for SLAU, forward duals over the ten values otherwise.
 template <typename T, bool SLAU>
-__global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, const double* lam,
-                                                       double* bar, double* bar_face, int dir) {
-  using D5 = Dual<T, 5>;
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, const double* lam, double* bxo,
+                                                      double* bar_face, int dir) {
   using D10 = Dual<T, 10>;
   const Dims& d = p.d;
   const int n = extent_of(d, dir);
   const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long nf = (long long)n * na * nb;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)n * na * nb) return;
-  const int c = 1 + (int)(t % n);
-  const long long r = t / n;
-  const int ta = 1 + (int)(r % na), tb = 1 + (int)(r / na);
+  if (t >= nf) return;
+  int c, ta, tb;
+  face_of(d, dir, t, c, ta, tb);
   const long long P = d.P, N = ncells(d);
   const long long st = pstride(d, dir);
   // mu = lambda(left) - lambda(right); ghost cells carry no residual
@@ -240,6 +252,14 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
     cell_of(dir, c, ta, tb, i, j, k);
 #pragma unroll
     for (int l = 0; l < 5; ++l) mu[l] -= (T)lam[cidx(d, i, j, k) + N * l];
+  }
+  bool any = false;
+#pragma unroll
+  for (int l = 0; l < 5; ++l) any |= mu[l] != T(0);
+  if (!any) {
+#pragma unroll
+    for (int m = 0; m < 10; ++m) bxo[m * nf + t] = 0.0;
+    return;
   }
   // the face states' values (the reconstruction in plain arithmetic)
   cell_of(dir, 0, ta, tb, i, j, k);
@@ -261,8 +281,6 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
   const long long fi = fidx(d, dir, i + (dir == 0 ? c : 0), j + (dir == 1 ? c : 0), k + (dir == 2 ? c : 0));
   const double* fc = b.faces[dir] + 4 * fi;
   const T mask_v = (T)wall_mask(p, dir, c);
-  // flux Jacobian, transposed onto mu: reverse mode for SLAU, forward
-  // duals over the ten face-state values for the other schemes
   T bx[10];
   if constexpr (SLAU) {
     slau_vjp<T>((T)p.gm, qL, qR, (T)fc[0], (T)fc[1], (T)fc[2], (T)fc[3], mask_v, mu, bx);
@@ -284,6 +302,8 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
       bx[m] = s;
     }
   }
+#pragma unroll
+  for (int m = 0; m < 10; ++m) bxo[m * nf + t] = (double)bx[m];
   // face metrics {A, nx, ny, nz} (the flux at fixed face states)
   if (bar_face) {
     using D4 = Dual<T, 4>;
@@ -303,28 +323,47 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_faces(Params p, DevBlock b, con
       if (s != T(0)) atomicAdd(bar_face + 4 * fi + m, (double)s);
     }
   }
-  // face states -> stencil cells, one variable at a time: qL (cell c-1)
-  // reaches cells c-3..c+1, qR (cell c) cells c-2..c+2; the six targets
-  // are summed in registers before one atomic add each
+}
+
+// one thread per (face, variable): the variable's two face states (cell
+// c-1's high side, cell c's low side) differentiated with respect to their
+// 5-cell stencils by forward duals, times the flux transpose of k_vjp_flux;
+// qL reaches cells c-3..c+1, qR cells c-2..c+2, and the six targets are
+// summed in registers before one atomic add each
+template <typename T>
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_recon(Params p, DevBlock b, const double* bxi, double* bar,
+                                                       int dir) {
+  using D5 = Dual<T, 5>;
+  const Dims& d = p.d;
+  const int n = extent_of(d, dir);
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long nf = (long long)n * na * nb;
+  const long long t5 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t5 >= 5 * nf) return;
+  const int l = (int)(t5 / nf);
+  const long long t = t5 - l * nf;
+  const T bl = (T)bxi[l * nf + t], br = (T)bxi[(5 + l) * nf + t];
+  if (bl == T(0) && br == T(0)) return;
+  int c, ta, tb, i, j, k;
+  face_of(d, dir, t, c, ta, tb);
+  cell_of(dir, 0, ta, tb, i, j, k);
+  const long long P = d.P, st = pstride(d, dir), c0 = pidx(d, i, j, k);
   VolConst<T, 5> vol{b.cells + 4 * c0, st, n};
   ConstLine<T, 5> pres{b.qp + c0 + P * 4, st};
-#pragma unroll 1
-  for (int l = 0; l < 5; ++l) {
-    T acc[6];
-    D5 Rm, Lp;
-    DualLine<T, 5> qa{b.qp + c0 + P * l, st, c - 1};
-    recon_cell<D5>(p, dir, c - 1, l + 1, qa, pres, vol, Rm, Lp);
+  T acc[6];
+  D5 Rm, Lp;
+  DualLine<T, 5> qa{b.qp + c0 + P * l, st, c - 1};
+  recon_cell<D5>(p, dir, c - 1, l + 1, qa, pres, vol, Rm, Lp);
 #pragma unroll
-    for (int s = 0; s < 5; ++s) acc[s] = bx[l] * Lp.d[s];
-    acc[5] = T(0);
-    DualLine<T, 5> qb{b.qp + c0 + P * l, st, c};
-    recon_cell<D5>(p, dir, c, l + 1, qb, pres, vol, Rm, Lp);
+  for (int s = 0; s < 5; ++s) acc[s] = bl * Lp.d[s];
+  acc[5] = T(0);
+  DualLine<T, 5> qb{b.qp + c0 + P * l, st, c};
+  recon_cell<D5>(p, dir, c, l + 1, qb, pres, vol, Rm, Lp);
 #pragma unroll
-    for (int s = 0; s < 5; ++s) acc[s + 1] += bx[5 + l] * Rm.d[s];
+  for (int s = 0; s < 5; ++s) acc[s + 1] += br * Rm.d[s];
 #pragma unroll
-    for (int s = 0; s < 6; ++s)
-      if (acc[s] != T(0)) atomicAdd(bar + c0 + (c - 3 + s) * st + P * l, (double)acc[s]);
-  }
+  for (int s = 0; s < 6; ++s)
+    if (acc[s] != T(0)) atomicAdd(bar + c0 + (c - 3 + s) * st + P * l, (double)acc[s]);
 }
 
 // ---- laminar viscous terms (gradients.f90, viscosity.f90, viscous.f90) -----
@@ -768,7 +807,7 @@ static void apply_ST(const Params& p, const DevBlock& b, const double* v, double
                      const Launcher& L) {
   const long long N = ncells(p.d);
   k_adj_precond<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p, b, v, w.mu);
-  launch_residual_vjp(p, b, 3, w.mu, w.bar, L, nullptr, w.grad);
+  launch_residual_vjp(p, b, 3, w.mu, w.bar, L, nullptr, w.grad, w.face);
   k_adj_combine<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p.d, out, 1.0, v, -1.0, w.bar, 0.0, nullptr, 0.0,
                                                  nullptr, nullptr);
   *L.count += 2;
@@ -813,8 +852,17 @@ void launch_adjoint_psi(const Params& p, const DevBlock& b, AdjointWork& w, doub
   *L.count += 2;
 }
 
+long long vjp_face_work_doubles(const Dims& d) {
+  long long m = 0;
+  for (int dir = 0; dir < 3; ++dir)
+    m = std::max<long long>(m, (long long)extent_of(d, dir) * ((dir == 0 ? d.jmx : d.imx) - 1) *
+                                   ((dir == 2 ? d.jmx : d.kmx) - 1));
+  return 10 * m;
+}
+
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
-                         double* bar, const Launcher& L, double* const* bar_faces, double* bar_grad) {
+                         double* bar, const Launcher& L, double* const* bar_faces, double* bar_grad,
+                         double* face_work) {
   const Dims& d = p.d;
   const bool visc = p.mu_ref != 0.0;
   cudaMemsetAsync(bar, 0, sizeof(double) * (size_t)d.P * d.nv, L.s);
@@ -824,10 +872,11 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
     const long long nf = (long long)n * ((dir == 0 ? d.jmx : d.imx) - 1) * ((dir == 2 ? d.jmx : d.kmx) - 1);
     double* bf = bar_faces ? bar_faces[dir] : nullptr;
     if (p.flux == FEST_FLUX_SLAU)
-      k_vjp_faces<double, true><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bf, dir);
+      k_vjp_flux<double, true><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
     else
-      k_vjp_faces<double, false><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bf, dir);
-    ++*L.count;
+      k_vjp_flux<double, false><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
+    k_vjp_recon<double><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+    *L.count += 2;
     if (visc) {
       k_vjp_viscous<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bar_grad, dir);
       ++*L.count;

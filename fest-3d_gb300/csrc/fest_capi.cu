@@ -34,6 +34,7 @@ struct fest_handle {
   double* d_vjp_bar = nullptr;  // adjoint work arrays, allocated on first use
   double* d_vjp_lam = nullptr;
   double* d_vjp_grad = nullptr;  // laminar adjoint: 12 per interior cell
+  double* d_vjp_face = nullptr;  // adjoint: one direction's face flux transposes
   double* d_lu = nullptr;        // LU-SGS work arrays, allocated on first use
   double* d_stage = nullptr;     // interior-cell staging for pageable host arrays
   int* h_err = nullptr;          // pinned host copy of the device error word
@@ -801,12 +802,14 @@ int fest_residual_vjp(fest_handle* h, const double* qp, int current_iter, const 
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
   if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
+  if (!h->d_vjp_face) RET(dalloc(h, &h->d_vjp_face, vjp_face_work_doubles(h->p.d)));
   if (qp) RET(up(h, h->d.qp, qp, z.qp));
   RET(up(h, h->d_vjp_lam, lambda, z.res));
   kmark(h, 0);
   launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
   RET(viscous_prep(h));
-  launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), nullptr, h->d_vjp_grad);
+  launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), nullptr, h->d_vjp_grad,
+                      h->d_vjp_face);
   kmark(h, 1);
   RET(down(h, dq, h->d_vjp_bar, z.qp));
   return finish(h);
@@ -822,6 +825,7 @@ int fest_residual_vjp_nodes(fest_handle* h, const double* qp, int current_iter, 
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
   if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
+  if (!h->d_vjp_face) RET(dalloc(h, &h->d_vjp_face, vjp_face_work_doubles(h->p.d)));
   const size_t n0 = h->allocs.size();
   double *bf[3] = {nullptr, nullptr, nullptr}, *bn = nullptr;
   int rc = FEST_OK;
@@ -835,7 +839,8 @@ int fest_residual_vjp_nodes(fest_handle* h, const double* qp, int current_iter, 
   else if (!rc) rc = cuda_status(cudaMemsetAsync(h->d_vjp_lam, 0, sizeof(double) * z.res, h->s));
   if (!rc) {
     launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
-    launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), bf);
+    launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), bf, nullptr,
+                        h->d_vjp_face);
     launch_geometry_vjp(h->p, h->d, bf, bn, h->L());
     rc = down(h, dnodes, bn, z.nodes);
   }
@@ -861,9 +866,11 @@ int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_i
   // the handle keeps this one: allocated before the solve's own work arrays,
   // which release() frees
   if (h->p.mu_ref != 0.0 && !h->d_vjp_grad) RET(dalloc(h, &h->d_vjp_grad, 12 * ncells(h->p.d)));
+  if (!h->d_vjp_face) RET(dalloc(h, &h->d_vjp_face, vjp_face_work_doubles(h->p.d)));
   AdjointWork w{};
   w.bar = h->d_vjp_bar;
   w.mu = h->d_vjp_lam;
+  w.face = h->d_vjp_face;
   const size_t n0 = h->allocs.size();
   int rc = FEST_OK;
   for (double** x : {&w.phi, &w.dJ, &w.a, &w.b, &w.c})

@@ -77,9 +77,12 @@ bool vjp_supported(const Params& p);
 // bar_faces (null, or three face-layout arrays, zeroed by the caller) also
 // receive (dR/dfaces)^T lam (inviscid blocks); bar_grad: 12 doubles per
 // interior cell of work space for laminar blocks
+// face_work: vjp_face_work_doubles(d) doubles of work space (the flux
+// transposes of one direction's faces)
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
-                         double* bar, const Launcher& L, double* const* bar_faces = nullptr,
-                         double* bar_grad = nullptr);
+                         double* bar, const Launcher& L, double* const* bar_faces, double* bar_grad,
+                         double* face_work);
+long long vjp_face_work_doubles(const Dims& d);
 // nodes-layout bar_nodes = (dfaces/dnodes)^T bar_faces, through the face
 // vectors and the ghost-node extrapolation (interior nodes carry the result)
 void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_faces, double* bar_nodes,
@@ -89,6 +92,7 @@ void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_
 struct AdjointWork {
   double *phi, *dJ, *a, *b, *c, *bar, *mu, *sq;
   double* grad;  // 12 per interior cell (laminar blocks)
+  double* face;  // vjp_face_work_doubles
 };
 // one step phi <- G^T phi + dJ/dq (G the integrator's map linearised at the
 // fixed point: forward Euler or TVD-RK3); sq += |change of phi|^2
