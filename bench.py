@@ -698,7 +698,13 @@ def run_adjoint_study(args):
     else:
         nodes = tuple(int(x) for x in spec.split(",") if x)
     t0 = time.perf_counter()
-    out = A.wall_force_study(lib, wall_nodes=nodes, log=lambda *a: print(*a, file=sys.stderr, flush=True))
+
+    def save(o):
+        with open(args.adjoint_study, "w") as f:
+            json.dump(o, f, indent=1)
+
+    out = A.wall_force_study(lib, wall_nodes=nodes, log=lambda *a: print(*a, file=sys.stderr, flush=True),
+                             progress=save)
     out["seconds"] = time.perf_counter() - t0
     with open(args.adjoint_study, "w") as f:
         json.dump(out, f, indent=1)

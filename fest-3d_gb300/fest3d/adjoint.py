@@ -282,7 +282,8 @@ def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angl
     checked by a central difference of two re-converged primal solutions
     (step fd_step, or fd_steps[param]; each re-solve from the converged
     state to the same drop), the re-solves spread over `threads` handles.
-    Returns a dict of everything measured."""
+    Returns a dict of everything measured; progress(dict), if given, sees
+    it after every stage and every checked parameter."""
     import time
     from concurrent.futures import ThreadPoolExecutor
     say = log or (lambda *a: None)
@@ -299,6 +300,8 @@ def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angl
     out["primal"] = {"drop": drop, "ref_norm": ref, "anderson_maps": maps, "iterations": iters + 1,
                      "seconds": time.perf_counter() - t0}
     say("primal", out["primal"])
+    if progress:
+        progress(out)
     t1 = time.perf_counter()
     Jf = h.get("Jfaces")
     J, dJ = wall_force(q, ext, Jf)
@@ -315,6 +318,8 @@ def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angl
     out["adjoint"] = {"drop": adrop, "gmres_products": products, "residual_vjp_calls": vjps,
                       "seconds": time.perf_counter() - t1, "J": J, "history": ahist}
     say("adjoint", out["adjoint"])
+    if progress:
+        progress(out)
     steps = dict(fd_steps or {})
 
     def fd(param):
@@ -335,6 +340,7 @@ def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angl
 
     t2 = time.perf_counter()
     rows = []
+    out["rows"] = rows
     with ThreadPoolExecutor(max_workers=threads) as ex:
         for param, g_fd, step, info in ex.map(fd, list(params) + list(wall_nodes)):
             g = grads[param]
@@ -345,6 +351,8 @@ def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angl
                          "fd_drops": [i["drop"] for i in info],
                          "fd_iterations": [i["iterations"] for i in info]})
             say(rows[-1]["param"], g, g_fd, rel)
+            if progress:
+                progress(out)
     out["fd_seconds"] = time.perf_counter() - t2
     out["rows"] = rows
     out["max_rel_diff"] = max(r["rel_diff"] for r in rows) if rows else None
