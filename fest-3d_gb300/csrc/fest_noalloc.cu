@@ -24,8 +24,9 @@
 // in time on the same device (different streams or host threads without
 // ordering between them) race on it and may return wrong norms: callers
 // serialise them.  The first call on each device does the setup (symbol
-// lookup, counter reset, and the runtime's lazy module load) and should
-// therefore come before any stream capture.
+// lookup, counter reset, and the runtime's lazy module load).  No call can
+// be part of a stream capture (each one synchronises its stream): a call
+// on a capturing stream returns FEST_ERR_ARG.
 #include <cmath>
 #include <mutex>
 
@@ -144,6 +145,14 @@ extern "C" int fest_find_resnorm_noalloc(const fest_extent* ext, const fest_flow
   if (rc) return rc;
   if (dev < 0 || dev >= kNaMaxDevices) return FEST_ERR_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
+  // every call synchronises its stream, which a capture cannot contain: a
+  // call on a capturing stream is refused before it touches the capture
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return FEST_ERR_ARG;
+  }
+  if (cap != cudaStreamCaptureStatusNone) return FEST_ERR_ARG;
   DeviceScratch& ds = g_dev[dev];
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);

@@ -374,9 +374,10 @@ int fest_measure_peak(int kind, double *tflops);
  * (FEST_ERR_SCRATCH otherwise); n_var must be 5 (Euler, laminar) or 7
  * (k-omega SST, scaled by tk_inf and tw_inf), FEST_ERR_ARG otherwise.  Calls that overlap in time on one device
  * race on that area and must be serialised by the caller.  The first call
- * on each device (with that device current) does the setup and should come
- * before any stream capture.  Runs on cuda_stream (NULL: the legacy default
- * stream) and returns after synchronising it. */
+ * on each device (with that device current) does the setup.  Runs on
+ * cuda_stream (NULL: the legacy default stream) and returns after
+ * synchronising it, so no call can be stream-captured: a call on a
+ * capturing stream returns FEST_ERR_ARG and leaves the capture intact. */
 int fest_find_resnorm_noalloc(const fest_extent *ext, const fest_flow *flow,
                               const double *residue, const double *F,
                               const double *G, const double *H,

@@ -57,3 +57,31 @@ def test_noalloc_resnorm_matches_handle_resnorm(gpu_lib, turb):
         out = np.zeros(ext.n_var + 1)
         abi.check(_call_noalloc(L, ext, flow, ptrs, out, stream), "fest_find_resnorm_noalloc")
         assert np.allclose(out, ref, rtol=1e-12, atol=1e-300), (call, out, ref)
+
+
+def test_noalloc_refuses_a_capturing_stream(gpu_lib):
+    """a call on a stream under capture returns FEST_ERR_ARG and leaves the
+    capture intact: the captured graph (one torch add) replays"""
+    import torch
+    ext, flow, scheme, bc, nodes, qp = small_case(nc=(9, 7, 6), ids=(-3, -4, -5, -4, -10, -10))
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
+    h.get_next_solution(blk["qp"].copy(order="F"), 1, 0.5)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    arrays = [torch.from_numpy(np.ascontiguousarray(h.get(n).ravel(order="F"))).to(dev)
+              for n in ("residue", "F", "G", "H")]
+    ptrs = [a.data_ptr() for a in arrays]
+    out = np.zeros(ext.n_var + 1)
+    # the first call on the device does its setup outside any capture
+    abi.check(_call_noalloc(gpu_lib, ext, flow, ptrs, out, torch.cuda.current_stream().cuda_stream), "setup")
+    x = torch.zeros(16, device=dev)
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            x.add_(1.0)
+            rc = _call_noalloc(gpu_lib, ext, flow, ptrs, out, s.cuda_stream)
+    assert rc == abi.FEST_ERR_ARG
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x.sum()) == 16.0  # captured, not run; the replay adds once
