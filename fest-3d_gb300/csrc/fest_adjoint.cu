@@ -80,8 +80,9 @@ __device__ __forceinline__ void cell_of(int dir, int c, int ta, int tb, int& i, 
 // directions of Dual<T, 10> cost about twenty.  The derivative conventions
 // at the kinks are the dual numbers' (fest_dual.cuh): fabs takes the sign
 // of its argument (+1 at 0), fmax2/fmin2 the branch they return, floor
-// and copysign none, sqrt 1/(2 sqrt(x)) (0 at 0).  nv = 5.
-template <typename T>
+// and copysign none, sqrt 1/(2 sqrt(x)) (0 at 0).  NV = 5, or 7 with k and
+// omega carried by the mass flux; bx[0..NV-1] left, bx[NV..2NV-1] right.
+template <typename T, int NV>
 __device__ __forceinline__ void slau_vjp(T gm, const T* qL, const T* qR, T A, T nx, T ny, T nz, T mask,
                                          const T* mu, T* bx) {
   const T rL = qL[0], uL = qL[1], vL = qL[2], wL = qL[3], pL = qL[4];
@@ -134,8 +135,15 @@ __device__ __forceinline__ void slau_vjp(T gm, const T* qL, const T* qR, T A, T 
   T b_rL = T(0), b_uL = m1 * Fp0, b_vL = m2 * Fp0, b_wL = m3 * Fp0, b_pL = T(0);
   T b_rR = T(0), b_uR = m1 * Fm0, b_vR = m2 * Fm0, b_wR = m3 * Fm0, b_pR = T(0);
   const T b_HL = m4 * Fp0, b_HR = m4 * Fm0;
-  const T b_Fp0 = m0 + m1 * uL + m2 * vL + m3 * wL + m4 * HL;
-  const T b_Fm0 = m0 + m1 * uR + m2 * vR + m3 * wR + m4 * HR;
+  T b_Fp0 = m0 + m1 * uL + m2 * vL + m3 * wL + m4 * HL;
+  T b_Fm0 = m0 + m1 * uR + m2 * vR + m3 * wR + m4 * HR;
+#pragma unroll
+  for (int l = 5; l < NV; ++l) {  // Fo[l] = (Fp0 qL[l] + Fm0 qR[l]) A
+    b_Fp0 += mu[l] * A * qL[l];
+    b_Fm0 += mu[l] * A * qR[l];
+    bx[l] = mu[l] * A * Fp0;
+    bx[NV + l] = mu[l] * A * Fm0;
+  }
   const T b_pbar = m1 * nx + m2 * ny + m3 * nz;
   const T sm = mass < T(0) ? T(-1) : T(1);
   const T b_mass0 = (b_Fp0 * T(0.5) * (T(1) + sm) + b_Fm0 * T(0.5) * (T(1) - sm)) * mask;
@@ -206,7 +214,7 @@ __device__ __forceinline__ void slau_vjp(T gm, const T* qL, const T* qR, T A, T 
   b_uL += b_VnL * nx; b_vL += b_VnL * ny; b_wL += b_VnL * nz;
   b_uR += b_VnR * nx; b_vR += b_VnR * ny; b_wR += b_VnR * nz;
   bx[0] = b_rL; bx[1] = b_uL; bx[2] = b_vL; bx[3] = b_wL; bx[4] = b_pL;
-  bx[5] = b_rR; bx[6] = b_uR; bx[7] = b_vR; bx[8] = b_wR; bx[9] = b_pR;
+  bx[NV + 0] = b_rR; bx[NV + 1] = b_uR; bx[NV + 2] = b_vR; bx[NV + 3] = b_wR; bx[NV + 4] = b_pR;
 }
 
 // faces of direction dir: faces 1..n along dir at the interior tangential
@@ -221,13 +229,13 @@ __device__ __forceinline__ void face_of(const Dims& d, int dir, long long t, int
 }
 
 // one thread per face of direction dir: mu = lambda(left) - lambda(right)
-// transposed through the flux onto the ten face-state values, stored as
+// transposed through the flux onto the 2 NV face-state values, stored as
 // bx[m * nf + t]; and, when bar_face is given, onto the face record.
-// Reverse mode for SLAU, forward duals over the ten values otherwise.
-template <typename T, bool SLAU>
+// Reverse mode for SLAU, forward duals over the 2 NV values otherwise.
+template <typename T, bool SLAU, int NV>
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, const double* lam, double* bxo,
                                                       double* bar_face, int dir) {
-  using D10 = Dual<T, 10>;
+  using D10 = Dual<T, 2 * NV>;
   const Dims& d = p.d;
   const int n = extent_of(d, dir);
   const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
@@ -239,37 +247,37 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, cons
   const long long P = d.P, N = ncells(d);
   const long long st = pstride(d, dir);
   // mu = lambda(left) - lambda(right); ghost cells carry no residual
-  T mu[5];
+  T mu[NV];
   int i, j, k;
 #pragma unroll
-  for (int l = 0; l < 5; ++l) mu[l] = T(0);
+  for (int l = 0; l < NV; ++l) mu[l] = T(0);
   if (c - 1 >= 1) {
     cell_of(dir, c - 1, ta, tb, i, j, k);
 #pragma unroll
-    for (int l = 0; l < 5; ++l) mu[l] += (T)lam[cidx(d, i, j, k) + N * l];
+    for (int l = 0; l < NV; ++l) mu[l] += (T)lam[cidx(d, i, j, k) + N * l];
   }
   if (c <= n - 1) {
     cell_of(dir, c, ta, tb, i, j, k);
 #pragma unroll
-    for (int l = 0; l < 5; ++l) mu[l] -= (T)lam[cidx(d, i, j, k) + N * l];
+    for (int l = 0; l < NV; ++l) mu[l] -= (T)lam[cidx(d, i, j, k) + N * l];
   }
   bool any = false;
 #pragma unroll
-  for (int l = 0; l < 5; ++l) any |= mu[l] != T(0);
+  for (int l = 0; l < NV; ++l) any |= mu[l] != T(0);
   if (!any) {
 #pragma unroll
-    for (int m = 0; m < 10; ++m) bxo[m * nf + t] = 0.0;
+    for (int m = 0; m < 2 * NV; ++m) bxo[m * nf + t] = 0.0;
     return;
   }
   // the face states' values (the reconstruction in plain arithmetic)
   cell_of(dir, 0, ta, tb, i, j, k);
   const long long c0 = pidx(d, i, j, k);
-  T qL[5], qR[5];
+  T qL[NV], qR[NV];
   {
     VolVal<T> vol{b.cells + 4 * c0, st, n};
     ValLine<T> pres{b.qp + c0 + P * 4, st};
 #pragma unroll
-    for (int l = 0; l < 5; ++l) {
+    for (int l = 0; l < NV; ++l) {
       T Rm, Lp;
       ValLine<T> q{b.qp + c0 + P * l, st};
       recon_cell<T>(p, dir, c - 1, l + 1, q, pres, vol, Rm, Lp);
@@ -281,35 +289,35 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, cons
   const long long fi = fidx(d, dir, i + (dir == 0 ? c : 0), j + (dir == 1 ? c : 0), k + (dir == 2 ? c : 0));
   const double* fc = b.faces[dir] + 4 * fi;
   const T mask_v = (T)wall_mask(p, dir, c);
-  T bx[10];
+  T bx[2 * NV];
   if constexpr (SLAU) {
-    slau_vjp<T>((T)p.gm, qL, qR, (T)fc[0], (T)fc[1], (T)fc[2], (T)fc[3], mask_v, mu, bx);
+    slau_vjp<T, NV>((T)p.gm, qL, qR, (T)fc[0], (T)fc[1], (T)fc[2], (T)fc[3], mask_v, mu, bx);
   } else {
-    D10 xl[5], xr[5], Fo[NVMAX];
+    D10 xl[NVMAX], xr[NVMAX], Fo[NVMAX];
 #pragma unroll
-    for (int l = 0; l < 5; ++l) {
+    for (int l = 0; l < NV; ++l) {
       xl[l] = D10::var(qL[l], l);
-      xr[l] = D10::var(qR[l], 5 + l);
+      xr[l] = D10::var(qR[l], NV + l);
     }
     const D10 A = D10::cst((T)fc[0]), nx = D10::cst((T)fc[1]), ny = D10::cst((T)fc[2]),
               nz = D10::cst((T)fc[3]);
     face_flux<D10>(p, xl, xr, A, nx, ny, nz, D10::cst(mask_v), Fo);
 #pragma unroll
-    for (int m = 0; m < 10; ++m) {
+    for (int m = 0; m < 2 * NV; ++m) {
       T s = T(0);
 #pragma unroll
-      for (int l = 0; l < 5; ++l) s += mu[l] * Fo[l].d[m];
+      for (int l = 0; l < NV; ++l) s += mu[l] * Fo[l].d[m];
       bx[m] = s;
     }
   }
 #pragma unroll
-  for (int m = 0; m < 10; ++m) bxo[m * nf + t] = (double)bx[m];
+  for (int m = 0; m < 2 * NV; ++m) bxo[m * nf + t] = (double)bx[m];
   // face metrics {A, nx, ny, nz} (the flux at fixed face states)
   if (bar_face) {
     using D4 = Dual<T, 4>;
-    D4 xl[5], xr[5], Fo[NVMAX];
+    D4 xl[NVMAX], xr[NVMAX], Fo[NVMAX];
 #pragma unroll
-    for (int l = 0; l < 5; ++l) {
+    for (int l = 0; l < NV; ++l) {
       xl[l] = D4::cst(qL[l]);
       xr[l] = D4::cst(qR[l]);
     }
@@ -319,7 +327,7 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, cons
     for (int m = 0; m < 4; ++m) {
       T s = T(0);
 #pragma unroll
-      for (int l = 0; l < 5; ++l) s += mu[l] * Fo[l].d[m];
+      for (int l = 0; l < NV; ++l) s += mu[l] * Fo[l].d[m];
       if (s != T(0)) atomicAdd(bar_face + 4 * fi + m, (double)s);
     }
   }
@@ -330,7 +338,7 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, cons
 // 5-cell stencils by forward duals, times the flux transpose of k_vjp_flux;
 // qL reaches cells c-3..c+1, qR cells c-2..c+2, and the six targets are
 // summed in registers before one atomic add each
-template <typename T>
+template <typename T, int NV>
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_recon(Params p, DevBlock b, const double* bxi, double* bar,
                                                        int dir) {
   using D5 = Dual<T, 5>;
@@ -339,10 +347,10 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_recon(Params p, DevBlock b, con
   const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
   const long long nf = (long long)n * na * nb;
   const long long t5 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t5 >= 5 * nf) return;
+  if (t5 >= NV * nf) return;
   const int l = (int)(t5 / nf);
   const long long t = t5 - l * nf;
-  const T bl = (T)bxi[l * nf + t], br = (T)bxi[(5 + l) * nf + t];
+  const T bl = (T)bxi[l * nf + t], br = (T)bxi[(NV + l) * nf + t];
   if (bl == T(0) && br == T(0)) return;
   int c, ta, tb, i, j, k;
   face_of(d, dir, t, c, ta, tb);
@@ -606,6 +614,416 @@ __device__ __forceinline__ long long icell_p(const Dims& d, int f, int m, int ta
   }
 }
 
+// ---- k-omega SST terms (viscous.f90:144-447, viscosity.f90:215-546,
+// source.f90:158-270, gradients.f90:276-676) ---------------------------------
+// Gradients here are 18 per cell, G[3 l + c] for variable l of u, v, w, T,
+// k, omega and component c, over the gradient range (0:imx, 0:jmx, 0:kmx).
+
+constexpr double kSstA1 = 0.31, kSstBstar = 0.09, kSstBeta1 = 0.075, kSstBeta2 = 0.0828,
+                 kSstSigK1 = 0.85, kSstSigK2 = 1.0, kSstSigW1 = 0.5, kSstSigW2 = 0.856, kSstKappa = 0.41;
+
+// The face's viscous flux with the SST terms as a function of its 35
+// inputs: x[0..17] the mean of the two cells' gradients, x[18..23] and
+// x[24..29] the left and right cells' u, v, w, T, k, omega, x[30], x[31]
+// their densities, x[32..34] the face's mean laminar viscosity, eddy
+// viscosity and F1.  Fv: the six terms the reference subtracts from
+// F(2:7) (momentum, energy, k, omega).
+template <typename D>
+__device__ __forceinline__ void visc_flux_sst_d(const Params& p, const D* x, const double* C0, const double* C1,
+                                                const double* fc, D* Fv) {
+  D G[3][6];
+#pragma unroll
+  for (int l = 0; l < 6; ++l)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) G[c][l] = x[3 * l + c];
+  const double dx0 = C1[1] - C0[1], dy0 = C1[2] - C0[2], dz0 = C1[3] - C0[3];
+  const D delx(dx0), dely(dy0), delz(dz0), dLR(::sqrt(dx0 * dx0 + dy0 * dy0 + dz0 * dz0));
+#pragma unroll
+  for (int l = 0; l < 6; ++l) {
+    const D del = x[24 + l] - x[18 + l];
+    const D nc = (del - (G[0][l] * delx + G[1][l] * dely + G[2][l] * delz)) / dLR;
+    G[0][l] = G[0][l] + (nc * delx / dLR);
+    G[1][l] = G[1][l] + (nc * dely / dLR);
+    G[2][l] = G[2][l] + (nc * delz / dLR);
+  }
+  const D mu_f = x[32], mut_f = x[33], F1 = x[34];
+  const D tm = mu_f + mut_f;
+  const D two(2.), three(3.), half(0.5);
+  const D dudx = G[0][0], dudy = G[1][0], dudz = G[2][0];
+  const D dvdx = G[0][1], dvdy = G[1][1], dvdz = G[2][1];
+  const D dwdx = G[0][2], dwdy = G[1][2], dwdz = G[2][2];
+  const D Txx = two * tm * (dudx - ((dudx + dvdy + dwdz) / three));
+  const D Tyy = two * tm * (dvdy - ((dudx + dvdy + dwdz) / three));
+  const D Tzz = two * tm * (dwdz - ((dudx + dvdy + dwdz) / three));
+  const D Txy = tm * (dvdx + dudy), Txz = tm * (dwdx + dudz), Tyz = tm * (dwdy + dvdz);
+  const D Kh = (mu_f / D(p.Pr) + mut_f / D(p.tPr)) * D(p.gm) * D(p.R) / D(p.gm - 1);
+  const D Qx = Kh * G[0][3], Qy = Kh * G[1][3], Qz = Kh * G[2][3];
+  const D A(fc[0]), nx(fc[1]), ny(fc[2]), nz(fc[3]);
+  const D uf = half * (x[18] + x[24]), vf = half * (x[19] + x[25]), wf = half * (x[20] + x[26]);
+  // viscous.f90:328-447
+  const D skf = D(kSstSigK1) * F1 + D(kSstSigK2) * (D(1.) - F1);
+  const D swf = D(kSstSigW1) * F1 + D(kSstSigW2) * (D(1.) - F1);
+  const D rhof = half * (x[30] + x[31]), tkf = half * (x[22] + x[28]);
+  const D Tk = D(-2.0) * rhof * tkf / D(3.0);
+  const D dk = G[0][4] * nx + G[1][4] * ny + G[2][4] * nz;
+  const D dw = G[0][5] * nx + G[1][5] * ny + G[2][5] * nz;
+  const D kdiff = A * ((mu_f + skf * mut_f) * dk);
+  Fv[0] = (Txx * nx + Txy * ny + Txz * nz) * A + Tk * nx * A;
+  Fv[1] = (Txy * nx + Tyy * ny + Tyz * nz) * A + Tk * ny * A;
+  Fv[2] = (Txz * nx + Tyz * ny + Tzz * nz) * A + Tk * nz * A;
+  Fv[3] = A * (((Txx * uf + Txy * vf + Txz * wf + Qx) * nx) + ((Txy * uf + Tyy * vf + Tyz * wf + Qy) * ny) +
+               ((Txz * uf + Tyz * vf + Tzz * wf + Qz) * nz)) + kdiff;
+  Fv[4] = kdiff;
+  Fv[5] = A * ((mu_f + swf * mut_f) * dw);
+}
+
+// adjoints of a cell's u, v, w, T, k, omega and rho into its primitive state
+__device__ __forceinline__ void give_sst(const Params& p, const DevBlock& b, double* bar, long long c,
+                                         const double* g, double grho) {
+  give_uvwT(p, b, bar, c, g);
+  const long long P = p.d.P;
+  if (g[4] != 0.0) atomicAdd(bar + c + 5 * P, g[4]);
+  if (g[5] != 0.0) atomicAdd(bar + c + 6 * P, g[5]);
+  if (grho != 0.0) atomicAdd(bar + c, grho);
+}
+
+// one thread per face of direction dir (the SST block's laminar and SST
+// viscous terms together): the transposed flux onto the mean gradient
+// (half to each cell's gradient adjoint barG, ghost cells included), the
+// cells' u, v, w, T, k, omega, rho, the laminar viscosity (through
+// Sutherland's law onto T) and the eddy viscosity and F1 (half to each
+// cell's barMut, barF1)
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_viscous_sst(Params p, DevBlock b, const double* lam, double* bar,
+                                                             double* barG, double* barMut, double* barF1, int dir) {
+  // the 35 input directions in five passes of seven (duals of 35 would
+  // not fit in registers)
+  using D = Dual<double, 7>;
+  const Dims& d = p.d;
+  const int n = extent_of(d, dir);
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * na * nb) return;
+  int c, ta, tb;
+  face_of(d, dir, t, c, ta, tb);
+  const long long P = d.P, N = ncells(d), NG = ngrad(d);
+  double mu[6] = {0, 0, 0, 0, 0, 0};
+  int i, j, k;
+  if (c - 1 >= 1) {
+    cell_of(dir, c - 1, ta, tb, i, j, k);
+    for (int l = 0; l < 6; ++l) mu[l] += lam[cidx(d, i, j, k) + N * (l + 1)];
+  }
+  if (c <= n - 1) {
+    cell_of(dir, c, ta, tb, i, j, k);
+    for (int l = 0; l < 6; ++l) mu[l] -= lam[cidx(d, i, j, k) + N * (l + 1)];
+  }
+  bool any = false;
+  for (int l = 0; l < 6; ++l) any |= mu[l] != 0.0;
+  if (!any) return;
+  int il, jl, kl, ir, jr, kr;
+  cell_of(dir, c - 1, ta, tb, il, jl, kl);
+  cell_of(dir, c, ta, tb, ir, jr, kr);
+  const long long cL = pidx(d, il, jl, kl), cR = pidx(d, ir, jr, kr);
+  const long long gL = gidx(d, il, jl, kl), gR = gidx(d, ir, jr, kr);
+  const double* q = b.qp;
+  const double TL = q[cL + 4 * P] / (q[cL] * p.R), TR = q[cR + 4 * P] / (q[cR] * p.R);
+  double xv[35];
+  for (int l = 0; l < 6; ++l)
+    for (int cc = 0; cc < 3; ++cc) xv[3 * l + cc] = 0.5 * (b.grad[cc][gL + NG * l] + b.grad[cc][gR + NG * l]);
+  {
+    const double vL[6] = {q[cL + P], q[cL + 2 * P], q[cL + 3 * P], TL, q[cL + 5 * P], q[cL + 6 * P]};
+    const double vR[6] = {q[cR + P], q[cR + 2 * P], q[cR + 3 * P], TR, q[cR + 5 * P], q[cR + 6 * P]};
+    for (int l = 0; l < 6; ++l) {
+      xv[18 + l] = vL[l];
+      xv[24 + l] = vR[l];
+    }
+  }
+  xv[30] = q[cL];
+  xv[31] = q[cR];
+  xv[32] = 0.5 * (b.mu[cL] + b.mu[cR]);
+  xv[33] = 0.5 * (b.mut[cL] + b.mut[cR]);
+  xv[34] = 0.5 * (b.F1[cL] + b.F1[cR]);
+  const long long fi = fidx(d, dir, ir, jr, kr);
+  double bx[35];
+#pragma unroll 1
+  for (int g0 = 0; g0 < 35; g0 += 7) {
+    D x[35], Fv[6];
+    for (int m = 0; m < 35; ++m) x[m] = D::var(xv[m], m - g0);  // seeds g0..g0+6 only
+    visc_flux_sst_d<D>(p, x, b.cells + 4 * cL, b.cells + 4 * cR, b.faces[dir] + 4 * fi, Fv);
+    for (int m = 0; m < 7; ++m) {
+      double s = 0.0;
+      for (int l = 0; l < 6; ++l) s -= mu[l] * Fv[l].d[m];
+      bx[g0 + m] = s;
+    }
+  }
+  for (int m = 0; m < 18; ++m)
+    if (bx[m] != 0.0) {
+      atomicAdd(barG + gL * 18 + m, 0.5 * bx[m]);
+      atomicAdd(barG + gR * 18 + m, 0.5 * bx[m]);
+    }
+  double gl[6], gr[6];
+  for (int l = 0; l < 6; ++l) {
+    gl[l] = bx[18 + l];
+    gr[l] = bx[24 + l];
+  }
+  gl[3] += 0.5 * bx[32] * dmu_dT(p, TL);
+  gr[3] += 0.5 * bx[32] * dmu_dT(p, TR);
+  give_sst(p, b, bar, cL, gl, bx[30]);
+  give_sst(p, b, bar, cR, gr, bx[31]);
+  if (bx[33] != 0.0) {
+    atomicAdd(barMut + cL, 0.5 * bx[33]);
+    atomicAdd(barMut + cR, 0.5 * bx[33]);
+  }
+  if (bx[34] != 0.0) {
+    atomicAdd(barF1 + cL, 0.5 * bx[34]);
+    atomicAdd(barF1 + cR, 0.5 * bx[34]);
+  }
+}
+
+// eddy viscosity and F1 of a cell (viscosity.f90:215-546) and, for an
+// interior cell, its SST source (source.f90:158-270), on duals over
+// (rho, k, omega, T, G[18]); the laminar viscosity from T
+template <typename D>
+__device__ __forceinline__ void sst_cell_d(const Params& p, const D* x, double dd, double vol, bool source,
+                                           D& mut, D& F1, D& Sk, D& Sw) {
+  const bool s2003 = p.turb == FEST_TURB_SST2003;
+  const D rho = x[0], tk = x[1], tw = x[2], T = x[3];
+  const D* G = x + 4;
+  D mu;
+  if (p.mu_var == FEST_MU_SUTHERLAND)
+    mu = D(p.mu_ref) * pow(T / D(p.T_ref), D(1.5)) * ((D(p.T_ref) + D(p.S)) / (T + D(p.S)));
+  else
+    mu = D(p.mu_ref);
+  const D d1(dd);
+  const D var1 = sqrt(tk) / (D(kSstBstar) * tw * d1);
+  const D var2 = D(500.) * (mu / rho) / ((d1 * d1) * tw);
+  const D arg2 = fmax2(D(2.) * var1, var2);
+  const D F = tanh(arg2 * arg2);
+  const D NUM = rho * D(kSstA1) * tk;
+  // G(component, variable) = G[3 (variable - 1) + component]
+  const D wx = G[7] - G[5], wy = G[2] - G[6], wz = G[3] - G[1];
+  const D vort = sqrt(wx * wx + wy * wy + wz * wz);
+  D DENOM;
+  if (s2003) {
+    const D sxx = G[0], syy = G[4], szz = G[8];
+    const D syz = G[7] + G[5], szx = G[2] + G[6], sxy = G[3] + G[1];
+    const D SijSij = (D(2.) * (sxx * sxx)) + (D(2.) * (syy * syy)) + (D(2.) * (szz * szz)) + syz * syz + szx * szx +
+                     sxy * sxy;
+    DENOM = fmax2(fmax2(D(kSstA1) * tw, sqrt(SijSij) * F), D(1.0e-10));
+  } else {
+    DENOM = fmax2(fmax2(D(kSstA1) * tw, vort * F), D(1.e-20));
+  }
+  mut = NUM / DENOM;
+  D CD = D(2.) * rho * D(kSstSigW2) * (G[12] * G[15] + G[13] * G[16] + G[14] * G[17]) / tw;
+  CD = fmax2(CD, D(s2003 ? 1.0e-10 : 1e-20));
+  const D right = D(4.) * (rho * D(kSstSigW2) * tk) / (CD * (d1 * d1));
+  const D arg1 = fmin2(fmax2(var1, var2), right);
+  const D a2 = arg1 * arg1;
+  F1 = tanh(a2 * a2);
+  if (!source) return;
+  const double lim = s2003 ? 10.0 : 20.0;
+  const double g1 = s2003 ? 5.0 / 9.0 : (kSstBeta1 / kSstBstar) - ((kSstSigW1 * (kSstKappa * kSstKappa)) / ::sqrt(kSstBstar));
+  const double g2 = s2003 ? 0.44 : (kSstBeta2 / kSstBstar) - ((kSstSigW2 * (kSstKappa * kSstKappa)) / ::sqrt(kSstBstar));
+  const D gama = D(g1) * F1 + D(g2) * (D(1.) - F1);
+  const D beta = D(kSstBeta1) * F1 + D(kSstBeta2) * (D(1.) - F1);
+  const D Dk = D(kSstBstar) * rho * tw * tk;
+  const D Dw = beta * rho * (tw * tw);
+  const D divergence = G[0] + G[4] + G[8];
+  D Pk = mut * (vort * vort) - ((D(2.0) / D(3.0)) * rho * tk * divergence);
+  Pk = fmin2(Pk, D(lim) * Dk);
+  const D Pw = (rho * gama / mut) * Pk;
+  const D lamda = (D(1.) - F1) * CD;
+  Sk = (Pk - Dk) * D(vol);
+  Sw = (Pw - Dw + lamda) * D(vol);
+}
+
+// the face id whose layer-1 ghost cell (i, j, k) of the gradient range is,
+// or -1 (interior, edge or corner)
+__device__ __forceinline__ int ghost_face_of(const Dims& d, int i, int j, int k) {
+  const int oi = (i == 0) + (i == d.imx), oj = (j == 0) + (j == d.jmx), ok = (k == 0) + (k == d.kmx);
+  if (oi + oj + ok != 1) return -1;
+  if (oi) return i == 0 ? 0 : 1;
+  if (oj) return j == 0 ? 2 : 3;
+  return k == 0 ? 4 : 5;
+}
+
+// ghost layer-1 eddy viscosity and F1 of faces -1..-9 are copies of the
+// interior cell's (the wall negating mu_t, viscosity.f90:287-340): their
+// adjoints move into the interior cell's
+__global__ void k_vjp_mut_ghost(Params p, double* barMut, double* barF1) {
+  const int f = blockIdx.z;
+  const Dims& d = p.d;
+  const int id = p.id[f];
+  if (!(id <= -1 && id >= -9)) return;
+  const int dir = f / 2;
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nb) return;
+  const int ta = 1 + (int)(t % na), tb = 1 + (int)(t / na);
+  const long long g = gcell_p(d, f, 1, ta, tb), in = icell_p(d, f, 1, ta, tb);
+  const double bm = barMut[g], bf = barF1[g];
+  barMut[g] = 0.0;
+  barF1[g] = 0.0;
+  if (bm != 0.0) atomicAdd(barMut + in, id == -5 ? -bm : bm);
+  if (bf != 0.0) atomicAdd(barF1 + in, bf);
+}
+
+// one thread per cell of the gradient range whose eddy viscosity and F1
+// come from its own state (interior cells, and the layer-1 ghost cells of
+// faces other than -1..-9): the transposed mu_t, F1 and (interior) source
+// onto its rho, k, omega, p and its gradient (barG)
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_sst_cell(Params p, DevBlock b, const double* lam, double* bar,
+                                                          double* barG, const double* barMut,
+                                                          const double* barF1) {
+  using D = Dual<double, 22>;
+  const Dims& d = p.d;
+  const long long NG = ngrad(d);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= NG) return;
+  const int i = (int)(t % (d.imx + 1));
+  const long long r = t / (d.imx + 1);
+  const int j = (int)(r % (d.jmx + 1)), k = (int)(r / (d.jmx + 1));
+  const bool interior = i >= 1 && i <= d.imx - 1 && j >= 1 && j <= d.jmx - 1 && k >= 1 && k <= d.kmx - 1;
+  if (!interior) {
+    const int f = ghost_face_of(d, i, j, k);
+    if (f < 0 || (p.id[f] <= -1 && p.id[f] >= -9)) return;
+  }
+  const long long c0 = pidx(d, i, j, k), P = d.P;
+  const double wm = barMut[c0], wf = barF1[c0];
+  double wk = 0.0, ww = 0.0;
+  if (interior) {
+    const long long ci = cidx(d, i, j, k), N = ncells(d);
+    wk = -lam[ci + 5 * N];  // the residual of k loses Sk, that of omega Sw
+    ww = -lam[ci + 6 * N];
+  }
+  if (wm == 0.0 && wf == 0.0 && wk == 0.0 && ww == 0.0) return;
+  const double* q = b.qp;
+  const double rho = q[c0], pr = q[c0 + 4 * P];
+  const double T = pr / (rho * p.R);
+  D x[22];
+  x[0] = D::var(rho, 0);
+  x[1] = D::var(q[c0 + 5 * P], 1);
+  x[2] = D::var(q[c0 + 6 * P], 2);
+  x[3] = D::var(T, 3);
+  for (int l = 0; l < 6; ++l)
+    for (int cc = 0; cc < 3; ++cc) x[4 + 3 * l + cc] = D::var(b.grad[cc][t + NG * l], 4 + 3 * l + cc);
+  D mut, F1, Sk, Sw;
+  sst_cell_d<D>(p, x, b.dist[c0], b.cells[4 * c0], interior, mut, F1, Sk, Sw);
+  double bx[22];
+  for (int m = 0; m < 22; ++m) {
+    double s = wm * mut.d[m] + wf * F1.d[m];
+    if (interior) s += wk * Sk.d[m] + ww * Sw.d[m];
+    bx[m] = s;
+  }
+  for (int m = 0; m < 18; ++m)
+    if (bx[4 + m] != 0.0) atomicAdd(barG + t * 18 + m, bx[4 + m]);
+  // T = p / (rho R)
+  const double grho = bx[0] - bx[3] * pr / (rho * rho * p.R), gp = bx[3] / (rho * p.R);
+  if (grho != 0.0) atomicAdd(bar + c0, grho);
+  if (gp != 0.0) atomicAdd(bar + c0 + 4 * P, gp);
+  if (bx[1] != 0.0) atomicAdd(bar + c0 + 5 * P, bx[1]);
+  if (bx[2] != 0.0) atomicAdd(bar + c0 + 6 * P, bx[2]);
+}
+
+// a layer-1 ghost cell's gradient of a face with a negative id
+// (apply_gradient_bc, gradients.f90:486-676) is the jump over the face
+// sigma (v_I - v_G) A n / V_I plus the interior gradient's tangential part
+// (adiabatic walls: minus the interior temperature gradient in place of
+// its jump); transposed onto the interior gradient and the two cells'
+// variables.  One thread per ghost column.
+__global__ void k_vjp_grad_bc(Params p, DevBlock b, double* barG, double* bar) {
+  const int f = blockIdx.z;
+  const Dims& d = p.d;
+  const int id = p.id[f];
+  if (!(id < 0)) return;
+  const int dir = f / 2, hi = f % 2;
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nb) return;
+  const int ta = 1 + (int)(t % na), tb = 1 + (int)(t / na);
+  const int n = extent_of(d, dir);
+  int gi, gj, gk, ii, ij, ik;
+  const int cg = hi ? n : 0, ci = hi ? n - 1 : 1;
+  if (dir == 0) { gi = cg; gj = ta; gk = tb; ii = ci; ij = ta; ik = tb; }
+  else if (dir == 1) { gi = ta; gj = cg; gk = tb; ii = ta; ij = ci; ik = tb; }
+  else { gi = ta; gj = tb; gk = cg; ii = ta; ij = tb; ik = ci; }
+  const long long og = gidx(d, gi, gj, gk), oi = gidx(d, ii, ij, ik);
+  double a[18];
+  bool any = false;
+  for (int m = 0; m < 18; ++m) {
+    a[m] = barG[og * 18 + m];
+    barG[og * 18 + m] = 0.0;
+    any |= a[m] != 0.0;
+  }
+  if (!any) return;
+  const int fcn = hi ? n : 1;
+  const double* fc = b.faces[dir] + 4 * fidx(d, dir, dir == 0 ? fcn : ta, dir == 1 ? fcn : (dir == 0 ? ta : tb),
+                                             dir == 2 ? fcn : tb);
+  const double nx = fc[1], ny = fc[2], nz = fc[3];
+  const long long cI = pidx(d, ii, ij, ik), cG = pidx(d, gi, gj, gk);
+  const double vI = b.cells[4 * cI];
+  const double cc3[3] = {fc[0] * nx / vI, fc[0] * ny / vI, fc[0] * nz / vI};
+  const double nn[3] = {nx, ny, nz};
+  const double sig = hi ? -1.0 : 1.0;
+  const bool adiab = id == -5 && (p.Tw[f] < 1. && p.Tw[f] >= 0.);
+  double gI[6] = {0, 0, 0, 0, 0, 0}, gG[6] = {0, 0, 0, 0, 0, 0};
+  for (int l = 0; l < 6; ++l) {
+    double dot = 0.0, s = 0.0;
+    for (int q = 0; q < 3; ++q) {
+      dot += a[3 * l + q] * nn[q];
+      s += a[3 * l + q] * cc3[q];
+    }
+    for (int q = 0; q < 3; ++q) {
+      double g = a[3 * l + q] - nn[q] * dot;           // the tangential part
+      if (adiab && l == 3) g -= a[3 * l + q];          // minus the interior T gradient
+      if (g != 0.0) atomicAdd(barG + oi * 18 + 3 * l + q, g);
+    }
+    if (!(adiab && l == 3)) {
+      gI[l] = sig * s;
+      gG[l] = -sig * s;
+    }
+  }
+  give_sst(p, b, bar, cI, gI, 0.0);
+  give_sst(p, b, bar, cG, gG, 0.0);
+}
+
+// one thread per interior cell: its gradient adjoint (18 values, barG)
+// through the Green-Gauss sum (gradients.f90:405-482) onto u, v, w, T, k,
+// omega of the cell and its six neighbours
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_grad_sst(Params p, DevBlock b, const double* barG, double* bar) {
+  const Dims& d = p.d;
+  const long long N = ncells(d);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= N) return;
+  const int i = 1 + (int)(t % (d.imx - 1));
+  const long long r = t / (d.imx - 1);
+  const int j = 1 + (int)(r % (d.jmx - 1)), k = 1 + (int)(r / (d.jmx - 1));
+  const double* g = barG + gidx(d, i, j, k) * 18;  // [variable][component]
+  bool any = false;
+  for (int m = 0; m < 18; ++m) any |= g[m] != 0.0;
+  if (!any) return;
+  const int ncomp = d.kmx > 2 ? 3 : 2;
+  const long long c0 = pidx(d, i, j, k);
+  const double vol2 = 2 * b.cells[4 * c0];
+  const double* fr[6] = {b.faces[0] + 4 * fidx(d, 0, i, j, k), b.faces[1] + 4 * fidx(d, 1, i, j, k),
+                         b.faces[2] + 4 * fidx(d, 2, i, j, k), b.faces[0] + 4 * fidx(d, 0, i + 1, j, k),
+                         b.faces[1] + 4 * fidx(d, 1, i, j + 1, k), b.faces[2] + 4 * fidx(d, 2, i, j, k + 1)};
+  const long long nbc[6] = {pidx(d, i - 1, j, k), pidx(d, i, j - 1, k), pidx(d, i, j, k - 1),
+                            pidx(d, i + 1, j, k), pidx(d, i, j + 1, k), pidx(d, i, j, k + 1)};
+  double own[6] = {0, 0, 0, 0, 0, 0};
+  for (int f = 0; f < 6; ++f) {
+    const double sg = f < 3 ? -1.0 : 1.0;
+    double gn[6];
+    for (int l = 0; l < 6; ++l) {
+      double s = 0.0;
+      for (int q = 0; q < ncomp; ++q) s += g[3 * l + q] * fr[f][1 + q];
+      gn[l] = sg * s * fr[f][0] / vol2;
+      own[l] += gn[l];
+    }
+    give_sst(p, b, bar, nbc[f], gn, 0.0);
+  }
+  give_sst(p, b, bar, c0, own, 0.0);
+}
+
 // the ghost cells' adjoints flow back into the interior cells the BC of
 // their face computed them from (bc_primitive.f90:160-206 and the
 // procedures it calls, at iteration iter); the ghost entries end at zero
@@ -647,16 +1065,46 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_ghosts(Params p, DevBlock b, do
     else if (dir == 1) { fi = ta; fj = c; fk = tb; }
     else { fi = ta; fj = tb; fk = c; }
   }
+  const int nv = d.nv;  // 5, or 7 with k and omega (bc_primitive.f90:160-206)
   switch (id) {
-    case -1: for (int l = 0; l < 5; ++l) none(l); break;
+    case -1: for (int l = 0; l < nv; ++l) none(l); break;
     case -2:
-    case -7: for (int l = 0; l < 5; ++l) flat(l); break;
-    case -3: for (int l = 0; l < 4; ++l) none(l); flat(4); break;
-    case -4: for (int l = 0; l < 4; ++l) flat(l); none(4); break;
+    case -7: for (int l = 0; l < nv; ++l) flat(l); break;
+    case -3: for (int l = 0; l < 4; ++l) none(l); flat(4); for (int l = 5; l < nv; ++l) none(l); break;
+    case -4: for (int l = 0; l < 4; ++l) flat(l); none(4); for (int l = 5; l < nv; ++l) flat(l); break;
     case -5:  // adiabatic wall (the host admits Tw in [0,1] only)
+      if (nv == 7) {
+        // set_omega_at_wall (bc_primitive.f90:564-643), last in the fill:
+        // omega_G(L) = 120 mu(Tf) / (rho_f beta1 (2 d_1)^2) - omega_I(L),
+        // Tf and rho_f the means over ghost and interior layer 1 (whose
+        // ghost values the wall's own copies made, so their adjoints go to
+        // the ghost entries the copies below then move inwards)
+        const long long g1 = gcell_p(d, f, 1, ta, tb), i1 = icell_p(d, f, 1, ta, tb);
+        const double rg = b.qp[g1], pg = b.qp[g1 + 4 * P], ri = b.qp[i1], pi = b.qp[i1 + 4 * P];
+        const double Tf = 0.5 * ((pg / rg) + (pi / ri)) / p.R;
+        const double Tr = p.T_ref, S = p.S;
+        const double mu = p.mu_ref * ::pow(Tf / Tr, 1.5) * ((Tr + S) / (Tf + S));
+        const double dmu = mu * (1.5 / Tf - 1.0 / (Tf + S));
+        const double rf = 0.5 * (rg + ri), dd = 2 * b.dist[i1];
+        const double W = 120 * mu / (rf * kSstBeta1 * (dd * dd));
+        double gT = 0.0, gR = 0.0;
+        for (int L = 1; L <= 3; ++L) {
+          const double a = take(L, 6);
+          give(L, 6, -a);
+          gT += a * W * dmu / mu;
+          gR += -a * W / rf;
+        }
+        // Tf = (pg/rg + pi/ri) / (2 R), rho_f = (rg + ri) / 2
+        bar[g1 + 4 * P] += gT * 0.5 / (rg * p.R);
+        bar[g1] += -gT * 0.5 * pg / (rg * rg * p.R) + 0.5 * gR;
+        give(1, 4, gT * 0.5 / (ri * p.R));
+        give(1, 0, -gT * 0.5 * pi / (ri * ri * p.R) + 0.5 * gR);
+        anti(5);
+      }
       symm(4); symm(0); anti(1); anti(2); anti(3);
       break;
     case -6: {  // slip wall: g = u - 2 (u.fn) fr  ->  bar_u += g_bar - 2 fn (fr.g_bar)
+      for (int l = 5; l < nv; ++l) symm(l);
       symm(0); symm(4);
       const long long in_n = fidx(d, dir, fi, fj, fk), in_r = fidx(d, 0, fi, fj, fk);
       const double* fn = b.faces[dir] + 4 * in_n;
@@ -710,13 +1158,13 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_ghosts(Params p, DevBlock b, do
         int na, nb, pa, pb;
         face_columns(d, f, na, nb);
         interface_map(p.part_orient[f], na, nb, ta, tb, pa, pb);
-        for (int l = 0; l < 5; ++l)
+        for (int l = 0; l < nv; ++l)
           for (int L = 1; L <= 3; ++L) {
             const double g = take(L, l);
             if (g != 0.0) atomicAdd(bar + icell_p(d, pf, L, pa, pb) + P * l, g);
           }
       } else {
-        for (int l = 0; l < 5; ++l) none(l);
+        for (int l = 0; l < nv; ++l) none(l);
       }
   }
 }
@@ -788,8 +1236,21 @@ __global__ void k_adj_psi(Dims d, const double* mu, double* psi) {  // psi = -mu
 
 }  // namespace
 
+long long vjp_grad_work_doubles(const Dims& d, bool sst) {
+  return sst ? 18 * ngrad(d) + 2 * d.P : 12 * ncells(d);
+}
+
 bool vjp_supported(const Params& p) {
-  if (p.turb != FEST_TURB_NONE || p.d.nv != 5) return false;
+  const bool sst = p.turb != FEST_TURB_NONE;
+  if (p.d.nv != (sst ? 7 : 5)) return false;
+  if (sst) {
+    // k-omega SST: viscous, and faces whose k and omega ghosts the
+    // transpose knows (no far-field or total-pressure faces, whose ghosts
+    // depend on the last column of the fill, and no block interfaces)
+    if (p.mu_ref == 0.0) return false;
+    for (int f = 0; f < 6; ++f)
+      if (p.id[f] == -8 || p.id[f] == -11 || p.id[f] >= 0) return false;
+  }
   if (p.pb[0] || p.pb[1] || p.pb[2]) return false;  // pressure switch couples variables
   if (ghosts_need_sequential(p) || p.d.kmx == 2) return false;
   for (int f = 0; f < 6; ++f) {
@@ -857,32 +1318,60 @@ long long vjp_face_work_doubles(const Dims& d) {
   for (int dir = 0; dir < 3; ++dir)
     m = std::max<long long>(m, (long long)extent_of(d, dir) * ((dir == 0 ? d.jmx : d.imx) - 1) *
                                    ((dir == 2 ? d.jmx : d.kmx) - 1));
-  return 10 * m;
+  return 2 * NVMAX * m;
 }
 
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
                          double* bar, const Launcher& L, double* const* bar_faces, double* bar_grad,
                          double* face_work) {
   const Dims& d = p.d;
-  const bool visc = p.mu_ref != 0.0;
+  const bool visc = p.mu_ref != 0.0, sst = p.turb != FEST_TURB_NONE;
   cudaMemsetAsync(bar, 0, sizeof(double) * (size_t)d.P * d.nv, L.s);
-  if (visc) cudaMemsetAsync(bar_grad, 0, sizeof(double) * 12 * (size_t)ncells(d), L.s);
+  if (visc) cudaMemsetAsync(bar_grad, 0, sizeof(double) * (size_t)vjp_grad_work_doubles(d, sst), L.s);
+  // SST: gradient adjoints over the gradient range, then mu_t and F1
+  double* barG = bar_grad;
+  double* barMut = sst ? bar_grad + 18 * ngrad(d) : nullptr;
+  double* barF1 = sst ? barMut + d.P : nullptr;
   for (int dir = 0; dir < 3; ++dir) {
     const int n = extent_of(d, dir);
     const long long nf = (long long)n * ((dir == 0 ? d.jmx : d.imx) - 1) * ((dir == 2 ? d.jmx : d.kmx) - 1);
     double* bf = bar_faces ? bar_faces[dir] : nullptr;
-    if (p.flux == FEST_FLUX_SLAU)
-      k_vjp_flux<double, true><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
-    else
-      k_vjp_flux<double, false><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
-    k_vjp_recon<double><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+    if (d.nv == 7) {
+      if (p.flux == FEST_FLUX_SLAU)
+        k_vjp_flux<double, true, 7><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
+      else
+        k_vjp_flux<double, false, 7><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
+      k_vjp_recon<double, 7><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+    } else {
+      if (p.flux == FEST_FLUX_SLAU)
+        k_vjp_flux<double, true, 5><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
+      else
+        k_vjp_flux<double, false, 5><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
+      k_vjp_recon<double, 5><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+    }
     *L.count += 2;
-    if (visc) {
+    if (sst) {
+      k_vjp_viscous_sst<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, barG, barMut, barF1, dir);
+      ++*L.count;
+    } else if (visc) {
       k_vjp_viscous<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bar_grad, dir);
       ++*L.count;
     }
   }
-  if (visc) {
+  long long wcol = 0;  // the largest face's columns
+  for (int dir = 0; dir < 3; ++dir)
+    wcol = std::max<long long>(wcol, (long long)((dir == 0 ? d.jmx : d.imx) - 1) *
+                                         ((dir == 2 ? d.jmx : d.kmx) - 1));
+  if (sst) {
+    // mu_t, F1 copies of ghost cells -> the interior cells' own; then every
+    // cell whose mu_t and F1 come from its own state (with its source);
+    // ghost gradients -> interior gradients; Green-Gauss -> the state
+    k_vjp_mut_ghost<<<dim3(nblocks(wcol), 1, 6), TPB_ADJ, 0, L.s>>>(p, barMut, barF1);
+    k_vjp_sst_cell<<<nblocks(ngrad(d)), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, barG, barMut, barF1);
+    k_vjp_grad_bc<<<dim3(nblocks(wcol), 1, 6), TPB_ADJ, 0, L.s>>>(p, b, barG, bar);
+    k_vjp_grad_sst<<<nblocks(ncells(d)), TPB_ADJ, 0, L.s>>>(p, b, barG, bar);
+    *L.count += 4;
+  } else if (visc) {
     k_vjp_grad<<<nblocks(ncells(d)), TPB_ADJ, 0, L.s>>>(p, b, bar_grad, bar);
     ++*L.count;
   }

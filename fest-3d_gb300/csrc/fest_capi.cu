@@ -33,7 +33,7 @@ struct fest_handle {
   FusedState* fused = nullptr;
   double* d_vjp_bar = nullptr;  // adjoint work arrays, allocated on first use
   double* d_vjp_lam = nullptr;
-  double* d_vjp_grad = nullptr;  // laminar adjoint: 12 per interior cell
+  double* d_vjp_grad = nullptr;  // viscous adjoint work (vjp_grad_work_doubles)
   double* d_vjp_face = nullptr;  // adjoint: one direction's face flux transposes
   double* d_lu = nullptr;        // LU-SGS work arrays, allocated on first use
   double* d_stage = nullptr;     // interior-cell staging for pageable host arrays
@@ -787,7 +787,8 @@ int fest_get_total_conservative_residue(fest_handle* h, double* qp, int current_
 // viscosity at the resident state, which the residual's VJP reads
 static int viscous_prep(fest_handle* h) {
   if (h->p.mu_ref == 0.0) return FEST_OK;
-  if (!h->d_vjp_grad) RET(dalloc(h, &h->d_vjp_grad, 12 * ncells(h->p.d)));
+  if (!h->d_vjp_grad)
+    RET(dalloc(h, &h->d_vjp_grad, vjp_grad_work_doubles(h->p.d, h->p.turb != FEST_TURB_NONE)));
   launch_temperature(h->p, h->d, h->L());
   launch_gradients(h->p, h->d, h->L());
   launch_viscosity(h->p, h->d, h->L());
@@ -858,6 +859,8 @@ int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_i
                        double* psi, int* n_done, double* drop) {
   if (!h || !dJdq || max_iters < 0) return FEST_ERR_ARG;
   if (!vjp_supported(h->p) || h->p.tstep != 'l' || needs_batch(h)) return FEST_ERR_ARG;
+  // the pseudo-time preconditioner maps the five mean-flow variables
+  if (h->p.d.nv != 5) return FEST_ERR_ARG;
   if (h->p.integ != FEST_TIME_NONE && h->p.integ != FEST_TIME_TVDRK3) return FEST_ERR_ARG;
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
@@ -865,7 +868,8 @@ int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_i
   if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
   // the handle keeps this one: allocated before the solve's own work arrays,
   // which release() frees
-  if (h->p.mu_ref != 0.0 && !h->d_vjp_grad) RET(dalloc(h, &h->d_vjp_grad, 12 * ncells(h->p.d)));
+  if (h->p.mu_ref != 0.0 && !h->d_vjp_grad)
+    RET(dalloc(h, &h->d_vjp_grad, vjp_grad_work_doubles(h->p.d, h->p.turb != FEST_TURB_NONE)));
   if (!h->d_vjp_face) RET(dalloc(h, &h->d_vjp_face, vjp_face_work_doubles(h->p.d)));
   AdjointWork w{};
   w.bar = h->d_vjp_bar;

@@ -91,6 +91,14 @@ FEST_DUAL Dual<T, N> sqrt(const Dual<T, N>& a) {
   return r;
 }
 FEST_DUAL Dual<T, N> fabs(const Dual<T, N>& a) { return a.v < T(0) ? -a : a; }
+FEST_DUAL Dual<T, N> tanh(const Dual<T, N>& a) {
+  Dual<T, N> r;
+  r.v = ::tanh(a.v);
+  const T g = T(1) - r.v * r.v;
+#pragma unroll
+  for (int n = 0; n < N; ++n) r.d[n] = a.d[n] * g;
+  return r;
+}
 FEST_DUAL Dual<T, N> floor(const Dual<T, N>& a) { return Dual<T, N>::cst(::floor(a.v)); }
 FEST_DUAL Dual<T, N> copysign(const Dual<T, N>& a, const Dual<T, N>& b) {
   return (signbit(a.v) == signbit(b.v)) ? a : -a;

@@ -83,6 +83,9 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
                          double* bar, const Launcher& L, double* const* bar_faces, double* bar_grad,
                          double* face_work);
 long long vjp_face_work_doubles(const Dims& d);
+// the bar_grad work space: 12 doubles per interior cell (laminar), or the
+// SST's gradient, eddy-viscosity and F1 adjoints
+long long vjp_grad_work_doubles(const Dims& d, bool sst);
 // nodes-layout bar_nodes = (dfaces/dnodes)^T bar_faces, through the face
 // vectors and the ghost-node extrapolation (interior nodes carry the result)
 void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_faces, double* bar_nodes,

@@ -146,10 +146,72 @@ def test_viscous_vjp_matches_oracle_finite_differences(gpu_lib, name):
     assert usable >= 3, f"{name}: only {usable} kink-free directions"
 
 
+# k-omega SST blocks: convective fluxes of seven variables, the viscous
+# terms with the eddy viscosity and the k, omega diffusion (viscous.f90:
+# 144-447), the eddy viscosity and F1 of every cell from its state and
+# gradient (viscosity.f90:215-546), the source (source.f90:158-270), the
+# gradients of u, v, w, T, k, omega with their BCs, and the ghost cells of
+# k and omega (wall omega of bc_primitive.f90:564-643); wall distances of a
+# wall face, molecular viscosity large enough that every term counts
+SST_CASES = {
+    "sst-muscl-ausmUP-walls": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ausmUP",
+                                                  turbulence="sst"),
+                                   ids=(-3, -4, -5, -6, -10, -10),
+                                   flow_kw=dict(mu_ref=0.3, mu_variation="sutherland_law", MInf=0.3)),
+    "sst-weno-slau-outlets": dict(scheme_kw=dict(interpolant="weno", scheme_name="slau", turbulence="sst"),
+                                  ids=(-3, -4, -6, -5, -10, -10),
+                                  flow_kw=dict(mu_ref=0.3, mu_variation="constant")),
+    "sst2003-none-ausm-supersonic": dict(scheme_kw=dict(interpolant="none", scheme_name="ausm",
+                                                        turbulence="sst2003"),
+                                         ids=(-1, -2, -5, -5, -6, -6),
+                                         flow_kw=dict(mu_ref=0.3, mu_variation="sutherland_law")),
+}
+
+
+@pytest.mark.parametrize("name", list(SST_CASES))
+def test_sst_vjp_matches_oracle_finite_differences(gpu_lib, name):
+    from fest3d import cases
+    kw = dict(SST_CASES[name])
+    ext, flow, scheme, bc, nodes, qp = small_case(nc=(10, 8, 6), turb=True, **kw)
+    wall = cases.wall_nodes_of(nodes, ext, bc)
+    blk, h = make_pair(ext, flow, scheme, bc, nodes, qp, wall=wall)
+    rng = np.random.default_rng(17)
+    lam = np.asfortranarray(rng.standard_normal((ext.imx - 1, ext.jmx - 1, ext.kmx - 1, ext.n_var)))
+    dq = h.residual_vjp(qp, IT, lam)
+    mask = interior_mask(ext)
+    assert np.all(dq * (1 - mask) == 0), "ghost entries of dq must be zero"
+    scale = var_scale(qp, ext)
+
+    def phi(q):
+        blk["qp"] = np.asfortranarray(q)
+        assert O.get_total_conservative_residue([blk], IT) == 0
+        blk.compute_temperature()
+        assert O.get_total_conservative_residue([blk], IT) == 0
+        return float(np.sum(lam * blk["residue"]))
+
+    def fd(v, e):
+        return (8 * (phi(qp + e * v) - phi(qp - e * v)) - (phi(qp + 2 * e * v) - phi(qp - 2 * e * v))) / (12 * e)
+
+    inner = np.argwhere(mask[..., 0] > 0)
+    usable = 0
+    for trial in range(8):
+        v = np.zeros(qp.shape)
+        for i, j, k in inner[rng.choice(len(inner), 24, replace=False)]:
+            v[i, j, k] = rng.standard_normal(ext.n_var) * scale
+        f1, f2 = fd(v, 1e-6), fd(v, 2e-7)
+        if abs(f1 - f2) > 1e-6 * max(abs(f1), abs(f2)):
+            continue  # a min/max switch inside the step
+        ad = float(np.sum(dq * v))
+        assert abs(f1 - ad) <= 1e-5 * max(abs(f1), abs(ad)), (name, trial, f1, f2, ad)
+        usable += 1
+    assert usable >= 3, f"{name}: only {usable} kink-free directions"
+
+
 def test_vjp_rejects_unsupported_blocks(gpu_lib):
-    """SST blocks have no residual VJP; laminar blocks no metric VJP."""
+    """SST blocks with far-field faces have no residual VJP; laminar blocks
+    no metric VJP."""
     ext, flow, scheme, bc, nodes, qp = small_case(
-        nc=(12, 9, 7), ids=(-3, -4, -5, -6, -10, -10), turb=True,
+        nc=(12, 9, 7), ids=(-8, -4, -5, -6, -10, -10), turb=True,
         flow_kw=dict(mu_ref=1e-2, mu_variation="constant"))
     blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
     lam = np.zeros((ext.imx - 1, ext.jmx - 1, ext.kmx - 1, ext.n_var), order="F")
