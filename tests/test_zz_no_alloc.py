@@ -59,6 +59,7 @@ def test_noalloc_resnorm_matches_handle_resnorm(gpu_lib, turb):
         assert np.allclose(out, ref, rtol=1e-12, atol=1e-300), (call, out, ref)
 
 
+@pytest.mark.gpu
 def test_noalloc_refuses_a_capturing_stream(gpu_lib):
     """a call on a stream under capture returns FEST_ERR_ARG and leaves the
     capture intact: the captured graph (one torch add) replays"""
