@@ -77,6 +77,10 @@ def parse():
                          "lower-wall nodes against central differences); writes JSON")
     ap.add_argument("--study-nodes", default="1-128",
                     help="lower-wall nodes of --adjoint-study: a range a-b or a comma list")
+    ap.add_argument("--study-fd-step", type=float, default=1e-6,
+                    help="the central-difference step of --adjoint-study")
+    ap.add_argument("--study-params", default="mach,angle",
+                    help="flow parameters of --adjoint-study (comma list, may be empty)")
     ap.add_argument("--sweep", default="", choices=["", "mixed", "fp64"],
                     help="instead of the bench line: step the workload block --sweep-iters "
                          "iterations at this precision and exit (a short run for profilers)")
@@ -703,8 +707,9 @@ def run_adjoint_study(args):
         with open(args.adjoint_study, "w") as f:
             json.dump(o, f, indent=1)
 
-    out = A.wall_force_study(lib, wall_nodes=nodes, log=lambda *a: print(*a, file=sys.stderr, flush=True),
-                             progress=save)
+    params = tuple(x for x in args.study_params.split(",") if x)
+    out = A.wall_force_study(lib, wall_nodes=nodes, params=params, fd_step=args.study_fd_step,
+                             log=lambda *a: print(*a, file=sys.stderr, flush=True), progress=save)
     out["seconds"] = time.perf_counter() - t0
     with open(args.adjoint_study, "w") as f:
         json.dump(out, f, indent=1)

@@ -30,9 +30,9 @@ constexpr int TPB_ADJ = 128;
 template <typename T, int N> struct DualLine {
   const double* base;  // variable l, cell at normal coordinate 0
   long long stride;
-  int center;  // seeds the cells center-2 .. center+2
+  int center;  // seeds the N cells center - N/2 .. center + N/2
   __device__ __forceinline__ Dual<T, N> operator()(int c) const {
-    return Dual<T, N>::var((T)base[c * stride], c - center + 2);
+    return Dual<T, N>::var((T)base[c * stride], c - center + N / 2);
   }
 };
 template <typename T, int N> struct ConstLine {
@@ -335,13 +335,15 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, cons
 
 // one thread per (face, variable): the variable's two face states (cell
 // c-1's high side, cell c's low side) differentiated with respect to their
-// 5-cell stencils by forward duals, times the flux transpose of k_vjp_flux;
-// qL reaches cells c-3..c+1, qR cells c-2..c+2, and the six targets are
-// summed in registers before one atomic add each
-template <typename T, int NV>
+// W-cell stencils (W = 5 for PPM and the WENOs, 3 for MUSCL and first
+// order, which read no further, boundary overrides included) by forward
+// duals, times the flux transpose of k_vjp_flux; qL reaches cells
+// c-1-W/2..c-1+W/2, qR c-W/2..c+W/2, and the W+1 targets are summed in
+// registers before one atomic add each
+template <typename T, int NV, int W>
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_recon(Params p, DevBlock b, const double* bxi, double* bar,
                                                        int dir) {
-  using D5 = Dual<T, 5>;
+  using D5 = Dual<T, W>;
   const Dims& d = p.d;
   const int n = extent_of(d, dir);
   const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
@@ -356,22 +358,22 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_recon(Params p, DevBlock b, con
   face_of(d, dir, t, c, ta, tb);
   cell_of(dir, 0, ta, tb, i, j, k);
   const long long P = d.P, st = pstride(d, dir), c0 = pidx(d, i, j, k);
-  VolConst<T, 5> vol{b.cells + 4 * c0, st, n};
-  ConstLine<T, 5> pres{b.qp + c0 + P * 4, st};
-  T acc[6];
+  VolConst<T, W> vol{b.cells + 4 * c0, st, n};
+  ConstLine<T, W> pres{b.qp + c0 + P * 4, st};
+  T acc[W + 1];
   D5 Rm, Lp;
-  DualLine<T, 5> qa{b.qp + c0 + P * l, st, c - 1};
+  DualLine<T, W> qa{b.qp + c0 + P * l, st, c - 1};
   recon_cell<D5>(p, dir, c - 1, l + 1, qa, pres, vol, Rm, Lp);
 #pragma unroll
-  for (int s = 0; s < 5; ++s) acc[s] = bl * Lp.d[s];
-  acc[5] = T(0);
-  DualLine<T, 5> qb{b.qp + c0 + P * l, st, c};
+  for (int s = 0; s < W; ++s) acc[s] = bl * Lp.d[s];
+  acc[W] = T(0);
+  DualLine<T, W> qb{b.qp + c0 + P * l, st, c};
   recon_cell<D5>(p, dir, c, l + 1, qb, pres, vol, Rm, Lp);
 #pragma unroll
-  for (int s = 0; s < 5; ++s) acc[s + 1] += br * Rm.d[s];
+  for (int s = 0; s < W; ++s) acc[s + 1] += br * Rm.d[s];
 #pragma unroll
-  for (int s = 0; s < 6; ++s)
-    if (acc[s] != T(0)) atomicAdd(bar + c0 + (c - 3 + s) * st + P * l, (double)acc[s]);
+  for (int s = 0; s <= W; ++s)
+    if (acc[s] != T(0)) atomicAdd(bar + c0 + (c - 1 - W / 2 + s) * st + P * l, (double)acc[s]);
 }
 
 // ---- laminar viscous terms (gradients.f90, viscosity.f90, viscous.f90) -----
@@ -1328,6 +1330,8 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
   const bool visc = p.mu_ref != 0.0, sst = p.turb != FEST_TURB_NONE;
   cudaMemsetAsync(bar, 0, sizeof(double) * (size_t)d.P * d.nv, L.s);
   if (visc) cudaMemsetAsync(bar_grad, 0, sizeof(double) * (size_t)vjp_grad_work_doubles(d, sst), L.s);
+  // MUSCL and first-order states read cells c-1..c+1 only
+  const bool narrow = p.interp == FEST_INTERP_MUSCL || p.interp == FEST_INTERP_NONE;
   // SST: gradient adjoints over the gradient range, then mu_t and F1
   double* barG = bar_grad;
   double* barMut = sst ? bar_grad + 18 * ngrad(d) : nullptr;
@@ -1341,13 +1345,19 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
         k_vjp_flux<double, true, 7><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
       else
         k_vjp_flux<double, false, 7><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
-      k_vjp_recon<double, 7><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+      if (narrow)
+        k_vjp_recon<double, 7, 3><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+      else
+        k_vjp_recon<double, 7, 5><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
     } else {
       if (p.flux == FEST_FLUX_SLAU)
         k_vjp_flux<double, true, 5><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
       else
         k_vjp_flux<double, false, 5><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
-      k_vjp_recon<double, 5><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+      if (narrow)
+        k_vjp_recon<double, 5, 3><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+      else
+        k_vjp_recon<double, 5, 5><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
     }
     *L.count += 2;
     if (sst) {
