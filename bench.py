@@ -56,10 +56,10 @@ def parse():
     ap.add_argument("--workload", default="bump", choices=["bump", "bump-512x192x16"],
                     help="bump: the headline 256x96x4 block; bump-512x192x16: the same case on a "
                          "1.6M-cell block (for profiling the sweep at a size that streams HBM)")
-    ap.add_argument("--converged", type=int, default=0, metavar="ITERS",
-                    help="instead of the bench line: run FP64 for ITERS iterations, then mixed "
-                         "until its wall Cp is within 1e-5 of FP64's (at most ITERS), and report "
-                         "both wall times")
+    ap.add_argument("--converged", type=int, default=0, metavar="MAPS",
+                    help="instead of the bench line: the bump's steady state in mixed precision "
+                         "and FP64 by Anderson-accelerated iterations (at most MAPS maps of 50 "
+                         "iterations each), with the wall Cp of the two compared")
     ap.add_argument("--plate", type=int, default=0, metavar="ITERS",
                     help="instead of the bench line: the two-block SST flat plate 192x128x2 for ITERS "
                          "iterations in mixed precision and FP64, with the skin-friction difference")
@@ -737,19 +737,23 @@ def run_sweep(args):
 
 
 def run_converged(args):
-    """Wall time for the mixed-precision solver to reach, on the bump, the
-    wall Cp of an FP64 run of args.converged iterations to within 1e-5."""
+    """The bump's steady state in mixed precision (from the free stream) and
+    in FP64 (from the mixed one), by Anderson-accelerated iterations of each
+    precision's own sweep (fest3d.adjoint.converge_accelerated, 50
+    iterations per map, at most args.converged maps): the mass-residual drop
+    each reaches against the first iteration's, its wall time, and the
+    wall Cp of the two steady states against each other.  Mixed precision
+    levels off at its rounding floor; FP64 stops at a 1e-12 drop."""
     import numpy as np
     import torch
     torch.cuda.set_device(0)
-    from fest3d import abi, build, cases
+    from fest3d import abi, build, cases, adjoint as A
     from fest3d.handle import Handle
     if not os.path.exists(abi.LIB_PATH):
         build.build()
     lib = abi.load()
     case = cases.bump_case()
     ext, flow, CFL = case["ext"], case["flow"], case["CFL"]
-    total = args.converged
 
     def make(prec):
         h = Handle(ext, flow, case["scheme"], case["bc"], lib=lib)
@@ -758,35 +762,28 @@ def run_converged(args):
         h.set_precision(prec)
         return h
 
-    out = {"mode": "converged wall Cp", "workload": case["name"], "fp64_iters": total}
-    h = make(abi.FEST_FP64)
-    it, t64, hist = 1, 0.0, []
-    while it <= total:
-        n = min(20000, total - it + 1)
+    out = {"mode": "converged wall Cp", "workload": case["name"], "maps_cap": args.converged}
+    res = {}
+    ref, start = None, None
+    for prec, name, tol in ((abi.FEST_MIXED, "mixed", 1e-12), (abi.FEST_FP64, "fp64", 1e-12)):
+        h = make(prec)
+        n1 = float(h.step(1, 1, CFL)[1])
+        ref = ref or n1
+        if start is not None:
+            h.upload_state(start)
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        norm = h.step(n, it, CFL)
-        t64 += time.perf_counter() - t0
-        it += n
-        hist.append([it - 1, float(norm[1])])
-    cp64 = wall_cp(h.download_state(), ext, flow)
-    out.update(fp64_seconds=t64, fp64_residual=hist)
-    h.close()
-    h = make(abi.FEST_MIXED)
-    it, t32, hist, reached = 1, 0.0, [], None
-    while it <= total:
-        n = min(10000, total - it + 1)
-        t0 = time.perf_counter()
-        norm = h.step(n, it, CFL)
-        t32 += time.perf_counter() - t0
-        it += n
-        d = float(np.abs(wall_cp(h.download_state(), ext, flow) - cp64).max())
-        hist.append([it - 1, float(norm[1]), d])
-        if reached is None and d <= 1e-5:
-            reached = {"iters": it - 1, "seconds": t32}
-            break
-    out.update(mixed_residual_and_cp_diff=hist, mixed_reached=reached,
-               mixed_seconds_run=t32,
-               speedup_to_fp64_cp=(t64 / reached["seconds"]) if reached else None)
+        q, it, drop, _, maps, iters = A.converge_accelerated(h, h.download_state(), CFL, first_iter=2, tol=tol,
+                                                             ref=ref, max_maps=args.converged)
+        start = q
+        sec = time.perf_counter() - t0
+        res[name] = {"q": q, "drop": drop, "maps": maps, "iterations": iters + 1, "seconds": sec}
+        h.close()
+    cp = {k: wall_cp(v["q"], ext, flow) for k, v in res.items()}
+    for k, v in res.items():
+        out[k] = {x: v[x] for x in ("drop", "maps", "iterations", "seconds")}
+    out["wall_cp_abs_err_mixed_vs_fp64"] = float(np.abs(cp["mixed"] - cp["fp64"]).max())
+    out["wall_cp_max_abs"] = float(np.abs(cp["fp64"]).max())
     print(json.dumps(out), flush=True)
 
 

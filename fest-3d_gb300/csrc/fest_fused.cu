@@ -1044,7 +1044,9 @@ int fused_run(FusedState* f, const Params& p, const DevBlock& b, int prec, int n
 const double* fused_current_state(const FusedState* f) { return f && f->seeded ? f->Q[f->cur] : nullptr; }
 
 // dense interior cells -> the FP64 state and (q32 non-null) its mirror,
-// converted as k_to_mirror converts them
+// converted as the sweep converts the states it writes (d2f: FP32
+// subnormals become zero), so that an unchanged state leaves the mirror
+// unchanged
 __global__ void k_import_interior(Dims d, int pitch, const double* __restrict__ src, double* __restrict__ q64,
                                   float* __restrict__ q32) {
   const long long nc = ncells(d), n = nc * d.nv;
@@ -1057,7 +1059,7 @@ __global__ void k_import_interior(Dims d, int pitch, const double* __restrict__ 
     const long long pp = pidx(d, i, j, k) + d.P * l;
     const double v = src[t];
     q64[pp] = v;
-    if (q32) q32[(pp / d.ni) * pitch + pp % d.ni] = (float)v;
+    if (q32) q32[(pp / d.ni) * pitch + pp % d.ni] = d2f(v);
   }
 }
 
