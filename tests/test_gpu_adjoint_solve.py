@@ -18,6 +18,22 @@ from fest3d import adjoint as A
 pytestmark = pytest.mark.gpu
 
 
+def test_wall_force_study_at_the_configuration_size(gpu_lib):
+    """The configuration itself: the 128x48x4 bump with unlimited MUSCL +
+    SLAU, the primal converged to a 1e-12 drop (Anderson-accelerated
+    explicit iterations), the adjoint to a 1e-10 drop (GMRES over the
+    fixed-point adjoint iteration); the inflow Mach number and the two
+    largest wall-node gradients (the inlet corner and the bump's flank)
+    against central differences (step 1e-6) of re-converged primal
+    solutions, to 2e-4.  The full run over all 128 nodes is committed with
+    its command line (bench.py --adjoint-study)."""
+    out = A.wall_force_study(gpu_lib, wall_nodes=(1, 65), params=("mach",), threads=3)
+    assert out["primal"]["drop"] <= 1e-12
+    assert out["adjoint"]["drop"] <= 1e-10
+    for r in out["rows"]:
+        assert r["rel_diff"] <= 2e-4, r
+
+
 def test_bump_wall_force_sensitivities(gpu_lib):
     case = A.adjoint_case(nc=(64, 24, 4), interpolant="none")
     h = A.make_handle(case, lib=gpu_lib)
