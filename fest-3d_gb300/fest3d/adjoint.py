@@ -272,7 +272,8 @@ def perturbed_case(case, param, delta):
 
 
 def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angle"), fd_step=1e-6,
-                     fd_steps=None, primal_tol=1e-12, adjoint_tol=1e-10, threads=4, log=None, progress=None):
+                     fd_steps=None, primal_tol=1e-12, adjoint_tol=1e-10, threads=4, log=None, progress=None,
+                     fd_tol=None):
     """The bump's wall-force sensitivities at 128x48x4 cells (Euler,
     unlimited MUSCL + SLAU, FP64): the primal converged to a primal_tol
     drop (Anderson-accelerated explicit iterations from the free stream),
