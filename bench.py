@@ -79,6 +79,9 @@ def parse():
                     help="lower-wall nodes of --adjoint-study: a range a-b or a comma list")
     ap.add_argument("--study-fd-step", type=float, default=1e-6,
                     help="the central-difference step of --adjoint-study")
+    ap.add_argument("--study-fd-tol", type=float, default=0.0,
+                    help="the residual drop the --adjoint-study re-solves reach (default: the "
+                         "primal's, 1e-12)")
     ap.add_argument("--study-params", default="mach,angle",
                     help="flow parameters of --adjoint-study (comma list, may be empty)")
     ap.add_argument("--sweep", default="", choices=["", "mixed", "fp64"],
@@ -709,6 +712,7 @@ def run_adjoint_study(args):
 
     params = tuple(x for x in args.study_params.split(",") if x)
     out = A.wall_force_study(lib, wall_nodes=nodes, params=params, fd_step=args.study_fd_step,
+                             fd_tol=args.study_fd_tol or None,
                              log=lambda *a: print(*a, file=sys.stderr, flush=True), progress=save)
     out["seconds"] = time.perf_counter() - t0
     with open(args.adjoint_study, "w") as f:

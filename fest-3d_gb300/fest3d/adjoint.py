@@ -282,7 +282,8 @@ def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angl
     angle and the y-displacements of the listed lower-wall nodes; each
     checked by a central difference of two re-converged primal solutions
     (step fd_step, or fd_steps[param]; each re-solve from the converged
-    state to the same drop), the re-solves spread over `threads` handles.
+    state to the same drop, or to fd_tol), the re-solves spread over
+    `threads` handles.
     Returns a dict of everything measured; progress(dict), if given, sees
     it after every stage and every checked parameter."""
     import time
@@ -332,7 +333,8 @@ def wall_force_study(lib, wall_nodes=tuple(range(1, 129)), params=("mach", "angl
         for sgn in (1.0, -1.0):
             c = perturbed_case(case, param, sgn * step)
             hp = make_handle(c, lib=lib)
-            qs, _, d, _, m, n = converge_accelerated(hp, start, CFL, first_iter=it, tol=primal_tol, ref=ref)
+            qs, _, d, _, m, n = converge_accelerated(hp, start, CFL, first_iter=it, tol=fd_tol or primal_tol,
+                                                     ref=ref, max_maps=6000)
             vals.append(wall_force(qs, ext, hp.get("Jfaces"))[0])
             info.append({"drop": d, "iterations": n})
             hp.close()
