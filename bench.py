@@ -84,9 +84,11 @@ def parse():
                          "primal's, 1e-12)")
     ap.add_argument("--study-params", default="mach,angle",
                     help="flow parameters of --adjoint-study (comma list, may be empty)")
-    ap.add_argument("--sweep", default="", choices=["", "mixed", "fp64"],
+    ap.add_argument("--sweep", default="", choices=["", "mixed", "fp64", "vjp"],
                     help="instead of the bench line: step the workload block --sweep-iters "
-                         "iterations at this precision and exit (a short run for profilers)")
+                         "iterations at this precision, or (vjp) evaluate --sweep-iters primal "
+                         "residuals and residual VJPs on the adjoint workload, and exit (a short "
+                         "run for profilers)")
     ap.add_argument("--sweep-iters", type=int, default=6)
     ap.add_argument("--c2-iters", type=int, default=C2_ITERS, metavar="ITERS",
                     help="iterations of the mixed-vs-FP64 bump report (wall Cp, entropy, residual "
@@ -729,6 +731,21 @@ def run_sweep(args):
     if not os.path.exists(abi.LIB_PATH):
         build.build()
     lib = abi.load()
+    if args.sweep == "vjp":
+        import numpy as np
+        from fest3d import adjoint as A
+        case = A.adjoint_case()
+        ext = case["ext"]
+        h = A.make_handle(case, lib=lib)
+        q = np.array(case["qp"], order="F")
+        lam = np.asfortranarray(np.random.default_rng(0).standard_normal(
+            (ext.imx - 1, ext.jmx - 1, ext.kmx - 1, 5)))
+        for _ in range(args.sweep_iters):
+            h.residual(q, 3)
+            h.residual_vjp(q, 3, lam)
+        print(json.dumps({"sweep": "vjp", "calls": args.sweep_iters, "launches": h.launches}), flush=True)
+        h.close()
+        return
     case = cases.bump_case() if args.workload == "bump" else cases.bump_case(nc=(512, 192, 16))
     h = Handle(case["ext"], case["flow"], case["scheme"], case["bc"], lib=lib)
     h.setup_geometry(case["nodes"])
