@@ -228,10 +228,39 @@ __device__ __forceinline__ void face_of(const Dims& d, int dir, long long t, int
   tb = 1 + (int)(r / na);
 }
 
+// one thread per (face, variable): the face's two states of that variable
+// (cell c-1's high side, cell c's low side), the reconstruction in plain
+// arithmetic, stored as w[l * nf + t] and w[(NV + l) * nf + t]
+template <typename T, int NV>
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_states(Params p, DevBlock b, double* w, int dir) {
+  const Dims& d = p.d;
+  const int n = extent_of(d, dir);
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
+  const long long nf = (long long)n * na * nb;
+  const long long tl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tl >= NV * nf) return;
+  const int l = (int)(tl / nf);
+  const long long t = tl - l * nf;
+  int c, ta, tb, i, j, k;
+  face_of(d, dir, t, c, ta, tb);
+  cell_of(dir, 0, ta, tb, i, j, k);
+  const long long P = d.P, st = pstride(d, dir), c0 = pidx(d, i, j, k);
+  VolVal<T> vol{b.cells + 4 * c0, st, n};
+  ValLine<T> pres{b.qp + c0 + P * 4, st};
+  ValLine<T> q{b.qp + c0 + P * l, st};
+  T Rm, Lp;
+  recon_cell<T>(p, dir, c - 1, l + 1, q, pres, vol, Rm, Lp);
+  w[l * nf + t] = (double)Lp;
+  recon_cell<T>(p, dir, c, l + 1, q, pres, vol, Rm, Lp);
+  w[(NV + l) * nf + t] = (double)Rm;
+}
+
 // one thread per face of direction dir: mu = lambda(left) - lambda(right)
-// transposed through the flux onto the 2 NV face-state values, stored as
-// bx[m * nf + t]; and, when bar_face is given, onto the face record.
-// Reverse mode for SLAU, forward duals over the 2 NV values otherwise.
+// transposed through the flux onto the 2 NV face-state values (read from
+// the work array k_vjp_states filled, overwritten in place by the
+// transposes, bx[m * nf + t]); and, when bar_face is given, onto the face
+// record.  Reverse mode for SLAU, forward duals over the 2 NV values
+// otherwise.
 template <typename T, bool SLAU, int NV>
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, const double* lam, double* bxo,
                                                       double* bar_face, int dir) {
@@ -244,8 +273,7 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, cons
   if (t >= nf) return;
   int c, ta, tb;
   face_of(d, dir, t, c, ta, tb);
-  const long long P = d.P, N = ncells(d);
-  const long long st = pstride(d, dir);
+  const long long N = ncells(d);
   // mu = lambda(left) - lambda(right); ghost cells carry no residual
   T mu[NV];
   int i, j, k;
@@ -269,22 +297,13 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, cons
     for (int m = 0; m < 2 * NV; ++m) bxo[m * nf + t] = 0.0;
     return;
   }
-  // the face states' values (the reconstruction in plain arithmetic)
+  // the face states' values (k_vjp_states)
   cell_of(dir, 0, ta, tb, i, j, k);
-  const long long c0 = pidx(d, i, j, k);
   T qL[NV], qR[NV];
-  {
-    VolVal<T> vol{b.cells + 4 * c0, st, n};
-    ValLine<T> pres{b.qp + c0 + P * 4, st};
 #pragma unroll
-    for (int l = 0; l < NV; ++l) {
-      T Rm, Lp;
-      ValLine<T> q{b.qp + c0 + P * l, st};
-      recon_cell<T>(p, dir, c - 1, l + 1, q, pres, vol, Rm, Lp);
-      qL[l] = Lp;
-      recon_cell<T>(p, dir, c, l + 1, q, pres, vol, Rm, Lp);
-      qR[l] = Rm;
-    }
+  for (int l = 0; l < NV; ++l) {
+    qL[l] = (T)bxo[l * nf + t];
+    qR[l] = (T)bxo[(NV + l) * nf + t];
   }
   const long long fi = fidx(d, dir, i + (dir == 0 ? c : 0), j + (dir == 1 ? c : 0), k + (dir == 2 ? c : 0));
   const double* fc = b.faces[dir] + 4 * fi;
@@ -1341,6 +1360,7 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
     const long long nf = (long long)n * ((dir == 0 ? d.jmx : d.imx) - 1) * ((dir == 2 ? d.jmx : d.kmx) - 1);
     double* bf = bar_faces ? bar_faces[dir] : nullptr;
     if (d.nv == 7) {
+      k_vjp_states<double, 7><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, dir);
       if (p.flux == FEST_FLUX_SLAU)
         k_vjp_flux<double, true, 7><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
       else
@@ -1350,6 +1370,7 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
       else
         k_vjp_recon<double, 7, 5><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
     } else {
+      k_vjp_states<double, 5><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, dir);
       if (p.flux == FEST_FLUX_SLAU)
         k_vjp_flux<double, true, 5><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
       else
@@ -1359,7 +1380,7 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
       else
         k_vjp_recon<double, 5, 5><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
     }
-    *L.count += 2;
+    *L.count += 3;
     if (sst) {
       k_vjp_viscous_sst<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, barG, barMut, barF1, dir);
       ++*L.count;
