@@ -38,6 +38,13 @@ struct fest_handle {
   double* d_lu = nullptr;        // LU-SGS work arrays, allocated on first use
   double* d_stage = nullptr;     // interior-cell staging for pageable host arrays
   int* h_err = nullptr;          // pinned host copy of the device error word
+  // state snapshot for the output writers (fest_snapshot_begin): the
+  // device copy, its error word, the copy stream and its two events
+  double* d_snap = nullptr;
+  int* h_snap_err = nullptr;
+  cudaStream_t snap_s = nullptr;
+  cudaEvent_t snap_ev[2] = {nullptr, nullptr};
+  bool snap_busy = false;
   // events around the device work of the last timed call (after its inputs
   // arrived, before its outputs leave): fest_last_kernel_ms
   cudaEvent_t kev[2] = {nullptr, nullptr};
@@ -515,10 +522,17 @@ int fest_destroy(fest_handle* h) {
   if (!h) return FEST_OK;
   if (h->s) cudaStreamSynchronize(h->s);
   cudaGetLastError();  // nothing of this handle's may linger for the next call
+  if (h->snap_busy) cudaEventSynchronize(h->snap_ev[1]);
+  if (h->snap_s) cudaStreamSynchronize(h->snap_s);
+  cudaGetLastError();
   if (h->fused) fused_destroy(h->fused);
   for (void* p : h->allocs) cudaFree(p);
   if (h->own) cudaStreamDestroy(h->own);
+  if (h->snap_s) cudaStreamDestroy(h->snap_s);
   if (h->h_err) cudaFreeHost(h->h_err);
+  if (h->h_snap_err) cudaFreeHost(h->h_snap_err);
+  for (cudaEvent_t e : h->snap_ev)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : h->kev)
     if (e) cudaEventDestroy(e);
   delete h;
@@ -637,6 +651,43 @@ int fest_download_state(fest_handle* h, double* qp) {
   const double* cur = fused_current_state(h->fused);
   RET(down(h, qp, cur ? cur : h->d.qp, h->p.d.P * h->p.d.nv));
   return finish(h);
+}
+
+// checkpoint (dump_solution.f90:27-52) without stopping the stepping: the
+// current state is copied on the device, in stream order after the work
+// already enqueued, and the copy crosses the link on a stream of its own,
+// so that steps enqueued after this call run while it travels.  The error
+// word is copied beside the state: a snapshot of a failed step says so.
+int fest_snapshot_begin(fest_handle* h, double* qp_host) {
+  if (!h || !qp_host || h->snap_busy) return FEST_ERR_ARG;
+  const long long n = h->p.d.P * h->p.d.nv;
+  if (!h->snap_s) {
+    CK(cudaStreamCreateWithFlags(&h->snap_s, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : h->snap_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CK(cudaMallocHost((void**)&h->h_snap_err, sizeof(int)));
+  }
+  if (!h->d_snap) RET(dalloc(h, &h->d_snap, n + 1));
+  const double* cur = fused_current_state(h->fused);
+  CK(cudaMemcpyAsync(h->d_snap, cur ? cur : h->d.qp, sizeof(double) * (size_t)n,
+                     cudaMemcpyDeviceToDevice, h->s));
+  CK(cudaMemcpyAsync(h->d_snap + n, h->d.err, sizeof(int), cudaMemcpyDeviceToDevice, h->s));
+  CK(cudaEventRecord(h->snap_ev[0], h->s));
+  CK(cudaStreamWaitEvent(h->snap_s, h->snap_ev[0], 0));
+  CK(cudaMemcpyAsync(qp_host, h->d_snap, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost,
+                     h->snap_s));
+  CK(cudaMemcpyAsync(h->h_snap_err, h->d_snap + n, sizeof(int), cudaMemcpyDeviceToHost,
+                     h->snap_s));
+  CK(cudaEventRecord(h->snap_ev[1], h->snap_s));
+  h->snap_busy = true;
+  return FEST_OK;
+}
+
+int fest_snapshot_wait(fest_handle* h) {
+  if (!h) return FEST_ERR_ARG;
+  if (!h->snap_busy) return FEST_OK;
+  h->snap_busy = false;
+  CK(cudaEventSynchronize(h->snap_ev[1]));
+  return *h->h_snap_err;
 }
 
 int fest_populate_ghost_primitive(fest_handle* h, double* qp, int current_iter) {

@@ -202,6 +202,8 @@ _SIGS = {
     "fest_set_wall_dist": [C.c_void_p, _DP],
     "fest_upload_state": [C.c_void_p, _DP],
     "fest_download_state": [C.c_void_p, _DP],
+    "fest_snapshot_begin": [C.c_void_p, _DP],
+    "fest_snapshot_wait": [C.c_void_p],
     "fest_populate_ghost_primitive": [C.c_void_p, _DP, C.c_int],
     "fest_compute_temperature": [C.c_void_p, _DP, _DP],
     "fest_compute_face_interpolant": [C.c_void_p, _DP, _DP, _DP, _DP, _DP, _DP, _DP],

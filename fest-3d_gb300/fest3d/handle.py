@@ -99,6 +99,67 @@ class Handle:
         self._call("fest_download_state", abi.ptr(q))
         return q
 
+    def snapshot_begin(self, q):
+        """Start copying the current state into q (padded shape, F-ordered
+        float64; pinned memory lets later steps overlap the copy) and return
+        at once (fest_snapshot_begin); q is complete when snapshot_wait
+        returns."""
+        if not (isinstance(q, np.ndarray) and q.dtype == np.float64 and q.flags.f_contiguous
+                and q.shape == tuple(self.shape["qp"])):
+            raise ValueError(f"q must be an F-ordered float64 array of shape {self.shape['qp']}")
+        self._call("fest_snapshot_begin", abi.ptr(q))
+        self._snap = q
+
+    def snapshot_wait(self):
+        """Wait for the snapshot begun last; FestError if the state it holds
+        comes from a failed step."""
+        try:
+            self._call("fest_snapshot_wait")
+        finally:
+            self._snap = None
+
+    def step_async(self, n, first_iter, CFL):
+        """Enqueue n iterations and return; errors surface at the next
+        synchronous call (last_device_error)."""
+        self._call("fest_step_async", int(n), int(first_iter), float(CFL))
+
+    def last_device_error(self):
+        self._call("fest_last_device_error")
+
+    def iterate(self, max_iters, CFL, checkpoint_iter, on_checkpoint, first_iter=1, q=None):
+        """Iterations first_iter..max_iters with the reference's checkpoint
+        schedule (dump_solution.f90:40-43: with checkpoint_iter != 0, every
+        checkpoint_iter-th iteration and the last one; none with 0):
+        on_checkpoint(iteration, qp) gets each of those states on the host
+        while the device steps on toward the next one.  q: the host buffer
+        the snapshots land in (pinned memory for the overlap; a new pageable
+        array if None).  on_checkpoint must be done with qp when it returns:
+        the next snapshot reuses it.  Returns the next iteration number."""
+        if checkpoint_iter < 0 or first_iter < 1:
+            raise ValueError("checkpoint_iter >= 0 and first_iter >= 1")
+        if q is None:
+            q = np.zeros(self.shape["qp"], order="F")
+        if checkpoint_iter == 0:
+            if max_iters >= first_iter:
+                self.step_async(max_iters - first_iter + 1, first_iter, CFL)
+            self.last_device_error()
+            return max(first_iter, max_iters + 1)
+        dumps = [it for it in range(first_iter, max_iters + 1)
+                 if it % checkpoint_iter == 0 or it == max_iters]
+        it, pending = first_iter, None
+        for d in dumps + [None]:
+            if d is not None:
+                self.step_async(d - it + 1, it, CFL)
+                it = d + 1
+            if pending is not None:
+                self.snapshot_wait()
+                on_checkpoint(pending, q)
+            if d is not None:
+                self.snapshot_begin(q)
+                pending = d
+        self.last_device_error()
+        return it
+
     def populate_ghost_primitive(self, qp, it):
         q = self._input(qp, "qp")
         self._call("fest_populate_ghost_primitive", abi.ptr(q), int(it))

@@ -174,6 +174,23 @@ int fest_set_wall_dist(fest_handle *h, const double *dist);
 /* ---- state ------------------------------------------------------------- */
 int fest_upload_state(fest_handle *h, const double *qp);
 int fest_download_state(fest_handle *h, double *qp);
+/* The state for a checkpoint (replaces the qp that solver.f90:186 hands to
+ * dump_solution.f90:27-52 checkpoint) while stepping goes on.
+ * fest_snapshot_begin enqueues a device copy of the current padded state
+ * after the work already on the handle's stream, and that copy's transfer
+ * into qp (the padded shape of fest_download_state) on a copy stream of the
+ * handle's own; it returns without waiting.  Steps enqueued afterwards
+ * (fest_step_async, fest_batch_step_async) run while the transfer travels,
+ * provided qp is pinned host memory (cudaHostAlloc / cudaMallocHost;
+ * pageable memory makes the call wait for the transfer).  qp must not be
+ * read before fest_snapshot_wait returns, which blocks until the transfer
+ * is complete and returns the device error word as it stood when the state
+ * was copied (FEST_OK, or the failed step's FEST_ERR_*; the word itself is
+ * left for fest_last_device_error).  One snapshot at a time: a second
+ * begin before the wait returns FEST_ERR_ARG; a wait with none pending
+ * returns FEST_OK. */
+int fest_snapshot_begin(fest_handle *h, double *qp);
+int fest_snapshot_wait(fest_handle *h);
 
 /* ---- module arrays held by the handle -----------------------------------
  * The reference keeps these as module variables (face_interpolant.f90:17-22,

@@ -53,6 +53,8 @@ def test_argument_validation_without_device(lib):
         rc = L.fest_create(C.byref(ext), C.byref(abi.make_flow()), C.byref(abi.make_scheme()),
                            C.byref(bc), C.byref(h))
         assert rc == abi.FEST_ERR_ARG, partners
+    assert L.fest_snapshot_begin(None, None) == abi.FEST_ERR_ARG
+    assert L.fest_snapshot_wait(None) == abi.FEST_ERR_ARG
     for fn in ("fest_destroy", "fest_find_resnorm", "fest_step"):
         assert getattr(L, fn)(None, *([None] if fn == "fest_find_resnorm" else
                                        [0, 0, 0.5, None] if fn == "fest_step" else [])) in (0, 1)
@@ -82,3 +84,54 @@ def test_handle_refuses_short_host_arrays():
         args[bad] = args[bad].ravel(order="F")[:-1]
         with pytest.raises(ValueError):
             h.set_metrics(*args)
+
+
+class _StreamStandIn:
+    """The calls Handle.iterate makes, on a state that is the number of
+    iterations done: work runs at once, which is the order the handle's
+    stream runs it in."""
+
+    def __init__(self, ext, first):
+        self.shape = {"qp": abi.shapes(ext)["qp"]}
+        self.done, self.log = first - 1, []
+
+    def step_async(self, n, first, CFL):
+        assert first == self.done + 1
+        self.done += n
+        self.log.append(("step", first, n))
+
+    def snapshot_begin(self, q):
+        q[...] = self.done
+        self.log.append(("begin", self.done))
+
+    def snapshot_wait(self):
+        self.log.append(("wait",))
+
+    def last_device_error(self):
+        self.log.append(("sync",))
+
+
+@pytest.mark.parametrize("max_iters,every,first", [(10, 3, 1), (9, 3, 1), (7, 0, 1), (12, 5, 4),
+                                                   (3, 10, 1)])
+def test_iterate_follows_the_reference_checkpoint_schedule(max_iters, every, first):
+    """Handle.iterate hands on_checkpoint the states of the iterations
+    dump_solution.f90:40-43 dumps (every checkpoint_iter-th and the last;
+    none when checkpoint_iter is 0), and enqueues the next iterations before
+    it waits for a snapshot."""
+    import numpy as np
+    from fest3d.handle import Handle
+    h = _StreamStandIn(abi.Extent(9, 7, 5, 5), first)
+    got = []
+    nxt = Handle.iterate(h, max_iters, 0.5, every, lambda it, q: got.append((it, float(q.flat[0]))),
+                         first_iter=first)
+    want = [] if every == 0 else [it for it in range(first, max_iters + 1)
+                                  if it % every == 0 or it == max_iters]
+    assert [it for it, _ in got] == want
+    assert all(v == it for it, v in got)  # each snapshot holds its own iteration's state
+    assert nxt == max_iters + 1 and h.done == max_iters and h.log[-1] == ("sync",)
+    # overlap: between a snapshot's begin and its wait, the next stretch of
+    # iterations is already enqueued
+    for a, b in zip(want, want[1:]):
+        i = h.log.index(("begin", a))
+        assert h.log[i + 1][0] == "step" and h.log[i + 2] == ("wait",)
+    assert np.all(np.isfinite([v for _, v in got]))

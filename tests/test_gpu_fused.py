@@ -314,3 +314,40 @@ def test_step_host_interior_equals_device_steps(gpu_lib, pinned):
         assert np.allclose(n1, n2, rtol=1e-13, atol=0)
     h1.close()
     h2.close()
+
+
+@pytest.mark.parametrize("precision", [abi.FEST_FP64, abi.FEST_MIXED], ids=["fp64", "mixed"])
+def test_checkpoint_snapshots_while_stepping(gpu_lib, precision):
+    """Handle.iterate with the reference's checkpoint schedule (every third
+    iteration and the last): each snapshot, copied into pinned memory while
+    the next iterations are already enqueued, is bit for bit the state that
+    synchronous steps and fest_download_state give at that iteration, and
+    stepping after the snapshots continues unchanged; one snapshot at a
+    time."""
+    import torch
+    case = cases.bump_case(nc=(64, 24, 4))
+    ext = case["ext"]
+    _, h1 = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    _, h2 = make_pair(ext, case["flow"], case["scheme"], case["bc"], case["nodes"], case["qp"])
+    for h in (h1, h2):
+        h.set_precision(precision)
+    buf = torch.empty(abi.shapes(ext)["qp"][::-1], dtype=torch.float64, pin_memory=True)
+    q = buf.numpy().T
+    got = []
+    nxt = h1.iterate(7, case["CFL"], 3, lambda it, qp: got.append((it, qp.copy(order="F"))), q=q)
+    assert nxt == 8 and [it for it, _ in got] == [3, 6, 7]
+    it = 1
+    for d, snap in got:
+        h2.step(d - it + 1, it, case["CFL"], with_norm=False)
+        it = d + 1
+        assert np.array_equal(snap, h2.download_state()), d
+    h1.step(2, 8, case["CFL"], with_norm=False)
+    h2.step(2, 8, case["CFL"], with_norm=False)
+    assert np.array_equal(h1.download_state(), h2.download_state())
+    h1.snapshot_begin(q)
+    with pytest.raises(abi.FestError):
+        h1.snapshot_begin(q)
+    h1.snapshot_wait()
+    assert np.array_equal(q, h2.download_state())
+    h1.close()
+    h2.close()
