@@ -337,23 +337,28 @@ int fest_batch_step_async(fest_batch *b, int n_iters, int first_iter, double CFL
  * state (ghost cells follow it through the BCs of the iteration), lambda in
  * the residue layout, dq in the qp layout (ghost entries zero).  qp
  * (nullable: the device state) is uploaded and its ghosts filled first.
- * FP64.  Inviscid and laminar blocks of the fused-path kind (n_var 5,
- * >= 4 interior cells per direction, no -9 face, no pressure switch,
- * adiabatic -5 walls; laminar: no interface ids >= 0), the laminar terms
- * with the temperature p/(rho R) of the state; FEST_ERR_ARG otherwise
- * (SST blocks). */
+ * FP64.  Inviscid, laminar and k-omega SST blocks of the fused-path kind
+ * (n_var 5, or 7 with SST; >= 4 interior cells per direction, no -9 face,
+ * no pressure switch, adiabatic -5 walls; viscous: no interface ids >= 0;
+ * SST: viscous, and no far-field (-8), total-pressure (-11) or interface
+ * faces, whose k and omega ghosts depend on the fill's last column), the
+ * viscous terms with the temperature p/(rho R) of the state; FEST_ERR_ARG
+ * otherwise. */
 int fest_residual_vjp(fest_handle *h, const double *qp, int current_iter,
                       const double *lambda, double *dq);
 /* No counterpart in the reference.  The same product with respect to the
  * grid nodes: dnodes = (dR/dnodes)^T lambda + (dfaces/dnodes)^T faces_bar,
  * through the face metrics of the fluxes and of the BCs (tangency normals,
- * Riemann normals), the face vectors and the ghost-node extrapolation
- * (grid.f90:137-236, geometry.f90).  dnodes in the nodes layout (interior
- * nodes carry the result, ghost nodes zero); lambda and the three
- * face-layout adjoints *_bar (an objective's explicit metric dependence)
- * are nullable; dq (nullable) receives fest_residual_vjp's result.  Same
- * restrictions as fest_residual_vjp, inviscid blocks only, and no WENO_NM
- * (volume weights). */
+ * Riemann normals), for laminar blocks also through the face records,
+ * volumes and centres that the Green-Gauss gradients, their BCs and the
+ * viscous fluxes read, then the face vectors, the cell volumes and centres
+ * and the ghost-node extrapolation (grid.f90:137-236, geometry.f90).
+ * dnodes in the nodes layout (interior nodes carry the result, ghost nodes
+ * zero); lambda and the three face-layout adjoints *_bar (an objective's
+ * explicit metric dependence) are nullable; dq (nullable) receives
+ * fest_residual_vjp's result.  Same restrictions as fest_residual_vjp,
+ * inviscid and laminar blocks only (SST wall distances depend on the nodes
+ * too), and no WENO_NM (volume weights). */
 int fest_residual_vjp_nodes(fest_handle *h, const double *qp, int current_iter,
                             const double *lambda, const double *Ifaces_bar,
                             const double *Jfaces_bar, const double *Kfaces_bar,
@@ -367,7 +372,10 @@ int fest_residual_vjp_nodes(fest_handle *h, const double *qp, int current_iter,
  * iteration does.  dJdq in the qp layout (interior entries used).
  * Stops after max_iters or when the RMS update has dropped by tol;
  * n_done, drop (nullable) report the iterations and that drop.  Then
- * dJ/dalpha = dJ/dalpha|_q + psi . dR/dalpha for any parameter alpha. */
+ * dJ/dalpha = dJ/dalpha|_q + psi . dR/dalpha for any parameter alpha.
+ * Inviscid and laminar blocks (n_var 5; the preconditioner P maps the five
+ * mean-flow variables): FEST_ERR_ARG for SST blocks, whose residual VJP
+ * fest_residual_vjp still gives. */
 int fest_adjoint_solve(fest_handle *h, const double *dJdq, double CFL,
                        int max_iters, double tol, double *psi, int *n_done,
                        double *drop);
