@@ -440,6 +440,46 @@ __device__ __forceinline__ void visc_flux_d(const Params& p, const D* x, const d
                ((Txz * uf + Tyz * vf + Tzz * wf + Qz) * nz));
 }
 
+// visc_flux_d's arithmetic as a function of the face's geometry instead:
+// g[0..3] the face record {A, nx, ny, nz}, g[4..6] and g[7..9] the left
+// and right cells' centres; x: the values of visc_flux_d's 21 inputs.
+template <typename D>
+__device__ __forceinline__ void visc_flux_geo_d(const Params& p, const double* x, const D* g, D* Fv) {
+  D G[3][4];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int l = 0; l < 4; ++l) G[c][l] = D(x[4 * c + l]);
+  const D delx = g[7] - g[4], dely = g[8] - g[5], delz = g[9] - g[6];
+  const D dLR = sqrt(delx * delx + dely * dely + delz * delz);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const D del = D(x[16 + l]) - D(x[12 + l]);
+    const D nc = (del - (G[0][l] * delx + G[1][l] * dely + G[2][l] * delz)) / dLR;
+    G[0][l] = G[0][l] + (nc * delx / dLR);
+    G[1][l] = G[1][l] + (nc * dely / dLR);
+    G[2][l] = G[2][l] + (nc * delz / dLR);
+  }
+  const D two(2.), three(3.), half(0.5);
+  const D tm(x[20]);
+  const D dudx = G[0][0], dudy = G[1][0], dudz = G[2][0];
+  const D dvdx = G[0][1], dvdy = G[1][1], dvdz = G[2][1];
+  const D dwdx = G[0][2], dwdy = G[1][2], dwdz = G[2][2];
+  const D Txx = two * tm * (dudx - ((dudx + dvdy + dwdz) / three));
+  const D Tyy = two * tm * (dvdy - ((dudx + dvdy + dwdz) / three));
+  const D Tzz = two * tm * (dwdz - ((dudx + dvdy + dwdz) / three));
+  const D Txy = tm * (dvdx + dudy), Txz = tm * (dwdx + dudz), Tyz = tm * (dwdy + dvdz);
+  const D Kh = (tm / D(p.Pr)) * D(p.gm) * D(p.R) / D(p.gm - 1);
+  const D Qx = Kh * G[0][3], Qy = Kh * G[1][3], Qz = Kh * G[2][3];
+  const D A = g[0], nx = g[1], ny = g[2], nz = g[3];
+  const D uf = half * (D(x[12]) + D(x[16])), vf = half * (D(x[13]) + D(x[17])), wf = half * (D(x[14]) + D(x[18]));
+  Fv[0] = (Txx * nx + Txy * ny + Txz * nz) * A;
+  Fv[1] = (Txy * nx + Tyy * ny + Tyz * nz) * A;
+  Fv[2] = (Txz * nx + Tyz * ny + Tzz * nz) * A;
+  Fv[3] = A * (((Txx * uf + Txy * vf + Txz * wf + Qx) * nx) + ((Txy * uf + Tyy * vf + Tyz * wf + Qy) * ny) +
+               ((Txz * uf + Tyz * vf + Tzz * wf + Qz) * nz));
+}
+
 // d mu / d T of calculate_viscosity (viscosity.f90:109-136; constant mu: 0)
 __device__ __forceinline__ double dmu_dT(const Params& p, double T) {
   if (p.mu_var != FEST_MU_SUTHERLAND) return 0.0;
@@ -467,8 +507,13 @@ __device__ __forceinline__ void give_uvwT(const Params& p, const DevBlock& b, do
 // minus sign).  Gradient adjoints go to barG (interior cells, 12 per cell
 // as [component][variable]); a ghost cell's gradient is its face's
 // gradient BC (gradients.f90:486-676) of the interior cell, transposed here.
+// With bar_face and bar_cells (metric adjoints, nullable) it also adds the
+// flux's derivatives with respect to the face record and the two cells'
+// centres, and those of a ghost gradient's BC with respect to the boundary
+// face record and the interior cell's volume.
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_viscous(Params p, DevBlock b, const double* lam, double* bar,
-                                                         double* barG, int dir) {
+                                                         double* barG, int dir, double* bar_face,
+                                                         double* bar_cells) {
   using D = Dual<double, 21>;
   const Dims& d = p.d;
   const int n = extent_of(d, dir);
@@ -519,6 +564,38 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_viscous(Params p, DevBlock b, c
     for (int l = 0; l < 4; ++l) s -= mu[l] * Fv[l].d[m];
     bx[m] = s;
   }
+  if (bar_face) {
+    // the same flux as a function of the face record and the cell centres
+    using DG = Dual<double, 10>;
+    double xv[21];
+#pragma unroll
+    for (int m = 0; m < 21; ++m) xv[m] = x[m].v;
+    const double* fc0 = b.faces[dir] + 4 * fi;
+    const double* CL = b.cells + 4 * cL + 1;
+    const double* CR = b.cells + 4 * cR + 1;
+    DG g[10], Fg[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) g[m] = DG::var(fc0[m], m);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      g[4 + m] = DG::var(CL[m], 4 + m);
+      g[7 + m] = DG::var(CR[m], 7 + m);
+    }
+    visc_flux_geo_d<DG>(p, xv, g, Fg);
+    double bg[10];
+#pragma unroll
+    for (int m = 0; m < 10; ++m) {
+      double s = 0.0;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) s -= mu[l] * Fg[l].d[m];
+      bg[m] = s;
+    }
+    for (int m = 0; m < 4; ++m) atomicAdd(bar_face + 4 * fi + m, bg[m]);
+    for (int m = 0; m < 3; ++m) {
+      atomicAdd(bar_cells + 4 * cL + 1 + m, bg[4 + m]);
+      atomicAdd(bar_cells + 4 * cR + 1 + m, bg[7 + m]);
+    }
+  }
   // cell values and the face viscosity
   double gLv[4] = {bx[12], bx[13], bx[14], bx[15]}, gRv[4] = {bx[16], bx[17], bx[18], bx[19]};
   gLv[3] += 0.5 * bx[20] * dmu_dT(p, TL);
@@ -561,6 +638,36 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_viscous(Params p, DevBlock b, c
       jI[3] = 0.0;
       jG[3] = 0.0;
     }
+    if (bar_face) {
+      // G_ghost(l) = sig (phi_I - phi_G) A n / V_I + G_I - n (G_I . n), the
+      // T row of an adiabatic wall -n (G_I . n) (gradients.f90:486-676):
+      // derivatives with respect to A, n and V_I
+      const long long gIc = side == 0 ? gR : gL;
+      const long long cG = side == 0 ? cL : cR;
+      const double A = fc[0];
+      const double TI = b.qp[cI + 4 * P] / (b.qp[cI] * p.R), TG = b.qp[cG + 4 * P] / (b.qp[cG] * p.R);
+      double bA = 0.0, bn[3] = {0.0, 0.0, 0.0}, bV = 0.0;
+      for (int l = 0; l < 4; ++l) {
+        double GI[3], gb[3];
+        for (int q = 0; q < 3; ++q) {
+          GI[q] = b.grad[q][gIc + NG * l];
+          gb[q] = gG[side][4 * q + l];
+        }
+        const double GIn = GI[0] * nn[0] + GI[1] * nn[1] + GI[2] * nn[2];
+        const double gbn = gb[0] * nn[0] + gb[1] * nn[1] + gb[2] * nn[2];
+        for (int q = 0; q < 3; ++q) bn[q] -= gb[q] * GIn + gbn * GI[q];
+        if (adiab && l == 3) continue;
+        const double diff = l == 3 ? TI - TG : b.qp[cI + P * (l + 1)] - b.qp[cG + P * (l + 1)];
+        const double sd = sig * diff / vI;
+        bA += sd * gbn;
+        for (int q = 0; q < 3; ++q) bn[q] += sd * A * gb[q];
+        bV -= sd * A * gbn / vI;
+      }
+      double* bfc = bar_face + 4 * fi;
+      atomicAdd(bfc, bA);
+      for (int q = 0; q < 3; ++q) atomicAdd(bfc + 1 + q, bn[q]);
+      atomicAdd(bar_cells + 4 * cI, bV);
+    }
     const int ci = side == 0 ? (int)cidx(d, ir, jr, kr) : (int)cidx(d, il, jl, kl);
     for (int m = 0; m < 12; ++m)
       if (gI[m] != 0.0) atomicAdd(barG + (long long)ci * 12 + m, gI[m]);
@@ -577,7 +684,11 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_viscous(Params p, DevBlock b, c
 // one thread per interior cell: its gradient adjoint through the
 // Green-Gauss sum (gradients.f90:405-482) onto u, v, w, T of the cell and
 // its six neighbours
-__global__ void __launch_bounds__(TPB_ADJ) k_vjp_grad(Params p, DevBlock b, const double* barG, double* bar) {
+// With bar_faces and bar_cells (nullable) it also adds the sum's
+// derivatives with respect to the six face records and the cell's volume.
+__global__ void __launch_bounds__(TPB_ADJ) k_vjp_grad(Params p, DevBlock b, const double* barG, double* bar,
+                                                      double* bf0, double* bf1, double* bf2,
+                                                      double* bar_cells) {
   const Dims& d = p.d;
   const long long N = ncells(d);
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -611,6 +722,35 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_grad(Params p, DevBlock b, cons
     give_uvwT(p, b, bar, nbc[f], gn);
   }
   give_uvwT(p, b, bar, c0, own);
+  if (!bf0) return;
+  // grad(q, l) = sum_f sg (phi_nb + phi_c)(l) n_q A / (2 V): face records and V
+  auto phi = [&](long long c, int l) {
+    return l == 3 ? b.qp[c + 4 * d.P] / (b.qp[c] * p.R) : b.qp[c + d.P * (l + 1)];
+  };
+  double* bfs[3] = {bf0, bf1, bf2};
+  const long long fix[6] = {fidx(d, 0, i, j, k), fidx(d, 1, i, j, k), fidx(d, 2, i, j, k),
+                            fidx(d, 0, i + 1, j, k), fidx(d, 1, i, j + 1, k), fidx(d, 2, i, j, k + 1)};
+  double pc[4];
+  for (int l = 0; l < 4; ++l) pc[l] = phi(c0, l);
+  for (int f = 0; f < 6; ++f) {
+    const double sg = f < 3 ? -1.0 : 1.0;
+    double bA = 0.0, bn[3] = {0.0, 0.0, 0.0};
+    for (int l = 0; l < 4; ++l) {
+      const double w = sg * (phi(nbc[f], l) + pc[l]) / vol2;
+      for (int q = 0; q < ncomp; ++q) {
+        bA += g[4 * q + l] * w * fr[f][1 + q];
+        bn[q] += g[4 * q + l] * w * fr[f][0];
+      }
+    }
+    double* o = bfs[f % 3] + 4 * fix[f];
+    atomicAdd(o, bA);
+    for (int q = 0; q < ncomp; ++q) atomicAdd(o + 1 + q, bn[q]);
+  }
+  const long long og = gidx(d, i, j, k), NG = ngrad(d);
+  double bV = 0.0;
+  for (int l = 0; l < 4; ++l)
+    for (int q = 0; q < ncomp; ++q) bV -= g[4 * q + l] * b.grad[q][og + NG * l];
+  atomicAdd(bar_cells + 4 * c0, bV / b.cells[4 * c0]);
 }
 
 // ghost (layer L) / interior (layer m) cell of face f at (ta, tb)
@@ -1344,7 +1484,7 @@ long long vjp_face_work_doubles(const Dims& d) {
 
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
                          double* bar, const Launcher& L, double* const* bar_faces, double* bar_grad,
-                         double* face_work) {
+                         double* face_work, double* bar_cells) {
   const Dims& d = p.d;
   const bool visc = p.mu_ref != 0.0, sst = p.turb != FEST_TURB_NONE;
   cudaMemsetAsync(bar, 0, sizeof(double) * (size_t)d.P * d.nv, L.s);
@@ -1385,7 +1525,8 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
       k_vjp_viscous_sst<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, barG, barMut, barF1, dir);
       ++*L.count;
     } else if (visc) {
-      k_vjp_viscous<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bar_grad, dir);
+      k_vjp_viscous<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, bar, bar_grad, dir,
+                                                       bar_cells ? bf : nullptr, bar_cells);
       ++*L.count;
     }
   }
@@ -1403,7 +1544,10 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
     k_vjp_grad_sst<<<nblocks(ncells(d)), TPB_ADJ, 0, L.s>>>(p, b, barG, bar);
     *L.count += 4;
   } else if (visc) {
-    k_vjp_grad<<<nblocks(ncells(d)), TPB_ADJ, 0, L.s>>>(p, b, bar_grad, bar);
+    const bool geo = bar_cells && bar_faces;
+    k_vjp_grad<<<nblocks(ncells(d)), TPB_ADJ, 0, L.s>>>(p, b, bar_grad, bar, geo ? bar_faces[0] : nullptr,
+                                                        geo ? bar_faces[1] : nullptr,
+                                                        geo ? bar_faces[2] : nullptr, bar_cells);
     ++*L.count;
   }
   long long wmax = 0;
@@ -1461,6 +1605,77 @@ __global__ void k_vjp_face_vectors(Dims d, const double* nd, const double* faces
   }
 }
 
+// transpose of the cell records {volume, cx, cy, cz} (geometry.f90, as
+// k_cells): the centre is the mean of the eight nodes; the volume, for the
+// cells of the range 0..imx, 0..jmx, 0..kmx, the larger of two sums of five
+// tetrahedra, each -(a x b).c/6 with a, b, c its edges from its first
+// node, whose derivatives are -(b x c)/6, -(c x a)/6, -(a x b)/6 for the
+// other three nodes and minus their sum for the first
+__device__ __forceinline__ void tet_vol_grad(const double* p1, const double* p2, const double* p3,
+                                             const double* p4, double bv, double* g1, double* g2,
+                                             double* g3, double* g4) {
+  double a[3], b[3], c[3];
+  for (int m = 0; m < 3; ++m) {
+    a[m] = p2[m] - p1[m];
+    b[m] = p3[m] - p1[m];
+    c[m] = p4[m] - p1[m];
+  }
+  const double s = -bv / 6.0;
+  const double ga[3] = {s * (b[1] * c[2] - b[2] * c[1]), s * (b[2] * c[0] - b[0] * c[2]),
+                        s * (b[0] * c[1] - b[1] * c[0])};
+  const double gb[3] = {s * (c[1] * a[2] - c[2] * a[1]), s * (c[2] * a[0] - c[0] * a[2]),
+                        s * (c[0] * a[1] - c[1] * a[0])};
+  const double gc[3] = {s * (a[1] * b[2] - a[2] * b[1]), s * (a[2] * b[0] - a[0] * b[2]),
+                        s * (a[0] * b[1] - a[1] * b[0])};
+  for (int m = 0; m < 3; ++m) {
+    g2[m] += ga[m];
+    g3[m] += gb[m];
+    g4[m] += gc[m];
+    g1[m] -= ga[m] + gb[m] + gc[m];
+  }
+}
+__device__ __forceinline__ double tet_vol(const double* p1, const double* p2, const double* p3,
+                                          const double* p4) {
+  const double v = (p4[0] - p1[0]) * ((p2[1] - p1[1]) * (p3[2] - p1[2]) - (p2[2] - p1[2]) * (p3[1] - p1[1])) +
+                   (p4[1] - p1[1]) * ((p2[2] - p1[2]) * (p3[0] - p1[0]) - (p2[0] - p1[0]) * (p3[2] - p1[2])) +
+                   (p4[2] - p1[2]) * ((p2[0] - p1[0]) * (p3[1] - p1[1]) - (p2[1] - p1[1]) * (p3[0] - p1[0]));
+  return -v / 6.;
+}
+__global__ void k_vjp_cells(Dims d, const double* nd, const double* bar_cells, double* bar_nodes) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.P) return;
+  const int i = -2 + (int)(t % d.ni);
+  const long long r = t / d.ni;
+  const int j = -2 + (int)(r % d.nj), k = -2 + (int)(r / d.nj);
+  const double* bc = bar_cells + 4 * pidx(d, i, j, k);
+  if (bc[0] == 0.0 && bc[1] == 0.0 && bc[2] == 0.0 && bc[3] == 0.0) return;
+  const long long ni[8] = {node_i(d, i, j, k),         node_i(d, i + 1, j, k),
+                           node_i(d, i + 1, j + 1, k), node_i(d, i, j + 1, k),
+                           node_i(d, i, j, k + 1),     node_i(d, i + 1, j, k + 1),
+                           node_i(d, i + 1, j + 1, k + 1), node_i(d, i, j + 1, k + 1)};
+  double g[8][3];
+  for (int n = 0; n < 8; ++n)
+    for (int m = 0; m < 3; ++m) g[n][m] = 0.125 * bc[1 + m];
+  if (bc[0] != 0.0 && i >= 0 && i <= d.imx && j >= 0 && j <= d.jmx && k >= 0 && k <= d.kmx) {
+    const double* P[8];
+    for (int n = 0; n < 8; ++n) P[n] = nd + ni[n];
+    // the two five-tetrahedron sums of k_cells, in its order
+    const int T1[5][4] = {{0, 4, 7, 5}, {6, 7, 5, 2}, {7, 3, 0, 2}, {5, 0, 2, 7}, {0, 1, 5, 2}};
+    const int T2[5][4] = {{1, 5, 4, 6}, {7, 4, 6, 3}, {4, 0, 1, 3}, {6, 1, 3, 4}, {1, 2, 6, 3}};
+    double v1 = 0., v = 0.;
+    for (int m = 0; m < 5; ++m) v1 = v1 + tet_vol(P[T1[m][0]], P[T1[m][1]], P[T1[m][2]], P[T1[m][3]]);
+    for (int m = 0; m < 5; ++m) v = v + tet_vol(P[T2[m][0]], P[T2[m][1]], P[T2[m][2]], P[T2[m][3]]);
+    // vol = fmax2(v, v1) = (v > v1 ? v : v1): the derivative of the sum it took
+    const int(*T)[4] = v > v1 ? T2 : T1;
+    for (int m = 0; m < 5; ++m)
+      tet_vol_grad(P[T[m][0]], P[T[m][1]], P[T[m][2]], P[T[m][3]], bc[0], g[T[m][0]], g[T[m][1]],
+                   g[T[m][2]], g[T[m][3]]);
+  }
+  for (int n = 0; n < 8; ++n)
+    for (int m = 0; m < 3; ++m)
+      if (g[n][m] != 0.0) atomicAdd(bar_nodes + ni[n] + m, g[n][m]);
+}
+
 // transpose of the ghost-node extrapolation of direction dir (grid.f90,
 // as k_ghost_nodes): its statements in reverse order
 __global__ void k_vjp_ghost_nodes(Dims d, double* bn, int dir) {
@@ -1492,12 +1707,16 @@ __global__ void k_vjp_ghost_nodes(Dims d, double* bn, int dir) {
 }  // namespace
 
 void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_faces, double* bar_nodes,
-                         const Launcher& L) {
+                         const Launcher& L, const double* bar_cells) {
   const Dims& d = p.d;
   cudaMemsetAsync(bar_nodes, 0, sizeof(double) * 3 * (size_t)(d.imx + 6) * (d.jmx + 6) * (d.kmx + 6), L.s);
   for (int dir = 0; dir < 3; ++dir) {
     const long long nf = (long long)(d.imx + 5 + (dir == 0)) * (d.jmx + 5 + (dir == 1)) * (d.kmx + 5 + (dir == 2));
     k_vjp_face_vectors<<<nblocks(nf), TPB_ADJ, 0, L.s>>>(d, b.nodes, b.faces[dir], bar_faces[dir], bar_nodes, dir);
+    ++*L.count;
+  }
+  if (bar_cells) {
+    k_vjp_cells<<<nblocks(d.P), TPB_ADJ, 0, L.s>>>(d, b.nodes, bar_cells, bar_nodes);
     ++*L.count;
   }
   for (int dir = 2; dir >= 0; --dir) {

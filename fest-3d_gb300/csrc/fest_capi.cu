@@ -871,18 +871,25 @@ int fest_residual_vjp_nodes(fest_handle* h, const double* qp, int current_iter, 
                             const double* Ifaces_bar, const double* Jfaces_bar,
                             const double* Kfaces_bar, double* dq, double* dnodes) {
   if (!h || !dnodes || needs_batch(h)) return FEST_ERR_ARG;
-  // metric adjoints of the inviscid residual only
-  if (!vjp_supported(h->p) || h->p.interp == FEST_INTERP_WENO_NM || h->p.mu_ref != 0.0) return FEST_ERR_ARG;
+  // metric adjoints of inviscid and laminar residuals (SST: the wall
+  // distances depend on the nodes too)
+  if (!vjp_supported(h->p) || h->p.interp == FEST_INTERP_WENO_NM || h->p.turb != FEST_TURB_NONE)
+    return FEST_ERR_ARG;
+  const bool visc = h->p.mu_ref != 0.0;
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);
   if (!h->d_vjp_bar) RET(dalloc(h, &h->d_vjp_bar, z.qp));
   if (!h->d_vjp_lam) RET(dalloc(h, &h->d_vjp_lam, z.res));
   if (!h->d_vjp_face) RET(dalloc(h, &h->d_vjp_face, vjp_face_work_doubles(h->p.d)));
+  // the handle keeps the gradient work array (viscous_prep would allocate
+  // it among this call's own temporaries otherwise)
+  if (visc && !h->d_vjp_grad) RET(dalloc(h, &h->d_vjp_grad, vjp_grad_work_doubles(h->p.d, false)));
   const size_t n0 = h->allocs.size();
-  double *bf[3] = {nullptr, nullptr, nullptr}, *bn = nullptr;
+  double *bf[3] = {nullptr, nullptr, nullptr}, *bn = nullptr, *bc = nullptr;
   int rc = FEST_OK;
   for (int dir = 0; dir < 3 && !rc; ++dir) rc = dalloc(h, &bf[dir], z.faces[dir]);
   if (!rc) rc = dalloc(h, &bn, z.nodes);
+  if (!rc && visc) rc = dalloc(h, &bc, z.cells);
   const double* fin[3] = {Ifaces_bar, Jfaces_bar, Kfaces_bar};
   for (int dir = 0; dir < 3 && !rc; ++dir)
     if (fin[dir]) rc = up(h, bf[dir], fin[dir], z.faces[dir]);
@@ -891,9 +898,12 @@ int fest_residual_vjp_nodes(fest_handle* h, const double* qp, int current_iter, 
   else if (!rc) rc = cuda_status(cudaMemsetAsync(h->d_vjp_lam, 0, sizeof(double) * z.res, h->s));
   if (!rc) {
     launch_ghosts(h->p, h->d, h->d_table, current_iter, h->L());
-    launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), bf, nullptr,
-                        h->d_vjp_face);
-    launch_geometry_vjp(h->p, h->d, bf, bn, h->L());
+    rc = viscous_prep(h);
+  }
+  if (!rc) {
+    launch_residual_vjp(h->p, h->d, current_iter, h->d_vjp_lam, h->d_vjp_bar, h->L(), bf, h->d_vjp_grad,
+                        h->d_vjp_face, bc);
+    launch_geometry_vjp(h->p, h->d, bf, bn, h->L(), bc);
     rc = down(h, dnodes, bn, z.nodes);
   }
   if (!rc && dq) rc = down(h, dq, h->d_vjp_bar, z.qp);

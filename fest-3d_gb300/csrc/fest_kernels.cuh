@@ -75,21 +75,25 @@ void launch_wall_dist(const Params& p, const DevBlock& b, const double* d_wall, 
 // viscosity of the state computed (launch_viscous_prep)
 bool vjp_supported(const Params& p);
 // bar_faces (null, or three face-layout arrays, zeroed by the caller) also
-// receive (dR/dfaces)^T lam (inviscid blocks); bar_grad: 12 doubles per
-// interior cell of work space for laminar blocks
+// receive (dR/dfaces)^T lam; bar_grad: 12 doubles per interior cell of work
+// space for laminar blocks
 // face_work: vjp_face_work_doubles(d) doubles of work space (the flux
 // transposes of one direction's faces)
+// bar_cells (laminar blocks with bar_faces: 4 doubles per padded cell,
+// zeroed by the caller) receives (dR/dcells)^T lam, the cell volumes' and
+// centres' share of the viscous terms
 void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const double* lam,
                          double* bar, const Launcher& L, double* const* bar_faces, double* bar_grad,
-                         double* face_work);
+                         double* face_work, double* bar_cells = nullptr);
 long long vjp_face_work_doubles(const Dims& d);
 // the bar_grad work space: 12 doubles per interior cell (laminar), or the
 // SST's gradient, eddy-viscosity and F1 adjoints
 long long vjp_grad_work_doubles(const Dims& d, bool sst);
-// nodes-layout bar_nodes = (dfaces/dnodes)^T bar_faces, through the face
-// vectors and the ghost-node extrapolation (interior nodes carry the result)
+// nodes-layout bar_nodes = (dfaces/dnodes)^T bar_faces + (dcells/dnodes)^T
+// bar_cells (nullable), through the face vectors, the cell volumes and
+// centres, and the ghost-node extrapolation (interior nodes carry the result)
 void launch_geometry_vjp(const Params& p, const DevBlock& b, double* const* bar_faces, double* bar_nodes,
-                         const Launcher& L);
+                         const Launcher& L, const double* bar_cells = nullptr);
 // work arrays of the fixed-point adjoint: phi, dJ, a, b, c, bar in the qp
 // layout, mu in the residue layout, sq one double
 struct AdjointWork {

@@ -208,8 +208,8 @@ def test_sst_vjp_matches_oracle_finite_differences(gpu_lib, name):
 
 
 def test_vjp_rejects_unsupported_blocks(gpu_lib):
-    """SST blocks with far-field faces have no residual VJP; laminar blocks
-    no metric VJP."""
+    """SST blocks with far-field faces have no residual VJP; SST blocks no
+    metric VJP."""
     ext, flow, scheme, bc, nodes, qp = small_case(
         nc=(12, 9, 7), ids=(-8, -4, -5, -6, -10, -10), turb=True,
         flow_kw=dict(mu_ref=1e-2, mu_variation="constant"))
@@ -219,7 +219,7 @@ def test_vjp_rejects_unsupported_blocks(gpu_lib):
         h.residual_vjp(qp, IT, lam)
     assert e.value.code == abi.FEST_ERR_ARG
     ext, flow, scheme, bc, nodes, qp = small_case(
-        nc=(12, 9, 7), ids=(-3, -4, -5, -6, -10, -10),
+        nc=(12, 9, 7), ids=(-3, -4, -5, -6, -10, -10), turb=True,
         flow_kw=dict(mu_ref=1e-2, mu_variation="constant"))
     blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
     lam = np.zeros((ext.imx - 1, ext.jmx - 1, ext.kmx - 1, ext.n_var), order="F")
@@ -279,6 +279,14 @@ NODE_CASES = {
                                                  klimiter_switch=0),
                                   ids=(-3, -4, -5, -6, -10, -10)),
     "none-vanleer": CASES["none-vanleer"],
+    # laminar: face records, volumes and centres in the Green-Gauss
+    # gradients, their wall and outlet BCs and the viscous fluxes
+    "lam-muscl-ausm-walls-nolim": dict(scheme_kw=dict(interpolant="muscl", scheme_name="ausm",
+                                                      ilimiter_switch=0, jlimiter_switch=0,
+                                                      klimiter_switch=0),
+                                       ids=(-3, -4, -5, -6, -10, -10),
+                                       flow_kw=dict(mu_ref=1.0, mu_variation="constant")),
+    "suth-none-vanleer-farfield": VISC_CASES["suth-none-vanleer-farfield"],
 }
 
 
@@ -286,7 +294,8 @@ NODE_CASES = {
 def test_node_vjp_matches_oracle_finite_differences(gpu_lib, name):
     """(dR/dnodes)^T lambda + (dfaces/dnodes)^T w against central
     differences of the oracle (geometry rebuilt from perturbed interior
-    nodes, residual at fixed state) for random lambda and face weights w."""
+    nodes, residual at fixed state) for random lambda and face weights w;
+    laminar blocks with the temperature of the state, as the state VJP."""
     ext, flow, scheme, bc, nodes, qp = small_case(nc=(12, 9, 7), **NODE_CASES[name])
     blk, h = make_pair(ext, flow, scheme, bc, nodes, qp)
     rng = np.random.default_rng(5)
@@ -302,6 +311,9 @@ def test_node_vjp_matches_oracle_finite_differences(gpu_lib, name):
         blk.setup_geometry()
         blk["qp"] = qp
         assert O.get_total_conservative_residue([blk], IT) == 0
+        if flow.mu_ref != 0.0:
+            blk.compute_temperature()
+            assert O.get_total_conservative_residue([blk], IT) == 0
         return float(np.sum(lam * blk["residue"])) + sum(
             float(np.sum(wf * blk[nm])) for wf, nm in zip(w, ("Ifaces", "Jfaces", "Kfaces")))
 
