@@ -661,11 +661,12 @@ int fest_download_state(fest_handle* h, double* qp) {
 int fest_snapshot_begin(fest_handle* h, double* qp_host) {
   if (!h || !qp_host || h->snap_busy) return FEST_ERR_ARG;
   const long long n = h->p.d.P * h->p.d.nv;
-  if (!h->snap_s) {
-    CK(cudaStreamCreateWithFlags(&h->snap_s, cudaStreamNonBlocking));
-    for (cudaEvent_t& e : h->snap_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    CK(cudaMallocHost((void**)&h->h_snap_err, sizeof(int)));
-  }
+  // the copy stream, its events and the pinned error word, made once (a
+  // part that failed is made again at the next call)
+  if (!h->snap_s) CK(cudaStreamCreateWithFlags(&h->snap_s, cudaStreamNonBlocking));
+  for (cudaEvent_t& e : h->snap_ev)
+    if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  if (!h->h_snap_err) CK(cudaMallocHost((void**)&h->h_snap_err, sizeof(int)));
   if (!h->d_snap) RET(dalloc(h, &h->d_snap, n + 1));
   const double* cur = fused_current_state(h->fused);
   CK(cudaMemcpyAsync(h->d_snap, cur ? cur : h->d.qp, sizeof(double) * (size_t)n,
