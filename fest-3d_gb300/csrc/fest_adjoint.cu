@@ -228,31 +228,45 @@ __device__ __forceinline__ void face_of(const Dims& d, int dir, long long t, int
   tb = 1 + (int)(r / na);
 }
 
-// one thread per (face, variable): the face's two states of that variable
-// (cell c-1's high side, cell c's low side), the reconstruction in plain
-// arithmetic, stored as w[l * nf + t] and w[(NV + l) * nf + t]
+// the cells 0..n of the line (ta, tb) along dir, whose reconstructions
+// give the states of faces 1..n: cell c's low side is face c's right
+// state, its high side face c+1's left state.  Face c of the line is entry
+// (c - 1) + n r of a face array (face_of), r = (ta - 1) + na (tb - 1).
+__device__ __forceinline__ void cell_line_of(const Dims& d, int dir, long long t, int& c, long long& r,
+                                             int& ta, int& tb) {
+  const int n = extent_of(d, dir);
+  const int na = (dir == 0 ? d.jmx : d.imx) - 1;
+  c = (int)(t % (n + 1));
+  r = t / (n + 1);
+  ta = 1 + (int)(r % na);
+  tb = 1 + (int)(r / na);
+}
+
+// one thread per (cell, variable) of cells 0..n: the cell's reconstruction
+// of that variable in plain arithmetic, its low side stored as face c's
+// right state w[(NV + l) nf + f] and its high side as face c+1's left state
+// w[l nf + f]
 template <typename T, int NV>
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_states(Params p, DevBlock b, double* w, int dir) {
   const Dims& d = p.d;
   const int n = extent_of(d, dir);
   const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
-  const long long nf = (long long)n * na * nb;
+  const long long nf = (long long)n * na * nb, ncl = (long long)(n + 1) * na * nb;
   const long long tl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (tl >= NV * nf) return;
-  const int l = (int)(tl / nf);
-  const long long t = tl - l * nf;
+  if (tl >= NV * ncl) return;
+  const int l = (int)(tl / ncl);
   int c, ta, tb, i, j, k;
-  face_of(d, dir, t, c, ta, tb);
+  long long r;
+  cell_line_of(d, dir, tl - l * ncl, c, r, ta, tb);
   cell_of(dir, 0, ta, tb, i, j, k);
   const long long P = d.P, st = pstride(d, dir), c0 = pidx(d, i, j, k);
   VolVal<T> vol{b.cells + 4 * c0, st, n};
   ValLine<T> pres{b.qp + c0 + P * 4, st};
   ValLine<T> q{b.qp + c0 + P * l, st};
   T Rm, Lp;
-  recon_cell<T>(p, dir, c - 1, l + 1, q, pres, vol, Rm, Lp);
-  w[l * nf + t] = (double)Lp;
   recon_cell<T>(p, dir, c, l + 1, q, pres, vol, Rm, Lp);
-  w[(NV + l) * nf + t] = (double)Rm;
+  if (c >= 1) w[(NV + l) * nf + (c - 1) + n * r] = (double)Rm;
+  if (c <= n - 1) w[l * nf + c + n * r] = (double)Lp;
 }
 
 // one thread per face of direction dir: mu = lambda(left) - lambda(right)
@@ -352,13 +366,13 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_flux(Params p, DevBlock b, cons
   }
 }
 
-// one thread per (face, variable): the variable's two face states (cell
-// c-1's high side, cell c's low side) differentiated with respect to their
-// W-cell stencils (W = 5 for PPM and the WENOs, 3 for MUSCL and first
-// order, which read no further, boundary overrides included) by forward
-// duals, times the flux transpose of k_vjp_flux; qL reaches cells
-// c-1-W/2..c-1+W/2, qR c-W/2..c+W/2, and the W+1 targets are summed in
-// registers before one atomic add each
+// one thread per (cell, variable) of cells 0..n: the cell's two face
+// states of that variable (its low side, face c's right state; its high
+// side, face c+1's left state) differentiated with respect to its W-cell
+// stencil (W = 5 for PPM and the WENOs, 3 for MUSCL and first order, which
+// read no further, boundary overrides included) by forward duals, times
+// the flux transposes of k_vjp_flux; the W targets c-W/2..c+W/2 are summed
+// in registers before one atomic add each
 template <typename T, int NV, int W>
 __global__ void __launch_bounds__(TPB_ADJ) k_vjp_recon(Params p, DevBlock b, const double* bxi, double* bar,
                                                        int dir) {
@@ -366,33 +380,28 @@ __global__ void __launch_bounds__(TPB_ADJ) k_vjp_recon(Params p, DevBlock b, con
   const Dims& d = p.d;
   const int n = extent_of(d, dir);
   const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
-  const long long nf = (long long)n * na * nb;
-  const long long t5 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t5 >= NV * nf) return;
-  const int l = (int)(t5 / nf);
-  const long long t = t5 - l * nf;
-  const T bl = (T)bxi[l * nf + t], br = (T)bxi[(NV + l) * nf + t];
-  if (bl == T(0) && br == T(0)) return;
+  const long long nf = (long long)n * na * nb, ncl = (long long)(n + 1) * na * nb;
+  const long long tl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tl >= NV * ncl) return;
+  const int l = (int)(tl / ncl);
   int c, ta, tb, i, j, k;
-  face_of(d, dir, t, c, ta, tb);
+  long long r;
+  cell_line_of(d, dir, tl - l * ncl, c, r, ta, tb);
+  const T br = c >= 1 ? (T)bxi[(NV + l) * nf + (c - 1) + n * r] : T(0);
+  const T bl = c <= n - 1 ? (T)bxi[l * nf + c + n * r] : T(0);
+  if (bl == T(0) && br == T(0)) return;
   cell_of(dir, 0, ta, tb, i, j, k);
   const long long P = d.P, st = pstride(d, dir), c0 = pidx(d, i, j, k);
   VolConst<T, W> vol{b.cells + 4 * c0, st, n};
   ConstLine<T, W> pres{b.qp + c0 + P * 4, st};
-  T acc[W + 1];
   D5 Rm, Lp;
-  DualLine<T, W> qa{b.qp + c0 + P * l, st, c - 1};
-  recon_cell<D5>(p, dir, c - 1, l + 1, qa, pres, vol, Rm, Lp);
+  DualLine<T, W> qa{b.qp + c0 + P * l, st, c};
+  recon_cell<D5>(p, dir, c, l + 1, qa, pres, vol, Rm, Lp);
 #pragma unroll
-  for (int s = 0; s < W; ++s) acc[s] = bl * Lp.d[s];
-  acc[W] = T(0);
-  DualLine<T, W> qb{b.qp + c0 + P * l, st, c};
-  recon_cell<D5>(p, dir, c, l + 1, qb, pres, vol, Rm, Lp);
-#pragma unroll
-  for (int s = 0; s < W; ++s) acc[s + 1] += br * Rm.d[s];
-#pragma unroll
-  for (int s = 0; s <= W; ++s)
-    if (acc[s] != T(0)) atomicAdd(bar + c0 + (c - 1 - W / 2 + s) * st + P * l, (double)acc[s]);
+  for (int s = 0; s < W; ++s) {
+    const T a = br * Rm.d[s] + bl * Lp.d[s];
+    if (a != T(0)) atomicAdd(bar + c0 + (c - W / 2 + s) * st + P * l, (double)a);
+  }
 }
 
 // ---- laminar viscous terms (gradients.f90, viscosity.f90, viscous.f90) -----
@@ -1498,27 +1507,29 @@ void launch_residual_vjp(const Params& p, const DevBlock& b, int iter, const dou
   for (int dir = 0; dir < 3; ++dir) {
     const int n = extent_of(d, dir);
     const long long nf = (long long)n * ((dir == 0 ? d.jmx : d.imx) - 1) * ((dir == 2 ? d.jmx : d.kmx) - 1);
+    // cells 0..n of every line: the per-(cell, variable) kernels
+    const long long ncl = nf / n * (n + 1);
     double* bf = bar_faces ? bar_faces[dir] : nullptr;
     if (d.nv == 7) {
-      k_vjp_states<double, 7><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, dir);
+      k_vjp_states<double, 7><<<nblocks(7 * ncl), TPB_ADJ, 0, L.s>>>(p, b, face_work, dir);
       if (p.flux == FEST_FLUX_SLAU)
         k_vjp_flux<double, true, 7><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
       else
         k_vjp_flux<double, false, 7><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
       if (narrow)
-        k_vjp_recon<double, 7, 3><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+        k_vjp_recon<double, 7, 3><<<nblocks(7 * ncl), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
       else
-        k_vjp_recon<double, 7, 5><<<nblocks(7 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+        k_vjp_recon<double, 7, 5><<<nblocks(7 * ncl), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
     } else {
-      k_vjp_states<double, 5><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, dir);
+      k_vjp_states<double, 5><<<nblocks(5 * ncl), TPB_ADJ, 0, L.s>>>(p, b, face_work, dir);
       if (p.flux == FEST_FLUX_SLAU)
         k_vjp_flux<double, true, 5><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
       else
         k_vjp_flux<double, false, 5><<<nblocks(nf), TPB_ADJ, 0, L.s>>>(p, b, lam, face_work, bf, dir);
       if (narrow)
-        k_vjp_recon<double, 5, 3><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+        k_vjp_recon<double, 5, 3><<<nblocks(5 * ncl), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
       else
-        k_vjp_recon<double, 5, 5><<<nblocks(5 * nf), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
+        k_vjp_recon<double, 5, 5><<<nblocks(5 * ncl), TPB_ADJ, 0, L.s>>>(p, b, face_work, bar, dir);
     }
     *L.count += 3;
     if (sst) {
