@@ -1358,7 +1358,21 @@ __global__ void k_adj_precond(Params p, DevBlock b, const double* phi, double* m
   const double g1 = p.gm - 1.0;
   const double f0 = phi[c], fu = phi[c + P], fv = phi[c + 2 * P], fw = phi[c + 3 * P], fp = phi[c + 4 * P];
   const double s = b.dt[ci] / b.cells[4 * c];
-  mu[ci] = s * (f0 - (u * fu + v * fv + w * fw) / rho + 0.5 * g1 * (u * u + v * v + w * w) * fp);
+  double m0 = f0 - (u * fu + v * fv + w * fw) / rho + 0.5 * g1 * (u * u + v * v + w * w) * fp;
+  if (d.nv == 7) {
+    // k = U6/rho, omega = U7/rho (no k in the energy, update.f90:377-386),
+    // and the point-implicit destruction that divides R6, R7 by
+    // 1 + beta omega dt and 1 + 2 beta omega dt (update.f90:395-398; its
+    // derivatives carry a factor R, zero at the fixed point)
+    const double tk = b.qp[c + 5 * P], tw = b.qp[c + 6 * P];
+    const double fk = phi[c + 5 * P], fo = phi[c + 6 * P];
+    const double F1 = b.F1[c], dt = b.dt[ci];
+    const double beta = 0.075 * F1 + (1. - F1) * 0.0828;
+    m0 -= (tk * fk + tw * fo) / rho;
+    mu[ci + 5 * N] = s * (fk / rho) / (1 + (beta * tw * dt));
+    mu[ci + 6 * N] = s * (fo / rho) / (1 + (2 * beta * tw * dt));
+  }
+  mu[ci] = s * m0;
   mu[ci + N] = s * (fu / rho - g1 * u * fp);
   mu[ci + 2 * N] = s * (fv / rho - g1 * v * fp);
   mu[ci + 3 * N] = s * (fw / rho - g1 * w * fp);
@@ -1379,7 +1393,7 @@ __global__ void k_adj_combine(Dims d, double* out, double c0, const double* x0, 
     const long long r = t / (d.imx - 1);
     const int j = 1 + (int)(r % (d.jmx - 1)), k = 1 + (int)(r / (d.jmx - 1));
     const long long c = pidx(d, i, j, k);
-    for (int l = 0; l < 5; ++l) {
+    for (int l = 0; l < d.nv; ++l) {
       const long long e = c + d.P * l;
       double v = c0 * x0[e];
       if (x1) v += c1 * x1[e];
@@ -1401,7 +1415,7 @@ __global__ void k_adj_combine(Dims d, double* out, double c0, const double* x0, 
 
 __global__ void k_adj_psi(Dims d, const double* mu, double* psi) {  // psi = -mu
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < ncells(d) * 5) psi[t] = -mu[t];
+  if (t < ncells(d) * d.nv) psi[t] = -mu[t];
 }
 
 }  // namespace
@@ -1479,7 +1493,7 @@ void launch_adjoint_psi(const Params& p, const DevBlock& b, AdjointWork& w, doub
     h = w.c;
   }
   k_adj_precond<<<nblocks(N), TPB_ADJ, 0, L.s>>>(p, b, h, w.mu);
-  k_adj_psi<<<nblocks(N * 5), TPB_ADJ, 0, L.s>>>(p.d, w.mu, psi);
+  k_adj_psi<<<nblocks(N * p.d.nv), TPB_ADJ, 0, L.s>>>(p.d, w.mu, psi);
   *L.count += 2;
 }
 

@@ -921,8 +921,6 @@ int fest_adjoint_solve(fest_handle* h, const double* dJdq, double CFL, int max_i
                        double* psi, int* n_done, double* drop) {
   if (!h || !dJdq || max_iters < 0) return FEST_ERR_ARG;
   if (!vjp_supported(h->p) || h->p.tstep != 'l' || needs_batch(h)) return FEST_ERR_ARG;
-  // the pseudo-time preconditioner maps the five mean-flow variables
-  if (h->p.d.nv != 5) return FEST_ERR_ARG;
   if (h->p.integ != FEST_TIME_NONE && h->p.integ != FEST_TIME_TVDRK3) return FEST_ERR_ARG;
   RET(sync_fused(h));
   Sizes z = sizes_of(h->p.d, h->p.n_grad);

@@ -373,9 +373,9 @@ int fest_residual_vjp_nodes(fest_handle *h, const double *qp, int current_iter,
  * Stops after max_iters or when the RMS update has dropped by tol;
  * n_done, drop (nullable) report the iterations and that drop.  Then
  * dJ/dalpha = dJ/dalpha|_q + psi . dR/dalpha for any parameter alpha.
- * Inviscid and laminar blocks (n_var 5; the preconditioner P maps the five
- * mean-flow variables): FEST_ERR_ARG for SST blocks, whose residual VJP
- * fest_residual_vjp still gives. */
+ * Blocks fest_residual_vjp supports, local time steps, forward Euler or
+ * TVD-RK3; for k-omega SST blocks P maps k and omega through U/rho and the
+ * update's point-implicit destruction factors (update.f90:395-398). */
 int fest_adjoint_solve(fest_handle *h, const double *dJdq, double CFL,
                        int max_iters, double tol, double *psi, int *n_done,
                        double *drop);
