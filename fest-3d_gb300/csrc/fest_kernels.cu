@@ -149,7 +149,8 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
   const Dims& d = p.d;
   double* q = b.qp;
   const long long P = d.P;
-  const bool sst = p.turb != FEST_TURB_NONE;
+  const bool sst = p.turb == FEST_TURB_SST || p.turb == FEST_TURB_SST2003;
+  const bool sa = p.turb == FEST_TURB_SA;  // tv: the sixth variable, treated as k is
   const int id = p.id[f];
   switch (id) {
     case -1:
@@ -160,6 +161,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         fix_col(p, q, f, ta, tb, 4, p.fix_w[f]);
         fix_col(p, q, f, ta, tb, 5, p.fix_p[f]);
         if (sst) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tw[f]); }
+        if (sa) fix_col(p, q, f, ta, tb, 6, p.fix_tv[f]);
       }
       break;
     case -2:
@@ -173,6 +175,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         fix_col(p, q, f, ta, tb, 3, p.fix_v[f]);
         fix_col(p, q, f, ta, tb, 4, p.fix_w[f]);
         if (sst) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tw[f]); }
+        if (sa) fix_col(p, q, f, ta, tb, 6, p.fix_tv[f]);
       }
       copy3_col(p, q, f, ta, tb, 5, CP_FLAT);
       break;
@@ -180,6 +183,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       for (int l = 1; l <= 4; ++l) copy3_col(p, q, f, ta, tb, l, CP_FLAT);
       if (iter <= 2) fix_col(p, q, f, ta, tb, 5, p.fix_p[f]);
       if (sst) { copy3_col(p, q, f, ta, tb, 6, CP_FLAT); copy3_col(p, q, f, ta, tb, 7, CP_FLAT); }
+      if (sa) copy3_col(p, q, f, ta, tb, 6, CP_FLAT);
       break;
     case -5: {  // wall (bc_primitive.f90:392-402)
       copy3_col(p, q, f, ta, tb, 5, CP_SYMM);
@@ -204,6 +208,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       copy3_col(p, q, f, ta, tb, 2, CP_ANTI);
       copy3_col(p, q, f, ta, tb, 3, CP_ANTI);
       copy3_col(p, q, f, ta, tb, 4, CP_ANTI);
+      if (sa) copy3_col(p, q, f, ta, tb, 6, CP_ANTI);
       if (sst) {
         copy3_col(p, q, f, ta, tb, 6, CP_ANTI);
         // set_omega_at_wall (bc_primitive.f90:564-643)
@@ -222,6 +227,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       copy3_col(p, q, f, ta, tb, 1, CP_SYMM);
       copy3_col(p, q, f, ta, tb, 5, CP_SYMM);
       if (sst) { copy3_col(p, q, f, ta, tb, 6, CP_SYMM); copy3_col(p, q, f, ta, tb, 7, CP_SYMM); }
+      if (sa) copy3_col(p, q, f, ta, tb, 6, CP_SYMM);
       int fi, fj, fk;
       bface_ijk(d, f, ta, tb, fi, fj, fk);
       const double* fn = b.faces[f / 2] + 4 * fidx(d, f / 2, fi, fj, fk);
@@ -244,6 +250,12 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         double Ulast = riemann_col(p, b, f, na, nb, false, tp);
         if (Ulast > 0.) { copy3_col(p, q, f, ta, tb, 6, CP_FLAT); copy3_col(p, q, f, ta, tb, 7, CP_FLAT); }
         else { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tw[f]); }
+      }
+      if (sa) {
+        int na = (f / 2 == 0 ? d.jmx : d.imx) - 1, nb = (f / 2 == 2 ? d.jmx : d.kmx) - 1;
+        double Ulast = riemann_col(p, b, f, na, nb, false, tp);
+        if (Ulast > 0.) copy3_col(p, q, f, ta, tb, 6, CP_FLAT);
+        else fix_col(p, q, f, ta, tb, 6, p.fix_tv[f]);
       }
     } break;
     default:
@@ -466,7 +478,29 @@ __global__ void k_gradient_bc(Params p, DevBlock b) {
   }
 }
 
-// calculate_viscosity (viscosity.f90:52-546): Sutherland mu, SST mu_t and F1
+// ---- Spalart-Allmaras (global/global_sa.f90:6-22) -----------------------
+constexpr double kSaCb1 = 0.1355, kSaCb2 = 0.6220, kSaCw2 = 0.3, kSaCw3 = 2.0, kSaSigma = 2. / 3.,
+                 kSaKappa = 0.41;
+__device__ __forceinline__ double sa_cw1() { return (kSaCb1 / (kSaKappa * kSaKappa)) + ((1 + kSaCb2) / kSaSigma); }
+// x**6 as gfortran expands an integer power: x2 = x*x, x4 = x2*x2, x4*x2
+__device__ __forceinline__ double sa_pow6(double x) {
+  const double x2 = x * x, x4 = x2 * x2;
+  return x4 * x2;
+}
+// the wall function fw(r) of source.f90:955-957 and update.f90:416-418
+__device__ __forceinline__ double sa_fw(double r) {
+  const double g = r + kSaCw2 * (sa_pow6(r) - r);
+  return g * pow((1.0 + sa_pow6(kSaCw3)) / (sa_pow6(g) + sa_pow6(kSaCw3)), 1.0 / 6.0);
+}
+// the cell's vorticity magnitude from its velocity gradients
+__device__ __forceinline__ double sa_vort(const DevBlock& b, long long og, long long NG) {
+  auto G = [&](int c, int l) { return b.grad[c][og + NG * (l - 1)]; };
+  const double a = G(1, 3) - G(2, 2), bb = G(2, 1) - G(0, 3), c = G(0, 2) - G(1, 1);
+  return sqrt(((a * a) + (bb * bb) + (c * c)));
+}
+
+// calculate_viscosity (viscosity.f90:52-546): Sutherland mu, SST mu_t and
+// F1, Spalart-Allmaras mu_t
 __global__ void k_viscosity(Params p, DevBlock b) {
   const Dims& d = p.d;
   R3 r = r3(0, d.imx, 0, d.jmx, 0, d.kmx);
@@ -479,6 +513,14 @@ __global__ void k_viscosity(Params p, DevBlock b) {
     b.mu[c0] = p.mu_ref * (pow(T / p.T_ref, 1.5)) * ((p.T_ref + p.S) / (T + p.S));
   }
   if (p.turb == FEST_TURB_NONE) return;
+  if (p.turb == FEST_TURB_SA) {  // viscosity.f90:149-160: mu_t = rho tv fv1
+    const double tv = q[c0 + 5 * d.P], density = q[c0];
+    const double xi = tv * density / b.mu[c0];
+    const double x3 = xi * xi * xi;
+    const double fv1 = x3 / (x3 + p.sa_cv1_3);
+    b.mut[c0] = density * tv * fv1;
+    return;
+  }
   const double bstar = 0.09, a1 = 0.31, sigma_w2 = 0.856;
   const long long og = gidx(d, i, j, k), NG = ngrad(d);
   auto G = [&](int c, int l) { return b.grad[c][og + NG * (l - 1)]; };
@@ -581,7 +623,22 @@ __global__ void k_viscous(Params p, DevBlock b, int dir) {
                                         ((Txy * uf + Tyy * vf + Tyz * wf + Qy) * ny) +
                                         ((Txz * uf + Tyz * vf + Tzz * wf + Qz) * nz)));
   bool bad = (F2 != F2) || (F3 != F3) || (F4 != F4) || (F5 != F5);
-  if (turb && !(dir == 2 && d.kmx == 2)) {
+  if (p.turb == FEST_TURB_SA) {
+    // compute_viscous_fluxes_sa (viscous.f90:570-656), every direction
+    double H[3];
+    for (int c = 0; c < 3; ++c) H[c] = 0.5 * (b.grad[c][g0 + NG * 4] + b.grad[c][g1 + NG * 4]);
+    const double dtv = q[c1 + 5 * P] - q[c0 + 5 * P];
+    const double nc = (dtv - (H[0] * delx + H[1] * dely + H[2] * delz)) / dLR;
+    H[0] = H[0] + (nc * delx / dLR);
+    H[1] = H[1] + (nc * dely / dLR);
+    H[2] = H[2] + (nc * delz / dLR);
+    const double rhoface = 0.5 * (q[c0] + q[c1]);
+    const double mutv = 0.5 * (q[c0 + 5 * P] + q[c1 + 5 * P]) * rhoface;
+    const double F6 = F[of + 5 * fl.N] - (A * ((mu_f + mutv) * (H[0] * nx + H[1] * ny + H[2] * nz))) / kSaSigma;
+    F[of + 5 * fl.N] = F6;
+    bad |= (F6 != F6);
+  }
+  if (turb && p.turb != FEST_TURB_SA && !(dir == 2 && d.kmx == 2)) {
     // SST diffusion (viscous.f90:378-444)
     const double sigma_k1 = 0.85, sigma_k2 = 1.0, sigma_w1 = 0.5, sigma_w2 = 0.856;
     double H[3][2];
@@ -636,12 +693,64 @@ __global__ void k_residue(Params p, DevBlock b) {
                        (b.flux[2][oz1 + fz.N * l] - b.flux[2][oz0 + fz.N * l]);
 }
 
+// add_sa_source (source.f90:845-983): the density gradient from the cell's
+// six face sums, whose k faces' normal reads (nx, nx, nx) as the reference
+// does (source.f90:913)
+__device__ void sa_source(const Params& p, const DevBlock& b, int i, int j, int k) {
+  const Dims& d = p.d;
+  const long long c0 = pidx(d, i, j, k), og = gidx(d, i, j, k), NG = ngrad(d), P = d.P;
+  const double* q = b.qp;
+  auto G = [&](int c, int l) { return b.grad[c][og + NG * (l - 1)]; };
+  const double density = q[c0], tv = q[c0 + 5 * P];
+  const long long nb[6] = {pidx(d, i - 1, j, k), pidx(d, i, j - 1, k), pidx(d, i, j, k - 1),
+                           pidx(d, i + 1, j, k), pidx(d, i, j + 1, k), pidx(d, i, j, k + 1)};
+  const double* fr[6] = {b.faces[0] + 4 * fidx(d, 0, i, j, k), b.faces[1] + 4 * fidx(d, 1, i, j, k),
+                         b.faces[2] + 4 * fidx(d, 2, i, j, k), b.faces[0] + 4 * fidx(d, 0, i + 1, j, k),
+                         b.faces[1] + 4 * fidx(d, 1, i, j + 1, k), b.faces[2] + 4 * fidx(d, 2, i, j, k + 1)};
+  double rf[6], nrm[6][3];
+  for (int f = 0; f < 6; ++f) {
+    rf[f] = q[nb[f]] + density;
+    for (int c = 0; c < 3; ++c) nrm[f][c] = fr[f][f == 2 ? 1 : 1 + c];
+  }
+  const double vol = b.cells[4 * c0];
+  double gr[3];
+  for (int c = 0; c < 3; ++c)
+    gr[c] = (-(rf[0]) * nrm[0][c] * fr[0][0] - (rf[1]) * nrm[1][c] * fr[1][0] - (rf[2]) * nrm[2][c] * fr[2][0] +
+             (rf[3]) * nrm[3][c] * fr[3][0] + (rf[4]) * nrm[4][c] * fr[4][0] + (rf[5]) * nrm[5][c] * fr[5][0]) /
+            (2.0 * vol);
+  const double vort = sa_vort(b, og, NG);
+  const double CD1 = kSaCb2 * ((G(0, 5) * G(0, 5)) + (G(1, 5) * G(1, 5)) + (G(2, 5) * G(2, 5)));
+  const double CD2 = ((gr[0] * G(0, 5)) + (gr[1] * G(1, 5)) + (gr[2] * G(2, 5)));
+  const double dd = b.dist[c0];
+  const double kd = kSaKappa * dd, kd2 = kd * kd;
+  const double nu = b.mu[c0] / density;
+  const double xi = tv / nu;
+  const double x3 = xi * xi * xi;
+  const double fv1 = x3 / (x3 + p.sa_cv1_3);
+  const double fv2 = 1.0 - xi / (1.0 + (xi * fv1));
+  const double Scap = fmax2(vort + (tv * fv2 / (kd2)), 0.3 * vort);
+  const double rr = fmin2(tv / (Scap * kd2), 10.0);
+  const double fw = sa_fw(rr);
+  const double td = tv / dd;
+  const double D_v = density * sa_cw1() * fw * (td * td);
+  const double P_v = density * kSaCb1 * Scap * tv;
+  const double lamda = density * CD1 / kSaSigma - CD2 * (nu + tv) / kSaSigma;
+  const double S_v = (P_v - D_v + lamda) * vol;
+  const long long o = cidx(d, i, j, k), N = ncells(d);
+  b.res[o + 5 * N] = b.res[o + 5 * N] - S_v;
+}
+
+// add_source_term_residue (source.f90:94-155): add_sa_source, or
 // add_sst_source (source.f90:158-270)
 __global__ void k_source(Params p, DevBlock b) {
   const Dims& d = p.d;
   R3 r = r3(1, d.imx - 1, 1, d.jmx - 1, 1, d.kmx - 1);
   int i, j, k;
   if (!decode(r, i, j, k)) return;
+  if (p.turb == FEST_TURB_SA) {
+    sa_source(p, b, i, j, k);
+    return;
+  }
   const double sigma_w1 = 0.5, sigma_w2 = 0.856, beta1 = 0.075, beta2 = 0.0828, bstar = 0.09,
                kap = 0.41;
   int limiter;
@@ -780,7 +889,22 @@ __global__ void k_update(Params p, DevBlock b, double TF, double SF, int TU, int
   for (int l = 0; l < NVMAX; ++l)
     if (l < nv) R[l] = b.res[o + N * l];
   const double dtc = b.dt[o];
-  if (p.turb != FEST_TURB_NONE) {
+  const bool sa = p.turb == FEST_TURB_SA;
+  if (sa) {
+    // update.f90:405-419, xi from the conservative U1(6) and the stage
+    // state's density as written there
+    const double vort = sa_vort(b, gidx(d, i, j, k), ngrad(d));
+    const double dd = b.dist[c0];
+    const double kd = kSaKappa * dd, kd2 = kd * kd;
+    const double xi = u1[5] * b.qp[c0] / b.mu[c0];
+    const double x3 = xi * xi * xi;
+    const double fv1 = x3 / (x3 + p.sa_cv1_3);
+    const double fv2 = 1.0 - xi / (1 + xi * fv1);
+    const double scap = vort + u1[5] * fv2 / (kd2);
+    const double rsa = fmin2(u1[5] / (scap * kd2), 10.0);
+    const double fw = sa_fw(rsa);
+    R[5] = R[5] / (1. + ((-1.0 * u1[0] * kSaCb1 * scap) + (2.0 * u1[0] * sa_cw1() * fw * u1[5] / (dd * dd))) * dtc);
+  } else if (p.turb != FEST_TURB_NONE) {
     double F1 = b.F1[c0];
     double beta = 0.075 * F1 + (1. - F1) * 0.0828;
     double w = b.qp[c0 + 6 * P];
@@ -814,7 +938,9 @@ __global__ void k_update(Params p, DevBlock b, double TF, double SF, int TU, int
     return;
   }
   for (int l = 0; l < 5; ++l) b.qp[c0 + P * l] = u2[l];
-  if (p.turb != FEST_TURB_NONE) {
+  if (sa) {
+    b.qp[c0 + 5 * P] = fmax2(u2[5], 1.e-12);  // update.f90:474-475
+  } else if (p.turb != FEST_TURB_NONE) {
     if (u2[5] >= 0.) b.qp[c0 + 5 * P] = u2[5];
     if (u2[6] >= 0.) b.qp[c0 + 6 * P] = u2[6];
   }

@@ -105,9 +105,10 @@ def uniform_state(ext, flow, tk=0.0, tw=0.0):
 
 
 def random_state(ext, seed=0, mach=0.3, amp=0.1, p0=101325.0, rho0=1.2, tk=1.0, tw=1000.0,
-                 rho_amp=None):
+                 rho_amp=None, tv=1e-4):
     """Smooth 3-mode Fourier field over the padded block: rho in
-    rho0*(1 +- amp), |u| up to mach*c, p0*(1 +- amp), positive tk/tw."""
+    rho0*(1 +- amp), |u| up to mach*c, p0*(1 +- amp), positive tk/tw
+    (seven variables) or tv (six, Spalart-Allmaras)."""
     rng = np.random.default_rng(seed)
     ni, nj, nk = ext.imx + 5, ext.jmx + 5, ext.kmx + 5
     I, J, K = np.meshgrid(np.arange(ni) / ni, np.arange(nj) / nj, np.arange(nk) / nk, indexing="ij")
@@ -128,7 +129,9 @@ def random_state(ext, seed=0, mach=0.3, amp=0.1, p0=101325.0, rho0=1.2, tk=1.0, 
     for l in (1, 2, 3):
         qp[..., l] = mach * c * field()
     qp[..., 4] = p0 * (1 + amp * field())
-    if ext.n_var > 5:
+    if ext.n_var == 6:
+        qp[..., 5] = tv * (1 + 0.5 * field())
+    elif ext.n_var > 5:
         qp[..., 5] = tk * (1 + 0.5 * field())
         qp[..., 6] = tw * (1 + 0.5 * field())
     return qp

@@ -23,7 +23,7 @@ class Handle:
         self.h = C.c_void_p()
         abi.check(self.lib.fest_create(C.byref(ext), C.byref(flow), C.byref(scheme), C.byref(bc),
                                        C.byref(self.h)), "fest_create")
-        ng = 6 if ext.n_var == 7 else 4
+        ng = abi.n_grad_for(ext.n_var)
         sh = abi.shapes(ext, ng)
         self.shape = {"qp": sh["qp"], "Temp": sh["pad"], "cells": sh["cells"],
                       "Ifaces": sh["Ifaces"], "Jfaces": sh["Jfaces"], "Kfaces": sh["Kfaces"],

@@ -65,7 +65,11 @@ enum { FEST_INTERP_NONE = 0, FEST_INTERP_MUSCL = 1, FEST_INTERP_PPM = 2,
 enum { FEST_TIME_NONE = 0, FEST_TIME_RK2 = 1, FEST_TIME_RK4 = 2,
        FEST_TIME_TVDRK2 = 3, FEST_TIME_TVDRK3 = 4, FEST_TIME_IMPLICIT = 5,
        FEST_TIME_PLUSGS = 6 };
-enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2 };
+/* FEST_TURB_SA: the Spalart-Allmaras model ('sa', n_var = 6, the sixth
+ * variable tv; viscosity.f90:149-213, viscous.f90:570-656,
+ * source.f90:845-983, update.f90:405-420,474-475), FP64 module path
+ * (fest_get_next_solution, fest_step with the explicit integrators) */
+enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2, FEST_TURB_SA = 3 };
 enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
 /* MUSCL limiter: the reference hard-codes Koren's alpha family
  * (muscl.f90:151,176); van Albada (muscl.f90:178, commented out there) is an
@@ -92,6 +96,7 @@ typedef struct {            /* flowtype, vartypes.f90:235-286 */
   double gm, R_gas, mu_ref, T_ref, Sutherland_temp, Pr, tPr;
   int mu_variation;         /* FEST_MU_* */
   int reserved;
+  double tv_inf;            /* Spalart-Allmaras free-stream tv (state.f90:106-109) */
 } fest_flow;
 
 typedef struct {            /* schemetype, vartypes.f90:197-232 */
@@ -138,6 +143,8 @@ typedef struct {            /* boundarytype, vartypes.f90:289-367 */
    * tangential directions swapped).  Tangential directions: (j, k) on i
    * faces, (i, k) on j faces, (i, j) on k faces.  Default 0 (aligned). */
   int partner_orient[6];
+  /* fixed tv of each face for Spalart-Allmaras blocks (read_bc.f90:112-115) */
+  double fixed_tv[6];
 } fest_bc;
 
 typedef struct fest_handle fest_handle;

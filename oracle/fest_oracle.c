@@ -20,6 +20,18 @@ static const double sigma_k1 = 0.85, sigma_k2 = 1.0, sigma_w1 = 0.5,
                     sigma_w2 = 0.856, beta1 = 0.075, beta2 = 0.0828,
                     bstar = 0.09, kappa_sst = 0.41, a1_sst = 0.31;
 
+/* ---- Spalart-Allmaras constants (global/global_sa.f90:6-22); the
+ * parameter powers cv1**3 and cw3**6 are folded by the compiler to the
+ * correctly rounded values pow gives */
+static const double cb1 = 0.1355, cb2 = 0.6220, cw2 = 0.3, cw3 = 2.0, cv1 = 7.1,
+                    sigma_sa = 2. / 3., kappa_sa = 0.41;
+#define CW1_SA ((cb1 / (kappa_sa * kappa_sa)) + ((1 + cb2) / sigma_sa))
+/* x**6 as gfortran expands an integer power: x2 = x*x, x4 = x2*x2, x4*x2 */
+static inline double pow6(double x) {
+  double x2 = x * x, x4 = x2 * x2;
+  return x4 * x2;
+}
+
 struct fo_block {
   fest_extent d;
   fest_flow flow;
@@ -127,7 +139,7 @@ fo_block *fo_create(const fest_extent *d, const fest_flow *flow,
   long N = (long)(imx - 1) * (jmx - 1) * (kmx - 1);
   long Ng = (long)(imx + 1) * (jmx + 1) * (kmx + 1);
   /* get_n_grad (gradients.f90:229-258) */
-  b->n_grad = (scheme->turbulence == FEST_TURB_NONE) ? 4 : 6;
+  b->n_grad = scheme->turbulence == FEST_TURB_NONE ? 4 : scheme->turbulence == FEST_TURB_SA ? 5 : 6;
   b->sz[FO_QP] = P * n;
   b->sz[FO_TEMP] = P;
   b->sz[FO_NODES] = (long)(imx + 6) * (jmx + 6) * (kmx + 6) * 3;
@@ -429,7 +441,11 @@ static void fixv(fo_block *b, int l, double val, int f) {
         *Qp(b, gi, gj, gk, l) = val;
       }
 }
-static int is_sst(const fo_block *b) { return b->sc.turbulence != FEST_TURB_NONE; }
+static int is_sst(const fo_block *b) {
+  return b->sc.turbulence == FEST_TURB_SST || b->sc.turbulence == FEST_TURB_SST2003;
+}
+static int is_sa(const fo_block *b) { return b->sc.turbulence == FEST_TURB_SA; }
+static int is_turb(const fo_block *b) { return b->sc.turbulence != FEST_TURB_NONE; }
 
 /* bc_primitive.f90:1778-1945 temp_based_density */
 static void temp_based_density(fo_block *b, int f) {
@@ -588,6 +604,10 @@ static void riemann_face(fo_block *b, int f, int total_pressure) {
     if (last_positive) { copy3(b, 6, CP_FLAT, f); copy3(b, 7, CP_FLAT, f); }
     else { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tw[f], f); }
   }
+  if (is_sa(b) && na > 0 && nb > 0) {
+    if (last_positive) copy3(b, 6, CP_FLAT, f);
+    else fixv(b, 6, b->bc.fixed_tv[f], f);
+  }
   /* plane copy of layer 1 into layers 2 and 3, all tangential indices */
   int imx = IMX, jmx = JMX, kmx = KMX;
   for (int l = 1; l <= NV; ++l)
@@ -740,7 +760,7 @@ static void corners(fo_block *b) {
 
 /* bc_primitive.f90:55-226 populate_ghost_primitive */
 int fo_populate_ghost_primitive(fo_block *b, int it) {
-  int sst = is_sst(b);
+  int sst = is_sst(b), sa = is_sa(b);
   for (int f = 0; f < 6; ++f) {
     switch (b->bc.id[f]) {
     case -1: /* supersonic_inlet */
@@ -751,6 +771,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
         fixv(b, 4, b->bc.fixed_z_speed[f], f);
         fixv(b, 5, b->bc.fixed_pressure[f], f);
         if (sst) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tw[f], f); }
+        if (sa) fixv(b, 6, b->bc.fixed_tv[f], f);
       }
       break;
     case -2: /* supersonic_outlet */
@@ -764,6 +785,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
         fixv(b, 3, b->bc.fixed_y_speed[f], f);
         fixv(b, 4, b->bc.fixed_z_speed[f], f);
         if (sst) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tw[f], f); }
+        if (sa) fixv(b, 6, b->bc.fixed_tv[f], f);
       }
       copy3(b, 5, CP_FLAT, f);
       break;
@@ -771,6 +793,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
       for (int l = 1; l <= 4; ++l) copy3(b, l, CP_FLAT, f);
       if (it <= 2) fixv(b, 5, b->bc.fixed_pressure[f], f);
       if (sst) { copy3(b, 6, CP_FLAT, f); copy3(b, 7, CP_FLAT, f); }
+      if (sa) copy3(b, 6, CP_FLAT, f);
       break;
     case -5: /* wall: pressure symm, temp_based_density, no_slip */
       copy3(b, 5, CP_SYMM, f);
@@ -779,11 +802,13 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
       copy3(b, 3, CP_ANTI, f);
       copy3(b, 4, CP_ANTI, f);
       if (sst) { copy3(b, 6, CP_ANTI, f); set_omega_at_wall(b, f); }
+      if (sa) copy3(b, 6, CP_ANTI, f);
       break;
     case -6: /* slip_wall */
       copy3(b, 1, CP_SYMM, f);
       copy3(b, 5, CP_SYMM, f);
       if (sst) { copy3(b, 6, CP_SYMM, f); copy3(b, 7, CP_SYMM, f); }
+      if (sa) copy3(b, 6, CP_SYMM, f);
       flow_tangency(b, f);
       break;
     case -8: riemann_face(b, f, 0); break;
@@ -1369,6 +1394,8 @@ int fo_evaluate_all_gradients(fo_block *b) {
       gradient_G(b, g[c], 5, q, 6, c);
       gradient_G(b, g[c], 6, q, 7, c);
     }
+  if (is_sa(b))  /* gradtv (gradients.f90:165-169) */
+    for (int c = 0; c < ncomp; ++c) gradient_G(b, g[c], 5, q, 6, c);
   int err = FEST_OK;
   for (int c = 0; c < 3; ++c)
     for (long p = 0; p < b->sz[FO_GX + c]; ++p)
@@ -1392,6 +1419,40 @@ int fo_calculate_viscosity(fo_block *b) {
           *at(mu, i, j, k, 1) = fl->mu_ref * (pow(T / fl->T_ref, 1.5)) *
                                 ((fl->T_ref + fl->Sutherland_temp) / (T + fl->Sutherland_temp));
         }
+  }
+  if (is_sa(b)) {
+    /* viscosity.f90:149-160: mu_t = rho tv fv1, xi = tv rho / mu */
+    OMP_FOR
+    for (int k = 0; k <= KMX; ++k)
+      for (int j = 0; j <= JMX; ++j)
+        for (int i = 0; i <= IMX; ++i) {
+          double tv = *at(q, i, j, k, 6), density = *at(q, i, j, k, 1);
+          double xi = tv * density / *at(mu, i, j, k, 1);
+          double x3 = xi * xi * xi;
+          double fv1 = x3 / (x3 + pow(cv1, 3.0));
+          *at(mut, i, j, k, 1) = density * tv * fv1;
+        }
+    /* ghost copies (viscosity.f90:162-212): faces -1..-9 but -5 copy layer 1,
+     * the wall negates it; interfaces keep their own */
+    for (int f = 0; f < 6; ++f) {
+      int id = b->bc.id[f];
+      double sgn;
+      if (id == -5) sgn = -1.0;
+      else if (id >= -9 && id <= -1) sgn = 1.0;
+      else continue;
+      int na, nb;
+      tang_range(b, f, &na, &nb);
+      for (int tb = 1; tb <= nb; ++tb)
+        for (int ta = 1; ta <= na; ++ta) {
+          int gi, gj, gk, ii, ij, ik;
+          ghost_ijk(b, f, 1, ta, tb, &gi, &gj, &gk);
+          inner_ijk(b, f, 1, ta, tb, &ii, &ij, &ik);
+          *at(mut, gi, gj, gk, 1) = sgn < 0 ? -*at(mut, ii, ij, ik, 1) : *at(mut, ii, ij, ik, 1);
+        }
+    }
+    for (long p = 0; p < b->sz[FO_MU]; ++p)
+      if (b->a[FO_MU][p] != b->a[FO_MU][p]) return FEST_ERR_NAN;
+    return FEST_OK;
   }
   if (!is_sst(b)) return FEST_OK;
   int s2003 = b->sc.turbulence == FEST_TURB_SST2003;
@@ -1460,7 +1521,7 @@ static void viscous_laminar(fo_block *b, int dir) {
   R4 fa = vfaces(b, dir), cl = vcells(b);
   const fest_flow *fl = &b->flow;
   int ii = dir == 0, jj = dir == 1, kk = dir == 2;
-  int turb = is_sst(b);
+  int turb = is_turb(b);
   OMP_FOR
   for (int k = 1; k <= KMX - 1 + kk; ++k)
     for (int j = 1; j <= JMX - 1 + jj; ++j)
@@ -1553,8 +1614,42 @@ static void viscous_sst(fo_block *b, int dir) {
       }
 }
 
+/* viscous.f90:570-656 compute_viscous_fluxes_sa */
+static void viscous_sa(fo_block *b, int dir) {
+  V q = vqp(b), mu = vpad(b, FO_MU), Fl = vflux(b, dir);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
+  R4 fa = vfaces(b, dir), cl = vcells(b);
+  int ii = dir == 0, jj = dir == 1, kk = dir == 2;
+  OMP_FOR
+  for (int k = 1; k <= KMX - 1 + kk; ++k)
+    for (int j = 1; j <= JMX - 1 + jj; ++j)
+      for (int i = 1; i <= IMX - 1 + ii; ++i) {
+        int im = i - ii, jm = j - jj, km = k - kk;
+        double dtvdx = 0.5 * (*at(g[0], im, jm, km, 5) + *at(g[0], i, j, k, 5));
+        double dtvdy = 0.5 * (*at(g[1], im, jm, km, 5) + *at(g[1], i, j, k, 5));
+        double dtvdz = 0.5 * (*at(g[2], im, jm, km, 5) + *at(g[2], i, j, k, 5));
+        const double *c1 = r4(cl, i, j, k), *c0 = r4(cl, im, jm, km);
+        double delx = c1[1] - c0[1], dely = c1[2] - c0[2], delz = c1[3] - c0[3];
+        double d_LR = sqrt(delx * delx + dely * dely + delz * delz);
+        double deltv = *at(q, i, j, k, 6) - *at(q, im, jm, km, 6);
+        double nc = (deltv - (dtvdx * delx + dtvdy * dely + dtvdz * delz)) / d_LR;
+        dtvdx = dtvdx + (nc * delx / d_LR);
+        dtvdy = dtvdy + (nc * dely / d_LR);
+        dtvdz = dtvdz + (nc * delz / d_LR);
+        double rhoface = 0.5 * (*at(q, im, jm, km, 1) + *at(q, i, j, k, 1));
+        double mu_f = 0.5 * (*at(mu, im, jm, km, 1) + *at(mu, i, j, k, 1));
+        double mut_f = 0.5 * (*at(q, im, jm, km, 6) + *at(q, i, j, k, 6)) * rhoface;
+        const double *fc = r4(fa, i, j, k);
+        double nx = fc[1], ny = fc[2], nz = fc[3], area = fc[0];
+        *at(Fl, i, j, k, 6) = *at(Fl, i, j, k, 6) -
+                              (area * ((mu_f + mut_f) * (dtvdx * nx + dtvdy * ny + dtvdz * nz))) / sigma_sa;
+      }
+}
+
 int fo_compute_viscous_fluxes(fo_block *b) {
   for (int dir = 0; dir < 3; ++dir) viscous_laminar(b, dir);
+  if (is_sa(b))
+    for (int dir = 0; dir < 3; ++dir) viscous_sa(b, dir);
   if (is_sst(b)) {
     viscous_sst(b, 0);
     viscous_sst(b, 1);
@@ -1566,8 +1661,65 @@ int fo_compute_viscous_fluxes(fo_block *b) {
   return FEST_OK;
 }
 
-/* source.f90:158-270 add_sst_source */
+/* source.f90:845-983 add_sa_source.  The density gradient comes from the
+ * six face sums of the cell; the k faces' normal reads (nx, nx, nx) as the
+ * reference does (source.f90:913). */
+static void sa_source(fo_block *b) {
+  V q = vqp(b), mu = vpad(b, FO_MU), dist = vpad(b, FO_DIST), r = vres(b);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
+  R4 If = vfaces(b, 0), Jf = vfaces(b, 1), Kf = vfaces(b, 2), cl = vcells(b);
+  OMP_FOR
+  for (int k = 1; k <= KMX - 1; ++k)
+    for (int j = 1; j <= JMX - 1; ++j)
+      for (int i = 1; i <= IMX - 1; ++i) {
+#define GR(c, l) (*at(g[c], i, j, k, l))
+        double density = *at(q, i, j, k, 1), tv = *at(q, i, j, k, 6);
+        double RhoFace[6] = {*at(q, i - 1, j, k, 1) + density, *at(q, i, j - 1, k, 1) + density,
+                             *at(q, i, j, k - 1, 1) + density, *at(q, i + 1, j, k, 1) + density,
+                             *at(q, i, j + 1, k, 1) + density, *at(q, i, j, k + 1, 1) + density};
+        const double *fI0 = r4(If, i, j, k), *fJ0 = r4(Jf, i, j, k), *fK0 = r4(Kf, i, j, k);
+        const double *fI1 = r4(If, i + 1, j, k), *fJ1 = r4(Jf, i, j + 1, k), *fK1 = r4(Kf, i, j, k + 1);
+        double Area[6] = {fI0[0], fJ0[0], fK0[0], fI1[0], fJ1[0], fK1[0]};
+        double Normal[6][3] = {{fI0[1], fI0[2], fI0[3]}, {fJ0[1], fJ0[2], fJ0[3]}, {fK0[1], fK0[1], fK0[1]},
+                               {fI1[1], fI1[2], fI1[3]}, {fJ1[1], fJ1[2], fJ1[3]}, {fK1[1], fK1[2], fK1[3]}};
+        double vol = r4(cl, i, j, k)[0];
+        double gr[3];
+        for (int c = 0; c < 3; ++c)
+          gr[c] = (-(RhoFace[0]) * Normal[0][c] * Area[0] - (RhoFace[1]) * Normal[1][c] * Area[1] -
+                   (RhoFace[2]) * Normal[2][c] * Area[2] + (RhoFace[3]) * Normal[3][c] * Area[3] +
+                   (RhoFace[4]) * Normal[4][c] * Area[4] + (RhoFace[5]) * Normal[5][c] * Area[5]) /
+                  (2.0 * vol);
+        double wa = GR(1, 3) - GR(2, 2), wb = GR(2, 1) - GR(0, 3), wc = GR(0, 2) - GR(1, 1);
+        double vort = sqrt(((wa * wa) + (wb * wb) + (wc * wc)));
+        double CD1 = cb2 * ((GR(0, 5) * GR(0, 5)) + (GR(1, 5) * GR(1, 5)) + (GR(2, 5) * GR(2, 5)));
+        double CD2 = ((gr[0] * GR(0, 5)) + (gr[1] * GR(1, 5)) + (gr[2] * GR(2, 5)));
+        double d = *at(dist, i, j, k, 1);
+        double kd = kappa_sa * d, kd2 = kd * kd;
+        double nu = *at(mu, i, j, k, 1) / density;
+        double xi = tv / nu;
+        double x3 = xi * xi * xi;
+        double fv1 = x3 / (x3 + pow(cv1, 3.0));
+        double fv2 = 1.0 - xi / (1.0 + (xi * fv1));
+        double Scap = fmax2(vort + (tv * fv2 / (kd2)), 0.3 * vort);
+        double rr = fmin2(tv / (Scap * kd2), 10.0);
+        double gg = rr + cw2 * (pow6(rr) - rr);
+        double fw = gg * pow((1.0 + pow6(cw3)) / (pow6(gg) + pow6(cw3)), 1.0 / 6.0);
+        double td = tv / d;
+        double D_v = density * CW1_SA * fw * (td * td);
+        double P_v = density * cb1 * Scap * tv;
+        double lamda = density * CD1 / sigma_sa - CD2 * (nu + tv) / sigma_sa;
+        double S_v = (P_v - D_v + lamda) * vol;
+        *at(r, i, j, k, 6) = *at(r, i, j, k, 6) - S_v;
+#undef GR
+      }
+}
+
+/* source.f90:94-155 add_source_term_residue: the SA and SST sources */
 void fo_add_source_term_residue(fo_block *b) {
+  if (is_sa(b)) {
+    sa_source(b);
+    return;
+  }
   if (!is_sst(b)) return;
   V q = vqp(b), mut = vpad(b, FO_MUT), F1v = vpad(b, FO_F1), r = vres(b);
   V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
@@ -1680,7 +1832,7 @@ static void local_time_step(fo_block *b, double CFL) {
         *at(dt, i, j, k, 1) = t * r4(cl, i, j, k)[0] * CFL;
       }
   if (b->flow.mu_ref != 0.0) viscous_time(b, 0, CFL);
-  if (b->flow.mu_ref != 0 && is_sst(b)) viscous_time(b, 1, CFL);
+  if (b->flow.mu_ref != 0 && is_turb(b)) viscous_time(b, 1, CFL);
 }
 
 void fo_compute_time_step(fo_block *b, double CFL) {
@@ -1708,7 +1860,9 @@ int fo_update_with(fo_block *b, double TF, double SF, int TU, int use_store) {
   V Rn = mkv(b->a[FO_RSTORE], 1, 1, 1, IMX - 1, JMX - 1, KMX - 1);
   R4 cl = vcells(b);
   double gm = b->flow.gm;
-  int n = NV, sst = is_sst(b);
+  int n = NV, sst = is_sst(b), sa = is_sa(b);
+  V mu = vpad(b, FO_MU), dist = vpad(b, FO_DIST);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
   int err = FEST_OK;
   OMP_FOR
   for (int k = 1; k <= KMX - 1; ++k)
@@ -1727,6 +1881,25 @@ int fo_update_with(fo_block *b, double TF, double SF, int TU, int use_store) {
           double w = *at(q, i, j, k, 7);
           R[5] = R[5] / (1 + (beta * w * dtc));
           R[6] = R[6] / (1 + (2 * beta * w * dtc));
+        }
+        if (sa) {
+          /* update.f90:405-419: xi from the conservative U1(6) and the
+           * stage state's density, as written there */
+#define GR(c, l) (*at(g[c], i, j, k, l))
+          double wa = GR(1, 3) - GR(2, 2), wb = GR(2, 1) - GR(0, 3), wc = GR(0, 2) - GR(1, 1);
+          double vort = sqrt(((wa * wa) + (wb * wb) + (wc * wc)));
+#undef GR
+          double d = *at(dist, i, j, k, 1);
+          double kd = kappa_sa * d, kd2 = kd * kd;
+          double xi = u1[5] * *at(q, i, j, k, 1) / *at(mu, i, j, k, 1);
+          double x3 = xi * xi * xi;
+          double fv1 = x3 / (x3 + pow(cv1, 3.0));
+          double fv2 = 1.0 - xi / (1 + xi * fv1);
+          double scap = vort + u1[5] * fv2 / (kd2);
+          double rsa = fmin2(u1[5] / (scap * kd2), 10.0);
+          double gg = rsa + cw2 * (pow6(rsa) - rsa);
+          double fw = gg * pow((1.0 + pow6(cw3)) / (pow6(gg) + pow6(cw3)), 1.0 / 6.0);
+          R[5] = R[5] / (1. + ((-1.0 * u1[0] * cb1 * scap) + (2.0 * u1[0] * CW1_SA * fw * u1[5] / (d * d))) * dtc);
         }
         if (use_store) {
           for (int l = 1; l <= n; ++l) *at(Rn, i, j, k, l) = *at(Rn, i, j, k, l) + SF * R[l - 1];
@@ -1753,6 +1926,7 @@ int fo_update_with(fo_block *b, double TF, double SF, int TU, int use_store) {
           if (u2[5] >= 0.) *at(q, i, j, k, 6) = u2[5];
           if (u2[6] >= 0.) *at(q, i, j, k, 7) = u2[6];
         }
+        if (sa) *at(q, i, j, k, 6) = fmax2(u2[5], 1.e-12); /* update.f90:474-475 */
       }
   return err;
 }
@@ -2138,7 +2312,7 @@ void fo_find_resnorm(fo_block **bl, int nb, double *out) {
     sc[1] = fl->density_inf * fl->vel_mag;
     sc[2] = sc[3] = sc[4] = fl->density_inf * fl->vel_mag * fl->vel_mag;
     sc[5] = (0.5 * fl->density_inf * (fl->vel_mag * fl->vel_mag * fl->vel_mag) + ((fl->gm / (fl->gm - 1.)) * fl->pressure_inf));
-    sc[6] = fl->density_inf * fl->vel_mag * fl->tk_inf;
+    sc[6] = fl->density_inf * fl->vel_mag * (b->sc.turbulence == FEST_TURB_SA ? fl->tv_inf : fl->tk_inf);
     sc[7] = fl->density_inf * fl->vel_mag * fl->tw_inf;
     V r = vres(b), F = vflux(b, 0), G = vflux(b, 1), H = vflux(b, 2);
     for (int l = 1; l <= n; ++l) {
