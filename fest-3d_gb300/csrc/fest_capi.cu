@@ -221,6 +221,8 @@ void fill_params(fest_handle* h) {
   // get_n_grad (gradients.f90:229-258)
   p.n_grad = s.turbulence == FEST_TURB_NONE ? 4 : s.turbulence == FEST_TURB_SA ? 5 : 6;
   p.sa_cv1_3 = pow(7.1, 3.0);
+  p.kkl_c025 = pow(0.09, 0.25);
+  p.kkl_c075 = pow(0.09, 0.75);
   // setup_bc (bc.f90:48-50)
   p.c2 = 1 + s.accur; p.c3 = 0.5 * s.accur; p.c1 = p.c2 - p.c3;
   const fest_bc& b = h->bc;
@@ -239,6 +241,7 @@ void fill_params(fest_handle* h) {
     p.fix_rho[i] = b.fixed_density[i]; p.fix_p[i] = b.fixed_pressure[i];
     p.fix_u[i] = b.fixed_x_speed[i]; p.fix_v[i] = b.fixed_y_speed[i]; p.fix_w[i] = b.fixed_z_speed[i];
     p.fix_tk[i] = b.fixed_tk[i]; p.fix_tw[i] = b.fixed_tw[i]; p.fix_tv[i] = b.fixed_tv[i];
+    p.fix_tkl[i] = b.fixed_tkl[i];
     p.Tw[i] = b.fixed_wall_temperature[i]; p.Tp[i] = b.fixed_Tpressure[i];
   }
   params_f32(p);
@@ -431,10 +434,10 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
   if (dims->n_var != nv_need) return FEST_ERR_ARG;
   if (scheme->scheme_name < 0 || scheme->scheme_name > 5) return FEST_ERR_ARG;
   if (scheme->interpolant < 0 || scheme->interpolant > 4) return FEST_ERR_ARG;
-  if (scheme->turbulence < 0 || scheme->turbulence > FEST_TURB_SA) return FEST_ERR_ARG;
-  // the implicit integrators' Spalart-Allmaras branches are not built
-  if (scheme->turbulence == FEST_TURB_SA && (scheme->time_step_accuracy == FEST_TIME_IMPLICIT ||
-                                             scheme->time_step_accuracy == FEST_TIME_PLUSGS))
+  if (scheme->turbulence < 0 || scheme->turbulence > FEST_TURB_KKL) return FEST_ERR_ARG;
+  // the implicit integrators' Spalart-Allmaras and k-kL branches are not built
+  if ((scheme->turbulence == FEST_TURB_SA || scheme->turbulence == FEST_TURB_KKL) &&
+      (scheme->time_step_accuracy == FEST_TIME_IMPLICIT || scheme->time_step_accuracy == FEST_TIME_PLUSGS))
     return FEST_ERR_ARG;
   if (scheme->time_step_accuracy < 0 || scheme->time_step_accuracy > FEST_TIME_PLUSGS) return FEST_ERR_ARG;
   if (scheme->time_stepping_method != 'l' && scheme->time_stepping_method != 'g') return FEST_ERR_ARG;
@@ -1014,7 +1017,7 @@ static void resnorm_assemble(const fest_handle* h, const double* sums, double* r
            ((f.gm / (f.gm - 1.)) * f.pressure_inf));
   // resnorm.f90:155-163: the sixth variable's scale is tv_inf's for SA
   sc[6] = f.density_inf * f.vel_mag * (h->sc.turbulence == FEST_TURB_SA ? f.tv_inf : f.tk_inf);
-  sc[7] = f.density_inf * f.vel_mag * f.tw_inf;
+  sc[7] = f.density_inf * f.vel_mag * (h->sc.turbulence == FEST_TURB_KKL ? f.tkl_inf : f.tw_inf);
   res_abs[0] = fabs(sums[0] / sc[0]);
   for (int l = 1; l <= h->p.d.nv; ++l) res_abs[l] = sqrt(sums[l] / (sc[l] * sc[l]));
 }

@@ -34,10 +34,12 @@ struct Params {
   int part_block[6], part_face[6], part_orient[6];
   int self_block;
   double c1, c2, c3;
-  double fix_rho[6], fix_p[6], fix_u[6], fix_v[6], fix_w[6], fix_tk[6], fix_tw[6], fix_tv[6];
+  double fix_rho[6], fix_p[6], fix_u[6], fix_v[6], fix_w[6], fix_tk[6], fix_tw[6], fix_tv[6], fix_tkl[6];
   // Spalart-Allmaras: cv1**3, folded on the host to the correctly rounded
   // power as the reference's compiler folds its parameter
   double sa_cv1_3;
+  // k-kL: cmu**0.25 and cmu**0.75, folded on the host likewise
+  double kkl_c025, kkl_c075;
   double Tw[6], Tp[6];
   // FP32 copies of the constants the FP32 sweep uses (rounded on the host,
   // so the device does no FP64 conversions for them)

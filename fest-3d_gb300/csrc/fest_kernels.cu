@@ -151,6 +151,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
   const long long P = d.P;
   const bool sst = p.turb == FEST_TURB_SST || p.turb == FEST_TURB_SST2003;
   const bool sa = p.turb == FEST_TURB_SA;  // tv: the sixth variable, treated as k is
+  const bool kkl = p.turb == FEST_TURB_KKL;  // k and kL, treated as k is
   const int id = p.id[f];
   switch (id) {
     case -1:
@@ -162,6 +163,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         fix_col(p, q, f, ta, tb, 5, p.fix_p[f]);
         if (sst) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tw[f]); }
         if (sa) fix_col(p, q, f, ta, tb, 6, p.fix_tv[f]);
+        if (kkl) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tkl[f]); }
       }
       break;
     case -2:
@@ -176,6 +178,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         fix_col(p, q, f, ta, tb, 4, p.fix_w[f]);
         if (sst) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tw[f]); }
         if (sa) fix_col(p, q, f, ta, tb, 6, p.fix_tv[f]);
+        if (kkl) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tkl[f]); }
       }
       copy3_col(p, q, f, ta, tb, 5, CP_FLAT);
       break;
@@ -184,6 +187,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       if (iter <= 2) fix_col(p, q, f, ta, tb, 5, p.fix_p[f]);
       if (sst) { copy3_col(p, q, f, ta, tb, 6, CP_FLAT); copy3_col(p, q, f, ta, tb, 7, CP_FLAT); }
       if (sa) copy3_col(p, q, f, ta, tb, 6, CP_FLAT);
+      if (kkl) { copy3_col(p, q, f, ta, tb, 6, CP_FLAT); copy3_col(p, q, f, ta, tb, 7, CP_FLAT); }
       break;
     case -5: {  // wall (bc_primitive.f90:392-402)
       copy3_col(p, q, f, ta, tb, 5, CP_SYMM);
@@ -209,6 +213,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       copy3_col(p, q, f, ta, tb, 3, CP_ANTI);
       copy3_col(p, q, f, ta, tb, 4, CP_ANTI);
       if (sa) copy3_col(p, q, f, ta, tb, 6, CP_ANTI);
+      if (kkl) { copy3_col(p, q, f, ta, tb, 6, CP_ANTI); copy3_col(p, q, f, ta, tb, 7, CP_ANTI); }
       if (sst) {
         copy3_col(p, q, f, ta, tb, 6, CP_ANTI);
         // set_omega_at_wall (bc_primitive.f90:564-643)
@@ -228,6 +233,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       copy3_col(p, q, f, ta, tb, 5, CP_SYMM);
       if (sst) { copy3_col(p, q, f, ta, tb, 6, CP_SYMM); copy3_col(p, q, f, ta, tb, 7, CP_SYMM); }
       if (sa) copy3_col(p, q, f, ta, tb, 6, CP_SYMM);
+      if (kkl) { copy3_col(p, q, f, ta, tb, 6, CP_SYMM); copy3_col(p, q, f, ta, tb, 7, CP_SYMM); }
       int fi, fj, fk;
       bface_ijk(d, f, ta, tb, fi, fj, fk);
       const double* fn = b.faces[f / 2] + 4 * fidx(d, f / 2, fi, fj, fk);
@@ -256,6 +262,12 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         double Ulast = riemann_col(p, b, f, na, nb, false, tp);
         if (Ulast > 0.) copy3_col(p, q, f, ta, tb, 6, CP_FLAT);
         else fix_col(p, q, f, ta, tb, 6, p.fix_tv[f]);
+      }
+      if (kkl) {
+        int na = (f / 2 == 0 ? d.jmx : d.imx) - 1, nb = (f / 2 == 2 ? d.jmx : d.kmx) - 1;
+        double Ulast = riemann_col(p, b, f, na, nb, false, tp);
+        if (Ulast > 0.) { copy3_col(p, q, f, ta, tb, 6, CP_FLAT); copy3_col(p, q, f, ta, tb, 7, CP_FLAT); }
+        else { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tkl[f]); }
       }
     } break;
     default:
@@ -513,6 +525,13 @@ __global__ void k_viscosity(Params p, DevBlock b) {
     b.mu[c0] = p.mu_ref * (pow(T / p.T_ref, 1.5)) * ((p.T_ref + p.S) / (T + p.S));
   }
   if (p.turb == FEST_TURB_NONE) return;
+  if (p.turb == FEST_TURB_KKL) {  // viscosity.f90:469-490
+    const double density = q[c0], tk = q[c0 + 5 * d.P], tkl = q[c0 + 6 * d.P];
+    double m = p.kkl_c025 * density * tkl / (fmax2(sqrt(tk), 1.e-20));
+    if (tkl < 1.e-14 || tk < 1.e-14) m = 0.0;
+    b.mut[c0] = m;
+    return;
+  }
   if (p.turb == FEST_TURB_SA) {  // viscosity.f90:149-160: mu_t = rho tv fv1
     const double tv = q[c0 + 5 * d.P], density = q[c0];
     const double xi = tv * density / b.mu[c0];
@@ -557,6 +576,7 @@ __global__ void k_viscosity_ghost(Params p, DevBlock b) {
   const Dims& d = p.d;
   const int id = p.id[f];
   if (id == -10 || id >= 0 || id == -11 || id < -9) return;
+  if (p.turb == FEST_TURB_KKL && id == -7) return;  // k-kL copies on -1..-4, -6, -8, -9 (viscosity.f90:491-531)
   const double sgn = (id == -5) ? -1.0 : 1.0;
   const int dir = f / 2;
   const int na = (dir == 0 ? d.jmx : d.imx) - 1, nb = (dir == 2 ? d.jmx : d.kmx) - 1;
@@ -638,7 +658,35 @@ __global__ void k_viscous(Params p, DevBlock b, int dir) {
     F[of + 5 * fl.N] = F6;
     bad |= (F6 != F6);
   }
-  if (turb && p.turb != FEST_TURB_SA && !(dir == 2 && d.kmx == 2)) {
+  if (p.turb == FEST_TURB_KKL) {
+    // compute_viscous_fluxes_kkl (viscous.f90:450-567), every direction
+    double H[3][2];
+    for (int c = 0; c < 3; ++c)
+      for (int l = 0; l < 2; ++l) H[c][l] = 0.5 * (b.grad[c][g0 + NG * (4 + l)] + b.grad[c][g1 + NG * (4 + l)]);
+    double dl[2] = {q[c1 + 5 * P] - q[c0 + 5 * P], q[c1 + 6 * P] - q[c0 + 6 * P]};
+    for (int l = 0; l < 2; ++l) {
+      double nc = (dl[l] - (H[0][l] * delx + H[1][l] * dely + H[2][l] * delz)) / dLR;
+      H[0][l] = H[0][l] + (nc * delx / dLR);
+      H[1][l] = H[1][l] + (nc * dely / dLR);
+      H[2][l] = H[2][l] + (nc * delz / dLR);
+    }
+    const double sigma_k = 1.0, sigma_phi = 1.0;
+    const double rhoface = 0.5 * (q[c0] + q[c1]);
+    const double tkface = 0.5 * (q[c0 + 5 * P] + q[c1 + 5 * P]);
+    const double Tk = -2.0 * rhoface * tkface / 3.0;
+    const double dk = H[0][0] * nx + H[1][0] * ny + H[2][0] * nz;
+    const double dkl = H[0][1] * nx + H[1][1] * ny + H[2][1] * nz;
+    F2 = F2 - (Tk * nx * A);
+    F3 = F3 - (Tk * ny * A);
+    F4 = F4 - (Tk * nz * A);
+    F5 = F5 - (A * ((mu_f + sigma_k * mut_f) * dk));
+    const double F6 = F[of + 5 * fl.N] - (A * ((mu_f + sigma_k * mut_f) * dk));
+    const double F7 = F[of + 6 * fl.N] - (A * ((mu_f + sigma_phi * mut_f) * dkl));
+    F[of + 5 * fl.N] = F6;
+    F[of + 6 * fl.N] = F7;
+    bad |= (F6 != F6) || (F7 != F7);
+  }
+  if (turb && p.turb != FEST_TURB_SA && p.turb != FEST_TURB_KKL && !(dir == 2 && d.kmx == 2)) {
     // SST diffusion (viscous.f90:378-444)
     const double sigma_k1 = 0.85, sigma_k2 = 1.0, sigma_w1 = 0.5, sigma_w2 = 0.856;
     double H[3][2];
@@ -740,8 +788,78 @@ __device__ void sa_source(const Params& p, const DevBlock& b, int i, int j, int 
   b.res[o + 5 * N] = b.res[o + 5 * N] - S_v;
 }
 
-// add_source_term_residue (source.f90:94-155): add_sa_source, or
-// add_sst_source (source.f90:158-270)
+// add_kkl_source (source.f90:607-832): production by the Reynolds stress,
+// the von Karman length from the velocity's second derivatives (Green-Gauss
+// sums of the cell gradients over the cell's faces) with its limiters, the
+// wall damping
+__device__ void kkl_source(const Params& p, const DevBlock& b, int i, int j, int k) {
+  const Dims& d = p.d;
+  const long long c0 = pidx(d, i, j, k), og = gidx(d, i, j, k), NG = ngrad(d), P = d.P;
+  const double* q = b.qp;
+  auto G = [&](int c, int l) { return b.grad[c][og + NG * (l - 1)]; };
+  const double density = q[c0], tk = q[c0 + 5 * P], tkl = q[c0 + 6 * P];
+  double S[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < 3; ++c) S[a][c] = 0.5 * (G(c, a + 1) + G(a, c + 1));
+  const double delv = G(0, 1) + G(1, 2) + G(2, 3);
+  const double mt = b.mut[c0];
+  double Pk = 0.;
+  for (int a = 0; a < 3; ++a) {
+    double T[3];
+    for (int c = 0; c < 3; ++c)
+      T[c] = a == c ? mt * (2 * S[a][c] - (2.0 / 3.0) * delv) - (2.0 / 3.0) * density * tk : mt * (2 * S[a][c]);
+    Pk = Pk + T[0] * G(0, a + 1) + T[1] * G(1, a + 1) + T[2] * G(2, a + 1);
+  }
+  const double Dk = p.kkl_c075 * density * (pow(tk, 2.5)) / fmax2(tkl, 1.e-20);
+  Pk = fmin2(Pk, 20 * Dk);
+  const double* fr[6] = {b.faces[0] + 4 * fidx(d, 0, i, j, k), b.faces[1] + 4 * fidx(d, 1, i, j, k),
+                         b.faces[2] + 4 * fidx(d, 2, i, j, k), b.faces[0] + 4 * fidx(d, 0, i + 1, j, k),
+                         b.faces[1] + 4 * fidx(d, 1, i, j + 1, k), b.faces[2] + 4 * fidx(d, 2, i, j, k + 1)};
+  const long long nb[6] = {gidx(d, i - 1, j, k), gidx(d, i, j - 1, k), gidx(d, i, j, k - 1),
+                           gidx(d, i + 1, j, k), gidx(d, i, j + 1, k), gidx(d, i, j, k + 1)};
+  const double vol2 = 2 * b.cells[4 * c0];
+  double lap[3];
+  for (int a = 0; a < 3; ++a) {
+    double sum = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      const double* gr = b.grad[c] + NG * a;
+      const double gc = gr[og];
+      double t = -((gr[nb[0]] + gc) * fr[0][1 + c] * fr[0][0]);
+      for (int f = 1; f < 6; ++f) {
+        const double v = (gr[nb[f]] + gc) * fr[f][1 + c] * fr[f][0];
+        t = f < 3 ? t - v : t + v;
+      }
+      sum = c == 0 ? t / vol2 : sum + t / vol2;
+    }
+    lap[a] = sum;
+  }
+  const double udd = sqrt((lap[0] * lap[0]) + (lap[1] * lap[1]) + (lap[2] * lap[2]));
+  double s2 = S[0][0] * S[0][0];
+  for (int n = 1; n < 9; ++n) s2 = s2 + S[n / 3][n % 3] * S[n / 3][n % 3];
+  const double ud = sqrt(2 * s2);
+  const double kap = 0.41;
+  double Lvk = kap * fabs(ud / fmax2(udd, 1.e-20));
+  const double fp = fmin2(fmax2(Pk / Dk, 0.5), 1.0);
+  const double dd = b.dist[c0], m = b.mu[c0];
+  Lvk = fmax2(Lvk, tkl / fmax2((tk * 10.0), 1.e-20));
+  Lvk = fmin2(Lvk, 1.3 * kap * dd * fp);
+  const double eta = density * dd * sqrt(0.3 * tk) / (20 * m);
+  const double e2 = eta * eta;
+  const double fphi = (1 + 4.7 * eta) / (1 + e2 * e2);
+  const double rr = tkl / fmax2(tk * Lvk, 1.e-20);
+  const double cphi1 = (1.2 - 0.97 * (rr * rr));
+  const double Pkl = cphi1 * tkl * Pk / fmax2(tk, 1.e-20);
+  const double Dkl = 0.13 * density * (pow(tk, 1.5));
+  const double vol = b.cells[4 * c0];
+  const double Sk = (Pk - Dk - 2 * m * tk / (dd * dd)) * vol;
+  const double Skl = (Pkl - Dkl - 6 * m * tkl * fphi / (dd * dd)) * vol;
+  const long long o = cidx(d, i, j, k), N = ncells(d);
+  b.res[o + 5 * N] = b.res[o + 5 * N] - Sk;
+  b.res[o + 6 * N] = b.res[o + 6 * N] - Skl;
+}
+
+// add_source_term_residue (source.f90:94-155): add_sa_source,
+// add_kkl_source, or add_sst_source (source.f90:158-270)
 __global__ void k_source(Params p, DevBlock b) {
   const Dims& d = p.d;
   R3 r = r3(1, d.imx - 1, 1, d.jmx - 1, 1, d.kmx - 1);
@@ -749,6 +867,10 @@ __global__ void k_source(Params p, DevBlock b) {
   if (!decode(r, i, j, k)) return;
   if (p.turb == FEST_TURB_SA) {
     sa_source(p, b, i, j, k);
+    return;
+  }
+  if (p.turb == FEST_TURB_KKL) {
+    kkl_source(p, b, i, j, k);
     return;
   }
   const double sigma_w1 = 0.5, sigma_w2 = 0.856, beta1 = 0.075, beta2 = 0.0828, bstar = 0.09,
@@ -904,6 +1026,15 @@ __global__ void k_update(Params p, DevBlock b, double TF, double SF, int TU, int
     const double rsa = fmin2(u1[5] / (scap * kd2), 10.0);
     const double fw = sa_fw(rsa);
     R[5] = R[5] / (1. + ((-1.0 * u1[0] * kSaCb1 * scap) + (2.0 * u1[0] * sa_cw1() * fw * u1[5] / (dd * dd))) * dtc);
+  } else if (p.turb == FEST_TURB_KKL) {
+    // update.f90:399-404, with the conservative U1(6), U1(7)
+    const double dd = b.dist[c0], m = b.mu[c0];
+    const double eta = u1[0] * dd * (sqrt(0.3 * u1[5]) / (20 * m));
+    const double e2 = eta * eta;
+    const double fphi = (1 + 4.7 * eta) / (1 + e2 * e2);
+    R[5] = R[5] / (1. + ((2.5 * ((p.kkl_c075 * sqrt(u1[0]) * (pow(u1[5], 1.5))) / fmax2(u1[6], 1.e-20))) +
+                         (2 * m / (dd * dd))) * dtc);
+    R[6] = R[6] / (1. + (6 * m * fphi / (dd * dd)) * dtc);
   } else if (p.turb != FEST_TURB_NONE) {
     double F1 = b.F1[c0];
     double beta = 0.075 * F1 + (1. - F1) * 0.0828;

@@ -69,7 +69,10 @@ enum { FEST_TIME_NONE = 0, FEST_TIME_RK2 = 1, FEST_TIME_RK4 = 2,
  * variable tv; viscosity.f90:149-213, viscous.f90:570-656,
  * source.f90:845-983, update.f90:405-420,474-475), FP64 module path
  * (fest_get_next_solution, fest_step with the explicit integrators) */
-enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2, FEST_TURB_SA = 3 };
+/* FEST_TURB_KKL: the k-kL model ('kkl', n_var = 7: k and kL;
+ * viscosity.f90:469-533, viscous.f90:450-567, source.f90:607-832,
+ * update.f90:399-404), FP64 module path as SA */
+enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2, FEST_TURB_SA = 3, FEST_TURB_KKL = 4 };
 enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
 /* MUSCL limiter: the reference hard-codes Koren's alpha family
  * (muscl.f90:151,176); van Albada (muscl.f90:178, commented out there) is an
@@ -97,6 +100,7 @@ typedef struct {            /* flowtype, vartypes.f90:235-286 */
   int mu_variation;         /* FEST_MU_* */
   int reserved;
   double tv_inf;            /* Spalart-Allmaras free-stream tv (state.f90:106-109) */
+  double tkl_inf;           /* k-kL free-stream kL (state.f90:101-103) */
 } fest_flow;
 
 typedef struct {            /* schemetype, vartypes.f90:197-232 */
@@ -145,6 +149,8 @@ typedef struct {            /* boundarytype, vartypes.f90:289-367 */
   int partner_orient[6];
   /* fixed tv of each face for Spalart-Allmaras blocks (read_bc.f90:112-115) */
   double fixed_tv[6];
+  /* fixed kL of each face for k-kL blocks (read_bc.f90) */
+  double fixed_tkl[6];
 } fest_bc;
 
 typedef struct fest_handle fest_handle;

@@ -32,6 +32,12 @@ static inline double pow6(double x) {
   return x4 * x2;
 }
 
+/* ---- k-kL constants (global/global_kkl.f90); cmu**0.25 and cmu**0.75
+ * are the correctly rounded powers a compiler folds them to */
+static const double kkl_zeta1 = 1.2, kkl_zeta2 = 0.97, kkl_zeta3 = 0.13, kkl_sigma_k = 1.0,
+                    kkl_sigma_phi = 1.0, kkl_cmu = 0.09, kkl_kappa = 0.41, kkl_c11 = 10.0, kkl_c12 = 1.3,
+                    kkl_cd1 = 4.7;
+
 struct fo_block {
   fest_extent d;
   fest_flow flow;
@@ -445,6 +451,7 @@ static int is_sst(const fo_block *b) {
   return b->sc.turbulence == FEST_TURB_SST || b->sc.turbulence == FEST_TURB_SST2003;
 }
 static int is_sa(const fo_block *b) { return b->sc.turbulence == FEST_TURB_SA; }
+static int is_kkl(const fo_block *b) { return b->sc.turbulence == FEST_TURB_KKL; }
 static int is_turb(const fo_block *b) { return b->sc.turbulence != FEST_TURB_NONE; }
 
 /* bc_primitive.f90:1778-1945 temp_based_density */
@@ -608,6 +615,10 @@ static void riemann_face(fo_block *b, int f, int total_pressure) {
     if (last_positive) copy3(b, 6, CP_FLAT, f);
     else fixv(b, 6, b->bc.fixed_tv[f], f);
   }
+  if (is_kkl(b) && na > 0 && nb > 0) {
+    if (last_positive) { copy3(b, 6, CP_FLAT, f); copy3(b, 7, CP_FLAT, f); }
+    else { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tkl[f], f); }
+  }
   /* plane copy of layer 1 into layers 2 and 3, all tangential indices */
   int imx = IMX, jmx = JMX, kmx = KMX;
   for (int l = 1; l <= NV; ++l)
@@ -760,7 +771,7 @@ static void corners(fo_block *b) {
 
 /* bc_primitive.f90:55-226 populate_ghost_primitive */
 int fo_populate_ghost_primitive(fo_block *b, int it) {
-  int sst = is_sst(b), sa = is_sa(b);
+  int sst = is_sst(b), sa = is_sa(b), kkl = is_kkl(b);
   for (int f = 0; f < 6; ++f) {
     switch (b->bc.id[f]) {
     case -1: /* supersonic_inlet */
@@ -772,6 +783,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
         fixv(b, 5, b->bc.fixed_pressure[f], f);
         if (sst) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tw[f], f); }
         if (sa) fixv(b, 6, b->bc.fixed_tv[f], f);
+        if (kkl) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tkl[f], f); }
       }
       break;
     case -2: /* supersonic_outlet */
@@ -786,6 +798,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
         fixv(b, 4, b->bc.fixed_z_speed[f], f);
         if (sst) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tw[f], f); }
         if (sa) fixv(b, 6, b->bc.fixed_tv[f], f);
+        if (kkl) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tkl[f], f); }
       }
       copy3(b, 5, CP_FLAT, f);
       break;
@@ -794,6 +807,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
       if (it <= 2) fixv(b, 5, b->bc.fixed_pressure[f], f);
       if (sst) { copy3(b, 6, CP_FLAT, f); copy3(b, 7, CP_FLAT, f); }
       if (sa) copy3(b, 6, CP_FLAT, f);
+      if (kkl) { copy3(b, 6, CP_FLAT, f); copy3(b, 7, CP_FLAT, f); }
       break;
     case -5: /* wall: pressure symm, temp_based_density, no_slip */
       copy3(b, 5, CP_SYMM, f);
@@ -803,12 +817,14 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
       copy3(b, 4, CP_ANTI, f);
       if (sst) { copy3(b, 6, CP_ANTI, f); set_omega_at_wall(b, f); }
       if (sa) copy3(b, 6, CP_ANTI, f);
+      if (kkl) { copy3(b, 6, CP_ANTI, f); copy3(b, 7, CP_ANTI, f); }
       break;
     case -6: /* slip_wall */
       copy3(b, 1, CP_SYMM, f);
       copy3(b, 5, CP_SYMM, f);
       if (sst) { copy3(b, 6, CP_SYMM, f); copy3(b, 7, CP_SYMM, f); }
       if (sa) copy3(b, 6, CP_SYMM, f);
+      if (kkl) { copy3(b, 6, CP_SYMM, f); copy3(b, 7, CP_SYMM, f); }
       flow_tangency(b, f);
       break;
     case -8: riemann_face(b, f, 0); break;
@@ -1389,7 +1405,7 @@ int fo_evaluate_all_gradients(fo_block *b) {
     gradient_G(b, g[c], 4, T, 1, c);
   }
   if (KMX <= 2) memset(b->a[FO_GZ], 0, sizeof(double) * (size_t)b->sz[FO_GZ]);
-  if (is_sst(b))
+  if (is_sst(b) || is_kkl(b))  /* gradtk, gradtw / gradtkl (gradients.f90:171-200) */
     for (int c = 0; c < ncomp; ++c) {
       gradient_G(b, g[c], 5, q, 6, c);
       gradient_G(b, g[c], 6, q, 7, c);
@@ -1439,6 +1455,40 @@ int fo_calculate_viscosity(fo_block *b) {
       double sgn;
       if (id == -5) sgn = -1.0;
       else if (id >= -9 && id <= -1) sgn = 1.0;
+      else continue;
+      int na, nb;
+      tang_range(b, f, &na, &nb);
+      for (int tb = 1; tb <= nb; ++tb)
+        for (int ta = 1; ta <= na; ++ta) {
+          int gi, gj, gk, ii, ij, ik;
+          ghost_ijk(b, f, 1, ta, tb, &gi, &gj, &gk);
+          inner_ijk(b, f, 1, ta, tb, &ii, &ij, &ik);
+          *at(mut, gi, gj, gk, 1) = sgn < 0 ? -*at(mut, ii, ij, ik, 1) : *at(mut, ii, ij, ik, 1);
+        }
+    }
+    for (long p = 0; p < b->sz[FO_MU]; ++p)
+      if (b->a[FO_MU][p] != b->a[FO_MU][p]) return FEST_ERR_NAN;
+    return FEST_OK;
+  }
+  if (is_kkl(b)) {
+    /* viscosity.f90:469-533: mu_t = cmu^0.25 rho kL / max(sqrt(k), 1e-20),
+     * zero where k or kL is below 1e-14 */
+    double c = pow(kkl_cmu, 0.25);
+    OMP_FOR
+    for (int k = 0; k <= KMX; ++k)
+      for (int j = 0; j <= JMX; ++j)
+        for (int i = 0; i <= IMX; ++i) {
+          double density = *at(q, i, j, k, 1), tk = *at(q, i, j, k, 6), tkl = *at(q, i, j, k, 7);
+          double m = c * density * tkl / (fmax2(sqrt(tk), 1.e-20));
+          if (tkl < 1.e-14 || tk < 1.e-14) m = 0.0;
+          *at(mut, i, j, k, 1) = m;
+        }
+    /* ghost copies: faces -1..-4, -6, -8, -9 copy layer 1, the wall negates it */
+    for (int f = 0; f < 6; ++f) {
+      int id = b->bc.id[f];
+      double sgn;
+      if (id == -5) sgn = -1.0;
+      else if ((id >= -4 && id <= -1) || id == -6 || id == -8 || id == -9) sgn = 1.0;
       else continue;
       int na, nb;
       tang_range(b, f, &na, &nb);
@@ -1646,8 +1696,52 @@ static void viscous_sa(fo_block *b, int dir) {
       }
 }
 
+/* viscous.f90:450-567 compute_viscous_fluxes_kkl */
+static void viscous_kkl(fo_block *b, int dir) {
+  V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), Fl = vflux(b, dir);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
+  R4 fa = vfaces(b, dir), cl = vcells(b);
+  int ii = dir == 0, jj = dir == 1, kk = dir == 2;
+  OMP_FOR
+  for (int k = 1; k <= KMX - 1 + kk; ++k)
+    for (int j = 1; j <= JMX - 1 + jj; ++j)
+      for (int i = 1; i <= IMX - 1 + ii; ++i) {
+        int im = i - ii, jm = j - jj, km = k - kk;
+        double G[3][2];
+        for (int c = 0; c < 3; ++c)
+          for (int l = 0; l < 2; ++l) G[c][l] = 0.5 * (*at(g[c], im, jm, km, 5 + l) + *at(g[c], i, j, k, 5 + l));
+        const double *c1 = r4(cl, i, j, k), *c0 = r4(cl, im, jm, km);
+        double delx = c1[1] - c0[1], dely = c1[2] - c0[2], delz = c1[3] - c0[3];
+        double d_LR = sqrt(delx * delx + dely * dely + delz * delz);
+        double del[2] = {*at(q, i, j, k, 6) - *at(q, im, jm, km, 6), *at(q, i, j, k, 7) - *at(q, im, jm, km, 7)};
+        for (int l = 0; l < 2; ++l) {
+          double nc = (del[l] - (G[0][l] * delx + G[1][l] * dely + G[2][l] * delz)) / d_LR;
+          G[0][l] = G[0][l] + (nc * delx / d_LR);
+          G[1][l] = G[1][l] + (nc * dely / d_LR);
+          G[2][l] = G[2][l] + (nc * delz / d_LR);
+        }
+        double mu_f = 0.5 * (*at(mu, im, jm, km, 1) + *at(mu, i, j, k, 1));
+        double mut_f = 0.5 * (*at(mut, im, jm, km, 1) + *at(mut, i, j, k, 1));
+        double rhoface = 0.5 * (*at(q, im, jm, km, 1) + *at(q, i, j, k, 1));
+        double tkface = 0.5 * (*at(q, im, jm, km, 6) + *at(q, i, j, k, 6));
+        double Tau_xx = -2.0 * rhoface * tkface / 3.0;
+        const double *fc = r4(fa, i, j, k);
+        double nx = fc[1], ny = fc[2], nz = fc[3], area = fc[0];
+        double dk = G[0][0] * nx + G[1][0] * ny + G[2][0] * nz;
+        double dkl = G[0][1] * nx + G[1][1] * ny + G[2][1] * nz;
+        *at(Fl, i, j, k, 2) = *at(Fl, i, j, k, 2) - (Tau_xx * nx * area);
+        *at(Fl, i, j, k, 3) = *at(Fl, i, j, k, 3) - (Tau_xx * ny * area);
+        *at(Fl, i, j, k, 4) = *at(Fl, i, j, k, 4) - (Tau_xx * nz * area);
+        *at(Fl, i, j, k, 5) = *at(Fl, i, j, k, 5) - (area * ((mu_f + kkl_sigma_k * mut_f) * dk));
+        *at(Fl, i, j, k, 6) = *at(Fl, i, j, k, 6) - (area * ((mu_f + kkl_sigma_k * mut_f) * dk));
+        *at(Fl, i, j, k, 7) = *at(Fl, i, j, k, 7) - (area * ((mu_f + kkl_sigma_phi * mut_f) * dkl));
+      }
+}
+
 int fo_compute_viscous_fluxes(fo_block *b) {
   for (int dir = 0; dir < 3; ++dir) viscous_laminar(b, dir);
+  if (is_kkl(b))
+    for (int dir = 0; dir < 3; ++dir) viscous_kkl(b, dir);
   if (is_sa(b))
     for (int dir = 0; dir < 3; ++dir) viscous_sa(b, dir);
   if (is_sst(b)) {
@@ -1714,10 +1808,93 @@ static void sa_source(fo_block *b) {
       }
 }
 
-/* source.f90:94-155 add_source_term_residue: the SA and SST sources */
+/* source.f90:607-832 add_kkl_source: production by the Reynolds stress,
+ * the von Karman length from the velocity's second derivatives (Green-Gauss
+ * sums of the gradients over the cell's faces) with its limiters, and the
+ * wall damping */
+static void kkl_source(fo_block *b) {
+  V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), dist = vpad(b, FO_DIST), r = vres(b);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
+  R4 If = vfaces(b, 0), Jf = vfaces(b, 1), Kf = vfaces(b, 2), cl = vcells(b);
+  const double c075 = pow(kkl_cmu, 0.75);
+  OMP_FOR
+  for (int k = 1; k <= KMX - 1; ++k)
+    for (int j = 1; j <= JMX - 1; ++j)
+      for (int i = 1; i <= IMX - 1; ++i) {
+#define GR(c, l) (*at(g[c], i, j, k, l))
+        double density = *at(q, i, j, k, 1), tk = *at(q, i, j, k, 6), tkl = *at(q, i, j, k, 7);
+        /* S(a, b) = (d u_a / d x_b + d u_b / d x_a) / 2 */
+        double S[3][3];
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < 3; ++c) S[a][c] = 0.5 * (GR(c, a + 1) + GR(a, c + 1));
+        double delv = GR(0, 1) + GR(1, 2) + GR(2, 3);
+        double mt = *at(mut, i, j, k, 1);
+        double Tau[3][3];
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < 3; ++c)
+            Tau[a][c] = a == c ? mt * (2 * S[a][c] - (2.0 / 3.0) * delv) - (2.0 / 3.0) * density * tk
+                               : mt * (2 * S[a][c]);
+        double P_k = 0.;
+        for (int a = 0; a < 3; ++a)
+          P_k = P_k + Tau[a][0] * GR(0, a + 1) + Tau[a][1] * GR(1, a + 1) + Tau[a][2] * GR(2, a + 1);
+        double D_k = c075 * density * (pow(tk, 2.5)) / fmax2(tkl, 1.e-20);
+        P_k = fmin2(P_k, 20 * D_k);
+        /* second derivatives d2(u_a)/d(x_c)2 */
+        const double *fr[6] = {r4(If, i, j, k), r4(Jf, i, j, k), r4(Kf, i, j, k),
+                               r4(If, i + 1, j, k), r4(Jf, i, j + 1, k), r4(Kf, i, j, k + 1)};
+        const int nb[6][3] = {{i - 1, j, k}, {i, j - 1, k}, {i, j, k - 1}, {i + 1, j, k}, {i, j + 1, k}, {i, j, k + 1}};
+        double vol2 = 2 * r4(cl, i, j, k)[0];
+        double lap[3];
+        for (int a = 0; a < 3; ++a) {
+          double sum = 0.0;
+          for (int c = 0; c < 3; ++c) {
+            double gc = *at(g[c], i, j, k, a + 1);
+            double t = -((*at(g[c], nb[0][0], nb[0][1], nb[0][2], a + 1) + gc) * fr[0][1 + c] * fr[0][0]);
+            for (int f = 1; f < 6; ++f) {
+              double v = (*at(g[c], nb[f][0], nb[f][1], nb[f][2], a + 1) + gc) * fr[f][1 + c] * fr[f][0];
+              t = f < 3 ? t - v : t + v;
+            }
+            sum = c == 0 ? t / vol2 : sum + t / vol2;
+          }
+          lap[a] = sum;
+        }
+        double udd = sqrt((lap[0] * lap[0]) + (lap[1] * lap[1]) + (lap[2] * lap[2]));
+        double s2 = 0.0;
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < 3; ++c) s2 = (a == 0 && c == 0) ? S[0][0] * S[0][0] : s2 + S[a][c] * S[a][c];
+        double ud = sqrt(2 * s2);
+        double Lvk = kkl_kappa * fabs(ud / fmax2(udd, 1.e-20));
+        double fp = fmin2(fmax2(P_k / D_k, 0.5), 1.0);
+        double d = *at(dist, i, j, k, 1), m = *at(mu, i, j, k, 1);
+        Lvk = fmax2(Lvk, tkl / fmax2((tk * kkl_c11), 1.e-20));
+        Lvk = fmin2(Lvk, kkl_c12 * kkl_kappa * d * fp);
+        double eta = density * d * sqrt(0.3 * tk) / (20 * m);
+        double e2 = eta * eta;
+        double fphi = (1 + kkl_cd1 * eta) / (1 + e2 * e2);
+        double cphi2 = kkl_zeta3;
+        double rr = tkl / fmax2(tk * Lvk, 1.e-20);
+        double cphi1 = (kkl_zeta1 - kkl_zeta2 * (rr * rr));
+        double P_kl = cphi1 * tkl * P_k / fmax2(tk, 1.e-20);
+        double D_kl = cphi2 * density * (pow(tk, 1.5));
+        double S_k = P_k - D_k - 2 * m * tk / (d * d);
+        double S_kl = P_kl - D_kl - 6 * m * tkl * fphi / (d * d);
+        double vol = r4(cl, i, j, k)[0];
+        S_k = S_k * vol;
+        S_kl = S_kl * vol;
+        *at(r, i, j, k, 6) = *at(r, i, j, k, 6) - S_k;
+        *at(r, i, j, k, 7) = *at(r, i, j, k, 7) - S_kl;
+#undef GR
+      }
+}
+
+/* source.f90:94-155 add_source_term_residue: the SA, k-kL and SST sources */
 void fo_add_source_term_residue(fo_block *b) {
   if (is_sa(b)) {
     sa_source(b);
+    return;
+  }
+  if (is_kkl(b)) {
+    kkl_source(b);
     return;
   }
   if (!is_sst(b)) return;
@@ -1860,7 +2037,7 @@ int fo_update_with(fo_block *b, double TF, double SF, int TU, int use_store) {
   V Rn = mkv(b->a[FO_RSTORE], 1, 1, 1, IMX - 1, JMX - 1, KMX - 1);
   R4 cl = vcells(b);
   double gm = b->flow.gm;
-  int n = NV, sst = is_sst(b), sa = is_sa(b);
+  int n = NV, sst = is_sst(b), sa = is_sa(b), kkl = is_kkl(b);
   V mu = vpad(b, FO_MU), dist = vpad(b, FO_DIST);
   V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
   int err = FEST_OK;
@@ -1881,6 +2058,16 @@ int fo_update_with(fo_block *b, double TF, double SF, int TU, int use_store) {
           double w = *at(q, i, j, k, 7);
           R[5] = R[5] / (1 + (beta * w * dtc));
           R[6] = R[6] / (1 + (2 * beta * w * dtc));
+        }
+        if (kkl) {
+          /* update.f90:399-404, with the conservative U1(6), U1(7) */
+          double d = *at(dist, i, j, k, 1), m = *at(mu, i, j, k, 1);
+          double eta = u1[0] * d * (sqrt(0.3 * u1[5]) / (20 * m));
+          double e2 = eta * eta;
+          double fphi = (1 + kkl_cd1 * eta) / (1 + e2 * e2);
+          R[5] = R[5] / (1. + ((2.5 * ((pow(kkl_cmu, 0.75) * sqrt(u1[0]) * (pow(u1[5], 1.5))) / fmax2(u1[6], 1.e-20))) +
+                               (2 * m / (d * d))) * dtc);
+          R[6] = R[6] / (1. + (6 * m * fphi / (d * d)) * dtc);
         }
         if (sa) {
           /* update.f90:405-419: xi from the conservative U1(6) and the
@@ -1922,7 +2109,7 @@ int fo_update_with(fo_block *b, double TF, double SF, int TU, int use_store) {
           continue;
         }
         for (int l = 1; l <= 5; ++l) *at(q, i, j, k, l) = u2[l - 1];
-        if (sst) {
+        if (sst || kkl) { /* update.f90:456-470 */
           if (u2[5] >= 0.) *at(q, i, j, k, 6) = u2[5];
           if (u2[6] >= 0.) *at(q, i, j, k, 7) = u2[6];
         }
@@ -2313,7 +2500,7 @@ void fo_find_resnorm(fo_block **bl, int nb, double *out) {
     sc[2] = sc[3] = sc[4] = fl->density_inf * fl->vel_mag * fl->vel_mag;
     sc[5] = (0.5 * fl->density_inf * (fl->vel_mag * fl->vel_mag * fl->vel_mag) + ((fl->gm / (fl->gm - 1.)) * fl->pressure_inf));
     sc[6] = fl->density_inf * fl->vel_mag * (b->sc.turbulence == FEST_TURB_SA ? fl->tv_inf : fl->tk_inf);
-    sc[7] = fl->density_inf * fl->vel_mag * fl->tw_inf;
+    sc[7] = fl->density_inf * fl->vel_mag * (b->sc.turbulence == FEST_TURB_KKL ? fl->tkl_inf : fl->tw_inf);
     V r = vres(b), F = vflux(b, 0), G = vflux(b, 1), H = vflux(b, 2);
     for (int l = 1; l <= n; ++l) {
       double s = 0.0;

@@ -86,22 +86,25 @@ def assert_residual(gpu_res, blk, rtol=RTOL, what="residue"):
 
 def small_case(nc=(9, 7, 6), ids=(-5, -5, -5, -3, -10, -10), scheme_kw=None, flow_kw=None,
                turb=False, perturb=0.15, seed=1, partners=None, fixed=None, state_mach=0.3):
-    # turb: False, True (k-omega SST, seven variables) or "sa" (six)
-    sa = turb == "sa"
+    # turb: False, True (k-omega SST, seven variables), "sa" (six) or
+    # "kkl" (seven: k and kL)
+    sa, kkl = turb == "sa", turb == "kkl"
     ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 6 if sa else 7 if turb else 5)
     fk = dict(density_inf=1.2, x_speed_inf=60.0, y_speed_inf=5.0, pressure_inf=101325.0)
     if sa:
         fk["tv_inf"] = 1.2e-4
+    if kkl:
+        fk["tk_inf"], fk["tkl_inf"] = 1.0, 2e-3
     fk.update(flow_kw or {})
     flow = abi.make_flow(**fk)
     sk = dict(scheme_name="ausm", interpolant="muscl")
     if turb:
-        sk["turbulence"] = "sa" if sa else "sst"
+        sk["turbulence"] = "sa" if sa else "kkl" if kkl else "sst"
     sk.update(scheme_kw or {})
     scheme = abi.make_scheme(**sk)
     fx = {k: [0.0] * 6 for k in ("fixed_density", "fixed_x_speed", "fixed_y_speed",
                                  "fixed_z_speed", "fixed_pressure", "fixed_tk", "fixed_tw",
-                                 "fixed_wall_temperature", "fixed_Tpressure", "fixed_tv")}
+                                 "fixed_wall_temperature", "fixed_Tpressure", "fixed_tv", "fixed_tkl")}
     for f in range(6):
         fx["fixed_density"][f] = 1.15 + 0.01 * f
         fx["fixed_x_speed"][f] = 40.0 + f
@@ -112,6 +115,7 @@ def small_case(nc=(9, 7, 6), ids=(-5, -5, -5, -3, -10, -10), scheme_kw=None, flo
         fx["fixed_tw"][f] = 900.0 + 10 * f
         fx["fixed_Tpressure"][f] = 104000.0 + 50 * f
         fx["fixed_tv"][f] = 1.1e-4 + 1e-6 * f
+        fx["fixed_tkl"][f] = 1.9e-3 + 2e-5 * f
     for k, v in (fixed or {}).items():
         fx[k] = list(v)
     if partners is None:
@@ -121,5 +125,5 @@ def small_case(nc=(9, 7, 6), ids=(-5, -5, -5, -3, -10, -10), scheme_kw=None, flo
                 partners[f] = (0, f ^ 1)
     bc = abi.make_bc(list(ids), partners=partners, **fx)
     nodes = cases.box_nodes(ext, L=(1.0, 0.8, 0.6), perturb=perturb, seed=seed)
-    qp = cases.random_state(ext, seed=seed + 7, mach=state_mach)
+    qp = cases.random_state(ext, seed=seed + 7, mach=state_mach, tw=2e-3 if kkl else 1000.0)
     return ext, flow, scheme, bc, nodes, qp

@@ -135,3 +135,22 @@ def test_iterate_follows_the_reference_checkpoint_schedule(max_iters, every, fir
         i = h.log.index(("begin", a))
         assert h.log[i + 1][0] == "step" and h.log[i + 2] == ("wait",)
     assert np.all(np.isfinite([v for _, v in got]))
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every field of fest_extent, fest_flow, fest_scheme and fest_bc sits
+    at the same offset in the ctypes mirrors as the C compiler places it
+    from include/fest_gpu.h (tests/abi_layout.c prints the C side)."""
+    import subprocess
+    exe = tmp_path / "abi_layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "abi_layout.c"), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                              text=True).stdout.split("\n") if line)
+    want = {}
+    for T, n in ((abi.Extent, "fest_extent"), (abi.Flow, "fest_flow"), (abi.Scheme, "fest_scheme"),
+                 (abi.BC, "fest_bc")):
+        want[n] = str(C.sizeof(T))
+        for f, _ in T._fields_:
+            want[f"{n}.{f}"] = str(getattr(T, f).offset)
+    assert got == want
