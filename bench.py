@@ -658,6 +658,10 @@ def run_ours(args):
                      "roofline": fp64_roof, "clocks": fp64["clocks"]},
             "mixed_over_fp64": rate(mixed) / rate(fp64),
             "wall_cp_abs_err_mixed_vs_fp64": cp_err,
+            "wall_cp_compare": {"iterations": int(mixed["it"] + prof_steps - 1),
+                                "note": "mixed and FP64 after the same number of iterations from the "
+                                        "uniform start, mid-transient; the converged comparison is "
+                                        "bench.py --converged"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_stage<float> (fused WENO5+SLAU sweep + update)",
