@@ -1427,6 +1427,7 @@ long long vjp_grad_work_doubles(const Dims& d, bool sst) {
 bool vjp_supported(const Params& p) {
   // no model or k-omega SST (the other models have no residual VJP)
   if (p.turb != FEST_TURB_NONE && p.turb != FEST_TURB_SST && p.turb != FEST_TURB_SST2003) return false;
+  if (p.transition != FEST_TRANSITION_NONE) return false;
   const bool sst = p.turb != FEST_TURB_NONE;
   if (p.d.nv != (sst ? 7 : 5)) return false;
   if (sst) {

@@ -223,6 +223,14 @@ void fill_params(fest_handle* h) {
   p.sa_cv1_3 = pow(7.1, 3.0);
   p.kkl_c025 = pow(0.09, 0.25);
   p.kkl_c075 = pow(0.09, 0.75);
+  // the free-stream Reynolds number per unit length (state.f90:89) and
+  // the 'bc' model's constants of it and of Tu (source.f90:576-581)
+  p.transition = s.transition;
+  if (s.transition == FEST_TRANSITION_BC) {
+    const double Re = f.density_inf * f.vel_mag * 1.0 / f.mu_ref;
+    p.bc_nu_cr = 5.0 / Re;
+    p.bc_re_theta_t = (803.73 * (pow((f.tu_inf + 0.6067), (-1.027))));
+  }
   // setup_bc (bc.f90:48-50)
   p.c2 = 1 + s.accur; p.c3 = 0.5 * s.accur; p.c1 = p.c2 - p.c3;
   const fest_bc& b = h->bc;
@@ -440,6 +448,13 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
       (scheme->time_step_accuracy == FEST_TIME_IMPLICIT || scheme->time_step_accuracy == FEST_TIME_PLUSGS))
     return FEST_ERR_ARG;
   if (scheme->time_step_accuracy < 0 || scheme->time_step_accuracy > FEST_TIME_PLUSGS) return FEST_ERR_ARG;
+  // the 'bc' transition model replaces the SA or SST source only
+  // (source.f90:124-143; the implicit integrators update SST-BC as SST,
+  // lusgs.f90:161-164); lctm2015 is not built
+  if (scheme->transition != FEST_TRANSITION_NONE && scheme->transition != FEST_TRANSITION_BC) return FEST_ERR_ARG;
+  if (scheme->transition == FEST_TRANSITION_BC &&
+      (scheme->turbulence == FEST_TURB_NONE || scheme->turbulence == FEST_TURB_KKL || flow->mu_ref <= 0.0))
+    return FEST_ERR_ARG;
   if (scheme->time_stepping_method != 'l' && scheme->time_stepping_method != 'g') return FEST_ERR_ARG;
   for (int f = 0; f < 6; ++f) {
     if (!valid_id(bc->id[f])) return FEST_ERR_ARG;

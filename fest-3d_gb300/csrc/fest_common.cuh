@@ -40,6 +40,11 @@ struct Params {
   double sa_cv1_3;
   // k-kL: cmu**0.25 and cmu**0.75, folded on the host likewise
   double kkl_c025, kkl_c075;
+  // the 'bc' transition model (FEST_TRANSITION_*): its critical eddy
+  // viscosity 5/Re and transition Reynolds number 803.73 (Tu + 0.6067)**-1.027,
+  // both uniform, taken on the host
+  int transition;
+  double bc_nu_cr, bc_re_theta_t;
   double Tw[6], Tp[6];
   // FP32 copies of the constants the FP32 sweep uses (rounded on the host,
   // so the device does no FP64 conversions for them)

@@ -456,7 +456,9 @@ bool fused_supported(const Params& p, int precision) {
   const bool mixed = precision == FEST_MIXED;
   const bool small_enough = (long long)p.d.P * p.d.nv < (1ll << 31);
   const bool sst = p.turb == FEST_TURB_SST || p.turb == FEST_TURB_SST2003;
-  const bool model = p.turb == FEST_TURB_NONE ? p.d.nv == 5 : (sst && p.mu_ref != 0.0 && p.d.nv == 7);
+  const bool model = p.turb == FEST_TURB_NONE ? p.d.nv == 5
+                                               : (sst && p.mu_ref != 0.0 && p.d.nv == 7 &&
+                                                  p.transition == FEST_TRANSITION_NONE);
   // the TVD integrators blend ghosts between fills, which order-dependent
   // directions would read; they take the module path
   const bool tvd = p.integ == FEST_TIME_TVDRK2 || p.integ == FEST_TIME_TVDRK3;

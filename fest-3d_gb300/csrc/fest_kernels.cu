@@ -741,9 +741,22 @@ __global__ void k_residue(Params p, DevBlock b) {
                        (b.flux[2][oz1 + fz.N * l] - b.flux[2][oz0 + fz.N * l]);
 }
 
+// the 'bc' transition model's intermittency (source.f90:571-589 and
+// 1159-1170) from the momentum-thickness Reynolds number re_v / 2.193
+// against its transition value and the eddy viscosity against its critical
+// value
+__device__ __forceinline__ double gamma_bc(const Params& p, double re_v, double nu_bc) {
+  const double re_theta = re_v / 2.193;
+  const double term1 = sqrt(fmax2(re_theta - p.bc_re_theta_t, 0.) / (0.002 * p.bc_re_theta_t));
+  const double term2 = sqrt(fmax2(nu_bc - p.bc_nu_cr, 0.0) / p.bc_nu_cr);
+  return 1.0 - exp(-(term1 + term2));
+}
+
 // add_sa_source (source.f90:845-983): the density gradient from the cell's
 // six face sums, whose k faces' normal reads (nx, nx, nx) as the reference
-// does (source.f90:913)
+// does (source.f90:913).  With the 'bc' transition model, add_saBC_source
+// (source.f90:985-1194): S-hat floored at 1e-10 instead of 0.3 Omega, the
+// production scaled by the intermittency and, as there, not by density
 __device__ void sa_source(const Params& p, const DevBlock& b, int i, int j, int k) {
   const Dims& d = p.d;
   const long long c0 = pidx(d, i, j, k), og = gidx(d, i, j, k), NG = ngrad(d), P = d.P;
@@ -776,6 +789,23 @@ __device__ void sa_source(const Params& p, const DevBlock& b, int i, int j, int 
   const double x3 = xi * xi * xi;
   const double fv1 = x3 / (x3 + p.sa_cv1_3);
   const double fv2 = 1.0 - xi / (1.0 + (xi * fv1));
+  const long long o = cidx(d, i, j, k), N = ncells(d);
+  if (p.transition == FEST_TRANSITION_BC) {
+    const double u = q[c0 + P], v = q[c0 + 2 * P], w = q[c0 + 3 * P];
+    const double vmag = sqrt(u * u + v * v + w * w);
+    const double d2 = dd * dd;
+    const double inv_k2_d2 = 1.0 / ((kSaKappa * kSaKappa) * d2);
+    const double Shat = fmax2(vort + tv * fv2 * inv_k2_d2, 1.0e-10);
+    const double inv_Shat = 1.0 / Shat;
+    const double nu_bc = (tv * fv1) / (vmag * dd);
+    const double re_v = d2 * vort / nu;
+    const double Prod = gamma_bc(p, re_v, nu_bc) * kSaCb1 * Shat * tv * vol;
+    const double fw = sa_fw(fmin2(tv * inv_Shat * inv_k2_d2, 10.0));
+    const double Dest = (sa_cw1() * fw * tv * tv / d2) * (vol);
+    const double lam = (density * CD1 / kSaSigma - CD2 * (nu + tv) / kSaSigma) * vol;
+    b.res[o + 5 * N] = b.res[o + 5 * N] - (Prod - Dest + lam);
+    return;
+  }
   const double Scap = fmax2(vort + (tv * fv2 / (kd2)), 0.3 * vort);
   const double rr = fmin2(tv / (Scap * kd2), 10.0);
   const double fw = sa_fw(rr);
@@ -784,7 +814,6 @@ __device__ void sa_source(const Params& p, const DevBlock& b, int i, int j, int 
   const double P_v = density * kSaCb1 * Scap * tv;
   const double lamda = density * CD1 / kSaSigma - CD2 * (nu + tv) / kSaSigma;
   const double S_v = (P_v - D_v + lamda) * vol;
-  const long long o = cidx(d, i, j, k), N = ncells(d);
   b.res[o + 5 * N] = b.res[o + 5 * N] - S_v;
 }
 
@@ -858,8 +887,11 @@ __device__ void kkl_source(const Params& p, const DevBlock& b, int i, int j, int
   b.res[o + 6 * N] = b.res[o + 6 * N] - Skl;
 }
 
-// add_source_term_residue (source.f90:94-155): add_sa_source,
-// add_kkl_source, or add_sst_source (source.f90:158-270)
+// add_source_term_residue (source.f90:94-155): add_sa_source (or
+// add_saBC_source), add_kkl_source, or add_sst_source (source.f90:158-270;
+// or add_sst_bc_source, source.f90:467-604: production mu_t Omega^2 limited
+// by 20 D_k, P_w from it before the intermittency scales it, the cross
+// diffusion unfloored, the SST constants whatever the variant)
 __global__ void k_source(Params p, DevBlock b) {
   const Dims& d = p.d;
   R3 r = r3(1, d.imx - 1, 1, d.jmx - 1, 1, d.kmx - 1);
@@ -875,9 +907,10 @@ __global__ void k_source(Params p, DevBlock b) {
   }
   const double sigma_w1 = 0.5, sigma_w2 = 0.856, beta1 = 0.075, beta2 = 0.0828, bstar = 0.09,
                kap = 0.41;
+  const bool bc = p.transition == FEST_TRANSITION_BC;
   int limiter;
   double gama1, gama2;
-  if (p.turb == FEST_TURB_SST2003) {
+  if (p.turb == FEST_TURB_SST2003 && !bc) {
     limiter = 10; gama1 = 5.0 / 9.0; gama2 = 0.44;
   } else {
     limiter = 20;
@@ -891,7 +924,7 @@ __global__ void k_source(Params p, DevBlock b) {
   double a = G(1, 3) - G(2, 2), bb = G(2, 1) - G(0, 3), c = G(0, 2) - G(1, 1);
   double vort = sqrt(((a * a) + (bb * bb) + (c * c)));
   double CD = 2 * rho * sigma_w2 * (G(0, 5) * G(0, 6) + G(1, 5) * G(1, 6) + G(2, 5) * G(2, 6)) / tw;
-  CD = fmax2(CD, cdmin);
+  if (!bc) CD = fmax2(CD, cdmin);
   double F1 = b.F1[c0];
   double gama = gama1 * F1 + gama2 * (1. - F1);
   double beta = beta1 * F1 + beta2 * (1. - F1);
@@ -899,9 +932,17 @@ __global__ void k_source(Params p, DevBlock b) {
   double Dw = beta * rho * (tw * tw);
   double divergence = G(0, 1) + G(1, 2) + G(2, 3);
   double mt = b.mut[c0];
-  double Pk = mt * (vort * vort) - ((2.0 / 3.0) * rho * tk * divergence);
+  double Pk = bc ? mt * (vort * vort) : mt * (vort * vort) - ((2.0 / 3.0) * rho * tk * divergence);
   Pk = fmin2(Pk, limiter * Dk);
   double Pw = (rho * gama / mt) * Pk;
+  if (bc) {
+    const double u = b.qp[c0 + d.P], v = b.qp[c0 + 2 * d.P], w = b.qp[c0 + 3 * d.P];
+    const double vmag = sqrt(u * u + v * v + w * w);
+    const double dd = b.dist[c0];
+    const double nu_bc = (mt / rho) / (vmag * dd);
+    const double re_v = rho * dd * dd * vort / b.mu[c0];
+    Pk = gamma_bc(p, re_v, nu_bc) * Pk;
+  }
   double Sk = (Pk - Dk) * b.cells[4 * c0];
   double Sw = (Pw - Dw + (1. - F1) * CD) * b.cells[4 * c0];
   const long long o = cidx(d, i, j, k), N = ncells(d);

@@ -32,6 +32,7 @@ FLUX = {"ausm": 0, "ausmP": 1, "ausmUP": 2, "slau": 3, "ldfss0": 4, "van_leer": 
 INTERP = {"none": 0, "muscl": 1, "ppm": 2, "weno": 3, "weno_NM": 4}
 TIME = {"none": 0, "RK2": 1, "RK4": 2, "TVDRK2": 3, "TVDRK3": 4, "implicit": 5, "plusgs": 6}
 TURB = {"none": 0, "sst": 1, "sst2003": 2, "sa": 3, "kkl": 4}
+TRANSITION = {"none": 0, "bc": 1}
 MU = {"constant": 0, "sutherland_law": 1}
 LIMITER = {"koren": 0, "van_albada": 1}
 FEST_FP64, FEST_MIXED = 0, 1
@@ -47,7 +48,8 @@ class Flow(C.Structure):
         "density_inf", "x_speed_inf", "y_speed_inf", "z_speed_inf", "pressure_inf",
         "tk_inf", "tw_inf", "vel_mag", "MInf", "gm", "R_gas", "mu_ref", "T_ref",
         "Sutherland_temp", "Pr", "tPr")] + [("mu_variation", C.c_int), ("reserved", C.c_int),
-                                            ("tv_inf", C.c_double), ("tkl_inf", C.c_double)]
+                                            ("tv_inf", C.c_double), ("tkl_inf", C.c_double),
+                                            ("tu_inf", C.c_double)]
 
 
 class Scheme(C.Structure):
@@ -56,7 +58,8 @@ class Scheme(C.Structure):
                 ("global_time_step", C.c_double)] + [(n, C.c_int) for n in (
                     "ilimiter_switch", "jlimiter_switch", "klimiter_switch",
                     "itlimiter_switch", "jtlimiter_switch", "ktlimiter_switch",
-                    "iPB_switch", "jPB_switch", "kPB_switch", "turbulence", "accur", "limiter")]
+                    "iPB_switch", "jPB_switch", "kPB_switch", "turbulence", "accur", "limiter",
+                    "transition")]
 
 
 D6 = C.c_double * 6
@@ -74,7 +77,7 @@ def make_flow(**kw):
     """flowtype with the reference defaults (vartypes.f90:236-285) and the
     derived vel_mag / MInf of init_infinity_values (state.f90:87-88)."""
     d = dict(density_inf=1.2, x_speed_inf=100.0, y_speed_inf=0.0, z_speed_inf=0.0,
-             pressure_inf=101325.0, tk_inf=0.0, tw_inf=0.0, tv_inf=0.0, tkl_inf=0.0, gm=1.4,
+             pressure_inf=101325.0, tk_inf=0.0, tw_inf=0.0, tv_inf=0.0, tkl_inf=0.0, tu_inf=0.0, gm=1.4,
              R_gas=287.0,
              mu_ref=0.0, T_ref=300.0, Sutherland_temp=110.0, Pr=0.7, tPr=0.9,
              mu_variation="constant")
@@ -113,7 +116,7 @@ def make_scheme(**kw):
              time_step_accuracy="none", global_time_step=-1.0, ilimiter_switch=1,
              jlimiter_switch=1, klimiter_switch=1, itlimiter_switch=1, jtlimiter_switch=1,
              ktlimiter_switch=1, iPB_switch=0, jPB_switch=0, kPB_switch=0, turbulence="none",
-             accur=1, limiter="koren")
+             accur=1, limiter="koren", transition="none")
     d.update(kw)
     s = Scheme()
     s.scheme_name = FLUX[d["scheme_name"]]
@@ -127,6 +130,7 @@ def make_scheme(**kw):
         setattr(s, k, int(d[k]))
     s.turbulence = TURB[d["turbulence"]]
     s.limiter = LIMITER[d["limiter"]]
+    s.transition = TRANSITION[d["transition"]]
     return s
 
 

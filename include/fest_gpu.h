@@ -74,6 +74,11 @@ enum { FEST_TIME_NONE = 0, FEST_TIME_RK2 = 1, FEST_TIME_RK4 = 2,
  * update.f90:399-404), FP64 module path as SA */
 enum { FEST_TURB_NONE = 0, FEST_TURB_SST = 1, FEST_TURB_SST2003 = 2, FEST_TURB_SA = 3, FEST_TURB_KKL = 4 };
 enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
+/* transition model (schemetype%transition): FEST_TRANSITION_BC, the
+ * algebraic 'bc' intermittency on the production of SA ('saBC',
+ * source.f90:985-1194) or k-omega SST (source.f90:467-604); FP64 module
+ * path, explicit integrators */
+enum { FEST_TRANSITION_NONE = 0, FEST_TRANSITION_BC = 1 };
 /* MUSCL limiter: the reference hard-codes Koren's alpha family
  * (muscl.f90:151,176); van Albada (muscl.f90:178, commented out there) is an
  * extension selectable here. */
@@ -101,6 +106,7 @@ typedef struct {            /* flowtype, vartypes.f90:235-286 */
   int reserved;
   double tv_inf;            /* Spalart-Allmaras free-stream tv (state.f90:106-109) */
   double tkl_inf;           /* k-kL free-stream kL (state.f90:101-103) */
+  double tu_inf;            /* free-stream turbulence intensity, percent (flow%tu_inf) */
 } fest_flow;
 
 typedef struct {            /* schemetype, vartypes.f90:197-232 */
@@ -115,6 +121,7 @@ typedef struct {            /* schemetype, vartypes.f90:197-232 */
   int turbulence;           /* FEST_TURB_* */
   int accur;                /* higher-order ghost switch (bc.f90:48-50) */
   int limiter;              /* FEST_LIMITER_* */
+  int transition;           /* FEST_TRANSITION_* */
 } fest_scheme;
 
 typedef struct {            /* boundarytype, vartypes.f90:289-367 */

@@ -1887,10 +1887,151 @@ static void kkl_source(fo_block *b) {
       }
 }
 
-/* source.f90:94-155 add_source_term_residue: the SA, k-kL and SST sources */
+/* the free-stream Reynolds number of init_infinity_values (state.f90:89),
+ * per unit length */
+static double reynolds_number(const fo_block *b) {
+  return b->flow.density_inf * b->flow.vel_mag * 1.0 / b->flow.mu_ref;
+}
+
+/* the 'bc' transition model's intermittency (source.f90:571-589 and
+ * 1159-1170): from the momentum-thickness Reynolds number against its
+ * transition value (Tu in percent) and the eddy viscosity against its
+ * critical value */
+static double gamma_bc(double re_v, double nu_bc, double Re, double tu) {
+  const double chi_1 = 0.002, chi_2 = 5.0;
+  double nu_cr = chi_2 / Re;
+  double re_theta = re_v / 2.193;
+  double re_theta_t = (803.73 * (pow((tu + 0.6067), (-1.027))));
+  double term1 = sqrt(fmax2(re_theta - re_theta_t, 0.) / (chi_1 * re_theta_t));
+  double term2 = sqrt(fmax2(nu_bc - nu_cr, 0.0) / nu_cr);
+  double term_exponential = (term1 + term2);
+  return 1.0 - exp(-term_exponential);
+}
+
+/* source.f90:985-1194 add_saBC_source: SA with the production scaled by
+ * the 'bc' intermittency (S-hat floored at 1e-10) */
+static void sa_bc_source(fo_block *b) {
+  V q = vqp(b), mu = vpad(b, FO_MU), dist = vpad(b, FO_DIST), r = vres(b);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
+  R4 If = vfaces(b, 0), Jf = vfaces(b, 1), Kf = vfaces(b, 2), cl = vcells(b);
+  const double Re = reynolds_number(b), tu = b->flow.tu_inf;
+  OMP_FOR
+  for (int k = 1; k <= KMX - 1; ++k)
+    for (int j = 1; j <= JMX - 1; ++j)
+      for (int i = 1; i <= IMX - 1; ++i) {
+#define GR(c, l) (*at(g[c], i, j, k, l))
+        double density = *at(q, i, j, k, 1), u = *at(q, i, j, k, 2), v = *at(q, i, j, k, 3), w = *at(q, i, j, k, 4);
+        double tv = *at(q, i, j, k, 6);
+        double vmag = sqrt(u * u + v * v + w * w);
+        double RhoFace[6] = {*at(q, i - 1, j, k, 1) + density, *at(q, i, j - 1, k, 1) + density,
+                             *at(q, i, j, k - 1, 1) + density, *at(q, i + 1, j, k, 1) + density,
+                             *at(q, i, j + 1, k, 1) + density, *at(q, i, j, k + 1, 1) + density};
+        const double *fI0 = r4(If, i, j, k), *fJ0 = r4(Jf, i, j, k), *fK0 = r4(Kf, i, j, k);
+        const double *fI1 = r4(If, i + 1, j, k), *fJ1 = r4(Jf, i, j + 1, k), *fK1 = r4(Kf, i, j, k + 1);
+        double Area[6] = {fI0[0], fJ0[0], fK0[0], fI1[0], fJ1[0], fK1[0]};
+        double Normal[6][3] = {{fI0[1], fI0[2], fI0[3]}, {fJ0[1], fJ0[2], fJ0[3]}, {fK0[1], fK0[1], fK0[1]},
+                               {fI1[1], fI1[2], fI1[3]}, {fJ1[1], fJ1[2], fJ1[3]}, {fK1[1], fK1[2], fK1[3]}};
+        double vol = r4(cl, i, j, k)[0];
+        double gr[3];
+        for (int c = 0; c < 3; ++c)
+          gr[c] = (-(RhoFace[0]) * Normal[0][c] * Area[0] - (RhoFace[1]) * Normal[1][c] * Area[1] -
+                   (RhoFace[2]) * Normal[2][c] * Area[2] + (RhoFace[3]) * Normal[3][c] * Area[3] +
+                   (RhoFace[4]) * Normal[4][c] * Area[4] + (RhoFace[5]) * Normal[5][c] * Area[5]) /
+                  (2 * vol);
+        double wa = GR(1, 3) - GR(2, 2), wb = GR(2, 1) - GR(0, 3), wc = GR(0, 2) - GR(1, 1);
+        double Omega = sqrt(((wa * wa) + (wb * wb) + (wc * wc)));
+        double CD1 = cb2 * ((GR(0, 5) * GR(0, 5)) + (GR(1, 5) * GR(1, 5)) + (GR(2, 5) * GR(2, 5)));
+        double CD2 = ((gr[0] * GR(0, 5)) + (gr[1] * GR(1, 5)) + (gr[2] * GR(2, 5)));
+        double dist_i = *at(dist, i, j, k, 1);
+        double dist_i_2 = dist_i * dist_i;
+        double k2 = kappa_sa * kappa_sa;
+        double nu = *at(mu, i, j, k, 1) / density;
+        double Ji = tv / nu, Ji_2 = Ji * Ji, Ji_3 = Ji_2 * Ji;
+        double fv1 = (Ji_3) / ((Ji_3) + (pow(cv1, 3.0)));
+        double fv2 = 1.0 - Ji / (1.0 + (Ji * fv1));
+        double S = Omega;
+        double inv_k2_d2 = 1.0 / (k2 * dist_i_2);
+        double Shat = S + tv * fv2 * inv_k2_d2;
+        Shat = fmax2(Shat, 1.0e-10);
+        double inv_Shat = 1.0 / Shat;
+        double nu_t = tv * fv1;
+        double nu_bc = nu_t / (vmag * dist_i);
+        double re_v = dist_i_2 * Omega / nu;
+        double gBC = gamma_bc(re_v, nu_bc, Re, tu);
+        double Production = gBC * cb1 * Shat * tv * vol;
+        double rr = fmin2(tv * inv_Shat * inv_k2_d2, 10.0);
+        double gg = rr + cw2 * (pow6(rr) - rr);
+        double g_6 = pow6(gg);
+        double glim = pow(((1.0 + pow6(cw3)) / (g_6 + pow6(cw3))), (1.0 / 6.0));
+        double fw = gg * glim;
+        double Destruction = (CW1_SA * fw * tv * tv / dist_i_2) * (vol);
+        double lamda = (density * CD1 / sigma_sa - CD2 * (nu + tv) / sigma_sa) * vol;
+        double S_v = (Production - Destruction + lamda);
+        *at(r, i, j, k, 6) = *at(r, i, j, k, 6) - S_v;
+#undef GR
+      }
+}
+
+/* source.f90:467-604 add_sst_bc_source: SST with the production mu_t
+ * Omega^2 (no divergence term, limited by 20 D_k), scaled by the 'bc'
+ * intermittency after P_w is taken from it, and the cross diffusion
+ * without its floor */
+static void sst_bc_source(fo_block *b) {
+  V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), F1v = vpad(b, FO_F1), dist = vpad(b, FO_DIST);
+  V r = vres(b);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
+  R4 cl = vcells(b);
+  const double Re = reynolds_number(b), TuL = b->flow.tu_inf;
+  double gama1 = (beta1 / bstar) - ((sigma_w1 * (kappa_sst * kappa_sst)) / sqrt(bstar));
+  double gama2 = (beta2 / bstar) - ((sigma_w2 * (kappa_sst * kappa_sst)) / sqrt(bstar));
+  OMP_FOR
+  for (int k = 1; k <= KMX - 1; ++k)
+    for (int j = 1; j <= JMX - 1; ++j)
+      for (int i = 1; i <= IMX - 1; ++i) {
+#define GR(c, l) (*at(g[c], i, j, k, l))
+        double density = *at(q, i, j, k, 1), tk = *at(q, i, j, k, 6), tw = *at(q, i, j, k, 7);
+        double wa = GR(1, 3) - GR(2, 2), wb = GR(2, 1) - GR(0, 3), wc = GR(0, 2) - GR(1, 1);
+        double vort = sqrt(((wa * wa) + (wb * wb) + (wc * wc)));
+        double CD = 2 * density * sigma_w2 * (GR(0, 5) * GR(0, 6) + GR(1, 5) * GR(1, 6) + GR(2, 5) * GR(2, 6)) / tw;
+        double F1 = *at(F1v, i, j, k, 1);
+        double gama = gama1 * F1 + gama2 * (1. - F1);
+        double beta = beta1 * F1 + beta2 * (1. - F1);
+        double D_k = bstar * density * tw * tk;
+        double D_w = beta * density * (tw * tw);
+        double mt = *at(mut, i, j, k, 1);
+        double P_k = mt * (vort * vort);
+        P_k = fmin2(P_k, 20.0 * D_k);
+        double P_w = (density * gama / mt) * P_k;
+        double lamda = (1. - F1) * CD;
+        double u = *at(q, i, j, k, 2), v = *at(q, i, j, k, 3), w = *at(q, i, j, k, 4);
+        double vmag = sqrt(u * u + v * v + w * w);
+        double nu_t = mt / density;
+        double d = *at(dist, i, j, k, 1);
+        double nu_bc = nu_t / (vmag * d);
+        double re_v = density * d * d * vort / *at(mu, i, j, k, 1);
+        P_k = gamma_bc(re_v, nu_bc, Re, TuL) * P_k;
+        double S_k = P_k - D_k;
+        double S_w = P_w - D_w + lamda;
+        double vol = r4(cl, i, j, k)[0];
+        S_k = S_k * vol;
+        S_w = S_w * vol;
+        *at(r, i, j, k, 6) = *at(r, i, j, k, 6) - S_k;
+        *at(r, i, j, k, 7) = *at(r, i, j, k, 7) - S_w;
+#undef GR
+      }
+}
+
+/* source.f90:94-155 add_source_term_residue: the SA (and saBC), k-kL and
+ * SST (and SST-BC) sources */
 void fo_add_source_term_residue(fo_block *b) {
+  const int bc_transition = b->sc.transition == FEST_TRANSITION_BC;
   if (is_sa(b)) {
-    sa_source(b);
+    if (bc_transition) sa_bc_source(b);
+    else sa_source(b);
+    return;
+  }
+  if (is_sst(b) && bc_transition) {
+    sst_bc_source(b);
     return;
   }
   if (is_kkl(b)) {

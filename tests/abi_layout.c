@@ -33,6 +33,7 @@ int main(void) {
   printf("fest_flow.reserved %zu\n", offsetof(fest_flow, reserved));
   printf("fest_flow.tv_inf %zu\n", offsetof(fest_flow, tv_inf));
   printf("fest_flow.tkl_inf %zu\n", offsetof(fest_flow, tkl_inf));
+  printf("fest_flow.tu_inf %zu\n", offsetof(fest_flow, tu_inf));
   printf("fest_scheme %zu\n", sizeof(fest_scheme));
   printf("fest_scheme.scheme_name %zu\n", offsetof(fest_scheme, scheme_name));
   printf("fest_scheme.interpolant %zu\n", offsetof(fest_scheme, interpolant));
@@ -51,6 +52,7 @@ int main(void) {
   printf("fest_scheme.turbulence %zu\n", offsetof(fest_scheme, turbulence));
   printf("fest_scheme.accur %zu\n", offsetof(fest_scheme, accur));
   printf("fest_scheme.limiter %zu\n", offsetof(fest_scheme, limiter));
+  printf("fest_scheme.transition %zu\n", offsetof(fest_scheme, transition));
   printf("fest_bc %zu\n", sizeof(fest_bc));
   printf("fest_bc.id %zu\n", offsetof(fest_bc, id));
   printf("fest_bc.partner_block %zu\n", offsetof(fest_bc, partner_block));
