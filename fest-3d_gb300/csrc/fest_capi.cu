@@ -220,6 +220,7 @@ void fill_params(fest_handle* h) {
   p.pb[0] = s.iPB_switch; p.pb[1] = s.jPB_switch; p.pb[2] = s.kPB_switch;
   // get_n_grad (gradients.f90:229-258)
   p.n_grad = s.turbulence == FEST_TURB_NONE ? 4 : s.turbulence == FEST_TURB_SA ? 5 : 6;
+  if (s.transition == FEST_TRANSITION_LCTM2015) p.n_grad += 1;  // gradients.f90:260-265
   p.sa_cv1_3 = pow(7.1, 3.0);
   p.kkl_c025 = pow(0.09, 0.25);
   p.kkl_c075 = pow(0.09, 0.75);
@@ -249,7 +250,7 @@ void fill_params(fest_handle* h) {
     p.fix_rho[i] = b.fixed_density[i]; p.fix_p[i] = b.fixed_pressure[i];
     p.fix_u[i] = b.fixed_x_speed[i]; p.fix_v[i] = b.fixed_y_speed[i]; p.fix_w[i] = b.fixed_z_speed[i];
     p.fix_tk[i] = b.fixed_tk[i]; p.fix_tw[i] = b.fixed_tw[i]; p.fix_tv[i] = b.fixed_tv[i];
-    p.fix_tkl[i] = b.fixed_tkl[i];
+    p.fix_tkl[i] = b.fixed_tkl[i]; p.fix_tgm[i] = b.fixed_tgm[i];
     p.Tw[i] = b.fixed_wall_temperature[i]; p.Tp[i] = b.fixed_Tpressure[i];
   }
   params_f32(p);
@@ -439,6 +440,7 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
   if (dims->imx < 2 || dims->jmx < 2 || dims->kmx < 2) return FEST_ERR_ARG;
   // set_n_var_value (state.f90:280-305)
   int nv_need = scheme->turbulence == FEST_TURB_NONE ? 5 : scheme->turbulence == FEST_TURB_SA ? 6 : 7;
+  if (scheme->transition == FEST_TRANSITION_LCTM2015) nv_need += 1;  // state.f90:308-318
   if (dims->n_var != nv_need) return FEST_ERR_ARG;
   if (scheme->scheme_name < 0 || scheme->scheme_name > 5) return FEST_ERR_ARG;
   if (scheme->interpolant < 0 || scheme->interpolant > 4) return FEST_ERR_ARG;
@@ -451,9 +453,15 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
   // the 'bc' transition model replaces the SA or SST source only
   // (source.f90:124-143; the implicit integrators update SST-BC as SST,
   // lusgs.f90:161-164); lctm2015 is not built
-  if (scheme->transition != FEST_TRANSITION_NONE && scheme->transition != FEST_TRANSITION_BC) return FEST_ERR_ARG;
+  if (scheme->transition < FEST_TRANSITION_NONE || scheme->transition > FEST_TRANSITION_LCTM2015) return FEST_ERR_ARG;
   if (scheme->transition == FEST_TRANSITION_BC &&
       (scheme->turbulence == FEST_TURB_NONE || scheme->turbulence == FEST_TURB_KKL || flow->mu_ref <= 0.0))
+    return FEST_ERR_ARG;
+  // LCTM2015 sits on k-omega SST (source.f90:134-143); PLU-SGS's LCTM2015
+  // update (plusgs.f90:2130-2624) is not built
+  if (scheme->transition == FEST_TRANSITION_LCTM2015 &&
+      (!(scheme->turbulence == FEST_TURB_SST || scheme->turbulence == FEST_TURB_SST2003) || flow->mu_ref <= 0.0 ||
+       scheme->time_step_accuracy == FEST_TIME_PLUSGS))
     return FEST_ERR_ARG;
   if (scheme->time_stepping_method != 'l' && scheme->time_stepping_method != 'g') return FEST_ERR_ARG;
   for (int f = 0; f < 6; ++f) {
@@ -1024,7 +1032,7 @@ int fest_get_next_solution(fest_handle* h, double* qp, int current_iter, double 
 // from the device sums of find_resnorm
 static void resnorm_assemble(const fest_handle* h, const double* sums, double* res_abs) {
   const fest_flow& f = h->flow;
-  double sc[NVMAX + 1];
+  double sc[NVMOD + 1];
   sc[0] = 1.;
   sc[1] = f.density_inf * f.vel_mag;
   sc[2] = sc[3] = sc[4] = f.density_inf * f.vel_mag * f.vel_mag;
@@ -1033,6 +1041,9 @@ static void resnorm_assemble(const fest_handle* h, const double* sums, double* r
   // resnorm.f90:155-163: the sixth variable's scale is tv_inf's for SA
   sc[6] = f.density_inf * f.vel_mag * (h->sc.turbulence == FEST_TURB_SA ? f.tv_inf : f.tk_inf);
   sc[7] = f.density_inf * f.vel_mag * (h->sc.turbulence == FEST_TURB_KKL ? f.tkl_inf : f.tw_inf);
+  // setup_scale (resnorm.f90:128-167) sets no scale for LCTM2015's
+  // intermittency: its norm is taken unscaled
+  sc[8] = 1.0;
   res_abs[0] = fabs(sums[0] / sc[0]);
   for (int l = 1; l <= h->p.d.nv; ++l) res_abs[l] = sqrt(sums[l] / (sc[l] * sc[l]));
 }
@@ -1040,7 +1051,7 @@ static void resnorm_assemble(const fest_handle* h, const double* sums, double* r
 int fest_find_resnorm(fest_handle* h, double* res_abs) {
   if (!h || !res_abs) return FEST_ERR_ARG;
   launch_resnorm(h->p, h->d, h->d_resnorm, h->L());
-  double sums[NVMAX + 1];
+  double sums[NVMOD + 1];
   RET(down(h, sums, h->d_resnorm, h->p.d.nv + 1));
   RET(finish(h));
   resnorm_assemble(h, sums, res_abs);
@@ -1088,7 +1099,7 @@ int fest_step_host_interior(fest_handle* h, double* q, int n_iters, int first_it
   }
   kmark(h, 0);
   RET(step_enqueue(h, n_iters, first_iter, CFL));
-  double sums[NVMAX + 1];
+  double sums[NVMOD + 1];
   if (res_abs) {
     launch_resnorm(h->p, h->d, h->d_resnorm, h->L());
     RET(down(h, sums, h->d_resnorm, h->p.d.nv + 1));
@@ -1108,7 +1119,7 @@ int fest_step_host(fest_handle* h, double* qp, int n_iters, int first_iter, doub
   if (h->fused) fused_invalidate(h->fused);
   kmark(h, 0);
   RET(step_enqueue(h, n_iters, first_iter, CFL));
-  double sums[NVMAX + 1];
+  double sums[NVMOD + 1];
   if (res_abs) {
     launch_resnorm(h->p, h->d, h->d_resnorm, h->L());
     RET(down(h, sums, h->d_resnorm, h->p.d.nv + 1));

@@ -11,6 +11,9 @@
 namespace fest {
 
 constexpr int NVMAX = 7;
+// the module kernels' bound: LCTM2015 adds the intermittency as an eighth
+// variable on the module path only (the fused sweep and the VJP keep NVMAX)
+constexpr int NVMOD = 8;
 
 struct Dims {
   int imx, jmx, kmx, nv;  // node counts (vartypes.f90:21-26) and n_var
@@ -34,7 +37,7 @@ struct Params {
   int part_block[6], part_face[6], part_orient[6];
   int self_block;
   double c1, c2, c3;
-  double fix_rho[6], fix_p[6], fix_u[6], fix_v[6], fix_w[6], fix_tk[6], fix_tw[6], fix_tv[6], fix_tkl[6];
+  double fix_rho[6], fix_p[6], fix_u[6], fix_v[6], fix_w[6], fix_tk[6], fix_tw[6], fix_tv[6], fix_tkl[6], fix_tgm[6];
   // Spalart-Allmaras: cv1**3, folded on the host to the correctly rounded
   // power as the reference's compiler folds its parameter
   double sa_cv1_3;
@@ -442,7 +445,7 @@ __device__ __forceinline__ void recon_cell(const Params& p, int dir, int c, int 
 
 // ---- convective fluxes: one face, all variables -----------------------------
 // ausm.f90:59-151, van_leer.f90:59-145, ldfss0.f90:59-160
-template <typename T>
+template <typename T, int NVL = NVMAX>
 __device__ __forceinline__ void flux_ausm_family(int kind, int nv, T gm, const T* qL, const T* qR,
                                                  T A, T nx, T ny, T nz, T mask, T* Fo) {
   T c = T(0.5) * (sq(dv(gm * qL[4], qL[0])) + sq(dv(gm * qR[4], qR[0])));
@@ -486,12 +489,12 @@ __device__ __forceinline__ void flux_ausm_family(int kind, int nv, T gm, const T
   Fo[3] = ((Fp0 * qL[3]) + (sDp * qL[4] * nz)) * A + ((Fm0 * qR[3]) + (sDm * qR[4] * nz)) * A;
   Fo[4] = (Fp0 * hL) * A + (Fm0 * hR) * A;
 #pragma unroll
-  for (int l = 5; l < NVMAX; ++l)
+  for (int l = 5; l < NVL; ++l)
     if (l < nv) Fo[l] = (Fp0 * qL[l]) * A + (Fm0 * qR[l]) * A;
 }
 
 // slau.f90:85-196, ausmP.f90:88-192, ausmUP.f90:92-210
-template <typename T>
+template <typename T, int NVL = NVMAX>
 __device__ __forceinline__ void flux_mass_family(int kind, int nv, T gm, T MInf, const T* qL,
                                                  const T* qR, T A, T nx, T ny, T nz, T mask,
                                                  T* Fo) {
@@ -577,19 +580,19 @@ __device__ __forceinline__ void flux_mass_family(int kind, int nv, T gm, T MInf,
   Fo[3] = ((Fp0 * wL + Fm0 * wR) + (pbar * nz)) * A;
   Fo[4] = (Fp0 * HL + Fm0 * HR) * A;
 #pragma unroll
-  for (int l = 5; l < NVMAX; ++l)
+  for (int l = 5; l < NVL; ++l)
     if (l < nv) Fo[l] = (Fp0 * qL[l] + Fm0 * qR[l]) * A;
 }
 
 // FLUX >= 0 fixes the scheme at compile time (the fused sweeps)
-template <typename T, int FLUX = -1>
+template <typename T, int FLUX = -1, int NVL = NVMAX>
 __device__ __forceinline__ void face_flux(const Params& p, const T* qL, const T* qR, T A, T nx,
                                           T ny, T nz, T mask, T* Fo) {
   const int kind = FLUX >= 0 ? FLUX : p.flux;
   if (kind == FEST_FLUX_AUSM || kind == FEST_FLUX_VAN_LEER || kind == FEST_FLUX_LDFSS0)
-    flux_ausm_family<T>(kind, p.d.nv, pv<T>(p.gm, p.f_gm), qL, qR, A, nx, ny, nz, mask, Fo);
+    flux_ausm_family<T, NVL>(kind, p.d.nv, pv<T>(p.gm, p.f_gm), qL, qR, A, nx, ny, nz, mask, Fo);
   else
-    flux_mass_family<T>(kind, p.d.nv, pv<T>(p.gm, p.f_gm), pv<T>(p.MInf, p.f_MInf), qL, qR, A, nx, ny, nz, mask,
+    flux_mass_family<T, NVL>(kind, p.d.nv, pv<T>(p.gm, p.f_gm), pv<T>(p.MInf, p.f_MInf), qL, qR, A, nx, ny, nz, mask,
                         Fo);
 }
 

@@ -152,6 +152,10 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
   const bool sst = p.turb == FEST_TURB_SST || p.turb == FEST_TURB_SST2003;
   const bool sa = p.turb == FEST_TURB_SA;  // tv: the sixth variable, treated as k is
   const bool kkl = p.turb == FEST_TURB_KKL;  // k and kL, treated as k is
+  // LCTM2015's intermittency: fixed where k is, else a flat copy, at walls
+  // too (bc_primitive.f90:258-264, 299-302, 339-345, 384-387, 436-439,
+  // 554-557, 715-753)
+  const bool lctm = p.transition == FEST_TRANSITION_LCTM2015;
   const int id = p.id[f];
   switch (id) {
     case -1:
@@ -164,6 +168,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         if (sst) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tw[f]); }
         if (sa) fix_col(p, q, f, ta, tb, 6, p.fix_tv[f]);
         if (kkl) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tkl[f]); }
+        if (lctm) fix_col(p, q, f, ta, tb, 8, p.fix_tgm[f]);
       }
       break;
     case -2:
@@ -179,6 +184,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         if (sst) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tw[f]); }
         if (sa) fix_col(p, q, f, ta, tb, 6, p.fix_tv[f]);
         if (kkl) { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tkl[f]); }
+        if (lctm) fix_col(p, q, f, ta, tb, 8, p.fix_tgm[f]);
       }
       copy3_col(p, q, f, ta, tb, 5, CP_FLAT);
       break;
@@ -188,6 +194,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       if (sst) { copy3_col(p, q, f, ta, tb, 6, CP_FLAT); copy3_col(p, q, f, ta, tb, 7, CP_FLAT); }
       if (sa) copy3_col(p, q, f, ta, tb, 6, CP_FLAT);
       if (kkl) { copy3_col(p, q, f, ta, tb, 6, CP_FLAT); copy3_col(p, q, f, ta, tb, 7, CP_FLAT); }
+      if (lctm) copy3_col(p, q, f, ta, tb, 8, CP_FLAT);
       break;
     case -5: {  // wall (bc_primitive.f90:392-402)
       copy3_col(p, q, f, ta, tb, 5, CP_SYMM);
@@ -214,6 +221,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       copy3_col(p, q, f, ta, tb, 4, CP_ANTI);
       if (sa) copy3_col(p, q, f, ta, tb, 6, CP_ANTI);
       if (kkl) { copy3_col(p, q, f, ta, tb, 6, CP_ANTI); copy3_col(p, q, f, ta, tb, 7, CP_ANTI); }
+      if (lctm) copy3_col(p, q, f, ta, tb, 8, CP_FLAT);
       if (sst) {
         copy3_col(p, q, f, ta, tb, 6, CP_ANTI);
         // set_omega_at_wall (bc_primitive.f90:564-643)
@@ -234,6 +242,7 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
       if (sst) { copy3_col(p, q, f, ta, tb, 6, CP_SYMM); copy3_col(p, q, f, ta, tb, 7, CP_SYMM); }
       if (sa) copy3_col(p, q, f, ta, tb, 6, CP_SYMM);
       if (kkl) { copy3_col(p, q, f, ta, tb, 6, CP_SYMM); copy3_col(p, q, f, ta, tb, 7, CP_SYMM); }
+      if (lctm) copy3_col(p, q, f, ta, tb, 8, CP_FLAT);
       int fi, fj, fk;
       bface_ijk(d, f, ta, tb, fi, fj, fk);
       const double* fn = b.faces[f / 2] + 4 * fidx(d, f / 2, fi, fj, fk);
@@ -268,6 +277,12 @@ __device__ void ghost_column(const Params& p, const DevBlock& b, const BlockRef*
         double Ulast = riemann_col(p, b, f, na, nb, false, tp);
         if (Ulast > 0.) { copy3_col(p, q, f, ta, tb, 6, CP_FLAT); copy3_col(p, q, f, ta, tb, 7, CP_FLAT); }
         else { fix_col(p, q, f, ta, tb, 6, p.fix_tk[f]); fix_col(p, q, f, ta, tb, 7, p.fix_tkl[f]); }
+      }
+      if (lctm) {
+        int na = (f / 2 == 0 ? d.jmx : d.imx) - 1, nb = (f / 2 == 2 ? d.jmx : d.kmx) - 1;
+        double Ulast = riemann_col(p, b, f, na, nb, false, tp);
+        if (Ulast > 0.) copy3_col(p, q, f, ta, tb, 8, CP_FLAT);
+        else fix_col(p, q, f, ta, tb, 8, p.fix_tgm[f]);
       }
     } break;
     default:
@@ -389,9 +404,9 @@ __global__ void k_fluxes(Params p, DevBlock b, int dir) {
   FSDim fs = fsdim(d, dir);
   FlDim fl = fldim(d, dir);
   const long long o = fsidx(fs, i, j, k);
-  double qL[NVMAX], qR[NVMAX], Fo[NVMAX];
+  double qL[NVMOD], qR[NVMOD], Fo[NVMOD];
 #pragma unroll
-  for (int l = 0; l < NVMAX; ++l) {
+  for (int l = 0; l < NVMOD; ++l) {
     if (l < d.nv) {
       qL[l] = b.fsL[dir][o + fs.N * l];
       qR[l] = b.fsR[dir][o + fs.N * l];
@@ -399,11 +414,11 @@ __global__ void k_fluxes(Params p, DevBlock b, int dir) {
   }
   const double* fc = b.faces[dir] + 4 * fidx(d, dir, i, j, k);
   const int f = dir == 0 ? i : dir == 1 ? j : k;
-  face_flux<double>(p, qL, qR, fc[0], fc[1], fc[2], fc[3], (double)wall_mask(p, dir, f), Fo);
+  face_flux<double, -1, NVMOD>(p, qL, qR, fc[0], fc[1], fc[2], fc[3], (double)wall_mask(p, dir, f), Fo);
   const long long of = flidx(fl, i, j, k);
   bool bad = false;
 #pragma unroll
-  for (int l = 0; l < NVMAX; ++l)
+  for (int l = 0; l < NVMOD; ++l)
     if (l < d.nv) {
       b.flux[dir][of + fl.N * l] = Fo[l];
       bad |= (Fo[l] != Fo[l]);
@@ -567,7 +582,17 @@ __global__ void k_viscosity(Params p, DevBlock b) {
   double right = 4 * (rho * sigma_w2 * tk) / (CD * (dd * dd));
   double arg1 = fmin2(fmax2(var1, var2), right);
   double a2 = arg1 * arg1;
-  b.F1[c0] = tanh(a2 * a2);
+  double F1 = tanh(a2 * a2);
+  if (p.transition == FEST_TRANSITION_LCTM2015) {
+    // viscosity.f90:265-280, 390-405: F1 raised to exp(-(var1/120)**8).
+    // The reference loop reads density and tk without setting them, so
+    // they hold its previous loop's last cell, (imx, jmx, kmx).
+    const long long cz = pidx(d, d.imx, d.jmx, d.kmx);
+    const double var1 = q[cz] * dd * sqrt(q[cz + 5 * d.P]) / b.mu[c0];
+    const double x = var1 / 120, x2 = x * x, x4 = x2 * x2;
+    F1 = fmax2(F1, exp(-(x4 * x4)));
+  }
+  b.F1[c0] = F1;
 }
 
 // ghost copies of mu_t / F1 (viscosity.f90:287-340)
@@ -716,6 +741,20 @@ __global__ void k_viscous(Params p, DevBlock b, int dir) {
     F[of + 5 * fl.N] = F6;
     F[of + 6 * fl.N] = F7;
     bad |= (F6 != F6) || (F7 != F7);
+  }
+  if (p.transition == FEST_TRANSITION_LCTM2015 && !(dir == 2 && d.kmx == 2)) {
+    // compute_viscous_fluxes_lctm2015 (viscous.f90:658-749): the
+    // intermittency diffused with mu + mu_t
+    double H[3];
+    for (int c = 0; c < 3; ++c) H[c] = 0.5 * (b.grad[c][g0 + NG * 6] + b.grad[c][g1 + NG * 6]);
+    const double dg = q[c1 + 7 * P] - q[c0 + 7 * P];
+    const double nc = (dg - (H[0] * delx + H[1] * dely + H[2] * delz)) / dLR;
+    H[0] = H[0] + (nc * delx / dLR);
+    H[1] = H[1] + (nc * dely / dLR);
+    H[2] = H[2] + (nc * delz / dLR);
+    const double F8 = F[of + 7 * fl.N] - (A * ((mu_f + mut_f) * (H[0] * nx + H[1] * ny + H[2] * nz)));
+    F[of + 7 * fl.N] = F8;
+    bad |= (F8 != F8);
   }
   F[of + fl.N] = F2;
   F[of + 2 * fl.N] = F3;
@@ -887,6 +926,80 @@ __device__ void kkl_source(const Params& p, const DevBlock& b, int i, int j, int
   b.res[o + 6 * N] = b.res[o + 6 * N] - Skl;
 }
 
+// add_sst_source_lctm2015 (source.f90:273-465): SST's source with the
+// production by vorticity times strain scaled by the intermittency, the
+// limited extra production, the floored destruction, and the
+// intermittency's own source; the pressure-gradient parameter from the
+// wall distance's gradient dotted with its unit vector (CC.f90:56-92, the
+// six face sums of the distance)
+__device__ void lctm_source(const Params& p, const DevBlock& b, int i, int j, int k) {
+  const Dims& d = p.d;
+  const long long c0 = pidx(d, i, j, k), og = gidx(d, i, j, k), NG = ngrad(d), P = d.P;
+  auto G = [&](int c, int l) { return b.grad[c][og + NG * (l - 1)]; };
+  const double sigma_w1 = 0.5, sigma_w2 = 0.856, beta1 = 0.075, beta2 = 0.0828, bstar = 0.09, kap = 0.41;
+  const bool s2003 = p.turb == FEST_TURB_SST2003;
+  const int limiter = s2003 ? 10 : 20;
+  double gama1 = (beta1 / bstar) - ((sigma_w1 * (kap * kap)) / sqrt(bstar));
+  double gama2 = (beta2 / bstar) - ((sigma_w2 * (kap * kap)) / sqrt(bstar));
+  if (s2003) { gama1 = 5.0 / 9.0; gama2 = 0.44; }
+  const double* q = b.qp;
+  const double density = q[c0], tk = q[c0 + 5 * P], tw = q[c0 + 6 * P], gm_ = q[c0 + 7 * P];
+  double vort, strain;
+  lctm_vort_strain(b, og, NG, vort, strain);
+  double CD = 2 * density * sigma_w2 * (G(0, 5) * G(0, 6) + G(1, 5) * G(1, 6) + G(2, 5) * G(2, 6)) / tw;
+  CD = fmax2(CD, s2003 ? 1.0e-10 : 1e-20);
+  const double F1 = b.F1[c0];
+  const double gama = gama1 * F1 + gama2 * (1. - F1);
+  const double beta = beta1 * F1 + beta2 * (1. - F1);
+  const double D_k = bstar * density * tw * tk;
+  const double D_w = beta * density * (tw * tw);
+  const double divergence = G(0, 1) + G(1, 2) + G(2, 3);
+  const double mt = b.mut[c0], m = b.mu[c0], dd = b.dist[c0];
+  double P_k = mt * (vort * strain) - ((2.0 / 3.0) * density * tk * divergence);
+  P_k = fmin2(P_k, limiter * D_k);
+  const double P_w = (density * gama / mt) * P_k;
+  const double lamda = (1. - F1) * CD;
+  const long long nb[6] = {pidx(d, i - 1, j, k), pidx(d, i, j - 1, k), pidx(d, i, j, k - 1),
+                           pidx(d, i + 1, j, k), pidx(d, i, j + 1, k), pidx(d, i, j, k + 1)};
+  const double* fr[6] = {b.faces[0] + 4 * fidx(d, 0, i, j, k), b.faces[1] + 4 * fidx(d, 1, i, j, k),
+                         b.faces[2] + 4 * fidx(d, 2, i, j, k), b.faces[0] + 4 * fidx(d, 0, i + 1, j, k),
+                         b.faces[1] + 4 * fidx(d, 1, i, j + 1, k), b.faces[2] + 4 * fidx(d, 2, i, j, k + 1)};
+  const double vol = b.cells[4 * c0];
+  double gd[3];
+  for (int c = 0; c < 3; ++c) {
+    double s = -((b.dist[nb[0]] + dd) * fr[0][1 + c] * fr[0][0]);
+    s = s - (b.dist[nb[1]] + dd) * fr[1][1 + c] * fr[1][0];
+    s = s - (b.dist[nb[2]] + dd) * fr[2][1 + c] * fr[2][0];
+    s = s + (b.dist[nb[3]] + dd) * fr[3][1 + c] * fr[3][0];
+    s = s + (b.dist[nb[4]] + dd) * fr[4][1 + c] * fr[4][0];
+    s = s + (b.dist[nb[5]] + dd) * fr[5][1 + c] * fr[5][0];
+    gd[c] = s / (2 * vol);
+  }
+  const double Vn = sqrt(gd[0] * gd[0] + gd[1] * gd[1] + gd[2] * gd[2]);
+  const double dvdy = gd[0] * (gd[0] / (Vn + 1e-12)) + gd[1] * (gd[1] / (Vn + 1e-12)) + gd[2] * (gd[2] / (Vn + 1e-12));
+  double lamd = (-7.57e-3) * (dvdy * dd * dd * density / m) + 0.0128;
+  lamd = fmin2(fmax2(lamd, -1.0), 1.0);
+  double Fpg = lamd >= 0.0 ? fmin2(1.0 + 14.68 * lamd, 1.5) : fmin2(1.0 - 7.34 * lamd, 3.0);
+  Fpg = fmax2(Fpg, 0.0);
+  const double TuL = fmin2(100.0 * sqrt(2.0 * tk / 3.0) / (tw * dd), 100.0);
+  const double Re_theta = 100.0 + 1000.0 * exp(-TuL * Fpg);
+  const double Rev = density * dd * dd * strain / m;
+  const double RT = density * tk / (m * tw);
+  double Fturb, Fonset;
+  lctm_onset(Rev, RT, Re_theta, Fturb, Fonset);
+  const double P_gm = 100 * density * strain * gm_ * (1.0 - gm_) * Fonset;
+  const double D_gm = 0.06 * density * vort * gm_ * Fturb * ((50.0 * gm_) - 1.0);
+  const double Fon_lim = fmin2(fmax2((Rev / (2.2 * 1100.0)) - 1.0, 0.0), 3.0);
+  const double Pk_lim = 5 * fmax2(gm_ - 0.2, 0.0) * (1.0 - gm_) * Fon_lim * fmax2(3 * m - mt, 0.0) * strain * vort;
+  const double S_k = gm_ * P_k - fmax2(gm_, 0.1) * D_k + Pk_lim;
+  const double S_w = P_w - D_w + lamda;
+  const double S_gm = P_gm - D_gm;
+  const long long o = cidx(d, i, j, k), N = ncells(d);
+  b.res[o + 5 * N] = b.res[o + 5 * N] - S_k * vol;
+  b.res[o + 6 * N] = b.res[o + 6 * N] - S_w * vol;
+  b.res[o + 7 * N] = b.res[o + 7 * N] - S_gm * vol;
+}
+
 // add_source_term_residue (source.f90:94-155): add_sa_source (or
 // add_saBC_source), add_kkl_source, or add_sst_source (source.f90:158-270;
 // or add_sst_bc_source, source.f90:467-604: production mu_t Omega^2 limited
@@ -903,6 +1016,10 @@ __global__ void k_source(Params p, DevBlock b) {
   }
   if (p.turb == FEST_TURB_KKL) {
     kkl_source(p, b, i, j, k);
+    return;
+  }
+  if (p.transition == FEST_TRANSITION_LCTM2015) {
+    lctm_source(p, b, i, j, k);
     return;
   }
   const double sigma_w1 = 0.5, sigma_w2 = 0.856, beta1 = 0.075, beta2 = 0.0828, bstar = 0.09,
@@ -1041,15 +1158,15 @@ __global__ void k_update(Params p, DevBlock b, double TF, double SF, int TU, int
   const double* Qu = use_store ? b.Ustore : b.qp;
   const int nv = d.nv;
   const double gm = p.gm;
-  double u1[NVMAX], u2[NVMAX], R[NVMAX];
+  double u1[NVMOD], u2[NVMOD], R[NVMOD];
   u1[0] = Qu[c0];
 #pragma unroll
-  for (int l = 1; l < NVMAX; ++l)
+  for (int l = 1; l < NVMOD; ++l)
     if (l < nv) u1[l] = Qu[c0 + P * l] * u1[0];
   double s1 = u1[1] * u1[1] + u1[2] * u1[2] + u1[3] * u1[3];
   u1[4] = (u1[4] / (gm - 1.) + 0.5 * s1) / u1[0];
 #pragma unroll
-  for (int l = 0; l < NVMAX; ++l)
+  for (int l = 0; l < NVMOD; ++l)
     if (l < nv) R[l] = b.res[o + N * l];
   const double dtc = b.dt[o];
   const bool sa = p.turb == FEST_TURB_SA;
@@ -1085,7 +1202,7 @@ __global__ void k_update(Params p, DevBlock b, double TF, double SF, int TU, int
   }
   if (use_store) {
 #pragma unroll
-    for (int l = 0; l < NVMAX; ++l)
+    for (int l = 0; l < NVMOD; ++l)
       if (l < nv) {
         double rn = b.Rstore[o + N * l] + SF * R[l];
         b.Rstore[o + N * l] = rn;
@@ -1094,16 +1211,16 @@ __global__ void k_update(Params p, DevBlock b, double TF, double SF, int TU, int
   }
   const double fac = (TF * dtc / b.cells[4 * c0]);
 #pragma unroll
-  for (int l = 0; l < NVMAX; ++l)
+  for (int l = 0; l < NVMOD; ++l)
     if (l < nv) u2[l] = u1[l] - R[l] * fac;
 #pragma unroll
-  for (int l = 1; l < NVMAX; ++l)
+  for (int l = 1; l < NVMOD; ++l)
     if (l < nv) u2[l] = u2[l] / u2[0];
   double s2 = u2[1] * u2[1] + u2[2] * u2[2] + u2[3] * u2[3];
   u2[4] = (gm - 1.) * u2[0] * (u2[4] - (0.5 * s2));
   bool bad = (u2[0] < 0.) || (u2[4] < 0.);
 #pragma unroll
-  for (int l = 0; l < NVMAX; ++l)
+  for (int l = 0; l < NVMOD; ++l)
     if (l < nv) bad |= (u2[l] != u2[l]);
   if (bad) {
     raise_error(b.err, FEST_ERR_NEGATIVE_STATE);
@@ -1128,8 +1245,8 @@ __global__ void k_resnorm_partial(Params p, DevBlock b, double* part, int nparts
   const Dims& d = p.d;
   __shared__ double sm[TPB];
   const long long N = ncells(d);
-  double acc[NVMAX + 1];
-  for (int l = 0; l <= NVMAX; ++l) acc[l] = 0.0;
+  double acc[NVMOD + 1];
+  for (int l = 0; l <= NVMOD; ++l) acc[l] = 0.0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long long)gridDim.x * blockDim.x)
     for (int l = 0; l < d.nv; ++l) {
       double v = b.res[t + N * l];

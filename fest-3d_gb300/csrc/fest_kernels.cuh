@@ -27,6 +27,31 @@ __host__ __device__ __forceinline__ long long mirror_index(const Dims& d, int pi
 }
 constexpr int kRedSlots = 1 << 16;
 
+// the vorticity and strain magnitudes of add_sst_source_lctm2015
+// (source.f90:347-362) and of lusgs.f90:2445-2460, from the cell gradients
+__device__ __forceinline__ void lctm_vort_strain(const DevBlock& b, long long og, long long NG, double& vort,
+                                                 double& strain) {
+  auto G = [&](int c, int l) { return b.grad[c][og + NG * (l - 1)]; };
+  const double wa = G(1, 3) - G(2, 2), wb = G(2, 1) - G(0, 3), wc = G(0, 2) - G(1, 1);
+  vort = ::sqrt(((wa * wa) + (wb * wb) + (wc * wc)));
+  const double sa = G(1, 3) + G(2, 2), sb = G(2, 1) + G(0, 3), sc = G(0, 2) + G(1, 1);
+  strain = ::sqrt((sa * sa) + (sb * sb) + (sc * sc) + 2 * (G(0, 1) * G(0, 1)) + 2 * (G(1, 2) * G(1, 2)) +
+                2 * (G(2, 3) * G(2, 3)));
+}
+
+// the onset terms shared by the source and the implicit update:
+// Fturb = ::exp(-(RT/2)^4) and max(min(Rev/(2.2 Re_theta), 2) -
+// max(1 - (RT/3.5)^3, 0), 0) (source.f90:433-440, lusgs.f90:2463-2470)
+__device__ __forceinline__ void lctm_onset(double Rev, double RT, double Re_theta, double& Fturb, double& Fonset) {
+  const double h = 0.5 * RT, h2 = h * h;
+  Fturb = ::exp(-(h2 * h2));
+  const double Fonset2 = fmin2(Rev / (2.2 * Re_theta), 2.0);
+  const double t3 = RT / 3.5;
+  const double Fonset3 = fmax2(1.0 - (t3 * t3) * t3, 0.0);
+  Fonset = fmax2(Fonset2 - Fonset3, 0.0);
+}
+
+
 // a block as seen by the interface exchange of another block
 struct BlockRef {
   DevBlock b;

@@ -2,7 +2,8 @@
 // the local time step, then update_with_lusgs (update.f90:215-218,
 // lusgs.f90:134-1196) or its low-Mach preconditioned form
 // update_with_plusgs (update.f90:219-222, plusgs.f90:139-1431), for laminar
-// and k-omega SST blocks, FP64.
+// and k-omega SST blocks, FP64; LU-SGS also for SST blocks with LCTM2015's
+// intermittency (update_lctm2015, lusgs.f90:2263-2700).
 //
 // The reference sweeps the interior cells forward (i fastest, then j, k)
 // computing dQ* from the dQ* of each cell's three lower neighbours, then
@@ -54,7 +55,8 @@ __device__ void lu_flux(const Params& p, const double* ql, const double* qr, con
 #pragma unroll
   for (int l = 5; l < N; ++l) {
     W[l] = U[l] / U[0];
-    W[l] = W[l] + 0.5 * (1. - copysign(1., W[l])) * (ql[l] - W[l]);
+    if (l < 7) W[l] = W[l] + 0.5 * (1. - copysign(1., W[l])) * (ql[l] - W[l]);
+    else W[l] = fmax2(W[l], 0.0);  // the intermittency (lusgs.f90:2783)
   }
   const double nx = f.nx, ny = f.ny, nz = f.nz;
   const double vn = (W[1] * nx) + (W[2] * ny) + (W[3] * nz);
@@ -96,6 +98,12 @@ __device__ void lu_flux(const Params& p, const double* ql, const double* qr, con
     // added, as lusgs.f90:1190-1191 has it
     out[5] = out[5] + (f.mu + sk * f.mut) * (g[3][0] * nx + g[3][1] * ny + g[3][2] * nz);
     out[6] = out[6] + (f.mu + sw * f.mut) * (g[4][0] * nx + g[4][1] * ny + g[4][2] * nz);
+  }
+  if constexpr (N == 8) {  // lctm2015Flux (lusgs.f90:2845-2851)
+    const double sk = kSigK1 * f.F1 + kSigK2 * (1.0 - f.F1), sw = kSigW1 * f.F1 + kSigW2 * (1.0 - f.F1);
+    out[5] = out[5] + (f.mu + sk * f.mut) * (g[3][0] * nx + g[3][1] * ny + g[3][2] * nz);
+    out[6] = out[6] + (f.mu + sw * f.mut) * (g[4][0] * nx + g[4][1] * ny + g[4][2] * nz);
+    out[7] = out[7] + (f.mu + f.mut) * (g[5][0] * nx + g[5][1] * ny + g[5][2] * nz);
   }
 #pragma unroll
   for (int l = 0; l < N; ++l) out[l] = out[l] * s;
@@ -242,10 +250,24 @@ __global__ void k_lu_prep(Params p, DevBlock b, LuDev u) {
   double D[N];
 #pragma unroll
   for (int l = 0; l < N; ++l) D[l] = (vol / b.dt[t]) + 0.5 * sumlam;
-  if constexpr (N == 7) {  // lusgs.f90:860-862: the destruction terms of k and omega
+  if constexpr (N >= 7) {  // lusgs.f90:860-862, 2439-2441: the destruction terms of k and omega
     const double f1 = b.F1[c0], beta = f1 * kBeta1 + (1.0 - f1) * kBeta2, w = q0[6];
     D[5] = (D[5] + (kBstar * w) * vol);
     D[6] = (D[6] + 2.0 * beta * w * vol);
+  }
+  if constexpr (N == 8) {  // lusgs.f90:2443-2475: the intermittency's source, linearised
+    double vort, strain;
+    lctm_vort_strain(b, gidx(d, i, j, k), ngrad(d), vort, strain);
+    const double density = q0[0], dd = b.dist[c0], m = b.mu[c0];
+    const double TuL = fmin2(100.0 * sqrt(2.0 * q0[5] / 3.0) / (q0[6] * dd), 100.0);
+    const double Re_theta = 100.0 + 1000.0 * exp(-TuL);
+    const double Rev = density * dd * dd * strain / m;
+    const double RT = density * q0[5] / (m * q0[6]);
+    double Fturb, Fonset;
+    lctm_onset(Rev, RT, Re_theta, Fturb, Fonset);
+    const double Dp = 100 * density * strain * Fonset * (1.0 - 2.0 * q0[7]);
+    const double De = 0.06 * vort * Fturb * density * (2.0 * 50.0 * q0[7] - 1.0);
+    D[7] = (D[7] + (-Dp + De) * vol);
   }
 #pragma unroll
   for (int l = 0; l < N; ++l) u.D[t + nc * l] = D[l];
@@ -349,8 +371,9 @@ __global__ void k_lu_apply(Params p, DevBlock b, LuDev u) {
 #pragma unroll
   for (int l = 0; l < 5; ++l) b.qp[c0 + P * l] = q[l];
 #pragma unroll
-  for (int l = 5; l < N; ++l)
+  for (int l = 5; l < N && l < 7; ++l)
     if (U[l] > 0) b.qp[c0 + P * l] = U[l] / U[0];
+  if constexpr (N == 8) b.qp[c0 + P * 7] = fmax2(U[7] / U[0], 0.0);  // lusgs.f90:2685-2687
   // a NaN or negative density/pressure (the reference carries it on; the
   // library reports it as update_with does, update.f90:448)
   if (!(q[0] >= 0.0) || !(q[4] >= 0.0)) raise_error(b.err, FEST_ERR_NEGATIVE_STATE);
@@ -398,7 +421,9 @@ void launch_lusgs(const Params& p, const DevBlock& b, double* scratch, const Lau
   u.dqs = u.Fold + 6 * d.nv * nc;
   u.dq = u.dqs + lu_count(d) * d.nv;
   const bool plus = p.integ == FEST_TIME_PLUSGS;
-  if (d.nv == 7) plus ? lusgs_t<7, true>(p, b, u, L) : lusgs_t<7, false>(p, b, u, L);
+  if (d.nv == 8) {
+    if (!plus) lusgs_t<8, false>(p, b, u, L);  // PLU-SGS with LCTM2015 is refused at creation
+  } else if (d.nv == 7) plus ? lusgs_t<7, true>(p, b, u, L) : lusgs_t<7, false>(p, b, u, L);
   else plus ? lusgs_t<5, true>(p, b, u, L) : lusgs_t<5, false>(p, b, u, L);
 }
 

@@ -32,7 +32,7 @@ FLUX = {"ausm": 0, "ausmP": 1, "ausmUP": 2, "slau": 3, "ldfss0": 4, "van_leer": 
 INTERP = {"none": 0, "muscl": 1, "ppm": 2, "weno": 3, "weno_NM": 4}
 TIME = {"none": 0, "RK2": 1, "RK4": 2, "TVDRK2": 3, "TVDRK3": 4, "implicit": 5, "plusgs": 6}
 TURB = {"none": 0, "sst": 1, "sst2003": 2, "sa": 3, "kkl": 4}
-TRANSITION = {"none": 0, "bc": 1}
+TRANSITION = {"none": 0, "bc": 1, "lctm2015": 2}
 MU = {"constant": 0, "sutherland_law": 1}
 LIMITER = {"koren": 0, "van_albada": 1}
 FEST_FP64, FEST_MIXED = 0, 1
@@ -49,7 +49,7 @@ class Flow(C.Structure):
         "tk_inf", "tw_inf", "vel_mag", "MInf", "gm", "R_gas", "mu_ref", "T_ref",
         "Sutherland_temp", "Pr", "tPr")] + [("mu_variation", C.c_int), ("reserved", C.c_int),
                                             ("tv_inf", C.c_double), ("tkl_inf", C.c_double),
-                                            ("tu_inf", C.c_double)]
+                                            ("tu_inf", C.c_double), ("tgm_inf", C.c_double)]
 
 
 class Scheme(C.Structure):
@@ -70,14 +70,15 @@ class BC(C.Structure):
     _fields_ = [("id", I6), ("partner_block", I6), ("partner_face", I6)] + [(n, D6) for n in (
         "fixed_density", "fixed_pressure", "fixed_x_speed", "fixed_y_speed", "fixed_z_speed",
         "fixed_tk", "fixed_tw", "fixed_wall_temperature", "fixed_Tpressure", "fixed_Ttemperature")] + [
-        ("block_id", C.c_int), ("partner_orient", I6), ("fixed_tv", D6), ("fixed_tkl", D6)]
+        ("block_id", C.c_int), ("partner_orient", I6), ("fixed_tv", D6), ("fixed_tkl", D6),
+        ("fixed_tgm", D6)]
 
 
 def make_flow(**kw):
     """flowtype with the reference defaults (vartypes.f90:236-285) and the
     derived vel_mag / MInf of init_infinity_values (state.f90:87-88)."""
     d = dict(density_inf=1.2, x_speed_inf=100.0, y_speed_inf=0.0, z_speed_inf=0.0,
-             pressure_inf=101325.0, tk_inf=0.0, tw_inf=0.0, tv_inf=0.0, tkl_inf=0.0, tu_inf=0.0, gm=1.4,
+             pressure_inf=101325.0, tk_inf=0.0, tw_inf=0.0, tv_inf=0.0, tkl_inf=0.0, tu_inf=1.0, tgm_inf=1.0, gm=1.4,
              R_gas=287.0,
              mu_ref=0.0, T_ref=300.0, Sutherland_temp=110.0, Pr=0.7, tPr=0.9,
              mu_variation="constant")
@@ -159,15 +160,16 @@ def make_bc(ids, partners=None, block_id=0, **fixed):
 
 
 def n_var_for(scheme):
-    """set_n_var_value (state.f90:280-305): 5, 6 for Spalart-Allmaras, 7 for
-    the two-equation models"""
-    return {0: 5, TURB["sa"]: 6}.get(scheme.turbulence, 7)
+    """set_n_var_value (state.f90:280-320): 5, 6 for Spalart-Allmaras, 7 for
+    the two-equation models, one more with LCTM2015's intermittency"""
+    n = {0: 5, TURB["sa"]: 6}.get(scheme.turbulence, 7)
+    return n + (scheme.transition == TRANSITION["lctm2015"])
 
 
 def n_grad_for(n_var):
-    """get_n_grad (gradients.f90:229-258): u, v, w, T and the turbulence
-    variables"""
-    return {5: 4, 6: 5}.get(n_var, 6)
+    """get_n_grad (gradients.f90:229-270): u, v, w, T and the turbulence
+    (and LCTM2015's intermittency) variables"""
+    return {5: 4, 6: 5, 8: 7}.get(n_var, 6)
 
 
 # ---- Fortran-shaped array helpers ----------------------------------------

@@ -108,7 +108,8 @@ def random_state(ext, seed=0, mach=0.3, amp=0.1, p0=101325.0, rho0=1.2, tk=1.0, 
                  rho_amp=None, tv=1e-4):
     """Smooth 3-mode Fourier field over the padded block: rho in
     rho0*(1 +- amp), |u| up to mach*c, p0*(1 +- amp), positive tk/tw
-    (seven variables) or tv (six, Spalart-Allmaras)."""
+    (seven variables) or tv (six, Spalart-Allmaras), and an intermittency in
+    (0.1, 0.9) (eight, LCTM2015)."""
     rng = np.random.default_rng(seed)
     ni, nj, nk = ext.imx + 5, ext.jmx + 5, ext.kmx + 5
     I, J, K = np.meshgrid(np.arange(ni) / ni, np.arange(nj) / nj, np.arange(nk) / nk, indexing="ij")
@@ -134,6 +135,8 @@ def random_state(ext, seed=0, mach=0.3, amp=0.1, p0=101325.0, rho0=1.2, tk=1.0, 
     elif ext.n_var > 5:
         qp[..., 5] = tk * (1 + 0.5 * field())
         qp[..., 6] = tw * (1 + 0.5 * field())
+    if ext.n_var == 8:  # LCTM2015's intermittency, inside (0, 1)
+        qp[..., 7] = 0.5 + 0.4 * field()
     return qp
 
 

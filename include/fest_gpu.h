@@ -77,8 +77,13 @@ enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
 /* transition model (schemetype%transition): FEST_TRANSITION_BC, the
  * algebraic 'bc' intermittency on the production of SA ('saBC',
  * source.f90:985-1194) or k-omega SST (source.f90:467-604); FP64 module
- * path, explicit integrators */
-enum { FEST_TRANSITION_NONE = 0, FEST_TRANSITION_BC = 1 };
+ * path, explicit integrators (and LU-SGS/PLU-SGS for SST-BC).
+ * FEST_TRANSITION_LCTM2015: Menter's 2015 one-equation intermittency model
+ * on k-omega SST (n_var = 8, the eighth variable the intermittency;
+ * source.f90:273-465, viscous.f90:658-749, viscosity.f90:265-280, CC.f90,
+ * lusgs.f90:2263-2700), FP64 module path, explicit integrators and
+ * LU-SGS */
+enum { FEST_TRANSITION_NONE = 0, FEST_TRANSITION_BC = 1, FEST_TRANSITION_LCTM2015 = 2 };
 /* MUSCL limiter: the reference hard-codes Koren's alpha family
  * (muscl.f90:151,176); van Albada (muscl.f90:178, commented out there) is an
  * extension selectable here. */
@@ -107,6 +112,7 @@ typedef struct {            /* flowtype, vartypes.f90:235-286 */
   double tv_inf;            /* Spalart-Allmaras free-stream tv (state.f90:106-109) */
   double tkl_inf;           /* k-kL free-stream kL (state.f90:101-103) */
   double tu_inf;            /* free-stream turbulence intensity, percent (flow%tu_inf) */
+  double tgm_inf;           /* LCTM2015 free-stream intermittency (state.f90:261-265) */
 } fest_flow;
 
 typedef struct {            /* schemetype, vartypes.f90:197-232 */
@@ -158,6 +164,8 @@ typedef struct {            /* boundarytype, vartypes.f90:289-367 */
   double fixed_tv[6];
   /* fixed kL of each face for k-kL blocks (read_bc.f90) */
   double fixed_tkl[6];
+  /* fixed intermittency of each face for LCTM2015 blocks (bc%fixed_tgm) */
+  double fixed_tgm[6];
 } fest_bc;
 
 typedef struct fest_handle fest_handle;

@@ -144,8 +144,9 @@ fo_block *fo_create(const fest_extent *d, const fest_flow *flow,
   long P = (long)(imx + 5) * (jmx + 5) * (kmx + 5);
   long N = (long)(imx - 1) * (jmx - 1) * (kmx - 1);
   long Ng = (long)(imx + 1) * (jmx + 1) * (kmx + 1);
-  /* get_n_grad (gradients.f90:229-258) */
+  /* get_n_grad (gradients.f90:229-270): LCTM2015 adds the intermittency's */
   b->n_grad = scheme->turbulence == FEST_TURB_NONE ? 4 : scheme->turbulence == FEST_TURB_SA ? 5 : 6;
+  if (scheme->transition == FEST_TRANSITION_LCTM2015) b->n_grad += 1;
   b->sz[FO_QP] = P * n;
   b->sz[FO_TEMP] = P;
   b->sz[FO_NODES] = (long)(imx + 6) * (jmx + 6) * (kmx + 6) * 3;
@@ -453,6 +454,9 @@ static int is_sst(const fo_block *b) {
 static int is_sa(const fo_block *b) { return b->sc.turbulence == FEST_TURB_SA; }
 static int is_kkl(const fo_block *b) { return b->sc.turbulence == FEST_TURB_KKL; }
 static int is_turb(const fo_block *b) { return b->sc.turbulence != FEST_TURB_NONE; }
+/* LCTM2015 (scheme%transition 'lctm2015' on SST): the eighth variable is
+ * the intermittency */
+static int is_lctm(const fo_block *b) { return b->sc.transition == FEST_TRANSITION_LCTM2015; }
 
 /* bc_primitive.f90:1778-1945 temp_based_density */
 static void temp_based_density(fo_block *b, int f) {
@@ -619,6 +623,10 @@ static void riemann_face(fo_block *b, int f, int total_pressure) {
     if (last_positive) { copy3(b, 6, CP_FLAT, f); copy3(b, 7, CP_FLAT, f); }
     else { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tkl[f], f); }
   }
+  if (is_lctm(b) && na > 0 && nb > 0) {
+    if (last_positive) copy3(b, 8, CP_FLAT, f);
+    else fixv(b, 8, b->bc.fixed_tgm[f], f);
+  }
   /* plane copy of layer 1 into layers 2 and 3, all tangential indices */
   int imx = IMX, jmx = JMX, kmx = KMX;
   for (int l = 1; l <= NV; ++l)
@@ -771,7 +779,7 @@ static void corners(fo_block *b) {
 
 /* bc_primitive.f90:55-226 populate_ghost_primitive */
 int fo_populate_ghost_primitive(fo_block *b, int it) {
-  int sst = is_sst(b), sa = is_sa(b), kkl = is_kkl(b);
+  int sst = is_sst(b), sa = is_sa(b), kkl = is_kkl(b), lctm = is_lctm(b);
   for (int f = 0; f < 6; ++f) {
     switch (b->bc.id[f]) {
     case -1: /* supersonic_inlet */
@@ -784,6 +792,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
         if (sst) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tw[f], f); }
         if (sa) fixv(b, 6, b->bc.fixed_tv[f], f);
         if (kkl) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tkl[f], f); }
+        if (lctm) fixv(b, 8, b->bc.fixed_tgm[f], f); /* bc_primitive.f90:258-264, 339-345 */
       }
       break;
     case -2: /* supersonic_outlet */
@@ -799,6 +808,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
         if (sst) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tw[f], f); }
         if (sa) fixv(b, 6, b->bc.fixed_tv[f], f);
         if (kkl) { fixv(b, 6, b->bc.fixed_tk[f], f); fixv(b, 7, b->bc.fixed_tkl[f], f); }
+        if (lctm) fixv(b, 8, b->bc.fixed_tgm[f], f); /* bc_primitive.f90:258-264, 339-345 */
       }
       copy3(b, 5, CP_FLAT, f);
       break;
@@ -808,6 +818,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
       if (sst) { copy3(b, 6, CP_FLAT, f); copy3(b, 7, CP_FLAT, f); }
       if (sa) copy3(b, 6, CP_FLAT, f);
       if (kkl) { copy3(b, 6, CP_FLAT, f); copy3(b, 7, CP_FLAT, f); }
+      if (lctm) copy3(b, 8, CP_FLAT, f); /* bc_primitive.f90:384-387 */
       break;
     case -5: /* wall: pressure symm, temp_based_density, no_slip */
       copy3(b, 5, CP_SYMM, f);
@@ -818,6 +829,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
       if (sst) { copy3(b, 6, CP_ANTI, f); set_omega_at_wall(b, f); }
       if (sa) copy3(b, 6, CP_ANTI, f);
       if (kkl) { copy3(b, 6, CP_ANTI, f); copy3(b, 7, CP_ANTI, f); }
+      if (lctm) copy3(b, 8, CP_FLAT, f); /* flat at the wall too (bc_primitive.f90:554-557) */
       break;
     case -6: /* slip_wall */
       copy3(b, 1, CP_SYMM, f);
@@ -825,6 +837,7 @@ int fo_populate_ghost_primitive(fo_block *b, int it) {
       if (sst) { copy3(b, 6, CP_SYMM, f); copy3(b, 7, CP_SYMM, f); }
       if (sa) copy3(b, 6, CP_SYMM, f);
       if (kkl) { copy3(b, 6, CP_SYMM, f); copy3(b, 7, CP_SYMM, f); }
+      if (lctm) copy3(b, 8, CP_FLAT, f); /* flat, not symm (bc_primitive.f90:436-439) */
       flow_tangency(b, f);
       break;
     case -8: riemann_face(b, f, 0); break;
@@ -1412,6 +1425,8 @@ int fo_evaluate_all_gradients(fo_block *b) {
     }
   if (is_sa(b))  /* gradtv (gradients.f90:165-169) */
     for (int c = 0; c < ncomp; ++c) gradient_G(b, g[c], 5, q, 6, c);
+  if (is_lctm(b))  /* gradtgm (gradients.f90:382-388) */
+    for (int c = 0; c < ncomp; ++c) gradient_G(b, g[c], 7, q, 8, c);
   int err = FEST_OK;
   for (int c = 0; c < 3; ++c)
     for (long p = 0; p < b->sz[FO_GX + c]; ++p)
@@ -1539,6 +1554,21 @@ int fo_calculate_viscosity(fo_block *b) {
         double a2 = arg1 * arg1;
         *at(F1, i, j, k, 1) = tanh(a2 * a2);
       }
+  if (is_lctm(b)) {
+    /* viscosity.f90:265-280, 390-405: F1 raised to exp(-(var1/120)**8).
+     * The loop there reads density and tk without setting them, so they
+     * hold the last cell of the loop before it, (imx, jmx, kmx). */
+    double rho_c = *at(q, IMX, JMX, KMX, 1), tk_c = *at(q, IMX, JMX, KMX, 6);
+    OMP_FOR
+    for (int k = 0; k <= KMX; ++k)
+      for (int j = 0; j <= JMX; ++j)
+        for (int i = 0; i <= IMX; ++i) {
+          double var1 = rho_c * *at(dist, i, j, k, 1) * sqrt(tk_c) / *at(mu, i, j, k, 1);
+          double x = var1 / 120, x2 = x * x, x4 = x2 * x2;
+          double var2 = exp(-(x4 * x4));
+          *at(F1, i, j, k, 1) = fmax2(*at(F1, i, j, k, 1), var2);
+        }
+  }
   /* ghost copies of mu_t and F1 (viscosity.f90:287-340, 405-460) */
   for (int f = 0; f < 6; ++f) {
     int id = b->bc.id[f];
@@ -1697,6 +1727,37 @@ static void viscous_sa(fo_block *b, int dir) {
 }
 
 /* viscous.f90:450-567 compute_viscous_fluxes_kkl */
+/* viscous.f90:658-749 compute_viscous_fluxes_lctm2015: the intermittency's
+ * diffusion with mu + mu_t, its face gradient corrected along the line of
+ * centres as the other variables' are */
+static void viscous_lctm(fo_block *b, int dir) {
+  V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), Fl = vflux(b, dir);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
+  R4 fa = vfaces(b, dir), cl = vcells(b);
+  int ii = dir == 0, jj = dir == 1, kk = dir == 2;
+  OMP_FOR
+  for (int k = 1; k <= KMX - 1 + kk; ++k)
+    for (int j = 1; j <= JMX - 1 + jj; ++j)
+      for (int i = 1; i <= IMX - 1 + ii; ++i) {
+        int im = i - ii, jm = j - jj, km = k - kk;
+        double G[3];
+        for (int c = 0; c < 3; ++c) G[c] = 0.5 * (*at(g[c], im, jm, km, 7) + *at(g[c], i, j, k, 7));
+        const double *c1 = r4(cl, i, j, k), *c0 = r4(cl, im, jm, km);
+        double delx = c1[1] - c0[1], dely = c1[2] - c0[2], delz = c1[3] - c0[3];
+        double d_LR = sqrt(delx * delx + dely * dely + delz * delz);
+        double deltgm = *at(q, i, j, k, 8) - *at(q, im, jm, km, 8);
+        double nc = (deltgm - (G[0] * delx + G[1] * dely + G[2] * delz)) / d_LR;
+        G[0] = G[0] + (nc * delx / d_LR);
+        G[1] = G[1] + (nc * dely / d_LR);
+        G[2] = G[2] + (nc * delz / d_LR);
+        double mu_f = 0.5 * (*at(mu, im, jm, km, 1) + *at(mu, i, j, k, 1));
+        double mut_f = 0.5 * (*at(mut, im, jm, km, 1) + *at(mut, i, j, k, 1));
+        const double *fc = r4(fa, i, j, k);
+        double nx = fc[1], ny = fc[2], nz = fc[3], area = fc[0];
+        *at(Fl, i, j, k, 8) = *at(Fl, i, j, k, 8) - (area * ((mu_f + mut_f) * (G[0] * nx + G[1] * ny + G[2] * nz)));
+      }
+}
+
 static void viscous_kkl(fo_block *b, int dir) {
   V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), Fl = vflux(b, dir);
   V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
@@ -1748,6 +1809,11 @@ int fo_compute_viscous_fluxes(fo_block *b) {
     viscous_sst(b, 0);
     viscous_sst(b, 1);
     if (KMX != 2) viscous_sst(b, 2);
+  }
+  if (is_lctm(b)) { /* viscous.f90:115-125 */
+    viscous_lctm(b, 0);
+    viscous_lctm(b, 1);
+    if (KMX != 2) viscous_lctm(b, 2);
   }
   for (int dir = 0; dir < 3; ++dir)
     for (long p = 0; p < b->sz[FO_F + dir]; ++p)
@@ -2021,8 +2087,102 @@ static void sst_bc_source(fo_block *b) {
       }
 }
 
+/* source.f90:273-465 add_sst_source_lctm2015: the SST source with the
+ * production by vorticity times strain, scaled by the intermittency, its
+ * limited extra production and the floored destruction, and the
+ * intermittency's own source (onset from the vorticity Reynolds number
+ * against 100 + 1000 exp(-Tu Fpg), Fpg from the wall-normal derivative of
+ * the wall distance, CC.f90); the SST constants of the variant (sst2003's
+ * gama1, gama2 and limiter 10) */
+static void lctm_source(fo_block *b) {
+  V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), F1v = vpad(b, FO_F1), dist = vpad(b, FO_DIST);
+  V r = vres(b);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
+  R4 fa[3] = {vfaces(b, 0), vfaces(b, 1), vfaces(b, 2)}, cl = vcells(b);
+  const int s2003 = b->sc.turbulence == FEST_TURB_SST2003;
+  const int limiter = s2003 ? 10 : 20;
+  const double cdmin = s2003 ? 1.0e-10 : 1e-20; /* 10.0**(-limiter) */
+  double gama1 = (beta1 / bstar) - ((sigma_w1 * (kappa_sst * kappa_sst)) / sqrt(bstar));
+  double gama2 = (beta2 / bstar) - ((sigma_w2 * (kappa_sst * kappa_sst)) / sqrt(bstar));
+  if (s2003) {
+    gama1 = 5.0 / 9.0;
+    gama2 = 0.44;
+  }
+  OMP_FOR
+  for (int k = 1; k <= KMX - 1; ++k)
+    for (int j = 1; j <= JMX - 1; ++j)
+      for (int i = 1; i <= IMX - 1; ++i) {
+#define GR(c, l) (*at(g[c], i, j, k, l))
+        double density = *at(q, i, j, k, 1), tk = *at(q, i, j, k, 6), tw = *at(q, i, j, k, 7);
+        double gm_ = *at(q, i, j, k, 8);
+        double wa = GR(1, 3) - GR(2, 2), wb = GR(2, 1) - GR(0, 3), wc = GR(0, 2) - GR(1, 1);
+        double vort = sqrt(((wa * wa) + (wb * wb) + (wc * wc)));
+        double sa_ = GR(1, 3) + GR(2, 2), sb = GR(2, 1) + GR(0, 3), sc_ = GR(0, 2) + GR(1, 1);
+        double strain = sqrt((sa_ * sa_) + (sb * sb) + (sc_ * sc_) + 2 * (GR(0, 1) * GR(0, 1)) +
+                             2 * (GR(1, 2) * GR(1, 2)) + 2 * (GR(2, 3) * GR(2, 3)));
+        double CD = 2 * density * sigma_w2 * (GR(0, 5) * GR(0, 6) + GR(1, 5) * GR(1, 6) + GR(2, 5) * GR(2, 6)) / tw;
+        CD = fmax2(CD, cdmin);
+        double F1 = *at(F1v, i, j, k, 1);
+        double gama = gama1 * F1 + gama2 * (1. - F1);
+        double beta = beta1 * F1 + beta2 * (1. - F1);
+        double D_k = bstar * density * tw * tk;
+        double D_w = beta * density * (tw * tw);
+        double divergence = GR(0, 1) + GR(1, 2) + GR(2, 3);
+        double mt = *at(mut, i, j, k, 1), m = *at(mu, i, j, k, 1), d = *at(dist, i, j, k, 1);
+        double P_k = mt * (vort * strain) - ((2.0 / 3.0) * density * tk * divergence);
+        P_k = fmin2(P_k, limiter * D_k);
+        double P_w = (density * gama / mt) * P_k;
+        double lamda = (1. - F1) * CD;
+        /* CC.f90:56-75, 87-92: the gradient of the wall distance (the same
+         * face sums as compute_gradient there) dotted with its unit vector */
+        double dd[3];
+        {
+          const double d0 = d;
+          const double dn[6] = {*at(dist, i - 1, j, k, 1), *at(dist, i, j - 1, k, 1), *at(dist, i, j, k - 1, 1),
+                                *at(dist, i + 1, j, k, 1), *at(dist, i, j + 1, k, 1), *at(dist, i, j, k + 1, 1)};
+          const double *fr[6] = {r4(fa[0], i, j, k), r4(fa[1], i, j, k), r4(fa[2], i, j, k),
+                                 r4(fa[0], i + 1, j, k), r4(fa[1], i, j + 1, k), r4(fa[2], i, j, k + 1)};
+          const double vol2 = 2 * r4(cl, i, j, k)[0];
+          for (int c = 0; c < 3; ++c)
+            dd[c] = (-(dn[0] + d0) * fr[0][1 + c] * fr[0][0] - (dn[1] + d0) * fr[1][1 + c] * fr[1][0] -
+                     (dn[2] + d0) * fr[2][1 + c] * fr[2][0] + (dn[3] + d0) * fr[3][1 + c] * fr[3][0] +
+                     (dn[4] + d0) * fr[4][1 + c] * fr[4][0] + (dn[5] + d0) * fr[5][1 + c] * fr[5][0]) /
+                    vol2;
+        }
+        double Vn = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+        double dvdy = dd[0] * (dd[0] / (Vn + 1e-12)) + dd[1] * (dd[1] / (Vn + 1e-12)) + dd[2] * (dd[2] / (Vn + 1e-12));
+        double lamd = (-7.57e-3) * (dvdy * d * d * density / m) + 0.0128;
+        lamd = fmin2(fmax2(lamd, -1.0), 1.0);
+        double Fpg = lamd >= 0.0 ? fmin2(1.0 + 14.68 * lamd, 1.5) : fmin2(1.0 - 7.34 * lamd, 3.0);
+        Fpg = fmax2(Fpg, 0.0);
+        double TuL = fmin2(100.0 * sqrt(2.0 * tk / 3.0) / (tw * d), 100.0);
+        double Re_theta = 100.0 + 1000.0 * exp(-TuL * Fpg);
+        double Rev = density * d * d * strain / m;
+        double RT = density * tk / (m * tw);
+        double h = 0.5 * RT, h2 = h * h;
+        double Fturb = exp(-(h2 * h2));
+        double Fonset1 = Rev / (2.2 * Re_theta);
+        double Fonset2 = fmin2(Fonset1, 2.0);
+        double t3 = RT / 3.5;
+        double Fonset3 = fmax2(1.0 - (t3 * t3) * t3, 0.0);
+        double Fonset = fmax2(Fonset2 - Fonset3, 0.0);
+        double P_gm = 100 * density * strain * gm_ * (1.0 - gm_) * Fonset;
+        double D_gm = 0.06 * density * vort * gm_ * Fturb * ((50.0 * gm_) - 1.0);
+        double Fon_lim = fmin2(fmax2((Rev / (2.2 * 1100.0)) - 1.0, 0.0), 3.0);
+        double Pk_lim = 5 * fmax2(gm_ - 0.2, 0.0) * (1.0 - gm_) * Fon_lim * fmax2(3 * m - mt, 0.0) * strain * vort;
+        double S_k = gm_ * P_k - fmax2(gm_, 0.1) * D_k + Pk_lim;
+        double S_w = P_w - D_w + lamda;
+        double S_gm = P_gm - D_gm;
+        double vol = r4(cl, i, j, k)[0];
+        *at(r, i, j, k, 6) = *at(r, i, j, k, 6) - S_k * vol;
+        *at(r, i, j, k, 7) = *at(r, i, j, k, 7) - S_w * vol;
+        *at(r, i, j, k, 8) = *at(r, i, j, k, 8) - S_gm * vol;
+#undef GR
+      }
+}
+
 /* source.f90:94-155 add_source_term_residue: the SA (and saBC), k-kL and
- * SST (and SST-BC) sources */
+ * SST (and SST-BC, LCTM2015) sources */
 void fo_add_source_term_residue(fo_block *b) {
   const int bc_transition = b->sc.transition == FEST_TRANSITION_BC;
   if (is_sa(b)) {
@@ -2032,6 +2192,10 @@ void fo_add_source_term_residue(fo_block *b) {
   }
   if (is_sst(b) && bc_transition) {
     sst_bc_source(b);
+    return;
+  }
+  if (is_sst(b) && is_lctm(b)) {
+    lctm_source(b);
     return;
   }
   if (is_kkl(b)) {
@@ -2361,11 +2525,13 @@ typedef struct { double A, nx, ny, nz, vol, mu, mut, F1; } lu_face;
  * neighbour state ql advanced by the conservative change du (k and omega
  * kept at ql's values where the advanced ones turn negative), less the
  * thin-layer viscous flux between that state and the cell state qr, times
- * the area; n = 5 (laminar) or 7 (SST) */
+ * the area; n = 5 (laminar), 7 (SST) or 8 (LCTM2015, lctm2015Flux of
+ * lusgs.f90:2702-2856: the intermittency floored at zero, not kept, and
+ * diffused with mu + mu_t) */
 static void lu_flux(const fest_flow *fl, int n, const double *ql, const double *qr, const double *du,
                     const lu_face *f, double *out) {
   const double gm = fl->gm, R = fl->R_gas;
-  double U[7], W[7];
+  double U[8], W[8];
   U[0] = ql[0];
   U[1] = ql[0] * ql[1];
   U[2] = ql[0] * ql[2];
@@ -2380,7 +2546,8 @@ static void lu_flux(const fest_flow *fl, int n, const double *ql, const double *
   W[4] = (gm - 1.0) * (U[4] - (0.5 * (U[1] * U[1] + U[2] * U[2] + U[3] * U[3]) / U[0]));
   for (int l = 5; l < n; ++l) {
     W[l] = U[l] / U[0];
-    W[l] = W[l] + 0.5 * (1. - fsign(1., W[l])) * (ql[l] - W[l]);
+    if (l < 7) W[l] = W[l] + 0.5 * (1. - fsign(1., W[l])) * (ql[l] - W[l]);
+    else W[l] = fmax2(W[l], 0.0);
   }
   const double nx = f->nx, ny = f->ny, nz = f->nz;
   double vn = (W[1] * nx) + (W[2] * ny) + (W[3] * nz);
@@ -2396,7 +2563,7 @@ static void lu_flux(const fest_flow *fl, int n, const double *ql, const double *
   const double mu = f->mu + f->mut, s = f->A;
   double T1 = W[4] / (W[0] * R), T2 = qr[4] / (qr[0] * R);
   double dT[3] = {(T2 - T1) * nx * s / f->vol, (T2 - T1) * ny * s / f->vol, (T2 - T1) * nz * s / f->vol};
-  double g[5][3]; /* g[c][d]: d(u, v, w, k, omega)/d(x_d) */
+  double g[6][3]; /* g[c][d]: d(u, v, w, k, omega, intermittency)/d(x_d) */
   for (int c = 0; c < 3 + (n - 5); ++c) {
     double dv = qr[c < 3 ? 1 + c : 2 + c] - W[c < 3 ? 1 + c : 2 + c];
     g[c][0] = dv * nx * s / f->vol;
@@ -2419,6 +2586,12 @@ static void lu_flux(const fest_flow *fl, int n, const double *ql, const double *
     /* added, as lusgs.f90:1190-1191 has it */
     out[5] = out[5] + (f->mu + sk * f->mut) * (g[3][0] * nx + g[3][1] * ny + g[3][2] * nz);
     out[6] = out[6] + (f->mu + sw * f->mut) * (g[4][0] * nx + g[4][1] * ny + g[4][2] * nz);
+  }
+  if (n == 8) {
+    double sk = sigma_k1 * f->F1 + sigma_k2 * (1.0 - f->F1), sw = sigma_w1 * f->F1 + sigma_w2 * (1.0 - f->F1);
+    out[5] = out[5] + (f->mu + sk * f->mut) * (g[3][0] * nx + g[3][1] * ny + g[3][2] * nz);
+    out[6] = out[6] + (f->mu + sw * f->mut) * (g[4][0] * nx + g[4][1] * ny + g[4][2] * nz);
+    out[7] = out[7] + (f->mu + f->mut) * (g[5][0] * nx + g[5][1] * ny + g[5][2] * nz);
   }
   for (int l = 0; l < n; ++l) out[l] = out[l] * s;
 }
@@ -2500,6 +2673,8 @@ static void lu_sgs(fo_block *b, int plus) {
   const fest_flow *fl = &b->flow;
   const int imx = IMX, jmx = JMX, kmx = KMX, n = NV, sst = is_sst(b);
   V q = vqp(b), mu = vpad(b, FO_MU), mut = vpad(b, FO_MUT), F1 = vpad(b, FO_F1), r = vres(b), dt = vdt(b);
+  V dist = vpad(b, FO_DIST);
+  V g[3] = {vgrad(b, 0), vgrad(b, 1), vgrad(b, 2)};
   R4 cl = vcells(b), fa[3] = {vfaces(b, 0), vfaces(b, 1), vfaces(b, 2)};
   size_t cnt = (size_t)(imx + 1) * (jmx + 1) * (kmx + 1) * n;
   V dqs = mkv((double *)calloc(cnt, sizeof(double)), 0, 0, 0, imx + 1, jmx + 1, kmx + 1);
@@ -2519,7 +2694,7 @@ static void lu_sgs(fo_block *b, int plus) {
         j = jmx - 1 - (c / (kmx - 1)) % (jmx - 1);
         i = imx - 1 - c / ((kmx - 1) * (jmx - 1));
       }
-      double q0[7], qn[6][7], lam[6], sumlam = 0., P[7][7], eps = 0.0;
+      double q0[8], qn[6][8], lam[6], sumlam = 0., P[7][7], eps = 0.0;
       lu_face fc[6];
       const double *c0 = r4(cl, i, j, k) + 1;
       for (int l = 0; l < n; ++l) q0[l] = *at(q, i, j, k, l + 1);
@@ -2544,29 +2719,52 @@ static void lu_sgs(fo_block *b, int plus) {
       }
       for (int s = 0; s < 6; ++s) sumlam = sumlam + lam[s];
       const double vol = r4(cl, i, j, k)[0];
-      double D[7];
+      double D[8];
       for (int l = 0; l < n; ++l) D[l] = (vol / *at(dt, i, j, k, 1)) + 0.5 * sumlam;
       if (sst) { /* lusgs.f90:860-862: the destruction terms of k and omega */
         double f1 = *at(F1, i, j, k, 1), beta = f1 * beta1 + (1.0 - f1) * beta2, w = q0[6];
         D[5] = (D[5] + (bstar * w) * vol);
         D[6] = (D[6] + 2.0 * beta * w * vol);
       }
-      double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+      if (n == 8) { /* lusgs.f90:2455-2475: the intermittency's source, linearised */
+#define GR(c, l) (*at(g[c], i, j, k, l))
+        double density = q0[0], d = *at(dist, i, j, k, 1), m = *at(mu, i, j, k, 1);
+        double wa = GR(1, 3) - GR(2, 2), wb = GR(2, 1) - GR(0, 3), wc = GR(0, 2) - GR(1, 1);
+        double vort = sqrt(((wa * wa) + (wb * wb) + (wc * wc)));
+        double sa_ = GR(1, 3) + GR(2, 2), sb = GR(2, 1) + GR(0, 3), sc_ = GR(0, 2) + GR(1, 1);
+        double strain = sqrt((sa_ * sa_) + (sb * sb) + (sc_ * sc_) + 2 * (GR(0, 1) * GR(0, 1)) +
+                             2 * (GR(1, 2) * GR(1, 2)) + 2 * (GR(2, 3) * GR(2, 3)));
+#undef GR
+        double TuL = fmin2(100.0 * sqrt(2.0 * q0[5] / 3.0) / (q0[6] * d), 100.0);
+        double Re_theta = 100.0 + 1000.0 * exp(-TuL);
+        double Rev = density * d * d * strain / m;
+        double RT = density * q0[5] / (m * q0[6]);
+        double h = 0.5 * RT, h2 = h * h;
+        double Fturb = exp(-(h2 * h2));
+        double Fonset2 = fmin2(Rev / (2.2 * Re_theta), 2.0);
+        double t3 = RT / 3.5;
+        double Fonset3 = fmax2(1.0 - (t3 * t3) * t3, 0.0);
+        double Fonset = fmax2(Fonset2 - Fonset3, 0.0);
+        double Dp = 100 * density * strain * Fonset * (1.0 - 2.0 * q0[7]);
+        double De = 0.06 * vort * Fturb * density * (2.0 * 50.0 * q0[7] - 1.0);
+        D[7] = (D[7] + (-Dp + De) * vol);
+      }
+      double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       for (int d = 0; d < 3; ++d) {
         int s = pass == 0 ? d : 3 + d;
         int ni = i + (pass ? off[d][0] : -off[d][0]), nj = j + (pass ? off[d][1] : -off[d][1]),
             nk = k + (pass ? off[d][2] : -off[d][2]);
         V src = pass == 0 ? dqs : dq;
-        double dn[7], zero[7] = {0, 0, 0, 0, 0, 0, 0}, fnew[7], fold[7];
+        double dn[8], zero[8] = {0, 0, 0, 0, 0, 0, 0, 0}, fnew[8], fold[8];
         for (int l = 0; l < n; ++l) dn[l] = *at(src, ni, nj, nk, l + 1);
         lu_flux(fl, n, qn[s], q0, dn, &fc[s], fnew);
         lu_flux(fl, n, qn[s], q0, zero, &fc[s], fold);
-        double df[7], pdf[7];
+        double df[8], pdf[8];
         for (int l = 0; l < n; ++l) df[l] = fnew[l] - fold[l];
         if (plus) plu_apply(n, P, df, pdf);
         for (int l = 0; l < n; ++l) acc[l] = acc[l] + ((plus ? pdf[l] : df[l]) - lam[s] * dn[l]);
       }
-      double rr[7], pr[7];
+      double rr[8], pr[8];
       for (int l = 0; l < n; ++l) rr[l] = *at(r, i, j, k, l + 1);
       if (plus) plu_apply(n, P, rr, pr);
       for (int l = 0; l < n; ++l) {
@@ -2581,7 +2779,7 @@ static void lu_sgs(fo_block *b, int plus) {
   for (int k = 1; k <= kmx - 1; ++k)
     for (int j = 1; j <= jmx - 1; ++j)
       for (int i = 1; i <= imx - 1; ++i) {
-        double *p[7], U[7];
+        double *p[8], U[8];
         for (int l = 0; l < n; ++l) p[l] = at(q, i, j, k, l + 1);
         U[0] = *p[0];
         U[1] = *p[0] * *p[1];
@@ -2595,8 +2793,12 @@ static void lu_sgs(fo_block *b, int plus) {
         *p[2] = U[2] / U[0];
         *p[3] = U[3] / U[0];
         *p[4] = (gm - 1.0) * (U[4] - (0.5 * (U[1] * U[1] + U[2] * U[2] + U[3] * U[3]) / U[0]));
-        for (int l = 5; l < n; ++l)
+        for (int l = 5; l < n && l < 7; ++l)
           if (U[l] > 0) *p[l] = U[l] / U[0];
+        if (n == 8) { /* lusgs.f90:2685-2687 */
+          *p[7] = U[7] / U[0];
+          *p[7] = fmax2(*p[7], 0.0);
+        }
       }
   free(dqs.p);
   free(dq.p);
@@ -2607,9 +2809,11 @@ static void lu_sgs(fo_block *b, int plus) {
  * plusgs.f90:161-170) */
 static int implicit_next_solution(fo_block **bl, int nb, int it, double CFL, int plus) {
   for (int n = 0; n < nb; ++n) {
-    int t = bl[n]->sc.turbulence;
-    if (!((t == FEST_TURB_NONE && bl[n]->d.n_var == 5) || ((t == FEST_TURB_SST || t == FEST_TURB_SST2003) && bl[n]->d.n_var == 7)))
+    int t = bl[n]->sc.turbulence, lctm = is_lctm(bl[n]);
+    if (!((t == FEST_TURB_NONE && bl[n]->d.n_var == 5) ||
+          ((t == FEST_TURB_SST || t == FEST_TURB_SST2003) && bl[n]->d.n_var == 7 + lctm)))
       return FEST_ERR_ARG;
+    if (lctm && plus) return FEST_ERR_ARG; /* PLU-SGS's LCTM2015 branch is not restated */
   }
   for (int n = 0; n < nb; ++n) fo_compute_temperature(bl[n]);
   int err = fo_get_total_conservative_residue(bl, nb, it);
@@ -2642,6 +2846,10 @@ void fo_find_resnorm(fo_block **bl, int nb, double *out) {
     sc[5] = (0.5 * fl->density_inf * (fl->vel_mag * fl->vel_mag * fl->vel_mag) + ((fl->gm / (fl->gm - 1.)) * fl->pressure_inf));
     sc[6] = fl->density_inf * fl->vel_mag * (b->sc.turbulence == FEST_TURB_SA ? fl->tv_inf : fl->tk_inf);
     sc[7] = fl->density_inf * fl->vel_mag * (b->sc.turbulence == FEST_TURB_KKL ? fl->tkl_inf : fl->tw_inf);
+    /* the intermittency's scale: setup_scale (resnorm.f90:128-167) leaves
+     * Res_scale(8) unset, so the norm of the eighth residual is taken
+     * unscaled */
+    sc[8] = 1.0;
     V r = vres(b), F = vflux(b, 0), G = vflux(b, 1), H = vflux(b, 2);
     for (int l = 1; l <= n; ++l) {
       double s = 0.0;

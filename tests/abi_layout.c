@@ -34,6 +34,7 @@ int main(void) {
   printf("fest_flow.tv_inf %zu\n", offsetof(fest_flow, tv_inf));
   printf("fest_flow.tkl_inf %zu\n", offsetof(fest_flow, tkl_inf));
   printf("fest_flow.tu_inf %zu\n", offsetof(fest_flow, tu_inf));
+  printf("fest_flow.tgm_inf %zu\n", offsetof(fest_flow, tgm_inf));
   printf("fest_scheme %zu\n", sizeof(fest_scheme));
   printf("fest_scheme.scheme_name %zu\n", offsetof(fest_scheme, scheme_name));
   printf("fest_scheme.interpolant %zu\n", offsetof(fest_scheme, interpolant));
@@ -71,5 +72,6 @@ int main(void) {
   printf("fest_bc.partner_orient %zu\n", offsetof(fest_bc, partner_orient));
   printf("fest_bc.fixed_tv %zu\n", offsetof(fest_bc, fixed_tv));
   printf("fest_bc.fixed_tkl %zu\n", offsetof(fest_bc, fixed_tkl));
+  printf("fest_bc.fixed_tgm %zu\n", offsetof(fest_bc, fixed_tgm));
   return 0;
 }

@@ -89,7 +89,8 @@ def small_case(nc=(9, 7, 6), ids=(-5, -5, -5, -3, -10, -10), scheme_kw=None, flo
     # turb: False, True (k-omega SST, seven variables), "sa" (six) or
     # "kkl" (seven: k and kL)
     sa, kkl = turb == "sa", turb == "kkl"
-    ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 6 if sa else 7 if turb else 5)
+    lctm = (scheme_kw or {}).get("transition") == "lctm2015"
+    ext = abi.Extent(nc[0] + 1, nc[1] + 1, nc[2] + 1, 6 if sa else 8 if lctm else 7 if turb else 5)
     fk = dict(density_inf=1.2, x_speed_inf=60.0, y_speed_inf=5.0, pressure_inf=101325.0)
     if sa:
         fk["tv_inf"] = 1.2e-4
@@ -104,7 +105,8 @@ def small_case(nc=(9, 7, 6), ids=(-5, -5, -5, -3, -10, -10), scheme_kw=None, flo
     scheme = abi.make_scheme(**sk)
     fx = {k: [0.0] * 6 for k in ("fixed_density", "fixed_x_speed", "fixed_y_speed",
                                  "fixed_z_speed", "fixed_pressure", "fixed_tk", "fixed_tw",
-                                 "fixed_wall_temperature", "fixed_Tpressure", "fixed_tv", "fixed_tkl")}
+                                 "fixed_wall_temperature", "fixed_Tpressure", "fixed_tv", "fixed_tkl",
+                                 "fixed_tgm")}
     for f in range(6):
         fx["fixed_density"][f] = 1.15 + 0.01 * f
         fx["fixed_x_speed"][f] = 40.0 + f
@@ -116,6 +118,7 @@ def small_case(nc=(9, 7, 6), ids=(-5, -5, -5, -3, -10, -10), scheme_kw=None, flo
         fx["fixed_Tpressure"][f] = 104000.0 + 50 * f
         fx["fixed_tv"][f] = 1.1e-4 + 1e-6 * f
         fx["fixed_tkl"][f] = 1.9e-3 + 2e-5 * f
+        fx["fixed_tgm"][f] = 0.9 + 0.01 * f
     for k, v in (fixed or {}).items():
         fx[k] = list(v)
     if partners is None:
