@@ -205,3 +205,26 @@ def test_create_refuses_transition_outside_sa_and_sst():
     assert create("sst", 7, abi.TRANSITION["bc"], mu_ref=0.0) == abi.FEST_ERR_ARG
     assert create("sst", 7, abi.TRANSITION["bc"]) != abi.FEST_ERR_ARG
     assert create("sa", 6, abi.TRANSITION["bc"]) != abi.FEST_ERR_ARG
+
+
+def test_sst_bc_runs_with_lusgs():
+    """The implicit integrators update SST-BC blocks as SST ones
+    (lusgs.f90:161-164): LU-SGS takes them, and its iterations differ from
+    plain SST's only through the source."""
+    out = []
+    for transition in ("bc", "none"):
+        ext, flow, scheme, bc, nodes, qp = small_case(
+            nc=(9, 7, 6), turb=True, ids=(-3, -4, -5, -6, -10, -10),
+            scheme_kw=dict(transition=transition, time_step_accuracy="implicit", scheme_name="ausmUP"),
+            flow_kw=dict(mu_ref=0.1, mu_variation="constant", tu_inf=3.0, tk_inf=1.0, tw_inf=1000.0))
+        blk = O.Block(ext, flow, scheme, bc)
+        blk["nodes"] = nodes
+        blk.setup_geometry()
+        blk["dist"] = 0.02 + np.abs(blk["cells"][2])
+        blk["qp"] = qp
+        for it in (1, 2):
+            assert O.lusgs_next_solution([blk], it, 20.0) == 0
+        out.append(np.array(blk["qp"]))
+    sl = (slice(3, ext.imx + 2), slice(3, ext.jmx + 2), slice(3, ext.kmx + 2))
+    assert np.all(np.isfinite(out[0][sl]))
+    assert np.abs(out[0][sl + (5,)] - out[1][sl + (5,)]).max() > 0.0
