@@ -457,11 +457,9 @@ int fest_create(const fest_extent* dims, const fest_flow* flow, const fest_schem
   if (scheme->transition == FEST_TRANSITION_BC &&
       (scheme->turbulence == FEST_TURB_NONE || scheme->turbulence == FEST_TURB_KKL || flow->mu_ref <= 0.0))
     return FEST_ERR_ARG;
-  // LCTM2015 sits on k-omega SST (source.f90:134-143); PLU-SGS's LCTM2015
-  // update (plusgs.f90:2130-2624) is not built
+  // LCTM2015 sits on k-omega SST (source.f90:134-143)
   if (scheme->transition == FEST_TRANSITION_LCTM2015 &&
-      (!(scheme->turbulence == FEST_TURB_SST || scheme->turbulence == FEST_TURB_SST2003) || flow->mu_ref <= 0.0 ||
-       scheme->time_step_accuracy == FEST_TIME_PLUSGS))
+      (!(scheme->turbulence == FEST_TURB_SST || scheme->turbulence == FEST_TURB_SST2003) || flow->mu_ref <= 0.0))
     return FEST_ERR_ARG;
   if (scheme->time_stepping_method != 'l' && scheme->time_stepping_method != 'g') return FEST_ERR_ARG;
   for (int f = 0; f < 6; ++f) {

@@ -2,8 +2,8 @@
 // the local time step, then update_with_lusgs (update.f90:215-218,
 // lusgs.f90:134-1196) or its low-Mach preconditioned form
 // update_with_plusgs (update.f90:219-222, plusgs.f90:139-1431), for laminar
-// and k-omega SST blocks, FP64; LU-SGS also for SST blocks with LCTM2015's
-// intermittency (update_lctm2015, lusgs.f90:2263-2700).
+// and k-omega SST blocks, FP64; both also for SST blocks with LCTM2015's
+// intermittency (update_lctm2015, lusgs.f90:2263-2700, plusgs.f90:2130-2624).
 //
 // The reference sweeps the interior cells forward (i fastest, then j, k)
 // computing dQ* from the dQ* of each cell's three lower neighbours, then
@@ -155,7 +155,9 @@ struct PluP {
     const double H = (gm * pr / (r * (gm - 1.0))) + 0.5 * (VMag);
     eps = fmin(1.0, fmax(M * M, p.MInf * p.MInf));
     const double factor = (1.0 - eps) * (gm - 1.0) / (SoundMag * SoundMag);
-    const double x[7] = {1.0, u, v, w, H, N == 7 ? q0[5 % N] : 0.0, N == 7 ? q0[6 % N] : 0.0};
+    // plusgs.f90:2338-2355 adds the intermittency to x and a zero to c
+    const double x[8] = {1.0, u, v, w, H, N >= 7 ? q0[5 % N] : 0.0, N >= 7 ? q0[6 % N] : 0.0,
+                         N == 8 ? q0[7 % N] : 0.0};
 #pragma unroll
     for (int i = 0; i < N; ++i) fx[i] = factor * x[i];
   }
@@ -168,10 +170,11 @@ struct PluP {
       s = s + ((i == 2 ? 1.0 : 0.0) - fx[i] * (-v)) * y[2];
       s = s + ((i == 3 ? 1.0 : 0.0) - fx[i] * (-w)) * y[3];
       s = s + ((i == 4 ? 1.0 : 0.0) - fx[i] * (1.)) * y[4];
-      if constexpr (N == 7) {
+      if constexpr (N >= 7) {
         s = s + ((i == 5 ? 1.0 : 0.0) - fx[i] * (-1.)) * y[5];
         s = s + ((i == 6 ? 1.0 : 0.0) - fx[i] * (0.)) * y[6];
       }
+      if constexpr (N == 8) s = s + ((i == 7 ? 1.0 : 0.0) - fx[i] * (0.)) * y[7];
       out[i] = s;
     }
   }
@@ -421,9 +424,8 @@ void launch_lusgs(const Params& p, const DevBlock& b, double* scratch, const Lau
   u.dqs = u.Fold + 6 * d.nv * nc;
   u.dq = u.dqs + lu_count(d) * d.nv;
   const bool plus = p.integ == FEST_TIME_PLUSGS;
-  if (d.nv == 8) {
-    if (!plus) lusgs_t<8, false>(p, b, u, L);  // PLU-SGS with LCTM2015 is refused at creation
-  } else if (d.nv == 7) plus ? lusgs_t<7, true>(p, b, u, L) : lusgs_t<7, false>(p, b, u, L);
+  if (d.nv == 8) plus ? lusgs_t<8, true>(p, b, u, L) : lusgs_t<8, false>(p, b, u, L);
+  else if (d.nv == 7) plus ? lusgs_t<7, true>(p, b, u, L) : lusgs_t<7, false>(p, b, u, L);
   else plus ? lusgs_t<5, true>(p, b, u, L) : lusgs_t<5, false>(p, b, u, L);
 }
 

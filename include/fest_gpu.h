@@ -81,8 +81,8 @@ enum { FEST_MU_CONSTANT = 0, FEST_MU_SUTHERLAND = 1 };
  * FEST_TRANSITION_LCTM2015: Menter's 2015 one-equation intermittency model
  * on k-omega SST (n_var = 8, the eighth variable the intermittency;
  * source.f90:273-465, viscous.f90:658-749, viscosity.f90:265-280, CC.f90,
- * lusgs.f90:2263-2700), FP64 module path, explicit integrators and
- * LU-SGS */
+ * lusgs.f90:2263-2700, plusgs.f90:2130-2624), FP64 module path, explicit
+ * integrators, LU-SGS and PLU-SGS */
 enum { FEST_TRANSITION_NONE = 0, FEST_TRANSITION_BC = 1, FEST_TRANSITION_LCTM2015 = 2 };
 /* MUSCL limiter: the reference hard-codes Koren's alpha family
  * (muscl.f90:151,176); van Albada (muscl.f90:178, commented out there) is an

@@ -2629,7 +2629,7 @@ static double plu_radius(const fest_flow *fl, const double *qa, const double *qb
  * inverse preconditioner P = I - factor x c^T, x = (1, u, v, w, H[, k,
  * omega]), c = (|V|^2/2, -u, -v, -w, 1[, -1, 0]), H with the reference's
  * 0.5 |V| (not |V|^2), each entry in the reference's evaluation order */
-static double plu_precond(const fest_flow *fl, int n, const double *q0, double P[7][7]) {
+static double plu_precond(const fest_flow *fl, int n, const double *q0, double P[8][8]) {
   const double gm = fl->gm;
   double r = q0[0], u = q0[1], v = q0[2], w = q0[3], p = q0[4];
   double VMag = sqrt(u * u + v * v + w * w);
@@ -2638,7 +2638,8 @@ static double plu_precond(const fest_flow *fl, int n, const double *q0, double P
   double H = (gm * p / (r * (gm - 1.0))) + 0.5 * (VMag);
   double eps = fmin(1.0, fmax(M * M, fl->MInf * fl->MInf));
   double factor = (1.0 - eps) * (gm - 1.0) / (SoundMag * SoundMag);
-  double x[7] = {1, u, v, w, H, n == 7 ? q0[5] : 0, n == 7 ? q0[6] : 0};
+  /* plusgs.f90:2338-2355: LCTM2015 adds the intermittency to x, a zero to c */
+  double x[8] = {1, u, v, w, H, n >= 7 ? q0[5] : 0, n >= 7 ? q0[6] : 0, n == 8 ? q0[7] : 0};
   for (int i = 0; i < n; ++i) {
     double fx = factor * x[i];
     P[i][0] = (i == 0 ? 1.0 : 0.0) - fx * VMag * VMag / 2.0;
@@ -2646,15 +2647,16 @@ static double plu_precond(const fest_flow *fl, int n, const double *q0, double P
     P[i][2] = (i == 2 ? 1.0 : 0.0) - fx * (-v);
     P[i][3] = (i == 3 ? 1.0 : 0.0) - fx * (-w);
     P[i][4] = (i == 4 ? 1.0 : 0.0) - fx * (1.);
-    if (n == 7) {
+    if (n >= 7) {
       P[i][5] = (i == 5 ? 1.0 : 0.0) - fx * (-1.);
       P[i][6] = (i == 6 ? 1.0 : 0.0) - fx * (0.);
     }
+    if (n == 8) P[i][7] = (i == 7 ? 1.0 : 0.0) - fx * (0.);
   }
   return eps;
 }
 
-static void plu_apply(int n, double P[7][7], const double *y, double *out) {
+static void plu_apply(int n, double P[8][8], const double *y, double *out) {
   for (int i = 0; i < n; ++i) {
     double s = 0.0;
     for (int j = 0; j < n; ++j) s = s + P[i][j] * y[j];
@@ -2694,7 +2696,7 @@ static void lu_sgs(fo_block *b, int plus) {
         j = jmx - 1 - (c / (kmx - 1)) % (jmx - 1);
         i = imx - 1 - c / ((kmx - 1) * (jmx - 1));
       }
-      double q0[8], qn[6][8], lam[6], sumlam = 0., P[7][7], eps = 0.0;
+      double q0[8], qn[6][8], lam[6], sumlam = 0., P[8][8], eps = 0.0;
       lu_face fc[6];
       const double *c0 = r4(cl, i, j, k) + 1;
       for (int l = 0; l < n; ++l) q0[l] = *at(q, i, j, k, l + 1);
@@ -2813,7 +2815,6 @@ static int implicit_next_solution(fo_block **bl, int nb, int it, double CFL, int
     if (!((t == FEST_TURB_NONE && bl[n]->d.n_var == 5) ||
           ((t == FEST_TURB_SST || t == FEST_TURB_SST2003) && bl[n]->d.n_var == 7 + lctm)))
       return FEST_ERR_ARG;
-    if (lctm && plus) return FEST_ERR_ARG; /* PLU-SGS's LCTM2015 branch is not restated */
   }
   for (int n = 0; n < nb; ++n) fo_compute_temperature(bl[n]);
   int err = fo_get_total_conservative_residue(bl, nb, it);
